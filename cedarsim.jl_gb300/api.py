@@ -1,0 +1,213 @@
+"""Host-side mirror of CedarSim's analysis entry points over the CUDA library.
+
+Reference entry point                                  here
+------------------------------------------------------ -------------------------
+CircuitIRODESystem(circ)  (src/circuitodesystem.jl:152) System(circuit)
+prob.f.f(out, du, u, p, t) / prob.f.jac(J, du, u, p, gamma, t)
+   (benchmarks/benchmark_common.jl:138,155)            System.f / System.jac
+dc!(circ)                 (src/sweeps.jl:437-448)        dc(circuit)
+tran!(circ, tspan)        (src/sweeps.jl:450-463)        tran(circuit, tspan, ...)
+CircuitSweep + tran!.     (src/sweeps.jl:390-435,488-502) Sweep(...).tran(...)
+
+Every computation runs in libcedar_gpu.so; nothing here falls back to the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import Optional, Sequence, Tuple, Union
+
+import numpy as np
+
+from . import abi
+from .abi import BatchHolder, BatchTuning, DescHolder, Stats, STATS_DTYPE, check, load_library, make_opts
+from .circuit import Circuit, Flat
+
+
+def _flat(c: Union[Circuit, Flat]) -> Flat:
+    return c.flatten() if isinstance(c, Circuit) else c
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class System:
+    """A compiled circuit on the GPU (the counterpart of CircuitIRODESystem)."""
+
+    def __init__(self, circuit: Union[Circuit, Flat]):
+        self.lib = load_library()
+        self.flat = _flat(circuit)
+        self._holder = DescHolder(self.flat)
+        h = C.c_void_p()
+        check(self.lib.cedar_ckt_create(C.byref(self._holder.desc), C.byref(h)))
+        self.handle = h
+        n, nj, nlu, nl = (C.c_int32() for _ in range(4))
+        check(self.lib.cedar_ckt_size(h, C.byref(n), C.byref(nj), C.byref(nlu), C.byref(nl)))
+        self.n, self.nnz_j, self.nnz_lu, self.n_levels = n.value, nj.value, nlu.value, nl.value
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h and h.value:
+            self.lib.cedar_ckt_destroy(h)
+            self.handle = None
+
+    @property
+    def names(self):
+        return self.flat.names
+
+    def pattern(self) -> Tuple[np.ndarray, np.ndarray]:
+        colptr = np.zeros(self.n + 1, np.int32)
+        rowidx = np.zeros(self.nnz_j, np.int32)
+        check(self.lib.cedar_ckt_pattern(self.handle, abi.ptr(colptr, C.c_int32), abi.ptr(rowidx, C.c_int32)))
+        return colptr, rowidx
+
+    def symbolic(self):
+        rm = np.zeros(self.n, np.int32)
+        order = np.zeros(self.n, np.int32)
+        cp = np.zeros(self.n + 1, np.int32)
+        ri = np.zeros(self.nnz_lu, np.int32)
+        check(self.lib.cedar_ckt_symbolic(self.handle, *(abi.ptr(a, C.c_int32) for a in (rm, order, cp, ri))))
+        return rm, order, cp, ri
+
+    # ---- DAECompiler-style residual / Jacobian
+    def f(self, out: np.ndarray, du: Optional[np.ndarray], u: np.ndarray, t: float) -> np.ndarray:
+        u = np.ascontiguousarray(u, np.float64)
+        du = None if du is None else np.ascontiguousarray(du, np.float64)
+        check(self.lib.cedar_eval(self.handle, _dp(u), None if du is None else _dp(du), float(t), 0.0, _dp(out), None))
+        return out
+
+    def jac(self, J: np.ndarray, du: Optional[np.ndarray], u: np.ndarray, gamma: float, t: float) -> np.ndarray:
+        """J (CSC values in pattern() order) = dF/du + gamma dF/du'."""
+        u = np.ascontiguousarray(u, np.float64)
+        check(self.lib.cedar_eval(self.handle, _dp(u), None, float(t), float(gamma), None, _dp(J)))
+        return J
+
+    def eval(self, u, du=None, t=0.0, gamma=0.0):
+        F = np.zeros(self.n)
+        J = np.zeros(self.nnz_j)
+        u = np.ascontiguousarray(u, np.float64)
+        du = None if du is None else np.ascontiguousarray(du, np.float64)
+        check(self.lib.cedar_eval(self.handle, _dp(u), None if du is None else _dp(du), float(t), float(gamma),
+                                  _dp(F), _dp(J)))
+        return F, J
+
+    def jac_dense(self, J: np.ndarray) -> np.ndarray:
+        cp, ri = self.pattern()
+        M = np.zeros((self.n, self.n))
+        for c in range(self.n):
+            M[ri[cp[c]:cp[c + 1]], c] = J[cp[c]:cp[c + 1]]
+        return M
+
+    def newton_solve(self, t: float, cj: float, hist: Optional[np.ndarray], x: np.ndarray):
+        x = np.ascontiguousarray(x, np.float64).copy()
+        st = Stats()
+        hist = None if hist is None else np.ascontiguousarray(hist, np.float64)
+        rc = self.lib.cedar_newton_solve(self.handle, float(t), float(cj), None if hist is None else _dp(hist), _dp(x),
+                                         C.byref(st))
+        return x, st, rc
+
+
+@dataclass
+class Solution:
+    t: np.ndarray
+    u: np.ndarray
+    names: list
+    stats: dict
+    retcode: str
+
+    def __getitem__(self, name):
+        return self.u[:, self.names.index(name)]
+
+
+def _stats_dict(st) -> dict:
+    return {k: getattr(st, k) for k, _ in Stats._fields_ if k != "pad"}
+
+
+def dc(circuit: Union[Circuit, Flat, System], t: float = 0.0, x0: Optional[np.ndarray] = None):
+    """DC operating point (CedarDCOp): Newton, then source stepping, then gmin stepping."""
+    sys = circuit if isinstance(circuit, System) else System(circuit)
+    x = np.zeros(sys.n) if x0 is None else np.ascontiguousarray(x0, np.float64).copy()
+    st = Stats()
+    check(sys.lib.cedar_dcop(sys.handle, float(t), _dp(x), C.byref(st)))
+    return x
+
+
+def tran(circuit: Union[Circuit, Flat, System], tspan: Tuple[float, float], method: str = "bdf2",
+         h: Optional[float] = None, adaptive: Optional[bool] = None, x0: Optional[np.ndarray] = None,
+         dcop: bool = True, reltol: float = 1e-6, abstol_v: float = 1e-9, abstol_i: float = 1e-12,
+         cap: int = 1 << 20, **kw) -> Solution:
+    """Transient analysis on the GPU (the counterpart of tran!(circ, tspan))."""
+    sys = circuit if isinstance(circuit, System) else System(circuit)
+    if adaptive is None:
+        adaptive = h is None
+    opts = make_opts(method, adaptive, tspan[0], tspan[1], h or 0.0, dcop, reltol, abstol_v, abstol_i, **kw)
+    x = np.zeros(sys.n) if x0 is None else np.ascontiguousarray(x0, np.float64).copy()
+    t_out = np.zeros(cap)
+    x_out = np.zeros((cap, sys.n))
+    n_out = C.c_int64()
+    st = Stats()
+    rc = sys.lib.cedar_tran_run(sys.handle, C.byref(opts), _dp(x), _dp(t_out), _dp(x_out), cap, C.byref(n_out),
+                                C.byref(st))
+    check(rc)
+    m = min(n_out.value, cap)
+    return Solution(t_out[:m].copy(), x_out[:m].copy(), sys.names, _stats_dict(st), abi.STATUS_NAMES[st.status])
+
+
+@dataclass
+class BatchResult:
+    x_final: np.ndarray      # [n_inst, n_max]
+    samples: Optional[np.ndarray]  # [n_inst, n_probes, n_samples]
+    stats: np.ndarray        # structured STATS_DTYPE
+
+
+class Sweep:
+    """Batched instances (a CircuitSweep / Monte Carlo over parameter blocks) on one GPU."""
+
+    def __init__(self, templates: Sequence[Union[Circuit, Flat]], inst_template, inst_par=None, inst_par_off=None,
+                 inst_x0=None, inst_x0_off=None, inst_dx=None, inst_dx_off=None, probes=None, n_samples: int = 0):
+        self.lib = load_library()
+        self.templates = [_flat(t) for t in templates]
+        self.holder = BatchHolder(self.templates, inst_template, inst_par, inst_par_off, inst_x0, inst_x0_off,
+                                  inst_dx, inst_dx_off, probes, n_samples)
+        h = C.c_void_p()
+        check(self.lib.cedar_batch_create(C.byref(self.holder.desc), C.byref(h)))
+        self.handle = h
+        nm = C.c_int32()
+        check(self.lib.cedar_batch_nmax(h, C.byref(nm)))
+        self.n_max = nm.value
+        self.n_inst = self.holder.n_inst
+        self.n_probes = 0 if probes is None else np.asarray(probes).shape[-1]
+        self.n_samples = n_samples if self.n_probes else 0
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h and h.value:
+            self.lib.cedar_batch_destroy(h)
+            self.handle = None
+
+    @property
+    def tuning(self) -> Tuple[int, int]:
+        t = BatchTuning()
+        check(self.lib.cedar_batch_get_tuning(self.handle, C.byref(t)))
+        return t.lanes_per_inst, t.warps_per_cta
+
+    def set_tuning(self, lanes_per_inst: int, warps_per_cta: int):
+        t = BatchTuning(lanes_per_inst, warps_per_cta)
+        check(self.lib.cedar_batch_set_tuning(self.handle, C.byref(t)))
+
+    def autotune(self, opts, horizon: float) -> Tuple[int, int]:
+        t = BatchTuning()
+        check(self.lib.cedar_batch_autotune(self.handle, C.byref(opts), float(horizon), C.byref(t)))
+        return t.lanes_per_inst, t.warps_per_cta
+
+    def run(self, opts, want_samples: bool = True) -> BatchResult:
+        xf = np.zeros((self.n_inst, self.n_max))
+        samp = np.zeros((self.n_inst, self.n_probes, self.n_samples)) if (want_samples and self.n_probes) else None
+        st = np.zeros(self.n_inst, STATS_DTYPE)
+        check(self.lib.cedar_batch_run(self.handle, C.byref(opts), _dp(xf), None if samp is None else _dp(samp),
+                                       st.ctypes.data_as(C.c_void_p)))
+        return BatchResult(xf, samp, st)
+
+    def tran(self, tspan, method="bdf2", reltol=1e-6, abstol_v=1e-9, dcop=True, **kw) -> BatchResult:
+        return self.run(make_opts(method, True, tspan[0], tspan[1], 0.0, dcop, reltol, abstol_v, **kw))

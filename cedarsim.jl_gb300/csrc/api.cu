@@ -1,0 +1,551 @@
+// api.cu — the C ABI (include/cedar.h) over the compiler and the kernels.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+#include "compile.h"
+#include "kernels.cuh"
+
+using namespace cedar;
+
+static_assert(sizeof(EngStats) == sizeof(cedar_stats), "stats layout");
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg) { g_err = msg; return code; }
+#define CUDA_TRY(expr)                                                                      \
+  do {                                                                                      \
+    cudaError_t _e = (expr);                                                                \
+    if (_e != cudaSuccess) return fail(CEDAR_ECUDA, std::string(#expr) + ": " + cudaGetErrorString(_e)); \
+  } while (0)
+
+// ------------------------------------------------------------ device template
+struct DevTemplate {
+  Template H;
+  void *buf = nullptr;
+  DTpl D{};
+  DTpl *D_dev = nullptr;
+  double *par_dev = nullptr;  // nominal raw params
+  ~DevTemplate() { if (buf) cudaFree(buf); if (D_dev) cudaFree(D_dev); if (par_dev) cudaFree(par_dev); }
+};
+
+struct Packer {
+  std::vector<char> bytes;
+  size_t add(const void *p, size_t n) {
+    size_t off = (bytes.size() + 255) & ~size_t(255);
+    bytes.resize(off + std::max<size_t>(n, 1));
+    if (n) std::memcpy(bytes.data() + off, p, n);
+    return off;
+  }
+  template <class T> size_t vec(const std::vector<T> &v) { return add(v.data(), v.size() * sizeof(T)); }
+};
+
+int compile_only(const cedar_ckt_desc *desc, std::unique_ptr<DevTemplate> &out, int ordering = ORDER_MIN_DEGREE) {
+  auto dt = std::make_unique<DevTemplate>();
+  std::string err;
+  if (!compile_template(desc, dt->H, err, ordering)) return fail(err.find("singular") != std::string::npos ? CEDAR_ESINGULAR : CEDAR_EINVAL, err);
+  out = std::move(dt);
+  return 0;
+}
+
+int upload_template(const cedar_ckt_desc *desc, std::unique_ptr<DevTemplate> &out, int ordering = ORDER_MIN_DEGREE) {
+  std::unique_ptr<DevTemplate> dt;
+  int rc0 = compile_only(desc, dt, ordering);
+  if (rc0) return rc0;
+  Template &H = dt->H;
+  std::vector<DGroup> grp; std::vector<int> dev_end; int nd = 0;
+  for (auto &g : H.groups) { grp.push_back({g.model, g.n_inst, g.ntx, g.term_off, g.par_off, g.dpar_off, g.out_off}); nd += g.n_inst; dev_end.push_back(nd); }
+  if (grp.empty()) { grp.push_back({0, 0, 0, 0, 0, 0, 0}); dev_end.push_back(0); }
+  auto pairs = [](const std::vector<int32_t> &a, const std::vector<int32_t> &b) {
+    std::vector<int2> p(a.size()); for (size_t k = 0; k < a.size(); ++k) p[k] = make_int2(a[k], b[k]); return p;
+  };
+  std::vector<int2> lu_pair = pairs(H.lu_pair_a, H.lu_pair_b), fw_pair = pairs(H.fw_lu, H.fw_col), bw_pair = pairs(H.bw_lu, H.bw_col);
+  std::vector<int> src_off, src_stride;
+  for (size_t k = 0; k < H.src_group.size(); ++k) {
+    const GroupInfo &g = H.groups[H.src_group[k]];
+    src_off.push_back(g.dpar_off + H.src_inst[k]); src_stride.push_back(g.n_inst);
+  }
+  std::vector<int> gs_row(H.n_nodes), gs_col(H.n_nodes);
+  for (int u = 0; u < H.n_nodes; ++u) { gs_row[u] = H.eq_pos[u]; gs_col[u] = H.iorder[u]; }
+  Packer P;
+  size_t o_grp = P.vec(grp), o_dev_end = P.vec(dev_end), o_term = P.vec(H.term_int), o_term_orig = P.vec(H.term_orig);
+  size_t o_jlu_ptr = P.vec(H.jlu_ptr), o_jlu_ent = P.vec(H.jlu_ent), o_fint_ptr = P.vec(H.fint_ptr), o_fint_ent = P.vec(H.fint_ent);
+  size_t o_qint_ptr = P.vec(H.qint_ptr), o_qint_ent = P.vec(H.qint_ent), o_jcsc_ptr = P.vec(H.jcsc_ptr), o_jcsc_ent = P.vec(H.jcsc_ent);
+  size_t o_forg_ptr = P.vec(H.forg_ptr), o_forg_ent = P.vec(H.forg_ent);
+  size_t o_lu_lvl = P.vec(H.lu_lvl_ptr), o_lu_slot = P.vec(H.lu_task_slot), o_lu_info = P.vec(H.lu_task_info), o_lu_pp = P.vec(H.lu_pair_ptr), o_lu_pair = P.vec(lu_pair);
+  size_t o_fw_lvl = P.vec(H.fw_lvl_ptr), o_fw_row = P.vec(H.fw_row), o_fw_ptr = P.vec(H.fw_ptr), o_fw_pair = P.vec(fw_pair);
+  size_t o_bw_lvl = P.vec(H.bw_lvl_ptr), o_bw_row = P.vec(H.bw_row), o_bw_ptr = P.vec(H.bw_ptr), o_bw_pair = P.vec(bw_pair);
+  size_t o_src_off = P.vec(src_off), o_src_stride = P.vec(src_stride), o_gs_slot = P.vec(H.gs_slot), o_gs_row = P.vec(gs_row), o_gs_col = P.vec(gs_col);
+  size_t o_is_node = P.vec(H.is_node_int), o_order = P.vec(H.order), o_iorder = P.vec(H.iorder), o_eq_pos = P.vec(H.eq_pos), o_pwl = P.vec(H.pwl);
+  CUDA_TRY(cudaMalloc(&dt->buf, P.bytes.size()));
+  CUDA_TRY(cudaMemcpy(dt->buf, P.bytes.data(), P.bytes.size(), cudaMemcpyHostToDevice));
+  char *b = (char *)dt->buf;
+  DTpl &D = dt->D;
+  D.n = H.n; D.n_nodes = H.n_nodes; D.nnz_lu = H.nnz_lu; D.n_out = H.n_out; D.n_groups = (int)H.groups.size();
+  D.n_dev = nd; D.n_src = (int)src_off.size(); D.lu_nlev = (int)H.lu_lvl_ptr.size() - 1;
+  D.fw_nlev = (int)H.fw_lvl_ptr.size() - 1; D.bw_nlev = (int)H.bw_lvl_ptr.size() - 1; D.n_csc = (int)H.j_rowidx.size();
+  D.dpar_size = H.dpar_size; D.gmin = H.gmin; D.vt = thermal_voltage(H.temp_c);
+  D.grp = (const DGroup *)(b + o_grp); D.dev_end = (const int *)(b + o_dev_end);
+  D.term = (const int *)(b + o_term); D.term_orig = (const int *)(b + o_term_orig);
+  D.jlu_ptr = (const int *)(b + o_jlu_ptr); D.jlu_ent = (const int *)(b + o_jlu_ent);
+  D.fint_ptr = (const int *)(b + o_fint_ptr); D.fint_ent = (const int *)(b + o_fint_ent);
+  D.qint_ptr = (const int *)(b + o_qint_ptr); D.qint_ent = (const int *)(b + o_qint_ent);
+  D.jcsc_ptr = (const int *)(b + o_jcsc_ptr); D.jcsc_ent = (const int *)(b + o_jcsc_ent);
+  D.forg_ptr = (const int *)(b + o_forg_ptr); D.forg_ent = (const int *)(b + o_forg_ent);
+  D.lu_lvl = (const int *)(b + o_lu_lvl); D.lu_slot = (const int *)(b + o_lu_slot); D.lu_info = (const int *)(b + o_lu_info);
+  D.lu_pp = (const int *)(b + o_lu_pp); D.lu_pair = (const int2 *)(b + o_lu_pair);
+  D.fw_lvl = (const int *)(b + o_fw_lvl); D.fw_row = (const int *)(b + o_fw_row); D.fw_ptr = (const int *)(b + o_fw_ptr); D.fw_pair = (const int2 *)(b + o_fw_pair);
+  D.bw_lvl = (const int *)(b + o_bw_lvl); D.bw_row = (const int *)(b + o_bw_row); D.bw_ptr = (const int *)(b + o_bw_ptr); D.bw_pair = (const int2 *)(b + o_bw_pair);
+  D.src_off = (const int *)(b + o_src_off); D.src_stride = (const int *)(b + o_src_stride);
+  D.gs_slot = (const int *)(b + o_gs_slot); D.gs_row = (const int *)(b + o_gs_row); D.gs_col = (const int *)(b + o_gs_col);
+  D.is_node = (const unsigned char *)(b + o_is_node); D.order = (const int *)(b + o_order); D.iorder = (const int *)(b + o_iorder);
+  D.eq_pos = (const int *)(b + o_eq_pos); D.pwl = (const double *)(b + o_pwl);
+  CUDA_TRY(cudaMalloc(&dt->D_dev, sizeof(DTpl)));
+  CUDA_TRY(cudaMemcpy(dt->D_dev, &D, sizeof(DTpl), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMalloc(&dt->par_dev, std::max<size_t>(1, H.par.size()) * sizeof(double)));
+  if (!H.par.empty()) CUDA_TRY(cudaMemcpy(dt->par_dev, H.par.data(), H.par.size() * sizeof(double), cudaMemcpyHostToDevice));
+  out = std::move(dt);
+  return 0;
+}
+
+EngOpts to_eng(const cedar_tran_opts *in) {
+  cedar_tran_opts o = *in;
+  double span = o.tstop - o.tstart;
+  if (o.max_newton <= 0) o.max_newton = 20;
+  if (o.max_steps <= 0) o.max_steps = 100000000;
+  if (o.reltol <= 0) o.reltol = 1e-6;
+  if (o.abstol_v <= 0) o.abstol_v = 1e-9;
+  if (o.abstol_i <= 0) o.abstol_i = 1e-12;
+  if (o.nr_factor <= 0) o.nr_factor = 1e-3;
+  if (o.hfirst_frac <= 0) o.hfirst_frac = 1e-2;
+  if (o.hmax <= 0) o.hmax = span / 50.0;
+  if (o.hmin <= 0) o.hmin = span * 1e-12;
+  EngOpts e;
+  e.method = o.method; e.adaptive = o.adaptive; e.dcop = o.dcop; e.max_newton = o.max_newton; e.max_steps = o.max_steps;
+  e.tstart = o.tstart; e.tstop = o.tstop; e.h = o.h; e.hmin = o.hmin; e.hmax = o.hmax; e.reltol = o.reltol;
+  e.abstol_v = o.abstol_v; e.abstol_i = o.abstol_i; e.nr_factor = o.nr_factor; e.hfirst_frac = o.hfirst_frac;
+  return e;
+}
+
+int check_opts(const cedar_tran_opts *o) {
+  if (!o) return fail(CEDAR_EINVAL, "null options");
+  if (!(o->tstop > o->tstart)) return fail(CEDAR_EINVAL, "tstop must exceed tstart");
+  if (o->method != CEDAR_TRAP && o->method != CEDAR_BDF2) return fail(CEDAR_EINVAL, "unknown method");
+  if (!o->adaptive && !(o->h > 0)) return fail(CEDAR_EINVAL, "fixed-step run needs h > 0");
+  if (o->adaptive && o->method != CEDAR_BDF2) return fail(CEDAR_EUNSUPPORTED, "adaptive stepping is BDF2 only");
+  return 0;
+}
+
+template <class T> struct DevBuf {
+  T *p = nullptr; size_t n = 0;
+  cudaError_t ensure(size_t m) {
+    if (m <= n) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr; n = 0;
+    cudaError_t e = cudaMalloc(&p, std::max<size_t>(m, 1) * sizeof(T));
+    if (e == cudaSuccess) n = m;
+    return e;
+  }
+  ~DevBuf() { if (p) cudaFree(p); }
+};
+
+}  // namespace
+
+struct cedar_ckt {
+  std::unique_ptr<DevTemplate> tpl;
+  cudaStream_t stream = nullptr;
+  DevBuf<double> dpar, x, xdot, F, J, dout, hist, ws, tout, xout;
+  DevBuf<EngStats> stats;
+  DevBuf<long long> count;
+  DevBuf<long long> off;
+  int threads = 128;
+  bool host_only = false;
+  ~cedar_ckt() { if (stream) cudaStreamDestroy(stream); }
+};
+
+struct cedar_batch {
+  std::vector<std::unique_ptr<DevTemplate>> tpls;
+  cudaStream_t stream = nullptr;
+  DevBuf<DTpl> d_tpls;
+  DevBuf<int> inst_tpl, queue, head, probes_int;
+  DevBuf<long long> raw_off, dpar_off, x0_off, dx_off;
+  DevBuf<double> raw, dpar, x0, dx, samples, xfinal, ws;
+  DevBuf<EngStats> stats;
+  int n_inst = 0, n_max = 0, np = 0, ns = 0, ws_stride = 0;
+  bool has_x0 = false, has_dx = false;
+  cedar_batch_tuning tune{};
+  ~cedar_batch() { if (stream) cudaStreamDestroy(stream); }
+};
+
+extern "C" {
+
+int cedar_last_error(char *buf, size_t len) {
+  if (buf && len) std::snprintf(buf, len, "%s", g_err.c_str());
+  return (int)g_err.size();
+}
+int cedar_version(void) { return 10000; }
+int cedar_model_nterm(int m) { return (m > 0 && m < CEDAR_NMODELS) ? model_info(m).nterm : -1; }
+int cedar_model_npar(int m) { return (m > 0 && m < CEDAR_NMODELS) ? model_info(m).npar : -1; }
+int cedar_model_has_branch(int m) { return (m > 0 && m < CEDAR_NMODELS) ? model_info(m).has_br : -1; }
+
+void cedar_tran_opts_default(cedar_tran_opts *o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->method = CEDAR_BDF2; o->adaptive = 1; o->dcop = 1; o->max_newton = 20; o->max_steps = 100000000;
+  o->tstart = 0; o->tstop = 0; o->h = 0; o->reltol = 1e-6; o->abstol_v = 1e-9; o->abstol_i = 1e-12;
+  o->nr_factor = 1e-3; o->hfirst_frac = 1e-2;
+}
+
+int cedar_ckt_create(const cedar_ckt_desc *desc, cedar_ckt **out) {
+  if (!desc || !out) return fail(CEDAR_EINVAL, "null argument");
+  *out = nullptr;
+  auto c = std::make_unique<cedar_ckt>();
+  int rc = upload_template(desc, c->tpl);
+  if (rc) return rc;
+  CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  const Template &H = c->tpl->H;
+  CUDA_TRY(c->dpar.ensure(H.dpar_size));
+  CUDA_TRY(c->off.ensure(2));
+  long long zero[2] = {0, 0};
+  CUDA_TRY(cudaMemcpyAsync(c->off.p, zero, sizeof(zero), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(launch_derive(c->tpl->D_dev, nullptr, c->off.p, c->tpl->par_dev, c->off.p + 1, c->dpar.p, 1, c->tpl->D.n_dev, c->stream));
+  int n = H.n;
+  CUDA_TRY(c->x.ensure(n)); CUDA_TRY(c->xdot.ensure(n)); CUDA_TRY(c->F.ensure(n)); CUDA_TRY(c->hist.ensure(n));
+  CUDA_TRY(c->J.ensure(H.j_rowidx.size())); CUDA_TRY(c->dout.ensure(H.n_out));
+  CUDA_TRY(c->stats.ensure(1)); CUDA_TRY(c->count.ensure(1));
+  size_t wsd = ws_doubles(H.n, H.nnz_lu, H.n_out);
+  if ((wsd + 64) * sizeof(double) > 160 * 1024) CUDA_TRY(c->ws.ensure(wsd));
+  int work = std::max(std::max(H.nnz_lu, n), c->tpl->D.n_dev);
+  c->threads = work >= 512 ? 512 : std::max(64, ((work + 31) / 32) * 32);
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  *out = c.release();
+  return 0;
+}
+
+int cedar_plan_create(const cedar_ckt_desc *desc, cedar_ckt **out) {
+  if (!desc || !out) return fail(CEDAR_EINVAL, "null argument");
+  *out = nullptr;
+  auto c = std::make_unique<cedar_ckt>();
+  int rc = compile_only(desc, c->tpl);
+  if (rc) return rc;
+  c->host_only = true;
+  *out = c.release();
+  return 0;
+}
+
+int cedar_ckt_destroy(cedar_ckt *c) { delete c; return 0; }
+
+int cedar_ckt_size(const cedar_ckt *c, int32_t *n, int32_t *nnz_j, int32_t *nnz_lu, int32_t *n_levels) {
+  if (!c) return fail(CEDAR_EINVAL, "null handle");
+  const Template &H = c->tpl->H;
+  if (n) *n = H.n;
+  if (nnz_j) *nnz_j = (int32_t)H.j_rowidx.size();
+  if (nnz_lu) *nnz_lu = H.nnz_lu;
+  if (n_levels) *n_levels = (int32_t)(H.lu_lvl_ptr.size() - 1);
+  return 0;
+}
+
+int cedar_ckt_pattern(const cedar_ckt *c, int32_t *colptr, int32_t *rowidx) {
+  if (!c) return fail(CEDAR_EINVAL, "null handle");
+  const Template &H = c->tpl->H;
+  if (colptr) std::memcpy(colptr, H.j_colptr.data(), H.j_colptr.size() * sizeof(int32_t));
+  if (rowidx) std::memcpy(rowidx, H.j_rowidx.data(), H.j_rowidx.size() * sizeof(int32_t));
+  return 0;
+}
+
+int cedar_ckt_symbolic(const cedar_ckt *c, int32_t *rowmatch, int32_t *order, int32_t *lu_colptr, int32_t *lu_rowidx) {
+  if (!c) return fail(CEDAR_EINVAL, "null handle");
+  const Template &H = c->tpl->H;
+  if (rowmatch) std::memcpy(rowmatch, H.rowmatch.data(), H.n * sizeof(int32_t));
+  if (order) std::memcpy(order, H.order.data(), H.n * sizeof(int32_t));
+  if (lu_colptr || lu_rowidx) {
+    std::vector<int32_t> cp(H.n + 1, 0), ri(H.nnz_lu);
+    for (int p = 0; p < H.n; ++p) for (int k = H.lu_rowptr[p]; k < H.lu_rowptr[p + 1]; ++k) cp[H.lu_colidx[k] + 1]++;
+    for (int q = 0; q < H.n; ++q) cp[q + 1] += cp[q];
+    std::vector<int32_t> fillp(cp.begin(), cp.end() - 1);
+    for (int p = 0; p < H.n; ++p) for (int k = H.lu_rowptr[p]; k < H.lu_rowptr[p + 1]; ++k) ri[fillp[H.lu_colidx[k]]++] = p;
+    if (lu_colptr) std::memcpy(lu_colptr, cp.data(), cp.size() * sizeof(int32_t));
+    if (lu_rowidx) std::memcpy(lu_rowidx, ri.data(), ri.size() * sizeof(int32_t));
+  }
+  return 0;
+}
+
+int cedar_eval_dev(cedar_ckt *c, const double *x, const double *xdot, double t, double cj, double *F, double *J) {
+  if (!c || !x) return fail(CEDAR_EINVAL, "null argument");
+  if (c->host_only) return fail(CEDAR_EINVAL, "host-only plan handle");
+  CUDA_TRY(launch_eval(c->tpl->D, c->tpl->D_dev, c->dpar.p, x, xdot, t, cj, c->dout.p, F, J, c->stream));
+  return 0;
+}
+
+int cedar_eval(cedar_ckt *c, const double *x, const double *xdot, double t, double cj, double *F, double *J) {
+  if (!c || !x) return fail(CEDAR_EINVAL, "null argument");
+  if (c->host_only) return fail(CEDAR_EINVAL, "host-only plan handle");
+  const Template &H = c->tpl->H;
+  size_t n = H.n, nj = H.j_rowidx.size();
+  CUDA_TRY(cudaMemcpyAsync(c->x.p, x, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if (xdot) CUDA_TRY(cudaMemcpyAsync(c->xdot.p, xdot, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(launch_eval(c->tpl->D, c->tpl->D_dev, c->dpar.p, c->x.p, xdot ? c->xdot.p : nullptr, t, cj, c->dout.p,
+                       F ? c->F.p : nullptr, J ? c->J.p : nullptr, c->stream));
+  if (F) CUDA_TRY(cudaMemcpyAsync(F, c->F.p, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (J) CUDA_TRY(cudaMemcpyAsync(J, c->J.p, nj * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+static int run_plain(cedar_ckt *c, int mode, const cedar_tran_opts *opts, double t, double cj, const double *hist,
+                     double *x, double *t_out, double *x_out, int64_t cap, int64_t *n_out, cedar_stats *stats) {
+  if (c->host_only) return fail(CEDAR_EINVAL, "host-only plan handle");
+  const Template &H = c->tpl->H;
+  size_t n = H.n;
+  PlainArgs a{};
+  a.T = c->tpl->D_dev; a.dpar = c->dpar.p; a.x = c->x.p; a.t = t; a.cj = cj; a.mode = mode;
+  cedar_tran_opts od; cedar_tran_opts_default(&od);
+  if (opts) od = *opts; else { od.tstart = 0; od.tstop = 1; }
+  a.opts = to_eng(&od);
+  CUDA_TRY(cudaMemcpyAsync(c->x.p, x, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if (hist) { CUDA_TRY(cudaMemcpyAsync(c->hist.p, hist, n * sizeof(double), cudaMemcpyHostToDevice, c->stream)); a.hist = c->hist.p; }
+  if (mode == 0 && t_out && cap > 0) {
+    CUDA_TRY(c->tout.ensure(cap)); CUDA_TRY(c->xout.ensure((size_t)cap * n));
+    a.t_out = c->tout.p; a.x_out = c->xout.p; a.cap = cap;
+  }
+  a.count = c->count.p; a.stats = c->stats.p; a.ws_global = c->ws.p;
+  CUDA_TRY(launch_plain(a, ws_doubles(H.n, H.nnz_lu, H.n_out), c->threads, c->stream));
+  EngStats st{}; long long cnt = 0;
+  CUDA_TRY(cudaMemcpyAsync(&st, c->stats.p, sizeof(st), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(&cnt, c->count.p, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(x, c->x.p, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  if (mode == 0 && a.t_out) {
+    long long m = std::min<long long>(cnt, cap);
+    CUDA_TRY(cudaMemcpy(t_out, c->tout.p, m * sizeof(double), cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(x_out, c->xout.p, (size_t)m * n * sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  if (n_out) *n_out = cnt;
+  if (stats) std::memcpy(stats, &st, sizeof(st));
+  if (mode == 0 && t_out && cnt > cap) return fail(CEDAR_ECAPACITY, "output capacity exceeded");
+  if (mode != 0 && st.status != CEDAR_ST_OK) return fail(CEDAR_ENOCONV, "Newton / DC operating point did not converge");
+  return 0;
+}
+
+int cedar_newton_solve(cedar_ckt *c, double t, double cj, const double *hist, double *x, cedar_stats *stats) {
+  if (!c || !x) return fail(CEDAR_EINVAL, "null argument");
+  return run_plain(c, 1, nullptr, t, cj, hist, x, nullptr, nullptr, 0, nullptr, stats);
+}
+
+int cedar_dcop(cedar_ckt *c, double t, double *x, cedar_stats *stats) {
+  if (!c || !x) return fail(CEDAR_EINVAL, "null argument");
+  return run_plain(c, 2, nullptr, t, 0.0, nullptr, x, nullptr, nullptr, 0, nullptr, stats);
+}
+
+int cedar_tran_run(cedar_ckt *c, const cedar_tran_opts *opts, const double *x0, double *t_out, double *x_out,
+                   int64_t cap, int64_t *n_out, cedar_stats *stats) {
+  if (!c || !x0) return fail(CEDAR_EINVAL, "null argument");
+  int rc = check_opts(opts); if (rc) return rc;
+  std::vector<double> x(x0, x0 + c->tpl->H.n);
+  return run_plain(c, 0, opts, opts->tstart, 0.0, nullptr, x.data(), t_out, x_out, cap, n_out, stats);
+}
+
+// ------------------------------------------------------------------ batch
+int cedar_batch_create(const cedar_batch_desc *d, cedar_batch **out) {
+  if (!d || !out) return fail(CEDAR_EINVAL, "null argument");
+  *out = nullptr;
+  if (d->n_templates <= 0 || d->n_inst < 0 || !d->templates || (d->n_inst > 0 && !d->inst_template))
+    return fail(CEDAR_EINVAL, "malformed batch description");
+  auto b = std::make_unique<cedar_batch>();
+  CUDA_TRY(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  std::vector<DTpl> hd;
+  for (int k = 0; k < d->n_templates; ++k) {
+    std::unique_ptr<DevTemplate> t;
+    int rc = upload_template(&d->templates[k], t);
+    if (rc) return rc;
+    b->n_max = std::max(b->n_max, t->H.n);
+    b->ws_stride = std::max(b->ws_stride, ws_doubles(t->H.n, t->H.nnz_lu, t->H.n_out));
+    hd.push_back(t->D);
+    b->tpls.push_back(std::move(t));
+  }
+  b->ws_stride = (b->ws_stride + 1) & ~1;
+  const int ni = d->n_inst;
+  b->n_inst = ni;
+  CUDA_TRY(b->d_tpls.ensure(hd.size()));
+  CUDA_TRY(cudaMemcpy(b->d_tpls.p, hd.data(), hd.size() * sizeof(DTpl), cudaMemcpyHostToDevice));
+  // raw parameter blocks: user blocks first, then nominal blocks per template
+  size_t user_len = 0;
+  for (int i = 0; i < ni; ++i) {
+    int k = d->inst_template[i];
+    if (k < 0 || k >= d->n_templates) return fail(CEDAR_EINVAL, "instance template out of range");
+    if (d->inst_par_off && d->inst_par_off[i] >= 0) {
+      if (!d->inst_par) return fail(CEDAR_EINVAL, "inst_par missing");
+      user_len = std::max<size_t>(user_len, (size_t)d->inst_par_off[i] + b->tpls[k]->H.par_size);
+    }
+  }
+  std::vector<double> raw(d->inst_par ? d->inst_par : (const double *)nullptr, d->inst_par ? d->inst_par + user_len : (const double *)nullptr);
+  std::vector<long long> nominal_off(d->n_templates);
+  for (int k = 0; k < d->n_templates; ++k) { nominal_off[k] = (long long)raw.size(); raw.insert(raw.end(), b->tpls[k]->H.par.begin(), b->tpls[k]->H.par.end()); }
+  std::vector<long long> raw_off(ni), dpar_off(ni), x0_off(ni, -1), dx_off(ni, -1);
+  std::vector<int> itpl(ni);
+  long long dsz = 0;
+  for (int i = 0; i < ni; ++i) {
+    int k = d->inst_template[i]; itpl[i] = k;
+    raw_off[i] = (d->inst_par_off && d->inst_par_off[i] >= 0) ? d->inst_par_off[i] : nominal_off[k];
+    dpar_off[i] = dsz; dsz += b->tpls[k]->H.dpar_size;
+    if (d->inst_x0_off && d->inst_x0 && d->inst_x0_off[i] >= 0) { x0_off[i] = d->inst_x0_off[i]; b->has_x0 = true; }
+    if (d->inst_dx_off && d->inst_dx && d->inst_dx_off[i] >= 0) { dx_off[i] = d->inst_dx_off[i]; b->has_dx = true; }
+  }
+  auto up = [&](auto &buf, const auto &vec) -> int {
+    CUDA_TRY(buf.ensure(vec.size()));
+    if (!vec.empty()) CUDA_TRY(cudaMemcpy(buf.p, vec.data(), vec.size() * sizeof(vec[0]), cudaMemcpyHostToDevice));
+    return 0;
+  };
+  int rc;
+  if ((rc = up(b->raw, raw)) || (rc = up(b->raw_off, raw_off)) || (rc = up(b->dpar_off, dpar_off)) || (rc = up(b->inst_tpl, itpl))) return rc;
+  CUDA_TRY(b->dpar.ensure(std::max<long long>(dsz, 1)));
+  int max_dev = 0; for (auto &t : b->tpls) max_dev = std::max(max_dev, t->D.n_dev);
+  CUDA_TRY(launch_derive(b->d_tpls.p, b->inst_tpl.p, b->raw_off.p, b->raw.p, b->dpar_off.p, b->dpar.p, ni, max_dev, b->stream));
+  // initial states / perturbations (original order)
+  if (b->has_x0) {
+    size_t len = 0; for (int i = 0; i < ni; ++i) if (x0_off[i] >= 0) len = std::max<size_t>(len, x0_off[i] + b->tpls[itpl[i]]->H.n);
+    std::vector<double> v(d->inst_x0, d->inst_x0 + len);
+    if ((rc = up(b->x0, v)) || (rc = up(b->x0_off, x0_off))) return rc;
+  }
+  if (b->has_dx) {
+    size_t len = 0; for (int i = 0; i < ni; ++i) if (dx_off[i] >= 0) len = std::max<size_t>(len, dx_off[i] + b->tpls[itpl[i]]->H.n);
+    std::vector<double> v(d->inst_dx, d->inst_dx + len);
+    if ((rc = up(b->dx, v)) || (rc = up(b->dx_off, dx_off))) return rc;
+  }
+  // probes (internal)
+  b->np = (d->n_probes > 0 && d->probes) ? d->n_probes : 0;
+  b->ns = b->np ? d->n_samples : 0;
+  if (b->np && b->ns < 2) return fail(CEDAR_EINVAL, "n_samples must be >= 2 with probes");
+  if (b->np) {
+    std::vector<int> pi((size_t)d->n_templates * b->np);
+    for (int k = 0; k < d->n_templates; ++k)
+      for (int p = 0; p < b->np; ++p) {
+        int u = d->probes[(size_t)k * b->np + p];
+        pi[(size_t)k * b->np + p] = (u >= 0 && u < b->tpls[k]->H.n) ? b->tpls[k]->H.iorder[u] : -1;
+      }
+    if ((rc = up(b->probes_int, pi))) return rc;
+  }
+  // queue: largest templates first (longest-processing-time first), stable by id
+  std::vector<int> q(ni);
+  for (int i = 0; i < ni; ++i) q[i] = i;
+  std::stable_sort(q.begin(), q.end(), [&](int a, int c) {
+    const Template &A = b->tpls[itpl[a]]->H, &C = b->tpls[itpl[c]]->H;
+    long long ca = (long long)A.nnz_lu + A.n_out, cc = (long long)C.nnz_lu + C.n_out;
+    if (ca != cc) return ca > cc;
+    return itpl[a] < itpl[c];
+  });
+  if ((rc = up(b->queue, q))) return rc;
+  CUDA_TRY(b->head.ensure(1));
+  CUDA_TRY(b->stats.ensure(std::max(ni, 1)));
+  CUDA_TRY(b->xfinal.ensure((size_t)std::max(ni, 1) * b->n_max));
+  if (b->np) CUDA_TRY(b->samples.ensure((size_t)std::max(ni, 1) * b->np * b->ns));
+  b->tune.lanes_per_inst = 8; b->tune.warps_per_cta = 4;
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  *out = b.release();
+  return 0;
+}
+
+int cedar_batch_destroy(cedar_batch *b) { delete b; return 0; }
+
+int cedar_batch_nmax(const cedar_batch *b, int32_t *n_max) {
+  if (!b || !n_max) return fail(CEDAR_EINVAL, "null argument");
+  *n_max = b->n_max;
+  return 0;
+}
+
+int cedar_batch_set_tuning(cedar_batch *b, const cedar_batch_tuning *t) {
+  if (!b || !t) return fail(CEDAR_EINVAL, "null argument");
+  int K = t->lanes_per_inst;
+  if (K != 1 && K != 2 && K != 4 && K != 8 && K != 16 && K != 32) return fail(CEDAR_EINVAL, "lanes_per_inst must be a power of two <= 32");
+  if (t->warps_per_cta < 1 || t->warps_per_cta > 8) return fail(CEDAR_EINVAL, "warps_per_cta must be 1..8");
+  b->tune = *t;
+  return 0;
+}
+
+int cedar_batch_get_tuning(const cedar_batch *b, cedar_batch_tuning *t) {
+  if (!b || !t) return fail(CEDAR_EINVAL, "null argument");
+  *t = b->tune;
+  return 0;
+}
+
+static int batch_launch(cedar_batch *b, const EngOpts &eo, const cedar_batch_tuning &tu, bool want_outputs) {
+  int K = tu.lanes_per_inst, warps = tu.warps_per_cta;
+  int tiles = warps * 32 / K;
+  size_t per_tile = (size_t)b->ws_stride * sizeof(double);
+  int smax = batch_max_smem_optin();
+  bool in_smem = (size_t)tiles * per_tile <= (size_t)smax;
+  size_t smem = in_smem ? (size_t)tiles * per_tile : 0;
+  int dev = 0, nsm = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  int per_sm = 1;
+  if (in_smem) {
+    int smsm = 0; CUDA_TRY(cudaDeviceGetAttribute(&smsm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+    per_sm = std::max(1, std::min(2048 / (warps * 32), (int)(smsm / std::max<size_t>(smem + 1024, 1))));
+  } else {
+    per_sm = std::max(1, 2048 / (warps * 32));
+  }
+  int grid = std::max(1, std::min(nsm * per_sm, (b->n_inst + tiles - 1) / tiles));
+  if (!in_smem) CUDA_TRY(b->ws.ensure((size_t)grid * tiles * b->ws_stride));
+  BatchDev bd{};
+  bd.tpls = b->d_tpls.p; bd.inst_tpl = b->inst_tpl.p; bd.inst_dpar = b->dpar_off.p; bd.dpar = b->dpar.p;
+  bd.x0_off = b->has_x0 ? b->x0_off.p : nullptr; bd.x0 = b->x0.p;
+  bd.dx_off = b->has_dx ? b->dx_off.p : nullptr; bd.dx = b->dx.p;
+  bd.probes_int = b->probes_int.p; bd.np = want_outputs ? b->np : 0; bd.ns = b->ns;
+  bd.samples = want_outputs ? b->samples.p : nullptr;
+  bd.x_final = want_outputs ? b->xfinal.p : nullptr; bd.n_max = b->n_max;
+  bd.stats = b->stats.p; bd.queue = b->queue.p; bd.head = b->head.p; bd.n_inst = b->n_inst;
+  bd.opts = eo; bd.ws_stride = b->ws_stride; bd.ws_global = b->ws.p; bd.ws_in_smem = in_smem ? 1 : 0;
+  CUDA_TRY(cudaMemsetAsync(b->head.p, 0, sizeof(int), b->stream));
+  if (want_outputs) CUDA_TRY(cudaMemsetAsync(b->xfinal.p, 0, (size_t)b->n_inst * b->n_max * sizeof(double), b->stream));
+  CUDA_TRY(launch_batch(bd, K, warps, grid, smem, b->stream));
+  return 0;
+}
+
+int cedar_batch_run(cedar_batch *b, const cedar_tran_opts *opts, double *x_final, double *samples, cedar_stats *stats) {
+  if (!b) return fail(CEDAR_EINVAL, "null handle");
+  int rc = check_opts(opts); if (rc) return rc;
+  if (b->n_inst == 0) return 0;
+  EngOpts eo = to_eng(opts);
+  if ((rc = batch_launch(b, eo, b->tune, true))) return rc;
+  if (x_final) CUDA_TRY(cudaMemcpyAsync(x_final, b->xfinal.p, (size_t)b->n_inst * b->n_max * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  if (samples && b->np) CUDA_TRY(cudaMemcpyAsync(samples, b->samples.p, (size_t)b->n_inst * b->np * b->ns * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  if (stats) CUDA_TRY(cudaMemcpyAsync(stats, b->stats.p, (size_t)b->n_inst * sizeof(EngStats), cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return 0;
+}
+
+int cedar_batch_autotune(cedar_batch *b, const cedar_tran_opts *opts, double horizon, cedar_batch_tuning *best) {
+  if (!b) return fail(CEDAR_EINVAL, "null handle");
+  int rc = check_opts(opts); if (rc) return rc;
+  cedar_tran_opts o = *opts;
+  if (horizon > 0 && o.tstart + horizon < o.tstop) o.tstop = o.tstart + horizon;
+  EngOpts eo = to_eng(&o);
+  eo.hmax = to_eng(opts).hmax;  // keep the full run's step bounds
+  const int Ks[] = {1, 2, 4, 8, 16, 32};
+  const int Ws[] = {2, 4, 8};
+  float best_ms = 1e30f; cedar_batch_tuning bt = b->tune;
+  cudaEvent_t e0, e1;
+  CUDA_TRY(cudaEventCreate(&e0)); CUDA_TRY(cudaEventCreate(&e1));
+  for (int K : Ks) for (int W : Ws) {
+    cedar_batch_tuning t{}; t.lanes_per_inst = K; t.warps_per_cta = W;
+    CUDA_TRY(cudaEventRecord(e0, b->stream));
+    if ((rc = batch_launch(b, eo, t, false))) return rc;
+    CUDA_TRY(cudaEventRecord(e1, b->stream));
+    CUDA_TRY(cudaEventSynchronize(e1));
+    float ms = 0; CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+    if (ms < best_ms) { best_ms = ms; bt = t; }
+  }
+  cudaEventDestroy(e0); cudaEventDestroy(e1);
+  b->tune = bt;
+  if (best) *best = bt;
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,396 @@
+// compile.cpp — host-side circuit compiler (see compile.h).
+//
+// The flattened device table is what a Julia `ccall` shim builds from an elaborated
+// CedarSim circuit (one row per device instance: model, terminal unknowns, SoA
+// parameters).  Everything below is computed once per topology on the host:
+//   1. stamps of every device (CedarSim KCL signs, src/simulate_ir.jl:54,112-120),
+//   2. the J pattern (union of G and C stamps) in CSC over the original unknowns,
+//   3. static pivoting: a structural row matching that puts a structurally nonzero
+//      entry on every diagonal (diagonal preferred, then augmenting paths — the
+//      maximum-transversal algorithm of Duff, ACM TOMS 7 (1981)); MNA branch rows
+//      of V sources / inductors with zero diagonals are paired with KCL rows here,
+//   4. a fill-reducing symmetric ordering of the matched matrix (exact minimum
+//      degree on the pattern of B + B^T, ties broken by the lower index),
+//   5. the LU fill pattern of the permuted matrix (no numerical pivoting at run
+//      time: "static pivoting", Li & Demmel, SuperLU_DIST, 1998),
+//   6. entry-wise (Crout) factorisation tasks and triangular-solve row tasks,
+//      grouped into dependency levels so that a thread group runs one level at a
+//      time with no atomics and a fixed summation order (bitwise reproducible).
+#include "compile.h"
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <set>
+
+namespace cedar {
+
+static const ModelInfo kModels[CEDAR_NMODELS] = {
+    {0, 0, 0, 0, 0},   // unused
+    {2, 2, 0, 2, 1},   // R    out: I, g                 dpar: m/r
+    {2, 2, 0, 3, 1},   // C    out: Fpart, cj*mc, Q      dpar: m*c
+    {2, 2, 1, 6, 2},   // L    out: mI, Vrow, m, 1, cj*l, l*I   dpar: m, l
+    {2, 10, 1, 4, 10}, // V    out: mI, V-vs, m, 1       dpar: raw
+    {2, 10, 0, 1, 10}, // I    out: m*is                 dpar: raw
+    {4, 2, 1, 5, 2},   // E    out: mI, V-gVc, m, 1, gain   dpar: gain, m
+    {4, 2, 0, 2, 1},   // G    out: m g Vc, m g          dpar: m*gain
+    {4, 7, 0, 4, 5},   // MOS1 out: mIds, mgm, mgds, m(gm+gds)  dpar: type beta vth lam m
+    {2, 4, 0, 2, 3},   // DIODE out: mI, mgd             dpar: IS*AREA, 1/(N Vt), m
+    {3, 2, 0, 4, 2},   // NLVCR out: mI, m dI/dVd, m dI/dVg, m dI/dVs(neg)  dpar: 2R, m
+};
+
+const ModelInfo &model_info(int model) { return kModels[model]; }
+
+void device_stamps(int model, const int *t, int ob, std::vector<Stamp> &J, std::vector<Stamp> &F,
+                   std::vector<Stamp> &Q) {
+  auto j = [&](int r, int c, int o, int neg) { if (r >= 0 && c >= 0) J.push_back({r, c, ob + o, neg}); };
+  auto f = [&](int r, int o, int neg) { if (r >= 0) F.push_back({r, -1, ob + o, neg}); };
+  auto q = [&](int r, int o, int neg) { if (r >= 0) Q.push_back({r, -1, ob + o, neg}); };
+  switch (model) {
+    case CEDAR_R: case CEDAR_DIODE:
+      f(t[0], 0, 1); f(t[1], 0, 0);
+      j(t[0], t[0], 1, 1); j(t[0], t[1], 1, 0); j(t[1], t[0], 1, 0); j(t[1], t[1], 1, 1);
+      break;
+    case CEDAR_C:
+      f(t[0], 0, 1); f(t[1], 0, 0);
+      j(t[0], t[0], 1, 1); j(t[0], t[1], 1, 0); j(t[1], t[0], 1, 0); j(t[1], t[1], 1, 1);
+      q(t[0], 2, 1); q(t[1], 2, 0);
+      break;
+    case CEDAR_L:
+      f(t[0], 0, 1); f(t[1], 0, 0); f(t[2], 1, 0);
+      j(t[0], t[2], 2, 1); j(t[1], t[2], 2, 0); j(t[2], t[0], 3, 0); j(t[2], t[1], 3, 1); j(t[2], t[2], 4, 1);
+      q(t[2], 5, 1);
+      break;
+    case CEDAR_V:
+      f(t[0], 0, 1); f(t[1], 0, 0); f(t[2], 1, 0);
+      j(t[0], t[2], 2, 1); j(t[1], t[2], 2, 0); j(t[2], t[0], 3, 0); j(t[2], t[1], 3, 1);
+      break;
+    case CEDAR_I:
+      f(t[0], 0, 1); f(t[1], 0, 0);
+      break;
+    case CEDAR_E:
+      f(t[0], 0, 1); f(t[1], 0, 0); f(t[4], 1, 0);
+      j(t[0], t[4], 2, 1); j(t[1], t[4], 2, 0); j(t[4], t[0], 3, 0); j(t[4], t[1], 3, 1);
+      j(t[4], t[2], 4, 1); j(t[4], t[3], 4, 0);
+      break;
+    case CEDAR_G:
+      f(t[0], 0, 1); f(t[1], 0, 0);
+      j(t[0], t[2], 1, 1); j(t[0], t[3], 1, 0); j(t[1], t[2], 1, 0); j(t[1], t[3], 1, 1);
+      break;
+    case CEDAR_MOS1:
+      f(t[0], 0, 1); f(t[2], 0, 0);
+      j(t[0], t[1], 1, 1); j(t[0], t[0], 2, 1); j(t[0], t[2], 3, 0);
+      j(t[2], t[1], 1, 0); j(t[2], t[0], 2, 0); j(t[2], t[2], 3, 1);
+      break;
+    case CEDAR_NLVCR:
+      f(t[0], 0, 1); f(t[2], 0, 0);
+      j(t[0], t[0], 1, 1); j(t[0], t[1], 2, 1); j(t[0], t[2], 3, 0);
+      j(t[2], t[0], 1, 0); j(t[2], t[1], 2, 0); j(t[2], t[2], 3, 1);
+      break;
+  }
+}
+
+// ------------------------------------------------------------- helpers
+static void build_program(int nslots, const std::vector<std::pair<int, int32_t>> &items,
+                          std::vector<int32_t> &ptr, std::vector<int32_t> &ent) {
+  // items: (slot, encoded entry) in deterministic device order; stable by slot
+  ptr.assign(nslots + 1, 0);
+  for (auto &it : items) ptr[it.first + 1]++;
+  for (int s = 0; s < nslots; ++s) ptr[s + 1] += ptr[s];
+  ent.assign(items.size(), 0);
+  std::vector<int32_t> fillp(ptr.begin(), ptr.end() - 1);
+  for (auto &it : items) ent[fillp[it.first]++] = it.second;
+}
+
+static int32_t enc(const Stamp &s) { return (s.out << 1) | (s.neg ? 1 : 0); }
+
+// Structural matching: colrows[u] sorted rows with a nonzero in column u.
+static bool match_columns(int n, const std::vector<std::vector<int>> &colrows,
+                          const std::vector<std::vector<int>> &rowcols, std::vector<int> &rowmatch) {
+  std::vector<int> mrow(n, -1), mcol(n, -1);  // mrow[e] = column matched to row e
+  for (int u = 0; u < n; ++u)
+    if (std::binary_search(colrows[u].begin(), colrows[u].end(), u)) { mrow[u] = u; mcol[u] = u; }
+  std::vector<int> visited(n, -1);
+  for (int u0 = 0; u0 < n; ++u0) {
+    if (mcol[u0] >= 0) continue;
+    // cheap assignment
+    bool done = false;
+    for (int e : colrows[u0]) if (mrow[e] < 0) { mrow[e] = u0; mcol[u0] = e; done = true; break; }
+    if (done) continue;
+    // iterative DFS for an augmenting path (column -> row -> matched column ...)
+    struct Fr { int u; size_t k; };
+    std::vector<Fr> st; std::vector<int> path_row;
+    st.push_back({u0, 0});
+    bool found = false;
+    while (!st.empty() && !found) {
+      Fr &fr = st.back();
+      if (fr.k >= colrows[fr.u].size()) { st.pop_back(); if (!path_row.empty()) path_row.pop_back(); continue; }
+      int e = colrows[fr.u][fr.k++];
+      if (visited[e] == u0) continue;
+      visited[e] = u0;
+      if (mrow[e] < 0) {
+        path_row.push_back(e);
+        // augment along the stack: column st[i].u takes row path_row[i]
+        for (size_t i = 0; i < st.size(); ++i) { int uu = st[i].u, ee = path_row[i]; mrow[ee] = uu; mcol[uu] = ee; }
+        found = true;
+      } else {
+        path_row.push_back(e);
+        st.push_back({mrow[e], 0});
+      }
+    }
+    if (!found) return false;
+  }
+  (void)rowcols;
+  rowmatch.assign(mcol.begin(), mcol.end());
+  return true;
+}
+
+// Exact minimum degree on an undirected graph (adjacency without self loops).
+static void min_degree(int n, std::vector<std::set<int>> adj, std::vector<int> &order) {
+  std::set<std::pair<int, int>> pq;
+  for (int v = 0; v < n; ++v) pq.insert({(int)adj[v].size(), v});
+  std::vector<char> alive(n, 1);
+  order.clear(); order.reserve(n);
+  while (!pq.empty()) {
+    int v = pq.begin()->second; pq.erase(pq.begin());
+    order.push_back(v); alive[v] = 0;
+    std::vector<int> N(adj[v].begin(), adj[v].end());
+    for (int a : N) {
+      pq.erase({(int)adj[a].size(), a});
+      adj[a].erase(v);
+      for (int b : N) if (b != a) adj[a].insert(b);
+      pq.insert({(int)adj[a].size(), a});
+    }
+    adj[v].clear();
+  }
+}
+
+bool compile_template(const cedar_ckt_desc *d, Template &T, std::string &err, int ordering) {
+  if (!d) { err = "null desc"; return false; }
+  if (d->n_nodes < 0 || d->n_branch < 0 || d->n_groups < 0 || (d->n_groups > 0 && !d->groups)) { err = "malformed desc"; return false; }
+  T = Template();
+  T.n_nodes = d->n_nodes; T.n_branch = d->n_branch; T.n = d->n_nodes + d->n_branch;
+  T.temp_c = d->temp_c; T.gmin = d->gmin;
+  const int n = T.n;
+  if (n <= 0) { err = "empty system"; return false; }
+  if (d->pwl && d->n_pwl > 0) T.pwl.assign(d->pwl, d->pwl + d->n_pwl);
+  // groups
+  int term_off = 0, par_off = 0, dpar_off = 0, out_off = 0;
+  for (int g = 0; g < d->n_groups; ++g) {
+    const cedar_devgroup &s = d->groups[g];
+    if (s.model <= 0 || s.model >= CEDAR_NMODELS) { err = "unknown model id " + std::to_string(s.model); return false; }
+    if (s.n_inst < 0) { err = "negative instance count"; return false; }
+    const ModelInfo &mi = kModels[s.model];
+    if (s.n_inst > 0 && (!s.term || !s.par || (mi.has_br && !s.branch))) { err = "group missing arrays"; return false; }
+    GroupInfo gi{};
+    gi.model = s.model; gi.n_inst = s.n_inst; gi.ntx = mi.nterm + mi.has_br;
+    gi.term_off = term_off; gi.par_off = par_off; gi.dpar_off = dpar_off; gi.out_off = out_off;
+    for (int i = 0; i < s.n_inst; ++i) {
+      for (int k = 0; k < mi.nterm; ++k) {
+        int u = s.term[(size_t)i * mi.nterm + k];
+        if (u < -1 || u >= n) { err = "terminal index out of range"; return false; }
+        T.term_orig.push_back(u);
+      }
+      if (mi.has_br) {
+        int b = s.branch[i];
+        if (b < T.n_nodes || b >= n) { err = "branch index out of range"; return false; }
+        T.term_orig.push_back(b);
+      }
+    }
+    for (size_t k = 0; k < (size_t)mi.npar * s.n_inst; ++k) T.par.push_back(s.par[k]);
+    // PWL references must lie inside the table
+    if ((s.model == CEDAR_V || s.model == CEDAR_I)) {
+      for (int i = 0; i < s.n_inst; ++i) {
+        int kind = (int)s.par[2 * s.n_inst + i];
+        if (kind < 0 || kind > 3) { err = "bad waveform kind"; return false; }
+        if (kind == CEDAR_WAVE_PWL) {
+          double off = s.par[3 * s.n_inst + i], np = s.par[4 * s.n_inst + i];
+          if (off < 0 || np < 1 || off + 2 * np > (double)T.pwl.size()) { err = "PWL reference outside table"; return false; }
+        }
+        if (kind != CEDAR_WAVE_DC) { T.src_group.push_back(g); T.src_inst.push_back(i); }
+      }
+    }
+    term_off += gi.ntx * s.n_inst; par_off += mi.npar * s.n_inst;
+    dpar_off += mi.ndpar * s.n_inst; out_off += mi.nout * s.n_inst;
+    T.groups.push_back(gi);
+  }
+  T.par_size = par_off; T.dpar_size = dpar_off; T.n_out = out_off;
+
+  // stamps in device order
+  std::vector<Stamp> SJ, SF, SQ;
+  for (const GroupInfo &g : T.groups) {
+    const ModelInfo &mi = kModels[g.model];
+    for (int i = 0; i < g.n_inst; ++i)
+      device_stamps(g.model, &T.term_orig[g.term_off + (size_t)i * g.ntx], g.out_off + i * mi.nout, SJ, SF, SQ);
+  }
+  // original pattern
+  std::vector<std::vector<int>> colrows(n), rowcols(n);
+  for (const Stamp &s : SJ) { colrows[s.col].push_back(s.row); rowcols[s.row].push_back(s.col); }
+  for (int u = 0; u < n; ++u) {
+    auto &v = colrows[u]; std::sort(v.begin(), v.end()); v.erase(std::unique(v.begin(), v.end()), v.end());
+    auto &w = rowcols[u]; std::sort(w.begin(), w.end()); w.erase(std::unique(w.begin(), w.end()), w.end());
+  }
+  T.j_colptr.assign(n + 1, 0);
+  for (int u = 0; u < n; ++u) T.j_colptr[u + 1] = T.j_colptr[u] + (int)colrows[u].size();
+  T.j_rowidx.clear();
+  for (int u = 0; u < n; ++u) for (int e : colrows[u]) T.j_rowidx.push_back(e);
+  for (int u = 0; u < n; ++u) if (colrows[u].empty()) { err = "structurally singular: unknown " + std::to_string(u) + " appears in no equation"; return false; }
+
+  // static pivoting
+  if (!match_columns(n, colrows, rowcols, T.rowmatch)) { err = "structurally singular system (no perfect matching)"; return false; }
+  // B[u'][u] = J[rowmatch[u']][u]; symmetric pattern of B + B^T
+  std::vector<int> eq2u(n);
+  for (int u = 0; u < n; ++u) eq2u[T.rowmatch[u]] = u;
+  std::vector<std::set<int>> adj(n);
+  for (int u = 0; u < n; ++u)
+    for (int e : colrows[u]) { int up = eq2u[e]; if (up != u) { adj[up].insert(u); adj[u].insert(up); } }
+  // node diagonals (KCL(u), u) join the factorisation pattern (not the J pattern)
+  // so that the DC gmin homotopy has a slot to stamp into; they take no part in
+  // the matching above, which only sees structurally nonzero entries.
+  for (int u = 0; u < T.n_nodes; ++u) {
+    auto &v = colrows[u];
+    if (!std::binary_search(v.begin(), v.end(), u)) { v.insert(std::lower_bound(v.begin(), v.end(), u), u); }
+    int up = eq2u[u]; if (up != u) { adj[up].insert(u); adj[u].insert(up); }
+  }
+  if (ordering == ORDER_NATURAL) { T.order.resize(n); for (int i = 0; i < n; ++i) T.order[i] = i; }
+  else min_degree(n, adj, T.order);
+  T.iorder.assign(n, 0);
+  for (int p = 0; p < n; ++p) T.iorder[T.order[p]] = p;
+  T.eq_pos.assign(n, 0);
+  for (int u = 0; u < n; ++u) T.eq_pos[T.rowmatch[u]] = T.iorder[u];
+  T.is_node_int.assign(n, 0);
+  for (int p = 0; p < n; ++p) T.is_node_int[p] = T.order[p] < T.n_nodes ? 1 : 0;
+  T.term_int.resize(T.term_orig.size());
+  for (size_t k = 0; k < T.term_orig.size(); ++k) T.term_int[k] = T.term_orig[k] < 0 ? -1 : T.iorder[T.term_orig[k]];
+
+  // symbolic LU of M[p][q] = J[eq(p)][order(q)]
+  std::vector<std::vector<int>> rows(n), cols(n);
+  for (int u = 0; u < n; ++u)
+    for (int e : colrows[u]) { int p = T.eq_pos[e], q = T.iorder[u]; rows[p].push_back(q); cols[q].push_back(p); }
+  for (int p = 0; p < n; ++p) { std::sort(rows[p].begin(), rows[p].end()); }
+  for (int k = 0; k < n; ++k) {
+    auto &ck = cols[k]; std::sort(ck.begin(), ck.end()); ck.erase(std::unique(ck.begin(), ck.end()), ck.end());
+    if (!std::binary_search(rows[k].begin(), rows[k].end(), k)) { err = "internal: missing diagonal after matching"; return false; }
+    std::vector<int> upper; for (int q : rows[k]) if (q > k) upper.push_back(q);
+    for (int i : ck) {
+      if (i <= k) continue;
+      std::vector<int> merged; merged.reserve(rows[i].size() + upper.size());
+      std::set_union(rows[i].begin(), rows[i].end(), upper.begin(), upper.end(), std::back_inserter(merged));
+      if (merged.size() != rows[i].size()) {
+        std::vector<int> added; std::set_difference(merged.begin(), merged.end(), rows[i].begin(), rows[i].end(), std::back_inserter(added));
+        for (int q : added) cols[q].push_back(i);
+        rows[i].swap(merged);
+      }
+    }
+  }
+  T.lu_rowptr.assign(n + 1, 0);
+  for (int p = 0; p < n; ++p) T.lu_rowptr[p + 1] = T.lu_rowptr[p] + (int)rows[p].size();
+  T.nnz_lu = T.lu_rowptr[n];
+  T.lu_colidx.clear(); T.lu_colidx.reserve(T.nnz_lu);
+  for (int p = 0; p < n; ++p) for (int q : rows[p]) T.lu_colidx.push_back(q);
+  T.lu_diag.assign(n, -1);
+  auto slot = [&](int p, int q) -> int {
+    auto b = T.lu_colidx.begin() + T.lu_rowptr[p], e = T.lu_colidx.begin() + T.lu_rowptr[p + 1];
+    auto it = std::lower_bound(b, e, q);
+    return (it != e && *it == q) ? (int)(it - T.lu_colidx.begin()) : -1;
+  };
+  for (int p = 0; p < n; ++p) T.lu_diag[p] = slot(p, p);
+  T.gs_slot.assign(T.n_nodes, -1);
+  for (int u = 0; u < T.n_nodes; ++u) T.gs_slot[u] = slot(T.eq_pos[u], T.iorder[u]);
+  // LU column structure (rows per column, sorted)
+  std::vector<std::vector<int>> lucol(n);
+  for (int p = 0; p < n; ++p) for (int q : rows[p]) lucol[q].push_back(p);
+
+  // stamp programs
+  {
+    std::vector<std::pair<int, int32_t>> it;
+    for (const Stamp &s : SJ) it.push_back({slot(T.eq_pos[s.row], T.iorder[s.col]), enc(s)});
+    build_program(T.nnz_lu, it, T.jlu_ptr, T.jlu_ent);
+    it.clear();
+    for (const Stamp &s : SJ) {
+      auto b = T.j_rowidx.begin() + T.j_colptr[s.col], e = T.j_rowidx.begin() + T.j_colptr[s.col + 1];
+      int k = (int)(std::lower_bound(b, e, s.row) - T.j_rowidx.begin());
+      it.push_back({k, enc(s)});
+    }
+    build_program((int)T.j_rowidx.size(), it, T.jcsc_ptr, T.jcsc_ent);
+    it.clear();
+    for (const Stamp &s : SF) it.push_back({T.eq_pos[s.row], enc(s)});
+    build_program(n, it, T.fint_ptr, T.fint_ent);
+    it.clear();
+    for (const Stamp &s : SF) it.push_back({s.row, enc(s)});
+    build_program(n, it, T.forg_ptr, T.forg_ent);
+    it.clear();
+    for (const Stamp &s : SQ) it.push_back({T.eq_pos[s.row], enc(s)});
+    build_program(n, it, T.qint_ptr, T.qint_ent);
+  }
+
+  // factorisation tasks
+  struct Task { int slot, info, lev; std::vector<std::pair<int, int>> pairs; };
+  std::vector<Task> tasks; tasks.reserve(T.nnz_lu);
+  std::vector<int> lev(T.nnz_lu, -1);
+  auto make_task = [&](int i, int j) {
+    int s = slot(i, j); int m = std::min(i, j);
+    Task tk; tk.slot = s; tk.info = (j << 2) | (i == j ? 1 : (i > j ? 2 : 0));
+    // pairs k < m with (i,k) and (k,j)
+    const int *ri = &T.lu_colidx[T.lu_rowptr[i]]; int nri = T.lu_rowptr[i + 1] - T.lu_rowptr[i];
+    const std::vector<int> &cj = lucol[j];
+    int a = 0, b = 0, L = 0;
+    while (a < nri && b < (int)cj.size()) {
+      int ka = ri[a], kb = cj[b];
+      if (ka >= m || kb >= m) break;
+      if (ka == kb) { int sa = T.lu_rowptr[i] + a, sb = slot(ka, j); tk.pairs.push_back({sa, sb}); L = std::max(L, std::max(lev[sa], lev[sb]) + 1); ++a; ++b; }
+      else if (ka < kb) ++a; else ++b;
+    }
+    if (i > j) L = std::max(L, lev[T.lu_diag[j]] + 1);
+    tk.lev = L; lev[s] = L;
+    tasks.push_back(std::move(tk));
+  };
+  for (int m = 0; m < n; ++m) {
+    make_task(m, m);
+    for (int k = T.lu_rowptr[m]; k < T.lu_rowptr[m + 1]; ++k) if (T.lu_colidx[k] > m) make_task(m, T.lu_colidx[k]);
+    for (int i : lucol[m]) if (i > m) make_task(i, m);
+  }
+  int nlev = 0; for (auto &t : tasks) nlev = std::max(nlev, t.lev + 1);
+  std::stable_sort(tasks.begin(), tasks.end(), [](const Task &a, const Task &b) {
+    if (a.lev != b.lev) return a.lev < b.lev;
+    return a.pairs.size() > b.pairs.size();
+  });
+  T.lu_lvl_ptr.assign(nlev + 1, 0);
+  for (auto &t : tasks) T.lu_lvl_ptr[t.lev + 1]++;
+  for (int l = 0; l < nlev; ++l) T.lu_lvl_ptr[l + 1] += T.lu_lvl_ptr[l];
+  T.lu_task_slot.clear(); T.lu_task_info.clear(); T.lu_pair_ptr.assign(1, 0); T.lu_pair_a.clear(); T.lu_pair_b.clear();
+  T.lu_flops = 0;
+  for (auto &t : tasks) {
+    T.lu_task_slot.push_back(t.slot); T.lu_task_info.push_back(t.info);
+    for (auto &p : t.pairs) { T.lu_pair_a.push_back(p.first); T.lu_pair_b.push_back(p.second); }
+    T.lu_pair_ptr.push_back((int)T.lu_pair_a.size());
+    T.lu_flops += 2 * (int64_t)t.pairs.size() + ((t.info & 3) != 0 ? 1 : 0);
+  }
+
+  // triangular solves
+  {
+    std::vector<int> lf(n, 0);
+    for (int i = 0; i < n; ++i) { int L = 0; for (int k = T.lu_rowptr[i]; k < T.lu_diag[i]; ++k) L = std::max(L, lf[T.lu_colidx[k]] + 1); lf[i] = L; }
+    std::vector<int> lb(n, 0);
+    for (int i = n - 1; i >= 0; --i) { int L = 0; for (int k = T.lu_diag[i] + 1; k < T.lu_rowptr[i + 1]; ++k) L = std::max(L, lb[T.lu_colidx[k]] + 1); lb[i] = L; }
+    auto emit = [&](const std::vector<int> &lv, bool fw, std::vector<int32_t> &lp, std::vector<int32_t> &rw,
+                    std::vector<int32_t> &pp, std::vector<int32_t> &pl, std::vector<int32_t> &pc) {
+      int nl = 0; for (int v : lv) nl = std::max(nl, v + 1);
+      std::vector<int> idx(n); for (int i = 0; i < n; ++i) idx[i] = i;
+      std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return lv[a] < lv[b]; });
+      lp.assign(nl + 1, 0); for (int i = 0; i < n; ++i) lp[lv[i] + 1]++;
+      for (int l = 0; l < nl; ++l) lp[l + 1] += lp[l];
+      rw.clear(); pp.assign(1, 0); pl.clear(); pc.clear();
+      for (int i : idx) {
+        rw.push_back(i);
+        int k0 = fw ? T.lu_rowptr[i] : T.lu_diag[i] + 1, k1 = fw ? T.lu_diag[i] : T.lu_rowptr[i + 1];
+        for (int k = k0; k < k1; ++k) { pl.push_back(k); pc.push_back(T.lu_colidx[k]); }
+        pp.push_back((int)pl.size());
+      }
+    };
+    emit(lf, true, T.fw_lvl_ptr, T.fw_row, T.fw_ptr, T.fw_lu, T.fw_col);
+    emit(lb, false, T.bw_lvl_ptr, T.bw_row, T.bw_ptr, T.bw_lu, T.bw_col);
+  }
+  return true;
+}
+
+}  // namespace cedar

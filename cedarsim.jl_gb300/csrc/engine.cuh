@@ -1,0 +1,539 @@
+// engine.cuh — per-instance transient engine, run by a cooperating thread group.
+//
+// One group (a tile of K lanes of a warp, or a whole CTA) owns one circuit
+// instance: its Newton iterate, integrator history, LU values and device
+// outputs live in the group's workspace (shared memory when it fits).  Each
+// Newton iteration is
+//   K1  device evaluation        (threads over devices)
+//   K2  stamping J and F          (threads over LU slots / rows, fixed-order sums)
+//   K4  LU refactorisation        (level by level, threads over entry tasks)
+//   K5  forward/back substitution (level by level, threads over rows)
+//   K6  update + convergence test (threads over unknowns, group vote)
+// with one group barrier per phase / level.  All control decisions are taken
+// redundantly by every thread from group-reduced values, so the group never
+// diverges; no atomics are used, so results are bitwise reproducible.
+#pragma once
+#include <cstdint>
+#include "models.cuh"
+
+namespace cedar {
+
+struct DGroup { int model, n_inst, ntx, term_off, par_off, dpar_off, out_off; };
+
+// Device view of a compiled template (all pointers to device memory).
+struct DTpl {
+  int n, n_nodes, nnz_lu, n_out, n_groups, n_dev, n_src, lu_nlev, fw_nlev, bw_nlev, n_csc, dpar_size;
+  double gmin, vt;
+  const DGroup *grp;
+  const int *dev_end;      // [n_groups] cumulative device count
+  const int *term;         // internal unknown per terminal (-1 ground)
+  const int *term_orig;    // original unknown per terminal
+  const int *jlu_ptr, *jlu_ent, *fint_ptr, *fint_ent, *qint_ptr, *qint_ent;
+  const int *jcsc_ptr, *jcsc_ent, *forg_ptr, *forg_ent;
+  const int *lu_lvl, *lu_slot, *lu_info, *lu_pp; const int2 *lu_pair;
+  const int *fw_lvl, *fw_row, *fw_ptr; const int2 *fw_pair;
+  const int *bw_lvl, *bw_row, *bw_ptr; const int2 *bw_pair;
+  const int *src_off, *src_stride;    // derived-param offset / stride per source
+  const int *gs_slot;                 // [n_nodes] LU slot of (KCL(u),u)
+  const int *gs_row;                  // [n_nodes] internal row of KCL(u)
+  const int *gs_col;                  // [n_nodes] internal column of u
+  const unsigned char *is_node;       // [n] internal
+  const int *order;                   // internal position -> original unknown
+  const int *iorder;                  // original unknown -> internal position
+  const int *eq_pos;                  // original equation -> internal row
+  const double *pwl;
+};
+
+// workspace size in doubles for one instance
+__host__ __device__ inline int ws_doubles(int n, int nnz_lu, int n_out) {
+  return 13 * n + nnz_lu + n_out + 8;
+}
+
+struct WS {
+  double *x, *xn, *xm1, *xm2, *qn, *qm1, *qd, *hist, *F, *lu, *rd, *dout, *qt, *xs, *x0;
+  __device__ void bind(double *base, int n, int nnz_lu, int n_out) {
+    double *p = base;
+    x = p; p += n; xn = p; p += n; xm1 = p; p += n; xm2 = p; p += n; qn = p; p += n; qm1 = p; p += n;
+    qd = p; p += n; hist = p; p += n; F = p; p += n; rd = p; p += n; qt = p; p += n; xs = p; p += n; x0 = p; p += n;
+    lu = p; p += nnz_lu; dout = p; p += n_out;
+  }
+};
+
+// ------------------------------------------------------------- thread groups
+template <int K>
+struct TileGroup {
+  unsigned mask; int rank;
+  static constexpr int size = K;
+  __device__ TileGroup() {
+    int lane = threadIdx.x & 31; rank = lane % K;
+    mask = (K == 32) ? 0xffffffffu : (((1u << K) - 1u) << (lane - rank));
+  }
+  __device__ __forceinline__ void sync() const { if (K > 1) __syncwarp(mask); }
+  __device__ __forceinline__ bool any(bool p) const { return K == 1 ? p : (__any_sync(mask, p) != 0); }
+  __device__ __forceinline__ double max(double v) const {
+#pragma unroll
+    for (int o = K / 2; o > 0; o >>= 1) { double w = __shfl_xor_sync(mask, v, o, K); v = w > v ? w : v; }
+    return v;
+  }
+  __device__ __forceinline__ double min(double v) const {
+#pragma unroll
+    for (int o = K / 2; o > 0; o >>= 1) { double w = __shfl_xor_sync(mask, v, o, K); v = w < v ? w : v; }
+    return v;
+  }
+  __device__ __forceinline__ int bcast(int v) const { return K == 1 ? v : __shfl_sync(mask, v, 0, K); }
+};
+
+struct BlockGroup {
+  int rank, size;
+  double *red;  // shared scratch of >= 32 doubles
+  __device__ BlockGroup(double *r) : rank(threadIdx.x), size(blockDim.x), red(r) {}
+  __device__ __forceinline__ void sync() const { __syncthreads(); }
+  __device__ __forceinline__ bool any(bool p) const { return __syncthreads_or(p) != 0; }
+  __device__ double reduce(double v, bool is_max) const {
+    for (int o = 16; o > 0; o >>= 1) { double w = __shfl_xor_sync(0xffffffffu, v, o); v = is_max ? (w > v ? w : v) : (w < v ? w : v); }
+    int warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[warp] = v;
+    __syncthreads();
+    double r = red[0];
+    for (int i = 1; i < nw; ++i) { double w = red[i]; r = is_max ? (w > r ? w : r) : (w < r ? w : r); }
+    __syncthreads();
+    return r;
+  }
+  __device__ double max(double v) const { return reduce(v, true); }
+  __device__ double min(double v) const { return reduce(v, false); }
+  __device__ int bcast(int v) const {
+    __syncthreads();
+    if (threadIdx.x == 0) ((int *)red)[0] = v;
+    __syncthreads();
+    int r = ((int *)red)[0];
+    __syncthreads();
+    return r;
+  }
+};
+
+// ------------------------------------------------------------- options
+struct EngOpts {
+  int method, adaptive, dcop, max_newton;
+  long long max_steps;
+  double tstart, tstop, h, hmin, hmax, reltol, abstol_v, abstol_i, nr_factor, hfirst_frac;
+};
+
+struct EngStats {
+  long long accepted, rejected, newton_iters, dc_iters;
+  double hmin_seen, hmax_seen;
+  int status;
+};
+
+// Output sink: record every accepted point (plain) and/or probe samples (batch).
+struct Sink {
+  double *t_out, *x_out; long long cap, count;   // record mode (x in original order)
+  const int *probes_int; int np, ns; double *samp; int next;
+  double tstart, tstop;
+};
+
+__device__ __forceinline__ double quant_factor(double f) {
+  double q = floor(f * 8.0) / 8.0;
+  return q < 0.125 ? 0.125 : (q > 2.0 ? 2.0 : q);
+}
+
+template <class G>
+struct Engine {
+  const DTpl &T;
+  const double *dp;   // derived params of this instance
+  WS w;
+  G g;
+
+  __device__ Engine(const DTpl &t, const double *dpar, double *ws, G grp) : T(t), dp(dpar), g(grp) {
+    w.bind(ws, T.n, T.nnz_lu, T.n_out);
+  }
+
+  // K1: evaluate devices at x (internal order); q_only restricts to charge devices
+  __device__ void eval_devices(const double *x, const EvalCtx &ctx, bool q_only) {
+    for (int d = g.rank; d < T.n_dev; d += g.size) {
+      int gi = 0;
+      while (d >= T.dev_end[gi]) ++gi;
+      const DGroup gr = T.grp[gi];
+      if (q_only && gr.model != CEDAR_C && gr.model != CEDAR_L) continue;
+      int i = d - (gi ? T.dev_end[gi - 1] : 0);
+      const int *tm = T.term + gr.term_off + i * gr.ntx;
+      double v[5];
+      for (int k = 0; k < gr.ntx; ++k) { int u = tm[k]; v[k] = u < 0 ? 0.0 : x[u]; }
+      eval_device(gr.model, dp + gr.dpar_off + i, gr.n_inst, v, nullptr, ctx, T.pwl,
+                  w.dout + gr.out_off + i * model_nout(gr.model));
+    }
+  }
+
+  __device__ __forceinline__ double gather(const int *ptr, const int *ent, int s, double acc) const {
+    int a = ptr[s], b = ptr[s + 1];
+    for (int k = a; k < b; ++k) { int e = ent[k]; double v = w.dout[e >> 1]; acc = (e & 1) ? acc - v : acc + v; }
+    return acc;
+  }
+
+  // K2: J slots and residual rows (F = hist + contributions)
+  __device__ void stamp(const double *hist, double gshunt, const double *x) {
+    for (int s = g.rank; s < T.nnz_lu; s += g.size) w.lu[s] = gather(T.jlu_ptr, T.jlu_ent, s, 0.0);
+    for (int r = g.rank; r < T.n; r += g.size) w.F[r] = gather(T.fint_ptr, T.fint_ent, r, hist ? hist[r] : 0.0);
+    if (gshunt != 0.0) {
+      g.sync();
+      for (int u = g.rank; u < T.n_nodes; u += g.size) {
+        w.lu[T.gs_slot[u]] -= gshunt;
+        w.F[T.gs_row[u]] -= gshunt * x[T.gs_col[u]];
+      }
+    }
+  }
+
+  // charges at x into qt (internal rows)
+  __device__ void eval_q(const double *x, const EvalCtx &ctx, double *q) {
+    eval_devices(x, ctx, true);
+    g.sync();
+    for (int r = g.rank; r < T.n; r += g.size) q[r] = gather(T.qint_ptr, T.qint_ent, r, 0.0);
+    g.sync();
+  }
+
+  // K4: level-scheduled Crout LU in place; returns false on a zero pivot
+  __device__ bool factor() {
+    bool bad = false;
+    for (int l = 0; l < T.lu_nlev; ++l) {
+      int t0 = T.lu_lvl[l], t1 = T.lu_lvl[l + 1];
+      for (int t = t0 + g.rank; t < t1; t += g.size) {
+        int s = T.lu_slot[t], info = T.lu_info[t];
+        double acc = w.lu[s];
+        for (int k = T.lu_pp[t]; k < T.lu_pp[t + 1]; ++k) { int2 p = T.lu_pair[k]; acc -= w.lu[p.x] * w.lu[p.y]; }
+        int kind = info & 3, j = info >> 2;
+        if (kind == 2) acc *= w.rd[j];
+        else if (kind == 1) {
+          if (!(fabs(acc) > 1e-300) || !(fabs(acc) < 1e300)) bad = true;
+          w.rd[j] = 1.0 / acc;
+        }
+        w.lu[s] = acc;
+      }
+      g.sync();
+    }
+    return !g.any(bad);
+  }
+
+  // K5: solve LU y = b in place (b = F)
+  __device__ void solve(double *b) {
+    for (int l = 0; l < T.fw_nlev; ++l) {
+      for (int t = T.fw_lvl[l] + g.rank; t < T.fw_lvl[l + 1]; t += g.size) {
+        int i = T.fw_row[t]; double acc = b[i];
+        for (int k = T.fw_ptr[t]; k < T.fw_ptr[t + 1]; ++k) { int2 p = T.fw_pair[k]; acc -= w.lu[p.x] * b[p.y]; }
+        b[i] = acc;
+      }
+      g.sync();
+    }
+    for (int l = 0; l < T.bw_nlev; ++l) {
+      for (int t = T.bw_lvl[l] + g.rank; t < T.bw_lvl[l + 1]; t += g.size) {
+        int i = T.bw_row[t]; double acc = b[i];
+        for (int k = T.bw_ptr[t]; k < T.bw_ptr[t + 1]; ++k) { int2 p = T.bw_pair[k]; acc -= w.lu[p.x] * b[p.y]; }
+        b[i] = acc * w.rd[i];
+      }
+      g.sync();
+    }
+  }
+
+  // Newton on Fi(x,t) + cj Fq(x) + hist = 0.  Returns iterations (>0), -iters on
+  // failure, 0 on a zero pivot.  Mirrors the oracle's newton().
+  __device__ int newton(double *x, const EvalCtx &ctx, const double *hist, double rel, double av, double ai,
+                        int maxit, double vlim, double gshunt) {
+    for (int it = 1; it <= maxit; ++it) {
+      eval_devices(x, ctx, false);
+      g.sync();
+      stamp(hist, gshunt, x);
+      g.sync();
+      if (!factor()) return 0;
+      solve(w.F);
+      // dx = -F ; finiteness and DC damping
+      bool nonfinite = false; double mx = 0.0;
+      for (int i = g.rank; i < T.n; i += g.size) {
+        double d = w.F[i];
+        if (!(fabs(d) < 1e300)) nonfinite = true;
+        if (T.is_node[i]) { double a = fabs(d); mx = a > mx ? a : mx; }
+      }
+      if (g.any(nonfinite)) return -it;
+      double scale = 1.0;
+      if (vlim > 0) { mx = g.max(mx); if (mx > vlim) scale = vlim / mx; }
+      bool conv = (scale == 1.0);
+      for (int i = g.rank; i < T.n; i += g.size) {
+        double d = -w.F[i] * scale;
+        double xi = x[i] + d;
+        x[i] = xi;
+        double lim = rel * fabs(xi) + (T.is_node[i] ? av : ai);
+        if (!(fabs(d) <= lim)) conv = false;
+      }
+      bool notconv = g.any(!conv);
+      g.sync();
+      if (!notconv) return it;
+    }
+    return -maxit;
+  }
+
+  __device__ void copy(double *dst, const double *src) {
+    for (int i = g.rank; i < T.n; i += g.size) dst[i] = src[i];
+  }
+  __device__ void fill(double *dst, double v) {
+    for (int i = g.rank; i < T.n; i += g.size) dst[i] = v;
+  }
+
+  __device__ double next_bp(double t, double eps) {
+    double best = 1e300;
+    for (int s = g.rank; s < T.n_src; s += g.size) {
+      double b = source_next_bp(dp + T.src_off[s], T.src_stride[s], t, eps, T.pwl);
+      best = b < best ? b : best;
+    }
+    return g.min(best);
+  }
+
+  // DC operating point (mirrors the oracle's dcop()); x internal order.
+  __device__ int dcop(double *x, double t, double rel, double av, double ai, long long *iters) {
+    const int maxit = 100; const double vlim = 0.5;
+    EvalCtx ctx{t, 0.0, 1.0, T.gmin, true, false};
+    copy(w.x0, x);
+    g.sync();
+    int r = newton(x, ctx, nullptr, rel, av, ai, maxit, vlim, 0.0);
+    *iters += r < 0 ? -r : r;
+    if (r > 0) return CEDAR_ST_OK;
+    fill(x, 0.0);
+    g.sync();
+    double lam = 0.0, dl = 0.1; int halv = 0; bool ok = true;
+    while (lam < 1.0) {
+      double ln = lam + dl < 1.0 ? lam + dl : 1.0;
+      copy(w.xs, x);
+      g.sync();
+      ctx.src_scale = ln;
+      r = newton(w.xs, ctx, nullptr, rel, av, ai, maxit, vlim, 0.0);
+      *iters += r < 0 ? -r : r;
+      if (r > 0) { copy(x, w.xs); g.sync(); lam = ln; halv = 0; dl = dl * 2 < 0.1 ? dl * 2 : 0.1; }
+      else { dl *= 0.5; if (++halv > 8) { ok = false; break; } }
+    }
+    ctx.src_scale = 1.0;
+    if (ok) return CEDAR_ST_OK;
+    copy(x, w.x0);
+    g.sync();
+    for (double gs = 1e-2; gs >= 1e-12 * 0.999; gs *= 0.1) {
+      r = newton(x, ctx, nullptr, rel, av, ai, maxit, vlim, gs);
+      *iters += r < 0 ? -r : r;
+      if (r <= 0) return CEDAR_ST_DCOP;
+    }
+    r = newton(x, ctx, nullptr, rel, av, ai, maxit, vlim, 0.0);
+    *iters += r < 0 ? -r : r;
+    return r > 0 ? CEDAR_ST_OK : CEDAR_ST_DCOP;
+  }
+
+  // ---- output sink helpers
+  __device__ void sink_point(Sink &sk, double t, const double *x) {
+    if (sk.t_out) {
+      if (sk.count < sk.cap) {
+        if (g.rank == 0) sk.t_out[sk.count] = t;
+        for (int i = g.rank; i < T.n; i += g.size) sk.x_out[sk.count * T.n + T.order[i]] = x[i];
+      }
+      sk.count++;
+    }
+  }
+  __device__ double sample_ts(const Sink &sk, int j) const {
+    return j == sk.ns - 1 ? sk.tstop : sk.tstart + (sk.tstop - sk.tstart) * ((double)j / (double)(sk.ns - 1));
+  }
+  __device__ void sink_start(Sink &sk, const double *x) {
+    if (!sk.samp || sk.ns <= 0) return;
+    for (int p = g.rank; p < sk.np; p += g.size) { int u = sk.probes_int[p]; sk.samp[(long long)p * sk.ns] = u >= 0 ? x[u] : 0.0; }
+    sk.next = 1;
+  }
+  __device__ void sink_step(Sink &sk, bool have0, double t0, const double *x0, double t1, const double *x1,
+                            double t2, const double *x2) {
+    if (!sk.samp) return;
+    while (sk.next < sk.ns && sample_ts(sk, sk.next) <= t2) {
+      double t = sample_ts(sk, sk.next);
+      for (int p = g.rank; p < sk.np; p += g.size) {
+        int u = sk.probes_int[p]; double v;
+        if (u < 0) v = 0.0;
+        else if (have0) {
+          double L0 = (t - t1) * (t - t2) / ((t0 - t1) * (t0 - t2));
+          double L1 = (t - t0) * (t - t2) / ((t1 - t0) * (t1 - t2));
+          double L2 = (t - t0) * (t - t1) / ((t2 - t0) * (t2 - t1));
+          v = x0[u] * L0 + x1[u] * L1 + x2[u] * L2;
+        } else {
+          double a = (t - t1) / (t2 - t1);
+          v = x1[u] + (x2[u] - x1[u]) * a;
+        }
+        sk.samp[(long long)p * sk.ns + sk.next] = v;
+      }
+      sk.next++;
+    }
+  }
+
+  // Whole transient (mirrors the oracle's tran()).  x: internal order, in/out.
+  __device__ void tran(double *x, const EngOpts &o, Sink &sk, EngStats &st, const double *perturb) {
+    const int n = T.n;
+    st.accepted = st.rejected = st.newton_iters = st.dc_iters = 0;
+    st.hmin_seen = 1e300; st.hmax_seen = 0; st.status = CEDAR_ST_OK;
+    const double rel = o.nr_factor * o.reltol, av = o.nr_factor * o.abstol_v, ai = o.nr_factor * o.abstol_i;
+    if (o.dcop) {
+      int s = dcop(x, o.tstart, rel, av, ai, &st.dc_iters);
+      if (s != CEDAR_ST_OK) { st.status = s; return; }
+    }
+    if (perturb) { for (int i = g.rank; i < n; i += g.size) x[i] += perturb[i]; g.sync(); }
+    EvalCtx ctx{o.tstart, 0.0, 1.0, T.gmin, false, false};
+    eval_q(x, ctx, w.qn);
+    copy(w.xn, x);
+    g.sync();
+    sink_point(sk, o.tstart, x);
+    sink_start(sk, x);
+    double *xp = x;   // Newton iterate / predictor lives in x
+    if (!o.adaptive) {
+      const double h = o.h;
+      const long long N = llround((o.tstop - o.tstart) / h);
+      fill(w.qd, 0.0);
+      double tprev = o.tstart, tprev2 = o.tstart; bool have_prev = false;
+      for (long long k = 1; k <= N; ++k) {
+        double t = (k == N) ? o.tstop : DADD(o.tstart, DMUL((double)k, h));
+        double hk = t - tprev, cj;
+        if (o.method == CEDAR_TRAP) {
+          cj = 2.0 / hk;
+          for (int i = g.rank; i < n; i += g.size) w.hist[i] = -cj * w.qn[i] - w.qd[i];
+        } else if (k == 1) {
+          cj = 1.0 / hk;
+          for (int i = g.rank; i < n; i += g.size) w.hist[i] = -w.qn[i] / hk;
+        } else {
+          cj = 1.5 / hk;
+          for (int i = g.rank; i < n; i += g.size) w.hist[i] = (-4.0 * w.qn[i] + w.qm1[i]) / (2.0 * hk);
+        }
+        if (k == 1) copy(xp, w.xn);
+        else for (int i = g.rank; i < n; i += g.size) xp[i] = 2.0 * w.xn[i] - w.xm1[i];
+        g.sync();
+        ctx.t = t; ctx.cj = cj;
+        int r = newton(xp, ctx, w.hist, rel, av, ai, o.max_newton, 0.0, 0.0);
+        st.newton_iters += r < 0 ? -r : r;
+        if (r <= 0) { st.status = r == 0 ? CEDAR_ST_ZERO_PIVOT : CEDAR_ST_NEWTON; copy(x, w.xn); g.sync(); return; }
+        eval_q(xp, ctx, w.qt);
+        for (int i = g.rank; i < n; i += g.size) {
+          if (o.method == CEDAR_TRAP) w.qd[i] = cj * w.qt[i] + w.hist[i];
+          w.qm1[i] = w.qn[i]; w.qn[i] = w.qt[i];
+        }
+        g.sync();
+        sink_step(sk, have_prev, tprev2, w.xm1, tprev, w.xn, t, xp);
+        g.sync();
+        bool nf = false;
+        for (int i = g.rank; i < n; i += g.size) { w.xm1[i] = w.xn[i]; w.xn[i] = xp[i]; if (!(fabs(xp[i]) < 1e300)) nf = true; }
+        nf = g.any(nf);
+        tprev2 = tprev; tprev = t; have_prev = true;
+        st.accepted++; st.hmin_seen = hk < st.hmin_seen ? hk : st.hmin_seen; st.hmax_seen = hk > st.hmax_seen ? hk : st.hmax_seen;
+        sink_point(sk, t, w.xn);
+        if (nf) { st.status = CEDAR_ST_NAN; return; }
+      }
+      return;
+    }
+    // ---- adaptive variable-step BDF2
+    const double span = o.tstop - o.tstart, eps_bp = span * 1e-12;
+    double t = o.tstart, tn1 = t, tn2 = t;
+    int npts = 1;
+    auto restart_h = [&](double tt) {
+      double nb = next_bp(tt, eps_bp); nb = nb < o.tstop ? nb : o.tstop;
+      double dist = nb - tt; dist = dist < o.hmax ? dist : o.hmax;
+      double hf = o.hfirst_frac * dist;
+      if (o.h > 0) hf = o.h < hf ? o.h : hf;
+      return hf;
+    };
+    double hnext = restart_h(t);
+    long long nsteps = 0;
+    while (t < o.tstop) {
+      if (++nsteps > o.max_steps) { st.status = CEDAR_ST_MAX_STEPS; break; }
+      double tb = next_bp(t, eps_bp); tb = tb < o.tstop ? tb : o.tstop;
+      double h = hnext < o.hmax ? hnext : o.hmax;
+      bool hit = false;
+      if (tb - t <= 1.1 * h) { h = tb - t; hit = true; }
+      double tnew = hit ? tb : t + h;
+      h = tnew - t;
+      int order = npts >= 2 ? 2 : 1;
+      double cj, h1 = t - tn1;
+      if (order == 1) {
+        cj = 1.0 / h;
+        for (int i = g.rank; i < n; i += g.size) w.hist[i] = -w.qn[i] / h;
+      } else {
+        double wr = h / h1;
+        cj = (1.0 + 2.0 * wr) / ((1.0 + wr) * h);
+        double a1 = -(1.0 + wr), a2 = wr * wr / (1.0 + wr);
+        for (int i = g.rank; i < n; i += g.size) w.hist[i] = (a1 * w.qn[i] + a2 * w.qm1[i]) / h;
+      }
+      if (npts >= 2) { double rr = h / h1; for (int i = g.rank; i < n; i += g.size) xp[i] = w.xn[i] + rr * (w.xn[i] - w.xm1[i]); }
+      else copy(xp, w.xn);
+      g.sync();
+      ctx.t = tnew; ctx.cj = cj;
+      int r = newton(xp, ctx, w.hist, rel, av, ai, o.max_newton, 0.0, 0.0);
+      st.newton_iters += r < 0 ? -r : r;
+      if (r <= 0) {
+        st.rejected++;
+        hnext = h * 0.125;
+        if (hnext < o.hmin) { st.status = r == 0 ? CEDAR_ST_ZERO_PIVOT : CEDAR_ST_DT_UNDERFLOW; break; }
+        continue;
+      }
+      double err = 0.0;
+      if (npts >= 3) {
+        double h2 = tn1 - tn2;
+        double coef = h * h * (h + h1) * (h + h1) / (2.0 * h + h1);
+        double e = 0.0;
+        for (int i = g.rank; i < n; i += g.size) {
+          if (!T.is_node[i]) continue;
+          double d10 = (xp[i] - w.xn[i]) / h;
+          double d21 = (w.xn[i] - w.xm1[i]) / h1;
+          double d32 = (w.xm1[i] - w.xm2[i]) / h2;
+          double dd2a = (d10 - d21) / (h + h1);
+          double dd2b = (d21 - d32) / (h1 + h2);
+          double dd3 = (dd2a - dd2b) / (h + h1 + h2);
+          double lte = fabs(dd3) * coef;
+          double ax = fabs(xp[i]), bx = fabs(w.xn[i]);
+          double sc = o.reltol * (ax > bx ? ax : bx) + o.abstol_v;
+          double q = lte / sc;
+          if (!(q <= 1e300)) q = 1e30;
+          e = q > e ? q : e;
+        }
+        err = g.max(e);
+      } else if (npts == 2) {
+        double e = 0.0;
+        for (int i = g.rank; i < n; i += g.size) {
+          if (!T.is_node[i]) continue;
+          double d10 = (xp[i] - w.xn[i]) / h;
+          double d21 = (w.xn[i] - w.xm1[i]) / h1;
+          double dd2 = (d10 - d21) / (h + h1);
+          double lte = fabs(dd2) * (h * h);
+          double ax = fabs(xp[i]), bx = fabs(w.xn[i]);
+          double sc = o.reltol * (ax > bx ? ax : bx) + o.abstol_v;
+          double q = lte / sc;
+          if (!(q <= 1e300)) q = 1e30;
+          e = q > e ? q : e;
+        }
+        err = g.max(e);
+      }
+      if (err > 1.0) {
+        st.rejected++;
+        hnext = h * quant_factor(0.9 * pow(err, -1.0 / 3.0));
+        if (hnext < o.hmin) { st.status = CEDAR_ST_DT_UNDERFLOW; break; }
+        continue;
+      }
+      eval_q(xp, ctx, w.qt);
+      for (int i = g.rank; i < n; i += g.size) { w.qm1[i] = w.qn[i]; w.qn[i] = w.qt[i]; }
+      g.sync();
+      sink_step(sk, npts >= 2, tn1, w.xm1, t, w.xn, tnew, xp);
+      g.sync();
+      bool nf = false;
+      for (int i = g.rank; i < n; i += g.size) {
+        w.xm2[i] = w.xm1[i]; w.xm1[i] = w.xn[i]; w.xn[i] = xp[i];
+        if (!(fabs(xp[i]) < 1e300)) nf = true;
+      }
+      nf = g.any(nf);
+      tn2 = tn1; tn1 = t; t = tnew;
+      st.accepted++; st.hmin_seen = h < st.hmin_seen ? h : st.hmin_seen; st.hmax_seen = h > st.hmax_seen ? h : st.hmax_seen;
+      sink_point(sk, t, w.xn);
+      if (nf) { st.status = CEDAR_ST_NAN; break; }
+      if (npts < 3) ++npts;
+      double fac = (err > 0.0) ? quant_factor(0.9 * pow(err, -1.0 / 3.0)) : 1.0;
+      hnext = h * fac;
+      if (hit && t < o.tstop) { npts = 1; hnext = restart_h(t); }
+    }
+    copy(x, w.xn);
+    g.sync();
+    if (st.status == CEDAR_ST_OK && t < o.tstop) st.status = CEDAR_ST_MAX_STEPS;
+  }
+};
+
+}  // namespace cedar

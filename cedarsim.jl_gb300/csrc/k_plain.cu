@@ -1,0 +1,133 @@
+// k_plain.cu — parameter derivation, the drop-in residual/Jacobian kernels
+// (cedar_eval) and the single-instance block engine (Newton / DC / transient).
+#include "kernels.cuh"
+
+namespace cedar {
+
+__device__ __forceinline__ int find_group(const DTpl &T, int d) {
+  int gi = 0;
+  while (d >= T.dev_end[gi]) ++gi;
+  return gi;
+}
+
+// One CTA per instance: raw parameter block -> derived parameter block.
+__global__ void derive_kernel(const DTpl *tpls, const int *inst_tpl, const long long *raw_off, const double *raw,
+                              const long long *dpar_off, double *dpar, int n_inst) {
+  int inst = blockIdx.x;
+  if (inst >= n_inst) return;
+  const DTpl &T = tpls[inst_tpl ? inst_tpl[inst] : 0];
+  const double *r = raw + raw_off[inst];
+  double *d = dpar + dpar_off[inst];
+  for (int dv = threadIdx.x; dv < T.n_dev; dv += blockDim.x) {
+    int gi = find_group(T, dv);
+    const DGroup gr = T.grp[gi];
+    int i = dv - (gi ? T.dev_end[gi - 1] : 0);
+    derive_one(gr.model, r + gr.par_off + i, gr.n_inst, d + gr.dpar_off + i, gr.n_inst, T.vt);
+  }
+}
+
+cudaError_t launch_derive(const DTpl *tpls_dev, const int *inst_tpl, const long long *raw_off, const double *raw,
+                          const long long *dpar_off, double *dpar, int n_inst, int max_dev, cudaStream_t s) {
+  if (n_inst <= 0) return cudaSuccess;
+  int threads = max_dev >= 256 ? 256 : ((max_dev + 31) / 32) * 32;
+  if (threads < 32) threads = 32;
+  derive_kernel<<<n_inst, threads, 0, s>>>(tpls_dev, inst_tpl, raw_off, raw, dpar_off, dpar, n_inst);
+  return cudaGetLastError();
+}
+
+// K1 (grid-wide): one thread per device instance.  Parameters are SoA, so a warp
+// reads each parameter as one contiguous 256-byte segment; outputs are written
+// contiguously per device (a warp writes one contiguous span).
+__global__ void eval_kernel(DTpl T, const double *dpar, const double *x, const double *xdot, double t, double cj,
+                            double *dout) {
+  int d = blockIdx.x * blockDim.x + threadIdx.x;
+  if (d >= T.n_dev) return;
+  int gi = find_group(T, d);
+  const DGroup gr = T.grp[gi];
+  int i = d - (gi ? T.dev_end[gi - 1] : 0);
+  const int *tm = T.term_orig + gr.term_off + i * gr.ntx;
+  double v[5], vd[5];
+  for (int k = 0; k < gr.ntx; ++k) {
+    int u = tm[k];
+    v[k] = u < 0 ? 0.0 : __ldg(x + u);
+    vd[k] = (u < 0 || !xdot) ? 0.0 : __ldg(xdot + u);
+  }
+  EvalCtx ctx{t, cj, 1.0, T.gmin, false, true};
+  eval_device(gr.model, dpar + gr.dpar_off + i, gr.n_inst, v, vd, ctx, T.pwl, dout + gr.out_off + i * model_nout(gr.model));
+}
+
+// K2+K3 (grid-wide): J values in CSC order and residual rows, fixed-order sums.
+__global__ void stamp_kernel(DTpl T, const double *dout, double *F, double *J) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (J && s < T.n_csc) {
+    double acc = 0.0;
+    for (int k = T.jcsc_ptr[s]; k < T.jcsc_ptr[s + 1]; ++k) { int e = __ldg(T.jcsc_ent + k); double v = __ldg(dout + (e >> 1)); acc = (e & 1) ? acc - v : acc + v; }
+    J[s] = acc;
+  }
+  if (F && s < T.n) {
+    double acc = 0.0;
+    for (int k = T.forg_ptr[s]; k < T.forg_ptr[s + 1]; ++k) { int e = __ldg(T.forg_ent + k); double v = __ldg(dout + (e >> 1)); acc = (e & 1) ? acc - v : acc + v; }
+    F[s] = acc;
+  }
+}
+
+cudaError_t launch_eval(const DTpl &T, const DTpl *T_dev, const double *dpar, const double *x, const double *xdot,
+                        double t, double cj, double *dout, double *F, double *J, cudaStream_t s) {
+  (void)T_dev;
+  const int th = 256;
+  if (T.n_dev > 0) eval_kernel<<<(T.n_dev + th - 1) / th, th, 0, s>>>(T, dpar, x, xdot, t, cj, dout);
+  int m = T.n_csc > T.n ? T.n_csc : T.n;
+  stamp_kernel<<<(m + th - 1) / th, th, 0, s>>>(T, dout, F, J);
+  return cudaGetLastError();
+}
+
+// Single instance on one CTA.  Workspace in dynamic shared memory when it fits,
+// else in global memory (a.ws_global).
+__global__ void plain_kernel(PlainArgs a) {
+  extern __shared__ double smem[];
+  double *red = smem;
+  double *ws = a.ws_global ? a.ws_global : smem + 64;
+  const DTpl &T = *a.T;
+  BlockGroup g(red);
+  Engine<BlockGroup> E(T, a.dpar, ws, g);
+  for (int i = g.rank; i < T.n; i += g.size) E.w.x[i] = a.x[T.order[i]];
+  g.sync();
+  const EngOpts &o = a.opts;
+  EngStats st{};
+  st.hmin_seen = 1e300;
+  const double rel = o.nr_factor * o.reltol, av = o.nr_factor * o.abstol_v, ai = o.nr_factor * o.abstol_i;
+  if (a.mode == 0) {
+    Sink sk{};
+    sk.t_out = a.t_out; sk.x_out = a.x_out; sk.cap = a.cap; sk.count = 0;
+    sk.tstart = o.tstart; sk.tstop = o.tstop;
+    E.tran(E.w.x, o, sk, st, nullptr);
+    if (threadIdx.x == 0 && a.count) *a.count = sk.count;
+  } else if (a.mode == 1) {
+    for (int e = g.rank; e < T.n; e += g.size) E.w.hist[T.eq_pos[e]] = a.hist ? a.hist[e] : 0.0;
+    g.sync();
+    EvalCtx ctx{a.t, a.cj, 1.0, T.gmin, false, false};
+    int r = E.newton(E.w.x, ctx, E.w.hist, rel, av, ai, o.max_newton, 0.0, 0.0);
+    st.newton_iters = r < 0 ? -r : r;
+    st.status = r > 0 ? CEDAR_ST_OK : (r == 0 ? CEDAR_ST_ZERO_PIVOT : CEDAR_ST_NEWTON);
+  } else {
+    long long it = 0;
+    st.status = E.dcop(E.w.x, a.t, rel, av, ai, &it);
+    st.dc_iters = it;
+  }
+  g.sync();
+  for (int i = g.rank; i < T.n; i += g.size) a.x[T.order[i]] = E.w.x[i];
+  if (threadIdx.x == 0 && a.stats) *a.stats = st;
+}
+
+cudaError_t launch_plain(const PlainArgs &a, int wsd, int threads, cudaStream_t s) {
+  size_t smem = 64 * sizeof(double);
+  if (!a.ws_global) smem += (size_t)wsd * sizeof(double);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(plain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  plain_kernel<<<1, threads, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace cedar

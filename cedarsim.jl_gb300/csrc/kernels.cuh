@@ -1,0 +1,56 @@
+// kernels.cuh — kernel launch interface shared by api.cu and the kernel TUs.
+#pragma once
+#include <cuda_runtime.h>
+#include "engine.cuh"
+
+namespace cedar {
+
+// Batched run description (device pointers).
+struct BatchDev {
+  const DTpl *tpls;              // [n_templates]
+  const int *inst_tpl;           // [n_inst]
+  const long long *inst_dpar;    // [n_inst] offset into dpar
+  const double *dpar;
+  const long long *x0_off; const double *x0;   // original order, -1 = zeros
+  const long long *dx_off; const double *dx;   // perturbation after DC op
+  const int *probes_int;         // [n_templates * np] internal unknowns
+  int np, ns;
+  double *samples;               // [n_inst * np * ns]
+  double *x_final; int n_max;    // [n_inst * n_max] original order
+  EngStats *stats;               // [n_inst]
+  const int *queue;              // dequeue order (instance ids)
+  int *head;                     // queue head counter
+  int n_inst;
+  EngOpts opts;
+  int ws_stride;                 // doubles per group workspace
+  double *ws_global;             // global workspaces when not in shared memory
+  int ws_in_smem;
+};
+
+// derive params for instances [0, n_inst): raw blocks -> dpar blocks
+cudaError_t launch_derive(const DTpl *tpls_dev, const int *inst_tpl, const long long *raw_off, const double *raw,
+                          const long long *dpar_off, double *dpar, int n_inst, int max_dev, cudaStream_t s);
+
+// cedar_eval: device outputs then CSC Jacobian values and residual rows
+cudaError_t launch_eval(const DTpl &T, const DTpl *T_dev, const double *dpar, const double *x, const double *xdot,
+                        double t, double cj, double *dout, double *F, double *J, cudaStream_t s);
+
+// single-instance block engine: mode 0 = transient, 1 = one Newton solve, 2 = DC op
+struct PlainArgs {
+  const DTpl *T; const double *dpar;
+  double *x;               // original order, in/out
+  const double *hist;      // original rows (mode 1) or null
+  double t, cj;
+  EngOpts opts;
+  double *t_out, *x_out; long long cap; long long *count;
+  EngStats *stats;
+  double *ws_global;
+  int mode;
+};
+cudaError_t launch_plain(const PlainArgs &a, int ws_doubles_n, int threads, cudaStream_t s);
+
+// batched persistent engine with K lanes per instance
+cudaError_t launch_batch(const BatchDev &b, int K, int warps_per_cta, int grid, size_t smem, cudaStream_t s);
+int batch_max_smem_optin();
+
+}  // namespace cedar

@@ -1,0 +1,154 @@
+"""Seeded synthetic circuits for the benchmark workloads.
+
+Randomness: Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers:
+as easy as 1, 2, 3", SC'11), keyed by (seed, workload id), counter =
+(instance, device, parameter, 0).  Normals by Box-Muller, uniforms as
+(u + 0.5) / 2^32.  The same numbers are produced on any host, so CPU and GPU runs
+see identical parameters.
+
+Workloads:
+  1. RC ladder: 100 sections, series R = 1 kOhm, shunt C = 1 pF per node, driven by
+     PULSE(0 1 0 1n 1n 50n 100n); trapezoidal, h = 0.1 ns, 0..1 us.
+  2. 31-stage CMOS inverter chain (level-1 MOSFETs): VDD = 1.8 V, Vth_n = 0.45,
+     Vth_p = -0.45, KP_n = 200 uA/V^2, KP_p = 80 uA/V^2, W/L = 2 (n) / 4 (p),
+     10 fF load per stage, input PULSE(0 1.8 0 50p 50p 950p 2n); BDF2, h = 1 ps, 0..20 ns.
+  3. Monte Carlo: 4096 chains with L drawn uniformly from {5, 7, ..., 63}; per
+     transistor Vth ~ N(nominal, 0.03 V), KP ~ nominal * exp(0.05 z); per instance
+     load C ~ U(5, 20) fF; adaptive BDF2 (reltol 1e-6, abstol 1e-9 V) to 20 ns.
+"""
+from __future__ import annotations
+
+import math
+from typing import List, Tuple
+
+import numpy as np
+
+from .circuit import Circuit, Flat, Pulse, MOS1, C as MODEL_C
+
+M0, M1 = np.uint64(0xD2511F53), np.uint64(0xCD9E8D57)
+W0, W1 = np.uint32(0x9E3779B9), np.uint32(0xBB67AE85)
+MASK32 = np.uint64(0xFFFFFFFF)
+
+
+def philox4x32_10(ctr: np.ndarray, key: np.ndarray) -> np.ndarray:
+    """Philox4x32-10 on a batch of counters.  ctr: (..., 4) uint32, key: (..., 2) uint32."""
+    c = [np.asarray(ctr[..., i], dtype=np.uint32).astype(np.uint64) for i in range(4)]
+    k0 = np.asarray(key[..., 0], dtype=np.uint32).copy()
+    k1 = np.asarray(key[..., 1], dtype=np.uint32).copy()
+    for r in range(10):
+        if r > 0:
+            k0 = (k0 + W0).astype(np.uint32)
+            k1 = (k1 + W1).astype(np.uint32)
+        p0 = M0 * c[0]
+        p1 = M1 * c[2]
+        hi0, lo0 = p0 >> np.uint64(32), p0 & MASK32
+        hi1, lo1 = p1 >> np.uint64(32), p1 & MASK32
+        c = [hi1 ^ c[1] ^ k0.astype(np.uint64), lo1, hi0 ^ c[3] ^ k1.astype(np.uint64), lo0]
+    return np.stack([x.astype(np.uint32) for x in c], axis=-1)
+
+
+class Stream:
+    """Counter-based stream: draw(i, d, p) -> 4 uint32 for instance i, device d, param p."""
+
+    def __init__(self, seed: int, workload: int):
+        self.key = np.array([seed & 0xFFFFFFFF, workload & 0xFFFFFFFF], dtype=np.uint32)
+
+    def bits(self, inst, dev, par) -> np.ndarray:
+        inst, dev, par = np.broadcast_arrays(np.asarray(inst), np.asarray(dev), np.asarray(par))
+        ctr = np.stack([inst.astype(np.uint32), dev.astype(np.uint32), par.astype(np.uint32),
+                        np.zeros(inst.shape, np.uint32)], axis=-1)
+        return philox4x32_10(ctr, np.broadcast_to(self.key, ctr.shape[:-1] + (2,)))
+
+    def uniform(self, inst, dev, par) -> np.ndarray:
+        b = self.bits(inst, dev, par)
+        return (b[..., 0].astype(np.float64) + 0.5) / 4294967296.0
+
+    def normal(self, inst, dev, par) -> np.ndarray:
+        b = self.bits(inst, dev, par)
+        u1 = (b[..., 0].astype(np.float64) + 0.5) / 4294967296.0
+        u2 = (b[..., 1].astype(np.float64) + 0.5) / 4294967296.0
+        return np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * math.pi * u2)
+
+
+# ---------------------------------------------------------------- workload 1
+def rc_ladder(sections: int = 100, r: float = 1e3, c: float = 1e-12,
+              wave: Pulse = Pulse(0.0, 1.0, 0.0, 1e-9, 1e-9, 50e-9, 100e-9)) -> Circuit:
+    ckt = Circuit()
+    ckt.V("V1", "n0", "0", wave=wave)
+    for k in range(1, sections + 1):
+        ckt.R(f"R{k}", f"n{k-1}", f"n{k}", r=r)
+        ckt.C(f"C{k}", f"n{k}", "0", c=c)
+    return ckt
+
+
+# ---------------------------------------------------------------- workload 2
+INV = dict(vdd=1.8, vth_n=0.45, vth_p=-0.45, kp_n=200e-6, kp_p=80e-6, wn=2e-6, ln=1e-6, wp=4e-6, lp=1e-6,
+           cload=10e-15)
+INV_PULSE = Pulse(0.0, 1.8, 0.0, 50e-12, 50e-12, 950e-12, 2e-9)
+
+
+def inverter_chain(stages: int = 31, cload: float = INV["cload"], wave: Pulse = INV_PULSE, **kw) -> Circuit:
+    p = dict(INV, **kw)
+    ckt = Circuit()
+    ckt.node("in"); ckt.node("vdd")
+    ckt.V("VIN", "in", "0", wave=wave)
+    ckt.V("VDD", "vdd", "0", dc=p["vdd"])
+    prev = "in"
+    for k in range(1, stages + 1):
+        out = f"out{k}"
+        ckt.mos1(f"MN{k}", out, prev, "0", "0", 1.0, p["wn"], p["ln"], p["kp_n"], p["vth_n"])
+        ckt.mos1(f"MP{k}", out, prev, "vdd", "vdd", -1.0, p["wp"], p["lp"], p["kp_p"], p["vth_p"])
+        ckt.C(f"CL{k}", out, "0", cload)
+        prev = out
+    return ckt
+
+
+# ---------------------------------------------------------------- workload 3
+MC_LENGTHS = list(range(5, 64, 2))
+
+
+def mc_chains(n_inst: int = 4096, seed: int = 20240607, workload: int = 3,
+              lengths: List[int] = MC_LENGTHS) -> Tuple[List[Flat], np.ndarray, np.ndarray, np.ndarray]:
+    """Monte Carlo chains.  Returns (templates, inst_template, inst_par, inst_par_off).
+
+    Template k is the chain of length lengths[k]; an instance's parameter block is
+    the template's block with its MOSFET VTO/KP and load C replaced.
+    Random draws: chain length  -> stream(i, 0, 0) uniform;
+                  load C        -> stream(i, 0, 1) uniform;
+                  MOSFET j Vth  -> stream(i, 1 + j, 0) normal;  KP -> stream(i, 1 + j, 1) normal.
+    """
+    st = Stream(seed, workload)
+    idx = np.arange(n_inst)
+    lsel = np.minimum((st.uniform(idx, 0, 0) * len(lengths)).astype(np.int64), len(lengths) - 1)
+    cl = 5e-15 + st.uniform(idx, 0, 1) * 15e-15
+    templates = [inverter_chain(L).flatten() for L in lengths]
+    blocks = []
+    offs = np.zeros(n_inst, np.int64)
+    pos = 0
+    for i in range(n_inst):
+        f = templates[lsel[i]]
+        blk = f.param_block().copy()
+        off_m = 0
+        for (model, term, br, par) in f.groups:
+            npar, ninst = par.shape
+            if model == MOS1:
+                j = np.arange(ninst)
+                vth_nom = par[4]
+                kp_nom = par[3]
+                z1 = st.normal(i, 1 + j, 0)
+                z2 = st.normal(i, 1 + j, 1)
+                blk[off_m + 4 * ninst: off_m + 5 * ninst] = vth_nom + 0.03 * z1 * np.sign(par[0])
+                blk[off_m + 3 * ninst: off_m + 4 * ninst] = kp_nom * np.exp(0.05 * z2)
+            elif model == MODEL_C:
+                blk[off_m + 0: off_m + ninst] = cl[i]
+            off_m += npar * ninst
+        offs[i] = pos
+        pos += blk.size
+        blocks.append(blk)
+    return templates, lsel.astype(np.int32), np.concatenate(blocks), offs
+
+
+def chain_output_probe(flat: Flat) -> int:
+    """Unknown index of the last stage output of a chain template."""
+    outs = [k for k, nm in enumerate(flat.names) if nm.startswith("out")]
+    return max(outs, key=lambda k: int(flat.names[k][3:]))

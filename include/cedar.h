@@ -1,0 +1,267 @@
+/*
+ * cedar.h — C ABI of the GB300 (sm_103a) transient engine for CedarSim circuits.
+ *
+ * The library replaces, under a Julia `ccall` layer, the per-Newton-iteration work
+ * that CedarSim's DAE residual does on the CPU today:
+ *   - device evaluation into currents I, charges Q and their voltage partials,
+ *   - stamping into fixed-pattern sparse G = dI/dx and C = dQ/dx,
+ *   - assembly of J = G + cj*C and of the residual F = I + dQ/dt,
+ *   - refactorisation and solution of J with a precomputed static-pivot ordering.
+ *
+ * Reference interfaces replaced (CedarSim 0.12.0):
+ *   - residual `f(out, du, u, p, t)` / Jacobian `jac(J, du, u, p, gamma, t)` that
+ *     DAECompiler emits and Sundials IDA / OrdinaryDiffEq consume
+ *     (benchmarks/benchmark_common.jl:138,155; src/sweeps.jl:453)   -> cedar_eval
+ *   - one implicit step of IDA's Newton (src/sweeps.jl:456)          -> cedar_newton_solve
+ *   - `tran!(circ, tspan)` = DAEProblem + solve(prob, IDA())
+ *     (src/sweeps.jl:450-463)                                        -> cedar_tran_run
+ *   - `dc!(circ)` with CedarDCOp initialisation (src/sweeps.jl:437-448,
+ *     src/dcop.jl:24-94)                                             -> cedar_dcop
+ *   - `CircuitSweep` + broadcast `dc!.`/`tran!.` over parameter points
+ *     (src/sweeps.jl:390-435,471-502)                                -> cedar_batch_*
+ *   - forward sensitivities through SciMLSensitivity
+ *     (test/sensitivity.jl:13-42)                                    -> cedar_adjoint_run
+ *
+ * Conventions
+ *   - Unknowns: x[0 .. n_nodes-1] are node voltages (ground excluded, index -1),
+ *     x[n_nodes .. n_nodes+n_branch-1] are branch currents of V sources, inductors
+ *     and VCVS, exactly the MNA unknowns CedarSim's `branch!` keeps
+ *     (src/simulate_ir.jl:112-120).
+ *   - Residual rows follow CedarSim's KCL sign: a branch current I flowing from
+ *     net+ to net- adds -m*I to KCL(net+) and +m*I to KCL(net-)
+ *     (src/simulate_ir.jl:54,115-116); m is the SPICE multiplicity
+ *     (ParallelInstances, src/simulate_ir.jl:56-75).
+ *   - F(x, xdot, t) = Fi(x, t) + d/dt Fq(x).  G = dFi/dx, C = dFq/dx, J = G + cj*C.
+ *   - All functions return 0 on success and a negative CEDAR_E* code on error;
+ *     cedar_last_error() returns the message of the calling thread's last error.
+ *   - Caller buffers are HOST memory unless a function name ends in `_dev`, in
+ *     which case they are device pointers on the handle's stream.
+ *   - Handles are not thread-safe; each handle owns one CUDA stream.
+ */
+#ifndef CEDAR_H
+#define CEDAR_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- error codes ---------------------------------------------------------- */
+#define CEDAR_OK            0
+#define CEDAR_EINVAL       -1   /* malformed description or argument          */
+#define CEDAR_ECUDA        -2   /* CUDA runtime error                          */
+#define CEDAR_ENOMEM       -3   /* allocation failure                          */
+#define CEDAR_ESINGULAR    -4   /* structurally singular system                */
+#define CEDAR_ENOCONV      -5   /* Newton / DC operating point did not converge*/
+#define CEDAR_ECAPACITY    -6   /* output buffer too small                     */
+#define CEDAR_EUNSUPPORTED -7   /* feature outside this build                  */
+
+/* ---- per-instance status words (never trap; set and retire) --------------- */
+#define CEDAR_ST_OK          0
+#define CEDAR_ST_NEWTON      1  /* Newton failed at minimum step               */
+#define CEDAR_ST_ZERO_PIVOT  2  /* |pivot| below threshold                      */
+#define CEDAR_ST_DT_UNDERFLOW 3 /* step fell below hmin                         */
+#define CEDAR_ST_MAX_STEPS   4  /* max_steps reached before tstop               */
+#define CEDAR_ST_NAN         5  /* non-finite value in the solution             */
+#define CEDAR_ST_DCOP        6  /* DC operating point failed                    */
+#define CEDAR_ST_WAIT_LIMIT  7  /* a bounded device-side wait gave up           */
+#define CEDAR_ST_NOT_RUN     8  /* instance never dequeued                      */
+
+/* ---- device models --------------------------------------------------------
+ * Parameter blocks are struct-of-arrays: par[p * n_inst + i].
+ * Terminals are unknown indices, -1 = ground.  `m` is the multiplicity.
+ *
+ *  model            terms            params (in order)                reference
+ *  R  resistor      p n              r m                              simpledevices.jl:49-77
+ *  C  capacitor     p n              c m                              simpledevices.jl:99-109
+ *  L  inductor      p n  (+branch)   l m                              simpledevices.jl:122-132
+ *  V  vsource       p n  (+branch)   m dc kind a0..a6                 simpledevices.jl:274-300
+ *  I  isource       p n              m dc kind a0..a6                 simpledevices.jl:315-339
+ *  E  vcvs          p n cp cn (+br)  gain m                           simpledevices.jl:341-356
+ *  G  vccs          p n cp cn        gain m                           simpledevices.jl:358-373
+ *  MOS1 (VA level-1 Shichman-Hodges)
+ *                   d g s b          type W L KP VTO LAMBDA m         (VA source in DESIGN)
+ *  DIODE (VA exponential diode)
+ *                   a c              IS N AREA m                      (VA source in DESIGN)
+ *  NLVCR (VA nonlinear VCR, ddx test model)
+ *                   d g s            R m                              test/NLVCR.va
+ *
+ * Source waveform kinds (params a0..a6), spectre_env.jl:43-69,144-176:
+ *   CEDAR_WAVE_DC    : value = dc
+ *   CEDAR_WAVE_PULSE : a0..a6 = v1 v2 td tr tf pw period
+ *   CEDAR_WAVE_PWL   : a0 = offset (in doubles) into desc->pwl, a1 = number of points;
+ *                      points are (t, v) pairs
+ *   CEDAR_WAVE_SIN   : a0..a6 = vo va freq td theta phase ncycles
+ * In DC analysis every source takes its `dc` parameter (simpledevices.jl:289-290).
+ * ------------------------------------------------------------------------- */
+enum {
+  CEDAR_R = 1, CEDAR_C = 2, CEDAR_L = 3, CEDAR_V = 4, CEDAR_I = 5,
+  CEDAR_E = 6, CEDAR_G = 7, CEDAR_MOS1 = 8, CEDAR_DIODE = 9, CEDAR_NLVCR = 10,
+  CEDAR_NMODELS = 11
+};
+enum { CEDAR_WAVE_DC = 0, CEDAR_WAVE_PULSE = 1, CEDAR_WAVE_PWL = 2, CEDAR_WAVE_SIN = 3 };
+
+typedef struct cedar_devgroup {
+  int32_t model;          /* CEDAR_R ...                                        */
+  int32_t n_inst;         /* number of instances in this group                  */
+  const int32_t *term;    /* [n_inst * n_term] unknown index per terminal       */
+  const int32_t *branch;  /* [n_inst] branch unknown (L, V, E), NULL otherwise  */
+  const double *par;      /* [n_par * n_inst] struct-of-arrays parameters       */
+} cedar_devgroup;
+
+typedef struct cedar_ckt_desc {
+  int32_t n_nodes;        /* node-voltage unknowns                              */
+  int32_t n_branch;       /* branch-current unknowns                            */
+  int32_t n_groups;
+  const cedar_devgroup *groups;
+  const double *pwl;      /* PWL point table referenced by CEDAR_WAVE_PWL       */
+  int64_t n_pwl;          /* doubles in pwl                                     */
+  double temp_c;          /* simulation temperature [C] (SimSpec.temp = 27)     */
+  double gmin;            /* junction/channel gmin (SimSpec.gmin = 1e-12)       */
+} cedar_ckt_desc;
+
+/* Terminal and parameter counts per model (index by model id). */
+int cedar_model_nterm(int model);
+int cedar_model_npar(int model);
+int cedar_model_has_branch(int model);
+
+/* ---- transient / DC options --------------------------------------------- */
+enum { CEDAR_TRAP = 0, CEDAR_BDF2 = 1 };
+
+typedef struct cedar_tran_opts {
+  int32_t method;         /* CEDAR_TRAP or CEDAR_BDF2                           */
+  int32_t adaptive;       /* 0: fixed step h; 1: LTE-controlled (BDF2 only)     */
+  int32_t dcop;           /* 1: DC operating point at tstart before stepping    */
+  int32_t max_newton;     /* Newton iterations per step (default 20)            */
+  int64_t max_steps;      /* accepted + rejected step limit                     */
+  double tstart, tstop;
+  double h;               /* fixed step, or 0 for automatic initial step        */
+  double hmin, hmax;      /* adaptive bounds (0 = automatic)                    */
+  double reltol;          /* LTE relative tolerance (1e-6)                      */
+  double abstol_v;        /* LTE absolute tolerance on node voltages (1e-9 V)   */
+  double abstol_i;        /* absolute tolerance on branch currents (1e-12 A)    */
+  double nr_factor;       /* Newton tolerance = nr_factor * LTE tolerance (1e-3)*/
+  double hfirst_frac;     /* first step after a breakpoint, as a fraction of the
+                             distance to the next breakpoint (1e-2)             */
+} cedar_tran_opts;
+
+/* Fill `o` with the defaults documented above (method BDF2, adaptive). */
+void cedar_tran_opts_default(cedar_tran_opts *o);
+
+typedef struct cedar_stats {
+  int64_t accepted;       /* accepted steps                                     */
+  int64_t rejected;       /* LTE + Newton rejections                            */
+  int64_t newton_iters;   /* Newton iterations (each = eval + refactor + solve) */
+  int64_t dc_iters;       /* Newton iterations spent in the DC operating point  */
+  double hmin_seen, hmax_seen;
+  int32_t status;         /* CEDAR_ST_*                                         */
+  int32_t pad;
+} cedar_stats;
+
+/* ---- library ------------------------------------------------------------- */
+int cedar_last_error(char *buf, size_t len);
+int cedar_version(void);
+
+/* ---- single circuit (plain drop-in) -------------------------------------- */
+typedef struct cedar_ckt cedar_ckt;
+
+/* Build the handle: computes the J pattern (CSC), stamp-slot maps, the static
+ * pivot (structural matching) and fill-reducing ordering, the LU fill pattern and
+ * its level schedule on the host, then copies everything to the device. */
+int cedar_ckt_create(const cedar_ckt_desc *desc, cedar_ckt **out);
+/* Host-only handle: runs the same analysis without touching the GPU.  Only
+ * cedar_ckt_size / _pattern / _symbolic / _destroy accept it. */
+int cedar_plan_create(const cedar_ckt_desc *desc, cedar_ckt **out);
+int cedar_ckt_destroy(cedar_ckt *ckt);
+int cedar_ckt_size(const cedar_ckt *ckt, int32_t *n, int32_t *nnz_j, int32_t *nnz_lu,
+                   int32_t *n_levels);
+
+/* J pattern in compressed-sparse-column form over the ORIGINAL unknown order:
+ * colptr[n+1], rowidx[nnz_j].  Jvals returned by cedar_eval follow this order. */
+int cedar_ckt_pattern(const cedar_ckt *ckt, int32_t *colptr, int32_t *rowidx);
+/* Static pivoting: rowmatch[u] = equation used as pivot row for unknown u;
+ * order[p] = unknown eliminated at position p (fill-reducing ordering);
+ * lu_colptr/lu_rowidx = pattern of L+U (incl. fill) in the permuted space. */
+int cedar_ckt_symbolic(const cedar_ckt *ckt, int32_t *rowmatch, int32_t *order,
+                       int32_t *lu_colptr, int32_t *lu_rowidx);
+
+/* Residual + Jacobian: F = Fi(x,t) + C(x)*xdot (xdot may be NULL = 0),
+ * Jvals = G + cj*C in the CSC order of cedar_ckt_pattern.  F or Jvals may be NULL.
+ * Mirrors DAECompiler's f(out, du, u, p, t) and jac(J, du, u, p, gamma, t). */
+int cedar_eval(cedar_ckt *ckt, const double *x, const double *xdot, double t, double cj,
+               double *F, double *Jvals);
+/* Same on device buffers (stream-ordered on the handle's stream). */
+int cedar_eval_dev(cedar_ckt *ckt, const double *x, const double *xdot, double t, double cj,
+                   double *F, double *Jvals);
+
+/* One implicit step: solve Fi(x, t) + cj*Fq(x) + hist = 0 for x by Newton with
+ * refactorisation every iteration.  hist (may be NULL) is the integrator history
+ * in Fq space.  x holds the initial guess on entry and the solution on exit. */
+int cedar_newton_solve(cedar_ckt *ckt, double t, double cj, const double *hist, double *x,
+                       cedar_stats *stats);
+
+/* DC operating point at time t (sources at their dc values, charges frozen),
+ * Newton with source stepping then gmin stepping. x: guess in, solution out. */
+int cedar_dcop(cedar_ckt *ckt, double t, double *x, cedar_stats *stats);
+
+/* Whole transient on the device.  x0: initial state (or DC guess when
+ * opts->dcop).  Every accepted time point is recorded into (t_out[cap],
+ * x_out[cap * n]) while it fits; *n_out receives the number recorded (it is the
+ * number of accepted points + 1 for the initial point; CEDAR_ECAPACITY if it
+ * exceeded cap, in which case the first cap points are returned). */
+int cedar_tran_run(cedar_ckt *ckt, const cedar_tran_opts *opts, const double *x0,
+                   double *t_out, double *x_out, int64_t cap, int64_t *n_out,
+                   cedar_stats *stats);
+
+/* ---- batched form ---------------------------------------------------------
+ * Instances share a topology template and differ in parameters (a CircuitSweep
+ * over ParamSim points).  inst_par holds each instance's full parameter block:
+ * the concatenation over the template's groups of its SoA parameter arrays
+ * (same layout as the template's own `par` arrays).  probes lists unknowns whose
+ * waveform is sampled on a uniform grid of n_samples points over [tstart, tstop]. */
+typedef struct cedar_batch_desc {
+  int32_t n_templates;
+  const cedar_ckt_desc *templates;
+  int32_t n_inst;
+  const int32_t *inst_template;   /* [n_inst]                                 */
+  const int64_t *inst_par_off;    /* [n_inst] offset into inst_par, -1 = nominal */
+  const double *inst_par;
+  const int64_t *inst_x0_off;     /* [n_inst] offset into inst_x0 or -1 (zeros)  */
+  const double *inst_x0;          /* initial state / DC guess per instance      */
+  const int64_t *inst_dx_off;     /* [n_inst] offset into inst_dx or -1          */
+  const double *inst_dx;          /* perturbation added after the DC op         */
+  int32_t n_probes;               /* probes per template (same count each)      */
+  const int32_t *probes;          /* [n_templates * n_probes] unknown indices   */
+  int32_t n_samples;              /* output samples per probe (>= 2), or 0      */
+} cedar_batch_desc;
+
+typedef struct cedar_batch cedar_batch;
+
+/* Lanes per instance and instances per CTA chosen by the autotuner (0 = auto). */
+typedef struct cedar_batch_tuning {
+  int32_t lanes_per_inst;         /* 1, 2, 4, 8, 16 or 32                       */
+  int32_t warps_per_cta;
+  int32_t reserved[6];
+} cedar_batch_tuning;
+
+int cedar_batch_create(const cedar_batch_desc *desc, cedar_batch **out);
+int cedar_batch_destroy(cedar_batch *b);
+/* Run every instance from tstart to tstop in one persistent launch.
+ *   x_final[n_inst * n_max]  final state per instance (may be NULL)
+ *   samples[n_inst * n_probes * n_samples] probe waveforms (may be NULL)
+ *   stats[n_inst]            per-instance counters and status (may be NULL) */
+int cedar_batch_run(cedar_batch *b, const cedar_tran_opts *opts, double *x_final,
+                    double *samples, cedar_stats *stats);
+int cedar_batch_set_tuning(cedar_batch *b, const cedar_batch_tuning *t);
+int cedar_batch_get_tuning(const cedar_batch *b, cedar_batch_tuning *t);
+/* Autotune: time each candidate tile shape on a short horizon and keep the best. */
+int cedar_batch_autotune(cedar_batch *b, const cedar_tran_opts *opts, double horizon,
+                         cedar_batch_tuning *best);
+int cedar_batch_nmax(const cedar_batch *b, int32_t *n_max);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CEDAR_H */

@@ -1,0 +1,767 @@
+// oracle.cpp — CPU FP64 restatement of CedarSim's transient hot path.
+//
+// TEST INFRASTRUCTURE ONLY.  Nothing in the product library links, loads or calls
+// this file; it is used by tests/ (as the checker), by __graft_entry__.smoke() and
+// by bench.py's CPU-baseline leg.
+//
+// What it restates (CedarSim 0.12.0, file:line within the CedarSim project):
+//   * KCL / branch sign convention and multiplicity:   src/simulate_ir.jl:28-54,112-120
+//   * device equations R, C, L, V, I, E, G:             src/simpledevices.jl:49-132,274-373
+//   * source waveforms pulse / pwl / sin, breakpoint rule (a corner belongs to the
+//     next segment):                                    src/spectre_env.jl:15-69,144-176
+//   * Verilog-A contribution semantics (I(a,b) <+ ..., current leaves a, enters b;
+//     ddx on a two-node probe = (d/dVa - d/dVb)/2):     src/vasim.jl:128-180,392-412,824-839
+//   * $temperature = temp + 273.15, SimSpec gmin=1e-12: src/va_env.jl:123, simulate_ir.jl:12-20
+//   * Jacobian = dF/du + gamma dF/du' as DAECompiler's dense jac(J,du,u,p,gamma,t)
+//     (benchmarks/benchmark_common.jl:152-158) — formed here densely by forward-mode
+//     dual numbers, the same way vasim.jl seeds ForwardDiff duals (vasim.jl:347-374),
+//     and factored by dense LU with partial pivoting, the default direct solve of
+//     Sundials IDA that tran! uses (src/sweeps.jl:456).
+// Integrators (fixed-step trapezoidal, fixed/variable-step BDF2 with LTE control),
+// Newton, and the DC homotopy are not in the reference (it delegates to IDA); they
+// restate the algorithm the GPU engine documents, so GPU and CPU take the same steps.
+//
+// Build: oracle/Makefile (g++ -O2 -fopenmp -ffp-contract=off -shared -fPIC).
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+#include <algorithm>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+#include "../include/cedar.h"
+
+namespace orc {
+
+// ---------------------------------------------------------------- dual numbers
+constexpr int ND = 6;
+struct Dual {
+  double v;
+  double d[ND];
+  Dual() : v(0) { for (int i = 0; i < ND; ++i) d[i] = 0; }
+  Dual(double x) : v(x) { for (int i = 0; i < ND; ++i) d[i] = 0; }
+  static Dual seed(double x, int k) { Dual r(x); if (k >= 0) r.d[k] = 1.0; return r; }
+};
+static inline Dual operator+(const Dual &a, const Dual &b) { Dual r; r.v = a.v + b.v; for (int i = 0; i < ND; ++i) r.d[i] = a.d[i] + b.d[i]; return r; }
+static inline Dual operator-(const Dual &a, const Dual &b) { Dual r; r.v = a.v - b.v; for (int i = 0; i < ND; ++i) r.d[i] = a.d[i] - b.d[i]; return r; }
+static inline Dual operator-(const Dual &a) { Dual r; r.v = -a.v; for (int i = 0; i < ND; ++i) r.d[i] = -a.d[i]; return r; }
+static inline Dual operator*(const Dual &a, const Dual &b) { Dual r; r.v = a.v * b.v; for (int i = 0; i < ND; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i]; return r; }
+static inline Dual operator*(double s, const Dual &b) { Dual r; r.v = s * b.v; for (int i = 0; i < ND; ++i) r.d[i] = s * b.d[i]; return r; }
+static inline Dual operator*(const Dual &b, double s) { return s * b; }
+static inline Dual operator/(const Dual &a, double s) { Dual r; r.v = a.v / s; for (int i = 0; i < ND; ++i) r.d[i] = a.d[i] / s; return r; }
+static inline Dual dexp_lim(const Dual &a) {
+  // limexp: exp(x) for x <= 80, linear continuation above (keeps Newton finite)
+  const double X = 80.0;
+  Dual r;
+  if (a.v <= X) { double e = std::exp(a.v); r.v = e; for (int i = 0; i < ND; ++i) r.d[i] = e * a.d[i]; }
+  else { double e = std::exp(X); r.v = e * (1.0 + (a.v - X)); for (int i = 0; i < ND; ++i) r.d[i] = e * a.d[i]; }
+  return r;
+}
+
+// ------------------------------------------------------------------ circuit
+struct Group {
+  int model = 0, n_inst = 0, nt = 0, np = 0;
+  std::vector<int> term, branch;
+  std::vector<double> par;
+  double p(int k, int i) const { return par[(size_t)k * n_inst + i]; }
+};
+struct Circuit {
+  int n_nodes = 0, n_branch = 0, n = 0;
+  std::vector<Group> groups;
+  std::vector<double> pwl;
+  double temp_c = 27.0, gmin = 1e-12;
+};
+
+static const int kNTerm[CEDAR_NMODELS] = {0, 2, 2, 2, 2, 2, 4, 4, 4, 2, 3};
+static const int kNPar[CEDAR_NMODELS]  = {0, 2, 2, 2, 10, 10, 2, 2, 7, 4, 2};
+static const int kHasBr[CEDAR_NMODELS] = {0, 0, 0, 1, 1, 0, 1, 0, 0, 0, 0};
+
+static bool load_circuit(const cedar_ckt_desc *d, Circuit &c, std::string &err) {
+  if (!d || d->n_nodes < 0 || d->n_branch < 0 || d->n_groups < 0) { err = "bad desc"; return false; }
+  c.n_nodes = d->n_nodes; c.n_branch = d->n_branch; c.n = d->n_nodes + d->n_branch;
+  c.temp_c = d->temp_c; c.gmin = d->gmin;
+  if (d->pwl && d->n_pwl > 0) c.pwl.assign(d->pwl, d->pwl + d->n_pwl);
+  for (int g = 0; g < d->n_groups; ++g) {
+    const cedar_devgroup &s = d->groups[g];
+    if (s.model <= 0 || s.model >= CEDAR_NMODELS || s.n_inst < 0) { err = "bad model"; return false; }
+    Group G; G.model = s.model; G.n_inst = s.n_inst; G.nt = kNTerm[s.model]; G.np = kNPar[s.model];
+    G.term.assign(s.term, s.term + (size_t)G.nt * G.n_inst);
+    if (kHasBr[s.model]) {
+      if (!s.branch) { err = "missing branch"; return false; }
+      G.branch.assign(s.branch, s.branch + G.n_inst);
+    }
+    G.par.assign(s.par, s.par + (size_t)G.np * G.n_inst);
+    for (int v : G.term) if (v < -1 || v >= c.n) { err = "terminal out of range"; return false; }
+    for (int v : G.branch) if (v < c.n_nodes || v >= c.n) { err = "branch out of range"; return false; }
+    c.groups.push_back(std::move(G));
+  }
+  return true;
+}
+
+// ------------------------------------------------------------------ sources
+// pwl_at_time (spectre_env.jl:43-69) with find_t_in_ts (:15-21): i = index of the
+// first time point strictly greater than t (a time point equal to t belongs to
+// the next segment).  ts/ys are strided views (stride 2 over (t, v) pairs).
+static double pwl_at_time(const double *tv, int npts, double t) {
+  // 0-based: i = first k with ts[k] > t
+  int i = 0;
+  while (i < npts && tv[2 * i] <= t) ++i;
+  if (i <= 0) return tv[1];
+  if (i >= npts) return tv[2 * (npts - 1) + 1];
+  double y0 = tv[2 * (i - 1) + 1], y1 = tv[2 * i + 1];
+  double t0 = tv[2 * (i - 1)], t1 = tv[2 * i];
+  if (y0 == y1) return y1;
+  if (t1 == t0) return (y0 + y1) / 2;
+  double slope = (y1 - y0) / (t1 - t0);
+  return y0 + (t - t0) * slope;
+}
+
+// Value of a V/I source at time t.  In DC analysis the `dc` parameter is used
+// (VoltageSource: sim_mode === :dcop -> VS.dc, simpledevices.jl:289-290).
+static double source_value(const Group &g, int i, double t, bool dc, const std::vector<double> &pwl) {
+  double dcv = g.p(1, i);
+  if (dc) return dcv;
+  int kind = (int)g.p(2, i);
+  double a[7]; for (int k = 0; k < 7; ++k) a[k] = g.p(3 + k, i);
+  switch (kind) {
+    case CEDAR_WAVE_DC: return dcv;
+    case CEDAR_WAVE_PULSE: {  // spectre_env.jl:153-166
+      double v1 = a[0], v2 = a[1], td = a[2], tr = a[3], tf = a[4], pw = a[5], per = a[6];
+      double tv[8] = {td, v1, td + tr, v2, td + tr + pw, v2, td + tr + pw + tf, v1};
+      double tm = std::fmod(t, per);  // rem_right_semi(t, r) = t % r
+      return pwl_at_time(tv, 4, tm);
+    }
+    case CEDAR_WAVE_PWL: {
+      int64_t off = (int64_t)a[0]; int np = (int)a[1];
+      return pwl_at_time(pwl.data() + off, np, t);
+    }
+    case CEDAR_WAVE_SIN: {  // spectre_env.jl:169-176 (sind = sin of degrees)
+      double vo = a[0], va = a[1], freq = a[2], td = a[3], theta = a[4], phase = a[5], nc = a[6];
+      if (td < t && t < nc / freq) {
+        double deg = 360.0 * freq * (t - td) + phase;
+        return vo + va * std::exp(-(t - td) * theta) * std::sin(deg * (M_PI / 180.0));
+      }
+      return vo + va * std::sin(phase * (M_PI / 180.0));
+    }
+  }
+  return dcv;
+}
+
+// Next source corner strictly after t + eps (time_periodic_singularities!,
+// spectre_env.jl:71-77,160-161): pulse corners repeat every period, pwl corners
+// once, sin starts at td.
+static double next_breakpoint(const Circuit &c, double t, double eps) {
+  double best = std::numeric_limits<double>::infinity();
+  for (const Group &g : c.groups) {
+    if (g.model != CEDAR_V && g.model != CEDAR_I) continue;
+    for (int i = 0; i < g.n_inst; ++i) {
+      int kind = (int)g.p(2, i);
+      if (kind == CEDAR_WAVE_PULSE) {
+        double td = g.p(5, i), tr = g.p(6, i), tf = g.p(7, i), pw = g.p(8, i), per = g.p(9, i);
+        double cs[4] = {td, td + tr, td + tr + pw, td + tr + pw + tf};
+        for (double cj : cs) {
+          double bp;
+          if (cj > t + eps) bp = cj;
+          else if (std::isfinite(per) && per > 0) {
+            double k = std::floor((t + eps - cj) / per) + 1.0;
+            bp = cj + k * per;
+            if (!(bp > t + eps)) bp = cj + (k + 1.0) * per;
+          } else continue;
+          best = std::min(best, bp);
+        }
+      } else if (kind == CEDAR_WAVE_PWL) {
+        int64_t off = (int64_t)g.p(3, i); int np = (int)g.p(4, i);
+        for (int k = 0; k < np; ++k) { double tk = c.pwl[off + 2 * k]; if (tk > t + eps) { best = std::min(best, tk); break; } }
+      } else if (kind == CEDAR_WAVE_SIN) {
+        double td = g.p(6, i);
+        if (td > t + eps) best = std::min(best, td);
+      }
+    }
+  }
+  return best;
+}
+
+// ---------------------------------------------------------------- evaluation
+// Dense accumulation of Fi, Fq, G = dFi/dx, C = dFq/dx at x.
+struct EvalOut {
+  int n;
+  std::vector<double> Fi, Fq, G, C;
+  explicit EvalOut(int n_) : n(n_), Fi(n_), Fq(n_), G((size_t)n_ * n_), C((size_t)n_ * n_) {}
+  void clear() { std::fill(Fi.begin(), Fi.end(), 0); std::fill(Fq.begin(), Fq.end(), 0);
+                 std::fill(G.begin(), G.end(), 0); std::fill(C.begin(), C.end(), 0); }
+};
+
+struct Acc {
+  EvalOut &o; const int *idx; int nin;
+  // add a contribution `val` to row `row` of Fi (q=false) or Fq (q=true)
+  void add(int row, const Dual &val, bool q) {
+    if (row < 0) return;
+    if (!q) o.Fi[row] += val.v; else o.Fq[row] += val.v;
+    double *M = q ? o.C.data() : o.G.data();
+    for (int k = 0; k < nin; ++k) if (idx[k] >= 0) M[(size_t)row * o.n + idx[k]] += val.d[k];
+  }
+};
+
+struct EvalCtx {
+  double t = 0; bool dc = false; double src_scale = 1.0; double gshunt = 0.0;
+};
+
+static Dual mos1_id(const Dual &vgs, const Dual &vds, double vth, double beta, double lam) {
+  // Level-1 Shichman-Hodges drain current for vds >= 0 (forward mode).
+  Dual vov = vgs - Dual(vth);
+  if (vov.v <= 0) return Dual(0.0);
+  Dual clm = Dual(1.0) + lam * vds;
+  if (vds.v < vov.v) return beta * (vov - 0.5 * vds) * vds * clm;
+  return (0.5 * beta) * vov * vov * clm;
+}
+
+static void eval_circuit(const Circuit &c, const double *x, const EvalCtx &ctx, EvalOut &o) {
+  o.clear();
+  auto X = [&](int u) { return u < 0 ? 0.0 : x[u]; };
+  const double Vt = 1.380649e-23 * (c.temp_c + 273.15) / 1.602176634e-19;
+  for (const Group &g : c.groups) {
+    for (int i = 0; i < g.n_inst; ++i) {
+      const int *tm = g.term.data() + (size_t)g.nt * i;
+      int idx[ND]; int nin = 0;
+      for (int k = 0; k < g.nt; ++k) idx[nin++] = tm[k];
+      int br = -1;
+      if (!g.branch.empty()) { br = g.branch[i]; idx[nin++] = br; }
+      Dual in[ND];
+      for (int k = 0; k < nin; ++k) in[k] = Dual::seed(X(idx[k]), idx[k] >= 0 ? k : -1);
+      Acc A{o, idx, nin};
+      switch (g.model) {
+        case CEDAR_R: {  // I - V/res = 0; kcl!(p, -m I), kcl!(n, +m I)
+          double r = g.p(0, i), m = g.p(1, i);
+          Dual I = (in[0] - in[1]) / r;
+          A.add(tm[0], -m * I, false); A.add(tm[1], m * I, false);
+        } break;
+        case CEDAR_C: {  // I - C ddt(V) = 0  -> charge C*V
+          double cap = g.p(0, i), m = g.p(1, i);
+          Dual Q = cap * (in[0] - in[1]);
+          A.add(tm[0], -m * Q, true); A.add(tm[1], m * Q, true);
+        } break;
+        case CEDAR_L: {  // V - L ddt(I) = 0, branch current unknown
+          double l = g.p(0, i), m = g.p(1, i);
+          Dual I = in[2];
+          A.add(tm[0], -m * I, false); A.add(tm[1], m * I, false);
+          A.add(br, in[0] - in[1], false); A.add(br, -l * I, true);
+        } break;
+        case CEDAR_V: {  // V - Vab = 0
+          double m = g.p(0, i);
+          double vs = source_value(g, i, ctx.t, ctx.dc, c.pwl) * ctx.src_scale;
+          Dual I = in[2];
+          A.add(tm[0], -m * I, false); A.add(tm[1], m * I, false);
+          A.add(br, in[0] - in[1] - Dual(vs), false);
+        } break;
+        case CEDAR_I: {  // I - Iab = 0
+          double m = g.p(0, i);
+          double is = source_value(g, i, ctx.t, ctx.dc, c.pwl) * ctx.src_scale;
+          A.add(tm[0], Dual(-m * is), false); A.add(tm[1], Dual(m * is), false);
+        } break;
+        case CEDAR_E: {  // V - gain (Vc+ - Vc-) = 0
+          double gain = g.p(0, i), m = g.p(1, i);
+          Dual I = in[4];
+          A.add(tm[0], -m * I, false); A.add(tm[1], m * I, false);
+          A.add(br, (in[0] - in[1]) - gain * (in[2] - in[3]), false);
+        } break;
+        case CEDAR_G: {  // I - gain (Vc+ - Vc-) = 0
+          double gain = g.p(0, i), m = g.p(1, i);
+          Dual I = gain * (in[2] - in[3]);
+          A.add(tm[0], -m * I, false); A.add(tm[1], m * I, false);
+        } break;
+        case CEDAR_MOS1: {
+          // module mos1(d,g,s,b): vgs = type*V(g,s), vds = type*V(d,s);
+          // symmetric in d/s: for vds < 0 the roles swap.
+          // I(d,s) <+ type*id + $simparam("gmin")*V(d,s)
+          double type = g.p(0, i), W = g.p(1, i), L = g.p(2, i), KP = g.p(3, i),
+                 VTO = g.p(4, i), LAM = g.p(5, i), m = g.p(6, i);
+          double beta = KP * W / L, vth = type * VTO;
+          Dual vgs = type * (in[1] - in[2]);
+          Dual vds = type * (in[0] - in[2]);
+          Dual id;
+          if (vds.v >= 0) id = mos1_id(vgs, vds, vth, beta, LAM);
+          else id = -mos1_id(vgs - vds, -vds, vth, beta, LAM);
+          Dual Ids = type * id + c.gmin * (in[0] - in[2]);
+          A.add(tm[0], -m * Ids, false); A.add(tm[2], m * Ids, false);
+        } break;
+        case CEDAR_DIODE: {
+          // I(a,c) <+ IS*AREA*(limexp(V(a,c)/(N*$vt)) - 1) + gmin*V(a,c)
+          double IS = g.p(0, i), N = g.p(1, i), AREA = g.p(2, i), m = g.p(3, i);
+          Dual v = in[0] - in[1];
+          Dual I = (IS * AREA) * (dexp_lim(v / (N * Vt)) - Dual(1.0)) + c.gmin * v;
+          A.add(tm[0], -m * I, false); A.add(tm[1], m * I, false);
+        } break;
+        case CEDAR_NLVCR: {
+          // test/NLVCR.va: cdrain = R*V(g,s)**2; I(d,s) <+ V(d,s)*ddx(cdrain, V(g,s))
+          // ddx over the two-node probe V(g,s) = (dc/dVg - dc/dVs)/2 (vasim.jl:400-411)
+          double R = g.p(0, i), m = g.p(1, i);
+          Dual vgs = in[1] - in[2];
+          Dual dcd = 2.0 * R * vgs;  // (2R vgs - (-2R vgs))/2
+          Dual I = (in[0] - in[2]) * dcd;
+          A.add(tm[0], -m * I, false); A.add(tm[2], m * I, false);
+        } break;
+      }
+    }
+  }
+  if (ctx.gshunt != 0.0) {
+    for (int k = 0; k < c.n_nodes; ++k) { o.Fi[k] += -ctx.gshunt * x[k]; o.G[(size_t)k * c.n + k] += -ctx.gshunt; }
+  }
+}
+
+// ------------------------------------------------------------------ dense LU
+// LU with partial pivoting (row interchanges), skipping structurally zero
+// multipliers and zero pivot-row entries.  Returns false on an exactly zero pivot.
+struct DenseLU {
+  int n; std::vector<double> a; std::vector<int> piv; std::vector<int> nzc;
+  explicit DenseLU(int n_) : n(n_), a((size_t)n_ * n_), piv(n_), nzc(n_) {}
+  bool factor() {
+    for (int k = 0; k < n; ++k) {
+      int p = k; double best = std::fabs(a[(size_t)k * n + k]);
+      for (int i = k + 1; i < n; ++i) { double v = std::fabs(a[(size_t)i * n + k]); if (v > best) { best = v; p = i; } }
+      piv[k] = p;
+      if (!(best > 0.0)) return false;
+      if (p != k) for (int j = 0; j < n; ++j) std::swap(a[(size_t)k * n + j], a[(size_t)p * n + j]);
+      double inv = 1.0 / a[(size_t)k * n + k];
+      int nn = 0;
+      for (int j = k + 1; j < n; ++j) if (a[(size_t)k * n + j] != 0.0) nzc[nn++] = j;
+      for (int i = k + 1; i < n; ++i) {
+        double &aik = a[(size_t)i * n + k];
+        if (aik == 0.0) continue;
+        double l = aik * inv; aik = l;
+        for (int q = 0; q < nn; ++q) { int j = nzc[q]; a[(size_t)i * n + j] -= l * a[(size_t)k * n + j]; }
+      }
+    }
+    return true;
+  }
+  void solve(double *b) const {
+    for (int k = 0; k < n; ++k) { if (piv[k] != k) std::swap(b[k], b[piv[k]]);
+      for (int i = k + 1; i < n; ++i) { double l = a[(size_t)i * n + k]; if (l != 0.0) b[i] -= l * b[k]; } }
+    for (int k = n - 1; k >= 0; --k) { double s = b[k];
+      for (int j = k + 1; j < n; ++j) { double u = a[(size_t)k * n + j]; if (u != 0.0) s -= u * b[j]; }
+      b[k] = s / a[(size_t)k * n + k]; }
+  }
+};
+
+// ------------------------------------------------------------------ Newton
+struct Tol { double rel, av, ai; };  // Newton tolerances (already scaled)
+
+struct Work {
+  const Circuit &c; EvalOut eo; DenseLU lu; std::vector<double> F, dx, xq;
+  explicit Work(const Circuit &c_) : c(c_), eo(c_.n), lu(c_.n), F(c_.n), dx(c_.n), xq(c_.n) {}
+};
+
+// Solve Fi(x,t) + cj*Fq(x) + hist = 0.  Convergence: |dx_i| <= rel*|x_i| + abs_i for
+// every unknown after the update.  DC damping limits the node-voltage update to
+// `vlim` (0 = off).  Returns iterations used (>0) or -iterations on failure,
+// or 0 on a zero pivot.
+static int newton(Work &w, double *x, const EvalCtx &ctx, double cj, const double *hist,
+                  const Tol &tol, int maxit, double vlim, int *zero_pivot) {
+  const Circuit &c = w.c; const int n = c.n;
+  *zero_pivot = 0;
+  for (int it = 1; it <= maxit; ++it) {
+    eval_circuit(c, x, ctx, w.eo);
+    for (int i = 0; i < n; ++i) w.F[i] = w.eo.Fi[i] + cj * w.eo.Fq[i] + (hist ? hist[i] : 0.0);
+    for (size_t k = 0; k < (size_t)n * n; ++k) w.lu.a[k] = w.eo.G[k] + cj * w.eo.C[k];
+    if (!w.lu.factor()) { *zero_pivot = 1; return 0; }
+    for (int i = 0; i < n; ++i) w.dx[i] = -w.F[i];
+    w.lu.solve(w.dx.data());
+    bool finite = true;
+    for (int i = 0; i < n; ++i) if (!std::isfinite(w.dx[i])) finite = false;
+    if (!finite) return -it;
+    double scale = 1.0;
+    if (vlim > 0) {
+      double mx = 0; for (int i = 0; i < c.n_nodes; ++i) mx = std::max(mx, std::fabs(w.dx[i]));
+      if (mx > vlim) scale = vlim / mx;
+    }
+    bool conv = (scale == 1.0);
+    for (int i = 0; i < n; ++i) {
+      double d = w.dx[i] * scale;
+      x[i] += d;
+      double lim = tol.rel * std::fabs(x[i]) + (i < c.n_nodes ? tol.av : tol.ai);
+      if (!(std::fabs(d) <= lim)) conv = false;
+    }
+    if (conv) return it;
+  }
+  return -maxit;
+}
+
+static void eval_q(Work &w, const double *x, const EvalCtx &ctx, double *q) {
+  eval_circuit(w.c, x, ctx, w.eo);
+  for (int i = 0; i < w.c.n; ++i) q[i] = w.eo.Fq[i];
+}
+
+// DC operating point: Newton (damped) from the guess; on failure, source stepping
+// lambda = 0.1 .. 1 (halving the increment on failure, at most 8 halvings per
+// increment); on failure, gmin stepping gshunt = 1e-2 .. 1e-12 then 0.
+static int dcop(Work &w, double *x, double t, const Tol &tol, int64_t *iters) {
+  const int n = w.c.n; const int maxit = 100; const double vlim = 0.5;
+  EvalCtx ctx; ctx.t = t; ctx.dc = true;
+  std::vector<double> x0(x, x + n), xs(n);
+  int zp = 0;
+  int r = newton(w, x, ctx, 0.0, nullptr, tol, maxit, vlim, &zp);
+  *iters += std::abs(r);
+  if (r > 0) return CEDAR_ST_OK;
+  // source stepping
+  std::fill(x, x + n, 0.0);
+  double lam = 0.0, dl = 0.1; int halv = 0; bool ok = true;
+  while (lam < 1.0) {
+    double ln = std::min(1.0, lam + dl);
+    std::copy(x, x + n, xs.begin());
+    ctx.src_scale = ln;
+    r = newton(w, xs.data(), ctx, 0.0, nullptr, tol, maxit, vlim, &zp);
+    *iters += std::abs(r);
+    if (r > 0) { std::copy(xs.begin(), xs.end(), x); lam = ln; halv = 0; dl = std::min(0.1, dl * 2); }
+    else { dl *= 0.5; if (++halv > 8) { ok = false; break; } }
+  }
+  ctx.src_scale = 1.0;
+  if (ok) return CEDAR_ST_OK;
+  // gmin stepping
+  std::copy(x0.begin(), x0.end(), x);
+  for (double gs = 1e-2; gs >= 1e-12 * 0.999; gs *= 0.1) {
+    ctx.gshunt = gs;
+    r = newton(w, x, ctx, 0.0, nullptr, tol, maxit, vlim, &zp);
+    *iters += std::abs(r);
+    if (r <= 0) return CEDAR_ST_DCOP;
+  }
+  ctx.gshunt = 0.0;
+  r = newton(w, x, ctx, 0.0, nullptr, tol, maxit, vlim, &zp);
+  *iters += std::abs(r);
+  return r > 0 ? CEDAR_ST_OK : CEDAR_ST_DCOP;
+}
+
+// ------------------------------------------------------------------ transient
+static void fill_defaults(const cedar_tran_opts *in, cedar_tran_opts &o) {
+  o = *in;
+  double span = o.tstop - o.tstart;
+  if (o.max_newton <= 0) o.max_newton = 20;
+  if (o.max_steps <= 0) o.max_steps = 100000000;
+  if (o.reltol <= 0) o.reltol = 1e-6;
+  if (o.abstol_v <= 0) o.abstol_v = 1e-9;
+  if (o.abstol_i <= 0) o.abstol_i = 1e-12;
+  if (o.nr_factor <= 0) o.nr_factor = 1e-3;
+  if (o.hfirst_frac <= 0) o.hfirst_frac = 1e-2;
+  if (o.hmax <= 0) o.hmax = span / 50.0;
+  if (o.hmin <= 0) o.hmin = span * 1e-12;
+}
+
+// Output sink: every accepted point, or uniform probe samples (quadratic
+// interpolation through the last three accepted points of the current segment,
+// linear when only two are available).
+struct Sink {
+  // all-points mode
+  double *t_out = nullptr, *x_out = nullptr; int64_t cap = 0, count = 0;
+  // samples mode
+  const int *probes = nullptr; int np = 0; int ns = 0; double *samp = nullptr; int next = 0;
+  double tstart = 0, tstop = 0;
+  int n = 0;
+  double ts(int j) const { return j == ns - 1 ? tstop : tstart + (tstop - tstart) * ((double)j / (double)(ns - 1)); }
+  void point(double t, const double *x) {
+    if (t_out) { if (count < cap) { t_out[count] = t; std::memcpy(x_out + (size_t)count * n, x, sizeof(double) * n); } count++; }
+  }
+  void start(const double *x) {
+    if (samp && ns > 0) { for (int p = 0; p < np; ++p) samp[(size_t)p * ns] = probes[p] >= 0 ? x[probes[p]] : 0.0; next = 1; }
+  }
+  // step from (t1,x1) to (t2,x2), previous point (t0,x0) valid if have0
+  void step(bool have0, double t0, const double *x0, double t1, const double *x1, double t2, const double *x2) {
+    if (!samp) return;
+    while (next < ns && ts(next) <= t2) {
+      double t = ts(next);
+      for (int p = 0; p < np; ++p) {
+        int u = probes[p]; double v;
+        if (u < 0) v = 0.0;
+        else if (have0) {
+          double L0 = (t - t1) * (t - t2) / ((t0 - t1) * (t0 - t2));
+          double L1 = (t - t0) * (t - t2) / ((t1 - t0) * (t1 - t2));
+          double L2 = (t - t0) * (t - t1) / ((t2 - t0) * (t2 - t1));
+          v = x0[u] * L0 + x1[u] * L1 + x2[u] * L2;
+        } else {
+          double a = (t - t1) / (t2 - t1);
+          v = x1[u] + (x2[u] - x1[u]) * a;
+        }
+        samp[(size_t)p * ns + next] = v;
+      }
+      ++next;
+    }
+  }
+};
+
+static double quant_factor(double f) {
+  // step-size factors are rounded down to multiples of 1/8 so that CPU and GPU
+  // (whose pow/rounding may differ in the last ulp) pick identical steps
+  double q = std::floor(f * 8.0) / 8.0;
+  return std::max(0.125, std::min(2.0, q));
+}
+
+static int tran(const Circuit &c, const cedar_tran_opts *opts_in, double *x, Sink &sink, cedar_stats &st,
+                const double *perturb) {
+  cedar_tran_opts o; fill_defaults(opts_in, o);
+  const int n = c.n; const int nn = c.n_nodes;
+  Work w(c);
+  st = cedar_stats{}; st.hmin_seen = std::numeric_limits<double>::infinity(); st.hmax_seen = 0;
+  Tol tol{o.nr_factor * o.reltol, o.nr_factor * o.abstol_v, o.nr_factor * o.abstol_i};
+  if (o.dcop) {
+    int s = dcop(w, x, o.tstart, tol, &st.dc_iters);
+    if (s != CEDAR_ST_OK) { st.status = s; return s; }
+  }
+  if (perturb) for (int i = 0; i < n; ++i) x[i] += perturb[i];
+  EvalCtx ctx; ctx.dc = false;
+  std::vector<double> qn(n), qm1(n), qd(n), hist(n), xn(n), xm1(n), xm2(n), xp(n), qt(n);
+  ctx.t = o.tstart; eval_q(w, x, ctx, qn.data());
+  std::copy(x, x + n, xn.begin());
+  sink.n = n; sink.tstart = o.tstart; sink.tstop = o.tstop;
+  sink.point(o.tstart, x); sink.start(x);
+  int zp = 0;
+  if (!o.adaptive) {
+    const double h = o.h;
+    const int64_t N = (int64_t)std::llround((o.tstop - o.tstart) / h);
+    std::fill(qd.begin(), qd.end(), 0.0);
+    double tprev = o.tstart, tprev2 = o.tstart; bool have_prev = false;
+    for (int64_t k = 1; k <= N; ++k) {
+      double t = (k == N) ? o.tstop : o.tstart + (double)k * h;
+      double hk = t - tprev;
+      double cj;
+      if (o.method == CEDAR_TRAP) {
+        cj = 2.0 / hk;
+        for (int i = 0; i < n; ++i) hist[i] = -cj * qn[i] - qd[i];
+      } else if (k == 1) {
+        cj = 1.0 / hk;
+        for (int i = 0; i < n; ++i) hist[i] = -qn[i] / hk;
+      } else {
+        cj = 1.5 / hk;
+        for (int i = 0; i < n; ++i) hist[i] = (-4.0 * qn[i] + qm1[i]) / (2.0 * hk);
+      }
+      if (k == 1) std::copy(xn.begin(), xn.end(), xp.begin());
+      else for (int i = 0; i < n; ++i) xp[i] = 2.0 * xn[i] - xm1[i];
+      ctx.t = t;
+      int r = newton(w, xp.data(), ctx, cj, hist.data(), tol, o.max_newton, 0.0, &zp);
+      st.newton_iters += std::abs(r);
+      if (r <= 0) { st.status = zp ? CEDAR_ST_ZERO_PIVOT : CEDAR_ST_NEWTON; std::copy(xn.begin(), xn.end(), x); return st.status; }
+      eval_q(w, xp.data(), ctx, qt.data());
+      if (o.method == CEDAR_TRAP) for (int i = 0; i < n; ++i) qd[i] = cj * qt[i] + hist[i];
+      qm1 = qn; qn = qt;
+      sink.step(have_prev, tprev2, xm1.data(), tprev, xn.data(), t, xp.data());
+      xm1 = xn; xn = xp; tprev2 = tprev; tprev = t; have_prev = true;
+      st.accepted++; st.hmin_seen = std::min(st.hmin_seen, hk); st.hmax_seen = std::max(st.hmax_seen, hk);
+      sink.point(t, xn.data());
+      for (int i = 0; i < n; ++i) if (!std::isfinite(xn[i])) { st.status = CEDAR_ST_NAN; std::copy(xn.begin(), xn.end(), x); return st.status; }
+    }
+    std::copy(xn.begin(), xn.end(), x);
+    st.status = CEDAR_ST_OK;
+    return CEDAR_ST_OK;
+  }
+
+  // ---- adaptive variable-step BDF2 ----
+  const double span = o.tstop - o.tstart;
+  const double eps_bp = span * 1e-12;
+  double t = o.tstart;
+  double tn1 = t, tn2 = t;   // t_{n-1}, t_{n-2}
+  int npts = 1;              // accepted points in the current segment (incl. t_n)
+  auto restart_h = [&](double tt) {
+    double nb = std::min(next_breakpoint(c, tt, eps_bp), o.tstop);
+    double hf = o.hfirst_frac * std::min(nb - tt, o.hmax);
+    if (o.h > 0) hf = std::min(hf, o.h);
+    return hf;
+  };
+  double hnext = restart_h(t);
+  int64_t nsteps = 0;
+  while (t < o.tstop) {
+    if (++nsteps > o.max_steps) { st.status = CEDAR_ST_MAX_STEPS; break; }
+    double tb = std::min(next_breakpoint(c, t, eps_bp), o.tstop);
+    double h = std::min(hnext, o.hmax);
+    bool hit = false;
+    if (tb - t <= 1.1 * h) { h = tb - t; hit = true; }
+    double tnew = hit ? tb : t + h;
+    h = tnew - t;
+    int order = npts >= 2 ? 2 : 1;
+    double cj, h1 = t - tn1;
+    if (order == 1) {
+      cj = 1.0 / h;
+      for (int i = 0; i < n; ++i) hist[i] = -qn[i] / h;
+    } else {
+      double wr = h / h1;
+      cj = (1.0 + 2.0 * wr) / ((1.0 + wr) * h);
+      double a1 = -(1.0 + wr), a2 = wr * wr / (1.0 + wr);
+      for (int i = 0; i < n; ++i) hist[i] = (a1 * qn[i] + a2 * qm1[i]) / h;
+    }
+    if (npts >= 2) { double r = h / h1; for (int i = 0; i < n; ++i) xp[i] = xn[i] + r * (xn[i] - xm1[i]); }
+    else std::copy(xn.begin(), xn.end(), xp.begin());
+    ctx.t = tnew;
+    int r = newton(w, xp.data(), ctx, cj, hist.data(), tol, o.max_newton, 0.0, &zp);
+    st.newton_iters += std::abs(r);
+    if (r <= 0) {
+      st.rejected++;
+      hnext = h * 0.125;
+      if (hnext < o.hmin) { st.status = zp ? CEDAR_ST_ZERO_PIVOT : CEDAR_ST_DT_UNDERFLOW; break; }
+      continue;
+    }
+    double err = 0.0;
+    if (npts >= 3) {
+      double h2 = tn1 - tn2;
+      // third divided difference over (tnew, t, tn1, tn2)
+      double coef = h * h * (h + h1) * (h + h1) / (2.0 * h + h1);
+      for (int i = 0; i < nn; ++i) {
+        double d10 = (xp[i] - xn[i]) / h;
+        double d21 = (xn[i] - xm1[i]) / h1;
+        double d32 = (xm1[i] - xm2[i]) / h2;
+        double dd2a = (d10 - d21) / (h + h1);
+        double dd2b = (d21 - d32) / (h1 + h2);
+        double dd3 = (dd2a - dd2b) / (h + h1 + h2);
+        double lte = std::fabs(dd3) * coef;
+        double sc = o.reltol * std::max(std::fabs(xp[i]), std::fabs(xn[i])) + o.abstol_v;
+        double q = lte / sc;
+        if (!(q <= 1e300)) q = 1e30;
+        err = std::max(err, q);
+      }
+    } else if (npts == 2) {
+      // second step after a (re)start: backward-Euler-type bound h^2 |x''| / 2 with
+      // x'' ~ 2 * second divided difference over (tnew, t, tn1)
+      for (int i = 0; i < nn; ++i) {
+        double d10 = (xp[i] - xn[i]) / h;
+        double d21 = (xn[i] - xm1[i]) / h1;
+        double dd2 = (d10 - d21) / (h + h1);
+        double lte = std::fabs(dd2) * (h * h);
+        double sc = o.reltol * std::max(std::fabs(xp[i]), std::fabs(xn[i])) + o.abstol_v;
+        double q = lte / sc;
+        if (!(q <= 1e300)) q = 1e30;
+        err = std::max(err, q);
+      }
+    }
+    if (!std::isfinite(err)) err = 1e30;
+    if (err > 1.0) {
+      st.rejected++;
+      hnext = h * quant_factor(0.9 * std::pow(err, -1.0 / 3.0));
+      if (hnext < o.hmin) { st.status = CEDAR_ST_DT_UNDERFLOW; break; }
+      continue;
+    }
+    // accept
+    eval_q(w, xp.data(), ctx, qt.data());
+    qm1 = qn; qn = qt;
+    sink.step(npts >= 2, tn1, xm1.data(), t, xn.data(), tnew, xp.data());
+    xm2 = xm1; xm1 = xn; xn = xp;
+    tn2 = tn1; tn1 = t; t = tnew;
+    st.accepted++; st.hmin_seen = std::min(st.hmin_seen, h); st.hmax_seen = std::max(st.hmax_seen, h);
+    sink.point(t, xn.data());
+    bool finite = true; for (int i = 0; i < n; ++i) if (!std::isfinite(xn[i])) finite = false;
+    if (!finite) { st.status = CEDAR_ST_NAN; break; }
+    if (npts < 3) ++npts;
+    double fac = (err > 0.0) ? quant_factor(0.9 * std::pow(err, -1.0 / 3.0)) : 1.0;
+    hnext = h * fac;
+    if (hit && t < o.tstop) { npts = 1; hnext = restart_h(t); }
+  }
+  std::copy(xn.begin(), xn.end(), x);
+  if (st.status == CEDAR_ST_OK && t < o.tstop) st.status = CEDAR_ST_MAX_STEPS;
+  return st.status;
+}
+
+static thread_local std::string g_err;
+
+}  // namespace orc
+
+using namespace orc;
+
+extern "C" {
+
+int oracle_last_error(char *buf, size_t len) {
+  if (buf && len) { std::snprintf(buf, len, "%s", g_err.c_str()); }
+  return (int)g_err.size();
+}
+
+// F = Fi + C*xdot (xdot may be NULL); dense G, C (row-major n*n, may be NULL).
+int oracle_eval(const cedar_ckt_desc *d, const double *x, const double *xdot, double t, int dc,
+                double *F, double *Fi, double *Fq, double *G, double *C) {
+  Circuit c; if (!load_circuit(d, c, g_err)) return CEDAR_EINVAL;
+  EvalOut o(c.n); EvalCtx ctx; ctx.t = t; ctx.dc = dc != 0;
+  eval_circuit(c, x, ctx, o);
+  const int n = c.n;
+  if (F) for (int i = 0; i < n; ++i) { double s = o.Fi[i]; if (xdot) for (int j = 0; j < n; ++j) s += o.C[(size_t)i * n + j] * xdot[j]; F[i] = s; }
+  if (Fi) std::memcpy(Fi, o.Fi.data(), sizeof(double) * n);
+  if (Fq) std::memcpy(Fq, o.Fq.data(), sizeof(double) * n);
+  if (G) std::memcpy(G, o.G.data(), sizeof(double) * n * n);
+  if (C) std::memcpy(C, o.C.data(), sizeof(double) * n * n);
+  return 0;
+}
+
+int oracle_dcop(const cedar_ckt_desc *d, const cedar_tran_opts *opts, double t, double *x, cedar_stats *st) {
+  Circuit c; if (!load_circuit(d, c, g_err)) return CEDAR_EINVAL;
+  cedar_tran_opts o; fill_defaults(opts, o);
+  Tol tol{o.nr_factor * o.reltol, o.nr_factor * o.abstol_v, o.nr_factor * o.abstol_i};
+  Work w(c); cedar_stats s{}; s.status = dcop(w, x, t, tol, &s.dc_iters);
+  if (st) *st = s;
+  return s.status == CEDAR_ST_OK ? 0 : CEDAR_ENOCONV;
+}
+
+int oracle_newton(const cedar_ckt_desc *d, const cedar_tran_opts *opts, double t, double cj,
+                  const double *hist, double *x, cedar_stats *st) {
+  Circuit c; if (!load_circuit(d, c, g_err)) return CEDAR_EINVAL;
+  cedar_tran_opts o; fill_defaults(opts, o);
+  Tol tol{o.nr_factor * o.reltol, o.nr_factor * o.abstol_v, o.nr_factor * o.abstol_i};
+  Work w(c); EvalCtx ctx; ctx.t = t; int zp = 0;
+  int r = newton(w, x, ctx, cj, hist, tol, o.max_newton, 0.0, &zp);
+  if (st) { *st = cedar_stats{}; st->newton_iters = std::abs(r); st->status = r > 0 ? 0 : (zp ? CEDAR_ST_ZERO_PIVOT : CEDAR_ST_NEWTON); }
+  return r > 0 ? 0 : CEDAR_ENOCONV;
+}
+
+int oracle_tran(const cedar_ckt_desc *d, const cedar_tran_opts *opts, double *x,
+                double *t_out, double *x_out, int64_t cap, int64_t *n_out, cedar_stats *st) {
+  Circuit c; if (!load_circuit(d, c, g_err)) return CEDAR_EINVAL;
+  Sink sink; sink.t_out = t_out; sink.x_out = x_out; sink.cap = cap;
+  cedar_stats s{};
+  tran(c, opts, x, sink, s, nullptr);
+  if (n_out) *n_out = sink.count;
+  if (st) *st = s;
+  if (t_out && sink.count > cap) return CEDAR_ECAPACITY;
+  return 0;
+}
+
+double oracle_next_breakpoint(const cedar_ckt_desc *d, double t, double eps) {
+  Circuit c; if (!load_circuit(d, c, g_err)) return -1;
+  return next_breakpoint(c, t, eps);
+}
+
+double oracle_source_value(const cedar_ckt_desc *d, int group, int inst, double t, int dc) {
+  Circuit c; if (!load_circuit(d, c, g_err)) return NAN;
+  return source_value(c.groups[group], inst, t, dc != 0, c.pwl);
+}
+
+// Batched Monte Carlo / sweep: each instance = template with its parameter block,
+// DC op (if opts->dcop) + perturbation + transient; OpenMP over instances.
+// inst_range: [i0, i1) subset (for bounded CPU baselines).  nthreads <= 0: all.
+int oracle_batch(const cedar_batch_desc *b, const cedar_tran_opts *opts, int32_t i0, int32_t i1,
+                 int32_t n_max, double *x_final, double *samples, cedar_stats *stats, int nthreads) {
+  if (!b || i0 < 0 || i1 > b->n_inst || i0 > i1) { g_err = "bad batch range"; return CEDAR_EINVAL; }
+  std::vector<Circuit> tmpl(b->n_templates);
+  for (int k = 0; k < b->n_templates; ++k) if (!load_circuit(&b->templates[k], tmpl[k], g_err)) return CEDAR_EINVAL;
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#else
+  nthreads = 1;
+#endif
+  int rc_all = 0;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+  for (int i = i0; i < i1; ++i) {
+    int k = b->inst_template[i];
+    Circuit c = tmpl[k];
+    if (b->inst_par_off && b->inst_par_off[i] >= 0) {
+      const double *p = b->inst_par + b->inst_par_off[i];
+      for (Group &g : c.groups) { std::copy(p, p + g.par.size(), g.par.begin()); p += g.par.size(); }
+    }
+    std::vector<double> x(c.n, 0.0);
+    if (b->inst_x0_off && b->inst_x0_off[i] >= 0) std::copy(b->inst_x0 + b->inst_x0_off[i], b->inst_x0 + b->inst_x0_off[i] + c.n, x.begin());
+    const double *dx = (b->inst_dx_off && b->inst_dx_off[i] >= 0) ? b->inst_dx + b->inst_dx_off[i] : nullptr;
+    Sink sink;
+    sink.np = b->n_probes; sink.ns = b->n_samples;
+    sink.probes = b->probes ? b->probes + (size_t)k * b->n_probes : nullptr;
+    if (samples && b->n_samples > 0 && b->n_probes > 0) sink.samp = samples + (size_t)(i - i0) * b->n_probes * b->n_samples;
+    cedar_stats s{};
+    tran(c, opts, x.data(), sink, s, dx);
+    if (x_final) { double *xf = x_final + (size_t)(i - i0) * n_max; for (int u = 0; u < n_max; ++u) xf[u] = u < c.n ? x[u] : 0.0; }
+    if (stats) stats[i - i0] = s;
+  }
+  return rc_all;
+}
+
+}  // extern "C"

@@ -1,0 +1,122 @@
+"""ctypes binding of the CPU oracle (oracle/oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg as the checker / reported baseline, never by the
+product package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import pathlib
+import subprocess
+
+import numpy as np
+
+HERE = pathlib.Path(__file__).resolve().parent
+LIB = HERE / "_build" / "liboracle.so"
+_lib = None
+
+
+def build(force: bool = False) -> pathlib.Path:
+    src = HERE / "oracle.cpp"
+    hdr = HERE.parent / "include" / "cedar.h"
+    if force or not LIB.exists() or max(src.stat().st_mtime, hdr.stat().st_mtime) > LIB.stat().st_mtime:
+        subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    return LIB
+
+
+def load(pkg):
+    """Load the oracle; `pkg` is the product package (for its descriptor types)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    build()
+    lib = C.CDLL(str(LIB))
+    abi = pkg.abi
+    dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int64)
+    lib.oracle_eval.restype = C.c_int
+    lib.oracle_eval.argtypes = [C.POINTER(abi.CktDesc), dp, dp, C.c_double, C.c_int, dp, dp, dp, dp, dp]
+    lib.oracle_dcop.restype = C.c_int
+    lib.oracle_dcop.argtypes = [C.POINTER(abi.CktDesc), C.POINTER(abi.TranOpts), C.c_double, dp, C.POINTER(abi.Stats)]
+    lib.oracle_newton.restype = C.c_int
+    lib.oracle_newton.argtypes = [C.POINTER(abi.CktDesc), C.POINTER(abi.TranOpts), C.c_double, C.c_double, dp, dp,
+                                  C.POINTER(abi.Stats)]
+    lib.oracle_tran.restype = C.c_int
+    lib.oracle_tran.argtypes = [C.POINTER(abi.CktDesc), C.POINTER(abi.TranOpts), dp, dp, dp, C.c_int64, ip,
+                                C.POINTER(abi.Stats)]
+    lib.oracle_next_breakpoint.restype = C.c_double
+    lib.oracle_next_breakpoint.argtypes = [C.POINTER(abi.CktDesc), C.c_double, C.c_double]
+    lib.oracle_source_value.restype = C.c_double
+    lib.oracle_source_value.argtypes = [C.POINTER(abi.CktDesc), C.c_int, C.c_int, C.c_double, C.c_int]
+    lib.oracle_batch.restype = C.c_int
+    lib.oracle_batch.argtypes = [C.POINTER(abi.BatchDesc), C.POINTER(abi.TranOpts), C.c_int32, C.c_int32, C.c_int32,
+                                 dp, dp, C.c_void_p, C.c_int]
+    lib.oracle_last_error.restype = C.c_int
+    lib.oracle_last_error.argtypes = [C.c_char_p, C.c_size_t]
+    _lib = lib
+    return lib
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Oracle:
+    def __init__(self, pkg):
+        self.pkg = pkg
+        self.lib = load(pkg)
+
+    def eval(self, flat, x, xdot=None, t=0.0, dc=False):
+        h = self.pkg.abi.DescHolder(flat)
+        n = flat.n
+        x = np.ascontiguousarray(x, np.float64)
+        xdot = None if xdot is None else np.ascontiguousarray(xdot, np.float64)
+        F, Fi, Fq = np.zeros(n), np.zeros(n), np.zeros(n)
+        G, Cm = np.zeros((n, n)), np.zeros((n, n))
+        rc = self.lib.oracle_eval(C.byref(h.desc), _dp(x), _dp(xdot), t, int(dc), _dp(F), _dp(Fi), _dp(Fq), _dp(G), _dp(Cm))
+        assert rc == 0
+        return F, Fi, Fq, G, Cm
+
+    def dcop(self, flat, t=0.0, x0=None, opts=None):
+        h = self.pkg.abi.DescHolder(flat)
+        x = np.zeros(flat.n) if x0 is None else np.ascontiguousarray(x0, np.float64).copy()
+        o = opts or self.pkg.make_opts(tstop=1.0)
+        st = self.pkg.abi.Stats()
+        rc = self.lib.oracle_dcop(C.byref(h.desc), C.byref(o), t, _dp(x), C.byref(st))
+        return x, st, rc
+
+    def newton(self, flat, t, cj, hist, x0, opts=None):
+        h = self.pkg.abi.DescHolder(flat)
+        x = np.ascontiguousarray(x0, np.float64).copy()
+        hist = None if hist is None else np.ascontiguousarray(hist, np.float64)
+        o = opts or self.pkg.make_opts(tstop=1.0)
+        st = self.pkg.abi.Stats()
+        rc = self.lib.oracle_newton(C.byref(h.desc), C.byref(o), t, cj, _dp(hist), _dp(x), C.byref(st))
+        return x, st, rc
+
+    def tran(self, flat, opts, x0=None, cap=1 << 20):
+        h = self.pkg.abi.DescHolder(flat)
+        x = np.zeros(flat.n) if x0 is None else np.ascontiguousarray(x0, np.float64).copy()
+        t_out = np.zeros(cap)
+        x_out = np.zeros((cap, flat.n))
+        n_out = C.c_int64()
+        st = self.pkg.abi.Stats()
+        rc = self.lib.oracle_tran(C.byref(h.desc), C.byref(opts), _dp(x), _dp(t_out), _dp(x_out), cap, C.byref(n_out), C.byref(st))
+        m = min(n_out.value, cap)
+        return t_out[:m].copy(), x_out[:m].copy(), st, rc
+
+    def batch(self, holder, opts, i0=0, i1=None, n_max=None, nthreads=0, want_samples=True):
+        i1 = holder.n_inst if i1 is None else i1
+        if n_max is None:
+            n_max = max(f.flat.n for f in holder.templates)
+        cnt = i1 - i0
+        xf = np.zeros((cnt, n_max))
+        np_ = holder.desc.n_probes
+        ns = holder.desc.n_samples
+        samp = np.zeros((cnt, np_, ns)) if (want_samples and np_ and ns) else None
+        st = np.zeros(cnt, self.pkg.abi.STATS_DTYPE)
+        rc = self.lib.oracle_batch(C.byref(holder.desc), C.byref(opts), i0, i1, n_max, _dp(xf), _dp(samp),
+                                   st.ctypes.data_as(C.c_void_p), nthreads)
+        assert rc == 0
+        return xf, samp, st
