@@ -171,14 +171,16 @@ struct Engine {
   }
 
   // K2: J slots and residual rows (F = hist + contributions)
-  __device__ void stamp(const double *hist, double gshunt, const double *x) {
+  // gshunt (DC homotopy): node rows get -gshunt * (x - xref) (xref null = ground)
+  __device__ void stamp(const double *hist, double gshunt, const double *x, const double *xref) {
     for (int s = g.rank; s < T.nnz_lu; s += g.size) w.lu[s] = gather(T.jlu_ptr, T.jlu_ent, s, 0.0);
     for (int r = g.rank; r < T.n; r += g.size) w.F[r] = gather(T.fint_ptr, T.fint_ent, r, hist ? hist[r] : 0.0);
     if (gshunt != 0.0) {
       g.sync();
       for (int u = g.rank; u < T.n_nodes; u += g.size) {
+        int c = T.gs_col[u];
         w.lu[T.gs_slot[u]] -= gshunt;
-        w.F[T.gs_row[u]] -= gshunt * x[T.gs_col[u]];
+        w.F[T.gs_row[u]] -= gshunt * (x[c] - (xref ? xref[c] : 0.0));
       }
     }
   }
@@ -236,11 +238,11 @@ struct Engine {
   // Newton on Fi(x,t) + cj Fq(x) + hist = 0.  Returns iterations (>0), -iters on
   // failure, 0 on a zero pivot.  Mirrors the oracle's newton().
   __device__ int newton(double *x, const EvalCtx &ctx, const double *hist, double rel, double av, double ai,
-                        int maxit, double vlim, double gshunt) {
+                        int maxit, double vlim, double gshunt, const double *xref = nullptr) {
     for (int it = 1; it <= maxit; ++it) {
       eval_devices(x, ctx, false);
       g.sync();
-      stamp(hist, gshunt, x);
+      stamp(hist, gshunt, x, xref);
       g.sync();
       if (!factor()) return 0;
       solve(w.F);
@@ -287,38 +289,59 @@ struct Engine {
 
   // DC operating point (mirrors the oracle's dcop()); x internal order.
   __device__ int dcop(double *x, double t, double rel, double av, double ai, long long *iters) {
-    const int maxit = 100; const double vlim = 0.5;
+    const int maxit = 100; const double vlim = 0.0;  // no damping: PTC bounds the steps
+    const long long budget = 20000;
     EvalCtx ctx{t, 0.0, 1.0, T.gmin, true, false};
     copy(w.x0, x);
     g.sync();
+    long long used = 0;
     int r = newton(x, ctx, nullptr, rel, av, ai, maxit, vlim, 0.0);
-    *iters += r < 0 ? -r : r;
-    if (r > 0) return CEDAR_ST_OK;
+    used += r < 0 ? -r : r;
+    if (r > 0) { *iters += used; return CEDAR_ST_OK; }
+    // pseudo-transient continuation (xr = w.xm1, scratch = w.xs)
+    double *xr = w.xm1;
+    for (int pass = 0; pass < 2; ++pass) {
+      const double pv = pass == 0 ? 0.5 : 0.0;
+      copy(xr, w.x0);
+      g.sync();
+      double gs = 1e-2; int fails = 0; bool ptc_ok = false;
+      while (used < budget && fails <= 60) {
+        copy(w.xs, xr);
+        g.sync();
+        r = newton(w.xs, ctx, nullptr, rel, av, ai, 50, pv, gs, xr);
+        used += r < 0 ? -r : r;
+        if (r > 0) {
+          copy(xr, w.xs);
+          g.sync();
+          if (gs <= 1e-14) { ptc_ok = true; break; }
+          gs *= 0.1;
+        } else { gs *= 4.0; ++fails; }
+      }
+      if (ptc_ok) {
+        copy(x, xr);
+        g.sync();
+        r = newton(x, ctx, nullptr, rel, av, ai, maxit, pv, 0.0);
+        used += r < 0 ? -r : r;
+        if (r > 0) { *iters += used; return CEDAR_ST_OK; }
+      }
+    }
+    // source stepping from zero
     fill(x, 0.0);
     g.sync();
     double lam = 0.0, dl = 0.1; int halv = 0; bool ok = true;
     while (lam < 1.0) {
+      if (used >= budget) { ok = false; break; }
       double ln = lam + dl < 1.0 ? lam + dl : 1.0;
       copy(w.xs, x);
       g.sync();
       ctx.src_scale = ln;
       r = newton(w.xs, ctx, nullptr, rel, av, ai, maxit, vlim, 0.0);
-      *iters += r < 0 ? -r : r;
+      used += r < 0 ? -r : r;
       if (r > 0) { copy(x, w.xs); g.sync(); lam = ln; halv = 0; dl = dl * 2 < 0.1 ? dl * 2 : 0.1; }
       else { dl *= 0.5; if (++halv > 8) { ok = false; break; } }
     }
-    ctx.src_scale = 1.0;
-    if (ok) return CEDAR_ST_OK;
-    copy(x, w.x0);
-    g.sync();
-    for (double gs = 1e-2; gs >= 1e-12 * 0.999; gs *= 0.1) {
-      r = newton(x, ctx, nullptr, rel, av, ai, maxit, vlim, gs);
-      *iters += r < 0 ? -r : r;
-      if (r <= 0) return CEDAR_ST_DCOP;
-    }
-    r = newton(x, ctx, nullptr, rel, av, ai, maxit, vlim, 0.0);
-    *iters += r < 0 ? -r : r;
-    return r > 0 ? CEDAR_ST_OK : CEDAR_ST_DCOP;
+    *iters += used;
+    return ok ? CEDAR_ST_OK : CEDAR_ST_DCOP;
   }
 
   // ---- output sink helpers

@@ -191,13 +191,13 @@ CEDAR_HD void eval_device(int model, const double *dp, int ds, const double *v, 
     case CEDAR_MOS1: {
       double type = dp[0], beta = dp[ds], vth = dp[2 * ds], lam = dp[3 * ds], m = dp[4 * ds];
       double vgs = type * (v[1] - v[2]), vds = type * (v[0] - v[2]);
-      double id, gm, gds;
-      if (vds >= 0) mos1_fwd(vgs, vds, vth, beta, lam, id, gm, gds);
-      else { double i1, g1, g2; mos1_fwd(vgs - vds, -vds, vth, beta, lam, i1, g1, g2); id = -i1; gm = -g1; gds = g1 + g2; }
+      // gsum = -dIds/dVs - gmin = gm + gds, formed without cancellation in reverse mode
+      double id, gm, gds, gsum;
+      if (vds >= 0) { mos1_fwd(vgs, vds, vth, beta, lam, id, gm, gds); gsum = gm + gds; }
+      else { double i1, g1, g2; mos1_fwd(vgs - vds, -vds, vth, beta, lam, i1, g1, g2); id = -i1; gm = -g1; gds = g1 + g2; gsum = g2; }
       double gmin = ctx.gmin;
       double ids = type * id + gmin * (v[0] - v[2]);
-      double gdd = gds + gmin;
-      out[0] = m * ids; out[1] = m * gm; out[2] = m * gdd; out[3] = m * (gm + gdd);
+      out[0] = m * ids; out[1] = m * gm; out[2] = m * (gds + gmin); out[3] = m * (gsum + gmin);
     } break;
     case CEDAR_DIODE: {
       double isat = dp[0], invnvt = dp[ds], m = dp[2 * ds];

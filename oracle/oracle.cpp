@@ -208,6 +208,7 @@ struct Acc {
 
 struct EvalCtx {
   double t = 0; bool dc = false; double src_scale = 1.0; double gshunt = 0.0;
+  const double *xref = nullptr;  // reference point of the gshunt term (null = ground)
 };
 
 static Dual mos1_id(const Dual &vgs, const Dual &vds, double vth, double beta, double lam) {
@@ -308,7 +309,10 @@ static void eval_circuit(const Circuit &c, const double *x, const EvalCtx &ctx, 
     }
   }
   if (ctx.gshunt != 0.0) {
-    for (int k = 0; k < c.n_nodes; ++k) { o.Fi[k] += -ctx.gshunt * x[k]; o.G[(size_t)k * c.n + k] += -ctx.gshunt; }
+    for (int k = 0; k < c.n_nodes; ++k) {
+      o.Fi[k] += -ctx.gshunt * (x[k] - (ctx.xref ? ctx.xref[k] : 0.0));
+      o.G[(size_t)k * c.n + k] += -ctx.gshunt;
+    }
   }
 }
 
@@ -394,43 +398,62 @@ static void eval_q(Work &w, const double *x, const EvalCtx &ctx, double *q) {
   for (int i = 0; i < w.c.n; ++i) q[i] = w.eo.Fq[i];
 }
 
-// DC operating point: Newton (damped) from the guess; on failure, source stepping
-// lambda = 0.1 .. 1 (halving the increment on failure, at most 8 halvings per
-// increment); on failure, gmin stepping gshunt = 1e-2 .. 1e-12 then 0.
+// DC operating point (CedarDCOp's role, src/dcop.jl:53-94): damped Newton from the
+// guess; on failure pseudo-transient continuation (Kelley & Keyes, SIAM J. Numer.
+// Anal. 35 (1998)); on failure source stepping lambda = 0.1 .. 1 (halving the
+// increment on failure, at most 8 halvings).  At most 20000 Newton iterations.
 static int dcop(Work &w, double *x, double t, const Tol &tol, int64_t *iters) {
-  const int n = w.c.n; const int maxit = 100; const double vlim = 0.5;
+  const int n = w.c.n; const int maxit = 100; const double vlim = 0.0;  // no damping: PTC bounds the steps
+  const int64_t budget = 20000;  // total Newton iterations this DC solve may spend
   EvalCtx ctx; ctx.t = t; ctx.dc = true;
-  std::vector<double> x0(x, x + n), xs(n);
+  std::vector<double> x0(x, x + n), xs(n), xr(n);
   int zp = 0;
+  int64_t used = 0;
   int r = newton(w, x, ctx, 0.0, nullptr, tol, maxit, vlim, &zp);
-  *iters += std::abs(r);
-  if (r > 0) return CEDAR_ST_OK;
-  // source stepping
+  used += std::abs(r);
+  if (r > 0) { *iters += used; return CEDAR_ST_OK; }
+  // pseudo-transient continuation: node rows get -gs (x - xr), xr = last accepted
+  // iterate; gs shrinks 10x after a converged level and grows 4x after a failed one.
+  // Pass 0 damps node updates to 0.5 V per iteration, pass 1 does not.
+  for (int pass = 0; pass < 2; ++pass) {
+    const double pv = pass == 0 ? 0.5 : 0.0;
+    std::copy(x0.begin(), x0.end(), xr.begin());
+    double gs = 1e-2; int fails = 0; bool ptc_ok = false;
+    while (used < budget && fails <= 60) {
+      std::copy(xr.begin(), xr.end(), xs.begin());
+      ctx.gshunt = gs; ctx.xref = xr.data();
+      r = newton(w, xs.data(), ctx, 0.0, nullptr, tol, 50, pv, &zp);
+      used += std::abs(r);
+      if (r > 0) {
+        std::copy(xs.begin(), xs.end(), xr.begin());
+        if (gs <= 1e-14) { ptc_ok = true; break; }
+        gs *= 0.1;
+      } else { gs *= 4.0; ++fails; }
+    }
+    ctx.gshunt = 0.0; ctx.xref = nullptr;
+    if (ptc_ok) {
+      std::copy(xr.begin(), xr.end(), x);
+      r = newton(w, x, ctx, 0.0, nullptr, tol, maxit, pv, &zp);
+      used += std::abs(r);
+      if (r > 0) { *iters += used; return CEDAR_ST_OK; }
+    }
+  }
+  // source stepping from zero
   std::fill(x, x + n, 0.0);
   double lam = 0.0, dl = 0.1; int halv = 0; bool ok = true;
   while (lam < 1.0) {
+    if (used >= budget) { ok = false; break; }
     double ln = std::min(1.0, lam + dl);
     std::copy(x, x + n, xs.begin());
     ctx.src_scale = ln;
     r = newton(w, xs.data(), ctx, 0.0, nullptr, tol, maxit, vlim, &zp);
-    *iters += std::abs(r);
+    used += std::abs(r);
     if (r > 0) { std::copy(xs.begin(), xs.end(), x); lam = ln; halv = 0; dl = std::min(0.1, dl * 2); }
     else { dl *= 0.5; if (++halv > 8) { ok = false; break; } }
   }
   ctx.src_scale = 1.0;
-  if (ok) return CEDAR_ST_OK;
-  // gmin stepping
-  std::copy(x0.begin(), x0.end(), x);
-  for (double gs = 1e-2; gs >= 1e-12 * 0.999; gs *= 0.1) {
-    ctx.gshunt = gs;
-    r = newton(w, x, ctx, 0.0, nullptr, tol, maxit, vlim, &zp);
-    *iters += std::abs(r);
-    if (r <= 0) return CEDAR_ST_DCOP;
-  }
-  ctx.gshunt = 0.0;
-  r = newton(w, x, ctx, 0.0, nullptr, tol, maxit, vlim, &zp);
-  *iters += std::abs(r);
-  return r > 0 ? CEDAR_ST_OK : CEDAR_ST_DCOP;
+  *iters += used;
+  return ok ? CEDAR_ST_OK : CEDAR_ST_DCOP;
 }
 
 // ------------------------------------------------------------------ transient
