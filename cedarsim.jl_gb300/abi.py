@@ -30,7 +30,9 @@ class DevGroup(C.Structure):
 class CktDesc(C.Structure):
     _fields_ = [("n_nodes", C.c_int32), ("n_branch", C.c_int32), ("n_groups", C.c_int32),
                 ("groups", C.POINTER(DevGroup)), ("pwl", c_double_p), ("n_pwl", C.c_int64),
-                ("temp_c", C.c_double), ("gmin", C.c_double)]
+                ("temp_c", C.c_double), ("gmin", C.c_double), ("ordering", C.c_int32), ("reserved", C.c_int32)]
+
+ORDER_AUTO, ORDER_MIN_DEGREE, ORDER_NESTED_DISSECTION = 0, 1, 2
 
 
 class TranOpts(C.Structure):
@@ -58,6 +60,13 @@ class BatchDesc(C.Structure):
                 ("inst_dx", c_double_p), ("n_probes", C.c_int32), ("probes", c_int32_p), ("n_samples", C.c_int32)]
 
 
+class Costs(C.Structure):
+    _fields_ = [("flops_eval", C.c_int64), ("flops_stamp", C.c_int64), ("flops_lu", C.c_int64),
+                ("flops_solve", C.c_int64), ("flops_update", C.c_int64), ("bytes", C.c_int64),
+                ("lu_levels", C.c_int32), ("fw_levels", C.c_int32), ("bw_levels", C.c_int32), ("nnz_lu", C.c_int32),
+                ("ordering", C.c_int32), ("pad", C.c_int32)]
+
+
 class BatchTuning(C.Structure):
     _fields_ = [("lanes_per_inst", C.c_int32), ("warps_per_cta", C.c_int32), ("reserved", C.c_int32 * 6)]
 
@@ -71,8 +80,10 @@ def ptr(a: Optional[np.ndarray], ctype):
 class DescHolder:
     """A CktDesc plus the arrays it references."""
 
-    def __init__(self, flat: Flat):
+    def __init__(self, flat: Flat, ordering: int = None):
         self.flat = flat
+        if ordering is None:
+            ordering = getattr(flat, "ordering", 0)
         self.keep: List[object] = []
         gs = (DevGroup * max(1, len(flat.groups)))()
         for k, (model, term, br, par) in enumerate(flat.groups):
@@ -89,7 +100,8 @@ class DescHolder:
         pwl = np.ascontiguousarray(flat.pwl, dtype=np.float64)
         self.keep.append(pwl)
         self.desc = CktDesc(flat.n_nodes, flat.n_branch, len(flat.groups), gs,
-                            ptr(pwl if pwl.size else None, C.c_double), pwl.size, flat.temp_c, flat.gmin)
+                            ptr(pwl if pwl.size else None, C.c_double), pwl.size, flat.temp_c, flat.gmin,
+                            int(ordering), 0)
 
 
 def make_opts(method="bdf2", adaptive=True, tstart=0.0, tstop=1.0, h=0.0, dcop=True, reltol=1e-6, abstol_v=1e-9,
@@ -141,8 +153,9 @@ LIB_PATH = PKG / "_build" / "libcedar_gpu.so"
 EXPORTS = [
     "cedar_last_error", "cedar_version", "cedar_model_nterm", "cedar_model_npar", "cedar_model_has_branch",
     "cedar_tran_opts_default", "cedar_ckt_create", "cedar_plan_create", "cedar_ckt_destroy", "cedar_ckt_size", "cedar_ckt_pattern",
-    "cedar_ckt_symbolic", "cedar_eval", "cedar_eval_dev", "cedar_newton_solve", "cedar_dcop", "cedar_tran_run",
-    "cedar_batch_create", "cedar_batch_destroy", "cedar_batch_run", "cedar_batch_set_tuning",
+    "cedar_ckt_costs", "cedar_ckt_symbolic", "cedar_eval", "cedar_eval_dev", "cedar_newton_solve", "cedar_dcop", "cedar_tran_run",
+    "cedar_batch_create", "cedar_batch_destroy", "cedar_batch_run", "cedar_batch_start", "cedar_batch_advance",
+    "cedar_batch_results", "cedar_batch_last_ms", "cedar_batch_set_tuning",
     "cedar_batch_get_tuning", "cedar_batch_autotune", "cedar_batch_nmax",
 ]
 
@@ -173,6 +186,7 @@ def load_library(build_if_missing: bool = True):
         "cedar_ckt_destroy": (C.c_int, [P]),
         "cedar_ckt_size": (C.c_int, [P, c_int32_p, c_int32_p, c_int32_p, c_int32_p]),
         "cedar_ckt_pattern": (C.c_int, [P, c_int32_p, c_int32_p]),
+        "cedar_ckt_costs": (C.c_int, [P, C.POINTER(Costs)]),
         "cedar_ckt_symbolic": (C.c_int, [P, c_int32_p, c_int32_p, c_int32_p, c_int32_p]),
         "cedar_eval": (C.c_int, [P, c_double_p, c_double_p, C.c_double, C.c_double, c_double_p, c_double_p]),
         "cedar_eval_dev": (C.c_int, [P, P, P, C.c_double, C.c_double, P, P]),
@@ -183,6 +197,10 @@ def load_library(build_if_missing: bool = True):
         "cedar_batch_create": (C.c_int, [C.POINTER(BatchDesc), C.POINTER(P)]),
         "cedar_batch_destroy": (C.c_int, [P]),
         "cedar_batch_run": (C.c_int, [P, C.POINTER(TranOpts), c_double_p, c_double_p, P]),
+        "cedar_batch_start": (C.c_int, [P, C.POINTER(TranOpts)]),
+        "cedar_batch_advance": (C.c_int, [P, C.c_double, c_int32_p]),
+        "cedar_batch_results": (C.c_int, [P, c_double_p, c_double_p, P]),
+        "cedar_batch_last_ms": (C.c_int, [P, c_double_p]),
         "cedar_batch_set_tuning": (C.c_int, [P, C.POINTER(BatchTuning)]),
         "cedar_batch_get_tuning": (C.c_int, [P, C.POINTER(BatchTuning)]),
         "cedar_batch_autotune": (C.c_int, [P, C.POINTER(TranOpts), C.c_double, C.POINTER(BatchTuning)]),

@@ -108,6 +108,20 @@ class System:
         return x, st, rc
 
 
+def costs(circuit: Union[Circuit, Flat]) -> dict:
+    """Algorithmic FP64 work and bytes of one Newton iteration (host-only analysis)."""
+    lib = load_library()
+    holder = DescHolder(_flat(circuit))
+    h = C.c_void_p()
+    check(lib.cedar_plan_create(C.byref(holder.desc), C.byref(h)))
+    try:
+        c = abi.Costs()
+        check(lib.cedar_ckt_costs(h, C.byref(c)))
+        return {k: getattr(c, k) for k, _ in abi.Costs._fields_}
+    finally:
+        lib.cedar_ckt_destroy(h)
+
+
 @dataclass
 class Solution:
     t: np.ndarray

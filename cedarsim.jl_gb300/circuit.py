@@ -117,6 +117,7 @@ class Flat:
     gmin: float
     names: List[str]                       # unknown names (nodes, then "<dev>.I" branches)
     devices: Dict[str, Tuple[int, int]]    # device name -> (group index, instance index)
+    ordering: int = 0                      # LU ordering: 0 auto, 1 min degree, 2 nested dissection
 
     @property
     def n(self) -> int:

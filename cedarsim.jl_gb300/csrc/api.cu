@@ -46,17 +46,19 @@ struct Packer {
   template <class T> size_t vec(const std::vector<T> &v) { return add(v.data(), v.size() * sizeof(T)); }
 };
 
-int compile_only(const cedar_ckt_desc *desc, std::unique_ptr<DevTemplate> &out, int ordering = ORDER_MIN_DEGREE) {
+int compile_only(const cedar_ckt_desc *desc, std::unique_ptr<DevTemplate> &out) {
   auto dt = std::make_unique<DevTemplate>();
   std::string err;
+  int ordering = desc ? desc->ordering : 0;
+  if (ordering < 0 || ordering > 2) return fail(CEDAR_EINVAL, "unknown ordering");
   if (!compile_template(desc, dt->H, err, ordering)) return fail(err.find("singular") != std::string::npos ? CEDAR_ESINGULAR : CEDAR_EINVAL, err);
   out = std::move(dt);
   return 0;
 }
 
-int upload_template(const cedar_ckt_desc *desc, std::unique_ptr<DevTemplate> &out, int ordering = ORDER_MIN_DEGREE) {
+int upload_template(const cedar_ckt_desc *desc, std::unique_ptr<DevTemplate> &out) {
   std::unique_ptr<DevTemplate> dt;
-  int rc0 = compile_only(desc, dt, ordering);
+  int rc0 = compile_only(desc, dt);
   if (rc0) return rc0;
   Template &H = dt->H;
   std::vector<DGroup> grp; std::vector<int> dev_end; int nd = 0;
@@ -71,6 +73,12 @@ int upload_template(const cedar_ckt_desc *desc, std::unique_ptr<DevTemplate> &ou
     const GroupInfo &g = H.groups[H.src_group[k]];
     src_off.push_back(g.dpar_off + H.src_inst[k]); src_stride.push_back(g.n_inst);
   }
+  std::vector<int> src_of_dev(std::max(nd, 1), -1);
+  for (size_t k = 0; k < H.src_group.size(); ++k) {
+    int base = 0;
+    for (int g = 0; g < H.src_group[k]; ++g) base += H.groups[g].n_inst;
+    src_of_dev[base + H.src_inst[k]] = (int)k;
+  }
   std::vector<int> gs_row(H.n_nodes), gs_col(H.n_nodes);
   for (int u = 0; u < H.n_nodes; ++u) { gs_row[u] = H.eq_pos[u]; gs_col[u] = H.iorder[u]; }
   Packer P;
@@ -81,6 +89,7 @@ int upload_template(const cedar_ckt_desc *desc, std::unique_ptr<DevTemplate> &ou
   size_t o_lu_lvl = P.vec(H.lu_lvl_ptr), o_lu_slot = P.vec(H.lu_task_slot), o_lu_info = P.vec(H.lu_task_info), o_lu_pp = P.vec(H.lu_pair_ptr), o_lu_pair = P.vec(lu_pair);
   size_t o_fw_lvl = P.vec(H.fw_lvl_ptr), o_fw_row = P.vec(H.fw_row), o_fw_ptr = P.vec(H.fw_ptr), o_fw_pair = P.vec(fw_pair);
   size_t o_bw_lvl = P.vec(H.bw_lvl_ptr), o_bw_row = P.vec(H.bw_row), o_bw_ptr = P.vec(H.bw_ptr), o_bw_pair = P.vec(bw_pair);
+  size_t o_src_of_dev = P.vec(src_of_dev);
   size_t o_src_off = P.vec(src_off), o_src_stride = P.vec(src_stride), o_gs_slot = P.vec(H.gs_slot), o_gs_row = P.vec(gs_row), o_gs_col = P.vec(gs_col);
   size_t o_is_node = P.vec(H.is_node_int), o_order = P.vec(H.order), o_iorder = P.vec(H.iorder), o_eq_pos = P.vec(H.eq_pos), o_pwl = P.vec(H.pwl);
   CUDA_TRY(cudaMalloc(&dt->buf, P.bytes.size()));
@@ -103,6 +112,7 @@ int upload_template(const cedar_ckt_desc *desc, std::unique_ptr<DevTemplate> &ou
   D.fw_lvl = (const int *)(b + o_fw_lvl); D.fw_row = (const int *)(b + o_fw_row); D.fw_ptr = (const int *)(b + o_fw_ptr); D.fw_pair = (const int2 *)(b + o_fw_pair);
   D.bw_lvl = (const int *)(b + o_bw_lvl); D.bw_row = (const int *)(b + o_bw_row); D.bw_ptr = (const int *)(b + o_bw_ptr); D.bw_pair = (const int2 *)(b + o_bw_pair);
   D.src_off = (const int *)(b + o_src_off); D.src_stride = (const int *)(b + o_src_stride);
+  D.src_of_dev = (const int *)(b + o_src_of_dev);
   D.gs_slot = (const int *)(b + o_gs_slot); D.gs_row = (const int *)(b + o_gs_row); D.gs_col = (const int *)(b + o_gs_col);
   D.is_node = (const unsigned char *)(b + o_is_node); D.order = (const int *)(b + o_order); D.iorder = (const int *)(b + o_iorder);
   D.eq_pos = (const int *)(b + o_eq_pos); D.pwl = (const double *)(b + o_pwl);
@@ -177,10 +187,21 @@ struct cedar_batch {
   DevBuf<long long> raw_off, dpar_off, x0_off, dx_off;
   DevBuf<double> raw, dpar, x0, dx, samples, xfinal, ws;
   DevBuf<EngStats> stats;
+  DevBuf<StateRow> rows;
+  DevBuf<double> row_vec;
+  DevBuf<int> n_running;
   int n_inst = 0, n_max = 0, np = 0, ns = 0, ws_stride = 0;
   bool has_x0 = false, has_dx = false;
   cedar_batch_tuning tune{};
-  ~cedar_batch() { if (stream) cudaStreamDestroy(stream); }
+  EngOpts run_opts{};   // options of the run in progress (cedar_batch_start)
+  bool started = false;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // bracket the last batch launch
+  bool timed = false;
+  ~cedar_batch() {
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (stream) cudaStreamDestroy(stream);
+  }
 };
 
 extern "C" {
@@ -219,8 +240,8 @@ int cedar_ckt_create(const cedar_ckt_desc *desc, cedar_ckt **out) {
   CUDA_TRY(c->x.ensure(n)); CUDA_TRY(c->xdot.ensure(n)); CUDA_TRY(c->F.ensure(n)); CUDA_TRY(c->hist.ensure(n));
   CUDA_TRY(c->J.ensure(H.j_rowidx.size())); CUDA_TRY(c->dout.ensure(H.n_out));
   CUDA_TRY(c->stats.ensure(1)); CUDA_TRY(c->count.ensure(1));
-  size_t wsd = ws_doubles(H.n, H.nnz_lu, H.n_out);
-  if ((wsd + 64) * sizeof(double) > 160 * 1024) CUDA_TRY(c->ws.ensure(wsd));
+  size_t wsd = ws_doubles(H.n, H.nnz_lu, H.n_out, (int)H.src_group.size());
+  if ((wsd + 128) * sizeof(double) > 160 * 1024) CUDA_TRY(c->ws.ensure(wsd));
   int work = std::max(std::max(H.nnz_lu, n), c->tpl->D.n_dev);
   c->threads = work >= 512 ? 512 : std::max(64, ((work + 31) / 32) * 32);
   CUDA_TRY(cudaStreamSynchronize(c->stream));
@@ -248,6 +269,50 @@ int cedar_ckt_size(const cedar_ckt *c, int32_t *n, int32_t *nnz_j, int32_t *nnz_
   if (nnz_j) *nnz_j = (int32_t)H.j_rowidx.size();
   if (nnz_lu) *nnz_lu = H.nnz_lu;
   if (n_levels) *n_levels = (int32_t)(H.lu_lvl_ptr.size() - 1);
+  return 0;
+}
+
+// FP64 operations of one device evaluation (add/sub/mul/div = 1, FMA = 2,
+// exp = 1; counted from the expressions in models.cuh, the source waveform as
+// 10 for a pulse/pwl/sin segment evaluation)
+static int model_flops(int m) {
+  switch (m) {
+    case CEDAR_R: return 2;
+    case CEDAR_C: return 4;
+    case CEDAR_L: return 7;
+    case CEDAR_V: return 13;
+    case CEDAR_I: return 11;
+    case CEDAR_E: return 5;
+    case CEDAR_G: return 2;
+    case CEDAR_MOS1: return 32;
+    case CEDAR_DIODE: return 13;
+    case CEDAR_NLVCR: return 10;
+  }
+  return 0;
+}
+
+int cedar_ckt_costs(const cedar_ckt *c, cedar_costs *o) {
+  if (!c || !o) return fail(CEDAR_EINVAL, "null argument");
+  const Template &H = c->tpl->H;
+  cedar_costs r{};
+  int64_t dev_bytes = 0;
+  for (const GroupInfo &g : H.groups) {
+    const ModelInfo &mi = model_info(g.model);
+    r.flops_eval += (int64_t)model_flops(g.model) * g.n_inst;
+    dev_bytes += (int64_t)g.n_inst * (8 * mi.ndpar + 4 * g.ntx + 8 * g.ntx + 16 * mi.nout);
+  }
+  r.flops_stamp = (int64_t)H.jlu_ent.size() + (int64_t)H.fint_ent.size() + H.n;
+  r.flops_lu = H.lu_flops;
+  r.flops_solve = 2 * ((int64_t)H.fw_lu.size() + (int64_t)H.bw_lu.size()) + H.n;
+  r.flops_update = 4 * (int64_t)H.n;
+  r.bytes = dev_bytes + 4 * (int64_t)(H.jlu_ent.size() + H.fint_ent.size()) + 16 * (int64_t)H.nnz_lu +
+            8 * 2 * (int64_t)H.lu_pair_a.size() + 8 * 2 * (int64_t)(H.fw_lu.size() + H.bw_lu.size()) + 8 * 6 * (int64_t)H.n;
+  r.lu_levels = (int32_t)H.lu_lvl_ptr.size() - 1;
+  r.fw_levels = (int32_t)H.fw_lvl_ptr.size() - 1;
+  r.bw_levels = (int32_t)H.bw_lvl_ptr.size() - 1;
+  r.nnz_lu = H.nnz_lu;
+  r.ordering = H.ordering;
+  *o = r;
   return 0;
 }
 
@@ -315,7 +380,7 @@ static int run_plain(cedar_ckt *c, int mode, const cedar_tran_opts *opts, double
     a.t_out = c->tout.p; a.x_out = c->xout.p; a.cap = cap;
   }
   a.count = c->count.p; a.stats = c->stats.p; a.ws_global = c->ws.p;
-  CUDA_TRY(launch_plain(a, ws_doubles(H.n, H.nnz_lu, H.n_out), c->threads, c->stream));
+  CUDA_TRY(launch_plain(a, ws_doubles(H.n, H.nnz_lu, H.n_out, (int)H.src_group.size()), c->threads, c->stream));
   EngStats st{}; long long cnt = 0;
   CUDA_TRY(cudaMemcpyAsync(&st, c->stats.p, sizeof(st), cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(cudaMemcpyAsync(&cnt, c->count.p, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
@@ -365,11 +430,13 @@ int cedar_batch_create(const cedar_batch_desc *d, cedar_batch **out) {
     int rc = upload_template(&d->templates[k], t);
     if (rc) return rc;
     b->n_max = std::max(b->n_max, t->H.n);
-    b->ws_stride = std::max(b->ws_stride, ws_doubles(t->H.n, t->H.nnz_lu, t->H.n_out));
+    b->ws_stride = std::max(b->ws_stride, ws_doubles(t->H.n, t->H.nnz_lu, t->H.n_out, (int)t->H.src_group.size()));
     hd.push_back(t->D);
     b->tpls.push_back(std::move(t));
   }
-  b->ws_stride = (b->ws_stride + 1) & ~1;
+  // slot workspaces start 8 doubles (64 B) past a 128-B multiple apart, so the
+  // slots of a warp touching the same offset fall in different shared-memory banks
+  b->ws_stride = ((b->ws_stride + 15) / 16) * 16 + 8;
   const int ni = d->n_inst;
   b->n_inst = ni;
   CUDA_TRY(b->d_tpls.ensure(hd.size()));
@@ -442,6 +509,9 @@ int cedar_batch_create(const cedar_batch_desc *d, cedar_batch **out) {
   });
   if ((rc = up(b->queue, q))) return rc;
   CUDA_TRY(b->head.ensure(1));
+  CUDA_TRY(b->n_running.ensure(1));
+  CUDA_TRY(b->rows.ensure(std::max(ni, 1)));
+  CUDA_TRY(b->row_vec.ensure((size_t)std::max(ni, 1) * 6 * b->n_max));
   CUDA_TRY(b->stats.ensure(std::max(ni, 1)));
   CUDA_TRY(b->xfinal.ensure((size_t)std::max(ni, 1) * b->n_max));
   if (b->np) CUDA_TRY(b->samples.ensure((size_t)std::max(ni, 1) * b->np * b->ns));
@@ -474,7 +544,8 @@ int cedar_batch_get_tuning(const cedar_batch *b, cedar_batch_tuning *t) {
   return 0;
 }
 
-static int batch_launch(cedar_batch *b, const EngOpts &eo, const cedar_batch_tuning &tu, bool want_outputs) {
+static int batch_launch(cedar_batch *b, const EngOpts &eo, const cedar_batch_tuning &tu, bool want_outputs,
+                        double t_until, bool fresh) {
   int K = tu.lanes_per_inst, warps = tu.warps_per_cta;
   int tiles = warps * 32 / K;
   size_t per_tile = (size_t)b->ws_stride * sizeof(double);
@@ -502,9 +573,60 @@ static int batch_launch(cedar_batch *b, const EngOpts &eo, const cedar_batch_tun
   bd.x_final = want_outputs ? b->xfinal.p : nullptr; bd.n_max = b->n_max;
   bd.stats = b->stats.p; bd.queue = b->queue.p; bd.head = b->head.p; bd.n_inst = b->n_inst;
   bd.opts = eo; bd.ws_stride = b->ws_stride; bd.ws_global = b->ws.p; bd.ws_in_smem = in_smem ? 1 : 0;
+  bd.t_until = t_until; bd.rows = b->rows.p; bd.row_vec = b->row_vec.p; bd.n_running = b->n_running.p;
   CUDA_TRY(cudaMemsetAsync(b->head.p, 0, sizeof(int), b->stream));
-  if (want_outputs) CUDA_TRY(cudaMemsetAsync(b->xfinal.p, 0, (size_t)b->n_inst * b->n_max * sizeof(double), b->stream));
+  CUDA_TRY(cudaMemsetAsync(b->n_running.p, 0, sizeof(int), b->stream));
+  if (fresh) {
+    CUDA_TRY(cudaMemsetAsync(b->rows.p, 0, (size_t)b->n_inst * sizeof(StateRow), b->stream));
+    if (want_outputs) CUDA_TRY(cudaMemsetAsync(b->xfinal.p, 0, (size_t)b->n_inst * b->n_max * sizeof(double), b->stream));
+  }
+  if (!b->ev0) { CUDA_TRY(cudaEventCreate(&b->ev0)); CUDA_TRY(cudaEventCreate(&b->ev1)); }
+  CUDA_TRY(cudaEventRecord(b->ev0, b->stream));
   CUDA_TRY(launch_batch(bd, K, warps, grid, smem, b->stream));
+  CUDA_TRY(cudaEventRecord(b->ev1, b->stream));
+  b->timed = true;
+  return 0;
+}
+
+int cedar_batch_last_ms(cedar_batch *b, double *ms) {
+  if (!b || !ms) return fail(CEDAR_EINVAL, "null argument");
+  if (!b->timed) return fail(CEDAR_EINVAL, "no batch launch recorded yet");
+  CUDA_TRY(cudaEventSynchronize(b->ev1));
+  float f = 0; CUDA_TRY(cudaEventElapsedTime(&f, b->ev0, b->ev1));
+  *ms = f;
+  return 0;
+}
+
+int cedar_batch_start(cedar_batch *b, const cedar_tran_opts *opts) {
+  if (!b) return fail(CEDAR_EINVAL, "null handle");
+  int rc = check_opts(opts); if (rc) return rc;
+  b->run_opts = to_eng(opts);
+  b->started = true;
+  CUDA_TRY(cudaMemsetAsync(b->rows.p, 0, (size_t)std::max(b->n_inst, 1) * sizeof(StateRow), b->stream));
+  CUDA_TRY(cudaMemsetAsync(b->xfinal.p, 0, (size_t)std::max(b->n_inst, 1) * b->n_max * sizeof(double), b->stream));
+  return 0;
+}
+
+int cedar_batch_advance(cedar_batch *b, double t_until, int32_t *n_running) {
+  if (!b) return fail(CEDAR_EINVAL, "null handle");
+  if (!b->started) return fail(CEDAR_EINVAL, "cedar_batch_start was not called");
+  int rc;
+  if (b->n_inst > 0 && (rc = batch_launch(b, b->run_opts, b->tune, true, t_until, false))) return rc;
+  if (n_running) {
+    int v = 0;
+    CUDA_TRY(cudaMemcpyAsync(&v, b->n_running.p, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    *n_running = v;
+  }
+  return 0;
+}
+
+int cedar_batch_results(cedar_batch *b, double *x_final, double *samples, cedar_stats *stats) {
+  if (!b) return fail(CEDAR_EINVAL, "null handle");
+  if (x_final) CUDA_TRY(cudaMemcpyAsync(x_final, b->xfinal.p, (size_t)b->n_inst * b->n_max * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  if (samples && b->np) CUDA_TRY(cudaMemcpyAsync(samples, b->samples.p, (size_t)b->n_inst * b->np * b->ns * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  if (stats) CUDA_TRY(cudaMemcpyAsync(stats, b->stats.p, (size_t)b->n_inst * sizeof(EngStats), cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
   return 0;
 }
 
@@ -512,8 +634,8 @@ int cedar_batch_run(cedar_batch *b, const cedar_tran_opts *opts, double *x_final
   if (!b) return fail(CEDAR_EINVAL, "null handle");
   int rc = check_opts(opts); if (rc) return rc;
   if (b->n_inst == 0) return 0;
-  EngOpts eo = to_eng(opts);
-  if ((rc = batch_launch(b, eo, b->tune, true))) return rc;
+  if ((rc = cedar_batch_start(b, opts))) return rc;
+  if ((rc = batch_launch(b, b->run_opts, b->tune, true, 1e300, false))) return rc;
   if (x_final) CUDA_TRY(cudaMemcpyAsync(x_final, b->xfinal.p, (size_t)b->n_inst * b->n_max * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
   if (samples && b->np) CUDA_TRY(cudaMemcpyAsync(samples, b->samples.p, (size_t)b->n_inst * b->np * b->ns * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
   if (stats) CUDA_TRY(cudaMemcpyAsync(stats, b->stats.p, (size_t)b->n_inst * sizeof(EngStats), cudaMemcpyDeviceToHost, b->stream));
@@ -536,7 +658,7 @@ int cedar_batch_autotune(cedar_batch *b, const cedar_tran_opts *opts, double hor
   for (int K : Ks) for (int W : Ws) {
     cedar_batch_tuning t{}; t.lanes_per_inst = K; t.warps_per_cta = W;
     CUDA_TRY(cudaEventRecord(e0, b->stream));
-    if ((rc = batch_launch(b, eo, t, false))) return rc;
+    if ((rc = batch_launch(b, eo, t, false, 1e300, true))) return rc;
     CUDA_TRY(cudaEventRecord(e1, b->stream));
     CUDA_TRY(cudaEventSynchronize(e1));
     float ms = 0; CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));

@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cmath>
 #include <map>
+#include <functional>
 #include <set>
 
 namespace cedar {
@@ -164,7 +165,103 @@ static void min_degree(int n, std::vector<std::set<int>> adj, std::vector<int> &
   }
 }
 
-bool compile_template(const cedar_ckt_desc *d, Template &T, std::string &err, int ordering) {
+
+// Nested dissection by level structures (George, SIAM J. Numer. Anal. 10 (1973);
+// George & Liu 1978): dense vertices (degree > max(16, 4 sqrt n)) are ordered
+// last; each connected component of the rest is split at the middle BFS level
+// from a pseudo-peripheral vertex, the two sides ordered recursively, the
+// separator after them.  Ties and traversal orders use the lowest index.
+static void nested_dissection(int n, const std::vector<std::set<int>> &adj, std::vector<int> &order) {
+  const int thresh = std::max(16, (int)(4.0 * std::sqrt((double)n)));
+  std::vector<char> dense(n, 0), in(n, 0), seen(n, 0);
+  for (int v = 0; v < n; ++v) dense[v] = (int)adj[v].size() > thresh;
+  order.clear();
+  auto bfs = [&](int root, std::vector<std::vector<int>> &levels) {
+    levels.clear();
+    std::vector<int> cur{root}; std::vector<int> mark;
+    seen[root] = 1; mark.push_back(root);
+    while (!cur.empty()) {
+      std::sort(cur.begin(), cur.end());
+      levels.push_back(cur);
+      std::vector<int> nxt;
+      for (int v : cur) for (int w : adj[v]) if (in[w] && !seen[w]) { seen[w] = 1; mark.push_back(w); nxt.push_back(w); }
+      cur.swap(nxt);
+    }
+    for (int v : mark) seen[v] = 0;
+  };
+  auto deg_in = [&](int v) { int d = 0; for (int w : adj[v]) d += in[w]; return d; };
+  std::function<void(std::vector<int>)> nd = [&](std::vector<int> V) {
+    std::sort(V.begin(), V.end());
+    for (int v : V) in[v] = 1;
+    // connected components, each from its smallest vertex
+    std::vector<std::vector<int>> comps;
+    for (int v : V) {
+      if (seen[v]) continue;
+      std::vector<int> comp{v}; seen[v] = 1;
+      for (size_t k = 0; k < comp.size(); ++k)
+        for (int w : adj[comp[k]]) if (in[w] && !seen[w]) { seen[w] = 1; comp.push_back(w); }
+      std::sort(comp.begin(), comp.end());
+      comps.push_back(comp);
+    }
+    for (int v : V) seen[v] = 0;
+    for (int v : V) in[v] = 0;
+    if (comps.size() > 1) { for (auto &c : comps) nd(c); return; }
+    std::vector<int> &C = comps[0];
+    if (C.size() <= 3) { for (int v : C) order.push_back(v); return; }
+    for (int v : C) in[v] = 1;
+    std::vector<std::vector<int>> levels, lv2;
+    bfs(C[0], levels);
+    for (int rep = 0; rep < 5; ++rep) {
+      int u = -1, best = 1 << 30;
+      for (int v : levels.back()) { int d = deg_in(v); if (d < best) { best = d; u = v; } }
+      bfs(u, lv2);
+      if (lv2.size() > levels.size()) levels.swap(lv2); else break;
+    }
+    const int m = (int)levels.size() - 1;
+    if (m < 2) { for (int v : C) in[v] = 0; for (int v : C) order.push_back(v); return; }
+    std::vector<int> S = levels[m / 2];
+    std::vector<char> sep(0);
+    std::vector<int> rest;
+    for (int v : C) in[v] = 0;
+    for (int v : S) in[v] = 2;  // mark separator
+    for (int v : C) if (in[v] != 2) rest.push_back(v);
+    for (int v : S) in[v] = 0;
+    nd(rest);
+    for (int v : S) order.push_back(v);
+  };
+  std::vector<int> V, D;
+  for (int v = 0; v < n; ++v) (dense[v] ? D : V).push_back(v);
+  if (!V.empty()) nd(V);
+  std::stable_sort(D.begin(), D.end(), [&](int a, int b) { return adj[a].size() < adj[b].size(); });
+  for (int v : D) order.push_back(v);
+}
+
+// Estimated critical path of one refactorisation + substitutions when every
+// level runs on a group of lanes: per level, the longest task (2 flops per
+// pair) plus the pivot reciprocal, plus a barrier.
+static double schedule_cost(const Template &T) {
+  double c = 0;
+  for (size_t l = 0; l + 1 < T.lu_lvl_ptr.size(); ++l) {
+    int maxp = 0; bool diag = false;
+    for (int t = T.lu_lvl_ptr[l]; t < T.lu_lvl_ptr[l + 1]; ++t) {
+      maxp = std::max(maxp, T.lu_pair_ptr[t + 1] - T.lu_pair_ptr[t]);
+      if ((T.lu_task_info[t] & 3) == 1) diag = true;
+    }
+    c += 4 + 2 * maxp + (diag ? 6 : 0);
+  }
+  auto rows = [&](const std::vector<int32_t> &lvl, const std::vector<int32_t> &ptr) {
+    for (size_t l = 0; l + 1 < lvl.size(); ++l) {
+      int maxp = 0;
+      for (int t = lvl[l]; t < lvl[l + 1]; ++t) maxp = std::max(maxp, ptr[t + 1] - ptr[t]);
+      c += 4 + 2 * maxp;
+    }
+  };
+  rows(T.fw_lvl_ptr, T.fw_ptr);
+  rows(T.bw_lvl_ptr, T.bw_ptr);
+  return c;
+}
+
+static bool compile_with(const cedar_ckt_desc *d, Template &T, std::string &err, int ordering) {
   if (!d) { err = "null desc"; return false; }
   if (d->n_nodes < 0 || d->n_branch < 0 || d->n_groups < 0 || (d->n_groups > 0 && !d->groups)) { err = "malformed desc"; return false; }
   T = Template();
@@ -252,7 +349,9 @@ bool compile_template(const cedar_ckt_desc *d, Template &T, std::string &err, in
     int up = eq2u[u]; if (up != u) { adj[up].insert(u); adj[u].insert(up); }
   }
   if (ordering == ORDER_NATURAL) { T.order.resize(n); for (int i = 0; i < n; ++i) T.order[i] = i; }
+  else if (ordering == ORDER_NESTED_DISSECTION) nested_dissection(n, adj, T.order);
   else min_degree(n, adj, T.order);
+  T.ordering = ordering;
   T.iorder.assign(n, 0);
   for (int p = 0; p < n; ++p) T.iorder[T.order[p]] = p;
   T.eq_pos.assign(n, 0);
@@ -390,6 +489,21 @@ bool compile_template(const cedar_ckt_desc *d, Template &T, std::string &err, in
     emit(lf, true, T.fw_lvl_ptr, T.fw_row, T.fw_ptr, T.fw_lu, T.fw_col);
     emit(lb, false, T.bw_lvl_ptr, T.bw_row, T.bw_ptr, T.bw_lu, T.bw_col);
   }
+  return true;
+}
+
+bool compile_template(const cedar_ckt_desc *d, Template &T, std::string &err, int ordering) {
+  if (ordering == ORDER_AUTO) {
+    Template A, B;
+    if (!compile_with(d, A, err, ORDER_MIN_DEGREE)) return false;
+    if (!compile_with(d, B, err, ORDER_NESTED_DISSECTION)) return false;
+    A.sched_cost = schedule_cost(A);
+    B.sched_cost = schedule_cost(B);
+    T = (B.sched_cost < A.sched_cost) ? std::move(B) : std::move(A);
+    return true;
+  }
+  if (!compile_with(d, T, err, ordering)) return false;
+  T.sched_cost = schedule_cost(T);
   return true;
 }
 

@@ -77,12 +77,14 @@ struct Template {
   std::vector<int32_t> gs_slot;
 
   int64_t lu_flops = 0;  // pair count (FMAs) + L scalings + reciprocals
+  int ordering = 0;       // ordering actually used
+  double sched_cost = 0;  // estimated critical path of LU + substitutions
 };
 
 // Ordering strategies for the fill-reducing symmetric permutation.
-enum Ordering { ORDER_MIN_DEGREE = 0, ORDER_NATURAL = 1 };
+enum Ordering { ORDER_AUTO = 0, ORDER_MIN_DEGREE = 1, ORDER_NESTED_DISSECTION = 2, ORDER_NATURAL = 3 };
 
 bool compile_template(const cedar_ckt_desc *d, Template &T, std::string &err,
-                      int ordering = ORDER_MIN_DEGREE);
+                      int ordering = ORDER_AUTO);
 
 }  // namespace cedar

@@ -34,6 +34,7 @@ struct DTpl {
   const int *fw_lvl, *fw_row, *fw_ptr; const int2 *fw_pair;
   const int *bw_lvl, *bw_row, *bw_ptr; const int2 *bw_pair;
   const int *src_off, *src_stride;    // derived-param offset / stride per source
+  const int *src_of_dev;              // [n_dev] time-varying source index, or -1
   const int *gs_slot;                 // [n_nodes] LU slot of (KCL(u),u)
   const int *gs_row;                  // [n_nodes] internal row of KCL(u)
   const int *gs_col;                  // [n_nodes] internal column of u
@@ -45,19 +46,70 @@ struct DTpl {
 };
 
 // workspace size in doubles for one instance
-__host__ __device__ inline int ws_doubles(int n, int nnz_lu, int n_out) {
-  return 13 * n + nnz_lu + n_out + 8;
+__host__ __device__ inline int ws_doubles(int n, int nnz_lu, int n_out, int n_src) {
+  return 13 * n + nnz_lu + n_out + n_src + 8;
 }
 
 struct WS {
-  double *x, *xn, *xm1, *xm2, *qn, *qm1, *qd, *hist, *F, *lu, *rd, *dout, *qt, *xs, *x0;
-  __device__ void bind(double *base, int n, int nnz_lu, int n_out) {
+  double *x, *xn, *xm1, *xm2, *qn, *qm1, *qd, *hist, *F, *lu, *rd, *dout, *qt, *xs, *x0, *srcv;
+  __device__ void bind(double *base, int n, int nnz_lu, int n_out, int n_src) {
     double *p = base;
     x = p; p += n; xn = p; p += n; xm1 = p; p += n; xm2 = p; p += n; qn = p; p += n; qm1 = p; p += n;
     qd = p; p += n; hist = p; p += n; F = p; p += n; rd = p; p += n; qt = p; p += n; xs = p; p += n; x0 = p; p += n;
-    lu = p; p += nnz_lu; dout = p; p += n_out;
+    lu = p; p += nnz_lu; dout = p; p += n_out; srcv = p; p += n_src;
   }
 };
+
+// Step-size factor: the largest k/8 (k = 1..16) with (k/8)^3 err <= 0.729, i.e.
+// k/8 <= 0.9 err^(-1/3).  (k/8)^3 = k^3/512 is exact, so CPU and GPU agree.
+__device__ __forceinline__ double step_factor(double err) {
+  if ((4096.0 / 512.0) * err <= 0.729) return 2.0;
+  if (!((1.0 / 512.0) * err <= 0.729)) return 0.125;
+  int lo = 1, hi = 16;
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (((double)(mid * mid * mid) / 512.0) * err <= 0.729) lo = mid; else hi = mid;
+  }
+  return lo * 0.125;
+}
+
+// Largest lte/sc ratio tracked as a fraction and compared by cross-multiplication
+// (one division per step instead of one per unknown).
+struct MaxRatio {
+  double num, den; bool bad;
+  __device__ MaxRatio() : num(0.0), den(1.0), bad(false) {}
+  __device__ __forceinline__ void add(double lte, double sc) {
+    if (!(lte <= 1e300) || !(sc > 0.0)) { bad = true; return; }
+    if (lte * den > num * sc) { num = lte; den = sc; }
+  }
+  __device__ __forceinline__ void merge(double n2, double d2, bool b2) {
+    bad = bad || b2;
+    if (n2 * den > num * d2) { num = n2; den = d2; }
+  }
+  __device__ __forceinline__ double value() const { return bad ? 1e30 : num / den; }
+};
+
+// Reciprocal of a pivot: hardware approximation refined by two Newton-Raphson
+// steps r <- r + r (1 - a r) (Flynn, 1970); within 1 ulp of 1/a for the normal
+// range the pivot check admits.
+__device__ __forceinline__ double pivot_rcp(double a) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(a));
+  r = fma(r, fma(-a, r, 1.0), r);
+  r = fma(r, fma(-a, r, 1.0), r);
+  return r;
+}
+
+// |a| in [2^-997, 2^997): pivot magnitude accepted by the static-pivot LU
+// (integer test on the exponent field, off the FP64 pipe)
+__device__ __forceinline__ bool pivot_ok(double a) {
+  unsigned e = (unsigned)(__double_as_longlong(a) >> 52) & 0x7ffu;
+  return e >= 26u && e < 2020u;
+}
+
+// integer-domain helpers for non-negative doubles (bit patterns order like integers)
+__device__ __forceinline__ long long abs_bits(double a) { return __double_as_longlong(a) & 0x7fffffffffffffffLL; }
+__device__ __forceinline__ bool finite_big(double a) { return abs_bits(a) < 0x7e37e43c8800759cLL; }  // |a| < 1e300
 
 // ------------------------------------------------------------- thread groups
 template <int K>
@@ -81,11 +133,21 @@ struct TileGroup {
     return v;
   }
   __device__ __forceinline__ int bcast(int v) const { return K == 1 ? v : __shfl_sync(mask, v, 0, K); }
+  __device__ double ratio(MaxRatio m) const {
+#pragma unroll
+    for (int o = K / 2; o > 0; o >>= 1) {
+      double n2 = __shfl_xor_sync(mask, m.num, o, K), d2 = __shfl_xor_sync(mask, m.den, o, K);
+      bool b2 = __shfl_xor_sync(mask, (int)m.bad, o, K) != 0;
+      m.merge(n2, d2, b2);
+    }
+    if (K > 1) { m.num = __shfl_sync(mask, m.num, 0, K); m.den = __shfl_sync(mask, m.den, 0, K); m.bad = __shfl_sync(mask, (int)m.bad, 0, K) != 0; }
+    return m.value();
+  }
 };
 
 struct BlockGroup {
   int rank, size;
-  double *red;  // shared scratch of >= 32 doubles
+  double *red;  // shared scratch of >= 96 doubles
   __device__ BlockGroup(double *r) : rank(threadIdx.x), size(blockDim.x), red(r) {}
   __device__ __forceinline__ void sync() const { __syncthreads(); }
   __device__ __forceinline__ bool any(bool p) const { return __syncthreads_or(p) != 0; }
@@ -102,6 +164,21 @@ struct BlockGroup {
   }
   __device__ double max(double v) const { return reduce(v, true); }
   __device__ double min(double v) const { return reduce(v, false); }
+  __device__ double ratio(MaxRatio m) const {
+    for (int o = 16; o > 0; o >>= 1) {
+      double n2 = __shfl_xor_sync(0xffffffffu, m.num, o), d2 = __shfl_xor_sync(0xffffffffu, m.den, o);
+      bool b2 = __shfl_xor_sync(0xffffffffu, (int)m.bad, o) != 0;
+      m.merge(n2, d2, b2);
+    }
+    int warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) { red[3 * warp] = m.num; red[3 * warp + 1] = m.den; red[3 * warp + 2] = m.bad ? 1.0 : 0.0; }
+    __syncthreads();
+    MaxRatio r; r.num = red[0]; r.den = red[1]; r.bad = red[2] != 0.0;
+    for (int i = 1; i < nw; ++i) r.merge(red[3 * i], red[3 * i + 1], red[3 * i + 2] != 0.0);
+    __syncthreads();
+    return r.value();
+  }
   __device__ int bcast(int v) const {
     __syncthreads();
     if (threadIdx.x == 0) ((int *)red)[0] = v;
@@ -122,7 +199,7 @@ struct EngOpts {
 struct EngStats {
   long long accepted, rejected, newton_iters, dc_iters;
   double hmin_seen, hmax_seen;
-  int status;
+  int status, pad;
 };
 
 // Output sink: record every accepted point (plain) and/or probe samples (batch).
@@ -132,11 +209,6 @@ struct Sink {
   double tstart, tstop;
 };
 
-__device__ __forceinline__ double quant_factor(double f) {
-  double q = floor(f * 8.0) / 8.0;
-  return q < 0.125 ? 0.125 : (q > 2.0 ? 2.0 : q);
-}
-
 template <class G>
 struct Engine {
   const DTpl &T;
@@ -145,7 +217,7 @@ struct Engine {
   G g;
 
   __device__ Engine(const DTpl &t, const double *dpar, double *ws, G grp) : T(t), dp(dpar), g(grp) {
-    w.bind(ws, T.n, T.nnz_lu, T.n_out);
+    w.bind(ws, T.n, T.nnz_lu, T.n_out, T.n_src);
   }
 
   // K1: evaluate devices at x (internal order); q_only restricts to charge devices
@@ -389,7 +461,7 @@ struct Engine {
   __device__ void tran(double *x, const EngOpts &o, Sink &sk, EngStats &st, const double *perturb) {
     const int n = T.n;
     st.accepted = st.rejected = st.newton_iters = st.dc_iters = 0;
-    st.hmin_seen = 1e300; st.hmax_seen = 0; st.status = CEDAR_ST_OK;
+    st.hmin_seen = 1e300; st.hmax_seen = 0; st.status = CEDAR_ST_OK; st.pad = 0;
     const double rel = o.nr_factor * o.reltol, av = o.nr_factor * o.abstol_v, ai = o.nr_factor * o.abstol_i;
     if (o.dcop) {
       int s = dcop(x, o.tstart, rel, av, ai, &st.dc_iters);
@@ -416,10 +488,11 @@ struct Engine {
           for (int i = g.rank; i < n; i += g.size) w.hist[i] = -cj * w.qn[i] - w.qd[i];
         } else if (k == 1) {
           cj = 1.0 / hk;
-          for (int i = g.rank; i < n; i += g.size) w.hist[i] = -w.qn[i] / hk;
+          for (int i = g.rank; i < n; i += g.size) w.hist[i] = -w.qn[i] * cj;
         } else {
           cj = 1.5 / hk;
-          for (int i = g.rank; i < n; i += g.size) w.hist[i] = (-4.0 * w.qn[i] + w.qm1[i]) / (2.0 * hk);
+          double r2h = 0.5 / hk;
+          for (int i = g.rank; i < n; i += g.size) w.hist[i] = (-4.0 * w.qn[i] + w.qm1[i]) * r2h;
         }
         if (k == 1) copy(xp, w.xn);
         else for (int i = g.rank; i < n; i += g.size) xp[i] = 2.0 * w.xn[i] - w.xm1[i];
@@ -471,12 +544,12 @@ struct Engine {
       double cj, h1 = t - tn1;
       if (order == 1) {
         cj = 1.0 / h;
-        for (int i = g.rank; i < n; i += g.size) w.hist[i] = -w.qn[i] / h;
+        for (int i = g.rank; i < n; i += g.size) w.hist[i] = -w.qn[i] * cj;
       } else {
-        double wr = h / h1;
+        double wr = h / h1, rh = 1.0 / h;
         cj = (1.0 + 2.0 * wr) / ((1.0 + wr) * h);
         double a1 = -(1.0 + wr), a2 = wr * wr / (1.0 + wr);
-        for (int i = g.rank; i < n; i += g.size) w.hist[i] = (a1 * w.qn[i] + a2 * w.qm1[i]) / h;
+        for (int i = g.rank; i < n; i += g.size) w.hist[i] = (a1 * w.qn[i] + a2 * w.qm1[i]) * rh;
       }
       if (npts >= 2) { double rr = h / h1; for (int i = g.rank; i < n; i += g.size) xp[i] = w.xn[i] + rr * (w.xn[i] - w.xm1[i]); }
       else copy(xp, w.xn);
@@ -493,43 +566,36 @@ struct Engine {
       double err = 0.0;
       if (npts >= 3) {
         double h2 = tn1 - tn2;
+        double rh = 1.0 / h, rh1 = 1.0 / h1, rh2 = 1.0 / h2;
+        double ra = 1.0 / (h + h1), rb = 1.0 / (h1 + h2), rc = 1.0 / (h + h1 + h2);
         double coef = h * h * (h + h1) * (h + h1) / (2.0 * h + h1);
-        double e = 0.0;
+        MaxRatio mr;
         for (int i = g.rank; i < n; i += g.size) {
           if (!T.is_node[i]) continue;
-          double d10 = (xp[i] - w.xn[i]) / h;
-          double d21 = (w.xn[i] - w.xm1[i]) / h1;
-          double d32 = (w.xm1[i] - w.xm2[i]) / h2;
-          double dd2a = (d10 - d21) / (h + h1);
-          double dd2b = (d21 - d32) / (h1 + h2);
-          double dd3 = (dd2a - dd2b) / (h + h1 + h2);
+          double d10 = (xp[i] - w.xn[i]) * rh;
+          double d21 = (w.xn[i] - w.xm1[i]) * rh1;
+          double d32 = (w.xm1[i] - w.xm2[i]) * rh2;
+          double dd3 = ((d10 - d21) * ra - (d21 - d32) * rb) * rc;
           double lte = fabs(dd3) * coef;
           double ax = fabs(xp[i]), bx = fabs(w.xn[i]);
-          double sc = o.reltol * (ax > bx ? ax : bx) + o.abstol_v;
-          double q = lte / sc;
-          if (!(q <= 1e300)) q = 1e30;
-          e = q > e ? q : e;
+          mr.add(lte, o.reltol * (ax > bx ? ax : bx) + o.abstol_v);
         }
-        err = g.max(e);
+        err = g.ratio(mr);
       } else if (npts == 2) {
-        double e = 0.0;
+        double rh = 1.0 / h, rh1 = 1.0 / h1, ra = 1.0 / (h + h1), hh = h * h;
+        MaxRatio mr;
         for (int i = g.rank; i < n; i += g.size) {
           if (!T.is_node[i]) continue;
-          double d10 = (xp[i] - w.xn[i]) / h;
-          double d21 = (w.xn[i] - w.xm1[i]) / h1;
-          double dd2 = (d10 - d21) / (h + h1);
-          double lte = fabs(dd2) * (h * h);
+          double dd2 = ((xp[i] - w.xn[i]) * rh - (w.xn[i] - w.xm1[i]) * rh1) * ra;
+          double lte = fabs(dd2) * hh;
           double ax = fabs(xp[i]), bx = fabs(w.xn[i]);
-          double sc = o.reltol * (ax > bx ? ax : bx) + o.abstol_v;
-          double q = lte / sc;
-          if (!(q <= 1e300)) q = 1e30;
-          e = q > e ? q : e;
+          mr.add(lte, o.reltol * (ax > bx ? ax : bx) + o.abstol_v);
         }
-        err = g.max(e);
+        err = g.ratio(mr);
       }
       if (err > 1.0) {
         st.rejected++;
-        hnext = h * quant_factor(0.9 * pow(err, -1.0 / 3.0));
+        hnext = h * step_factor(err);
         if (hnext < o.hmin) { st.status = CEDAR_ST_DT_UNDERFLOW; break; }
         continue;
       }
@@ -549,7 +615,7 @@ struct Engine {
       sink_point(sk, t, w.xn);
       if (nf) { st.status = CEDAR_ST_NAN; break; }
       if (npts < 3) ++npts;
-      double fac = (err > 0.0) ? quant_factor(0.9 * pow(err, -1.0 / 3.0)) : 1.0;
+      double fac = (err > 0.0) ? step_factor(err) : 1.0;
       hnext = h * fac;
       if (hit && t < o.tstop) { npts = 1; hnext = restart_h(t); }
     }

@@ -52,6 +52,8 @@ struct Slot {
   double t, tn1, tn2, h, h1, hnext, tnew, tprev, tprev2, cj;
   int npts; bool hit, have_prev, has_pert;
   Sink sk;
+  double ts_next;         // time of sample sk.next
+  double tb_cache;        // next source corner (see next_bp)
   double nrel, nav, nai;  // Newton tolerances
 
   // slot-level collectives (divergent phase: only this slot's lanes participate)
@@ -66,6 +68,19 @@ struct Slot {
 #pragma unroll
     for (int o = K / 2; o > 0; o >>= 1) { double u = __shfl_xor_sync(smask, v, o, K); v = u < v ? u : v; }
     return v;
+  }
+  __device__ double sratio(MaxRatio m) const {
+#pragma unroll
+    for (int o = K / 2; o > 0; o >>= 1) {
+      double n2 = __shfl_xor_sync(smask, m.num, o, K), d2 = __shfl_xor_sync(smask, m.den, o, K);
+      bool b2 = __shfl_xor_sync(smask, (int)m.bad, o, K) != 0;
+      m.merge(n2, d2, b2);
+    }
+    if (K > 1) {
+      m.num = __shfl_sync(smask, m.num, 0, K); m.den = __shfl_sync(smask, m.den, 0, K);
+      m.bad = __shfl_sync(smask, (int)m.bad, 0, K) != 0;
+    }
+    return m.value();
   }
   __device__ __forceinline__ void copy(double *d, const double *s) { for (int i = rank; i < T->n; i += K) d[i] = s[i]; }
   __device__ __forceinline__ void fill(double *d, double v) { for (int i = rank; i < T->n; i += K) d[i] = v; }
@@ -96,22 +111,31 @@ struct Slot {
     ssync();
   }
 
+  // Next source corner after tt.  The value found at an earlier time t0 <= tt stays
+  // the answer while tt + eps is below it (no corner lies in between), so it is
+  // recomputed only after the step lands on it.
   __device__ double next_bp(double tt, double eps) {
+    if (DADD(tt, eps) < tb_cache) return tb_cache;
     double best = 1e300;
     for (int s = rank; s < T->n_src; s += K) {
       double b = source_next_bp(dp + T->src_off[s], T->src_stride[s], tt, eps, T->pwl);
       best = b < best ? b : best;
     }
-    return smin(best);
+    tb_cache = smin(best);
+    return tb_cache;
   }
 
   __device__ void issue(double *x, const double *hist, const double *xref, double tt, double cjv, double src,
                         double gsh, double vlim, bool dc, int maxit, int next_rp) {
     jx = x; jhist = hist; jxref = xref; jt = tt; jcj = cjv; jsrc = src; jgs = gsh; jvlim = vlim; jdc = dc;
     jmaxit = maxit; jit = 0; jres = JOB_RUNNING; active = true; rp = next_rp;
+    // time-varying source values are fixed for the whole Newton solve
+    for (int s = rank; s < T->n_src; s += K)
+      w.srcv[s] = source_value(dp + T->src_off[s], T->src_stride[s], tt, dc, T->pwl) * src;
+    ssync();
   }
 
-  // ---- output sink (samples only)
+  // ---- output sink (samples only); ts_next caches the time of sample sk.next
   __device__ double sample_ts(int j) const {
     return j == sk.ns - 1 ? sk.tstop : sk.tstart + (sk.tstop - sk.tstart) * ((double)j / (double)(sk.ns - 1));
   }
@@ -119,11 +143,12 @@ struct Slot {
     if (!sk.samp) return;
     for (int p = rank; p < sk.np; p += K) { int u = sk.probes_int[p]; sk.samp[(long long)p * sk.ns] = u >= 0 ? x[u] : 0.0; }
     sk.next = 1;
+    ts_next = sk.ns > 1 ? sample_ts(1) : 1e300;
   }
   __device__ void sink_step(bool have0, double t0, const double *x0, double t1, const double *x1, double t2, const double *x2) {
     if (!sk.samp) return;
-    while (sk.next < sk.ns && sample_ts(sk.next) <= t2) {
-      double tt = sample_ts(sk.next);
+    while (sk.next < sk.ns && ts_next <= t2) {
+      double tt = ts_next;
       for (int p = rank; p < sk.np; p += K) {
         int u = sk.probes_int[p]; double v;
         if (u < 0) v = 0.0;
@@ -139,6 +164,7 @@ struct Slot {
         sk.samp[(long long)p * sk.ns + sk.next] = v;
       }
       sk.next++;
+      ts_next = sk.next < sk.ns ? sample_ts(sk.next) : 1e300;
     }
   }
 
@@ -167,10 +193,25 @@ struct Slot {
           job = K == 1 ? job : __shfl_sync(smask, job, 0, K);
           if (job >= b.n_inst) { rp = RP_IDLE; active = false; return; }
           inst = b.queue[job];
+          const int flags = b.rows ? b.rows[inst].flags : 0;
+          if (flags & ROW_FINISHED) continue;
           const int ti = b.inst_tpl[inst];
           T = &b.tpls[ti];
           dp = b.dpar + b.inst_dpar[inst];
-          w.bind(ws, T->n, T->nnz_lu, T->n_out);
+          w.bind(ws, T->n, T->nnz_lu, T->n_out, T->n_src);
+          tb_cache = -1e300;
+          if (rank == 0) atomicAdd(b.n_running, 1);
+          if (flags & ROW_STARTED) {
+            // resume a run stopped at a window boundary
+            sk = Sink{};
+            sk.probes_int = b.probes_int ? b.probes_int + (size_t)ti * b.np : nullptr;
+            sk.np = b.np; sk.ns = b.ns;
+            sk.samp = (b.samples && b.np > 0 && b.ns > 0) ? b.samples + (size_t)inst * b.np * b.ns : nullptr;
+            sk.tstart = o.tstart; sk.tstop = o.tstop;
+            load_row(b);
+            if (o.adaptive) goto ada_begin;
+            goto fix_issue;
+          }
           const long long xo = b.x0_off ? b.x0_off[inst] : -1;
           for (int i = rank; i < T->n; i += K) w.x[i] = xo >= 0 ? b.x0[xo + T->order[i]] : 0.0;
           const long long dxo = b.dx_off ? b.dx_off[inst] : -1;
@@ -182,7 +223,7 @@ struct Slot {
           sk.samp = (b.samples && b.np > 0 && b.ns > 0) ? b.samples + (size_t)inst * b.np * b.ns : nullptr;
           sk.tstart = o.tstart; sk.tstop = o.tstop;
           st.accepted = st.rejected = st.newton_iters = st.dc_iters = 0;
-          st.hmin_seen = 1e300; st.hmax_seen = 0; st.status = CEDAR_ST_OK;
+          st.hmin_seen = 1e300; st.hmax_seen = 0; st.status = CEDAR_ST_OK; st.pad = 0;
           ssync();
           if (o.dcop) {
             copy(w.x0, w.x);
@@ -262,43 +303,36 @@ struct Slot {
           double err = 0.0;
           if (npts >= 3) {
             double h2 = tn1 - tn2;
+            double rh = 1.0 / h, rh1 = 1.0 / h1, rh2 = 1.0 / h2;
+            double ra = 1.0 / (h + h1), rb = 1.0 / (h1 + h2), rc = 1.0 / (h + h1 + h2);
             double coef = h * h * (h + h1) * (h + h1) / (2.0 * h + h1);
-            double e = 0.0;
+            MaxRatio mr;
             for (int i = rank; i < n; i += K) {
               if (!T->is_node[i]) continue;
-              double d10 = (xp[i] - w.xn[i]) / h;
-              double d21 = (w.xn[i] - w.xm1[i]) / h1;
-              double d32 = (w.xm1[i] - w.xm2[i]) / h2;
-              double dd2a = (d10 - d21) / (h + h1);
-              double dd2b = (d21 - d32) / (h1 + h2);
-              double dd3 = (dd2a - dd2b) / (h + h1 + h2);
+              double d10 = (xp[i] - w.xn[i]) * rh;
+              double d21 = (w.xn[i] - w.xm1[i]) * rh1;
+              double d32 = (w.xm1[i] - w.xm2[i]) * rh2;
+              double dd3 = ((d10 - d21) * ra - (d21 - d32) * rb) * rc;
               double lte = fabs(dd3) * coef;
               double ax = fabs(xp[i]), bx = fabs(w.xn[i]);
-              double sc = o.reltol * (ax > bx ? ax : bx) + o.abstol_v;
-              double q = lte / sc;
-              if (!(q <= 1e300)) q = 1e30;
-              e = q > e ? q : e;
+              mr.add(lte, o.reltol * (ax > bx ? ax : bx) + o.abstol_v);
             }
-            err = smax(e);
+            err = sratio(mr);
           } else if (npts == 2) {
-            double e = 0.0;
+            double rh = 1.0 / h, rh1 = 1.0 / h1, ra = 1.0 / (h + h1), hh = h * h;
+            MaxRatio mr;
             for (int i = rank; i < n; i += K) {
               if (!T->is_node[i]) continue;
-              double d10 = (xp[i] - w.xn[i]) / h;
-              double d21 = (w.xn[i] - w.xm1[i]) / h1;
-              double dd2 = (d10 - d21) / (h + h1);
-              double lte = fabs(dd2) * (h * h);
+              double dd2 = ((xp[i] - w.xn[i]) * rh - (w.xn[i] - w.xm1[i]) * rh1) * ra;
+              double lte = fabs(dd2) * hh;
               double ax = fabs(xp[i]), bx = fabs(w.xn[i]);
-              double sc = o.reltol * (ax > bx ? ax : bx) + o.abstol_v;
-              double q = lte / sc;
-              if (!(q <= 1e300)) q = 1e30;
-              e = q > e ? q : e;
+              mr.add(lte, o.reltol * (ax > bx ? ax : bx) + o.abstol_v);
             }
-            err = smax(e);
+            err = sratio(mr);
           }
           if (err > 1.0) {
             st.rejected++;
-            hnext = h * quant_factor(0.9 * pow(err, -1.0 / 3.0));
+            hnext = h * step_factor(err);
             if (hnext < o.hmin) { st.status = CEDAR_ST_DT_UNDERFLOW; goto ada_end; }
             goto ada_begin;
           }
@@ -317,7 +351,7 @@ struct Slot {
           st.accepted++; st.hmin_seen = h < st.hmin_seen ? h : st.hmin_seen; st.hmax_seen = h > st.hmax_seen ? h : st.hmax_seen;
           if (nf) { st.status = CEDAR_ST_NAN; goto ada_end; }
           if (npts < 3) ++npts;
-          double fac = (err > 0.0) ? quant_factor(0.9 * pow(err, -1.0 / 3.0)) : 1.0;
+          double fac = (err > 0.0) ? step_factor(err) : 1.0;
           hnext = h * fac;
           if (hit && t < o.tstop) { npts = 1; hnext = restart_h(t, o); }
           goto ada_begin;
@@ -363,6 +397,7 @@ struct Slot {
       copy(w.xn, w.x);
       ssync();
       sink_start(w.x);
+      if (rank == 0 && b.rows) b.rows[inst].flags = ROW_STARTED;
       if (!o.adaptive) {
         fill(w.qd, 0.0);
         ssync();
@@ -376,6 +411,7 @@ struct Slot {
       goto ada_begin;
     fix_issue: {
       if (k > N) goto retire;
+      if (tprev >= b.t_until) { save_row(b); rp = RP_NEWINST; continue; }
       t = (k == N) ? o.tstop : DADD(o.tstart, DMUL((double)k, o.h));
       double hk = t - tprev;
       if (o.method == CEDAR_TRAP) {
@@ -383,10 +419,11 @@ struct Slot {
         for (int i = rank; i < T->n; i += K) w.hist[i] = -cj * w.qn[i] - w.qd[i];
       } else if (k == 1) {
         cj = 1.0 / hk;
-        for (int i = rank; i < T->n; i += K) w.hist[i] = -w.qn[i] / hk;
+        for (int i = rank; i < T->n; i += K) w.hist[i] = -w.qn[i] * cj;
       } else {
         cj = 1.5 / hk;
-        for (int i = rank; i < T->n; i += K) w.hist[i] = (-4.0 * w.qn[i] + w.qm1[i]) / (2.0 * hk);
+        const double r2h = 0.5 / hk;
+        for (int i = rank; i < T->n; i += K) w.hist[i] = (-4.0 * w.qn[i] + w.qm1[i]) * r2h;
       }
       if (k == 1) copy(w.x, w.xn);
       else for (int i = rank; i < T->n; i += K) w.x[i] = 2.0 * w.xn[i] - w.xm1[i];
@@ -396,6 +433,7 @@ struct Slot {
     }
     ada_begin: {
       if (!(t < o.tstop)) goto ada_end;
+      if (t >= b.t_until) { save_row(b); rp = RP_NEWINST; continue; }
       if (++nsteps > o.max_steps) { st.status = CEDAR_ST_MAX_STEPS; goto ada_end; }
       const double eps_bp = (o.tstop - o.tstart) * 1e-12;
       double tb = next_bp(t, eps_bp); tb = tb < o.tstop ? tb : o.tstop;
@@ -407,12 +445,12 @@ struct Slot {
       h1 = t - tn1;
       if (npts < 2) {
         cj = 1.0 / h;
-        for (int i = rank; i < T->n; i += K) w.hist[i] = -w.qn[i] / h;
+        for (int i = rank; i < T->n; i += K) w.hist[i] = -w.qn[i] * cj;
       } else {
-        double wr = h / h1;
+        double wr = h / h1, rh = 1.0 / h;
         cj = (1.0 + 2.0 * wr) / ((1.0 + wr) * h);
         double a1 = -(1.0 + wr), a2 = wr * wr / (1.0 + wr);
-        for (int i = rank; i < T->n; i += K) w.hist[i] = (a1 * w.qn[i] + a2 * w.qm1[i]) / h;
+        for (int i = rank; i < T->n; i += K) w.hist[i] = (a1 * w.qn[i] + a2 * w.qm1[i]) * rh;
       }
       if (npts >= 2) { double rr = h / h1; for (int i = rank; i < T->n; i += K) w.x[i] = w.xn[i] + rr * (w.xn[i] - w.xm1[i]); }
       else copy(w.x, w.xn);
@@ -432,9 +470,44 @@ struct Slot {
       if (b.x_final)
         for (int i = rank; i < T->n; i += K) b.x_final[(size_t)inst * b.n_max + T->order[i]] = w.x[i];
       if (rank == 0 && b.stats) b.stats[inst] = st;
+      if (rank == 0 && b.rows) b.rows[inst].flags = ROW_STARTED | ROW_FINISHED;
+      if (rank == 0) atomicSub(b.n_running, 1);
       ssync();
       rp = RP_NEWINST;
     }
+  }
+
+  // ---- window boundaries: integrator state to / from the instance's state row
+  __device__ void save_row(const BatchDev &b) {
+    double *v = b.row_vec + (size_t)inst * 6 * b.n_max;
+    const int n = T->n;
+    for (int i = rank; i < n; i += K) {
+      v[i] = w.xn[i]; v[b.n_max + i] = w.xm1[i]; v[2 * b.n_max + i] = w.xm2[i];
+      v[3 * b.n_max + i] = w.qn[i]; v[4 * b.n_max + i] = w.qm1[i]; v[5 * b.n_max + i] = w.qd[i];
+    }
+    if (rank == 0) {
+      StateRow &r = b.rows[inst];
+      r.t = t; r.tn1 = tn1; r.tn2 = tn2; r.hnext = hnext; r.tprev = tprev; r.tprev2 = tprev2;
+      r.k = k; r.nsteps = nsteps; r.st = st; r.npts = npts; r.have_prev = have_prev ? 1 : 0;
+      r.next_sample = sk.next; r.flags = ROW_STARTED;
+      if (b.stats) b.stats[inst] = st;
+    }
+    ssync();
+  }
+  __device__ void load_row(const BatchDev &b) {
+    const double *v = b.row_vec + (size_t)inst * 6 * b.n_max;
+    const int n = T->n;
+    for (int i = rank; i < n; i += K) {
+      w.xn[i] = v[i]; w.xm1[i] = v[b.n_max + i]; w.xm2[i] = v[2 * b.n_max + i];
+      w.qn[i] = v[3 * b.n_max + i]; w.qm1[i] = v[4 * b.n_max + i]; w.qd[i] = v[5 * b.n_max + i];
+    }
+    const StateRow &r = b.rows[inst];
+    t = r.t; tn1 = r.tn1; tn2 = r.tn2; hnext = r.hnext; tprev = r.tprev; tprev2 = r.tprev2;
+    k = r.k; nsteps = r.nsteps; st = r.st; npts = r.npts; have_prev = r.have_prev != 0;
+    sk.next = r.next_sample;
+    ts_next = (sk.samp && sk.next < sk.ns) ? sample_ts(sk.next) : 1e300;
+    N = llround((b.opts.tstop - b.opts.tstart) / b.opts.h);
+    ssync();
   }
 };
 
@@ -460,7 +533,10 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am) {
       const int *tm = T.term + gr.term_off + i * gr.ntx;
       double v[5];
       for (int kk = 0; kk < gr.ntx; ++kk) { int u = tm[kk]; v[kk] = u < 0 ? 0.0 : x[u]; }
-      eval_device(gr.model, s.dp + gr.dpar_off + i, gr.n_inst, v, nullptr, ctx, T.pwl, s.w.dout + gr.out_off + i * model_nout(gr.model));
+      double *out = s.w.dout + gr.out_off + i * model_nout(gr.model);
+      const int si = (gr.model == CEDAR_V || gr.model == CEDAR_I) ? T.src_of_dev[d] : -1;
+      if (si >= 0) eval_source_value(gr.model, s.dp + gr.dpar_off + i, v, s.w.srcv[si], out);
+      else eval_device(gr.model, s.dp + gr.dpar_off + i, gr.n_inst, v, nullptr, ctx, T.pwl, out);
     }
   }
   __syncwarp(am);
@@ -489,8 +565,8 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am) {
         int kind = info & 3, j = info >> 2;
         if (kind == 2) acc *= s.w.rd[j];
         else if (kind == 1) {
-          if (!(fabs(acc) > 1e-300) || !(fabs(acc) < 1e300)) bad = true;
-          s.w.rd[j] = 1.0 / acc;
+          if (!pivot_ok(acc)) bad = true;
+          s.w.rd[j] = pivot_rcp(acc);
         }
         s.w.lu[q] = acc;
       }
@@ -524,19 +600,25 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am) {
     __syncwarp(am);
   }
   // K6: finiteness, DC damping, update, convergence vote
-  bool nonfinite = false; double mx = 0.0;
+  // magnitudes are compared as integers (the bit patterns of non-negative doubles
+  // order like the values), keeping these tests off the FP64 pipe
+  bool nonfinite = false; long long mxb = 0;
+  const bool damp = s.jvlim > 0;
   if (!slot_bad) {
     for (int i = rank; i < T.n; i += K) {
-      double d = b[i];
-      if (!(fabs(d) < 1e300)) nonfinite = true;
-      if (T.is_node[i]) { double a = fabs(d); mx = a > mx ? a : mx; }
+      long long ab = abs_bits(b[i]);
+      if (ab >= 0x7e37e43c8800759cLL) nonfinite = true;  // |d| >= 1e300 or NaN
+      if (damp && T.is_node[i]) mxb = ab > mxb ? ab : mxb;
     }
   }
   const bool slot_nf = (__ballot_sync(am, nonfinite) & s.smask) != 0;
-#pragma unroll
-  for (int o = K / 2; o > 0; o >>= 1) { double u = __shfl_xor_sync(am, mx, o, K); mx = u > mx ? u : mx; }
   double scale = 1.0;
-  if (s.jvlim > 0 && mx > s.jvlim) scale = s.jvlim / mx;
+  if (__any_sync(am, damp)) {
+#pragma unroll
+    for (int o = K / 2; o > 0; o >>= 1) { long long u = __shfl_xor_sync(am, mxb, o, K); mxb = u > mxb ? u : mxb; }
+    const double mx = __longlong_as_double(mxb);
+    if (damp && mx > s.jvlim) scale = s.jvlim / mx;
+  }
   bool conv = (scale == 1.0);
   if (!slot_bad && !slot_nf) {
     for (int i = rank; i < T.n; i += K) {
@@ -544,7 +626,7 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am) {
       double xi = s.jx[i] + d;
       s.jx[i] = xi;
       double lim = s.nrel * fabs(xi) + (T.is_node[i] ? s.nav : s.nai);
-      if (!(fabs(d) <= lim)) conv = false;
+      if (abs_bits(d) > abs_bits(lim)) conv = false;
     }
   }
   const bool slot_notconv = (__ballot_sync(am, !conv) & s.smask) != 0;

@@ -86,7 +86,7 @@ cudaError_t launch_eval(const DTpl &T, const DTpl *T_dev, const double *dpar, co
 __global__ void plain_kernel(PlainArgs a) {
   extern __shared__ double smem[];
   double *red = smem;
-  double *ws = a.ws_global ? a.ws_global : smem + 64;
+  double *ws = a.ws_global ? a.ws_global : smem + 128;
   const DTpl &T = *a.T;
   BlockGroup g(red);
   Engine<BlockGroup> E(T, a.dpar, ws, g);
@@ -120,7 +120,7 @@ __global__ void plain_kernel(PlainArgs a) {
 }
 
 cudaError_t launch_plain(const PlainArgs &a, int wsd, int threads, cudaStream_t s) {
-  size_t smem = 64 * sizeof(double);
+  size_t smem = 128 * sizeof(double);
   if (!a.ws_global) smem += (size_t)wsd * sizeof(double);
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(plain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -25,7 +25,22 @@ struct BatchDev {
   int ws_stride;                 // doubles per group workspace
   double *ws_global;             // global workspaces when not in shared memory
   int ws_in_smem;
+  // resumable runs: every instance stops at its first step starting at or after
+  // t_until (a soft stop: the step sequence is the one of an uninterrupted run),
+  // leaving its integrator state in rows / row_vec for the next launch
+  double t_until;
+  struct StateRow *rows;         // [n_inst]
+  double *row_vec;               // [n_inst * 6 * n_max]: xn xm1 xm2 qn qm1 qd
+  int *n_running;                // instances left unfinished by this launch
 };
+
+struct StateRow {
+  double t, tn1, tn2, hnext, tprev, tprev2;
+  long long k, nsteps;
+  EngStats st;
+  int npts, have_prev, next_sample, flags;  // flags: 1 started, 2 finished
+};
+constexpr int ROW_STARTED = 1, ROW_FINISHED = 2;
 
 // derive params for instances [0, n_inst): raw blocks -> dpar blocks
 cudaError_t launch_derive(const DTpl *tpls_dev, const int *inst_tpl, const long long *raw_off, const double *raw,

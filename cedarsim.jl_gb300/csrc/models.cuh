@@ -131,6 +131,14 @@ struct EvalCtx {
   bool xdot;    // F part of charges = C * xdot (cedar_eval) instead of cj * Q (Newton)
 };
 
+// V / I source outputs given the source value vs (already scaled); same layout
+// as eval_device.  Used when vs is cached once per Newton solve.
+CEDAR_HD void eval_source_value(int model, const double *dp, const double *v, double vs, double *out) {
+  double m = dp[0];
+  if (model == CEDAR_V) { out[0] = m * v[2]; out[1] = (v[0] - v[1]) - vs; out[2] = m; out[3] = 1.0; }
+  else out[0] = m * vs;
+}
+
 // level-1 forward-mode current and partials (vds >= 0)
 CEDAR_HD void mos1_fwd(double vgs, double vds, double vth, double beta, double lam,
                        double &id, double &gm, double &gds) {

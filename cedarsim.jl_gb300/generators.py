@@ -148,6 +148,85 @@ def mc_chains(n_inst: int = 4096, seed: int = 20240607, workload: int = 3,
     return templates, lsel.astype(np.int32), np.concatenate(blocks), offs
 
 
+# ---------------------------------------------------------------- workload 4
+RING = dict(stages=15, vdd=1.8, vbn=1.0, vbp=0.8, rsup=100.0, csup=100e-15, cload=5e-15)
+
+
+def ring_oscillator(stages: int = RING["stages"], diode_is=None, diode_n=None, **kw) -> Circuit:
+    """Current-starved ring oscillator.  Stage k (input out_{k-1}, out_0 = out_N):
+    MP_starve (ps_k <- vbp, source vdd_k), MP (out_k <- out_{k-1}, source ps_k),
+    MN (out_k <- out_{k-1}, source ns_k), MN_starve (ns_k <- vbn, source 0),
+    100 Ohm from VDD to vdd_k with 100 fF to ground, a Verilog-A exponential diode
+    out_k -> vdd_k, and a 5 fF load on out_k (level-1 MOSFETs carry no charge, so
+    the load is what gives each stage its delay)."""
+    p = dict(INV, **RING)
+    p.update(kw)
+    ckt = Circuit()
+    for nm in ("vdd", "vbn", "vbp"):
+        ckt.node(nm)
+    ckt.V("VDD", "vdd", "0", dc=p["vdd"])
+    ckt.V("VBN", "vbn", "0", dc=p["vbn"])
+    ckt.V("VBP", "vbp", "0", dc=p["vbp"])
+    for k in range(1, stages + 1):
+        inp = f"out{stages if k == 1 else k - 1}"
+        out, vk, ps, ns = f"out{k}", f"vdd{k}", f"ps{k}", f"ns{k}"
+        ckt.R(f"RS{k}", "vdd", vk, r=p["rsup"])
+        ckt.C(f"CS{k}", vk, "0", p["csup"])
+        ckt.mos1(f"MPS{k}", ps, "vbp", vk, vk, -1.0, p["wp"], p["lp"], p["kp_p"], p["vth_p"])
+        ckt.mos1(f"MP{k}", out, inp, ps, vk, -1.0, p["wp"], p["lp"], p["kp_p"], p["vth_p"])
+        ckt.mos1(f"MN{k}", out, inp, ns, "0", 1.0, p["wn"], p["ln"], p["kp_n"], p["vth_n"])
+        ckt.mos1(f"MNS{k}", ns, "vbn", "0", "0", 1.0, p["wn"], p["ln"], p["kp_n"], p["vth_n"])
+        isv = 1e-15 if diode_is is None else diode_is[k - 1]
+        nv = 1.1 if diode_n is None else diode_n[k - 1]
+        ckt.diode(f"D{k}", out, vk, IS=isv, N=nv)
+        ckt.C(f"CL{k}", out, "0", p["cload"])
+    return ckt
+
+
+def mc_rings(n_inst: int = 1024, seed: int = 20240607, workload: int = 4):
+    """Ring-oscillator sweep: per instance Is ~ loguniform(1e-16, 1e-14) A and
+    n ~ U(1.0, 1.2) per diode; DC operating point perturbed by N(0, 1 mV) on every
+    node.  Returns (template, inst_template, inst_par, inst_par_off, inst_dx, inst_dx_off).
+    Draws: diode j Is -> stream(i, 1 + j, 0) uniform; n -> stream(i, 1 + j, 1);
+           node u perturbation -> stream(i, 1000 + u, 0) normal."""
+    from .circuit import DIODE as MODEL_D
+    st = Stream(seed, workload)
+    flat = ring_oscillator().flatten()
+    base = flat.param_block()
+    blocks, offs = [], np.zeros(n_inst, np.int64)
+    dxs, dx_off = [], np.zeros(n_inst, np.int64)
+    for i in range(n_inst):
+        blk = base.copy()
+        off_m = 0
+        for (model, term, br, par) in flat.groups:
+            npar, ninst = par.shape
+            if model == MODEL_D:
+                j = np.arange(ninst)
+                u1 = st.uniform(i, 1 + j, 0)
+                u2 = st.uniform(i, 1 + j, 1)
+                blk[off_m: off_m + ninst] = 10.0 ** (-16.0 + 2.0 * u1)          # IS
+                blk[off_m + ninst: off_m + 2 * ninst] = 1.0 + 0.2 * u2          # N
+            off_m += npar * ninst
+        offs[i] = i * base.size
+        blocks.append(blk)
+        dx = np.zeros(flat.n)
+        u = np.arange(flat.n_nodes)
+        dx[:flat.n_nodes] = 1e-3 * st.normal(i, 1000 + u, 0)
+        dx_off[i] = i * flat.n
+        dxs.append(dx)
+    return [flat], np.zeros(n_inst, np.int32), np.concatenate(blocks), offs, np.concatenate(dxs), dx_off
+
+
+def instance_flat(template: Flat, block: np.ndarray) -> Flat:
+    """The template with one instance's parameter block substituted (a stand-alone circuit)."""
+    groups, p = [], 0
+    for (model, term, br, par) in template.groups:
+        groups.append((model, term, br, np.ascontiguousarray(block[p:p + par.size].reshape(par.shape))))
+        p += par.size
+    return Flat(template.n_nodes, template.n_branch, groups, template.pwl, template.temp_c, template.gmin,
+                template.names, template.devices, template.ordering)
+
+
 def chain_output_probe(flat: Flat) -> int:
     """Unknown index of the last stage output of a chain template."""
     outs = [k for k, nm in enumerate(flat.names) if nm.startswith("out")]

@@ -120,7 +120,14 @@ typedef struct cedar_ckt_desc {
   int64_t n_pwl;          /* doubles in pwl                                     */
   double temp_c;          /* simulation temperature [C] (SimSpec.temp = 27)     */
   double gmin;            /* junction/channel gmin (SimSpec.gmin = 1e-12)       */
+  int32_t ordering;       /* CEDAR_ORDER_AUTO (0), _MIN_DEGREE or _NESTED_DISSECTION */
+  int32_t reserved;
 } cedar_ckt_desc;
+
+/* Fill-reducing ordering of the static-pivot LU.  AUTO computes both and keeps
+ * the one whose level-scheduled factorisation + substitutions have the shorter
+ * estimated critical path (ties: minimum degree). */
+enum { CEDAR_ORDER_AUTO = 0, CEDAR_ORDER_MIN_DEGREE = 1, CEDAR_ORDER_NESTED_DISSECTION = 2 };
 
 /* Terminal and parameter counts per model (index by model id). */
 int cedar_model_nterm(int model);
@@ -177,6 +184,22 @@ int cedar_plan_create(const cedar_ckt_desc *desc, cedar_ckt **out);
 int cedar_ckt_destroy(cedar_ckt *ckt);
 int cedar_ckt_size(const cedar_ckt *ckt, int32_t *n, int32_t *nnz_j, int32_t *nnz_lu,
                    int32_t *n_levels);
+
+/* Algorithmic work of one Newton iteration of this circuit (for roofline
+ * accounting): FP64 operations by phase (an FMA counts 2, a reciprocal 1) and the
+ * bytes an iteration must move when nothing stays on chip. */
+typedef struct cedar_costs {
+  int64_t flops_eval;    /* device evaluation                                   */
+  int64_t flops_stamp;   /* J slot and residual-row sums                        */
+  int64_t flops_lu;      /* numeric refactorisation                             */
+  int64_t flops_solve;   /* forward + backward substitution                     */
+  int64_t flops_update;  /* Newton update and convergence test                  */
+  int64_t bytes;         /* params + terminals + outputs + J/LU + vectors       */
+  int32_t lu_levels, fw_levels, bw_levels, nnz_lu;
+  int32_t ordering;      /* CEDAR_ORDER_* actually used                         */
+  int32_t pad;
+} cedar_costs;
+int cedar_ckt_costs(const cedar_ckt *ckt, cedar_costs *out);
 
 /* J pattern in compressed-sparse-column form over the ORIGINAL unknown order:
  * colptr[n+1], rowidx[nnz_j].  Jvals returned by cedar_eval follow this order. */
@@ -254,6 +277,16 @@ int cedar_batch_destroy(cedar_batch *b);
  *   stats[n_inst]            per-instance counters and status (may be NULL) */
 int cedar_batch_run(cedar_batch *b, const cedar_tran_opts *opts, double *x_final,
                     double *samples, cedar_stats *stats);
+/* Windowed form of cedar_batch_run: start a run (DC operating points happen in
+ * the first advance), advance every unfinished instance to its first step that
+ * starts at or after t_until (a soft stop that leaves the step sequence of an
+ * uninterrupted run unchanged; integrator state stays on the device), then read
+ * the results.  n_running receives the number of instances still unfinished. */
+int cedar_batch_start(cedar_batch *b, const cedar_tran_opts *opts);
+int cedar_batch_advance(cedar_batch *b, double t_until, int32_t *n_running);
+int cedar_batch_results(cedar_batch *b, double *x_final, double *samples, cedar_stats *stats);
+/* Device time of the last batch launch (CUDA events on the handle's stream). */
+int cedar_batch_last_ms(cedar_batch *b, double *ms);
 int cedar_batch_set_tuning(cedar_batch *b, const cedar_batch_tuning *t);
 int cedar_batch_get_tuning(const cedar_batch *b, cedar_batch_tuning *t);
 /* Autotune: time each candidate tile shape on a short horizon and keep the best. */

@@ -512,12 +512,28 @@ struct Sink {
   }
 };
 
-static double quant_factor(double f) {
-  // step-size factors are rounded down to multiples of 1/8 so that CPU and GPU
-  // (whose pow/rounding may differ in the last ulp) pick identical steps
-  double q = std::floor(f * 8.0) / 8.0;
-  return std::max(0.125, std::min(2.0, q));
+// Step-size factor: the largest k/8 (k = 1..16) with k/8 <= 0.9 err^(-1/3), i.e.
+// (k/8)^3 err <= 0.729; (k/8)^3 = k^3/512 is exact.  Quantising the factor makes
+// CPU and GPU (whose last-ulp rounding may differ) pick identical steps.
+static double step_factor(double err) {
+  auto c = [](int k) { return (double)(k * k * k) / 512.0; };
+  if (c(16) * err <= 0.729) return 2.0;
+  if (!(c(1) * err <= 0.729)) return 0.125;
+  int lo = 1, hi = 16;
+  while (hi - lo > 1) { int mid = (lo + hi) / 2; if (c(mid) * err <= 0.729) lo = mid; else hi = mid; }
+  return lo / 8.0;
 }
+
+// Largest ratio lte/sc over unknowns, tracked as a fraction (num/den) compared by
+// cross-multiplication so that one division per step suffices.
+struct MaxRatio {
+  double num = 0.0, den = 1.0; bool bad = false;
+  void add(double lte, double sc) {
+    if (!(lte <= 1e300) || !(sc > 0.0)) { bad = true; return; }
+    if (lte * den > num * sc) { num = lte; den = sc; }
+  }
+  double value() const { return bad ? 1e30 : num / den; }
+};
 
 static int tran(const Circuit &c, const cedar_tran_opts *opts_in, double *x, Sink &sink, cedar_stats &st,
                 const double *perturb) {
@@ -552,10 +568,11 @@ static int tran(const Circuit &c, const cedar_tran_opts *opts_in, double *x, Sin
         for (int i = 0; i < n; ++i) hist[i] = -cj * qn[i] - qd[i];
       } else if (k == 1) {
         cj = 1.0 / hk;
-        for (int i = 0; i < n; ++i) hist[i] = -qn[i] / hk;
+        for (int i = 0; i < n; ++i) hist[i] = -qn[i] * cj;
       } else {
         cj = 1.5 / hk;
-        for (int i = 0; i < n; ++i) hist[i] = (-4.0 * qn[i] + qm1[i]) / (2.0 * hk);
+        double r2h = 0.5 / hk;
+        for (int i = 0; i < n; ++i) hist[i] = (-4.0 * qn[i] + qm1[i]) * r2h;
       }
       if (k == 1) std::copy(xn.begin(), xn.end(), xp.begin());
       else for (int i = 0; i < n; ++i) xp[i] = 2.0 * xn[i] - xm1[i];
@@ -603,12 +620,12 @@ static int tran(const Circuit &c, const cedar_tran_opts *opts_in, double *x, Sin
     double cj, h1 = t - tn1;
     if (order == 1) {
       cj = 1.0 / h;
-      for (int i = 0; i < n; ++i) hist[i] = -qn[i] / h;
+      for (int i = 0; i < n; ++i) hist[i] = -qn[i] * cj;
     } else {
-      double wr = h / h1;
+      double wr = h / h1, rh = 1.0 / h;
       cj = (1.0 + 2.0 * wr) / ((1.0 + wr) * h);
       double a1 = -(1.0 + wr), a2 = wr * wr / (1.0 + wr);
-      for (int i = 0; i < n; ++i) hist[i] = (a1 * qn[i] + a2 * qm1[i]) / h;
+      for (int i = 0; i < n; ++i) hist[i] = (a1 * qn[i] + a2 * qm1[i]) * rh;
     }
     if (npts >= 2) { double r = h / h1; for (int i = 0; i < n; ++i) xp[i] = xn[i] + r * (xn[i] - xm1[i]); }
     else std::copy(xn.begin(), xn.end(), xp.begin());
@@ -623,40 +640,40 @@ static int tran(const Circuit &c, const cedar_tran_opts *opts_in, double *x, Sin
     }
     double err = 0.0;
     if (npts >= 3) {
+      // third divided difference over (tnew, t, tn1, tn2); the BDF2 local error is
+      // x^(3) h^2 (h+h1)^2 / (6 (2h+h1)) with x^(3) ~ 6 dd3
       double h2 = tn1 - tn2;
-      // third divided difference over (tnew, t, tn1, tn2)
+      double rh = 1.0 / h, rh1 = 1.0 / h1, rh2 = 1.0 / h2;
+      double ra = 1.0 / (h + h1), rb = 1.0 / (h1 + h2), rc = 1.0 / (h + h1 + h2);
       double coef = h * h * (h + h1) * (h + h1) / (2.0 * h + h1);
+      MaxRatio mr;
       for (int i = 0; i < nn; ++i) {
-        double d10 = (xp[i] - xn[i]) / h;
-        double d21 = (xn[i] - xm1[i]) / h1;
-        double d32 = (xm1[i] - xm2[i]) / h2;
-        double dd2a = (d10 - d21) / (h + h1);
-        double dd2b = (d21 - d32) / (h1 + h2);
-        double dd3 = (dd2a - dd2b) / (h + h1 + h2);
+        double d10 = (xp[i] - xn[i]) * rh;
+        double d21 = (xn[i] - xm1[i]) * rh1;
+        double d32 = (xm1[i] - xm2[i]) * rh2;
+        double dd3 = ((d10 - d21) * ra - (d21 - d32) * rb) * rc;
         double lte = std::fabs(dd3) * coef;
         double sc = o.reltol * std::max(std::fabs(xp[i]), std::fabs(xn[i])) + o.abstol_v;
-        double q = lte / sc;
-        if (!(q <= 1e300)) q = 1e30;
-        err = std::max(err, q);
+        mr.add(lte, sc);
       }
+      err = mr.value();
     } else if (npts == 2) {
       // second step after a (re)start: backward-Euler-type bound h^2 |x''| / 2 with
       // x'' ~ 2 * second divided difference over (tnew, t, tn1)
+      double rh = 1.0 / h, rh1 = 1.0 / h1, ra = 1.0 / (h + h1), hh = h * h;
+      MaxRatio mr;
       for (int i = 0; i < nn; ++i) {
-        double d10 = (xp[i] - xn[i]) / h;
-        double d21 = (xn[i] - xm1[i]) / h1;
-        double dd2 = (d10 - d21) / (h + h1);
-        double lte = std::fabs(dd2) * (h * h);
+        double dd2 = ((xp[i] - xn[i]) * rh - (xn[i] - xm1[i]) * rh1) * ra;
+        double lte = std::fabs(dd2) * hh;
         double sc = o.reltol * std::max(std::fabs(xp[i]), std::fabs(xn[i])) + o.abstol_v;
-        double q = lte / sc;
-        if (!(q <= 1e300)) q = 1e30;
-        err = std::max(err, q);
+        mr.add(lte, sc);
       }
+      err = mr.value();
     }
     if (!std::isfinite(err)) err = 1e30;
     if (err > 1.0) {
       st.rejected++;
-      hnext = h * quant_factor(0.9 * std::pow(err, -1.0 / 3.0));
+      hnext = h * step_factor(err);
       if (hnext < o.hmin) { st.status = CEDAR_ST_DT_UNDERFLOW; break; }
       continue;
     }
@@ -671,7 +688,7 @@ static int tran(const Circuit &c, const cedar_tran_opts *opts_in, double *x, Sin
     bool finite = true; for (int i = 0; i < n; ++i) if (!std::isfinite(xn[i])) finite = false;
     if (!finite) { st.status = CEDAR_ST_NAN; break; }
     if (npts < 3) ++npts;
-    double fac = (err > 0.0) ? quant_factor(0.9 * std::pow(err, -1.0 / 3.0)) : 1.0;
+    double fac = (err > 0.0) ? step_factor(err) : 1.0;
     hnext = h * fac;
     if (hit && t < o.tstop) { npts = 1; hnext = restart_h(t); }
   }

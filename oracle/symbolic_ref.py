@@ -148,3 +148,87 @@ def analyze(flat):
     lu = {(p, q) for p in range(n) for q in rows[p]}
     lcp, lri = csc(lu, n)
     return colptr, rowidx, rm, order, lcp, lri
+
+
+def nested_dissection(adj: List[Set[int]]) -> List[int]:
+    """Level-structure nested dissection (George 1973): dense vertices last; split
+    each component at the middle BFS level from a pseudo-peripheral vertex."""
+    import math
+    n = len(adj)
+    thresh = max(16, int(4.0 * math.sqrt(n)))
+    dense = [len(adj[v]) > thresh for v in range(n)]
+    order: List[int] = []
+
+    def bfs(root, member):
+        levels, cur, seen = [], [root], {root}
+        while cur:
+            cur = sorted(cur)
+            levels.append(cur)
+            nxt = []
+            for v in cur:
+                for w in sorted(adj[v]):
+                    if w in member and w not in seen:
+                        seen.add(w); nxt.append(w)
+            cur = nxt
+        return levels
+
+    def nd(V):
+        V = sorted(V)
+        member = set(V)
+        comps, seen = [], set()
+        for v in V:
+            if v in seen:
+                continue
+            comp, k = [v], 0
+            seen.add(v)
+            while k < len(comp):
+                for w in sorted(adj[comp[k]]):
+                    if w in member and w not in seen:
+                        seen.add(w); comp.append(w)
+                k += 1
+            comps.append(sorted(comp))
+        if len(comps) > 1:
+            for c in comps:
+                nd(c)
+            return
+        C = comps[0]
+        if len(C) <= 3:
+            order.extend(C)
+            return
+        member = set(C)
+        deg = lambda v: sum(1 for w in adj[v] if w in member)
+        levels = bfs(C[0], member)
+        for _ in range(5):
+            u = min(levels[-1], key=lambda v: (deg(v), v))
+            lv2 = bfs(u, member)
+            if len(lv2) > len(levels):
+                levels = lv2
+            else:
+                break
+        m = len(levels) - 1
+        if m < 2:
+            order.extend(C)
+            return
+        S = levels[m // 2]
+        nd([v for v in C if v not in set(S)])
+        order.extend(S)
+
+    V = [v for v in range(n) if not dense[v]]
+    D = [v for v in range(n) if dense[v]]
+    if V:
+        nd(V)
+    order.extend(sorted(D, key=lambda v: len(adj[v])))
+    return order
+
+
+def analyze_with(flat, ordering: int):
+    """analyze() with a forced ordering: 1 minimum degree, 2 nested dissection."""
+    global min_degree
+    if ordering == 2:
+        saved = min_degree
+        try:
+            min_degree = nested_dissection
+            return analyze(flat)
+        finally:
+            min_degree = saved
+    return analyze(flat)

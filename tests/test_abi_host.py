@@ -81,18 +81,31 @@ CASES = {
 }
 
 
+@pytest.mark.parametrize("ordering", [1, 2])
 @pytest.mark.parametrize("case", sorted(CASES))
-def test_symbolic_bit_exact(pkg, symref, case):
+def test_symbolic_bit_exact(pkg, symref, case, ordering):
+    """J pattern, static pivot, ordering (minimum degree / nested dissection) and LU
+    fill equal the independent restatement bit for bit."""
     flat = CASES[case](pkg).flatten()
+    flat.ordering = ordering
     got = lib_analysis(pkg, flat)
-    want = symref.analyze(flat)
+    want = symref.analyze_with(flat, ordering)
     names = ["J colptr", "J rowidx", "rowmatch", "order", "LU colptr", "LU rowidx"]
     for nm, g, w in zip(names, got, want):
         assert list(g) == list(w), nm
 
 
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_auto_ordering_picks_one_of_the_two(pkg, symref, case):
+    flat = CASES[case](pkg).flatten()
+    flat.ordering = 0
+    order = list(lib_analysis(pkg, flat)[3])
+    assert order in (list(symref.analyze_with(flat, 1)[3]), list(symref.analyze_with(flat, 2)[3]))
+
+
 def test_rc_ladder_sizes(pkg):
     flat = pkg.generators.rc_ladder(100).flatten()
+    flat.ordering = 1
     cp, ri, rm, order, lcp, lri = lib_analysis(pkg, flat)
     assert flat.n == 102 and len(ri) == 303   # n = 102, nnz(J) = 303
     assert len(lri) == 303                    # no fill under the chosen ordering

@@ -15,6 +15,7 @@ from tests import circuits as K
 pytestmark = pytest.mark.gpu
 
 RTOL_EVAL = 1e-12
+STAT_KEYS = ("accepted", "rejected", "newton_iters", "dc_iters", "hmin_seen", "hmax_seen", "status")
 RELTOL, ABSTOL = 1e-6, 1e-9
 
 
@@ -167,4 +168,33 @@ def test_batch_tile_shapes_bitwise_identical(gpu, pkg):
             continue
         assert np.array_equal(r.samples, base.samples)
         assert np.array_equal(r.x_final, base.x_final)
-        assert np.array_equal(r.stats, base.stats)
+        for k in STAT_KEYS:
+            assert np.array_equal(r.stats[k], base.stats[k]), k
+
+
+def test_batch_windows_match_uninterrupted_run(gpu, pkg):
+    """Advancing in time windows (soft stops, state kept on the device) reproduces
+    an uninterrupted run bit for bit."""
+    import ctypes as C
+    templates, itpl, par, off, probes = small_mc(pkg, n_inst=24, seed=3)
+    o = pkg.make_opts("bdf2", True, 0.0, 1.2e-9, 0.0, True)
+    sw = pkg.Sweep(templates, itpl, par, off, probes=probes, n_samples=25)
+    full = sw.run(o)
+    lib = sw.lib
+    pkg.abi.check(lib.cedar_batch_start(sw.handle, C.byref(o)))
+    nrun = C.c_int32()
+    edges = [0.1e-9, 0.35e-9, 0.7e-9, 1.2e-9]
+    for k, e in enumerate(edges):
+        pkg.abi.check(lib.cedar_batch_advance(sw.handle, e, C.byref(nrun)))
+        if k < len(edges) - 1:
+            assert nrun.value == sw.n_inst
+    assert nrun.value == 0
+    xf = np.zeros_like(full.x_final)
+    samp = np.zeros_like(full.samples)
+    st = np.zeros_like(full.stats)
+    pkg.abi.check(lib.cedar_batch_results(sw.handle, xf.ctypes.data_as(C.POINTER(C.c_double)),
+                                          samp.ctypes.data_as(C.POINTER(C.c_double)), st.ctypes.data_as(C.c_void_p)))
+    assert np.array_equal(xf, full.x_final)
+    assert np.array_equal(samp, full.samples)
+    for k in STAT_KEYS:
+        assert np.array_equal(st[k], full.stats[k]), k
