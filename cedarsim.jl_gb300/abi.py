@@ -67,6 +67,11 @@ class Costs(C.Structure):
                 ("ordering", C.c_int32), ("pad", C.c_int32)]
 
 
+class Objective(C.Structure):
+    _fields_ = [("vnode", C.c_int32), ("ibranch", C.c_int32), ("probe", C.c_int32), ("pad", C.c_int32),
+                ("level", C.c_double), ("w_energy", C.c_double), ("w_delay", C.c_double), ("w_final", C.c_double)]
+
+
 class BatchTuning(C.Structure):
     _fields_ = [("lanes_per_inst", C.c_int32), ("warps_per_cta", C.c_int32), ("reserved", C.c_int32 * 6)]
 

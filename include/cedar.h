@@ -124,6 +124,19 @@ typedef struct cedar_ckt_desc {
   int32_t reserved;
 } cedar_ckt_desc;
 
+/* Objective of the discrete adjoint (per instance, over the accepted steps):
+ *   Phi = w_energy * sum_n h_n (P_n + P_{n-1}) / 2          supply energy
+ *       + w_delay  * (t50 - tstar)^2                         crossing-delay error
+ *       + w_final  * x_N[probe]                              final value
+ * with P = -x[vnode] * x[ibranch] (power delivered by the V source whose branch
+ * current is ibranch) and t50 the first crossing of x[probe] through `level`
+ * between consecutive accepted points (linear interpolation); no crossing gives
+ * a zero delay term.  Indices are original unknowns. */
+typedef struct cedar_objective {
+  int32_t vnode, ibranch, probe, pad;
+  double level, w_energy, w_delay, w_final;
+} cedar_objective;
+
 /* Fill-reducing ordering of the static-pivot LU.  AUTO computes both and keeps
  * the one whose level-scheduled factorisation + substitutions have the shorter
  * estimated critical path (ties: minimum degree). */

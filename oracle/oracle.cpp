@@ -341,9 +341,12 @@ struct DenseLU {
     }
     return true;
   }
+  // factor() swaps whole rows (the stored multipliers too), so P A = L U: apply
+  // every swap to b first, then substitute.
   void solve(double *b) const {
-    for (int k = 0; k < n; ++k) { if (piv[k] != k) std::swap(b[k], b[piv[k]]);
-      for (int i = k + 1; i < n; ++i) { double l = a[(size_t)i * n + k]; if (l != 0.0) b[i] -= l * b[k]; } }
+    for (int k = 0; k < n; ++k) if (piv[k] != k) std::swap(b[k], b[piv[k]]);
+    for (int k = 0; k < n; ++k)
+      for (int i = k + 1; i < n; ++i) { double l = a[(size_t)i * n + k]; if (l != 0.0) b[i] -= l * b[k]; }
     for (int k = n - 1; k >= 0; --k) { double s = b[k];
       for (int j = k + 1; j < n; ++j) { double u = a[(size_t)k * n + j]; if (u != 0.0) s -= u * b[j]; }
       b[k] = s / a[(size_t)k * n + k]; }
@@ -481,6 +484,9 @@ struct Sink {
   const int *probes = nullptr; int np = 0; int ns = 0; double *samp = nullptr; int next = 0;
   double tstart = 0, tstop = 0;
   int n = 0;
+  // accepted-step recorder (time, BDF order) for adjoint replay
+  std::vector<double> *rec_t = nullptr; std::vector<signed char> *rec_ord = nullptr;
+  void record(double t, int ord) { if (rec_t) { rec_t->push_back(t); rec_ord->push_back((signed char)ord); } }
   double ts(int j) const { return j == ns - 1 ? tstop : tstart + (tstop - tstart) * ((double)j / (double)(ns - 1)); }
   void point(double t, const double *x) {
     if (t_out) { if (count < cap) { t_out[count] = t; std::memcpy(x_out + (size_t)count * n, x, sizeof(double) * n); } count++; }
@@ -587,6 +593,7 @@ static int tran(const Circuit &c, const cedar_tran_opts *opts_in, double *x, Sin
       xm1 = xn; xn = xp; tprev2 = tprev; tprev = t; have_prev = true;
       st.accepted++; st.hmin_seen = std::min(st.hmin_seen, hk); st.hmax_seen = std::max(st.hmax_seen, hk);
       sink.point(t, xn.data());
+      sink.record(t, o.method == CEDAR_TRAP ? 3 : (k == 1 ? 1 : 2));
       for (int i = 0; i < n; ++i) if (!std::isfinite(xn[i])) { st.status = CEDAR_ST_NAN; std::copy(xn.begin(), xn.end(), x); return st.status; }
     }
     std::copy(xn.begin(), xn.end(), x);
@@ -685,6 +692,7 @@ static int tran(const Circuit &c, const cedar_tran_opts *opts_in, double *x, Sin
     tn2 = tn1; tn1 = t; t = tnew;
     st.accepted++; st.hmin_seen = std::min(st.hmin_seen, h); st.hmax_seen = std::max(st.hmax_seen, h);
     sink.point(t, xn.data());
+    sink.record(t, order);
     bool finite = true; for (int i = 0; i < n; ++i) if (!std::isfinite(xn[i])) finite = false;
     if (!finite) { st.status = CEDAR_ST_NAN; break; }
     if (npts < 3) ++npts;
@@ -695,6 +703,179 @@ static int tran(const Circuit &c, const cedar_tran_opts *opts_in, double *x, Sin
   std::copy(xn.begin(), xn.end(), x);
   if (st.status == CEDAR_ST_OK && t < o.tstop) st.status = CEDAR_ST_MAX_STEPS;
   return st.status;
+}
+
+// ------------------------------------------------------------------ adjoint
+// Discrete adjoint of the BDF2/BE step sequence (test/sensitivity.jl:13-42 is the
+// reference's differentiation path, forward mode through SciMLSensitivity; this
+// restates the gradient of the discrete solution, treating the accepted step
+// sequence as fixed and each step's Newton solution as exact).
+//   R_0(x_0) = Fi_dc(x_0) = 0                                   (DC operating point)
+//   R_n = Fi(x_n, t_n) + cj_n Fq(x_n) + b1_n Fq(x_{n-1}) + b2_n Fq(x_{n-2}) = 0
+//   J_n^T lam_n = -(dPhi/dx_n + b1_{n+1} C(x_n)^T lam_{n+1} + b2_{n+2} C(x_n)^T lam_{n+2})
+//   dPhi/dp = sum_n lam_n^T dR_n/dp            (p: MOS1 widths W, resistor values r)
+struct StepSeq { std::vector<double> T; std::vector<signed char> ord; };  // T[0] = tstart
+
+static void step_coef(const StepSeq &S, size_t n, double &cj, double &b1, double &b2, double &rh, double &a1, double &a2) {
+  double h = S.T[n] - S.T[n - 1];
+  if (S.ord[n] != 2) { cj = 1.0 / h; b1 = -cj; b2 = 0.0; rh = 0; a1 = 0; a2 = 0; return; }
+  double h1 = S.T[n - 1] - S.T[n - 2];
+  double wr = h / h1;
+  rh = 1.0 / h;
+  cj = (1.0 + 2.0 * wr) / ((1.0 + wr) * h);
+  a1 = -(1.0 + wr); a2 = wr * wr / (1.0 + wr);
+  b1 = a1 * rh; b2 = a2 * rh;
+}
+
+// Replay the recorded steps (DC operating point first); X[n*nv + u] = x_n.
+static int replay(const Circuit &c, const cedar_tran_opts &o, const StepSeq &S, std::vector<double> &X,
+                  const double *perturb, int64_t *iters) {
+  const int n = c.n; const size_t N = S.T.size() - 1;
+  Work w(c);
+  Tol tol{o.nr_factor * o.reltol, o.nr_factor * o.abstol_v, o.nr_factor * o.abstol_i};
+  std::vector<double> x(n, 0.0), qn(n), qm1(n), hist(n), xp(n), qt(n);
+  int64_t dci = 0;
+  if (o.dcop) { int s = dcop(w, x.data(), o.tstart, tol, &dci); if (s != CEDAR_ST_OK) return s; }
+  if (perturb) for (int i = 0; i < n; ++i) x[i] += perturb[i];
+  X.assign((N + 1) * n, 0.0);
+  std::copy(x.begin(), x.end(), X.begin());
+  EvalCtx ctx; ctx.t = o.tstart;
+  eval_q(w, x.data(), ctx, qn.data());
+  int zp = 0;
+  for (size_t k = 1; k <= N; ++k) {
+    double cj, b1, b2, rh, a1, a2;
+    step_coef(S, k, cj, b1, b2, rh, a1, a2);
+    const double *xn = &X[(k - 1) * n];
+    if (S.ord[k] != 2) for (int i = 0; i < n; ++i) hist[i] = -qn[i] * cj;
+    else for (int i = 0; i < n; ++i) hist[i] = (a1 * qn[i] + a2 * qm1[i]) * rh;
+    if (S.ord[k] == 2) {
+      const double *xm1 = &X[(k - 2) * n];
+      double r = (S.T[k] - S.T[k - 1]) / (S.T[k - 1] - S.T[k - 2]);
+      for (int i = 0; i < n; ++i) xp[i] = xn[i] + r * (xn[i] - xm1[i]);
+    } else std::copy(xn, xn + n, xp.begin());
+    ctx.t = S.T[k];
+    int r = newton(w, xp.data(), ctx, cj, hist.data(), tol, o.max_newton, 0.0, &zp);
+    if (iters) *iters += std::abs(r);
+    if (r <= 0) return zp ? CEDAR_ST_ZERO_PIVOT : CEDAR_ST_NEWTON;
+    std::copy(xp.begin(), xp.end(), X.begin() + k * n);
+    eval_q(w, xp.data(), ctx, qt.data());
+    qm1 = qn; qn = qt;
+  }
+  return CEDAR_ST_OK;
+}
+
+struct ObjVal { double phi; long k50; double t50; };
+
+static ObjVal objective(const cedar_objective &ob, double tstar, const StepSeq &S, const std::vector<double> &X, int n) {
+  const size_t N = S.T.size() - 1;
+  auto P = [&](size_t k) { return -X[k * n + ob.vnode] * X[k * n + ob.ibranch]; };
+  double E = 0;
+  for (size_t k = 1; k <= N; ++k) E += (S.T[k] - S.T[k - 1]) * (P(k) + P(k - 1)) / 2.0;
+  ObjVal v{0, -1, 0};
+  for (size_t k = 1; k <= N; ++k) {
+    double v0 = X[(k - 1) * n + ob.probe], v1 = X[k * n + ob.probe];
+    double a = v0 - ob.level, b = v1 - ob.level;
+    if ((a < 0 && b >= 0) || (a > 0 && b <= 0)) {
+      v.k50 = (long)k;
+      v.t50 = S.T[k - 1] + (ob.level - v0) * (S.T[k] - S.T[k - 1]) / (v1 - v0);
+      break;
+    }
+  }
+  double D = v.k50 > 0 ? (v.t50 - tstar) * (v.t50 - tstar) : 0.0;
+  v.phi = ob.w_energy * E + ob.w_delay * D + ob.w_final * X[N * n + ob.probe];
+  return v;
+}
+
+static int n_params(const Circuit &c) {
+  int np = 0;
+  for (const Group &g : c.groups) if (g.model == CEDAR_MOS1 || g.model == CEDAR_R) np += g.n_inst;
+  return np;
+}
+
+// grad += lam^T dFi/dp at x (MOS1: d/dW of m*Ids; R: d/dr of m*V/r)
+static void accumulate_dp(const Circuit &c, const double *x, const double *lam, double *grad) {
+  auto X = [&](int u) { return u < 0 ? 0.0 : x[u]; };
+  auto L = [&](int u) { return u < 0 ? 0.0 : lam[u]; };
+  int k = 0;
+  for (const Group &g : c.groups) {
+    if (g.model != CEDAR_MOS1 && g.model != CEDAR_R) continue;
+    for (int i = 0; i < g.n_inst; ++i, ++k) {
+      const int *tm = g.term.data() + (size_t)g.nt * i;
+      if (g.model == CEDAR_MOS1) {
+        double type = g.p(0, i), W = g.p(1, i), Lc = g.p(2, i), KP = g.p(3, i), VTO = g.p(4, i), LAM = g.p(5, i), m = g.p(6, i);
+        double beta = KP * W / Lc, vth = type * VTO;
+        Dual vgs = Dual(type * (X(tm[1]) - X(tm[2]))), vds = Dual(type * (X(tm[0]) - X(tm[2])));
+        double id = vds.v >= 0 ? mos1_id(vgs, vds, vth, beta, LAM).v : -mos1_id(vgs - vds, -vds, vth, beta, LAM).v;
+        double dI = m * type * id / W;  // d(m Ids)/dW; KCL(d) gets -m Ids, KCL(s) +m Ids
+        grad[k] += -dI * L(tm[0]) + dI * L(tm[2]);
+      } else {
+        double r = g.p(0, i), m = g.p(1, i);
+        double V = X(tm[0]) - X(tm[1]);
+        double dI = -m * V / (r * r);  // d(m V/r)/dr
+        grad[k] += -dI * L(tm[0]) + dI * L(tm[1]);
+      }
+    }
+  }
+}
+
+static int adjoint(const Circuit &c, const cedar_tran_opts &o, const StepSeq &S, const cedar_objective &ob, double tstar,
+                   const double *perturb, double *phi, double *grad) {
+  const int n = c.n; const size_t N = S.T.size() - 1;
+  std::vector<double> X;
+  int s = replay(c, o, S, X, perturb, nullptr);
+  if (s != CEDAR_ST_OK) return s;
+  ObjVal v = objective(ob, tstar, S, X, n);
+  if (phi) *phi = v.phi;
+  const int np = n_params(c);
+  std::fill(grad, grad + np, 0.0);
+  // dPhi/dx_k
+  std::vector<double> g((N + 1) * n, 0.0);
+  for (size_t k = 0; k <= N; ++k) {
+    double hk = k >= 1 ? S.T[k] - S.T[k - 1] : 0.0, hk1 = k + 1 <= N ? S.T[k + 1] - S.T[k] : 0.0;
+    double ck = ob.w_energy * (hk + hk1) / 2.0;
+    g[k * n + ob.vnode] += ck * (-X[k * n + ob.ibranch]);
+    g[k * n + ob.ibranch] += ck * (-X[k * n + ob.vnode]);
+  }
+  if (v.k50 > 0 && ob.w_delay != 0.0) {
+    size_t k = (size_t)v.k50;
+    double v0 = X[(k - 1) * n + ob.probe], v1 = X[k * n + ob.probe];
+    double a = ob.level - v0, d = v1 - v0, D = S.T[k] - S.T[k - 1];
+    double dD = ob.w_delay * 2.0 * (v.t50 - tstar);
+    g[(k - 1) * n + ob.probe] += dD * D * (a - d) / (d * d);
+    g[k * n + ob.probe] += dD * (-D * a) / (d * d);
+  }
+  g[N * n + ob.probe] += ob.w_final;
+  // backward sweep
+  Work w(c);
+  std::vector<double> lam((N + 1) * n, 0.0), rhs(n), Ct(n);
+  DenseLU lu(n);
+  for (long k = (long)N; k >= 0; --k) {
+    const double *xk = &X[(size_t)k * n];
+    EvalCtx ctx; ctx.t = k > 0 ? S.T[k] : o.tstart; ctx.dc = (k == 0);
+    eval_circuit(c, xk, ctx, w.eo);
+    for (int i = 0; i < n; ++i) rhs[i] = -g[(size_t)k * n + i];
+    for (int step = 1; step <= 2; ++step) {
+      size_t m = (size_t)k + step;
+      if (m > N) break;
+      double cj, b1, b2, rh, a1, a2;
+      step_coef(S, m, cj, b1, b2, rh, a1, a2);
+      double b = step == 1 ? b1 : b2;
+      if (b == 0.0) continue;
+      const double *lm = &lam[m * n];
+      for (int u = 0; u < n; ++u) { double acc = 0; for (int e = 0; e < n; ++e) acc += w.eo.C[(size_t)e * n + u] * lm[e]; Ct[u] = acc; }
+      for (int u = 0; u < n; ++u) rhs[u] -= b * Ct[u];
+    }
+    double cjk = 0.0, b1, b2, rh, a1, a2;
+    if (k > 0) step_coef(S, (size_t)k, cjk, b1, b2, rh, a1, a2);
+    // J^T
+    for (int e = 0; e < n; ++e) for (int u = 0; u < n; ++u)
+      lu.a[(size_t)u * n + e] = w.eo.G[(size_t)e * n + u] + cjk * w.eo.C[(size_t)e * n + u];
+    if (!lu.factor()) return CEDAR_ST_ZERO_PIVOT;
+    lu.solve(rhs.data());
+    std::copy(rhs.begin(), rhs.end(), lam.begin() + (size_t)k * n);
+    accumulate_dp(c, xk, rhs.data(), grad);
+  }
+  return CEDAR_ST_OK;
 }
 
 static thread_local std::string g_err;
@@ -755,6 +936,52 @@ int oracle_tran(const cedar_ckt_desc *d, const cedar_tran_opts *opts, double *x,
   if (st) *st = s;
   if (t_out && sink.count > cap) return CEDAR_ECAPACITY;
   return 0;
+}
+
+
+// Forward adaptive (or fixed BDF2) run that records the accepted steps, then the
+// discrete adjoint along them with the Newton tolerance of `replay_opts`.
+// grad: one entry per MOS1 (W) and R (r) device in group order.  The recorded
+// steps are returned through t_rec/ord (capacity cap, count *nrec).
+int oracle_adjoint(const cedar_ckt_desc *d, const cedar_tran_opts *fwd_opts, const cedar_tran_opts *replay_opts,
+                   const cedar_objective *ob, double tstar, const double *perturb, double *phi, double *grad,
+                   double *t_rec, signed char *ord_rec, int64_t cap, int64_t *nrec) {
+  Circuit c; if (!load_circuit(d, c, g_err)) return CEDAR_EINVAL;
+  std::vector<double> x(c.n, 0.0);
+  Sink sink; StepSeq S; S.T.push_back(fwd_opts->tstart); S.ord.push_back(0);
+  std::vector<double> rt; std::vector<signed char> ro;
+  sink.rec_t = &rt; sink.rec_ord = &ro;
+  cedar_stats st{};
+  tran(c, fwd_opts, x.data(), sink, st, perturb);
+  if (st.status != CEDAR_ST_OK) { g_err = "forward run failed"; return CEDAR_ENOCONV; }
+  for (size_t k = 0; k < rt.size(); ++k) { S.T.push_back(rt[k]); S.ord.push_back(ro[k]); }
+  if (nrec) *nrec = (int64_t)rt.size();
+  if (t_rec) for (size_t k = 0; k < rt.size() && (int64_t)k < cap; ++k) { t_rec[k] = rt[k]; ord_rec[k] = ro[k]; }
+  cedar_tran_opts o; fill_defaults(replay_opts, o);
+  int s = adjoint(c, o, S, *ob, tstar, perturb, phi, grad);
+  if (s != CEDAR_ST_OK) { g_err = "adjoint failed"; return CEDAR_ENOCONV; }
+  return 0;
+}
+
+// Phi along a recorded step sequence (used for central finite differences with
+// the step sequence held fixed).
+int oracle_replay_phi(const cedar_ckt_desc *d, const cedar_tran_opts *replay_opts, const double *t_rec,
+                      const signed char *ord_rec, int64_t nrec, const cedar_objective *ob, double tstar,
+                      const double *perturb, double *phi) {
+  Circuit c; if (!load_circuit(d, c, g_err)) return CEDAR_EINVAL;
+  cedar_tran_opts o; fill_defaults(replay_opts, o);
+  StepSeq S; S.T.push_back(o.tstart); S.ord.push_back(0);
+  for (int64_t k = 0; k < nrec; ++k) { S.T.push_back(t_rec[k]); S.ord.push_back(ord_rec[k]); }
+  std::vector<double> X;
+  int s = replay(c, o, S, X, perturb, nullptr);
+  if (s != CEDAR_ST_OK) { g_err = "replay failed"; return CEDAR_ENOCONV; }
+  *phi = objective(*ob, tstar, S, X, c.n).phi;
+  return 0;
+}
+
+int oracle_n_params(const cedar_ckt_desc *d) {
+  Circuit c; if (!load_circuit(d, c, g_err)) return -1;
+  return n_params(c);
 }
 
 double oracle_next_breakpoint(const cedar_ckt_desc *d, double t, double eps) {

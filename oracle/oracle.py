@@ -52,6 +52,13 @@ def load(pkg):
     lib.oracle_batch.restype = C.c_int
     lib.oracle_batch.argtypes = [C.POINTER(abi.BatchDesc), C.POINTER(abi.TranOpts), C.c_int32, C.c_int32, C.c_int32,
                                  dp, dp, C.c_void_p, C.c_int]
+    obj_p, to_p, cd_p = C.POINTER(abi.Objective), C.POINTER(abi.TranOpts), C.POINTER(abi.CktDesc)
+    lib.oracle_adjoint.restype = C.c_int
+    lib.oracle_adjoint.argtypes = [cd_p, to_p, to_p, obj_p, C.c_double, dp, dp, dp, dp, C.c_void_p, C.c_int64, ip]
+    lib.oracle_replay_phi.restype = C.c_int
+    lib.oracle_replay_phi.argtypes = [cd_p, to_p, dp, C.c_void_p, C.c_int64, obj_p, C.c_double, dp, dp]
+    lib.oracle_n_params.restype = C.c_int
+    lib.oracle_n_params.argtypes = [cd_p]
     lib.oracle_last_error.restype = C.c_int
     lib.oracle_last_error.argtypes = [C.c_char_p, C.c_size_t]
     _lib = lib
@@ -120,3 +127,34 @@ class Oracle:
                                    st.ctypes.data_as(C.c_void_p), nthreads)
         assert rc == 0
         return xf, samp, st
+
+    def adjoint(self, flat, fwd_opts, replay_opts, obj, tstar, perturb=None, cap=1 << 22):
+        """Forward run recording its accepted steps, then the discrete adjoint along
+        them.  Returns (phi, grad[MOS1 W..., R r...], t_rec, ord_rec)."""
+        h = self.pkg.abi.DescHolder(flat)
+        npar = self.lib.oracle_n_params(C.byref(h.desc))
+        grad = np.zeros(max(npar, 1))
+        t_rec = np.zeros(cap)
+        ord_rec = np.zeros(cap, np.int8)
+        nrec = C.c_int64()
+        phi = C.c_double()
+        pert = None if perturb is None else np.ascontiguousarray(perturb, np.float64)
+        rc = self.lib.oracle_adjoint(C.byref(h.desc), C.byref(fwd_opts), C.byref(replay_opts), C.byref(obj), tstar,
+                                     _dp(pert), C.byref(phi), _dp(grad), _dp(t_rec),
+                                     ord_rec.ctypes.data_as(C.c_void_p), cap, C.byref(nrec))
+        assert rc == 0, rc
+        m = min(nrec.value, cap)
+        return phi.value, grad[:npar].copy(), t_rec[:m].copy(), ord_rec[:m].copy()
+
+    def replay_phi(self, flat, replay_opts, t_rec, ord_rec, obj, tstar, perturb=None):
+        """The objective along a fixed step sequence (central differences use this)."""
+        h = self.pkg.abi.DescHolder(flat)
+        t_rec = np.ascontiguousarray(t_rec, np.float64)
+        ord_rec = np.ascontiguousarray(ord_rec, np.int8)
+        phi = C.c_double()
+        pert = None if perturb is None else np.ascontiguousarray(perturb, np.float64)
+        rc = self.lib.oracle_replay_phi(C.byref(h.desc), C.byref(replay_opts), _dp(t_rec),
+                                        ord_rec.ctypes.data_as(C.c_void_p), len(t_rec), C.byref(obj), tstar,
+                                        _dp(pert), C.byref(phi))
+        assert rc == 0, rc
+        return phi.value
