@@ -348,6 +348,21 @@ int cedar_eval_dev(cedar_ckt *c, const double *x, const double *xdot, double t, 
   return 0;
 }
 
+int cedar_eval_dev_noalloc(cedar_ckt *c, const double *x, const double *xdot, double t, double cj, double *F,
+                           double *J, void *stream) {
+  if (!c || !x) return fail(CEDAR_EINVAL, "null argument");
+  if (c->host_only) return fail(CEDAR_EINVAL, "host-only plan handle");
+  const DTpl &T = c->tpl->D;
+  if (T.n_out > kEvalScratchMax)
+    return fail(CEDAR_EINVAL, "circuit has " + std::to_string(T.n_out) + " device outputs; the allocation-free "
+                "evaluation holds at most " + std::to_string(kEvalScratchMax));
+  double *scratch = nullptr;
+  CUDA_TRY(eval_scratch_address(&scratch));
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+  CUDA_TRY(launch_eval(T, c->tpl->D_dev, c->dpar.p, x, xdot, t, cj, scratch, F, J, s));
+  return 0;
+}
+
 int cedar_eval(cedar_ckt *c, const double *x, const double *xdot, double t, double cj, double *F, double *J) {
   if (!c || !x) return fail(CEDAR_EINVAL, "null argument");
   if (c->host_only) return fail(CEDAR_EINVAL, "host-only plan handle");

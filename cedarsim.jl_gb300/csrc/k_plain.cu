@@ -1,5 +1,6 @@
 // k_plain.cu — parameter derivation, the drop-in residual/Jacobian kernels
 // (cedar_eval) and the single-instance block engine (Newton / DC / transient).
+#include <mutex>
 #include "kernels.cuh"
 
 namespace cedar {
@@ -79,6 +80,40 @@ cudaError_t launch_eval(const DTpl &T, const DTpl *T_dev, const double *dpar, co
   int m = T.n_csc > T.n ? T.n_csc : T.n;
   stamp_kernel<<<(m + th - 1) / th, th, 0, s>>>(T, dout, F, J);
   return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the residual / Jacobian evaluation.
+//
+// The device outputs that eval_kernel writes and stamp_kernel reads normally live
+// in a buffer the handle allocates.  For callers that may not allocate device
+// memory at the point of the call, this scratch is instead a file-scope device
+// array of fixed size that every GPU loading this library holds until the
+// process exits.  Host code cannot use the array's name as a device address: the
+// address is looked up once per device with cudaGetSymbolAddress, with that
+// device current, and cached.  Every call shares the one array per device, so
+// calls whose kernels overlap on the GPU race on it; serialise them (one stream,
+// or events).  eval_kernel overwrites every output slot it uses before
+// stamp_kernel reads it, so nothing needs clearing between calls.
+static __device__ __align__(256) double g_eval_scratch[kEvalScratchMax];
+
+static std::mutex g_scratch_mu;
+static double *g_scratch_ptr[kMaxDevices] = {};
+
+cudaError_t eval_scratch_address(double **ptr) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lk(g_scratch_mu);
+  if (!g_scratch_ptr[dev]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_eval_scratch);
+    if (e != cudaSuccess) return e;
+    g_scratch_ptr[dev] = static_cast<double *>(p);
+  }
+  *ptr = g_scratch_ptr[dev];
+  return cudaSuccess;
 }
 
 // Single instance on one CTA.  Workspace in dynamic shared memory when it fits,

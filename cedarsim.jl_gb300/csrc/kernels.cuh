@@ -50,6 +50,14 @@ cudaError_t launch_derive(const DTpl *tpls_dev, const int *inst_tpl, const long 
 cudaError_t launch_eval(const DTpl &T, const DTpl *T_dev, const double *dpar, const double *x, const double *xdot,
                         double t, double cj, double *dout, double *F, double *J, cudaStream_t s);
 
+// Fixed-size device scratch for the allocation-free evaluation entry point:
+// kEvalScratchMax doubles (2 MiB) per device, i.e. circuits with at most that many
+// device outputs.  eval_scratch_address returns its device address for the
+// current device (looked up once per device, then cached).
+constexpr int kEvalScratchMax = 1 << 18;
+constexpr int kMaxDevices = 64;
+cudaError_t eval_scratch_address(double **ptr);
+
 // single-instance block engine: mode 0 = transient, 1 = one Newton solve, 2 = DC op
 struct PlainArgs {
   const DTpl *T; const double *dpar;

@@ -232,6 +232,23 @@ int cedar_eval(cedar_ckt *ckt, const double *x, const double *xdot, double t, do
 int cedar_eval_dev(cedar_ckt *ckt, const double *x, const double *xdot, double t, double cj,
                    double *F, double *Jvals);
 
+/* Same as cedar_eval_dev, for callers that may not allocate device memory at the
+ * point of the call: real-time solver loops that ban allocation after set-up,
+ * and hosts whose device memory is reserved up front by another runtime's pool
+ * allocator (a cudaMalloc there fails or stalls the host's own work).
+ * It has no counterpart in the reference.  It calls no cudaMalloc or cudaFree:
+ * its scratch (the per-device model outputs, at most 262144 doubles = 2 MiB, a
+ * larger circuit returns CEDAR_EINVAL) is a fixed array that every GPU loading
+ * the library holds until the process exits.  The first call on a device looks
+ * up that array's device address (cudaGetSymbolAddress with the device current)
+ * and caches it, so make the first call on each device before any stream
+ * capture.  All calls on a device share the array: calls whose kernels overlap
+ * on the GPU race, so order them (same stream, or events).  stream: a
+ * cudaStream_t, or NULL for the handle's stream.  The handle itself is created
+ * (and allocates) beforehand with cedar_ckt_create. */
+int cedar_eval_dev_noalloc(cedar_ckt *ckt, const double *x, const double *xdot, double t, double cj,
+                           double *F, double *Jvals, void *stream);
+
 /* One implicit step: solve Fi(x, t) + cj*Fq(x) + hist = 0 for x by Newton with
  * refactorisation every iteration.  hist (may be NULL) is the integrator history
  * in Fq space.  x holds the initial guess on entry and the solution on exit. */
