@@ -162,6 +162,7 @@ EXPORTS = [
     "cedar_batch_create", "cedar_batch_destroy", "cedar_batch_run", "cedar_batch_start", "cedar_batch_advance",
     "cedar_batch_results", "cedar_batch_last_ms", "cedar_batch_set_tuning",
     "cedar_batch_get_tuning", "cedar_batch_autotune", "cedar_batch_nmax",
+    "cedar_adjoint_run", "cedar_adjoint_nparams", "cedar_adjoint_tape", "cedar_adjoint_last_ms",
 ]
 
 _lib = None
@@ -211,6 +212,11 @@ def load_library(build_if_missing: bool = True):
         "cedar_batch_get_tuning": (C.c_int, [P, C.POINTER(BatchTuning)]),
         "cedar_batch_autotune": (C.c_int, [P, C.POINTER(TranOpts), C.c_double, C.POINTER(BatchTuning)]),
         "cedar_batch_nmax": (C.c_int, [P, c_int32_p]),
+        "cedar_adjoint_run": (C.c_int, [P, C.POINTER(TranOpts), C.POINTER(Objective), c_double_p, C.c_int64,
+                                        c_double_p, c_double_p, c_int32_p, P]),
+        "cedar_adjoint_nparams": (C.c_int, [P, c_int32_p, c_int32_p]),
+        "cedar_adjoint_tape": (C.c_int, [P, C.c_int32, c_double_p, P, C.c_int64, c_int64_p]),
+        "cedar_adjoint_last_ms": (C.c_int, [P, c_double_p, c_double_p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

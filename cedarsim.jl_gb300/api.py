@@ -8,6 +8,7 @@ prob.f.f(out, du, u, p, t) / prob.f.jac(J, du, u, p, gamma, t)
 dc!(circ)                 (src/sweeps.jl:437-448)        dc(circuit)
 tran!(circ, tspan)        (src/sweeps.jl:450-463)        tran(circuit, tspan, ...)
 CircuitSweep + tran!.     (src/sweeps.jl:390-435,488-502) Sweep(...).tran(...)
+forward sensitivities     (test/sensitivity.jl:13-42)    Sweep(...).adjoint(...)
 
 Every computation runs in libcedar_gpu.so; nothing here falls back to the CPU.
 """
@@ -225,3 +226,51 @@ class Sweep:
 
     def tran(self, tspan, method="bdf2", reltol=1e-6, abstol_v=1e-9, dcop=True, **kw) -> BatchResult:
         return self.run(make_opts(method, True, tspan[0], tspan[1], 0.0, dcop, reltol, abstol_v, **kw))
+
+    def nparams(self) -> Tuple[np.ndarray, int]:
+        """Differentiable parameters per template (MOS1 widths, resistor values) and their maximum."""
+        per = np.zeros(len(self.templates), np.int32)
+        m = C.c_int32()
+        check(self.lib.cedar_adjoint_nparams(self.handle, per.ctypes.data_as(C.POINTER(C.c_int32)), C.byref(m)))
+        return per, m.value
+
+    def adjoint(self, opts, objectives, tstar=None, tape_cap: int = 0) -> "AdjointResult":
+        """Objective and its gradient by the discrete adjoint, for every instance.
+
+        objectives: one abi.Objective per template (original unknown indices).
+        tstar: target crossing time per instance (or None)."""
+        per, np_max = self.nparams()
+        obj = (abi.Objective * len(self.templates))(*objectives)
+        ts = None if tstar is None else np.ascontiguousarray(tstar, np.float64)
+        phi = np.zeros(self.n_inst)
+        grad = np.zeros((self.n_inst, max(np_max, 1)))
+        status = np.zeros(self.n_inst, np.int32)
+        st = np.zeros(self.n_inst, STATS_DTYPE)
+        check(self.lib.cedar_adjoint_run(self.handle, C.byref(opts), obj, None if ts is None else _dp(ts),
+                                         int(tape_cap), _dp(phi), _dp(grad),
+                                         status.ctypes.data_as(C.POINTER(C.c_int32)), st.ctypes.data_as(C.c_void_p)))
+        f, b = C.c_double(), C.c_double()
+        check(self.lib.cedar_adjoint_last_ms(self.handle, C.byref(f), C.byref(b)))
+        return AdjointResult(phi, grad[:, :np_max], status, st, per, f.value, b.value)
+
+    def tape(self, inst: int):
+        """Times and orders of the accepted steps the last adjoint run recorded for one instance."""
+        n = C.c_int64()
+        check(self.lib.cedar_adjoint_tape(self.handle, int(inst), None, None, 0, C.byref(n)))
+        t = np.zeros(n.value)
+        o = np.zeros(n.value, np.int8)
+        check(self.lib.cedar_adjoint_tape(self.handle, int(inst), _dp(t), o.ctypes.data_as(C.c_void_p), n.value,
+                                          C.byref(n)))
+        return t, o
+
+
+@dataclass
+class AdjointResult:
+    phi: np.ndarray          # [n_inst]
+    grad: np.ndarray         # [n_inst, np_max]; row i valid up to nparams[template(i)]
+    status: np.ndarray       # [n_inst] CEDAR_ST_*
+    stats: np.ndarray        # forward counters
+    nparams: np.ndarray      # per template
+    fwd_ms: float            # device time of the recording forward run
+    bwd_ms: float            # device time of the backward kernel
+

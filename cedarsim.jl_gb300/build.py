@@ -21,7 +21,7 @@ INCLUDE = PKG.parent / "include"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", "-I", str(INCLUDE)]
-SOURCES = ["api.cu", "k_plain.cu", "k_batch.cu", "compile.cpp"]
+SOURCES = ["api.cu", "k_plain.cu", "k_batch.cu", "k_adjoint.cu", "compile.cpp"]
 
 
 def _nvcc() -> str:

@@ -92,6 +92,10 @@ int upload_template(const cedar_ckt_desc *desc, std::unique_ptr<DevTemplate> &ou
   size_t o_src_of_dev = P.vec(src_of_dev);
   size_t o_src_off = P.vec(src_off), o_src_stride = P.vec(src_stride), o_gs_slot = P.vec(H.gs_slot), o_gs_row = P.vec(gs_row), o_gs_col = P.vec(gs_col);
   size_t o_is_node = P.vec(H.is_node_int), o_order = P.vec(H.order), o_iorder = P.vec(H.iorder), o_eq_pos = P.vec(H.eq_pos), o_pwl = P.vec(H.pwl);
+  std::vector<int2> tf_pair = pairs(H.tf_lu, H.tf_col), tb_pair = pairs(H.tb_lu, H.tb_col), ct_ent = pairs(H.ct_ent, H.ct_row);
+  size_t o_tf_lvl = P.vec(H.tf_lvl_ptr), o_tf_row = P.vec(H.tf_row), o_tf_ptr = P.vec(H.tf_ptr), o_tf_pair = P.vec(tf_pair);
+  size_t o_tb_lvl = P.vec(H.tb_lvl_ptr), o_tb_row = P.vec(H.tb_row), o_tb_ptr = P.vec(H.tb_ptr), o_tb_pair = P.vec(tb_pair);
+  size_t o_ct_ptr = P.vec(H.ct_ptr), o_ct_ent = P.vec(ct_ent), o_adj_goff = P.vec(H.adj_goff);
   CUDA_TRY(cudaMalloc(&dt->buf, P.bytes.size()));
   CUDA_TRY(cudaMemcpy(dt->buf, P.bytes.data(), P.bytes.size(), cudaMemcpyHostToDevice));
   char *b = (char *)dt->buf;
@@ -116,6 +120,10 @@ int upload_template(const cedar_ckt_desc *desc, std::unique_ptr<DevTemplate> &ou
   D.gs_slot = (const int *)(b + o_gs_slot); D.gs_row = (const int *)(b + o_gs_row); D.gs_col = (const int *)(b + o_gs_col);
   D.is_node = (const unsigned char *)(b + o_is_node); D.order = (const int *)(b + o_order); D.iorder = (const int *)(b + o_iorder);
   D.eq_pos = (const int *)(b + o_eq_pos); D.pwl = (const double *)(b + o_pwl);
+  D.tf_nlev = (int)H.tf_lvl_ptr.size() - 1; D.tb_nlev = (int)H.tb_lvl_ptr.size() - 1; D.n_adj = H.n_adj;
+  D.tf_lvl = (const int *)(b + o_tf_lvl); D.tf_row = (const int *)(b + o_tf_row); D.tf_ptr = (const int *)(b + o_tf_ptr); D.tf_pair = (const int2 *)(b + o_tf_pair);
+  D.tb_lvl = (const int *)(b + o_tb_lvl); D.tb_row = (const int *)(b + o_tb_row); D.tb_ptr = (const int *)(b + o_tb_ptr); D.tb_pair = (const int2 *)(b + o_tb_pair);
+  D.ct_ptr = (const int *)(b + o_ct_ptr); D.ct_ent = (const int2 *)(b + o_ct_ent); D.adj_goff = (const int *)(b + o_adj_goff);
   CUDA_TRY(cudaMalloc(&dt->D_dev, sizeof(DTpl)));
   CUDA_TRY(cudaMemcpy(dt->D_dev, &D, sizeof(DTpl), cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMalloc(&dt->par_dev, std::max<size_t>(1, H.par.size()) * sizeof(double)));
@@ -197,9 +205,19 @@ struct cedar_batch {
   bool started = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // bracket the last batch launch
   bool timed = false;
+  // discrete adjoint: tape, checkpoints, replayed segments, results
+  DevBuf<double> tape_t, tape_p, tape_v, ckpt, segx, adj_phi, adj_grad, adj_tstar;
+  DevBuf<signed char> tape_ord;
+  DevBuf<int4> obj_idx;
+  DevBuf<AdjObj> adj_obj;
+  DevBuf<int> adj_status;
+  cudaEvent_t ev2 = nullptr;   // end of the last adjoint's backward kernel
+  bool adj_timed = false;
+  long long tape_cap = 0;      // steps per instance of the last adjoint's tape
   ~cedar_batch() {
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
+    if (ev2) cudaEventDestroy(ev2);
     if (stream) cudaStreamDestroy(stream);
   }
 };
@@ -559,14 +577,14 @@ int cedar_batch_get_tuning(const cedar_batch *b, cedar_batch_tuning *t) {
   return 0;
 }
 
-static int batch_launch(cedar_batch *b, const EngOpts &eo, const cedar_batch_tuning &tu, bool want_outputs,
-                        double t_until, bool fresh) {
-  int K = tu.lanes_per_inst, warps = tu.warps_per_cta;
+// Grid and shared memory of a persistent launch: slot workspaces of `stride`
+// doubles in shared memory when a CTA's slots fit, else in global memory.
+static int launch_geometry(int K, int warps, int stride, int n_inst, bool &in_smem, size_t &smem, int &grid) {
   int tiles = warps * 32 / K;
-  size_t per_tile = (size_t)b->ws_stride * sizeof(double);
+  size_t per_tile = (size_t)stride * sizeof(double);
   int smax = batch_max_smem_optin();
-  bool in_smem = (size_t)tiles * per_tile <= (size_t)smax;
-  size_t smem = in_smem ? (size_t)tiles * per_tile : 0;
+  in_smem = (size_t)tiles * per_tile <= (size_t)smax;
+  smem = in_smem ? (size_t)tiles * per_tile : 0;
   int dev = 0, nsm = 0;
   CUDA_TRY(cudaGetDevice(&dev));
   CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -577,7 +595,17 @@ static int batch_launch(cedar_batch *b, const EngOpts &eo, const cedar_batch_tun
   } else {
     per_sm = std::max(1, 2048 / (warps * 32));
   }
-  int grid = std::max(1, std::min(nsm * per_sm, (b->n_inst + tiles - 1) / tiles));
+  grid = std::max(1, std::min(nsm * per_sm, (n_inst + tiles - 1) / tiles));
+  return 0;
+}
+
+static int batch_launch(cedar_batch *b, const EngOpts &eo, const cedar_batch_tuning &tu, bool want_outputs,
+                        double t_until, bool fresh, const BatchDev *tape = nullptr, BatchDev *used = nullptr) {
+  int K = tu.lanes_per_inst, warps = tu.warps_per_cta;
+  int tiles = warps * 32 / K;
+  bool in_smem = false; size_t smem = 0; int grid = 1;
+  int rc = launch_geometry(K, warps, b->ws_stride, b->n_inst, in_smem, smem, grid);
+  if (rc) return rc;
   if (!in_smem) CUDA_TRY(b->ws.ensure((size_t)grid * tiles * b->ws_stride));
   BatchDev bd{};
   bd.tpls = b->d_tpls.p; bd.inst_tpl = b->inst_tpl.p; bd.inst_dpar = b->dpar_off.p; bd.dpar = b->dpar.p;
@@ -589,6 +617,11 @@ static int batch_launch(cedar_batch *b, const EngOpts &eo, const cedar_batch_tun
   bd.stats = b->stats.p; bd.queue = b->queue.p; bd.head = b->head.p; bd.n_inst = b->n_inst;
   bd.opts = eo; bd.ws_stride = b->ws_stride; bd.ws_global = b->ws.p; bd.ws_in_smem = in_smem ? 1 : 0;
   bd.t_until = t_until; bd.rows = b->rows.p; bd.row_vec = b->row_vec.p; bd.n_running = b->n_running.p;
+  if (tape) {
+    bd.tape_t = tape->tape_t; bd.tape_ord = tape->tape_ord; bd.tape_p = tape->tape_p; bd.tape_v = tape->tape_v;
+    bd.tape_cap = tape->tape_cap; bd.ckpt = tape->ckpt; bd.ckpt_every = tape->ckpt_every; bd.obj_idx = tape->obj_idx;
+  }
+  if (used) *used = bd;
   CUDA_TRY(cudaMemsetAsync(b->head.p, 0, sizeof(int), b->stream));
   CUDA_TRY(cudaMemsetAsync(b->n_running.p, 0, sizeof(int), b->stream));
   if (fresh) {
@@ -655,6 +688,116 @@ int cedar_batch_run(cedar_batch *b, const cedar_tran_opts *opts, double *x_final
   if (samples && b->np) CUDA_TRY(cudaMemcpyAsync(samples, b->samples.p, (size_t)b->n_inst * b->np * b->ns * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
   if (stats) CUDA_TRY(cudaMemcpyAsync(stats, b->stats.p, (size_t)b->n_inst * sizeof(EngStats), cudaMemcpyDeviceToHost, b->stream));
   CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return 0;
+}
+
+// ------------------------------------------------------------------ adjoint
+int cedar_adjoint_nparams(const cedar_batch *b, int32_t *np_per_template, int32_t *np_max) {
+  if (!b) return fail(CEDAR_EINVAL, "null handle");
+  int m = 0;
+  for (size_t k = 0; k < b->tpls.size(); ++k) {
+    if (np_per_template) np_per_template[k] = b->tpls[k]->H.n_adj;
+    m = std::max(m, b->tpls[k]->H.n_adj);
+  }
+  if (np_max) *np_max = m;
+  return 0;
+}
+
+int cedar_adjoint_run(cedar_batch *b, const cedar_tran_opts *opts, const cedar_objective *obj, const double *tstar,
+                      int64_t tape_cap, double *phi, double *grad, int32_t *status, cedar_stats *stats) {
+  if (!b || !obj) return fail(CEDAR_EINVAL, "null argument");
+  int rc = check_opts(opts); if (rc) return rc;
+  if (!opts->adaptive || opts->method != CEDAR_BDF2)
+    return fail(CEDAR_EUNSUPPORTED, "the adjoint follows adaptive BDF2 runs");
+  if (b->has_dx) return fail(CEDAR_EUNSUPPORTED, "the adjoint does not take state perturbations (inst_dx)");
+  if (b->n_inst == 0) return 0;
+  const long long cap = tape_cap > 0 ? tape_cap : (1LL << 19);
+  const int every = 64;
+  const int ni = b->n_inst, nt = (int)b->tpls.size();
+  std::vector<int4> oi(nt);
+  std::vector<AdjObj> ao(nt);
+  int np_max = 0;
+  for (int k = 0; k < nt; ++k) {
+    const Template &H = b->tpls[k]->H;
+    const cedar_objective &o = obj[k];
+    if (o.vnode < 0 || o.vnode >= H.n_nodes || o.ibranch < H.n_nodes || o.ibranch >= H.n || o.probe < 0 || o.probe >= H.n)
+      return fail(CEDAR_EINVAL, "objective index out of range for template " + std::to_string(k));
+    oi[k] = make_int4(H.iorder[o.vnode], H.iorder[o.ibranch], H.iorder[o.probe], 0);
+    ao[k] = AdjObj{oi[k].x, oi[k].y, oi[k].z, 0, o.level, o.w_energy, o.w_delay, o.w_final};
+    np_max = std::max(np_max, H.n_adj);
+  }
+  const size_t ts = (size_t)ni * (size_t)tape_stride(cap);
+  CUDA_TRY(b->tape_t.ensure(ts)); CUDA_TRY(b->tape_p.ensure(ts)); CUDA_TRY(b->tape_v.ensure(ts));
+  CUDA_TRY(b->tape_ord.ensure(ts));
+  CUDA_TRY(b->ckpt.ensure((size_t)ni * ckpt_count(cap, every) * 2 * b->n_max));
+  CUDA_TRY(b->segx.ensure((size_t)ni * (every + 1) * b->n_max));
+  CUDA_TRY(b->adj_phi.ensure(ni)); CUDA_TRY(b->adj_grad.ensure((size_t)ni * std::max(np_max, 1)));
+  CUDA_TRY(b->adj_status.ensure(ni));
+  CUDA_TRY(b->obj_idx.ensure(nt)); CUDA_TRY(b->adj_obj.ensure(nt));
+  CUDA_TRY(cudaMemcpyAsync(b->obj_idx.p, oi.data(), nt * sizeof(int4), cudaMemcpyHostToDevice, b->stream));
+  CUDA_TRY(cudaMemcpyAsync(b->adj_obj.p, ao.data(), nt * sizeof(AdjObj), cudaMemcpyHostToDevice, b->stream));
+  if (tstar) {
+    CUDA_TRY(b->adj_tstar.ensure(ni));
+    CUDA_TRY(cudaMemcpyAsync(b->adj_tstar.p, tstar, ni * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+  }
+  // forward with the tape on
+  if ((rc = cedar_batch_start(b, opts))) return rc;
+  BatchDev tape{};
+  tape.tape_t = b->tape_t.p; tape.tape_ord = b->tape_ord.p; tape.tape_p = b->tape_p.p; tape.tape_v = b->tape_v.p;
+  tape.tape_cap = cap; tape.ckpt = b->ckpt.p; tape.ckpt_every = every; tape.obj_idx = b->obj_idx.p;
+  b->tape_cap = cap;
+  BatchDev used{};
+  if ((rc = batch_launch(b, b->run_opts, b->tune, true, 1e300, false, &tape, &used))) return rc;
+  // backward
+  const int K = b->tune.lanes_per_inst, warps = b->tune.warps_per_cta, tiles = warps * 32 / K;
+  int stride = 0;
+  for (auto &t : b->tpls) stride = std::max(stride, ws_doubles(t->H.n, t->H.nnz_lu, t->H.n_out, (int)t->H.src_group.size()) + t->H.n_adj);
+  stride = ((stride + 15) / 16) * 16 + 8;
+  bool in_smem = false; size_t smem = 0; int grid = 1;
+  if ((rc = launch_geometry(K, warps, stride, ni, in_smem, smem, grid))) return rc;
+  if (!in_smem) CUDA_TRY(b->ws.ensure((size_t)grid * tiles * stride));
+  AdjDev a{};
+  a.b = used;
+  a.b.ws_stride = stride; a.b.ws_in_smem = in_smem ? 1 : 0; a.b.ws_global = b->ws.p;
+  a.raw_off = b->raw_off.p; a.raw = b->raw.p; a.obj = b->adj_obj.p; a.tstar = tstar ? b->adj_tstar.p : nullptr;
+  a.phi = b->adj_phi.p; a.grad = b->adj_grad.p; a.np_max = np_max; a.status = b->adj_status.p;
+  a.segx = b->segx.p; a.fwd = b->stats.p;
+  CUDA_TRY(cudaMemsetAsync(b->head.p, 0, sizeof(int), b->stream));
+  if (!b->ev2) CUDA_TRY(cudaEventCreate(&b->ev2));
+  CUDA_TRY(launch_adjoint(a, K, warps, grid, smem, b->stream));
+  CUDA_TRY(cudaEventRecord(b->ev2, b->stream));
+  b->adj_timed = true;
+  if (phi) CUDA_TRY(cudaMemcpyAsync(phi, b->adj_phi.p, ni * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  if (grad && np_max) CUDA_TRY(cudaMemcpyAsync(grad, b->adj_grad.p, (size_t)ni * np_max * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  if (status) CUDA_TRY(cudaMemcpyAsync(status, b->adj_status.p, ni * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  if (stats) CUDA_TRY(cudaMemcpyAsync(stats, b->stats.p, (size_t)ni * sizeof(EngStats), cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return 0;
+}
+
+int cedar_adjoint_tape(cedar_batch *b, int32_t inst, double *t, int8_t *ord, int64_t cap, int64_t *n_steps) {
+  if (!b) return fail(CEDAR_EINVAL, "null handle");
+  if (!b->adj_timed) return fail(CEDAR_EINVAL, "no adjoint run recorded yet");
+  if (inst < 0 || inst >= b->n_inst) return fail(CEDAR_EINVAL, "instance out of range");
+  EngStats st{};
+  CUDA_TRY(cudaMemcpy(&st, b->stats.p + inst, sizeof(EngStats), cudaMemcpyDeviceToHost));
+  const long long n = st.accepted, stride = tape_stride(b->tape_cap);
+  if (n_steps) *n_steps = n;
+  const long long m = std::min<long long>(n, std::max<int64_t>(cap, 0));
+  if (m > 0 && t) CUDA_TRY(cudaMemcpy(t, b->tape_t.p + (size_t)inst * stride + 1, m * sizeof(double), cudaMemcpyDeviceToHost));
+  if (m > 0 && ord) CUDA_TRY(cudaMemcpy(ord, b->tape_ord.p + (size_t)inst * stride + 1, m, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+int cedar_adjoint_last_ms(cedar_batch *b, double *fwd_ms, double *bwd_ms) {
+  if (!b) return fail(CEDAR_EINVAL, "null handle");
+  if (!b->adj_timed) return fail(CEDAR_EINVAL, "no adjoint run recorded yet");
+  CUDA_TRY(cudaEventSynchronize(b->ev2));
+  float f = 0, g = 0;
+  CUDA_TRY(cudaEventElapsedTime(&f, b->ev0, b->ev1));
+  CUDA_TRY(cudaEventElapsedTime(&g, b->ev1, b->ev2));
+  if (fwd_ms) *fwd_ms = f;
+  if (bwd_ms) *bwd_ms = g;
   return 0;
 }
 

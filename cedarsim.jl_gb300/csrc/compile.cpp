@@ -104,6 +104,12 @@ static void build_program(int nslots, const std::vector<std::pair<int, int32_t>>
 
 static int32_t enc(const Stamp &s) { return (s.out << 1) | (s.neg ? 1 : 0); }
 
+// Outputs that hold cj * dQ/dV (the C part of J = G + cj C): capacitor out 1,
+// inductor out 4 (see eval_device).
+static bool is_charge_partial(int model, int local_out) {
+  return (model == CEDAR_C && local_out == 1) || (model == CEDAR_L && local_out == 4);
+}
+
 // Structural matching: colrows[u] sorted rows with a nonzero in column u.
 static bool match_columns(int n, const std::vector<std::vector<int>> &colrows,
                           const std::vector<std::vector<int>> &rowcols, std::vector<int> &rowmatch) {
@@ -312,12 +318,21 @@ static bool compile_with(const cedar_ckt_desc *d, Template &T, std::string &err,
   }
   T.par_size = par_off; T.dpar_size = dpar_off; T.n_out = out_off;
 
-  // stamps in device order
+  // stamps in device order; SJq marks J stamps carrying a charge partial (cj dQ/dV)
   std::vector<Stamp> SJ, SF, SQ;
+  std::vector<char> SJq;
+  T.adj_goff.clear(); T.n_adj = 0;
   for (const GroupInfo &g : T.groups) {
     const ModelInfo &mi = kModels[g.model];
-    for (int i = 0; i < g.n_inst; ++i)
-      device_stamps(g.model, &T.term_orig[g.term_off + (size_t)i * g.ntx], g.out_off + i * mi.nout, SJ, SF, SQ);
+    for (int i = 0; i < g.n_inst; ++i) {
+      const int ob = g.out_off + i * mi.nout;
+      size_t before = SJ.size();
+      device_stamps(g.model, &T.term_orig[g.term_off + (size_t)i * g.ntx], ob, SJ, SF, SQ);
+      for (size_t k = before; k < SJ.size(); ++k) SJq.push_back(is_charge_partial(g.model, SJ[k].out - ob) ? 1 : 0);
+    }
+    const bool diff = (g.model == CEDAR_MOS1 || g.model == CEDAR_R);
+    T.adj_goff.push_back(diff ? T.n_adj : -1);
+    if (diff) T.n_adj += g.n_inst;
   }
   // original pattern
   std::vector<std::vector<int>> colrows(n), rowcols(n);
@@ -420,6 +435,15 @@ static bool compile_with(const cedar_ckt_desc *d, Template &T, std::string &err,
     it.clear();
     for (const Stamp &s : SQ) it.push_back({T.eq_pos[s.row], enc(s)});
     build_program(n, it, T.qint_ptr, T.qint_ent);
+    // C^T program: per internal column q, the charge-partial stamps of column q
+    // with their internal rows, in device order
+    std::vector<std::pair<int, int32_t>> ic;
+    std::vector<int32_t> rowsof;
+    for (size_t k = 0; k < SJ.size(); ++k) if (SJq[k]) { ic.push_back({T.iorder[SJ[k].col], (int32_t)rowsof.size()}); rowsof.push_back((int32_t)k); }
+    std::vector<int32_t> idx;
+    build_program(n, ic, T.ct_ptr, idx);
+    T.ct_ent.resize(idx.size()); T.ct_row.resize(idx.size());
+    for (size_t e = 0; e < idx.size(); ++e) { const Stamp &st = SJ[rowsof[idx[e]]]; T.ct_ent[e] = enc(st); T.ct_row[e] = T.eq_pos[st.row]; }
   }
 
   // factorisation tasks
@@ -488,6 +512,29 @@ static bool compile_with(const cedar_ckt_desc *d, Template &T, std::string &err,
     };
     emit(lf, true, T.fw_lvl_ptr, T.fw_row, T.fw_ptr, T.fw_lu, T.fw_col);
     emit(lb, false, T.bw_lvl_ptr, T.bw_row, T.bw_ptr, T.bw_lu, T.bw_col);
+
+    // transposed substitutions for J^T lam = r with J = L U (adjoint):
+    //   U^T z = r:   z_i = (r_i - sum_{j<i} U[j][i] z_j) / U[i][i]   (column i of U above the diagonal)
+    //   L^T lam = z: lam_i = z_i - sum_{j>i} L[j][i] lam_j          (column i of L below the diagonal)
+    std::vector<int> tfl(n, 0), tbl(n, 0);
+    for (int i = 0; i < n; ++i) { int L = 0; for (int p : lucol[i]) if (p < i) L = std::max(L, tfl[p] + 1); tfl[i] = L; }
+    for (int i = n - 1; i >= 0; --i) { int L = 0; for (int p : lucol[i]) if (p > i) L = std::max(L, tbl[p] + 1); tbl[i] = L; }
+    auto emit_t = [&](const std::vector<int> &lv, bool upper, std::vector<int32_t> &lp, std::vector<int32_t> &rw,
+                      std::vector<int32_t> &pp, std::vector<int32_t> &pl, std::vector<int32_t> &pc) {
+      int nl = 0; for (int v : lv) nl = std::max(nl, v + 1);
+      std::vector<int> idx(n); for (int i = 0; i < n; ++i) idx[i] = i;
+      std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return lv[a] < lv[b]; });
+      lp.assign(nl + 1, 0); for (int i = 0; i < n; ++i) lp[lv[i] + 1]++;
+      for (int l = 0; l < nl; ++l) lp[l + 1] += lp[l];
+      rw.clear(); pp.assign(1, 0); pl.clear(); pc.clear();
+      for (int i : idx) {
+        rw.push_back(i);
+        for (int p : lucol[i]) if (upper ? p < i : p > i) { pl.push_back(slot(p, i)); pc.push_back(p); }
+        pp.push_back((int)pl.size());
+      }
+    };
+    emit_t(tfl, true, T.tf_lvl_ptr, T.tf_row, T.tf_ptr, T.tf_lu, T.tf_col);
+    emit_t(tbl, false, T.tb_lvl_ptr, T.tb_row, T.tb_ptr, T.tb_lu, T.tb_col);
   }
   return true;
 }

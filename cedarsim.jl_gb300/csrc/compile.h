@@ -71,6 +71,15 @@ struct Template {
   // triangular solves (row tasks by level)
   std::vector<int32_t> fw_lvl_ptr, fw_row, fw_ptr, fw_lu, fw_col;
   std::vector<int32_t> bw_lvl_ptr, bw_row, bw_ptr, bw_lu, bw_col;
+  // transposed substitutions (adjoint), same layout as fw/bw
+  std::vector<int32_t> tf_lvl_ptr, tf_row, tf_ptr, tf_lu, tf_col;
+  std::vector<int32_t> tb_lvl_ptr, tb_row, tb_ptr, tb_lu, tb_col;
+  // C^T program per internal column: entry ((out << 1) | neg) and internal row
+  std::vector<int32_t> ct_ptr, ct_ent, ct_row;
+  // adjoint parameters: first gradient index of each group (-1: none); MOS1
+  // widths and resistor values, in group order
+  std::vector<int32_t> adj_goff;
+  int n_adj = 0;
   // time-varying sources (global device index), for breakpoint search
   std::vector<int32_t> src_group, src_inst;
   // LU slot of (KCL(u), u) per node u, used by the DC gmin-stepping homotopy

@@ -43,6 +43,14 @@ struct DTpl {
   const int *iorder;                  // original unknown -> internal position
   const int *eq_pos;                  // original equation -> internal row
   const double *pwl;
+  // discrete adjoint: transposed substitutions (U^T then L^T, row-task layout as
+  // fw/bw), C^T program per internal column ((out << 1) | neg, internal row) and
+  // the first gradient index of each group (-1: no differentiable parameter)
+  int tf_nlev, tb_nlev, n_adj, pad_adj;
+  const int *tf_lvl, *tf_row, *tf_ptr; const int2 *tf_pair;
+  const int *tb_lvl, *tb_row, *tb_ptr; const int2 *tb_pair;
+  const int *ct_ptr; const int2 *ct_ent;
+  const int *adj_goff;
 };
 
 // workspace size in doubles for one instance

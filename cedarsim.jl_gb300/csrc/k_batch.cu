@@ -1,643 +1,7 @@
-// k_batch.cu — batched persistent engine: thousands of sweep / Monte Carlo
-// instances of uneven sizes in one launch.
-//
-// A warp holds 32/K instance slots of K lanes each.  Every slot runs its own
-// instance (own step size, Newton state, integrator history and DC homotopy, all
-// in the slot's shared-memory workspace), but the expensive part — one Newton
-// iteration: device evaluation, stamping, level-scheduled LU, substitutions and
-// update — is executed by all active slots of the warp together, so the warp
-// stays converged and a level of the LU schedule with one task per instance
-// costs one FP64 instruction for the whole warp instead of one per instance.
-// Everything else (step control, LTE, breakpoints, DC homotopy bookkeeping,
-// output sampling) is a per-slot resumable state machine that mirrors the
-// straight-line algorithm of engine.cuh (and of the CPU oracle) decision for
-// decision.  A slot that retires an instance takes the next one from a
-// device-side queue (one fetch-and-add; no slot ever waits on another warp).
-#include <climits>
-#include "kernels.cuh"
+// k_batch.cu — batched persistent engine: the transient kernel and its launch.
+#include "batch_slot.cuh"
 
 namespace cedar {
-
-namespace {
-
-constexpr unsigned FULL = 0xffffffffu;
-constexpr int JOB_RUNNING = INT_MIN;  // job result while iterating
-constexpr int JOB_ZERO_PIVOT = 0;     // result of a zero pivot
-
-enum Resume : int {
-  RP_NEWINST, RP_DC0, RP_PTC, RP_PTCFIN, RP_SRC, RP_FIX, RP_ADA, RP_IDLE
-};
-
-template <int K>
-struct Slot {
-  // ---- lane geometry
-  unsigned smask;  // lanes of this slot
-  int rank;        // lane within the slot
-  // ---- instance
-  int inst;
-  const DTpl *T;
-  const double *dp;
-  WS w;
-  // ---- Newton job in flight
-  double *jx; const double *jhist; const double *jxref;
-  double jt, jcj, jsrc, jgs, jvlim;
-  int jit, jmaxit, jres;
-  bool jdc, active;
-  int rp;
-  // ---- DC homotopy
-  long long used; int pass, fails, halv; double gs, lam, dl, ln;
-  // ---- transient
-  EngStats st;
-  long long k, N, nsteps;
-  double t, tn1, tn2, h, h1, hnext, tnew, tprev, tprev2, cj;
-  int npts; bool hit, have_prev, has_pert;
-  Sink sk;
-  double ts_next;         // time of sample sk.next
-  double tb_cache;        // next source corner (see next_bp)
-  double nrel, nav, nai;  // Newton tolerances
-
-  // slot-level collectives (divergent phase: only this slot's lanes participate)
-  __device__ __forceinline__ void ssync() const { if (K > 1) __syncwarp(smask); }
-  __device__ __forceinline__ bool sany(bool p) const { return K == 1 ? p : (__any_sync(smask, p) != 0); }
-  __device__ __forceinline__ double smax(double v) const {
-#pragma unroll
-    for (int o = K / 2; o > 0; o >>= 1) { double u = __shfl_xor_sync(smask, v, o, K); v = u > v ? u : v; }
-    return v;
-  }
-  __device__ __forceinline__ double smin(double v) const {
-#pragma unroll
-    for (int o = K / 2; o > 0; o >>= 1) { double u = __shfl_xor_sync(smask, v, o, K); v = u < v ? u : v; }
-    return v;
-  }
-  __device__ double sratio(MaxRatio m) const {
-#pragma unroll
-    for (int o = K / 2; o > 0; o >>= 1) {
-      double n2 = __shfl_xor_sync(smask, m.num, o, K), d2 = __shfl_xor_sync(smask, m.den, o, K);
-      bool b2 = __shfl_xor_sync(smask, (int)m.bad, o, K) != 0;
-      m.merge(n2, d2, b2);
-    }
-    if (K > 1) {
-      m.num = __shfl_sync(smask, m.num, 0, K); m.den = __shfl_sync(smask, m.den, 0, K);
-      m.bad = __shfl_sync(smask, (int)m.bad, 0, K) != 0;
-    }
-    return m.value();
-  }
-  __device__ __forceinline__ void copy(double *d, const double *s) { for (int i = rank; i < T->n; i += K) d[i] = s[i]; }
-  __device__ __forceinline__ void fill(double *d, double v) { for (int i = rank; i < T->n; i += K) d[i] = v; }
-
-  __device__ __forceinline__ double gather(const int *ptr, const int *ent, int s, double acc) const {
-    int a = ptr[s], b = ptr[s + 1];
-    for (int q = a; q < b; ++q) { int e = ent[q]; double v = w.dout[e >> 1]; acc = (e & 1) ? acc - v : acc + v; }
-    return acc;
-  }
-
-  // charges at x into q (slot-level)
-  __device__ void eval_q(const double *x, double tt, double *q) {
-    const DTpl &TT = *T;
-    EvalCtx ctx{tt, 0.0, 1.0, TT.gmin, false, false};
-    for (int d = rank; d < TT.n_dev; d += K) {
-      int gi = 0;
-      while (d >= TT.dev_end[gi]) ++gi;
-      const DGroup gr = TT.grp[gi];
-      if (gr.model != CEDAR_C && gr.model != CEDAR_L) continue;
-      int i = d - (gi ? TT.dev_end[gi - 1] : 0);
-      const int *tm = TT.term + gr.term_off + i * gr.ntx;
-      double v[5];
-      for (int kk = 0; kk < gr.ntx; ++kk) { int u = tm[kk]; v[kk] = u < 0 ? 0.0 : x[u]; }
-      eval_device(gr.model, dp + gr.dpar_off + i, gr.n_inst, v, nullptr, ctx, TT.pwl, w.dout + gr.out_off + i * model_nout(gr.model));
-    }
-    ssync();
-    for (int r = rank; r < TT.n; r += K) q[r] = gather(TT.qint_ptr, TT.qint_ent, r, 0.0);
-    ssync();
-  }
-
-  // Next source corner after tt.  The value found at an earlier time t0 <= tt stays
-  // the answer while tt + eps is below it (no corner lies in between), so it is
-  // recomputed only after the step lands on it.
-  __device__ double next_bp(double tt, double eps) {
-    if (DADD(tt, eps) < tb_cache) return tb_cache;
-    double best = 1e300;
-    for (int s = rank; s < T->n_src; s += K) {
-      double b = source_next_bp(dp + T->src_off[s], T->src_stride[s], tt, eps, T->pwl);
-      best = b < best ? b : best;
-    }
-    tb_cache = smin(best);
-    return tb_cache;
-  }
-
-  __device__ void issue(double *x, const double *hist, const double *xref, double tt, double cjv, double src,
-                        double gsh, double vlim, bool dc, int maxit, int next_rp) {
-    jx = x; jhist = hist; jxref = xref; jt = tt; jcj = cjv; jsrc = src; jgs = gsh; jvlim = vlim; jdc = dc;
-    jmaxit = maxit; jit = 0; jres = JOB_RUNNING; active = true; rp = next_rp;
-    // time-varying source values are fixed for the whole Newton solve
-    for (int s = rank; s < T->n_src; s += K)
-      w.srcv[s] = source_value(dp + T->src_off[s], T->src_stride[s], tt, dc, T->pwl) * src;
-    ssync();
-  }
-
-  // ---- output sink (samples only); ts_next caches the time of sample sk.next
-  __device__ double sample_ts(int j) const {
-    return j == sk.ns - 1 ? sk.tstop : sk.tstart + (sk.tstop - sk.tstart) * ((double)j / (double)(sk.ns - 1));
-  }
-  __device__ void sink_start(const double *x) {
-    if (!sk.samp) return;
-    for (int p = rank; p < sk.np; p += K) { int u = sk.probes_int[p]; sk.samp[(long long)p * sk.ns] = u >= 0 ? x[u] : 0.0; }
-    sk.next = 1;
-    ts_next = sk.ns > 1 ? sample_ts(1) : 1e300;
-  }
-  __device__ void sink_step(bool have0, double t0, const double *x0, double t1, const double *x1, double t2, const double *x2) {
-    if (!sk.samp) return;
-    while (sk.next < sk.ns && ts_next <= t2) {
-      double tt = ts_next;
-      for (int p = rank; p < sk.np; p += K) {
-        int u = sk.probes_int[p]; double v;
-        if (u < 0) v = 0.0;
-        else if (have0) {
-          double L0 = (tt - t1) * (tt - t2) / ((t0 - t1) * (t0 - t2));
-          double L1 = (tt - t0) * (tt - t2) / ((t1 - t0) * (t1 - t2));
-          double L2 = (tt - t0) * (tt - t1) / ((t2 - t0) * (t2 - t1));
-          v = x0[u] * L0 + x1[u] * L1 + x2[u] * L2;
-        } else {
-          double a = (tt - t1) / (t2 - t1);
-          v = x1[u] + (x2[u] - x1[u]) * a;
-        }
-        sk.samp[(long long)p * sk.ns + sk.next] = v;
-      }
-      sk.next++;
-      ts_next = sk.next < sk.ns ? sample_ts(sk.next) : 1e300;
-    }
-  }
-
-  __device__ double restart_h(double tt, const EngOpts &o) {
-    double nb = next_bp(tt, (o.tstop - o.tstart) * 1e-12); nb = nb < o.tstop ? nb : o.tstop;
-    double dist = nb - tt; dist = dist < o.hmax ? dist : o.hmax;
-    double hf = o.hfirst_frac * dist;
-    if (o.h > 0) hf = o.h < hf ? o.h : hf;
-    return hf;
-  }
-
-  __device__ __forceinline__ int absr(int r) const { return r < 0 ? -r : r; }
-
-  // Advance this slot's state machine until it issues a Newton job or goes idle.
-  __device__ void resume(const BatchDev &b, double *ws) {
-    const EngOpts &o = b.opts;
-    const long long budget = 20000;
-    for (;;) {
-      switch (rp) {
-        case RP_IDLE:
-          active = false;
-          return;
-        case RP_NEWINST: {
-          int job = 0;
-          if (rank == 0) job = atomicAdd(b.head, 1);
-          job = K == 1 ? job : __shfl_sync(smask, job, 0, K);
-          if (job >= b.n_inst) { rp = RP_IDLE; active = false; return; }
-          inst = b.queue[job];
-          const int flags = b.rows ? b.rows[inst].flags : 0;
-          if (flags & ROW_FINISHED) continue;
-          const int ti = b.inst_tpl[inst];
-          T = &b.tpls[ti];
-          dp = b.dpar + b.inst_dpar[inst];
-          w.bind(ws, T->n, T->nnz_lu, T->n_out, T->n_src);
-          tb_cache = -1e300;
-          if (rank == 0) atomicAdd(b.n_running, 1);
-          if (flags & ROW_STARTED) {
-            // resume a run stopped at a window boundary
-            sk = Sink{};
-            sk.probes_int = b.probes_int ? b.probes_int + (size_t)ti * b.np : nullptr;
-            sk.np = b.np; sk.ns = b.ns;
-            sk.samp = (b.samples && b.np > 0 && b.ns > 0) ? b.samples + (size_t)inst * b.np * b.ns : nullptr;
-            sk.tstart = o.tstart; sk.tstop = o.tstop;
-            load_row(b);
-            if (o.adaptive) goto ada_begin;
-            goto fix_issue;
-          }
-          const long long xo = b.x0_off ? b.x0_off[inst] : -1;
-          for (int i = rank; i < T->n; i += K) w.x[i] = xo >= 0 ? b.x0[xo + T->order[i]] : 0.0;
-          const long long dxo = b.dx_off ? b.dx_off[inst] : -1;
-          has_pert = dxo >= 0;
-          if (has_pert) for (int i = rank; i < T->n; i += K) w.qt[i] = b.dx[dxo + T->order[i]];
-          sk = Sink{};
-          sk.probes_int = b.probes_int ? b.probes_int + (size_t)ti * b.np : nullptr;
-          sk.np = b.np; sk.ns = b.ns;
-          sk.samp = (b.samples && b.np > 0 && b.ns > 0) ? b.samples + (size_t)inst * b.np * b.ns : nullptr;
-          sk.tstart = o.tstart; sk.tstop = o.tstop;
-          st.accepted = st.rejected = st.newton_iters = st.dc_iters = 0;
-          st.hmin_seen = 1e300; st.hmax_seen = 0; st.status = CEDAR_ST_OK; st.pad = 0;
-          ssync();
-          if (o.dcop) {
-            copy(w.x0, w.x);
-            ssync();
-            used = 0;
-            issue(w.x, nullptr, nullptr, o.tstart, 0.0, 1.0, 0.0, 0.0, true, 100, RP_DC0);
-            return;
-          }
-          goto tran_init;
-        }
-        // ----------------------------------------------------------- DC homotopy
-        case RP_DC0:
-          used += absr(jres);
-          if (jres > 0) goto dc_ok;
-          pass = 0;
-          goto ptc_begin;
-        case RP_PTC:
-          used += absr(jres);
-          if (jres > 0) {
-            copy(w.xm1, w.xs);
-            ssync();
-            if (gs <= 1e-14) {
-              copy(w.x, w.xm1);
-              ssync();
-              issue(w.x, nullptr, nullptr, o.tstart, 0.0, 1.0, 0.0, pass == 0 ? 0.5 : 0.0, true, 100, RP_PTCFIN);
-              return;
-            }
-            gs *= 0.1;
-          } else { gs *= 4.0; ++fails; }
-          goto ptc_issue;
-        case RP_PTCFIN:
-          used += absr(jres);
-          if (jres > 0) goto dc_ok;
-          goto ptc_end;
-        case RP_SRC:
-          used += absr(jres);
-          if (jres > 0) { copy(w.x, w.xs); ssync(); lam = ln; halv = 0; dl = dl * 2 < 0.1 ? dl * 2 : 0.1; }
-          else { dl *= 0.5; if (++halv > 8) goto dc_fail; }
-          goto src_issue;
-        // ----------------------------------------------------------- transient
-        case RP_FIX: {
-          st.newton_iters += absr(jres);
-          if (jres <= 0) {
-            st.status = jres == 0 ? CEDAR_ST_ZERO_PIVOT : CEDAR_ST_NEWTON;
-            copy(w.x, w.xn); ssync();
-            goto retire;
-          }
-          double *xp = w.x;
-          eval_q(xp, t, w.qt);
-          for (int i = rank; i < T->n; i += K) {
-            if (o.method == CEDAR_TRAP) w.qd[i] = cj * w.qt[i] + w.hist[i];
-            w.qm1[i] = w.qn[i]; w.qn[i] = w.qt[i];
-          }
-          ssync();
-          sink_step(have_prev, tprev2, w.xm1, tprev, w.xn, t, xp);
-          ssync();
-          bool nf = false;
-          for (int i = rank; i < T->n; i += K) { w.xm1[i] = w.xn[i]; w.xn[i] = xp[i]; if (!(fabs(xp[i]) < 1e300)) nf = true; }
-          nf = sany(nf);
-          double hk = t - tprev;
-          tprev2 = tprev; tprev = t; have_prev = true;
-          st.accepted++; st.hmin_seen = hk < st.hmin_seen ? hk : st.hmin_seen; st.hmax_seen = hk > st.hmax_seen ? hk : st.hmax_seen;
-          if (nf) { st.status = CEDAR_ST_NAN; goto retire; }
-          ++k;
-          goto fix_issue;
-        }
-        case RP_ADA: {
-          st.newton_iters += absr(jres);
-          double *xp = w.x;
-          const int n = T->n;
-          if (jres <= 0) {
-            st.rejected++;
-            hnext = h * 0.125;
-            if (hnext < o.hmin) { st.status = jres == 0 ? CEDAR_ST_ZERO_PIVOT : CEDAR_ST_DT_UNDERFLOW; goto ada_end; }
-            goto ada_begin;
-          }
-          double err = 0.0;
-          if (npts >= 3) {
-            double h2 = tn1 - tn2;
-            double rh = 1.0 / h, rh1 = 1.0 / h1, rh2 = 1.0 / h2;
-            double ra = 1.0 / (h + h1), rb = 1.0 / (h1 + h2), rc = 1.0 / (h + h1 + h2);
-            double coef = h * h * (h + h1) * (h + h1) / (2.0 * h + h1);
-            MaxRatio mr;
-            for (int i = rank; i < n; i += K) {
-              if (!T->is_node[i]) continue;
-              double d10 = (xp[i] - w.xn[i]) * rh;
-              double d21 = (w.xn[i] - w.xm1[i]) * rh1;
-              double d32 = (w.xm1[i] - w.xm2[i]) * rh2;
-              double dd3 = ((d10 - d21) * ra - (d21 - d32) * rb) * rc;
-              double lte = fabs(dd3) * coef;
-              double ax = fabs(xp[i]), bx = fabs(w.xn[i]);
-              mr.add(lte, o.reltol * (ax > bx ? ax : bx) + o.abstol_v);
-            }
-            err = sratio(mr);
-          } else if (npts == 2) {
-            double rh = 1.0 / h, rh1 = 1.0 / h1, ra = 1.0 / (h + h1), hh = h * h;
-            MaxRatio mr;
-            for (int i = rank; i < n; i += K) {
-              if (!T->is_node[i]) continue;
-              double dd2 = ((xp[i] - w.xn[i]) * rh - (w.xn[i] - w.xm1[i]) * rh1) * ra;
-              double lte = fabs(dd2) * hh;
-              double ax = fabs(xp[i]), bx = fabs(w.xn[i]);
-              mr.add(lte, o.reltol * (ax > bx ? ax : bx) + o.abstol_v);
-            }
-            err = sratio(mr);
-          }
-          if (err > 1.0) {
-            st.rejected++;
-            hnext = h * step_factor(err);
-            if (hnext < o.hmin) { st.status = CEDAR_ST_DT_UNDERFLOW; goto ada_end; }
-            goto ada_begin;
-          }
-          eval_q(xp, tnew, w.qt);
-          for (int i = rank; i < n; i += K) { w.qm1[i] = w.qn[i]; w.qn[i] = w.qt[i]; }
-          ssync();
-          sink_step(npts >= 2, tn1, w.xm1, t, w.xn, tnew, xp);
-          ssync();
-          bool nf = false;
-          for (int i = rank; i < n; i += K) {
-            w.xm2[i] = w.xm1[i]; w.xm1[i] = w.xn[i]; w.xn[i] = xp[i];
-            if (!(fabs(xp[i]) < 1e300)) nf = true;
-          }
-          nf = sany(nf);
-          tn2 = tn1; tn1 = t; t = tnew;
-          st.accepted++; st.hmin_seen = h < st.hmin_seen ? h : st.hmin_seen; st.hmax_seen = h > st.hmax_seen ? h : st.hmax_seen;
-          if (nf) { st.status = CEDAR_ST_NAN; goto ada_end; }
-          if (npts < 3) ++npts;
-          double fac = (err > 0.0) ? step_factor(err) : 1.0;
-          hnext = h * fac;
-          if (hit && t < o.tstop) { npts = 1; hnext = restart_h(t, o); }
-          goto ada_begin;
-        }
-        default:
-          rp = RP_IDLE; active = false; return;
-      }
-
-      // ------------------------------------------------------------- shared tails
-    ptc_begin:
-      copy(w.xm1, w.x0);
-      ssync();
-      gs = 1e-2; fails = 0;
-    ptc_issue:
-      if (used < budget && fails <= 60) {
-        copy(w.xs, w.xm1);
-        ssync();
-        issue(w.xs, nullptr, w.xm1, o.tstart, 0.0, 1.0, gs, pass == 0 ? 0.5 : 0.0, true, 50, RP_PTC);
-        return;
-      }
-    ptc_end:
-      if (++pass < 2) goto ptc_begin;
-      fill(w.x, 0.0);
-      ssync();
-      lam = 0.0; dl = 0.1; halv = 0;
-    src_issue:
-      if (!(lam < 1.0)) goto dc_ok;
-      if (used >= budget) goto dc_fail;
-      ln = lam + dl < 1.0 ? lam + dl : 1.0;
-      copy(w.xs, w.x);
-      ssync();
-      issue(w.xs, nullptr, nullptr, o.tstart, 0.0, ln, 0.0, 0.0, true, 100, RP_SRC);
-      return;
-    dc_fail:
-      st.dc_iters += used;
-      st.status = CEDAR_ST_DCOP;
-      goto retire_x;
-    dc_ok:
-      st.dc_iters += used;
-    tran_init:
-      if (has_pert) { for (int i = rank; i < T->n; i += K) w.x[i] += w.qt[i]; ssync(); }
-      eval_q(w.x, o.tstart, w.qn);
-      copy(w.xn, w.x);
-      ssync();
-      sink_start(w.x);
-      if (rank == 0 && b.rows) b.rows[inst].flags = ROW_STARTED;
-      if (!o.adaptive) {
-        fill(w.qd, 0.0);
-        ssync();
-        tprev = tprev2 = o.tstart; have_prev = false;
-        N = llround((o.tstop - o.tstart) / o.h);
-        k = 1;
-        goto fix_issue;
-      }
-      t = tn1 = tn2 = o.tstart; npts = 1; nsteps = 0;
-      hnext = restart_h(t, o);
-      goto ada_begin;
-    fix_issue: {
-      if (k > N) goto retire;
-      if (tprev >= b.t_until) { save_row(b); rp = RP_NEWINST; continue; }
-      t = (k == N) ? o.tstop : DADD(o.tstart, DMUL((double)k, o.h));
-      double hk = t - tprev;
-      if (o.method == CEDAR_TRAP) {
-        cj = 2.0 / hk;
-        for (int i = rank; i < T->n; i += K) w.hist[i] = -cj * w.qn[i] - w.qd[i];
-      } else if (k == 1) {
-        cj = 1.0 / hk;
-        for (int i = rank; i < T->n; i += K) w.hist[i] = -w.qn[i] * cj;
-      } else {
-        cj = 1.5 / hk;
-        const double r2h = 0.5 / hk;
-        for (int i = rank; i < T->n; i += K) w.hist[i] = (-4.0 * w.qn[i] + w.qm1[i]) * r2h;
-      }
-      if (k == 1) copy(w.x, w.xn);
-      else for (int i = rank; i < T->n; i += K) w.x[i] = 2.0 * w.xn[i] - w.xm1[i];
-      ssync();
-      issue(w.x, w.hist, nullptr, t, cj, 1.0, 0.0, 0.0, false, o.max_newton, RP_FIX);
-      return;
-    }
-    ada_begin: {
-      if (!(t < o.tstop)) goto ada_end;
-      if (t >= b.t_until) { save_row(b); rp = RP_NEWINST; continue; }
-      if (++nsteps > o.max_steps) { st.status = CEDAR_ST_MAX_STEPS; goto ada_end; }
-      const double eps_bp = (o.tstop - o.tstart) * 1e-12;
-      double tb = next_bp(t, eps_bp); tb = tb < o.tstop ? tb : o.tstop;
-      h = hnext < o.hmax ? hnext : o.hmax;
-      hit = false;
-      if (tb - t <= 1.1 * h) { h = tb - t; hit = true; }
-      tnew = hit ? tb : t + h;
-      h = tnew - t;
-      h1 = t - tn1;
-      if (npts < 2) {
-        cj = 1.0 / h;
-        for (int i = rank; i < T->n; i += K) w.hist[i] = -w.qn[i] * cj;
-      } else {
-        double wr = h / h1, rh = 1.0 / h;
-        cj = (1.0 + 2.0 * wr) / ((1.0 + wr) * h);
-        double a1 = -(1.0 + wr), a2 = wr * wr / (1.0 + wr);
-        for (int i = rank; i < T->n; i += K) w.hist[i] = (a1 * w.qn[i] + a2 * w.qm1[i]) * rh;
-      }
-      if (npts >= 2) { double rr = h / h1; for (int i = rank; i < T->n; i += K) w.x[i] = w.xn[i] + rr * (w.xn[i] - w.xm1[i]); }
-      else copy(w.x, w.xn);
-      ssync();
-      issue(w.x, w.hist, nullptr, tnew, cj, 1.0, 0.0, 0.0, false, o.max_newton, RP_ADA);
-      return;
-    }
-    ada_end:
-      copy(w.x, w.xn);
-      ssync();
-      if (st.status == CEDAR_ST_OK && t < o.tstop) st.status = CEDAR_ST_MAX_STEPS;
-      goto retire_x;
-    retire:
-      copy(w.x, w.xn);
-      ssync();
-    retire_x:
-      if (b.x_final)
-        for (int i = rank; i < T->n; i += K) b.x_final[(size_t)inst * b.n_max + T->order[i]] = w.x[i];
-      if (rank == 0 && b.stats) b.stats[inst] = st;
-      if (rank == 0 && b.rows) b.rows[inst].flags = ROW_STARTED | ROW_FINISHED;
-      if (rank == 0) atomicSub(b.n_running, 1);
-      ssync();
-      rp = RP_NEWINST;
-    }
-  }
-
-  // ---- window boundaries: integrator state to / from the instance's state row
-  __device__ void save_row(const BatchDev &b) {
-    double *v = b.row_vec + (size_t)inst * 6 * b.n_max;
-    const int n = T->n;
-    for (int i = rank; i < n; i += K) {
-      v[i] = w.xn[i]; v[b.n_max + i] = w.xm1[i]; v[2 * b.n_max + i] = w.xm2[i];
-      v[3 * b.n_max + i] = w.qn[i]; v[4 * b.n_max + i] = w.qm1[i]; v[5 * b.n_max + i] = w.qd[i];
-    }
-    if (rank == 0) {
-      StateRow &r = b.rows[inst];
-      r.t = t; r.tn1 = tn1; r.tn2 = tn2; r.hnext = hnext; r.tprev = tprev; r.tprev2 = tprev2;
-      r.k = k; r.nsteps = nsteps; r.st = st; r.npts = npts; r.have_prev = have_prev ? 1 : 0;
-      r.next_sample = sk.next; r.flags = ROW_STARTED;
-      if (b.stats) b.stats[inst] = st;
-    }
-    ssync();
-  }
-  __device__ void load_row(const BatchDev &b) {
-    const double *v = b.row_vec + (size_t)inst * 6 * b.n_max;
-    const int n = T->n;
-    for (int i = rank; i < n; i += K) {
-      w.xn[i] = v[i]; w.xm1[i] = v[b.n_max + i]; w.xm2[i] = v[2 * b.n_max + i];
-      w.qn[i] = v[3 * b.n_max + i]; w.qm1[i] = v[4 * b.n_max + i]; w.qd[i] = v[5 * b.n_max + i];
-    }
-    const StateRow &r = b.rows[inst];
-    t = r.t; tn1 = r.tn1; tn2 = r.tn2; hnext = r.hnext; tprev = r.tprev; tprev2 = r.tprev2;
-    k = r.k; nsteps = r.nsteps; st = r.st; npts = r.npts; have_prev = r.have_prev != 0;
-    sk.next = r.next_sample;
-    ts_next = (sk.samp && sk.next < sk.ns) ? sample_ts(sk.next) : 1e300;
-    N = llround((b.opts.tstop - b.opts.tstart) / b.opts.h);
-    ssync();
-  }
-};
-
-}  // namespace
-
-// One Newton iteration for every active slot of the warp (warp-collective over
-// the active lanes `am`).  Loops that contain barriers run to the warp-wide
-// maximum trip count so that every lane meets every barrier.
-template <int K>
-__device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am) {
-  const DTpl &T = *s.T;
-  const int rank = s.rank;
-  const int it = s.jit + 1;
-  // K1: device evaluation
-  {
-    EvalCtx ctx{s.jt, s.jcj, s.jsrc, T.gmin, s.jdc, false};
-    const double *x = s.jx;
-    for (int d = rank; d < T.n_dev; d += K) {
-      int gi = 0;
-      while (d >= T.dev_end[gi]) ++gi;
-      const DGroup gr = T.grp[gi];
-      int i = d - (gi ? T.dev_end[gi - 1] : 0);
-      const int *tm = T.term + gr.term_off + i * gr.ntx;
-      double v[5];
-      for (int kk = 0; kk < gr.ntx; ++kk) { int u = tm[kk]; v[kk] = u < 0 ? 0.0 : x[u]; }
-      double *out = s.w.dout + gr.out_off + i * model_nout(gr.model);
-      const int si = (gr.model == CEDAR_V || gr.model == CEDAR_I) ? T.src_of_dev[d] : -1;
-      if (si >= 0) eval_source_value(gr.model, s.dp + gr.dpar_off + i, v, s.w.srcv[si], out);
-      else eval_device(gr.model, s.dp + gr.dpar_off + i, gr.n_inst, v, nullptr, ctx, T.pwl, out);
-    }
-  }
-  __syncwarp(am);
-  // K2: stamping (fixed-order gathers)
-  for (int q = rank; q < T.nnz_lu; q += K) s.w.lu[q] = s.gather(T.jlu_ptr, T.jlu_ent, q, 0.0);
-  for (int r = rank; r < T.n; r += K) s.w.F[r] = s.gather(T.fint_ptr, T.fint_ent, r, s.jhist ? s.jhist[r] : 0.0);
-  __syncwarp(am);
-  if (s.jgs != 0.0) {
-    for (int u = rank; u < T.n_nodes; u += K) {
-      int c = T.gs_col[u];
-      s.w.lu[T.gs_slot[u]] -= s.jgs;
-      s.w.F[T.gs_row[u]] -= s.jgs * (s.jx[c] - (s.jxref ? s.jxref[c] : 0.0));
-    }
-  }
-  __syncwarp(am);
-  // K4: LU by levels
-  bool bad = false;
-  const int nl_lu = __reduce_max_sync(am, T.lu_nlev);
-  for (int l = 0; l < nl_lu; ++l) {
-    if (l < T.lu_nlev) {
-      int t1 = T.lu_lvl[l + 1];
-      for (int t = T.lu_lvl[l] + rank; t < t1; t += K) {
-        int q = T.lu_slot[t], info = T.lu_info[t];
-        double acc = s.w.lu[q];
-        for (int p = T.lu_pp[t]; p < T.lu_pp[t + 1]; ++p) { int2 pr = T.lu_pair[p]; acc -= s.w.lu[pr.x] * s.w.lu[pr.y]; }
-        int kind = info & 3, j = info >> 2;
-        if (kind == 2) acc *= s.w.rd[j];
-        else if (kind == 1) {
-          if (!pivot_ok(acc)) bad = true;
-          s.w.rd[j] = pivot_rcp(acc);
-        }
-        s.w.lu[q] = acc;
-      }
-    }
-    __syncwarp(am);
-  }
-  const unsigned bal_bad = __ballot_sync(am, bad);
-  const bool slot_bad = (bal_bad & s.smask) != 0;
-  // K5: substitutions (skipped by slots with a zero pivot; bounds stay uniform)
-  double *b = s.w.F;
-  const int nl_fw = __reduce_max_sync(am, T.fw_nlev);
-  for (int l = 0; l < nl_fw; ++l) {
-    if (!slot_bad && l < T.fw_nlev) {
-      for (int t = T.fw_lvl[l] + rank; t < T.fw_lvl[l + 1]; t += K) {
-        int i = T.fw_row[t]; double acc = b[i];
-        for (int p = T.fw_ptr[t]; p < T.fw_ptr[t + 1]; ++p) { int2 pr = T.fw_pair[p]; acc -= s.w.lu[pr.x] * b[pr.y]; }
-        b[i] = acc;
-      }
-    }
-    __syncwarp(am);
-  }
-  const int nl_bw = __reduce_max_sync(am, T.bw_nlev);
-  for (int l = 0; l < nl_bw; ++l) {
-    if (!slot_bad && l < T.bw_nlev) {
-      for (int t = T.bw_lvl[l] + rank; t < T.bw_lvl[l + 1]; t += K) {
-        int i = T.bw_row[t]; double acc = b[i];
-        for (int p = T.bw_ptr[t]; p < T.bw_ptr[t + 1]; ++p) { int2 pr = T.bw_pair[p]; acc -= s.w.lu[pr.x] * b[pr.y]; }
-        b[i] = acc * s.w.rd[i];
-      }
-    }
-    __syncwarp(am);
-  }
-  // K6: finiteness, DC damping, update, convergence vote
-  // magnitudes are compared as integers (the bit patterns of non-negative doubles
-  // order like the values), keeping these tests off the FP64 pipe
-  bool nonfinite = false; long long mxb = 0;
-  const bool damp = s.jvlim > 0;
-  if (!slot_bad) {
-    for (int i = rank; i < T.n; i += K) {
-      long long ab = abs_bits(b[i]);
-      if (ab >= 0x7e37e43c8800759cLL) nonfinite = true;  // |d| >= 1e300 or NaN
-      if (damp && T.is_node[i]) mxb = ab > mxb ? ab : mxb;
-    }
-  }
-  const bool slot_nf = (__ballot_sync(am, nonfinite) & s.smask) != 0;
-  double scale = 1.0;
-  if (__any_sync(am, damp)) {
-#pragma unroll
-    for (int o = K / 2; o > 0; o >>= 1) { long long u = __shfl_xor_sync(am, mxb, o, K); mxb = u > mxb ? u : mxb; }
-    const double mx = __longlong_as_double(mxb);
-    if (damp && mx > s.jvlim) scale = s.jvlim / mx;
-  }
-  bool conv = (scale == 1.0);
-  if (!slot_bad && !slot_nf) {
-    for (int i = rank; i < T.n; i += K) {
-      double d = -b[i] * scale;
-      double xi = s.jx[i] + d;
-      s.jx[i] = xi;
-      double lim = s.nrel * fabs(xi) + (T.is_node[i] ? s.nav : s.nai);
-      if (abs_bits(d) > abs_bits(lim)) conv = false;
-    }
-  }
-  const bool slot_notconv = (__ballot_sync(am, !conv) & s.smask) != 0;
-  __syncwarp(am);
-  s.jit = it;
-  if (slot_bad) s.jres = JOB_ZERO_PIVOT;
-  else if (slot_nf) s.jres = -it;
-  else if (!slot_notconv) s.jres = it;
-  else if (it >= s.jmaxit) s.jres = -s.jmaxit;
-  if (s.jres != JOB_RUNNING) s.active = false;
-}
 
 template <int K>
 __global__ void __launch_bounds__(256, 1) batch_kernel(BatchDev b) {

@@ -32,7 +32,35 @@ struct BatchDev {
   struct StateRow *rows;         // [n_inst]
   double *row_vec;               // [n_inst * 6 * n_max]: xn xm1 xm2 qn qm1 qd
   int *n_running;                // instances left unfinished by this launch
+  // adjoint tape (forward recording; tape_t == null: off).  Per instance
+  // tape_cap + 1 entries (entry 0 = the start point, entry k = accepted step k)
+  // of time, order (1 = BE, 2 = BDF2), supply power and probe value, and every
+  // ckpt_every steps a checkpoint (x_k, x_{k-1}) in internal order.
+  double *tape_t; signed char *tape_ord; double *tape_p, *tape_v;
+  long long tape_cap;
+  double *ckpt; int ckpt_every;
+  const int4 *obj_idx;           // [n_templates] internal (vnode, ibranch, probe, 0)
 };
+
+// slice helpers of the adjoint tape
+__host__ __device__ inline long long tape_stride(long long cap) { return cap + 1; }
+__host__ __device__ inline long long ckpt_count(long long cap, int every) { return cap / every + 1; }
+
+// Discrete adjoint launch (k_adjoint.cu): replays each instance's recorded steps
+// segment by segment from its checkpoints and sweeps the adjoint backwards.
+struct AdjObj { int iv, ib, ip, pad; double level, w_energy, w_delay, w_final; };  // internal indices
+struct AdjDev {
+  BatchDev b;                    // templates, parameters, tape, queue, options
+  const long long *raw_off; const double *raw;   // raw parameter blocks (W, r)
+  const AdjObj *obj;             // [n_templates]
+  const double *tstar;           // [n_inst]
+  double *phi;                   // [n_inst]
+  double *grad; int np_max;      // [n_inst * np_max]
+  int *status;                   // [n_inst]
+  double *segx;                  // [n_inst * (ckpt_every + 1) * n_max] replayed states
+  const EngStats *fwd;           // forward stats (steps taken, status)
+};
+cudaError_t launch_adjoint(const AdjDev &a, int K, int warps_per_cta, int grid, size_t smem, cudaStream_t s);
 
 struct StateRow {
   double t, tn1, tn2, hnext, tprev, tprev2;

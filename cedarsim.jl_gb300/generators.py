@@ -148,6 +148,31 @@ def mc_chains(n_inst: int = 4096, seed: int = 20240607, workload: int = 3,
     return templates, lsel.astype(np.int32), np.concatenate(blocks), offs
 
 
+# ---------------------------------------------------------------- workload 5
+ADJ_LENGTHS = list(range(31, 64, 2))   # 62..126 transistor widths per instance
+ADJ_LEVEL = 0.9                        # 50 % of VDD
+ADJ_W_ENERGY = 1e15                    # J -> fJ
+ADJ_W_DELAY = 1e24                     # s^2 -> ps^2
+
+
+def adjoint_chains(n_inst: int = 512, seed: int = 20240607, workload: int = 5, lengths: List[int] = ADJ_LENGTHS):
+    """Monte Carlo chains for the discrete adjoint: the chains of mc_chains with
+    L in {31, 33, .., 63}, the per-template objective (supply energy through VDD +
+    squared error of the last output's first 50 % crossing against t*) and a seeded
+    target t* per instance: L * 20 ps * U(0.8, 1.2), drawn from stream(i, 0, 2).
+
+    Returns (templates, inst_template, inst_par, inst_par_off, objectives, tstar) with
+    objectives[k] = (vnode, ibranch, probe, level, w_energy, w_delay, w_final)."""
+    templates, itpl, par, off = mc_chains(n_inst, seed=seed, workload=workload, lengths=lengths)
+    st = Stream(seed, workload)
+    u = st.uniform(np.arange(n_inst), 0, 2)
+    L = np.array(lengths)[itpl]
+    tstar = L * 20e-12 * (0.8 + 0.4 * u)
+    objectives = [(f.index("vdd"), f.index("VDD.I"), chain_output_probe(f), ADJ_LEVEL, ADJ_W_ENERGY, ADJ_W_DELAY, 0.0)
+                  for f in templates]
+    return templates, itpl, par, off, objectives, tstar
+
+
 # ---------------------------------------------------------------- workload 4
 RING = dict(stages=15, vdd=1.8, vbn=1.0, vbp=0.8, rsup=100.0, csup=100e-15, cload=5e-15)
 

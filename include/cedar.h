@@ -324,6 +324,39 @@ int cedar_batch_autotune(cedar_batch *b, const cedar_tran_opts *opts, double hor
                          cedar_batch_tuning *best);
 int cedar_batch_nmax(const cedar_batch *b, int32_t *n_max);
 
+/* ---- discrete adjoint ------------------------------------------------------
+ * Replaces the reference's parameter sensitivities of a transient
+ * (ODEForwardSensitivityProblem + extract_local_sensitivities,
+ * test/sensitivity.jl:13-42) with the gradient of a scalar objective
+ * (cedar_objective) by the discrete adjoint, for every instance of a batch.
+ *
+ * cedar_adjoint_run runs the batch forward (adaptive BDF2 only, no inst_dx)
+ * recording each instance's accepted steps on a device tape (tape_cap steps per
+ * instance, <= 0: 2^19; an instance needing more ends with CEDAR_ST_MAX_STEPS)
+ * with a state checkpoint every 64 steps, then sweeps backwards: each 64-step
+ * segment is recomputed from its checkpoint, and J_k^T lam_k = -(dPhi/dx_k +
+ * C^T (b1 lam_{k+1} + b2 lam_{k+2})) is solved with J_k factorised at the
+ * step's solution (transposed substitutions), down to the DC operating point.
+ * The gradient lam^T dFi/dp covers every MOS1 width W and resistor value r, per
+ * template in group order (cedar_adjoint_nparams gives the counts).
+ *   obj[n_templates]       objective per template (original unknown indices)
+ *   tstar[n_inst]          target crossing time per instance (NULL: 0)
+ *   phi[n_inst]            objective value
+ *   grad[n_inst * np_max]  gradient (entries past the template's count are 0)
+ *   status[n_inst]         CEDAR_ST_* of the instance (forward or backward)
+ *   stats[n_inst]          forward counters
+ * Every output may be NULL.  Results of failed instances are NaN. */
+int cedar_adjoint_run(cedar_batch *b, const cedar_tran_opts *opts, const cedar_objective *obj,
+                      const double *tstar, int64_t tape_cap, double *phi, double *grad,
+                      int32_t *status, cedar_stats *stats);
+int cedar_adjoint_nparams(const cedar_batch *b, int32_t *np_per_template, int32_t *np_max);
+/* The step sequence the last adjoint run recorded for one instance: times and
+ * orders (1 = BE, 2 = BDF2) of its accepted steps (at most cap of them), for
+ * finite-difference checks that replay the same steps. */
+int cedar_adjoint_tape(cedar_batch *b, int32_t inst, double *t, int8_t *ord, int64_t cap, int64_t *n_steps);
+/* Device time of the last adjoint run's forward and backward kernels. */
+int cedar_adjoint_last_ms(cedar_batch *b, double *fwd_ms, double *bwd_ms);
+
 #ifdef __cplusplus
 }
 #endif
