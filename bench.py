@@ -37,7 +37,6 @@ sys.path.insert(0, ROOT)
 METRIC = "MC transient inst-steps/s, batched vs plain GPU @1e-6 reltol; adjoint grads/s"
 UNIT = "instance-timesteps/s"
 TSTOP = 20e-9
-FP64_PEAK_TFLOPS = 1.2557  # measured DFMA throughput on this GB300 pool (profiles/fp64_peak.md)
 
 
 def parse():
@@ -57,6 +56,11 @@ def parse():
     p.add_argument("--plain-inst", type=int, default=4)
     p.add_argument("--plain-tstop", type=float, default=2e-9)
     p.add_argument("--tstop-ns", type=float, default=20.0, help="transient length (20 ns for the headline)")
+    p.add_argument("--fp64-probe", action="store_true", help="print the FP64 issue-rate probe (1, 8, 32 lanes) and exit")
+    p.add_argument("--no-adjoint", action="store_true")
+    p.add_argument("--adj-inst", type=int, default=512, help="instances of the adjoint workload")
+    p.add_argument("--adj-tstop-ns", type=float, default=20.0)
+    p.add_argument("--adj-ref-inst", type=int, default=16, help="instances in the CPU adjoint sample")
     return p.parse_args()
 
 
@@ -167,6 +171,34 @@ def barrier(dist):
         dist.barrier()
 
 
+def adjoint_workload(pkg, args):
+    templates, itpl, par, off, objs, tstar = pkg.generators.adjoint_chains(args.adj_inst, seed=args.seed)
+    objectives = [pkg.abi.Objective(int(a), int(b), int(c), 0, float(l), float(we), float(wd), float(wf))
+                  for (a, b, c, l, we, wd, wf) in objs]
+    return templates, itpl, par, off, objectives, tstar
+
+
+ADJ_WORKLOAD = ("512 MC chains L in {31..63}, supply energy + 50% crossing delay objective, "
+                "adaptive BDF2 to 20 ns, checkpoint every 64 steps, gradient w.r.t. every MOSFET width")
+
+
+def reference_adjoint(args, pkg, orc):
+    """The oracle's adjoint (OpenMP over instances) on a bounded random sample."""
+    templates, itpl, par, off, objectives, tstar = adjoint_workload(pkg, args)
+    k = max(1, min(args.adj_ref_inst, args.adj_inst))
+    sel = np.sort(np.random.default_rng(5).choice(args.adj_inst, size=k, replace=False))
+    sub = pkg.abi.BatchHolder(templates, itpl[sel], par, off[sel])
+    cores = os.cpu_count() or 1
+    o = opts_for(pkg, args.adj_tstop_ns * 1e-9)
+    t0 = time.perf_counter()
+    phi, g, st = orc.adjoint_batch(sub, o, objectives, tstar[sel], nthreads=cores)
+    dt = time.perf_counter() - t0
+    ok = int((st == 0).sum())
+    return {"value": ok / dt, "unit": "instance-gradients/s", "cores": cores, "kind": "port",
+            "sample": f"{k} randomly chosen instances of the {args.adj_inst}, each forward 0..{args.adj_tstop_ns:g} ns + replay + adjoint",
+            "seconds": dt, "failed": k - ok}
+
+
 def run_reference(args, pkg):
     """CPU restatement of the path (the oracle) on a bounded sample per step."""
     import __graft_entry__ as ge
@@ -189,7 +221,8 @@ def run_reference(args, pkg):
             total_time += dt
     v = total_steps / total_time
     sample = f"{args.steps} x {k} randomly chosen instances of the {args.n_inst}, each run 0..20 ns (DC op included)"
-    return {"metric": METRIC, "impl": "reference", "value": v, "unit": UNIT, "n_gpus": args.gpus,
+    adj = None if args.no_adjoint else reference_adjoint(args, pkg, orc)
+    return {"metric": METRIC, "impl": "reference", "value": v, "unit": UNIT, "n_gpus": args.gpus, "adjoint": adj,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_time / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded Philox4x32-10)",
@@ -208,8 +241,21 @@ def main():
             print(json.dumps(run_reference(args, pkg)), flush=True)
         return
     import torch
-    pkg.load_library()
+    lib0 = pkg.load_library()
     torch.cuda.init()
+    import ctypes as C
+    if args.fp64_probe:
+        out = {}
+        for lanes in (32, 8, 1):
+            gf, ms = C.c_double(), C.c_double()
+            pkg.abi.check(lib0.cedar_fp64_probe(lanes, 4096, C.byref(gf), C.byref(ms)))
+            out[str(lanes)] = {"useful_gflops": gf.value, "ms": ms.value}
+        print(json.dumps({"fp64_probe": out}), flush=True)
+        return
+    # FP64 peak measured live on this GPU (all lanes active): the roofline denominator
+    gf = C.c_double()
+    pkg.abi.check(lib0.cedar_fp64_probe(32, 4096, C.byref(gf), None))
+    fp64_peak = gf.value / 1e3
     templates, itpl, par, off, probes = workload(pkg, args.n_inst, args.seed)
     mine = shard(itpl, templates, rank, world)
     n_samples = 201
@@ -222,7 +268,6 @@ def main():
     edges = [tstop * (k + 1) / nwin for k in range(nwin)]
     edges[-1] = tstop
     lib = sw.lib
-    import ctypes as C
     pkg.abi.check(lib.cedar_batch_start(sw.handle, C.byref(o)))
     nrun = C.c_int32()
     # warm-up windows (DC operating points happen in the first)
@@ -297,19 +342,41 @@ def main():
             f = g.instance_flat(templates[itpl[i]], par[off[i]:off[i] + templates[itpl[i]].param_block().size])
             s0 = pkg.System(f)
             t0 = time.perf_counter()
-            sol = pkg.tran(s0, (0.0, args.plain_tstop), method="bdf2", cap=4)
+            sol = pkg.tran(s0, (0.0, args.plain_tstop), method="bdf2", cap=1 << 17)
             tt += time.perf_counter() - t0
             acc += sol.stats["accepted"]
         plain = {"value": acc / tt, "unit": UNIT, "sample": f"{args.plain_inst} random instances, each one "
                  f"cedar_tran_run (one CTA) from DC to {args.plain_tstop * 1e9:g} ns", "seconds": tt}
+    # discrete adjoint (workload 5) through the C ABI
+    adj = None
+    if not args.no_adjoint:
+        t5, i5, p5, o5_off, obj5, ts5 = adjoint_workload(pkg, args)
+        sw5 = pkg.Sweep(t5, i5, p5, o5_off)
+        if args.lanes:
+            sw5.set_tuning(args.lanes, args.warps or 4)
+        sw5.adjoint(opts_for(pkg, 0.05e-9), obj5, ts5)          # warm-up
+        r5 = sw5.adjoint(opts_for(pkg, args.adj_tstop_ns * 1e-9), obj5, ts5)
+        ok5 = r5.status == 0
+        secs = (r5.fwd_ms + r5.bwd_ms) / 1e3
+        per, npm = sw5.nparams()
+        adj = {"metric": "adjoint gradients/s", "value": float(ok5.sum()) / secs, "unit": "instance-gradients/s",
+               "param_derivatives_per_s": float(per[i5][ok5].sum()) / secs, "fwd_ms": r5.fwd_ms, "bwd_ms": r5.bwd_ms,
+               "failed_instances": int((~ok5).sum()), "workload": ADJ_WORKLOAD, "n_inst": args.adj_inst,
+               "params_per_instance": [int(per.min()), int(per.max())],
+               "accepted_steps_mean": float(r5.stats["accepted"].mean()), "tuning": list(sw5.tuning),
+               "timing": "CUDA events around the recording forward and the backward kernel"}
+        del sw5
     cpu = None
     if not args.no_cpu_baseline:
         cpu_line = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
-                                   "--steps", "1", "--warmup", "0", "--ref-inst", "64"],
+                                   "--steps", "1", "--warmup", "0", "--ref-inst", "64"]
+                                  + (["--no-adjoint"] if args.no_adjoint else []),
                                   capture_output=True, text=True, timeout=900)
         try:
             ref = json.loads(cpu_line.stdout.strip().splitlines()[-1])
             cpu = ref["cpu_baseline"]
+            if adj is not None and ref.get("adjoint"):
+                adj["cpu_baseline"] = ref["adjoint"]
         except Exception:
             cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                    "sample": "failed: " + cpu_line.stderr[-300:]}
@@ -323,11 +390,12 @@ def main():
                    "parallelism": f"instances sharded over {world} GPU(s), no collective"},
         "newton_iters_per_s": iters_all / dt, "failed_instances": bad, "host_wall_s": wall,
         "launch_ms": dev_ms,
-        "roofline": {"bound": "fp64", "achieved": achieved, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
-                     "frac": achieved / FP64_PEAK_TFLOPS, "traffic": None,
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp64_peak, "traffic": None,
                      "note": "algorithmic FP64 flops per Newton iteration (cedar_ckt_costs) x iterations / time; "
-                             "peak = measured DFMA rate (no FP64 entry in MEASURED_PEAKS.json)"},
-        "cpu_baseline": cpu, "e2e": e2e, "plain_gpu": plain, "clocks": clk, "gpu_launches": args.steps,
+                             "peak = DFMA rate measured in this run by cedar_fp64_probe (MEASURED_PEAKS.json "
+                             "has no FP64 entry); the kernel keeps its state on chip, so HBM is not its bound"},
+        "cpu_baseline": cpu, "e2e": e2e, "plain_gpu": plain, "adjoint": adj, "clocks": clk, "gpu_launches": args.steps,
     }
     print(json.dumps(line), flush=True)
 

@@ -163,6 +163,7 @@ EXPORTS = [
     "cedar_batch_results", "cedar_batch_last_ms", "cedar_batch_set_tuning",
     "cedar_batch_get_tuning", "cedar_batch_autotune", "cedar_batch_nmax",
     "cedar_adjoint_run", "cedar_adjoint_nparams", "cedar_adjoint_tape", "cedar_adjoint_last_ms",
+    "cedar_fp64_probe",
 ]
 
 _lib = None
@@ -217,6 +218,7 @@ def load_library(build_if_missing: bool = True):
         "cedar_adjoint_nparams": (C.c_int, [P, c_int32_p, c_int32_p]),
         "cedar_adjoint_tape": (C.c_int, [P, C.c_int32, c_double_p, P, C.c_int64, c_int64_p]),
         "cedar_adjoint_last_ms": (C.c_int, [P, c_double_p, c_double_p]),
+        "cedar_fp64_probe": (C.c_int, [C.c_int32, C.c_int32, c_double_p, c_double_p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -140,7 +140,8 @@ def _stats_dict(st) -> dict:
 
 
 def dc(circuit: Union[Circuit, Flat, System], t: float = 0.0, x0: Optional[np.ndarray] = None):
-    """DC operating point (CedarDCOp): Newton, then source stepping, then gmin stepping."""
+    """DC operating point (CedarDCOp's role): Newton, then pseudo-transient continuation, then
+    source stepping; rerun with dense partial pivoting if the static pivot order fails."""
     sys = circuit if isinstance(circuit, System) else System(circuit)
     x = np.zeros(sys.n) if x0 is None else np.ascontiguousarray(x0, np.float64).copy()
     st = Stats()

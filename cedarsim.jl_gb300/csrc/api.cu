@@ -96,6 +96,30 @@ int upload_template(const cedar_ckt_desc *desc, std::unique_ptr<DevTemplate> &ou
   size_t o_tf_lvl = P.vec(H.tf_lvl_ptr), o_tf_row = P.vec(H.tf_row), o_tf_ptr = P.vec(H.tf_ptr), o_tf_pair = P.vec(tf_pair);
   size_t o_tb_lvl = P.vec(H.tb_lvl_ptr), o_tb_row = P.vec(H.tb_row), o_tb_ptr = P.vec(H.tb_ptr), o_tb_pair = P.vec(tb_pair);
   size_t o_ct_ptr = P.vec(H.ct_ptr), o_ct_ent = P.vec(ct_ent), o_adj_goff = P.vec(H.adj_goff);
+  std::vector<int> mg_grp;
+  int mg_ptr[CEDAR_NMODELS + 1] = {0};
+  for (int m = 0; m < CEDAR_NMODELS; ++m) {
+    mg_ptr[m] = (int)mg_grp.size();
+    for (size_t g = 0; g < H.groups.size(); ++g) if (H.groups[g].model == m) mg_grp.push_back((int)g);
+  }
+  mg_ptr[CEDAR_NMODELS] = (int)mg_grp.size();
+  size_t o_mg_grp = P.vec(mg_grp);
+  std::vector<int> eq_of_pos(H.n);
+  for (int e = 0; e < H.n; ++e) eq_of_pos[H.eq_pos[e]] = e;
+  std::vector<int2> lu_orig(std::max(H.nnz_lu, 1));
+  for (int p = 0; p < H.n; ++p)
+    for (int k = H.lu_rowptr[p]; k < H.lu_rowptr[p + 1]; ++k) lu_orig[k] = make_int2(eq_of_pos[p], H.order[H.lu_colidx[k]]);
+  size_t o_lu_orig = P.vec(lu_orig);
+  std::vector<int4> lu_task(std::max<size_t>(H.lu_task_slot.size(), 1));
+  for (size_t t = 0; t < H.lu_task_slot.size(); ++t)
+    lu_task[t] = make_int4(H.lu_task_slot[t], H.lu_task_info[t], H.lu_pair_ptr[t], H.lu_pair_ptr[t + 1]);
+  auto row_tasks = [](const std::vector<int32_t> &row, const std::vector<int32_t> &ptr) {
+    std::vector<int4> v(std::max<size_t>(row.size(), 1));
+    for (size_t t = 0; t < row.size(); ++t) v[t] = make_int4(row[t], ptr[t], ptr[t + 1], 0);
+    return v;
+  };
+  size_t o_lu_task = P.vec(lu_task), o_fw_task = P.vec(row_tasks(H.fw_row, H.fw_ptr)), o_bw_task = P.vec(row_tasks(H.bw_row, H.bw_ptr));
+  size_t o_tf_task = P.vec(row_tasks(H.tf_row, H.tf_ptr)), o_tb_task = P.vec(row_tasks(H.tb_row, H.tb_ptr));
   CUDA_TRY(cudaMalloc(&dt->buf, P.bytes.size()));
   CUDA_TRY(cudaMemcpy(dt->buf, P.bytes.data(), P.bytes.size(), cudaMemcpyHostToDevice));
   char *b = (char *)dt->buf;
@@ -124,6 +148,11 @@ int upload_template(const cedar_ckt_desc *desc, std::unique_ptr<DevTemplate> &ou
   D.tf_lvl = (const int *)(b + o_tf_lvl); D.tf_row = (const int *)(b + o_tf_row); D.tf_ptr = (const int *)(b + o_tf_ptr); D.tf_pair = (const int2 *)(b + o_tf_pair);
   D.tb_lvl = (const int *)(b + o_tb_lvl); D.tb_row = (const int *)(b + o_tb_row); D.tb_ptr = (const int *)(b + o_tb_ptr); D.tb_pair = (const int2 *)(b + o_tb_pair);
   D.ct_ptr = (const int *)(b + o_ct_ptr); D.ct_ent = (const int2 *)(b + o_ct_ent); D.adj_goff = (const int *)(b + o_adj_goff);
+  for (int m = 0; m <= CEDAR_NMODELS; ++m) D.mg_ptr[m] = mg_ptr[m];
+  D.mg_grp = (const int *)(b + o_mg_grp);
+  D.lu_orig = (const int2 *)(b + o_lu_orig);
+  D.lu_task = (const int4 *)(b + o_lu_task); D.fw_task = (const int4 *)(b + o_fw_task); D.bw_task = (const int4 *)(b + o_bw_task);
+  D.tf_task = (const int4 *)(b + o_tf_task); D.tb_task = (const int4 *)(b + o_tb_task);
   CUDA_TRY(cudaMalloc(&dt->D_dev, sizeof(DTpl)));
   CUDA_TRY(cudaMemcpy(dt->D_dev, &D, sizeof(DTpl), cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMalloc(&dt->par_dev, std::max<size_t>(1, H.par.size()) * sizeof(double)));
@@ -178,7 +207,7 @@ template <class T> struct DevBuf {
 struct cedar_ckt {
   std::unique_ptr<DevTemplate> tpl;
   cudaStream_t stream = nullptr;
-  DevBuf<double> dpar, x, xdot, F, J, dout, hist, ws, tout, xout;
+  DevBuf<double> dpar, x, xdot, F, J, dout, hist, ws, tout, xout, dense;
   DevBuf<EngStats> stats;
   DevBuf<long long> count;
   DevBuf<long long> off;
@@ -191,9 +220,10 @@ struct cedar_batch {
   std::vector<std::unique_ptr<DevTemplate>> tpls;
   cudaStream_t stream = nullptr;
   DevBuf<DTpl> d_tpls;
-  DevBuf<int> inst_tpl, queue, head, probes_int;
+  DevBuf<int> inst_tpl, queue, head, probes_int, qblk_beg, qblk_head;
+  int n_qblk = 0;
   DevBuf<long long> raw_off, dpar_off, x0_off, dx_off;
-  DevBuf<double> raw, dpar, x0, dx, samples, xfinal, ws;
+  DevBuf<double> raw, dpar, x0, dx, samples, xfinal, ws, dense_ws;
   DevBuf<EngStats> stats;
   DevBuf<StateRow> rows;
   DevBuf<double> row_vec;
@@ -403,6 +433,10 @@ static int run_plain(cedar_ckt *c, int mode, const cedar_tran_opts *opts, double
   size_t n = H.n;
   PlainArgs a{};
   a.T = c->tpl->D_dev; a.dpar = c->dpar.p; a.x = c->x.p; a.t = t; a.cj = cj; a.mode = mode;
+  if (n <= 1024) {  // dense DC fallback scratch: (n + 2) n doubles
+    CUDA_TRY(c->dense.ensure((n + 2) * n));
+    a.dense = c->dense.p;
+  }
   cedar_tran_opts od; cedar_tran_opts_default(&od);
   if (opts) od = *opts; else { od.tstart = 0; od.tstop = 1; }
   a.opts = to_eng(&od);
@@ -541,6 +575,13 @@ int cedar_batch_create(const cedar_batch_desc *d, cedar_batch **out) {
     return itpl[a] < itpl[c];
   });
   if ((rc = up(b->queue, q))) return rc;
+  // template blocks of the queue
+  std::vector<int> qb;
+  for (int i = 0; i < ni; ++i) if (i == 0 || itpl[q[i]] != itpl[q[i - 1]]) qb.push_back(i);
+  qb.push_back(ni);
+  b->n_qblk = (int)qb.size() - 1;
+  if ((rc = up(b->qblk_beg, qb))) return rc;
+  CUDA_TRY(b->qblk_head.ensure(std::max(b->n_qblk, 1)));
   CUDA_TRY(b->head.ensure(1));
   CUDA_TRY(b->n_running.ensure(1));
   CUDA_TRY(b->rows.ensure(std::max(ni, 1)));
@@ -548,7 +589,7 @@ int cedar_batch_create(const cedar_batch_desc *d, cedar_batch **out) {
   CUDA_TRY(b->stats.ensure(std::max(ni, 1)));
   CUDA_TRY(b->xfinal.ensure((size_t)std::max(ni, 1) * b->n_max));
   if (b->np) CUDA_TRY(b->samples.ensure((size_t)std::max(ni, 1) * b->np * b->ns));
-  b->tune.lanes_per_inst = 8; b->tune.warps_per_cta = 4;
+  b->tune.lanes_per_inst = 32; b->tune.warps_per_cta = 4;  // best of the measured sweep on GB300
   CUDA_TRY(cudaStreamSynchronize(b->stream));
   *out = b.release();
   return 0;
@@ -599,6 +640,10 @@ static int launch_geometry(int K, int warps, int stride, int n_inst, bool &in_sm
   return 0;
 }
 
+// Largest circuit whose batched DC operating point may fall back to dense
+// partial pivoting ((n + 2) n doubles of scratch per resident slot).
+constexpr int kDenseNmax = 256;
+
 static int batch_launch(cedar_batch *b, const EngOpts &eo, const cedar_batch_tuning &tu, bool want_outputs,
                         double t_until, bool fresh, const BatchDev *tape = nullptr, BatchDev *used = nullptr) {
   int K = tu.lanes_per_inst, warps = tu.warps_per_cta;
@@ -606,8 +651,21 @@ static int batch_launch(cedar_batch *b, const EngOpts &eo, const cedar_batch_tun
   bool in_smem = false; size_t smem = 0; int grid = 1;
   int rc = launch_geometry(K, warps, b->ws_stride, b->n_inst, in_smem, smem, grid);
   if (rc) return rc;
+  {
+    // a persistent grid of exactly the CTAs that can be resident at once
+    int per_sm = 1, dev = 0, nsm = 0;
+    CUDA_TRY(configure_batch(K, warps, smem, &per_sm));
+    CUDA_TRY(cudaGetDevice(&dev));
+    CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    grid = std::max(1, std::min(nsm * per_sm, (b->n_inst + tiles - 1) / tiles));
+  }
   if (!in_smem) CUDA_TRY(b->ws.ensure((size_t)grid * tiles * b->ws_stride));
+  // dense DC fallback scratch (circuits of at most kDenseNmax unknowns)
+  const long long dstride = ((long long)(b->n_max + 2) * b->n_max + 31) / 32 * 32;
+  const bool dense_ok = b->n_max <= kDenseNmax;
+  if (dense_ok) CUDA_TRY(b->dense_ws.ensure((size_t)grid * tiles * dstride));
   BatchDev bd{};
+  bd.dense_ws = dense_ok ? b->dense_ws.p : nullptr; bd.dense_stride = dstride; bd.dense_nmax = kDenseNmax;
   bd.tpls = b->d_tpls.p; bd.inst_tpl = b->inst_tpl.p; bd.inst_dpar = b->dpar_off.p; bd.dpar = b->dpar.p;
   bd.x0_off = b->has_x0 ? b->x0_off.p : nullptr; bd.x0 = b->x0.p;
   bd.dx_off = b->has_dx ? b->dx_off.p : nullptr; bd.dx = b->dx.p;
@@ -615,6 +673,7 @@ static int batch_launch(cedar_batch *b, const EngOpts &eo, const cedar_batch_tun
   bd.samples = want_outputs ? b->samples.p : nullptr;
   bd.x_final = want_outputs ? b->xfinal.p : nullptr; bd.n_max = b->n_max;
   bd.stats = b->stats.p; bd.queue = b->queue.p; bd.head = b->head.p; bd.n_inst = b->n_inst;
+  bd.qblk_beg = b->qblk_beg.p; bd.qblk_head = b->qblk_head.p; bd.n_qblk = b->n_qblk;
   bd.opts = eo; bd.ws_stride = b->ws_stride; bd.ws_global = b->ws.p; bd.ws_in_smem = in_smem ? 1 : 0;
   bd.t_until = t_until; bd.rows = b->rows.p; bd.row_vec = b->row_vec.p; bd.n_running = b->n_running.p;
   if (tape) {
@@ -623,6 +682,7 @@ static int batch_launch(cedar_batch *b, const EngOpts &eo, const cedar_batch_tun
   }
   if (used) *used = bd;
   CUDA_TRY(cudaMemsetAsync(b->head.p, 0, sizeof(int), b->stream));
+  CUDA_TRY(cudaMemsetAsync(b->qblk_head.p, 0, std::max(b->n_qblk, 1) * sizeof(int), b->stream));
   CUDA_TRY(cudaMemsetAsync(b->n_running.p, 0, sizeof(int), b->stream));
   if (fresh) {
     CUDA_TRY(cudaMemsetAsync(b->rows.p, 0, (size_t)b->n_inst * sizeof(StateRow), b->stream));
@@ -763,6 +823,7 @@ int cedar_adjoint_run(cedar_batch *b, const cedar_tran_opts *opts, const cedar_o
   a.phi = b->adj_phi.p; a.grad = b->adj_grad.p; a.np_max = np_max; a.status = b->adj_status.p;
   a.segx = b->segx.p; a.fwd = b->stats.p;
   CUDA_TRY(cudaMemsetAsync(b->head.p, 0, sizeof(int), b->stream));
+  CUDA_TRY(cudaMemsetAsync(b->qblk_head.p, 0, std::max(b->n_qblk, 1) * sizeof(int), b->stream));
   if (!b->ev2) CUDA_TRY(cudaEventCreate(&b->ev2));
   CUDA_TRY(launch_adjoint(a, K, warps, grid, smem, b->stream));
   CUDA_TRY(cudaEventRecord(b->ev2, b->stream));
@@ -798,6 +859,12 @@ int cedar_adjoint_last_ms(cedar_batch *b, double *fwd_ms, double *bwd_ms) {
   CUDA_TRY(cudaEventElapsedTime(&g, b->ev1, b->ev2));
   if (fwd_ms) *fwd_ms = f;
   if (bwd_ms) *bwd_ms = g;
+  return 0;
+}
+
+int cedar_fp64_probe(int32_t active_lanes, int32_t iters, double *gflops, double *ms) {
+  if (active_lanes < 1 || active_lanes > 32 || iters < 1) return fail(CEDAR_EINVAL, "active_lanes 1..32, iters >= 1");
+  CUDA_TRY(launch_fp64_probe(active_lanes, iters, gflops, ms));
   return 0;
 }
 

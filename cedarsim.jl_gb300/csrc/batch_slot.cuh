@@ -26,6 +26,32 @@ namespace cedar {
 namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
+
+// Visit the devices of a template model by model, in a fixed model order, so
+// that the lanes of a warp evaluate one model at a time whatever templates its
+// slots run (the model switch in eval_device is then uniform across the warp).
+// fn(gr, i, d): group, instance within the group, device index.  Collective over
+// the lanes in `mask`; charges_only restricts the walk to capacitors and inductors.
+template <int K, class Fn>
+__device__ __forceinline__ void for_devices_by_model(const DTpl &T, int rank, unsigned mask, bool charges_only, Fn &&fn) {
+  for (int m = 1; m < CEDAR_NMODELS; ++m) {
+    if (charges_only && m != CEDAR_C && m != CEDAR_L) continue;
+    const int g0 = T.mg_ptr[m], ng = T.mg_ptr[m + 1] - g0;
+    const int ngmax = __reduce_max_sync(mask, ng);
+    for (int q = 0; q < ngmax; ++q) {
+      const int gi = q < ng ? T.mg_grp[g0 + q] : -1;
+      DGroup gr{};
+      if (gi >= 0) gr = T.grp[gi];
+      const int cnt = gi >= 0 ? gr.n_inst : 0;
+      const int rounds = __reduce_max_sync(mask, (cnt + K - 1) / K);
+      const int dbase = gi > 0 ? T.dev_end[gi - 1] : 0;
+      for (int r = 0; r < rounds; ++r) {
+        const int i = rank + r * K;
+        if (i < cnt) fn(gr, i, dbase + i);
+      }
+    }
+  }
+}
 constexpr int JOB_RUNNING = INT_MIN;  // job result while iterating
 constexpr int JOB_ZERO_PIVOT = 0;     // result of a zero pivot
 
@@ -35,9 +61,12 @@ enum Resume : int {
 
 template <int K>
 struct Slot {
-  // ---- lane geometry
-  unsigned smask;  // lanes of this slot
-  int rank;        // lane within the slot
+  // ---- lane geometry (per lane, from the thread index: the Slot object itself
+  // lives in shared memory, one copy per slot, written identically by its lanes)
+  __device__ __forceinline__ int rank() const { return (int)(threadIdx.x & (K - 1)); }
+  __device__ __forceinline__ unsigned smask() const {
+    return K == 32 ? FULL : (((1u << K) - 1u) << ((threadIdx.x & 31) & ~(K - 1)));
+  }
   // ---- instance
   int inst;
   const DTpl *T;
@@ -56,39 +85,41 @@ struct Slot {
   long long k, N, nsteps;
   double t, tn1, tn2, h, h1, hnext, tnew, tprev, tprev2, cj;
   int npts; bool hit, have_prev, has_pert;
+  int gsi, qblk;          // global slot index; queue block (template) last drawn from
+  bool dense, jdense;     // DC homotopy rerun with dense partial pivoting; the job's mode
   Sink sk;
   double ts_next;         // time of sample sk.next
   double tb_cache;        // next source corner (see next_bp)
   double nrel, nav, nai;  // Newton tolerances
 
   // slot-level collectives (divergent phase: only this slot's lanes participate)
-  __device__ __forceinline__ void ssync() const { if (K > 1) __syncwarp(smask); }
-  __device__ __forceinline__ bool sany(bool p) const { return K == 1 ? p : (__any_sync(smask, p) != 0); }
+  __device__ __forceinline__ void ssync() const { if (K > 1) __syncwarp(smask()); }
+  __device__ __forceinline__ bool sany(bool p) const { return K == 1 ? p : (__any_sync(smask(), p) != 0); }
   __device__ __forceinline__ double smax(double v) const {
 #pragma unroll
-    for (int o = K / 2; o > 0; o >>= 1) { double u = __shfl_xor_sync(smask, v, o, K); v = u > v ? u : v; }
+    for (int o = K / 2; o > 0; o >>= 1) { double u = __shfl_xor_sync(smask(), v, o, K); v = u > v ? u : v; }
     return v;
   }
   __device__ __forceinline__ double smin(double v) const {
 #pragma unroll
-    for (int o = K / 2; o > 0; o >>= 1) { double u = __shfl_xor_sync(smask, v, o, K); v = u < v ? u : v; }
+    for (int o = K / 2; o > 0; o >>= 1) { double u = __shfl_xor_sync(smask(), v, o, K); v = u < v ? u : v; }
     return v;
   }
   __device__ double sratio(MaxRatio m) const {
 #pragma unroll
     for (int o = K / 2; o > 0; o >>= 1) {
-      double n2 = __shfl_xor_sync(smask, m.num, o, K), d2 = __shfl_xor_sync(smask, m.den, o, K);
-      bool b2 = __shfl_xor_sync(smask, (int)m.bad, o, K) != 0;
+      double n2 = __shfl_xor_sync(smask(), m.num, o, K), d2 = __shfl_xor_sync(smask(), m.den, o, K);
+      bool b2 = __shfl_xor_sync(smask(), (int)m.bad, o, K) != 0;
       m.merge(n2, d2, b2);
     }
     if (K > 1) {
-      m.num = __shfl_sync(smask, m.num, 0, K); m.den = __shfl_sync(smask, m.den, 0, K);
-      m.bad = __shfl_sync(smask, (int)m.bad, 0, K) != 0;
+      m.num = __shfl_sync(smask(), m.num, 0, K); m.den = __shfl_sync(smask(), m.den, 0, K);
+      m.bad = __shfl_sync(smask(), (int)m.bad, 0, K) != 0;
     }
     return m.value();
   }
-  __device__ __forceinline__ void copy(double *d, const double *s) { for (int i = rank; i < T->n; i += K) d[i] = s[i]; }
-  __device__ __forceinline__ void fill(double *d, double v) { for (int i = rank; i < T->n; i += K) d[i] = v; }
+  __device__ __forceinline__ void copy(double *d, const double *s) { for (int i = rank(); i < T->n; i += K) d[i] = s[i]; }
+  __device__ __forceinline__ void fill(double *d, double v) { for (int i = rank(); i < T->n; i += K) d[i] = v; }
 
   __device__ __forceinline__ double gather(const int *ptr, const int *ent, int s, double acc) const {
     int a = ptr[s], b = ptr[s + 1];
@@ -100,19 +131,14 @@ struct Slot {
   __device__ void eval_q(const double *x, double tt, double *q) {
     const DTpl &TT = *T;
     EvalCtx ctx{tt, 0.0, 1.0, TT.gmin, false, false};
-    for (int d = rank; d < TT.n_dev; d += K) {
-      int gi = 0;
-      while (d >= TT.dev_end[gi]) ++gi;
-      const DGroup gr = TT.grp[gi];
-      if (gr.model != CEDAR_C && gr.model != CEDAR_L) continue;
-      int i = d - (gi ? TT.dev_end[gi - 1] : 0);
+    for_devices_by_model<K>(TT, rank(), smask(), true, [&](const DGroup &gr, int i, int) {
       const int *tm = TT.term + gr.term_off + i * gr.ntx;
       double v[5];
       for (int kk = 0; kk < gr.ntx; ++kk) { int u = tm[kk]; v[kk] = u < 0 ? 0.0 : x[u]; }
       eval_device(gr.model, dp + gr.dpar_off + i, gr.n_inst, v, nullptr, ctx, TT.pwl, w.dout + gr.out_off + i * model_nout(gr.model));
-    }
+    });
     ssync();
-    for (int r = rank; r < TT.n; r += K) q[r] = gather(TT.qint_ptr, TT.qint_ent, r, 0.0);
+    for (int r = rank(); r < TT.n; r += K) q[r] = gather(TT.qint_ptr, TT.qint_ent, r, 0.0);
     ssync();
   }
 
@@ -122,7 +148,7 @@ struct Slot {
   __device__ double next_bp(double tt, double eps) {
     if (DADD(tt, eps) < tb_cache) return tb_cache;
     double best = 1e300;
-    for (int s = rank; s < T->n_src; s += K) {
+    for (int s = rank(); s < T->n_src; s += K) {
       double b = source_next_bp(dp + T->src_off[s], T->src_stride[s], tt, eps, T->pwl);
       best = b < best ? b : best;
     }
@@ -133,9 +159,9 @@ struct Slot {
   __device__ void issue(double *x, const double *hist, const double *xref, double tt, double cjv, double src,
                         double gsh, double vlim, bool dc, int maxit, int next_rp) {
     jx = x; jhist = hist; jxref = xref; jt = tt; jcj = cjv; jsrc = src; jgs = gsh; jvlim = vlim; jdc = dc;
-    jmaxit = maxit; jit = 0; jres = JOB_RUNNING; active = true; rp = next_rp;
+    jmaxit = maxit; jit = 0; jres = JOB_RUNNING; active = true; rp = next_rp; jdense = dense;
     // time-varying source values are fixed for the whole Newton solve
-    for (int s = rank; s < T->n_src; s += K)
+    for (int s = rank(); s < T->n_src; s += K)
       w.srcv[s] = source_value(dp + T->src_off[s], T->src_stride[s], tt, dc, T->pwl) * src;
     ssync();
   }
@@ -146,7 +172,7 @@ struct Slot {
   }
   __device__ void sink_start(const double *x) {
     if (!sk.samp) return;
-    for (int p = rank; p < sk.np; p += K) { int u = sk.probes_int[p]; sk.samp[(long long)p * sk.ns] = u >= 0 ? x[u] : 0.0; }
+    for (int p = rank(); p < sk.np; p += K) { int u = sk.probes_int[p]; sk.samp[(long long)p * sk.ns] = u >= 0 ? x[u] : 0.0; }
     sk.next = 1;
     ts_next = sk.ns > 1 ? sample_ts(1) : 1e300;
   }
@@ -154,7 +180,7 @@ struct Slot {
     if (!sk.samp) return;
     while (sk.next < sk.ns && ts_next <= t2) {
       double tt = ts_next;
-      for (int p = rank; p < sk.np; p += K) {
+      for (int p = rank(); p < sk.np; p += K) {
         int u = sk.probes_int[p]; double v;
         if (u < 0) v = 0.0;
         else if (have0) {
@@ -183,6 +209,33 @@ struct Slot {
 
   __device__ __forceinline__ int absr(int r) const { return r < 0 ? -r : r; }
 
+  // Next instance for this slot, or -1 when every block is drained.  The queue
+  // holds one block per template (largest templates first); a slot keeps drawing
+  // from the block it drew from last, so the slots of a warp tend to run the same
+  // template and execute the same task lists in lockstep.  A slot's first draw
+  // comes from the block holding queue position gsi.  At most n_qblk attempts.
+  __device__ int dequeue(const BatchDev &b) {
+    int inst_next = -1;
+    if (rank() == 0) {
+      if (qblk < 0) {
+        const int p = gsi < b.n_inst ? gsi : b.n_inst - 1;
+        int lo = 0, hi = b.n_qblk;
+        while (hi - lo > 1) { int mid = (lo + hi) >> 1; if (b.qblk_beg[mid] <= p) lo = mid; else hi = mid; }
+        qblk = lo;
+      }
+      for (int t = 0; t < b.n_qblk; ++t) {
+        int j = qblk + t;
+        if (j >= b.n_qblk) j -= b.n_qblk;
+        const int cnt = b.qblk_beg[j + 1] - b.qblk_beg[j];
+        if (*((volatile int *)&b.qblk_head[j]) >= cnt) continue;
+        const int pos = atomicAdd(&b.qblk_head[j], 1);
+        if (pos < cnt) { qblk = j; inst_next = b.queue[b.qblk_beg[j] + pos]; break; }
+      }
+    }
+    if (K > 1) { inst_next = __shfl_sync(smask(), inst_next, 0, K); qblk = __shfl_sync(smask(), qblk, 0, K); }
+    return inst_next;
+  }
+
   // Variable-step BE (o2 false) or BDF2 step of length h after a step h1: sets cj,
   // the history w.hist (Fq space) and the predictor w.x from w.xn, w.xm1, w.qn,
   // w.qm1.  Shared by the transient and the adjoint's replay of recorded steps,
@@ -190,15 +243,15 @@ struct Slot {
   __device__ void prepare_step(bool o2, double h, double h1) {
     if (!o2) {
       cj = 1.0 / h;
-      for (int i = rank; i < T->n; i += K) w.hist[i] = -w.qn[i] * cj;
+      for (int i = rank(); i < T->n; i += K) w.hist[i] = -w.qn[i] * cj;
       copy(w.x, w.xn);
     } else {
       double wr = h / h1, rh = 1.0 / h;
       cj = (1.0 + 2.0 * wr) / ((1.0 + wr) * h);
       double a1 = -(1.0 + wr), a2 = wr * wr / (1.0 + wr);
-      for (int i = rank; i < T->n; i += K) w.hist[i] = (a1 * w.qn[i] + a2 * w.qm1[i]) * rh;
+      for (int i = rank(); i < T->n; i += K) w.hist[i] = (a1 * w.qn[i] + a2 * w.qm1[i]) * rh;
       double rr = h / h1;
-      for (int i = rank; i < T->n; i += K) w.x[i] = w.xn[i] + rr * (w.xn[i] - w.xm1[i]);
+      for (int i = rank(); i < T->n; i += K) w.x[i] = w.xn[i] + rr * (w.xn[i] - w.xm1[i]);
     }
     ssync();
   }
@@ -213,11 +266,9 @@ struct Slot {
           active = false;
           return;
         case RP_NEWINST: {
-          int job = 0;
-          if (rank == 0) job = atomicAdd(b.head, 1);
-          job = K == 1 ? job : __shfl_sync(smask, job, 0, K);
-          if (job >= b.n_inst) { rp = RP_IDLE; active = false; return; }
-          inst = b.queue[job];
+          const int job = dequeue(b);
+          if (job < 0) { rp = RP_IDLE; active = false; return; }
+          inst = job;
           const int flags = b.rows ? b.rows[inst].flags : 0;
           if (flags & ROW_FINISHED) continue;
           const int ti = b.inst_tpl[inst];
@@ -225,7 +276,8 @@ struct Slot {
           dp = b.dpar + b.inst_dpar[inst];
           w.bind(ws, T->n, T->nnz_lu, T->n_out, T->n_src);
           tb_cache = -1e300;
-          if (rank == 0) atomicAdd(b.n_running, 1);
+          dense = false;
+          if (rank() == 0) atomicAdd(b.n_running, 1);
           if (flags & ROW_STARTED) {
             // resume a run stopped at a window boundary
             sk = Sink{};
@@ -238,10 +290,11 @@ struct Slot {
             goto fix_issue;
           }
           const long long xo = b.x0_off ? b.x0_off[inst] : -1;
-          for (int i = rank; i < T->n; i += K) w.x[i] = xo >= 0 ? b.x0[xo + T->order[i]] : 0.0;
+          for (int i = rank(); i < T->n; i += K) w.x[i] = xo >= 0 ? b.x0[xo + T->order[i]] : 0.0;
           const long long dxo = b.dx_off ? b.dx_off[inst] : -1;
           has_pert = dxo >= 0;
-          if (has_pert) for (int i = rank; i < T->n; i += K) w.qt[i] = b.dx[dxo + T->order[i]];
+          // the perturbation waits in qn (first written after the DC operating point)
+          if (has_pert) for (int i = rank(); i < T->n; i += K) w.qn[i] = b.dx[dxo + T->order[i]];
           sk = Sink{};
           sk.probes_int = b.probes_int ? b.probes_int + (size_t)ti * b.np : nullptr;
           sk.np = b.np; sk.ns = b.ns;
@@ -298,7 +351,7 @@ struct Slot {
           }
           double *xp = w.x;
           eval_q(xp, t, w.qt);
-          for (int i = rank; i < T->n; i += K) {
+          for (int i = rank(); i < T->n; i += K) {
             if (o.method == CEDAR_TRAP) w.qd[i] = cj * w.qt[i] + w.hist[i];
             w.qm1[i] = w.qn[i]; w.qn[i] = w.qt[i];
           }
@@ -306,7 +359,7 @@ struct Slot {
           sink_step(have_prev, tprev2, w.xm1, tprev, w.xn, t, xp);
           ssync();
           bool nf = false;
-          for (int i = rank; i < T->n; i += K) { w.xm1[i] = w.xn[i]; w.xn[i] = xp[i]; if (!(fabs(xp[i]) < 1e300)) nf = true; }
+          for (int i = rank(); i < T->n; i += K) { w.xm1[i] = w.xn[i]; w.xn[i] = xp[i]; if (!(fabs(xp[i]) < 1e300)) nf = true; }
           nf = sany(nf);
           double hk = t - tprev;
           tprev2 = tprev; tprev = t; have_prev = true;
@@ -332,7 +385,7 @@ struct Slot {
             double ra = 1.0 / (h + h1), rb = 1.0 / (h1 + h2), rc = 1.0 / (h + h1 + h2);
             double coef = h * h * (h + h1) * (h + h1) / (2.0 * h + h1);
             MaxRatio mr;
-            for (int i = rank; i < n; i += K) {
+            for (int i = rank(); i < n; i += K) {
               if (!T->is_node[i]) continue;
               double d10 = (xp[i] - w.xn[i]) * rh;
               double d21 = (w.xn[i] - w.xm1[i]) * rh1;
@@ -346,7 +399,7 @@ struct Slot {
           } else if (npts == 2) {
             double rh = 1.0 / h, rh1 = 1.0 / h1, ra = 1.0 / (h + h1), hh = h * h;
             MaxRatio mr;
-            for (int i = rank; i < n; i += K) {
+            for (int i = rank(); i < n; i += K) {
               if (!T->is_node[i]) continue;
               double dd2 = ((xp[i] - w.xn[i]) * rh - (w.xn[i] - w.xm1[i]) * rh1) * ra;
               double lte = fabs(dd2) * hh;
@@ -362,12 +415,12 @@ struct Slot {
             goto ada_begin;
           }
           eval_q(xp, tnew, w.qt);
-          for (int i = rank; i < n; i += K) { w.qm1[i] = w.qn[i]; w.qn[i] = w.qt[i]; }
+          for (int i = rank(); i < n; i += K) { w.qm1[i] = w.qn[i]; w.qn[i] = w.qt[i]; }
           ssync();
           sink_step(npts >= 2, tn1, w.xm1, t, w.xn, tnew, xp);
           ssync();
           bool nf = false;
-          for (int i = rank; i < n; i += K) {
+          for (int i = rank(); i < n; i += K) {
             w.xm2[i] = w.xm1[i]; w.xm1[i] = w.xn[i]; w.xn[i] = xp[i];
             if (!(fabs(xp[i]) < 1e300)) nf = true;
           }
@@ -413,17 +466,29 @@ struct Slot {
       return;
     dc_fail:
       st.dc_iters += used;
+      if (!dense && b.dense_ws && T->n <= b.dense_nmax) {
+        // The static pivot order can be numerically useless at a DC point (e.g. a
+        // MOSFET output node whose only conductance is gmin next to a large gm):
+        // rerun the whole homotopy from the initial guess with dense partial
+        // pivoting, as the oracle factorises.
+        dense = true;
+        copy(w.x, w.x0);
+        ssync();
+        used = 0;
+        issue(w.x, nullptr, nullptr, o.tstart, 0.0, 1.0, 0.0, 0.0, true, 100, RP_DC0);
+        return;
+      }
       st.status = CEDAR_ST_DCOP;
       goto retire_x;
     dc_ok:
       st.dc_iters += used;
     tran_init:
-      if (has_pert) { for (int i = rank; i < T->n; i += K) w.x[i] += w.qt[i]; ssync(); }
+      if (has_pert) { for (int i = rank(); i < T->n; i += K) w.x[i] += w.qn[i]; ssync(); }
       eval_q(w.x, o.tstart, w.qn);
       copy(w.xn, w.x);
       ssync();
       sink_start(w.x);
-      if (rank == 0 && b.rows) b.rows[inst].flags = ROW_STARTED;
+      if (rank() == 0 && b.rows) b.rows[inst].flags = ROW_STARTED;
       if (!o.adaptive) {
         fill(w.qd, 0.0);
         ssync();
@@ -443,17 +508,17 @@ struct Slot {
       double hk = t - tprev;
       if (o.method == CEDAR_TRAP) {
         cj = 2.0 / hk;
-        for (int i = rank; i < T->n; i += K) w.hist[i] = -cj * w.qn[i] - w.qd[i];
+        for (int i = rank(); i < T->n; i += K) w.hist[i] = -cj * w.qn[i] - w.qd[i];
       } else if (k == 1) {
         cj = 1.0 / hk;
-        for (int i = rank; i < T->n; i += K) w.hist[i] = -w.qn[i] * cj;
+        for (int i = rank(); i < T->n; i += K) w.hist[i] = -w.qn[i] * cj;
       } else {
         cj = 1.5 / hk;
         const double r2h = 0.5 / hk;
-        for (int i = rank; i < T->n; i += K) w.hist[i] = (-4.0 * w.qn[i] + w.qm1[i]) * r2h;
+        for (int i = rank(); i < T->n; i += K) w.hist[i] = (-4.0 * w.qn[i] + w.qm1[i]) * r2h;
       }
       if (k == 1) copy(w.x, w.xn);
-      else for (int i = rank; i < T->n; i += K) w.x[i] = 2.0 * w.xn[i] - w.xm1[i];
+      else for (int i = rank(); i < T->n; i += K) w.x[i] = 2.0 * w.xn[i] - w.xm1[i];
       ssync();
       issue(w.x, w.hist, nullptr, t, cj, 1.0, 0.0, 0.0, false, o.max_newton, RP_FIX);
       return;
@@ -484,10 +549,10 @@ struct Slot {
       ssync();
     retire_x:
       if (b.x_final)
-        for (int i = rank; i < T->n; i += K) b.x_final[(size_t)inst * b.n_max + T->order[i]] = w.x[i];
-      if (rank == 0 && b.stats) b.stats[inst] = st;
-      if (rank == 0 && b.rows) b.rows[inst].flags = ROW_STARTED | ROW_FINISHED;
-      if (rank == 0) atomicSub(b.n_running, 1);
+        for (int i = rank(); i < T->n; i += K) b.x_final[(size_t)inst * b.n_max + T->order[i]] = w.x[i];
+      if (rank() == 0 && b.stats) b.stats[inst] = st;
+      if (rank() == 0 && b.rows) b.rows[inst].flags = ROW_STARTED | ROW_FINISHED;
+      if (rank() == 0) atomicSub(b.n_running, 1);
       ssync();
       rp = RP_NEWINST;
     }
@@ -499,7 +564,7 @@ struct Slot {
     if (k > b.tape_cap) return false;
     ssync();
     const int4 oi = b.obj_idx[b.inst_tpl[inst]];
-    if (rank == 0) {
+    if (rank() == 0) {
       const long long e = (long long)inst * tape_stride(b.tape_cap) + k;
       b.tape_t[e] = tk; b.tape_ord[e] = (signed char)ord;
       b.tape_p[e] = -(w.xn[oi.x] * w.xn[oi.y]);
@@ -508,7 +573,7 @@ struct Slot {
     if (k % b.ckpt_every == 0) {
       double *c = b.ckpt + ((long long)inst * ckpt_count(b.tape_cap, b.ckpt_every) + k / b.ckpt_every) * 2 * b.n_max;
       const double *prev = k == 0 ? w.xn : w.xm1;
-      for (int i = rank; i < T->n; i += K) { c[i] = w.xn[i]; c[b.n_max + i] = prev[i]; }
+      for (int i = rank(); i < T->n; i += K) { c[i] = w.xn[i]; c[b.n_max + i] = prev[i]; }
     }
     return true;
   }
@@ -517,11 +582,11 @@ struct Slot {
   __device__ void save_row(const BatchDev &b) {
     double *v = b.row_vec + (size_t)inst * 6 * b.n_max;
     const int n = T->n;
-    for (int i = rank; i < n; i += K) {
+    for (int i = rank(); i < n; i += K) {
       v[i] = w.xn[i]; v[b.n_max + i] = w.xm1[i]; v[2 * b.n_max + i] = w.xm2[i];
       v[3 * b.n_max + i] = w.qn[i]; v[4 * b.n_max + i] = w.qm1[i]; v[5 * b.n_max + i] = w.qd[i];
     }
-    if (rank == 0) {
+    if (rank() == 0) {
       StateRow &r = b.rows[inst];
       r.t = t; r.tn1 = tn1; r.tn2 = tn2; r.hnext = hnext; r.tprev = tprev; r.tprev2 = tprev2;
       r.k = k; r.nsteps = nsteps; r.st = st; r.npts = npts; r.have_prev = have_prev ? 1 : 0;
@@ -533,7 +598,7 @@ struct Slot {
   __device__ void load_row(const BatchDev &b) {
     const double *v = b.row_vec + (size_t)inst * 6 * b.n_max;
     const int n = T->n;
-    for (int i = rank; i < n; i += K) {
+    for (int i = rank(); i < n; i += K) {
       w.xn[i] = v[i]; w.xm1[i] = v[b.n_max + i]; w.xm2[i] = v[2 * b.n_max + i];
       w.qn[i] = v[3 * b.n_max + i]; w.qm1[i] = v[4 * b.n_max + i]; w.qd[i] = v[5 * b.n_max + i];
     }
@@ -552,20 +617,82 @@ struct Slot {
 // One Newton iteration for every active slot of the warp (warp-collective over
 // the active lanes `am`).  Loops that contain barriers run to the warp-wide
 // maximum trip count so that every lane meets every barrier.
+// Dense LU with partial pivoting (first maximum of a column wins; whole rows are
+// swapped) and solve of J y = F for one slot, on the slot's lanes; J is scattered
+// from the LU slots into a row-major n x n matrix in original order (scratch in
+// global memory, b.dense_ws).  Every sum has a fixed order, independent of K.
+// Returns false on a zero pivot.  y goes to s.w.F in internal order.
 template <int K>
-__device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am) {
+__device__ bool dense_factor_solve(Slot<K> &s, const BatchDev &b) {
   const DTpl &T = *s.T;
-  const int rank = s.rank;
+  const int n = T.n, ld = b.n_max, rank = s.rank();
+  double *A = b.dense_ws + (size_t)s.gsi * b.dense_stride;
+  double *rhs = A + (size_t)ld * ld;
+  int *piv = reinterpret_cast<int *>(rhs + ld);
+  for (int i = 0; i < n; ++i)
+    for (int j = rank; j < n; j += K) A[(size_t)i * ld + j] = 0.0;
+  s.ssync();
+  for (int q = rank; q < T.nnz_lu; q += K) { const int2 rc = T.lu_orig[q]; A[(size_t)rc.x * ld + rc.y] = s.w.lu[q]; }
+  for (int e = rank; e < n; e += K) rhs[e] = s.w.F[T.eq_pos[e]];
+  s.ssync();
+  for (int k = 0; k < n; ++k) {
+    double best = -1.0; int p = k;
+    for (int i = k + rank; i < n; i += K) { const double v = fabs(A[(size_t)i * ld + k]); if (v > best) { best = v; p = i; } }
+#pragma unroll
+    for (int o = K / 2; o > 0; o >>= 1) {
+      const double bv = __shfl_xor_sync(s.smask(), best, o, K);
+      const int bp = __shfl_xor_sync(s.smask(), p, o, K);
+      if (bv > best || (bv == best && bp < p)) { best = bv; p = bp; }
+    }
+    if (!(best > 0.0)) return false;
+    if (rank == 0) piv[k] = p;
+    if (p != k)
+      for (int j = rank; j < n; j += K) {
+        const double t = A[(size_t)k * ld + j]; A[(size_t)k * ld + j] = A[(size_t)p * ld + j]; A[(size_t)p * ld + j] = t;
+      }
+    s.ssync();
+    const double inv = 1.0 / A[(size_t)k * ld + k];
+    for (int i = k + 1 + rank; i < n; i += K) {
+      double *Ai = A + (size_t)i * ld;
+      const double aik = Ai[k];
+      if (aik == 0.0) continue;
+      const double l = aik * inv;
+      Ai[k] = l;
+      const double *Ak = A + (size_t)k * ld;
+      for (int j = k + 1; j < n; ++j) Ai[j] -= l * Ak[j];
+    }
+    s.ssync();
+  }
+  if (rank == 0)
+    for (int k = 0; k < n; ++k) if (piv[k] != k) { const double t = rhs[k]; rhs[k] = rhs[piv[k]]; rhs[piv[k]] = t; }
+  s.ssync();
+  for (int k = 0; k < n; ++k) {
+    const double bk = rhs[k];
+    for (int i = k + 1 + rank; i < n; i += K) { const double l = A[(size_t)i * ld + k]; if (l != 0.0) rhs[i] -= l * bk; }
+    s.ssync();
+  }
+  for (int k = n - 1; k >= 0; --k) {
+    if (rank == 0) rhs[k] = rhs[k] / A[(size_t)k * ld + k];
+    s.ssync();
+    const double bk = rhs[k];
+    for (int i = rank; i < k; i += K) rhs[i] -= A[(size_t)i * ld + k] * bk;
+    s.ssync();
+  }
+  for (int u = rank; u < n; u += K) s.w.F[T.iorder[u]] = rhs[u];
+  s.ssync();
+  return true;
+}
+
+template <int K, bool DENSE = false>
+__device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am, const BatchDev *bd = nullptr) {
+  const DTpl &T = *s.T;
+  const int rank = s.rank();
   const int it = s.jit + 1;
-  // K1: device evaluation
+  // K1: device evaluation, one model at a time across the warp
   {
     EvalCtx ctx{s.jt, s.jcj, s.jsrc, T.gmin, s.jdc, false};
     const double *x = s.jx;
-    for (int d = rank; d < T.n_dev; d += K) {
-      int gi = 0;
-      while (d >= T.dev_end[gi]) ++gi;
-      const DGroup gr = T.grp[gi];
-      int i = d - (gi ? T.dev_end[gi - 1] : 0);
+    for_devices_by_model<K>(T, rank, am, false, [&](const DGroup &gr, int i, int d) {
       const int *tm = T.term + gr.term_off + i * gr.ntx;
       double v[5];
       for (int kk = 0; kk < gr.ntx; ++kk) { int u = tm[kk]; v[kk] = u < 0 ? 0.0 : x[u]; }
@@ -573,7 +700,7 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am) {
       const int si = (gr.model == CEDAR_V || gr.model == CEDAR_I) ? T.src_of_dev[d] : -1;
       if (si >= 0) eval_source_value(gr.model, s.dp + gr.dpar_off + i, v, s.w.srcv[si], out);
       else eval_device(gr.model, s.dp + gr.dpar_off + i, gr.n_inst, v, nullptr, ctx, T.pwl, out);
-    }
+    });
   }
   __syncwarp(am);
   // K2: stamping (fixed-order gathers)
@@ -588,6 +715,12 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am) {
     }
   }
   __syncwarp(am);
+  bool slot_bad = false;
+  double *b = s.w.F;
+  if constexpr (DENSE) {
+    slot_bad = !dense_factor_solve(s, *bd);
+    __syncwarp(am);
+  } else {
   // K4: LU by levels
   bool bad = false;
   const int nl_lu = __reduce_max_sync(am, T.lu_nlev);
@@ -595,9 +728,10 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am) {
     if (l < T.lu_nlev) {
       int t1 = T.lu_lvl[l + 1];
       for (int t = T.lu_lvl[l] + rank; t < t1; t += K) {
-        int q = T.lu_slot[t], info = T.lu_info[t];
+        const int4 tk = T.lu_task[t];
+        int q = tk.x, info = tk.y;
         double acc = s.w.lu[q];
-        for (int p = T.lu_pp[t]; p < T.lu_pp[t + 1]; ++p) { int2 pr = T.lu_pair[p]; acc -= s.w.lu[pr.x] * s.w.lu[pr.y]; }
+        for (int p = tk.z; p < tk.w; ++p) { int2 pr = T.lu_pair[p]; acc -= s.w.lu[pr.x] * s.w.lu[pr.y]; }
         int kind = info & 3, j = info >> 2;
         if (kind == 2) acc *= s.w.rd[j];
         else if (kind == 1) {
@@ -610,15 +744,15 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am) {
     __syncwarp(am);
   }
   const unsigned bal_bad = __ballot_sync(am, bad);
-  const bool slot_bad = (bal_bad & s.smask) != 0;
+  slot_bad = (bal_bad & s.smask()) != 0;
   // K5: substitutions (skipped by slots with a zero pivot; bounds stay uniform)
-  double *b = s.w.F;
   const int nl_fw = __reduce_max_sync(am, T.fw_nlev);
   for (int l = 0; l < nl_fw; ++l) {
     if (!slot_bad && l < T.fw_nlev) {
       for (int t = T.fw_lvl[l] + rank; t < T.fw_lvl[l + 1]; t += K) {
-        int i = T.fw_row[t]; double acc = b[i];
-        for (int p = T.fw_ptr[t]; p < T.fw_ptr[t + 1]; ++p) { int2 pr = T.fw_pair[p]; acc -= s.w.lu[pr.x] * b[pr.y]; }
+        const int4 tk = T.fw_task[t];
+        int i = tk.x; double acc = b[i];
+        for (int p = tk.y; p < tk.z; ++p) { int2 pr = T.fw_pair[p]; acc -= s.w.lu[pr.x] * b[pr.y]; }
         b[i] = acc;
       }
     }
@@ -628,13 +762,15 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am) {
   for (int l = 0; l < nl_bw; ++l) {
     if (!slot_bad && l < T.bw_nlev) {
       for (int t = T.bw_lvl[l] + rank; t < T.bw_lvl[l + 1]; t += K) {
-        int i = T.bw_row[t]; double acc = b[i];
-        for (int p = T.bw_ptr[t]; p < T.bw_ptr[t + 1]; ++p) { int2 pr = T.bw_pair[p]; acc -= s.w.lu[pr.x] * b[pr.y]; }
+        const int4 tk = T.bw_task[t];
+        int i = tk.x; double acc = b[i];
+        for (int p = tk.y; p < tk.z; ++p) { int2 pr = T.bw_pair[p]; acc -= s.w.lu[pr.x] * b[pr.y]; }
         b[i] = acc * s.w.rd[i];
       }
     }
     __syncwarp(am);
   }
+  }  // sparse
   // K6: finiteness, DC damping, update, convergence vote
   // magnitudes are compared as integers (the bit patterns of non-negative doubles
   // order like the values), keeping these tests off the FP64 pipe
@@ -647,7 +783,7 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am) {
       if (damp && T.is_node[i]) mxb = ab > mxb ? ab : mxb;
     }
   }
-  const bool slot_nf = (__ballot_sync(am, nonfinite) & s.smask) != 0;
+  const bool slot_nf = (__ballot_sync(am, nonfinite) & s.smask()) != 0;
   double scale = 1.0;
   if (__any_sync(am, damp)) {
 #pragma unroll
@@ -665,7 +801,7 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am) {
       if (abs_bits(d) > abs_bits(lim)) conv = false;
     }
   }
-  const bool slot_notconv = (__ballot_sync(am, !conv) & s.smask) != 0;
+  const bool slot_notconv = (__ballot_sync(am, !conv) & s.smask()) != 0;
   __syncwarp(am);
   s.jit = it;
   if (slot_bad) s.jres = JOB_ZERO_PIVOT;

@@ -47,6 +47,14 @@ struct DTpl {
   // fw/bw), C^T program per internal column ((out << 1) | neg, internal row) and
   // the first gradient index of each group (-1: no differentiable parameter)
   int tf_nlev, tb_nlev, n_adj, pad_adj;
+  // groups by model: mg_grp[mg_ptr[m] .. mg_ptr[m + 1]) are the groups of model m
+  int mg_ptr[CEDAR_NMODELS + 1];
+  const int *mg_grp;
+  // original (equation, unknown) of every LU slot, for the dense DC fallback
+  const int2 *lu_orig;
+  // the same task lists packed one 16-byte record per task: LU (slot, info,
+  // first pair, end pair); substitutions (row, first pair, end pair, 0)
+  const int4 *lu_task, *fw_task, *bw_task, *tf_task, *tb_task;
   const int *tf_lvl, *tf_row, *tf_ptr; const int2 *tf_pair;
   const int *tb_lvl, *tb_row, *tb_ptr; const int2 *tb_pair;
   const int *ct_ptr; const int2 *ct_ent;
@@ -55,16 +63,22 @@ struct DTpl {
 
 // workspace size in doubles for one instance
 __host__ __device__ inline int ws_doubles(int n, int nnz_lu, int n_out, int n_src) {
-  return 13 * n + nnz_lu + n_out + n_src + 8;
+  return 10 * n + nnz_lu + n_out + n_src + 8;
 }
 
+// One instance's workspace.  Vectors whose lifetimes never overlap share
+// storage: the DC-only start point x0 and trial xs live in xm2 (adaptive BDF2
+// history) and qd (trapezoidal derivative), which the transient first writes
+// after the DC operating point; the charges at an accepted point (qt) live in F,
+// which is dead once the step's Newton solve is over.
 struct WS {
   double *x, *xn, *xm1, *xm2, *qn, *qm1, *qd, *hist, *F, *lu, *rd, *dout, *qt, *xs, *x0, *srcv;
   __device__ void bind(double *base, int n, int nnz_lu, int n_out, int n_src) {
     double *p = base;
     x = p; p += n; xn = p; p += n; xm1 = p; p += n; xm2 = p; p += n; qn = p; p += n; qm1 = p; p += n;
-    qd = p; p += n; hist = p; p += n; F = p; p += n; rd = p; p += n; qt = p; p += n; xs = p; p += n; x0 = p; p += n;
+    qd = p; p += n; hist = p; p += n; F = p; p += n; rd = p; p += n;
     lu = p; p += nnz_lu; dout = p; p += n_out; srcv = p; p += n_src;
+    x0 = xm2; xs = qd; qt = F;
   }
 };
 
@@ -224,8 +238,67 @@ struct Engine {
   WS w;
   G g;
 
+  double *dense = nullptr;   // (n + 2) n doubles for the dense DC fallback, or null
+  bool dense_mode = false;   // factorise with dense partial pivoting (DC fallback)
+
   __device__ Engine(const DTpl &t, const double *dpar, double *ws, G grp) : T(t), dp(dpar), g(grp) {
     w.bind(ws, T.n, T.nnz_lu, T.n_out, T.n_src);
+  }
+
+  // Dense LU with partial pivoting (first maximum of a column wins; whole rows
+  // swapped) of J scattered from the LU slots in original order, then J y = F;
+  // y goes to w.F in internal order.  Fixed-order sums.  False on a zero pivot.
+  __device__ bool dense_solve() {
+    const int n = T.n;
+    double *A = dense, *rhs = dense + (size_t)n * n;
+    int *piv = reinterpret_cast<int *>(rhs + n);
+    for (int i = g.rank; i < n * n; i += g.size) A[i] = 0.0;
+    g.sync();
+    for (int q = g.rank; q < T.nnz_lu; q += g.size) { const int2 rc = T.lu_orig[q]; A[(size_t)rc.x * n + rc.y] = w.lu[q]; }
+    for (int e = g.rank; e < n; e += g.size) rhs[e] = w.F[T.eq_pos[e]];
+    g.sync();
+    for (int k = 0; k < n; ++k) {
+      double lb = -1.0; int li = n;
+      for (int i = k + g.rank; i < n; i += g.size) { const double v = fabs(A[(size_t)i * n + k]); if (v > lb) { lb = v; li = i; } }
+      const double best = g.max(lb);
+      if (!(best > 0.0)) return false;
+      const int p = (int)g.min(lb == best ? (double)li : 1e300);
+      if (g.rank == 0) piv[k] = p;
+      if (p != k)
+        for (int j = g.rank; j < n; j += g.size) {
+          const double t = A[(size_t)k * n + j]; A[(size_t)k * n + j] = A[(size_t)p * n + j]; A[(size_t)p * n + j] = t;
+        }
+      g.sync();
+      const double inv = 1.0 / A[(size_t)k * n + k];
+      for (int i = k + 1 + g.rank; i < n; i += g.size) {
+        double *Ai = A + (size_t)i * n;
+        const double aik = Ai[k];
+        if (aik == 0.0) continue;
+        const double l = aik * inv;
+        Ai[k] = l;
+        const double *Ak = A + (size_t)k * n;
+        for (int j = k + 1; j < n; ++j) Ai[j] -= l * Ak[j];
+      }
+      g.sync();
+    }
+    if (g.rank == 0)
+      for (int k = 0; k < n; ++k) if (piv[k] != k) { const double t = rhs[k]; rhs[k] = rhs[piv[k]]; rhs[piv[k]] = t; }
+    g.sync();
+    for (int k = 0; k < n; ++k) {
+      const double bk = rhs[k];
+      for (int i = k + 1 + g.rank; i < n; i += g.size) { const double l = A[(size_t)i * n + k]; if (l != 0.0) rhs[i] -= l * bk; }
+      g.sync();
+    }
+    for (int k = n - 1; k >= 0; --k) {
+      if (g.rank == 0) rhs[k] = rhs[k] / A[(size_t)k * n + k];
+      g.sync();
+      const double bk = rhs[k];
+      for (int i = g.rank; i < k; i += g.size) rhs[i] -= A[(size_t)i * n + k] * bk;
+      g.sync();
+    }
+    for (int u = g.rank; u < n; u += g.size) w.F[T.iorder[u]] = rhs[u];
+    g.sync();
+    return true;
   }
 
   // K1: evaluate devices at x (internal order); q_only restricts to charge devices
@@ -324,8 +397,8 @@ struct Engine {
       g.sync();
       stamp(hist, gshunt, x, xref);
       g.sync();
-      if (!factor()) return 0;
-      solve(w.F);
+      if (dense_mode) { if (!dense_solve()) return 0; }
+      else { if (!factor()) return 0; solve(w.F); }
       // dx = -F ; finiteness and DC damping
       bool nonfinite = false; double mx = 0.0;
       for (int i = g.rank; i < T.n; i += g.size) {
@@ -368,7 +441,22 @@ struct Engine {
   }
 
   // DC operating point (mirrors the oracle's dcop()); x internal order.
+  // DC operating point; when the homotopy fails with the static pivot order and
+  // dense scratch is available, the whole homotopy reruns from the initial guess
+  // with dense partial pivoting.
   __device__ int dcop(double *x, double t, double rel, double av, double ai, long long *iters) {
+    int r = dcop_pass(x, t, rel, av, ai, iters);
+    if (r == CEDAR_ST_DCOP && dense && T.n > 0) {
+      copy(x, w.x0);
+      g.sync();
+      dense_mode = true;
+      r = dcop_pass(x, t, rel, av, ai, iters);
+      dense_mode = false;
+    }
+    return r;
+  }
+
+  __device__ int dcop_pass(double *x, double t, double rel, double av, double ai, long long *iters) {
     const int maxit = 100; const double vlim = 0.0;  // no damping: PTC bounds the steps
     const long long budget = 20000;
     EvalCtx ctx{t, 0.0, 1.0, T.gmin, true, false};

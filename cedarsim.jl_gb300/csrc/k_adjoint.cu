@@ -34,7 +34,7 @@ struct AdjSlot : Slot<K> {
   long long N, s0, s1, js, kb, k50;
   int cseg, np, astatus;
   double t50, tstar, gd0, gd1, phi;
-  double *la, *lb, *lc;            // lambda_{k+1}, lambda_{k+2}, the step being solved
+  double *la, *lb, *lc;            // lambda_{k+1}, lambda_{k+2}, the step being solved (scratch)
   double *gacc;                    // gradient accumulators (workspace)
   double *seg;                     // replayed states of the current segment
   const double *tt, *tp, *tv;      // tape of this instance
@@ -65,8 +65,8 @@ __device__ void adj_finish(AdjSlot<K> &s, const AdjDev &a) {
   const BatchDev &b = a.b;
   const bool ok = s.astatus == CEDAR_ST_OK;
   double *g = a.grad + (long long)s.inst * a.np_max;
-  for (int p = s.rank; p < a.np_max; p += K) g[p] = (ok && p < s.np) ? s.gacc[p] : (ok ? 0.0 : __longlong_as_double(0x7ff8000000000000LL));
-  if (s.rank == 0) {
+  for (int p = s.rank(); p < a.np_max; p += K) g[p] = (ok && p < s.np) ? s.gacc[p] : (ok ? 0.0 : __longlong_as_double(0x7ff8000000000000LL));
+  if (s.rank() == 0) {
     a.phi[s.inst] = ok ? s.phi : __longlong_as_double(0x7ff8000000000000LL);
     a.status[s.inst] = s.astatus;
   }
@@ -87,11 +87,9 @@ __device__ void adj_resume(AdjSlot<K> &s, const AdjDev &a, double *ws) {
         s.active = false; s.bactive = false;
         return;
       case AP_NEWINST: {
-        int job = 0;
-        if (s.rank == 0) job = atomicAdd(b.head, 1);
-        job = K == 1 ? job : __shfl_sync(s.smask, job, 0, K);
-        if (job >= b.n_inst) { s.rp = AP_IDLE; s.active = false; s.bactive = false; return; }
-        s.inst = b.queue[job];
+        const int job = s.dequeue(b);
+        if (job < 0) { s.rp = AP_IDLE; s.active = false; s.bactive = false; return; }
+        s.inst = job;
         const int ti = b.inst_tpl[s.inst];
         s.T = &b.tpls[ti];
         const DTpl &T = *s.T;
@@ -115,7 +113,7 @@ __device__ void adj_resume(AdjSlot<K> &s, const AdjDev &a, double *ws) {
         // objective (rank 0, sequential: the oracle's summation order)
         double E = 0.0, t50 = 0.0, gd0 = 0.0, gd1 = 0.0, phi = 0.0;
         long long k50 = -1;
-        if (s.rank == 0) {
+        if (s.rank() == 0) {
           for (long long k = 1; k <= s.N; ++k) E += (s.tt[k] - s.tt[k - 1]) * (s.tp[k] + s.tp[k - 1]) / 2.0;
           for (long long k = 1; k <= s.N; ++k) {
             const double v0 = s.tv[k - 1], v1 = s.tv[k];
@@ -137,14 +135,16 @@ __device__ void adj_resume(AdjSlot<K> &s, const AdjDev &a, double *ws) {
           }
         }
         if (K > 1) {
-          k50 = __shfl_sync(s.smask, k50, 0, K); t50 = __shfl_sync(s.smask, t50, 0, K);
-          gd0 = __shfl_sync(s.smask, gd0, 0, K); gd1 = __shfl_sync(s.smask, gd1, 0, K);
-          phi = __shfl_sync(s.smask, phi, 0, K);
+          k50 = __shfl_sync(s.smask(), k50, 0, K); t50 = __shfl_sync(s.smask(), t50, 0, K);
+          gd0 = __shfl_sync(s.smask(), gd0, 0, K); gd1 = __shfl_sync(s.smask(), gd1, 0, K);
+          phi = __shfl_sync(s.smask(), phi, 0, K);
         }
         s.k50 = k50; s.t50 = t50; s.gd0 = gd0; s.gd1 = gd1; s.phi = phi;
-        s.la = s.w.xm2; s.lb = s.w.qd; s.lc = s.w.xs;
+        // lambda_{k+1}, lambda_{k+2} live in vectors the replay never touches; the
+        // step being solved uses F, which is scratch between Newton solves
+        s.la = s.w.xm2; s.lb = s.w.qd; s.lc = s.w.F;
         s.fill(s.la, 0.0); s.fill(s.lb, 0.0);
-        for (int p = s.rank; p < s.np; p += K) s.gacc[p] = 0.0;
+        for (int p = s.rank(); p < s.np; p += K) s.gacc[p] = 0.0;
         s.ssync();
         s.cseg = s.N >= 1 ? (int)((s.N - 1) / every) : 0;
         goto seg_begin;
@@ -154,7 +154,7 @@ __device__ void adj_resume(AdjSlot<K> &s, const AdjDev &a, double *ws) {
         const DTpl &T = *s.T;
         s.eval_q(s.w.x, s.tt[s.js], s.w.qt);
         double *dst = s.seg + (s.js - s.s0) * b.n_max;
-        for (int i = s.rank; i < T.n; i += K) {
+        for (int i = s.rank(); i < T.n; i += K) {
           s.w.qm1[i] = s.w.qn[i]; s.w.qn[i] = s.w.qt[i];
           s.w.xm1[i] = s.w.xn[i]; s.w.xn[i] = s.w.x[i]; dst[i] = s.w.x[i];
         }
@@ -164,8 +164,9 @@ __device__ void adj_resume(AdjSlot<K> &s, const AdjDev &a, double *ws) {
       }
       case AP_BACKED: {
         if (s.astatus != CEDAR_ST_OK) { adj_finish(s, a); continue; }
-        double *t = s.lb; s.lb = s.la; s.la = s.lc; s.lc = t;
         if (s.kb == 0) { adj_finish(s, a); continue; }
+        for (int i = s.rank(); i < s.T->n; i += K) { s.lb[i] = s.la[i]; s.la[i] = s.lc[i]; }
+        s.ssync();
         --s.kb;
         goto back_issue;
       }
@@ -178,7 +179,7 @@ __device__ void adj_resume(AdjSlot<K> &s, const AdjDev &a, double *ws) {
       s.s0 = (long long)s.cseg * every;
       s.s1 = s.s0 + every < s.N ? s.s0 + every : s.N;
       const double *c = b.ckpt + ((long long)s.inst * ckpt_count(b.tape_cap, every) + s.cseg) * 2 * b.n_max;
-      for (int i = s.rank; i < T.n; i += K) { s.w.xn[i] = c[i]; s.w.xm1[i] = c[b.n_max + i]; s.seg[i] = c[i]; }
+      for (int i = s.rank(); i < T.n; i += K) { s.w.xn[i] = c[i]; s.w.xm1[i] = c[b.n_max + i]; s.seg[i] = c[i]; }
       s.ssync();
       s.eval_q(s.w.xn, s.tt[s.s0], s.w.qn);
       if (s.s0 >= 1) s.eval_q(s.w.xm1, s.tt[s.s0 - 1], s.w.qm1);
@@ -221,23 +222,19 @@ __device__ void adj_resume(AdjSlot<K> &s, const AdjDev &a, double *ws) {
 template <int K>
 __device__ __forceinline__ void backward_step(AdjSlot<K> &s, const AdjDev &a, unsigned ab) {
   const DTpl &T = *s.T;
-  const int rank = s.rank;
+  const int rank = s.rank();
   const double *x = s.bx;
   // (1) C partials at x (charge devices with cj = 1) when later steps couple back
   const bool couple = (s.cb1 != 0.0 || s.cb2 != 0.0);
+  const unsigned cm = __ballot_sync(ab, couple);
   if (couple) {
     EvalCtx ctx{s.bt, 1.0, 1.0, T.gmin, false, false};
-    for (int d = rank; d < T.n_dev; d += K) {
-      int gi = 0;
-      while (d >= T.dev_end[gi]) ++gi;
-      const DGroup gr = T.grp[gi];
-      if (gr.model != CEDAR_C && gr.model != CEDAR_L) continue;
-      int i = d - (gi ? T.dev_end[gi - 1] : 0);
+    for_devices_by_model<K>(T, rank, cm, true, [&](const DGroup &gr, int i, int) {
       const int *tm = T.term + gr.term_off + i * gr.ntx;
       double v[5];
       for (int kk = 0; kk < gr.ntx; ++kk) { int u = tm[kk]; v[kk] = u < 0 ? 0.0 : x[u]; }
       eval_device(gr.model, s.dp + gr.dpar_off + i, gr.n_inst, v, nullptr, ctx, T.pwl, s.w.dout + gr.out_off + i * model_nout(gr.model));
-    }
+    });
   }
   __syncwarp(ab);
   // right-hand side: -(dPhi/dx_k + C^T (cb1 lam_{k+1} + cb2 lam_{k+2}))
@@ -261,16 +258,12 @@ __device__ __forceinline__ void backward_step(AdjSlot<K> &s, const AdjDev &a, un
   // (2) J_k = G + cj_k C at x_k (DC Jacobian at k = 0)
   {
     EvalCtx ctx{s.bt, s.bcj, 1.0, T.gmin, s.bdc, false};
-    for (int d = rank; d < T.n_dev; d += K) {
-      int gi = 0;
-      while (d >= T.dev_end[gi]) ++gi;
-      const DGroup gr = T.grp[gi];
-      int i = d - (gi ? T.dev_end[gi - 1] : 0);
+    for_devices_by_model<K>(T, rank, ab, false, [&](const DGroup &gr, int i, int) {
       const int *tm = T.term + gr.term_off + i * gr.ntx;
       double v[5];
       for (int kk = 0; kk < gr.ntx; ++kk) { int u = tm[kk]; v[kk] = u < 0 ? 0.0 : x[u]; }
       eval_device(gr.model, s.dp + gr.dpar_off + i, gr.n_inst, v, nullptr, ctx, T.pwl, s.w.dout + gr.out_off + i * model_nout(gr.model));
-    }
+    });
   }
   __syncwarp(ab);
   for (int q = rank; q < T.nnz_lu; q += K) s.w.lu[q] = s.gather(T.jlu_ptr, T.jlu_ent, q, 0.0);
@@ -282,9 +275,10 @@ __device__ __forceinline__ void backward_step(AdjSlot<K> &s, const AdjDev &a, un
     if (l < T.lu_nlev) {
       int t1 = T.lu_lvl[l + 1];
       for (int t = T.lu_lvl[l] + rank; t < t1; t += K) {
-        int q = T.lu_slot[t], info = T.lu_info[t];
+        const int4 tk = T.lu_task[t];
+        int q = tk.x, info = tk.y;
         double acc = s.w.lu[q];
-        for (int p = T.lu_pp[t]; p < T.lu_pp[t + 1]; ++p) { int2 pr = T.lu_pair[p]; acc -= s.w.lu[pr.x] * s.w.lu[pr.y]; }
+        for (int p = tk.z; p < tk.w; ++p) { int2 pr = T.lu_pair[p]; acc -= s.w.lu[pr.x] * s.w.lu[pr.y]; }
         int kind = info & 3, jj = info >> 2;
         if (kind == 2) acc *= s.w.rd[jj];
         else if (kind == 1) {
@@ -296,15 +290,16 @@ __device__ __forceinline__ void backward_step(AdjSlot<K> &s, const AdjDev &a, un
     }
     __syncwarp(ab);
   }
-  const bool slot_bad = (__ballot_sync(ab, bad) & s.smask) != 0;
+  const bool slot_bad = (__ballot_sync(ab, bad) & s.smask()) != 0;
   // (4) U^T z = r, then L^T lam = z, in place in lc
   double *r = s.lc;
   const int nl_tf = __reduce_max_sync(ab, T.tf_nlev);
   for (int l = 0; l < nl_tf; ++l) {
     if (!slot_bad && l < T.tf_nlev) {
       for (int t = T.tf_lvl[l] + rank; t < T.tf_lvl[l + 1]; t += K) {
-        int i = T.tf_row[t]; double acc = r[i];
-        for (int p = T.tf_ptr[t]; p < T.tf_ptr[t + 1]; ++p) { int2 pr = T.tf_pair[p]; acc -= s.w.lu[pr.x] * r[pr.y]; }
+        const int4 tk = T.tf_task[t];
+        int i = tk.x; double acc = r[i];
+        for (int p = tk.y; p < tk.z; ++p) { int2 pr = T.tf_pair[p]; acc -= s.w.lu[pr.x] * r[pr.y]; }
         r[i] = acc * s.w.rd[i];
       }
     }
@@ -314,8 +309,9 @@ __device__ __forceinline__ void backward_step(AdjSlot<K> &s, const AdjDev &a, un
   for (int l = 0; l < nl_tb; ++l) {
     if (!slot_bad && l < T.tb_nlev) {
       for (int t = T.tb_lvl[l] + rank; t < T.tb_lvl[l + 1]; t += K) {
-        int i = T.tb_row[t]; double acc = r[i];
-        for (int p = T.tb_ptr[t]; p < T.tb_ptr[t + 1]; ++p) { int2 pr = T.tb_pair[p]; acc -= s.w.lu[pr.x] * r[pr.y]; }
+        const int4 tk = T.tb_task[t];
+        int i = tk.x; double acc = r[i];
+        for (int p = tk.y; p < tk.z; ++p) { int2 pr = T.tb_pair[p]; acc -= s.w.lu[pr.x] * r[pr.y]; }
         r[i] = acc;
       }
     }
@@ -360,15 +356,13 @@ template <int K>
 __global__ void __launch_bounds__(256, 1) adjoint_kernel(AdjDev a) {
   extern __shared__ double smem[];
   const BatchDev &b = a.b;
-  const int lane = threadIdx.x & 31;
   AdjSlot<K> s;
-  s.rank = lane % K;
-  s.smask = (K == 32) ? FULL : (((1u << K) - 1u) << (lane - s.rank));
   const int slots_per_block = blockDim.x / K;
   const int slot = threadIdx.x / K;
   double *ws = b.ws_in_smem ? smem + (size_t)slot * b.ws_stride
                             : b.ws_global + ((size_t)blockIdx.x * slots_per_block + slot) * b.ws_stride;
   s.rp = AP_NEWINST; s.active = false; s.bactive = false;
+  s.gsi = blockIdx.x * slots_per_block + slot; s.qblk = -1; s.dense = false; s.jdense = false;
   s.nrel = b.opts.nr_factor * b.opts.reltol; s.nav = b.opts.nr_factor * b.opts.abstol_v;
   s.nai = b.opts.nr_factor * b.opts.abstol_i;
   for (;;) {
@@ -377,7 +371,7 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(AdjDev a) {
     const unsigned am = __ballot_sync(FULL, s.active);
     const unsigned ab = __ballot_sync(FULL, s.bactive);
     if ((am | ab) == 0) break;
-    if (s.active) newton_iteration(s, am);
+    if (s.active) newton_iteration<K, false>(s, am);
     __syncwarp();
     if (s.bactive) backward_step(s, a, ab);
     __syncwarp();
@@ -386,12 +380,17 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(AdjDev a) {
 
 template <int K>
 cudaError_t launch_adj_k(const AdjDev &a, int warps, int grid, size_t smem, cudaStream_t st) {
-  static int configured = -1;
-  if ((int)smem > 48 * 1024 && configured < (int)smem) {
-    cudaError_t e = cudaFuncSetAttribute(adjoint_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    configured = (int)smem;
-  }
+  cudaError_t e = cudaFuncSetAttribute(adjoint_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int nb = 0;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, adjoint_kernel<K>, warps * 32, smem)) != cudaSuccess) return e;
+  if (nb < 1) nb = 1;
+  int dev = 0, smsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&smsm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  int pct = (int)(100.0 * (double)nb * (double)(smem + 1024) / (double)(smsm > 0 ? smsm : 1)) + 1;
+  pct = pct > 100 ? 100 : pct;
+  if ((e = cudaFuncSetAttribute(adjoint_kernel<K>, cudaFuncAttributePreferredSharedMemoryCarveout, pct)) != cudaSuccess) return e;
   adjoint_kernel<K><<<grid, warps * 32, smem, st>>>(a);
   return cudaGetLastError();
 }

@@ -116,6 +116,54 @@ cudaError_t eval_scratch_address(double **ptr) {
   return cudaSuccess;
 }
 
+// ---------------------------------------------------------------------------
+// FP64 issue-rate probe: the denominator of the batched kernel's roofline.
+// Every thread of lanes below `active_lanes` runs 8 independent DFMA chains of
+// `iters` steps; registers only, no memory traffic in the loop.
+__global__ void fp64_probe_kernel(double *sink, int iters, int active_lanes) {
+  const int lane = threadIdx.x & 31;
+  double a0 = 1e-9 * threadIdx.x, a1 = a0 + 0.125, a2 = a0 + 0.25, a3 = a0 + 0.375;
+  double a4 = a0 + 0.5, a5 = a0 + 0.625, a6 = a0 + 0.75, a7 = a0 + 0.875;
+  const double m = 0.9999999, c = 1e-7;
+  if (lane < active_lanes) {
+    for (int i = 0; i < iters; ++i) {
+      a0 = fma(a0, m, c); a1 = fma(a1, m, c); a2 = fma(a2, m, c); a3 = fma(a3, m, c);
+      a4 = fma(a4, m, c); a5 = fma(a5, m, c); a6 = fma(a6, m, c); a7 = fma(a7, m, c);
+    }
+  }
+  const double r = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+  if (r == -1.0) sink[blockIdx.x] = r;  // never true; keeps the chains live
+}
+
+cudaError_t launch_fp64_probe(int active_lanes, int iters, double *gflops, double *ms) {
+  int dev = 0, nsm = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  const int blocks = nsm * 8, threads = 256;
+  double *sink = nullptr;
+  if ((e = cudaMalloc(&sink, blocks * sizeof(double))) != cudaSuccess) return e;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0); cudaEventCreate(&e1);
+  float best = 1e30f;
+  for (int rep = 0; rep < 6; ++rep) {   // first launch warms up; best of the rest
+    cudaEventRecord(e0);
+    fp64_probe_kernel<<<blocks, threads>>>(sink, iters, active_lanes);
+    cudaEventRecord(e1);
+    if ((e = cudaEventSynchronize(e1)) != cudaSuccess) break;
+    float t = 0; cudaEventElapsedTime(&t, e0, e1);
+    if (rep > 0 && t < best) best = t;
+  }
+  cudaEventDestroy(e0); cudaEventDestroy(e1);
+  cudaFree(sink);
+  if (e != cudaSuccess) return e;
+  // useful flops: 2 per FMA on the active lanes only
+  const double fmas = 8.0 * iters * (double)blocks * threads * (active_lanes / 32.0);
+  if (gflops) *gflops = 2.0 * fmas / (best * 1e-3) / 1e9;
+  if (ms) *ms = best;
+  return cudaGetLastError();
+}
+
 // Single instance on one CTA.  Workspace in dynamic shared memory when it fits,
 // else in global memory (a.ws_global).
 __global__ void plain_kernel(PlainArgs a) {
@@ -125,6 +173,7 @@ __global__ void plain_kernel(PlainArgs a) {
   const DTpl &T = *a.T;
   BlockGroup g(red);
   Engine<BlockGroup> E(T, a.dpar, ws, g);
+  E.dense = a.dense;
   for (int i = g.rank; i < T.n; i += g.size) E.w.x[i] = a.x[T.order[i]];
   g.sync();
   const EngOpts &o = a.opts;

@@ -18,8 +18,11 @@ struct BatchDev {
   double *samples;               // [n_inst * np * ns]
   double *x_final; int n_max;    // [n_inst * n_max] original order
   EngStats *stats;               // [n_inst]
-  const int *queue;              // dequeue order (instance ids)
-  int *head;                     // queue head counter
+  const int *queue;              // dequeue order (instance ids), in blocks of one template
+  int *head;                     // (unused by the kernels; kept zero)
+  const int *qblk_beg;           // [n_qblk + 1] start of each template block in queue
+  int *qblk_head;                // [n_qblk] next position to take in each block
+  int n_qblk;
   int n_inst;
   EngOpts opts;
   int ws_stride;                 // doubles per group workspace
@@ -40,6 +43,9 @@ struct BatchDev {
   long long tape_cap;
   double *ckpt; int ckpt_every;
   const int4 *obj_idx;           // [n_templates] internal (vnode, ibranch, probe, 0)
+  // dense DC fallback scratch: per global slot dense_stride doubles (an n_max x
+  // n_max matrix, a right-hand side and the pivots); null: no fallback
+  double *dense_ws; long long dense_stride; int dense_nmax;
 };
 
 // slice helpers of the adjoint tape
@@ -96,12 +102,19 @@ struct PlainArgs {
   double *t_out, *x_out; long long cap; long long *count;
   EngStats *stats;
   double *ws_global;
+  double *dense;           // (n + 2) n doubles for the dense DC fallback, or null
   int mode;
 };
 cudaError_t launch_plain(const PlainArgs &a, int ws_doubles_n, int threads, cudaStream_t s);
 
+// FP64 issue-rate probe (8 DFMA chains per thread, lanes >= active_lanes idle)
+cudaError_t launch_fp64_probe(int active_lanes, int iters, double *gflops, double *ms);
+
 // batched persistent engine with K lanes per instance
 cudaError_t launch_batch(const BatchDev &b, int K, int warps_per_cta, int grid, size_t smem, cudaStream_t s);
+// set the launch attributes of batch_kernel<K> for this shape and report its
+// resident CTAs per SM (registers and shared memory both counted)
+cudaError_t configure_batch(int K, int warps_per_cta, size_t smem, int *per_sm);
 int batch_max_smem_optin();
 
 }  // namespace cedar

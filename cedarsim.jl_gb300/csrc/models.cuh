@@ -139,23 +139,23 @@ CEDAR_HD void eval_source_value(int model, const double *dp, const double *v, do
   else out[0] = m * vs;
 }
 
-// level-1 forward-mode current and partials (vds >= 0)
+// level-1 forward-mode current and partials (vds >= 0).  Both the triode and the
+// saturation expressions are formed and the region selects one: a warp whose
+// lanes sit in different regions then runs one instruction stream instead of
+// one per region (an FP64 instruction costs the same with 1 or 32 active lanes).
 CEDAR_HD void mos1_fwd(double vgs, double vds, double vth, double beta, double lam,
                        double &id, double &gm, double &gds) {
-  double vov = vgs - vth;
-  if (vov <= 0) { id = 0; gm = 0; gds = 0; return; }
-  double clm = 1.0 + lam * vds;
-  if (vds < vov) {
-    double a = (vov - 0.5 * vds) * vds;
-    id = beta * a * clm;
-    gm = beta * vds * clm;
-    gds = beta * (vov - vds) * clm + beta * a * lam;
-  } else {
-    double a = 0.5 * vov * vov;
-    id = beta * a * clm;
-    gm = beta * vov * clm;
-    gds = beta * a * lam;
-  }
+  const double vov = vgs - vth;
+  const double clm = 1.0 + lam * vds;
+  const double at = (vov - 0.5 * vds) * vds;          // triode
+  const double id_t = beta * at * clm, gm_t = beta * vds * clm;
+  const double gds_t = beta * (vov - vds) * clm + beta * at * lam;
+  const double as = 0.5 * vov * vov;                  // saturation
+  const double id_s = beta * as * clm, gm_s = beta * vov * clm, gds_s = beta * as * lam;
+  const bool off = vov <= 0, tri = vds < vov;
+  id = off ? 0.0 : (tri ? id_t : id_s);
+  gm = off ? 0.0 : (tri ? gm_t : gm_s);
+  gds = off ? 0.0 : (tri ? gds_t : gds_s);
 }
 
 // Evaluate one device.  v[k]: terminal (+branch) unknown values, vd[k]: their
@@ -200,9 +200,12 @@ CEDAR_HD void eval_device(int model, const double *dp, int ds, const double *v, 
       double type = dp[0], beta = dp[ds], vth = dp[2 * ds], lam = dp[3 * ds], m = dp[4 * ds];
       double vgs = type * (v[1] - v[2]), vds = type * (v[0] - v[2]);
       // gsum = -dIds/dVs - gmin = gm + gds, formed without cancellation in reverse mode
-      double id, gm, gds, gsum;
-      if (vds >= 0) { mos1_fwd(vgs, vds, vth, beta, lam, id, gm, gds); gsum = gm + gds; }
-      else { double i1, g1, g2; mos1_fwd(vgs - vds, -vds, vth, beta, lam, i1, g1, g2); id = -i1; gm = -g1; gds = g1 + g2; gsum = g2; }
+      // source/drain exchange for vds < 0, by selection (no divergent branch)
+      const bool fwd = vds >= 0;
+      double i1, g1, g2;
+      mos1_fwd(fwd ? vgs : vgs - vds, fwd ? vds : -vds, vth, beta, lam, i1, g1, g2);
+      const double s12 = g1 + g2;
+      const double id = fwd ? i1 : -i1, gm = fwd ? g1 : -g1, gds = fwd ? g2 : s12, gsum = fwd ? s12 : g2;
       double gmin = ctx.gmin;
       double ids = type * id + gmin * (v[0] - v[2]);
       out[0] = m * ids; out[1] = m * gm; out[2] = m * (gds + gmin); out[3] = m * (gsum + gmin);

@@ -357,6 +357,13 @@ int cedar_adjoint_tape(cedar_batch *b, int32_t inst, double *t, int8_t *ord, int
 /* Device time of the last adjoint run's forward and backward kernels. */
 int cedar_adjoint_last_ms(cedar_batch *b, double *fwd_ms, double *bwd_ms);
 
+/* ---- measurement ------------------------------------------------------------
+ * FP64 issue-rate probe, the denominator of the batched kernel's roofline (no
+ * counterpart in the reference): every lane below active_lanes of 8 x 256-thread
+ * CTAs per SM runs 8 independent DFMA chains of iters steps; gflops counts 2 flops
+ * per FMA on the active lanes, best of 5 timed launches (CUDA events). */
+int cedar_fp64_probe(int32_t active_lanes, int32_t iters, double *gflops, double *ms);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1031,4 +1031,50 @@ int oracle_batch(const cedar_batch_desc *b, const cedar_tran_opts *opts, int32_t
   return rc_all;
 }
 
+// Adjoint over a range of batch instances with OpenMP (the CPU baseline of the
+// GPU adjoint): forward run recording its steps, then the adjoint along them with
+// the same options.  obj[n_templates], tstar[n_inst]; phi[i1 - i0],
+// grad[(i1 - i0) * np_max]; status[i1 - i0] (0 or the forward's status).
+int oracle_adjoint_batch(const cedar_batch_desc *b, const cedar_tran_opts *opts, const cedar_objective *obj,
+                         const double *tstar, int32_t i0, int32_t i1, int32_t np_max, double *phi, double *grad,
+                         int32_t *status, int nthreads) {
+  if (!b || i0 < 0 || i1 > b->n_inst || i0 > i1) { g_err = "bad batch range"; return CEDAR_EINVAL; }
+  std::vector<Circuit> tmpl(b->n_templates);
+  for (int k = 0; k < b->n_templates; ++k) if (!load_circuit(&b->templates[k], tmpl[k], g_err)) return CEDAR_EINVAL;
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#else
+  nthreads = 1;
+#endif
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+  for (int i = i0; i < i1; ++i) {
+    const int k = b->inst_template[i];
+    Circuit c = tmpl[k];
+    if (b->inst_par_off && b->inst_par_off[i] >= 0) {
+      const double *p = b->inst_par + b->inst_par_off[i];
+      for (Group &g : c.groups) { std::copy(p, p + g.par.size(), g.par.begin()); p += g.par.size(); }
+    }
+    std::vector<double> x(c.n, 0.0), rt;
+    std::vector<signed char> ro;
+    Sink sink; sink.rec_t = &rt; sink.rec_ord = &ro;
+    cedar_stats st{};
+    tran(c, opts, x.data(), sink, st, nullptr);
+    double *g = grad + (size_t)(i - i0) * np_max;
+    std::fill(g, g + np_max, 0.0);
+    int s = st.status;
+    if (s == CEDAR_ST_OK) {
+      StepSeq S; S.T.push_back(opts->tstart); S.ord.push_back(0);
+      for (size_t q = 0; q < rt.size(); ++q) { S.T.push_back(rt[q]); S.ord.push_back(ro[q]); }
+      cedar_tran_opts o; fill_defaults(opts, o);
+      std::vector<double> gi(std::max(n_params(c), 1), 0.0);
+      double ph = 0.0;
+      s = adjoint(c, o, S, obj[k], tstar ? tstar[i] : 0.0, nullptr, &ph, gi.data());
+      phi[i - i0] = ph;
+      for (int q = 0; q < n_params(c) && q < np_max; ++q) g[q] = gi[q];
+    }
+    if (status) status[i - i0] = s;
+  }
+  return 0;
+}
+
 }  // extern "C"

@@ -57,6 +57,9 @@ def load(pkg):
     lib.oracle_adjoint.argtypes = [cd_p, to_p, to_p, obj_p, C.c_double, dp, dp, dp, dp, C.c_void_p, C.c_int64, ip]
     lib.oracle_replay_phi.restype = C.c_int
     lib.oracle_replay_phi.argtypes = [cd_p, to_p, dp, C.c_void_p, C.c_int64, obj_p, C.c_double, dp, dp]
+    lib.oracle_adjoint_batch.restype = C.c_int
+    lib.oracle_adjoint_batch.argtypes = [C.POINTER(abi.BatchDesc), to_p, obj_p, dp, C.c_int32, C.c_int32, C.c_int32,
+                                         dp, dp, C.POINTER(C.c_int32), C.c_int]
     lib.oracle_n_params.restype = C.c_int
     lib.oracle_n_params.argtypes = [cd_p]
     lib.oracle_last_error.restype = C.c_int
@@ -158,3 +161,20 @@ class Oracle:
                                         _dp(pert), C.byref(phi))
         assert rc == 0, rc
         return phi.value
+
+    def adjoint_batch(self, holder, opts, objectives, tstar, i0=0, i1=None, np_max=None, nthreads=0):
+        """Oracle adjoint over batch instances [i0, i1) with OpenMP; objectives per template."""
+        i1 = holder.n_inst if i1 is None else i1
+        if np_max is None:
+            np_max = max(self.lib.oracle_n_params(C.byref(t.desc)) for t in holder.templates)
+        cnt = i1 - i0
+        obj = (self.pkg.abi.Objective * len(objectives))(*objectives)
+        ts = np.ascontiguousarray(tstar, np.float64)
+        phi = np.zeros(cnt)
+        grad = np.zeros((cnt, max(np_max, 1)))
+        status = np.zeros(cnt, np.int32)
+        rc = self.lib.oracle_adjoint_batch(C.byref(holder.desc), C.byref(opts), obj, _dp(ts), i0, i1, np_max,
+                                           _dp(phi), _dp(grad), status.ctypes.data_as(C.POINTER(C.c_int32)), nthreads)
+        assert rc == 0, rc
+        return phi, grad[:, :np_max], status
+
