@@ -21,7 +21,13 @@ INCLUDE = PKG.parent / "include"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", "-I", str(INCLUDE)]
-SOURCES = ["api.cu", "k_plain.cu", "k_batch.cu", "k_adjoint.cu", "compile.cpp"]
+LANES = (1, 2, 4, 8, 16, 32)
+# (source, object, extra flags): the batched and adjoint kernels are compiled once
+# per lanes-per-instance value so the instantiations build in parallel
+SOURCES = ([("api.cu", "api.cu.o", []), ("k_plain.cu", "k_plain.cu.o", []), ("k_dispatch.cu", "k_dispatch.cu.o", []),
+            ("compile.cpp", "compile.cpp.o", [])]
+           + [("k_batch.cu", f"k_batch.k{k}.o", [f"-DCEDAR_LANES={k}"]) for k in LANES]
+           + [("k_adjoint.cu", f"k_adjoint.k{k}.o", [f"-DCEDAR_LANES={k}"]) for k in LANES])
 
 
 def _nvcc() -> str:
@@ -45,9 +51,10 @@ def build(force: bool = False, verbose: bool = False) -> pathlib.Path:
     BUILD.mkdir(parents=True, exist_ok=True)
     nvcc = _nvcc()
 
-    def compile_one(src: str) -> str:
-        obj = BUILD / (src + ".o")
-        cmd = [nvcc, *ARCH, *NVCC_FLAGS, "-c", str(CSRC / src), "-o", str(obj)]
+    def compile_one(item) -> str:
+        src, objname, extra = item
+        obj = BUILD / objname
+        cmd = [nvcc, *ARCH, *NVCC_FLAGS, *extra, "-c", str(CSRC / src), "-o", str(obj)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {src}:\n{r.stdout}\n{r.stderr}")
@@ -55,7 +62,7 @@ def build(force: bool = False, verbose: bool = False) -> pathlib.Path:
             print(r.stdout, r.stderr)
         return str(obj)
 
-    with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+    with cf.ThreadPoolExecutor(max_workers=min(len(SOURCES), max(2, os.cpu_count() or 2))) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     tmp = LIB.with_suffix(".so.tmp")
     cmd = [nvcc, *ARCH, "-shared", "-o", str(tmp), *objs, "-lcudart_static", "-lrt", "-ldl", "-lpthread"]

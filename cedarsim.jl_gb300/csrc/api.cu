@@ -654,7 +654,7 @@ static int batch_launch(cedar_batch *b, const EngOpts &eo, const cedar_batch_tun
   {
     // a persistent grid of exactly the CTAs that can be resident at once
     int per_sm = 1, dev = 0, nsm = 0;
-    CUDA_TRY(configure_batch(K, warps, smem, &per_sm));
+    CUDA_TRY(configure_batch(K, warps, smem, in_smem, &per_sm));
     CUDA_TRY(cudaGetDevice(&dev));
     CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     grid = std::max(1, std::min(nsm * per_sm, (b->n_inst + tiles - 1) / tiles));

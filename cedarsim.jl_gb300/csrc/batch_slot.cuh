@@ -34,6 +34,16 @@ constexpr unsigned FULL = 0xffffffffu;
 // the lanes in `mask`; charges_only restricts the walk to capacitors and inductors.
 template <int K, class Fn>
 __device__ __forceinline__ void for_devices_by_model(const DTpl &T, int rank, unsigned mask, bool charges_only, Fn &&fn) {
+  if constexpr (K == 32) {
+    // one slot per warp: no other slot to diverge from, so walk the groups in
+    // template order without the per-model bookkeeping
+    for (int gi = 0; gi < T.n_groups; ++gi) {
+      const DGroup gr = T.grp[gi];
+      if (charges_only && gr.model != CEDAR_C && gr.model != CEDAR_L) continue;
+      const int dbase = gi > 0 ? T.dev_end[gi - 1] : 0;
+      for (int i = rank; i < gr.n_inst; i += K) fn(gr, i, dbase + i);
+    }
+  } else {
   for (int m = 1; m < CEDAR_NMODELS; ++m) {
     if (charges_only && m != CEDAR_C && m != CEDAR_L) continue;
     const int g0 = T.mg_ptr[m], ng = T.mg_ptr[m + 1] - g0;
@@ -50,6 +60,7 @@ __device__ __forceinline__ void for_devices_by_model(const DTpl &T, int rank, un
         if (i < cnt) fn(gr, i, dbase + i);
       }
     }
+  }
   }
 }
 constexpr int JOB_RUNNING = INT_MIN;  // job result while iterating
@@ -688,35 +699,57 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am, const 
   const DTpl &T = *s.T;
   const int rank = s.rank();
   const int it = s.jit + 1;
+  // the slot's workspace pointers and job fields, read once
+  double *const lu = s.w.lu, *const F = s.w.F, *const rd = s.w.rd, *const dout = s.w.dout;
+  double *const jx = s.jx;
+  const double *const jhist = s.jhist;
+  const double *const dp = s.dp;
+  const double *const srcv = s.w.srcv;
+  const double jgs = s.jgs;
+  // two accumulators (even / odd entries) halve the dependent add chain
+  // two accumulators (even / odd entries) halve the dependent add chain
+  auto gather = [&](const int *ptr, const int *ent, int q, double acc) {
+    const int a = ptr[q], e1 = ptr[q + 1];
+    double acc1 = 0.0;
+    int k = a;
+    for (; k + 1 < e1; k += 2) {
+      const int e0 = ent[k], e2 = ent[k + 1];
+      const double v0 = dout[e0 >> 1], v2 = dout[e2 >> 1];
+      acc = (e0 & 1) ? acc - v0 : acc + v0;
+      acc1 = (e2 & 1) ? acc1 - v2 : acc1 + v2;
+    }
+    if (k < e1) { const int e0 = ent[k]; const double v0 = dout[e0 >> 1]; acc = (e0 & 1) ? acc - v0 : acc + v0; }
+    return acc + acc1;
+  };
   // K1: device evaluation, one model at a time across the warp
   {
     EvalCtx ctx{s.jt, s.jcj, s.jsrc, T.gmin, s.jdc, false};
-    const double *x = s.jx;
+    const double *x = jx;
     for_devices_by_model<K>(T, rank, am, false, [&](const DGroup &gr, int i, int d) {
       const int *tm = T.term + gr.term_off + i * gr.ntx;
       double v[5];
       for (int kk = 0; kk < gr.ntx; ++kk) { int u = tm[kk]; v[kk] = u < 0 ? 0.0 : x[u]; }
-      double *out = s.w.dout + gr.out_off + i * model_nout(gr.model);
+      double *out = dout + gr.out_off + i * model_nout(gr.model);
       const int si = (gr.model == CEDAR_V || gr.model == CEDAR_I) ? T.src_of_dev[d] : -1;
-      if (si >= 0) eval_source_value(gr.model, s.dp + gr.dpar_off + i, v, s.w.srcv[si], out);
-      else eval_device(gr.model, s.dp + gr.dpar_off + i, gr.n_inst, v, nullptr, ctx, T.pwl, out);
+      if (si >= 0) eval_source_value(gr.model, dp + gr.dpar_off + i, v, srcv[si], out);
+      else eval_device(gr.model, dp + gr.dpar_off + i, gr.n_inst, v, nullptr, ctx, T.pwl, out);
     });
   }
   __syncwarp(am);
   // K2: stamping (fixed-order gathers)
-  for (int q = rank; q < T.nnz_lu; q += K) s.w.lu[q] = s.gather(T.jlu_ptr, T.jlu_ent, q, 0.0);
-  for (int r = rank; r < T.n; r += K) s.w.F[r] = s.gather(T.fint_ptr, T.fint_ent, r, s.jhist ? s.jhist[r] : 0.0);
+  for (int q = rank; q < T.nnz_lu; q += K) lu[q] = gather(T.jlu_ptr, T.jlu_ent, q, 0.0);
+  for (int r = rank; r < T.n; r += K) F[r] = gather(T.fint_ptr, T.fint_ent, r, jhist ? jhist[r] : 0.0);
   __syncwarp(am);
-  if (s.jgs != 0.0) {
+  if (jgs != 0.0) {
     for (int u = rank; u < T.n_nodes; u += K) {
       int c = T.gs_col[u];
-      s.w.lu[T.gs_slot[u]] -= s.jgs;
-      s.w.F[T.gs_row[u]] -= s.jgs * (s.jx[c] - (s.jxref ? s.jxref[c] : 0.0));
+      lu[T.gs_slot[u]] -= jgs;
+      F[T.gs_row[u]] -= jgs * (jx[c] - (s.jxref ? s.jxref[c] : 0.0));
     }
   }
   __syncwarp(am);
   bool slot_bad = false;
-  double *b = s.w.F;
+  double *b = F;
   if constexpr (DENSE) {
     slot_bad = !dense_factor_solve(s, *bd);
     __syncwarp(am);
@@ -730,15 +763,21 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am, const 
       for (int t = T.lu_lvl[l] + rank; t < t1; t += K) {
         const int4 tk = T.lu_task[t];
         int q = tk.x, info = tk.y;
-        double acc = s.w.lu[q];
-        for (int p = tk.z; p < tk.w; ++p) { int2 pr = T.lu_pair[p]; acc -= s.w.lu[pr.x] * s.w.lu[pr.y]; }
+        double acc = lu[q], acc1 = 0.0;
+        int p = tk.z;
+        for (; p + 1 < tk.w; p += 2) {
+          const int2 p0 = T.lu_pair[p], p1 = T.lu_pair[p + 1];
+          acc -= lu[p0.x] * lu[p0.y]; acc1 -= lu[p1.x] * lu[p1.y];
+        }
+        if (p < tk.w) { const int2 p0 = T.lu_pair[p]; acc -= lu[p0.x] * lu[p0.y]; }
+        acc += acc1;
         int kind = info & 3, j = info >> 2;
-        if (kind == 2) acc *= s.w.rd[j];
+        if (kind == 2) acc *= rd[j];
         else if (kind == 1) {
           if (!pivot_ok(acc)) bad = true;
-          s.w.rd[j] = pivot_rcp(acc);
+          rd[j] = pivot_rcp(acc);
         }
-        s.w.lu[q] = acc;
+        lu[q] = acc;
       }
     }
     __syncwarp(am);
@@ -752,7 +791,14 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am, const 
       for (int t = T.fw_lvl[l] + rank; t < T.fw_lvl[l + 1]; t += K) {
         const int4 tk = T.fw_task[t];
         int i = tk.x; double acc = b[i];
-        for (int p = tk.y; p < tk.z; ++p) { int2 pr = T.fw_pair[p]; acc -= s.w.lu[pr.x] * b[pr.y]; }
+        double acc1 = 0.0;
+        int p = tk.y;
+        for (; p + 1 < tk.z; p += 2) {
+          const int2 p0 = T.fw_pair[p], p1 = T.fw_pair[p + 1];
+          acc -= lu[p0.x] * b[p0.y]; acc1 -= lu[p1.x] * b[p1.y];
+        }
+        if (p < tk.z) { const int2 p0 = T.fw_pair[p]; acc -= lu[p0.x] * b[p0.y]; }
+        acc += acc1;
         b[i] = acc;
       }
     }
@@ -764,8 +810,15 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am, const 
       for (int t = T.bw_lvl[l] + rank; t < T.bw_lvl[l + 1]; t += K) {
         const int4 tk = T.bw_task[t];
         int i = tk.x; double acc = b[i];
-        for (int p = tk.y; p < tk.z; ++p) { int2 pr = T.bw_pair[p]; acc -= s.w.lu[pr.x] * b[pr.y]; }
-        b[i] = acc * s.w.rd[i];
+        double acc1 = 0.0;
+        int p = tk.y;
+        for (; p + 1 < tk.z; p += 2) {
+          const int2 p0 = T.bw_pair[p], p1 = T.bw_pair[p + 1];
+          acc -= lu[p0.x] * b[p0.y]; acc1 -= lu[p1.x] * b[p1.y];
+        }
+        if (p < tk.z) { const int2 p0 = T.bw_pair[p]; acc -= lu[p0.x] * b[p0.y]; }
+        acc += acc1;
+        b[i] = acc * rd[i];
       }
     }
     __syncwarp(am);
@@ -795,8 +848,8 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am, const 
   if (!slot_bad && !slot_nf) {
     for (int i = rank; i < T.n; i += K) {
       double d = -b[i] * scale;
-      double xi = s.jx[i] + d;
-      s.jx[i] = xi;
+      double xi = jx[i] + d;
+      jx[i] = xi;
       double lim = s.nrel * fabs(xi) + (T.is_node[i] ? s.nav : s.nai);
       if (abs_bits(d) > abs_bits(lim)) conv = false;
     }

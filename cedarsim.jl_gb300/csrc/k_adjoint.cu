@@ -352,15 +352,16 @@ __device__ __forceinline__ void backward_step(AdjSlot<K> &s, const AdjDev &a, un
   s.bactive = false;
 }
 
-template <int K>
+template <int K, bool SMEM>
 __global__ void __launch_bounds__(256, 1) adjoint_kernel(AdjDev a) {
   extern __shared__ double smem[];
   const BatchDev &b = a.b;
   AdjSlot<K> s;
   const int slots_per_block = blockDim.x / K;
   const int slot = threadIdx.x / K;
-  double *ws = b.ws_in_smem ? smem + (size_t)slot * b.ws_stride
-                            : b.ws_global + ((size_t)blockIdx.x * slots_per_block + slot) * b.ws_stride;
+  double *ws;
+  if constexpr (SMEM) ws = smem + (size_t)slot * b.ws_stride;
+  else ws = b.ws_global + ((size_t)blockIdx.x * slots_per_block + slot) * b.ws_stride;
   s.rp = AP_NEWINST; s.active = false; s.bactive = false;
   s.gsi = blockIdx.x * slots_per_block + slot; s.qblk = -1; s.dense = false; s.jdense = false;
   s.nrel = b.opts.nr_factor * b.opts.reltol; s.nav = b.opts.nr_factor * b.opts.abstol_v;
@@ -378,35 +379,35 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(AdjDev a) {
   }
 }
 
-template <int K>
-cudaError_t launch_adj_k(const AdjDev &a, int warps, int grid, size_t smem, cudaStream_t st) {
-  cudaError_t e = cudaFuncSetAttribute(adjoint_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+template <int K, bool SMEM>
+cudaError_t launch_adj_ks(const AdjDev &a, int warps, int grid, size_t smem, cudaStream_t st) {
+  cudaError_t e = cudaFuncSetAttribute(adjoint_kernel<K, SMEM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int nb = 0;
-  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, adjoint_kernel<K>, warps * 32, smem)) != cudaSuccess) return e;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, adjoint_kernel<K, SMEM>, warps * 32, smem)) != cudaSuccess) return e;
   if (nb < 1) nb = 1;
   int dev = 0, smsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&smsm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
   int pct = (int)(100.0 * (double)nb * (double)(smem + 1024) / (double)(smsm > 0 ? smsm : 1)) + 1;
   pct = pct > 100 ? 100 : pct;
-  if ((e = cudaFuncSetAttribute(adjoint_kernel<K>, cudaFuncAttributePreferredSharedMemoryCarveout, pct)) != cudaSuccess) return e;
-  adjoint_kernel<K><<<grid, warps * 32, smem, st>>>(a);
+  if ((e = cudaFuncSetAttribute(adjoint_kernel<K, SMEM>, cudaFuncAttributePreferredSharedMemoryCarveout, pct)) != cudaSuccess) return e;
+  adjoint_kernel<K, SMEM><<<grid, warps * 32, smem, st>>>(a);
   return cudaGetLastError();
 }
 
 }  // namespace
 
-cudaError_t launch_adjoint(const AdjDev &a, int K, int warps, int grid, size_t smem, cudaStream_t st) {
-  switch (K) {
-    case 1: return launch_adj_k<1>(a, warps, grid, smem, st);
-    case 2: return launch_adj_k<2>(a, warps, grid, smem, st);
-    case 4: return launch_adj_k<4>(a, warps, grid, smem, st);
-    case 8: return launch_adj_k<8>(a, warps, grid, smem, st);
-    case 16: return launch_adj_k<16>(a, warps, grid, smem, st);
-    case 32: return launch_adj_k<32>(a, warps, grid, smem, st);
-  }
-  return cudaErrorInvalidValue;
+#ifndef CEDAR_LANES
+#error "compile with -DCEDAR_LANES=<lanes per instance>"
+#endif
+#define CEDAR_CAT2(a, b) a##b
+#define CEDAR_CAT(a, b) CEDAR_CAT2(a, b)
+
+// compiled once per lanes-per-instance value (-DCEDAR_LANES=K); k_dispatch.cu selects one
+cudaError_t CEDAR_CAT(launch_adjoint_k, CEDAR_LANES)(const AdjDev &a, int warps, int grid, size_t smem, cudaStream_t st) {
+  constexpr int K = CEDAR_LANES;
+  return a.b.ws_in_smem ? launch_adj_ks<K, true>(a, warps, grid, smem, st) : launch_adj_ks<K, false>(a, warps, grid, smem, st);
 }
 
 }  // namespace cedar

@@ -10,14 +10,18 @@ namespace cedar {
 #define CEDAR_BATCH_MIN_BLOCKS 1
 #endif
 
-template <int K>
+// SMEM: the slot workspaces live in shared memory.  Fixing this at compile time
+// lets every workspace pointer derive from the shared-memory base, so the
+// compiler issues shared-memory loads and stores rather than generic ones.
+template <int K, bool SMEM>
 __global__ void __launch_bounds__(256, CEDAR_BATCH_MIN_BLOCKS) batch_kernel(BatchDev b) {
   extern __shared__ double smem[];
   Slot<K> s;
   const int slots_per_block = blockDim.x / K;
   const int slot = threadIdx.x / K;
-  double *ws = b.ws_in_smem ? smem + (size_t)slot * b.ws_stride
-                            : b.ws_global + ((size_t)blockIdx.x * slots_per_block + slot) * b.ws_stride;
+  double *ws;
+  if constexpr (SMEM) ws = smem + (size_t)slot * b.ws_stride;
+  else ws = b.ws_global + ((size_t)blockIdx.x * slots_per_block + slot) * b.ws_stride;
   s.rp = RP_NEWINST; s.active = false;
   s.gsi = blockIdx.x * slots_per_block + slot; s.qblk = -1; s.dense = false; s.jdense = false;
   s.nrel = b.opts.nr_factor * b.opts.reltol; s.nav = b.opts.nr_factor * b.opts.abstol_v;
@@ -58,42 +62,25 @@ static cudaError_t configure(F *kern, int threads, size_t smem, int *per_sm) {
   return cudaSuccess;
 }
 
-template <int K>
-static cudaError_t launch_k(const BatchDev &b, int warps, int grid, size_t smem, cudaStream_t st) {
-  batch_kernel<K><<<grid, warps * 32, smem, st>>>(b);
+// This file is compiled once per lanes-per-instance value (-DCEDAR_LANES=K, see
+// build.py) so the instantiations build in parallel; k_dispatch.cu selects one.
+#ifndef CEDAR_LANES
+#error "compile with -DCEDAR_LANES=<lanes per instance>"
+#endif
+#define CEDAR_CAT2(a, b) a##b
+#define CEDAR_CAT(a, b) CEDAR_CAT2(a, b)
+
+cudaError_t CEDAR_CAT(launch_batch_k, CEDAR_LANES)(const BatchDev &b, int warps, int grid, size_t smem, cudaStream_t st) {
+  constexpr int K = CEDAR_LANES;
+  if (b.ws_in_smem) batch_kernel<K, true><<<grid, warps * 32, smem, st>>>(b);
+  else batch_kernel<K, false><<<grid, warps * 32, smem, st>>>(b);
   return cudaGetLastError();
 }
 
-cudaError_t launch_batch(const BatchDev &b, int K, int warps, int grid, size_t smem, cudaStream_t st) {
-  switch (K) {
-    case 1: return launch_k<1>(b, warps, grid, smem, st);
-    case 2: return launch_k<2>(b, warps, grid, smem, st);
-    case 4: return launch_k<4>(b, warps, grid, smem, st);
-    case 8: return launch_k<8>(b, warps, grid, smem, st);
-    case 16: return launch_k<16>(b, warps, grid, smem, st);
-    case 32: return launch_k<32>(b, warps, grid, smem, st);
-  }
-  return cudaErrorInvalidValue;
-}
-
-cudaError_t configure_batch(int K, int warps, size_t smem, int *per_sm) {
+cudaError_t CEDAR_CAT(configure_batch_k, CEDAR_LANES)(int warps, size_t smem, bool in_smem, int *per_sm) {
+  constexpr int K = CEDAR_LANES;
   const int th = warps * 32;
-  switch (K) {
-    case 1: return configure(batch_kernel<1>, th, smem, per_sm);
-    case 2: return configure(batch_kernel<2>, th, smem, per_sm);
-    case 4: return configure(batch_kernel<4>, th, smem, per_sm);
-    case 8: return configure(batch_kernel<8>, th, smem, per_sm);
-    case 16: return configure(batch_kernel<16>, th, smem, per_sm);
-    case 32: return configure(batch_kernel<32>, th, smem, per_sm);
-  }
-  return cudaErrorInvalidValue;
-}
-
-int batch_max_smem_optin() {
-  int dev = 0, v = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  return v;
+  return in_smem ? configure(batch_kernel<K, true>, th, smem, per_sm) : configure(batch_kernel<K, false>, th, smem, per_sm);
 }
 
 }  // namespace cedar

@@ -112,9 +112,9 @@ cudaError_t launch_fp64_probe(int active_lanes, int iters, double *gflops, doubl
 
 // batched persistent engine with K lanes per instance
 cudaError_t launch_batch(const BatchDev &b, int K, int warps_per_cta, int grid, size_t smem, cudaStream_t s);
-// set the launch attributes of batch_kernel<K> for this shape and report its
+// (k_dispatch.cu) set the launch attributes of batch_kernel<K> for this shape and report its
 // resident CTAs per SM (registers and shared memory both counted)
-cudaError_t configure_batch(int K, int warps_per_cta, size_t smem, int *per_sm);
+cudaError_t configure_batch(int K, int warps_per_cta, size_t smem, bool ws_in_smem, int *per_sm);
 int batch_max_smem_optin();
 
 }  // namespace cedar
