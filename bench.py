@@ -58,6 +58,8 @@ def parse():
     p.add_argument("--tstop-ns", type=float, default=20.0, help="transient length (20 ns for the headline)")
     p.add_argument("--fp64-probe", action="store_true", help="print the FP64 issue-rate probe (1, 8, 32 lanes) and exit")
     p.add_argument("--no-adjoint", action="store_true")
+    p.add_argument("--no-eval", action="store_true", help="skip the cedar_eval HBM leg")
+    p.add_argument("--eval-stages", type=int, default=1_000_000, help="inverter-chain stages of the cedar_eval leg")
     p.add_argument("--adj-inst", type=int, default=512, help="instances of the adjoint workload")
     p.add_argument("--adj-tstop-ns", type=float, default=20.0)
     p.add_argument("--adj-ref-inst", type=int, default=16, help="instances in the CPU adjoint sample")
@@ -197,6 +199,56 @@ def reference_adjoint(args, pkg, orc):
     return {"value": ok / dt, "unit": "instance-gradients/s", "cores": cores, "kind": "port",
             "sample": f"{k} randomly chosen instances of the {args.adj_inst}, each forward 0..{args.adj_tstop_ns:g} ns + replay + adjoint",
             "seconds": dt, "failed": k - ok}
+
+
+def measure_eval(pkg, args, torch, C):
+    """cedar_eval_dev (device evaluation + CSC stamping, the drop-in residual /
+    Jacobian boundary) on one large chain: inputs resident in HBM and larger than
+    L2, CUDA events on the handle's stream, algorithmic bytes from cedar_ckt_costs."""
+    f = pkg.generators.inverter_chain_flat(args.eval_stages)
+    sy = pkg.System(f)
+    lib = sy.lib
+    dev = torch.device("cuda:0")
+    g = torch.Generator(device=dev).manual_seed(7)
+    x = torch.rand(sy.n, dtype=torch.float64, device=dev, generator=g) * 1.8
+    xd = torch.randn(sy.n, dtype=torch.float64, device=dev, generator=g) * 1e9
+    F = torch.empty(sy.n, dtype=torch.float64, device=dev)
+    J = torch.empty(sy.nnz_j, dtype=torch.float64, device=dev)
+    costs = pkg.abi.Costs()
+    pkg.abi.check(lib.cedar_ckt_costs(sy.handle, C.byref(costs)))
+    sp = C.c_void_p()
+    pkg.abi.check(lib.cedar_ckt_stream(sy.handle, C.byref(sp)))
+    st = torch.cuda.ExternalStream(sp.value)
+    torch.cuda.synchronize()
+    ptr = lambda t: C.c_void_p(t.data_ptr())
+    call = lambda: pkg.abi.check(lib.cedar_eval_dev(sy.handle, ptr(x), ptr(xd), 1e-9, 1e12, ptr(F), ptr(J)))
+    for _ in range(3):
+        call()
+    reps = 20
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        call()
+    e1.record(st)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    peak = hbm_peak_gbs()
+    gbs = costs.bytes_eval / (ms * 1e-3) / 1e9
+    ok = bool(torch.isfinite(F).all().item() and torch.isfinite(J).all().item())
+    return {"workload": f"{args.eval_stages}-stage inverter chain ({3 * args.eval_stages} devices, n = {sy.n}, "
+                        f"nnz(J) = {sy.nnz_j}), one cedar_eval_dev per call",
+            "bytes_per_call": int(costs.bytes_eval), "ms_per_call": ms, "achieved_gbs": gbs, "peak_gbs": peak,
+            "frac": gbs / peak, "finite": ok, "kernels": ["eval_kernel", "stamp_kernel"],
+            "l2": "inputs and outputs of one call exceed L2 (129 MB)",
+            "timing": f"CUDA events on the handle's stream around {reps} calls after 3 warm-up calls"}
+
+
+def hbm_peak_gbs():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"])
+    except Exception:
+        return 6800.0   # fallback figure for GB300 when the measured file is absent
 
 
 def run_reference(args, pkg):
@@ -366,6 +418,7 @@ def main():
                "accepted_steps_mean": float(r5.stats["accepted"].mean()), "tuning": list(sw5.tuning),
                "timing": "CUDA events around the recording forward and the backward kernel"}
         del sw5
+    eval_leg = None if args.no_eval else measure_eval(pkg, args, torch, C)
     cpu = None
     if not args.no_cpu_baseline:
         cpu_line = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
@@ -395,7 +448,8 @@ def main():
                      "note": "algorithmic FP64 flops per Newton iteration (cedar_ckt_costs) x iterations / time; "
                              "peak = DFMA rate measured in this run by cedar_fp64_probe (MEASURED_PEAKS.json "
                              "has no FP64 entry); the kernel keeps its state on chip, so HBM is not its bound"},
-        "cpu_baseline": cpu, "e2e": e2e, "plain_gpu": plain, "adjoint": adj, "clocks": clk, "gpu_launches": args.steps,
+        "cpu_baseline": cpu, "e2e": e2e, "plain_gpu": plain, "adjoint": adj, "eval_hbm": eval_leg,
+        "clocks": clk, "gpu_launches": args.steps,
     }
     print(json.dumps(line), flush=True)
 

@@ -64,7 +64,7 @@ class Costs(C.Structure):
     _fields_ = [("flops_eval", C.c_int64), ("flops_stamp", C.c_int64), ("flops_lu", C.c_int64),
                 ("flops_solve", C.c_int64), ("flops_update", C.c_int64), ("bytes", C.c_int64),
                 ("lu_levels", C.c_int32), ("fw_levels", C.c_int32), ("bw_levels", C.c_int32), ("nnz_lu", C.c_int32),
-                ("ordering", C.c_int32), ("pad", C.c_int32)]
+                ("ordering", C.c_int32), ("pad", C.c_int32), ("bytes_eval", C.c_int64)]
 
 
 class Objective(C.Structure):
@@ -163,7 +163,7 @@ EXPORTS = [
     "cedar_batch_results", "cedar_batch_last_ms", "cedar_batch_set_tuning",
     "cedar_batch_get_tuning", "cedar_batch_autotune", "cedar_batch_nmax",
     "cedar_adjoint_run", "cedar_adjoint_nparams", "cedar_adjoint_tape", "cedar_adjoint_last_ms",
-    "cedar_fp64_probe",
+    "cedar_fp64_probe", "cedar_ckt_stream",
 ]
 
 _lib = None
@@ -219,6 +219,7 @@ def load_library(build_if_missing: bool = True):
         "cedar_adjoint_tape": (C.c_int, [P, C.c_int32, c_double_p, P, C.c_int64, c_int64_p]),
         "cedar_adjoint_last_ms": (C.c_int, [P, c_double_p, c_double_p]),
         "cedar_fp64_probe": (C.c_int, [C.c_int32, C.c_int32, c_double_p, c_double_p]),
+        "cedar_ckt_stream": (C.c_int, [P, C.POINTER(P)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

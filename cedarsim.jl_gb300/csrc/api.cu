@@ -355,6 +355,16 @@ int cedar_ckt_costs(const cedar_ckt *c, cedar_costs *o) {
   r.flops_update = 4 * (int64_t)H.n;
   r.bytes = dev_bytes + 4 * (int64_t)(H.jlu_ent.size() + H.fint_ent.size()) + 16 * (int64_t)H.nnz_lu +
             8 * 2 * (int64_t)H.lu_pair_a.size() + 8 * 2 * (int64_t)(H.fw_lu.size() + H.bw_lu.size()) + 8 * 6 * (int64_t)H.n;
+  {
+    int64_t eb = 0;
+    for (const GroupInfo &g : H.groups) {
+      const ModelInfo &mi = model_info(g.model);
+      eb += (int64_t)g.n_inst * (8 * mi.ndpar + 4 * g.ntx + 8 * g.ntx + 8 * mi.nout);
+    }
+    const int64_t ent = (int64_t)H.jcsc_ent.size() + (int64_t)H.forg_ent.size();
+    const int64_t ncsc = (int64_t)H.j_rowidx.size();
+    r.bytes_eval = eb + 12 * ent + 4 * (ncsc + 1 + H.n + 1) + 8 * (ncsc + H.n);
+  }
   r.lu_levels = (int32_t)H.lu_lvl_ptr.size() - 1;
   r.fw_levels = (int32_t)H.fw_lvl_ptr.size() - 1;
   r.bw_levels = (int32_t)H.bw_lvl_ptr.size() - 1;
@@ -386,6 +396,12 @@ int cedar_ckt_symbolic(const cedar_ckt *c, int32_t *rowmatch, int32_t *order, in
     if (lu_colptr) std::memcpy(lu_colptr, cp.data(), cp.size() * sizeof(int32_t));
     if (lu_rowidx) std::memcpy(lu_rowidx, ri.data(), ri.size() * sizeof(int32_t));
   }
+  return 0;
+}
+
+int cedar_ckt_stream(const cedar_ckt *c, void **stream) {
+  if (!c || !stream) return fail(CEDAR_EINVAL, "null argument");
+  *stream = static_cast<void *>(c->stream);
   return 0;
 }
 

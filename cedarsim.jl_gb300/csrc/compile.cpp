@@ -376,24 +376,34 @@ static bool compile_with(const cedar_ckt_desc *d, Template &T, std::string &err,
   T.term_int.resize(T.term_orig.size());
   for (size_t k = 0; k < T.term_orig.size(); ++k) T.term_int[k] = T.term_orig[k] < 0 ? -1 : T.iorder[T.term_orig[k]];
 
-  // symbolic LU of M[p][q] = J[eq(p)][order(q)]
-  std::vector<std::vector<int>> rows(n), cols(n);
+  // symbolic LU of M[p][q] = J[eq(p)][order(q)], row by row ("up-looking"): the
+  // pattern of row i is its own pattern closed under k -> U(k) = {q > k in row k}
+  // for every k < i in it (rows k < i already final).  A marker array makes each
+  // row cost O(its fill work), so a dense supply row costs O(n), not O(n^2).
+  std::vector<std::vector<int>> rows(n);
   for (int u = 0; u < n; ++u)
-    for (int e : colrows[u]) { int p = T.eq_pos[e], q = T.iorder[u]; rows[p].push_back(q); cols[q].push_back(p); }
-  for (int p = 0; p < n; ++p) { std::sort(rows[p].begin(), rows[p].end()); }
-  for (int k = 0; k < n; ++k) {
-    auto &ck = cols[k]; std::sort(ck.begin(), ck.end()); ck.erase(std::unique(ck.begin(), ck.end()), ck.end());
-    if (!std::binary_search(rows[k].begin(), rows[k].end(), k)) { err = "internal: missing diagonal after matching"; return false; }
-    std::vector<int> upper; for (int q : rows[k]) if (q > k) upper.push_back(q);
-    for (int i : ck) {
-      if (i <= k) continue;
-      std::vector<int> merged; merged.reserve(rows[i].size() + upper.size());
-      std::set_union(rows[i].begin(), rows[i].end(), upper.begin(), upper.end(), std::back_inserter(merged));
-      if (merged.size() != rows[i].size()) {
-        std::vector<int> added; std::set_difference(merged.begin(), merged.end(), rows[i].begin(), rows[i].end(), std::back_inserter(added));
-        for (int q : added) cols[q].push_back(i);
-        rows[i].swap(merged);
+    for (int e : colrows[u]) rows[T.eq_pos[e]].push_back(T.iorder[u]);
+  {
+    std::vector<int> mark(n, -1), work;
+    std::vector<int> first_upper(n, 0);  // position of the first entry > k in final row k
+    for (int i = 0; i < n; ++i) {
+      std::vector<int> &ri = rows[i];
+      std::vector<int> pat;
+      pat.reserve(ri.size() * 2);
+      work.clear();
+      for (int q : ri) if (mark[q] != i) { mark[q] = i; pat.push_back(q); if (q < i) work.push_back(q); }
+      while (!work.empty()) {
+        const int k = work.back(); work.pop_back();
+        const std::vector<int> &rk = rows[k];
+        for (size_t t = first_upper[k]; t < rk.size(); ++t) {
+          const int q = rk[t];
+          if (mark[q] != i) { mark[q] = i; pat.push_back(q); if (q < i) work.push_back(q); }
+        }
       }
+      std::sort(pat.begin(), pat.end());
+      if (!std::binary_search(pat.begin(), pat.end(), i)) { err = "internal: missing diagonal after matching"; return false; }
+      ri.swap(pat);
+      first_upper[i] = (int)(std::upper_bound(ri.begin(), ri.end(), i) - ri.begin());
     }
   }
   T.lu_rowptr.assign(n + 1, 0);
@@ -454,14 +464,27 @@ static bool compile_with(const cedar_ckt_desc *d, Template &T, std::string &err,
     int s = slot(i, j); int m = std::min(i, j);
     Task tk; tk.slot = s; tk.info = (j << 2) | (i == j ? 1 : (i > j ? 2 : 0));
     // pairs k < m with (i,k) and (k,j)
-    const int *ri = &T.lu_colidx[T.lu_rowptr[i]]; int nri = T.lu_rowptr[i + 1] - T.lu_rowptr[i];
+    // walk the shorter of (row i below m) and (column j below m), binary-search the
+    // other: a dense supply row then costs O(its column lengths), not O(n) per task
+    const int *ri = &T.lu_colidx[T.lu_rowptr[i]];
+    const int nri = (int)(std::lower_bound(ri, ri + (T.lu_rowptr[i + 1] - T.lu_rowptr[i]), m) - ri);
     const std::vector<int> &cj = lucol[j];
-    int a = 0, b = 0, L = 0;
-    while (a < nri && b < (int)cj.size()) {
-      int ka = ri[a], kb = cj[b];
-      if (ka >= m || kb >= m) break;
-      if (ka == kb) { int sa = T.lu_rowptr[i] + a, sb = slot(ka, j); tk.pairs.push_back({sa, sb}); L = std::max(L, std::max(lev[sa], lev[sb]) + 1); ++a; ++b; }
-      else if (ka < kb) ++a; else ++b;
+    const int ncj = (int)(std::lower_bound(cj.begin(), cj.end(), m) - cj.begin());
+    int L = 0;
+    auto add_pair = [&](int k, int sa) {
+      const int sb = slot(k, j);
+      tk.pairs.push_back({sa, sb});
+      L = std::max(L, std::max(lev[sa], lev[sb]) + 1);
+    };
+    if (nri <= ncj) {
+      for (int a = 0; a < nri; ++a)
+        if (std::binary_search(cj.begin(), cj.begin() + ncj, ri[a])) add_pair(ri[a], T.lu_rowptr[i] + a);
+    } else {
+      for (int b = 0; b < ncj; ++b) {
+        const int k = cj[b];
+        const int *it = std::lower_bound(ri, ri + nri, k);
+        if (it != ri + nri && *it == k) add_pair(k, T.lu_rowptr[i] + (int)(it - ri));
+      }
     }
     if (i > j) L = std::max(L, lev[T.lu_diag[j]] + 1);
     tk.lev = L; lev[s] = L;

@@ -103,6 +103,40 @@ def inverter_chain(stages: int = 31, cload: float = INV["cload"], wave: Pulse = 
     return ckt
 
 
+def inverter_chain_flat(stages: int, cload: float = INV["cload"], wave: Pulse = INV_PULSE, ordering: int = 1) -> Flat:
+    """The flattened inverter chain built directly with numpy (same devices, nodes
+    and parameters as inverter_chain(stages).flatten(); the per-device name index
+    is left empty), for chains of a million stages.  Nodes: in, vdd, out1..outL;
+    branches: VIN.I, VDD.I."""
+    from .circuit import V as MODEL_V, WAVE_PULSE
+    L = int(stages)
+    n_nodes = L + 2
+    k = np.arange(1, L + 1)
+    out = 1 + k
+    inp = np.where(k == 1, 0, out - 1)
+    cap_term = np.stack([out, np.full(L, -1)], axis=1)
+    cap_par = np.stack([np.full(L, cload), np.ones(L)])
+    vterm = np.array([[0, -1], [1, -1]])
+    vbr = np.array([n_nodes, n_nodes + 1])
+    vpar = np.zeros((10, 2))
+    vpar[0] = 1.0
+    vpar[1] = [wave.v1, INV["vdd"]]
+    vpar[2] = [WAVE_PULSE, 0.0]
+    vpar[3:10, 0] = [wave.v1, wave.v2, wave.td, wave.tr, wave.tf, wave.pw, wave.per]
+    # MOSFETs in device order MN1, MP1, MN2, MP2, ...
+    d = np.repeat(out, 2); g = np.repeat(inp, 2)
+    is_p = np.tile([False, True], L)
+    src = np.where(is_p, 1, -1); bulk = src
+    mterm = np.stack([d, g, src, bulk], axis=1)
+    mpar = np.stack([np.where(is_p, -1.0, 1.0), np.where(is_p, INV["wp"], INV["wn"]), np.where(is_p, INV["lp"], INV["ln"]),
+                     np.where(is_p, INV["kp_p"], INV["kp_n"]), np.where(is_p, INV["vth_p"], INV["vth_n"]),
+                     np.zeros(2 * L), np.ones(2 * L)])
+    groups = [(MODEL_C, cap_term.astype(np.int32), None, cap_par), (MODEL_V, vterm.astype(np.int32), vbr.astype(np.int32), vpar),
+              (MOS1, mterm.astype(np.int32), None, mpar)]
+    names = ["in", "vdd"] + [f"out{i}" for i in range(1, L + 1)] + ["VIN.I", "VDD.I"]
+    return Flat(n_nodes, 2, groups, np.zeros(0), 27.0, 1e-12, names, {}, ordering)
+
+
 # ---------------------------------------------------------------- workload 3
 MC_LENGTHS = list(range(5, 64, 2))
 

@@ -211,8 +211,15 @@ typedef struct cedar_costs {
   int32_t lu_levels, fw_levels, bw_levels, nnz_lu;
   int32_t ordering;      /* CEDAR_ORDER_* actually used                         */
   int32_t pad;
+  int64_t bytes_eval;    /* one cedar_eval_dev: derived params, terminal indices,
+                            x gathers and outputs of every device, then stamp
+                            entries, output reads, J and F written             */
 } cedar_costs;
 int cedar_ckt_costs(const cedar_ckt *ckt, cedar_costs *out);
+/* The CUDA stream a handle's device work runs on (cedar_eval_dev and the
+ * single-circuit entry points), for callers that order or time their own work
+ * against it. */
+int cedar_ckt_stream(const cedar_ckt *ckt, void **stream);
 
 /* J pattern in compressed-sparse-column form over the ORIGINAL unknown order:
  * colptr[n+1], rowidx[nnz_j].  Jvals returned by cedar_eval follow this order. */

@@ -128,3 +128,15 @@ def test_errors(pkg):
     assert rc == -1
     # null descriptor
     assert lib.cedar_plan_create(None, C.byref(C.c_void_p())) == -1
+
+
+def test_vectorised_chain_generator_matches_builder(pkg):
+    """inverter_chain_flat (numpy, for million-stage chains) builds exactly what
+    the netlist builder flattens."""
+    for L in (1, 2, 9):
+        a = pkg.generators.inverter_chain(L).flatten()
+        b = pkg.generators.inverter_chain_flat(L)
+        assert (a.n_nodes, a.n_branch, a.names) == (b.n_nodes, b.n_branch, b.names)
+        for (ma, ta, ba, pa), (mb, tb, bb, pb) in zip(a.groups, b.groups):
+            assert ma == mb and np.array_equal(ta, tb) and np.array_equal(pa, pb)
+            assert (ba is None and bb is None) or np.array_equal(ba, bb)
