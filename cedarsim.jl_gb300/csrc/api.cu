@@ -13,6 +13,8 @@
 using namespace cedar;
 
 static_assert(sizeof(EngStats) == sizeof(cedar_stats), "stats layout");
+static_assert(kLongGatherHost == kLongGather && kLongEvalHost == kLongEval, "long gather thresholds");
+static_assert(kLongChunk == 64, "cedar_eval long-list chunk (k_plain.cu kLongChunkDev)");
 
 namespace {
 
@@ -120,6 +122,8 @@ int upload_template(const cedar_ckt_desc *desc, std::unique_ptr<DevTemplate> &ou
   };
   size_t o_lu_task = P.vec(lu_task), o_fw_task = P.vec(row_tasks(H.fw_row, H.fw_ptr)), o_bw_task = P.vec(row_tasks(H.bw_row, H.bw_ptr));
   size_t o_tf_task = P.vec(row_tasks(H.tf_row, H.tf_ptr)), o_tb_task = P.vec(row_tasks(H.tb_row, H.tb_ptr));
+  size_t o_long_lu = P.vec(H.long_lu), o_long_fi = P.vec(H.long_fi), o_long_jc = P.vec(H.long_jc), o_long_fo = P.vec(H.long_fo);
+  size_t o_long_off = P.vec(H.long_jc_fo_off);
   CUDA_TRY(cudaMalloc(&dt->buf, P.bytes.size()));
   CUDA_TRY(cudaMemcpy(dt->buf, P.bytes.data(), P.bytes.size(), cudaMemcpyHostToDevice));
   char *b = (char *)dt->buf;
@@ -153,6 +157,11 @@ int upload_template(const cedar_ckt_desc *desc, std::unique_ptr<DevTemplate> &ou
   D.lu_orig = (const int2 *)(b + o_lu_orig);
   D.lu_task = (const int4 *)(b + o_lu_task); D.fw_task = (const int4 *)(b + o_fw_task); D.bw_task = (const int4 *)(b + o_bw_task);
   D.tf_task = (const int4 *)(b + o_tf_task); D.tb_task = (const int4 *)(b + o_tb_task);
+  D.n_long_lu = (int)H.long_lu.size(); D.n_long_fi = (int)H.long_fi.size();
+  D.n_long_jc = (int)H.long_jc.size(); D.n_long_fo = (int)H.long_fo.size();
+  D.long_lu = (const int *)(b + o_long_lu); D.long_fi = (const int *)(b + o_long_fi);
+  D.long_jc = (const int *)(b + o_long_jc); D.long_fo = (const int *)(b + o_long_fo);
+  D.long_off = (const int *)(b + o_long_off); D.n_long_part = H.long_jc_fo_off.back();
   CUDA_TRY(cudaMalloc(&dt->D_dev, sizeof(DTpl)));
   CUDA_TRY(cudaMemcpy(dt->D_dev, &D, sizeof(DTpl), cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMalloc(&dt->par_dev, std::max<size_t>(1, H.par.size()) * sizeof(double)));
@@ -207,7 +216,7 @@ template <class T> struct DevBuf {
 struct cedar_ckt {
   std::unique_ptr<DevTemplate> tpl;
   cudaStream_t stream = nullptr;
-  DevBuf<double> dpar, x, xdot, F, J, dout, hist, ws, tout, xout, dense;
+  DevBuf<double> dpar, x, xdot, F, J, dout, hist, ws, tout, xout, dense, part;
   DevBuf<EngStats> stats;
   DevBuf<long long> count;
   DevBuf<long long> off;
@@ -287,6 +296,7 @@ int cedar_ckt_create(const cedar_ckt_desc *desc, cedar_ckt **out) {
   int n = H.n;
   CUDA_TRY(c->x.ensure(n)); CUDA_TRY(c->xdot.ensure(n)); CUDA_TRY(c->F.ensure(n)); CUDA_TRY(c->hist.ensure(n));
   CUDA_TRY(c->J.ensure(H.j_rowidx.size())); CUDA_TRY(c->dout.ensure(H.n_out));
+  CUDA_TRY(c->part.ensure(std::max(1, H.long_jc_fo_off.back())));
   CUDA_TRY(c->stats.ensure(1)); CUDA_TRY(c->count.ensure(1));
   size_t wsd = ws_doubles(H.n, H.nnz_lu, H.n_out, (int)H.src_group.size());
   if ((wsd + 128) * sizeof(double) > 160 * 1024) CUDA_TRY(c->ws.ensure(wsd));
@@ -408,7 +418,7 @@ int cedar_ckt_stream(const cedar_ckt *c, void **stream) {
 int cedar_eval_dev(cedar_ckt *c, const double *x, const double *xdot, double t, double cj, double *F, double *J) {
   if (!c || !x) return fail(CEDAR_EINVAL, "null argument");
   if (c->host_only) return fail(CEDAR_EINVAL, "host-only plan handle");
-  CUDA_TRY(launch_eval(c->tpl->D, c->tpl->D_dev, c->dpar.p, x, xdot, t, cj, c->dout.p, F, J, c->stream));
+  CUDA_TRY(launch_eval(c->tpl->D, c->tpl->D_dev, c->dpar.p, x, xdot, t, cj, c->dout.p, c->part.p, F, J, c->stream));
   return 0;
 }
 
@@ -417,13 +427,14 @@ int cedar_eval_dev_noalloc(cedar_ckt *c, const double *x, const double *xdot, do
   if (!c || !x) return fail(CEDAR_EINVAL, "null argument");
   if (c->host_only) return fail(CEDAR_EINVAL, "host-only plan handle");
   const DTpl &T = c->tpl->D;
-  if (T.n_out > kEvalScratchMax)
-    return fail(CEDAR_EINVAL, "circuit has " + std::to_string(T.n_out) + " device outputs; the allocation-free "
+  if ((long long)T.n_out + T.n_long_part > kEvalScratchMax)
+    return fail(CEDAR_EINVAL, "circuit needs " + std::to_string((long long)T.n_out + T.n_long_part) +
+                " doubles of evaluation scratch (device outputs and long-row partial sums); the allocation-free "
                 "evaluation holds at most " + std::to_string(kEvalScratchMax));
   double *scratch = nullptr;
   CUDA_TRY(eval_scratch_address(&scratch));
   cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
-  CUDA_TRY(launch_eval(T, c->tpl->D_dev, c->dpar.p, x, xdot, t, cj, scratch, F, J, s));
+  CUDA_TRY(launch_eval(T, c->tpl->D_dev, c->dpar.p, x, xdot, t, cj, scratch, scratch + T.n_out, F, J, s));
   return 0;
 }
 
@@ -435,7 +446,7 @@ int cedar_eval(cedar_ckt *c, const double *x, const double *xdot, double t, doub
   CUDA_TRY(cudaMemcpyAsync(c->x.p, x, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   if (xdot) CUDA_TRY(cudaMemcpyAsync(c->xdot.p, xdot, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   CUDA_TRY(launch_eval(c->tpl->D, c->tpl->D_dev, c->dpar.p, c->x.p, xdot ? c->xdot.p : nullptr, t, cj, c->dout.p,
-                       F ? c->F.p : nullptr, J ? c->J.p : nullptr, c->stream));
+                       c->part.p, F ? c->F.p : nullptr, J ? c->J.p : nullptr, c->stream));
   if (F) CUDA_TRY(cudaMemcpyAsync(F, c->F.p, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   if (J) CUDA_TRY(cudaMemcpyAsync(J, c->J.p, nj * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(cudaStreamSynchronize(c->stream));

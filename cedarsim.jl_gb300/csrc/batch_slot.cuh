@@ -737,8 +737,22 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am, const 
   }
   __syncwarp(am);
   // K2: stamping (fixed-order gathers)
-  for (int q = rank; q < T.nnz_lu; q += K) lu[q] = gather(T.jlu_ptr, T.jlu_ent, q, 0.0);
-  for (int r = rank; r < T.n; r += K) F[r] = gather(T.fint_ptr, T.fint_ent, r, jhist ? jhist[r] : 0.0);
+  // lists longer than kLongGather (supply rails) are left to the slot-collective
+  // sums below
+  for (int q = rank; q < T.nnz_lu; q += K)
+    if (T.jlu_ptr[q + 1] - T.jlu_ptr[q] <= kLongGather) lu[q] = gather(T.jlu_ptr, T.jlu_ent, q, 0.0);
+  for (int r = rank; r < T.n; r += K)
+    if (T.fint_ptr[r + 1] - T.fint_ptr[r] <= kLongGather) F[r] = gather(T.fint_ptr, T.fint_ent, r, jhist ? jhist[r] : 0.0);
+  for (int t = 0; t < T.n_long_lu; ++t) {
+    const int q = T.long_lu[t];
+    const double v = long_gather<K>(T.jlu_ptr, T.jlu_ent, q, dout, rank, s.smask());
+    if (rank == 0) lu[q] = v;
+  }
+  for (int t = 0; t < T.n_long_fi; ++t) {
+    const int r = T.long_fi[t];
+    const double v = long_gather<K>(T.fint_ptr, T.fint_ent, r, dout, rank, s.smask());
+    if (rank == 0) F[r] = (jhist ? jhist[r] : 0.0) + v;
+  }
   __syncwarp(am);
   if (jgs != 0.0) {
     for (int u = rank; u < T.n_nodes; u += K) {

@@ -445,6 +445,17 @@ static bool compile_with(const cedar_ckt_desc *d, Template &T, std::string &err,
     it.clear();
     for (const Stamp &s : SQ) it.push_back({T.eq_pos[s.row], enc(s)});
     build_program(n, it, T.qint_ptr, T.qint_ent);
+    auto longs = [](const std::vector<int32_t> &ptr, int lim, std::vector<int32_t> &out) {
+      out.clear();
+      for (size_t q = 0; q + 1 < ptr.size(); ++q) if (ptr[q + 1] - ptr[q] > lim) out.push_back((int32_t)q);
+    };
+    longs(T.jlu_ptr, kLongGatherHost, T.long_lu);
+    longs(T.fint_ptr, kLongGatherHost, T.long_fi);
+    longs(T.jcsc_ptr, kLongEvalHost, T.long_jc);
+    longs(T.forg_ptr, kLongEvalHost, T.long_fo);
+    T.long_jc_fo_off.assign(1, 0);
+    for (int32_t q : T.long_jc) T.long_jc_fo_off.push_back(T.long_jc_fo_off.back() + (T.jcsc_ptr[q + 1] - T.jcsc_ptr[q] + kLongChunk - 1) / kLongChunk);
+    for (int32_t q : T.long_fo) T.long_jc_fo_off.push_back(T.long_jc_fo_off.back() + (T.forg_ptr[q + 1] - T.forg_ptr[q] + kLongChunk - 1) / kLongChunk);
     // C^T program: per internal column q, the charge-partial stamps of column q
     // with their internal rows, in device order
     std::vector<std::pair<int, int32_t>> ic;

@@ -76,6 +76,10 @@ struct Template {
   std::vector<int32_t> tb_lvl_ptr, tb_row, tb_ptr, tb_lu, tb_col;
   // C^T program per internal column: entry ((out << 1) | neg) and internal row
   std::vector<int32_t> ct_ptr, ct_ent, ct_row;
+  // gather lists longer than kLongGather (in-engine programs) or kLongEval
+  // (cedar_eval programs): summed cooperatively (fixed chunks, fixed tree)
+  std::vector<int32_t> long_jc_fo_off;  // chunk offsets (kLongChunk entries each) of long_jc then long_fo
+  std::vector<int32_t> long_lu, long_fi, long_jc, long_fo;
   // adjoint parameters: first gradient index of each group (-1: none); MOS1
   // widths and resistor values, in group order
   std::vector<int32_t> adj_goff;
@@ -89,6 +93,12 @@ struct Template {
   int ordering = 0;       // ordering actually used
   double sched_cost = 0;  // estimated critical path of LU + substitutions
 };
+
+// Gather lists longer than these are summed cooperatively on the device (must
+// equal kLongGather / kLongEval of engine.cuh).
+constexpr int kLongGatherHost = 16, kLongEvalHost = 64;
+// cedar_eval sums a long list in chunks of this many entries (one thread each)
+constexpr int kLongChunk = 64;
 
 // Ordering strategies for the fill-reducing symmetric permutation.
 enum Ordering { ORDER_AUTO = 0, ORDER_MIN_DEGREE = 1, ORDER_NESTED_DISSECTION = 2, ORDER_NATURAL = 3 };

@@ -55,11 +55,52 @@ struct DTpl {
   // the same task lists packed one 16-byte record per task: LU (slot, info,
   // first pair, end pair); substitutions (row, first pair, end pair, 0)
   const int4 *lu_task, *fw_task, *bw_task, *tf_task, *tb_task;
+  // long gather lists (see kLongGather / kLongEval): LU slots, residual rows
+  // (internal), CSC slots and residual rows (original order)
+  int n_long_lu, n_long_fi, n_long_jc, n_long_fo;
+  const int *long_lu, *long_fi, *long_jc, *long_fo;
+  // cedar_eval: chunk offsets of the long CSC slots then the long residual rows
+  // (n_long_jc + n_long_fo + 1 entries); n_long_part chunks in all
+  const int *long_off; int n_long_part, pad_long;
   const int *tf_lvl, *tf_row, *tf_ptr; const int2 *tf_pair;
   const int *tb_lvl, *tb_row, *tb_ptr; const int2 *tb_pair;
   const int *ct_ptr; const int2 *ct_ent;
   const int *adj_goff;
 };
+
+// Gather lists longer than these are summed cooperatively in 32 fixed chunks
+// combined by a fixed pairwise tree (in-engine stamp programs / cedar_eval's).
+constexpr int kLongGather = 16;
+constexpr int kLongEval = 64;
+
+// Sum of a long gather list (entries (out << 1) | neg into dout) by the K lanes
+// of a group (mask, rank): the list is cut into 32 fixed chunks, each summed in
+// order, and the chunk sums are combined by a fixed pairwise tree.  A lane owns
+// chunks [rank * 32/K, (rank + 1) * 32/K), so the lower tree levels are lane-local
+// and the upper ones a butterfly: the result is the same bits for every K.
+template <int K>
+__device__ __forceinline__ double long_gather(const int *ptr, const int *ent, int q, const double *dout, int rank,
+                                              unsigned mask) {
+  const int a = ptr[q], len = ptr[q + 1] - a;
+  constexpr int PER = 32 / K;
+  double part[PER];
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    const int c = rank * PER + j;
+    const int c0 = a + (int)(((long long)len * c) >> 5), c1 = a + (int)(((long long)len * (c + 1)) >> 5);
+    double acc = 0.0;
+    for (int k = c0; k < c1; ++k) { const int e = ent[k]; const double v = dout[e >> 1]; acc = (e & 1) ? acc - v : acc + v; }
+    part[j] = acc;
+  }
+#pragma unroll
+  for (int w = 1; w < PER; w <<= 1)
+#pragma unroll
+    for (int j = 0; j + w < PER; j += 2 * w) part[j] = part[j] + part[j + w];
+  double v = part[0];
+#pragma unroll
+  for (int o = 1; o < K; o <<= 1) { const double u = __shfl_xor_sync(mask, v, o, K); v = (rank & o) ? u + v : v + u; }
+  return v;
+}
 
 // workspace size in doubles for one instance
 __host__ __device__ inline int ws_doubles(int n, int nnz_lu, int n_out, int n_src) {
@@ -326,8 +367,23 @@ struct Engine {
   // K2: J slots and residual rows (F = hist + contributions)
   // gshunt (DC homotopy): node rows get -gshunt * (x - xref) (xref null = ground)
   __device__ void stamp(const double *hist, double gshunt, const double *x, const double *xref) {
-    for (int s = g.rank; s < T.nnz_lu; s += g.size) w.lu[s] = gather(T.jlu_ptr, T.jlu_ent, s, 0.0);
-    for (int r = g.rank; r < T.n; r += g.size) w.F[r] = gather(T.fint_ptr, T.fint_ent, r, hist ? hist[r] : 0.0);
+    for (int s = g.rank; s < T.nnz_lu; s += g.size)
+      if (T.jlu_ptr[s + 1] - T.jlu_ptr[s] <= kLongGather) w.lu[s] = gather(T.jlu_ptr, T.jlu_ent, s, 0.0);
+    for (int r = g.rank; r < T.n; r += g.size)
+      if (T.fint_ptr[r + 1] - T.fint_ptr[r] <= kLongGather) w.F[r] = gather(T.fint_ptr, T.fint_ent, r, hist ? hist[r] : 0.0);
+    // long lists (supply rails): the first warp sums each in fixed chunks
+    if (g.rank < 32) {
+      for (int t = 0; t < T.n_long_lu; ++t) {
+        const int q = T.long_lu[t];
+        const double v = long_gather<32>(T.jlu_ptr, T.jlu_ent, q, w.dout, g.rank, 0xffffffffu);
+        if (g.rank == 0) w.lu[q] = v;
+      }
+      for (int t = 0; t < T.n_long_fi; ++t) {
+        const int r = T.long_fi[t];
+        const double v = long_gather<32>(T.fint_ptr, T.fint_ent, r, w.dout, g.rank, 0xffffffffu);
+        if (g.rank == 0) w.F[r] = (hist ? hist[r] : 0.0) + v;
+      }
+    }
     if (gshunt != 0.0) {
       g.sync();
       for (int u = g.rank; u < T.n_nodes; u += g.size) {

@@ -266,7 +266,13 @@ __device__ __forceinline__ void backward_step(AdjSlot<K> &s, const AdjDev &a, un
     });
   }
   __syncwarp(ab);
-  for (int q = rank; q < T.nnz_lu; q += K) s.w.lu[q] = s.gather(T.jlu_ptr, T.jlu_ent, q, 0.0);
+  for (int q = rank; q < T.nnz_lu; q += K)
+    if (T.jlu_ptr[q + 1] - T.jlu_ptr[q] <= kLongGather) s.w.lu[q] = s.gather(T.jlu_ptr, T.jlu_ent, q, 0.0);
+  for (int t = 0; t < T.n_long_lu; ++t) {
+    const int q = T.long_lu[t];
+    const double v = long_gather<K>(T.jlu_ptr, T.jlu_ent, q, s.w.dout, rank, s.smask());
+    if (rank == 0) s.w.lu[q] = v;
+  }
   __syncwarp(ab);
   // (3) LU by levels
   bool bad = false;
@@ -320,30 +326,29 @@ __device__ __forceinline__ void backward_step(AdjSlot<K> &s, const AdjDev &a, un
   // (5) parameter partials: grad += lam^T dFi/dp (each lane owns its devices);
   // the KCL equation of terminal unknown u sits in internal row eq_pos[u]
   if (!slot_bad) {
-    for (int d = rank; d < T.n_dev; d += K) {
-      int gi = 0;
-      while (d >= T.dev_end[gi]) ++gi;
+    for (int gi = 0; gi < T.n_groups; ++gi) {
       const int goff = T.adj_goff[gi];
       if (goff < 0) continue;
       const DGroup gr = T.grp[gi];
-      const int i = d - (gi ? T.dev_end[gi - 1] : 0);
-      const int *to = T.term_orig + gr.term_off + i * gr.ntx;
-      const int *tm = T.term + gr.term_off + i * gr.ntx;
-      const double o0 = s.w.dout[gr.out_off + i * model_nout(gr.model)];
-      if (gr.model == CEDAR_MOS1) {
-        // d(m Ids)/dW = m type id / W (id is linear in beta = KP W / L); KCL(d) -, KCL(s) +
-        const double W = s.raw[gr.par_off + gr.n_inst + i];
-        const double m = s.dp[gr.dpar_off + 4 * gr.n_inst + i];
-        const double vd = tm[0] < 0 ? 0.0 : x[tm[0]], vs = tm[2] < 0 ? 0.0 : x[tm[2]];
-        const double dI = (o0 - m * (T.gmin * (vd - vs))) / W;
-        const double ld = to[0] < 0 ? 0.0 : r[T.eq_pos[to[0]]], ls = to[2] < 0 ? 0.0 : r[T.eq_pos[to[2]]];
-        s.gacc[goff + i] += -dI * ld + dI * ls;
-      } else {
-        // d(m V / r)/dr = -out0 / r; KCL(p) -, KCL(n) +
-        const double rr = s.raw[gr.par_off + i];
-        const double dI = -o0 / rr;
-        const double lp = to[0] < 0 ? 0.0 : r[T.eq_pos[to[0]]], ln = to[1] < 0 ? 0.0 : r[T.eq_pos[to[1]]];
-        s.gacc[goff + i] += -dI * lp + dI * ln;
+      for (int i = rank; i < gr.n_inst; i += K) {
+        const int *to = T.term_orig + gr.term_off + i * gr.ntx;
+        const int *tm = T.term + gr.term_off + i * gr.ntx;
+        const double o0 = s.w.dout[gr.out_off + i * model_nout(gr.model)];
+        if (gr.model == CEDAR_MOS1) {
+          // d(m Ids)/dW = m type id / W (id is linear in beta = KP W / L); KCL(d) -, KCL(s) +
+          const double W = s.raw[gr.par_off + gr.n_inst + i];
+          const double m = s.dp[gr.dpar_off + 4 * gr.n_inst + i];
+          const double vd = tm[0] < 0 ? 0.0 : x[tm[0]], vs = tm[2] < 0 ? 0.0 : x[tm[2]];
+          const double dI = (o0 - m * (T.gmin * (vd - vs))) / W;
+          const double ld = to[0] < 0 ? 0.0 : r[T.eq_pos[to[0]]], ls = to[2] < 0 ? 0.0 : r[T.eq_pos[to[2]]];
+          s.gacc[goff + i] += -dI * ld + dI * ls;
+        } else {
+          // d(m V / r)/dr = -out0 / r; KCL(p) -, KCL(n) +
+          const double rr = s.raw[gr.par_off + i];
+          const double dI = -o0 / rr;
+          const double lp = to[0] < 0 ? 0.0 : r[T.eq_pos[to[0]]], ln = to[1] < 0 ? 0.0 : r[T.eq_pos[to[1]]];
+          s.gacc[goff + i] += -dI * lp + dI * ln;
+        }
       }
     }
   }

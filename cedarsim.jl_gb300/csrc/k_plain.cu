@@ -58,27 +58,77 @@ __global__ void eval_kernel(DTpl T, const double *dpar, const double *x, const d
 }
 
 // K2+K3 (grid-wide): J values in CSC order and residual rows, fixed-order sums.
+// Lists longer than kLongEval (supply rails) are left to stamp_long_kernel.
 __global__ void stamp_kernel(DTpl T, const double *dout, double *F, double *J) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (J && s < T.n_csc) {
+  if (J && s < T.n_csc && T.jcsc_ptr[s + 1] - T.jcsc_ptr[s] <= kLongEval) {
     double acc = 0.0;
     for (int k = T.jcsc_ptr[s]; k < T.jcsc_ptr[s + 1]; ++k) { int e = __ldg(T.jcsc_ent + k); double v = __ldg(dout + (e >> 1)); acc = (e & 1) ? acc - v : acc + v; }
     J[s] = acc;
   }
-  if (F && s < T.n) {
+  if (F && s < T.n && T.forg_ptr[s + 1] - T.forg_ptr[s] <= kLongEval) {
     double acc = 0.0;
     for (int k = T.forg_ptr[s]; k < T.forg_ptr[s + 1]; ++k) { int e = __ldg(T.forg_ent + k); double v = __ldg(dout + (e >> 1)); acc = (e & 1) ? acc - v : acc + v; }
     F[s] = acc;
   }
 }
 
+// Long lists (supply rails), pass 1: one thread per fixed chunk of kLongChunk
+// entries, summed in order into part[] (chunk p of list i at long_off[i] + p).
+constexpr int kLongChunkDev = 64;
+__global__ void stamp_long_part_kernel(DTpl T, const double *dout, double *part) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= T.n_long_part) return;
+  const int nl = T.n_long_jc + T.n_long_fo;
+  int lo = 0, hi = nl;                       // list i with long_off[i] <= p < long_off[i + 1]
+  while (hi - lo > 1) { const int mid = (lo + hi) >> 1; if (T.long_off[mid] <= p) lo = mid; else hi = mid; }
+  const bool is_j = lo < T.n_long_jc;
+  const int q = is_j ? T.long_jc[lo] : T.long_fo[lo - T.n_long_jc];
+  const int *ptr = is_j ? T.jcsc_ptr : T.forg_ptr, *ent = is_j ? T.jcsc_ent : T.forg_ent;
+  const int k0 = ptr[q] + (p - T.long_off[lo]) * kLongChunkDev;
+  const int k1 = min(k0 + kLongChunkDev, ptr[q + 1]);
+  double acc = 0.0;
+  for (int k = k0; k < k1; ++k) { const int e = __ldg(ent + k); const double v = __ldg(dout + (e >> 1)); acc = (e & 1) ? acc - v : acc + v; }
+  part[p] = acc;
+}
+
+// Pass 2: one CTA per long list; thread t sums its contiguous share of the
+// list's chunk sums in order, then a fixed pairwise tree over the threads.
+constexpr int kLongThreads = 256;
+__global__ void __launch_bounds__(kLongThreads) stamp_long_final_kernel(DTpl T, const double *part, double *F, double *J) {
+  __shared__ double red[kLongThreads];
+  const int i = blockIdx.x;
+  const bool is_j = i < T.n_long_jc;
+  const int q = is_j ? T.long_jc[i] : T.long_fo[i - T.n_long_jc];
+  const int p0 = T.long_off[i], np = T.long_off[i + 1] - p0;
+  const int a = p0 + (int)(((long long)np * threadIdx.x) / kLongThreads);
+  const int b = p0 + (int)(((long long)np * (threadIdx.x + 1)) / kLongThreads);
+  double acc = 0.0;
+  for (int k = a; k < b; ++k) acc += part[k];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = 1; w < kLongThreads; w <<= 1) {
+    if ((threadIdx.x & (2 * w - 1)) == 0) red[threadIdx.x] = red[threadIdx.x] + red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    if (is_j) { if (J) J[q] = red[0]; }
+    else if (F) F[q] = red[0];
+  }
+}
+
 cudaError_t launch_eval(const DTpl &T, const DTpl *T_dev, const double *dpar, const double *x, const double *xdot,
-                        double t, double cj, double *dout, double *F, double *J, cudaStream_t s) {
+                        double t, double cj, double *dout, double *part, double *F, double *J, cudaStream_t s) {
   (void)T_dev;
   const int th = 256;
   if (T.n_dev > 0) eval_kernel<<<(T.n_dev + th - 1) / th, th, 0, s>>>(T, dpar, x, xdot, t, cj, dout);
   int m = T.n_csc > T.n ? T.n_csc : T.n;
   stamp_kernel<<<(m + th - 1) / th, th, 0, s>>>(T, dout, F, J);
+  const int nlong = T.n_long_jc + T.n_long_fo;
+  if (nlong > 0) {
+    stamp_long_part_kernel<<<(T.n_long_part + th - 1) / th, th, 0, s>>>(T, dout, part);
+    stamp_long_final_kernel<<<nlong, kLongThreads, 0, s>>>(T, part, F, J);
+  }
   return cudaGetLastError();
 }
 

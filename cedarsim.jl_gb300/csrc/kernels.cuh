@@ -81,8 +81,9 @@ cudaError_t launch_derive(const DTpl *tpls_dev, const int *inst_tpl, const long 
                           const long long *dpar_off, double *dpar, int n_inst, int max_dev, cudaStream_t s);
 
 // cedar_eval: device outputs then CSC Jacobian values and residual rows
+// (dout: n_out doubles; part: n_long_part doubles for the long-list partial sums)
 cudaError_t launch_eval(const DTpl &T, const DTpl *T_dev, const double *dpar, const double *x, const double *xdot,
-                        double t, double cj, double *dout, double *F, double *J, cudaStream_t s);
+                        double t, double cj, double *dout, double *part, double *F, double *J, cudaStream_t s);
 
 // Fixed-size device scratch for the allocation-free evaluation entry point:
 // kEvalScratchMax doubles (2 MiB) per device, i.e. circuits with at most that many

@@ -244,8 +244,9 @@ int cedar_eval_dev(cedar_ckt *ckt, const double *x, const double *xdot, double t
  * and hosts whose device memory is reserved up front by another runtime's pool
  * allocator (a cudaMalloc there fails or stalls the host's own work).
  * It has no counterpart in the reference.  It calls no cudaMalloc or cudaFree:
- * its scratch (the per-device model outputs, at most 262144 doubles = 2 MiB, a
- * larger circuit returns CEDAR_EINVAL) is a fixed array that every GPU loading
+ * its scratch (the per-device model outputs plus the partial sums of
+ * supply-rail rows, at most 262144 doubles = 2 MiB; a larger circuit returns
+ * CEDAR_EINVAL) is a fixed array that every GPU loading
  * the library holds until the process exits.  The first call on a device looks
  * up that array's device address (cudaGetSymbolAddress with the device current)
  * and caches it, so make the first call on each device before any stream

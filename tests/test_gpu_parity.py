@@ -28,6 +28,8 @@ def random_state(flat, rng, scale=1.8):
 EVAL_CASES = {
     "rc_ladder": lambda pkg: pkg.generators.rc_ladder(100),
     "inverter_chain_7": lambda pkg: pkg.generators.inverter_chain(7),
+    # supply-rail lists of 200+ entries take the cooperative long-list sums
+    "inverter_chain_100": lambda pkg: pkg.generators.inverter_chain(100),
     "mixed": K.mixed,
     "spice_sources": K.spice_sources,
     "nlvcr": K.nlvcr,
