@@ -59,6 +59,9 @@ def parse():
     p.add_argument("--fp64-probe", action="store_true", help="print the FP64 issue-rate probe (1, 8, 32 lanes) and exit")
     p.add_argument("--no-adjoint", action="store_true")
     p.add_argument("--no-eval", action="store_true", help="skip the cedar_eval HBM leg")
+    p.add_argument("--no-rings", action="store_true", help="skip the ring-oscillator leg")
+    p.add_argument("--ring-inst", type=int, default=1024)
+    p.add_argument("--ring-tstop-ns", type=float, default=50.0)
     p.add_argument("--eval-stages", type=int, default=1_000_000, help="inverter-chain stages of the cedar_eval leg")
     p.add_argument("--adj-inst", type=int, default=512, help="instances of the adjoint workload")
     p.add_argument("--adj-tstop-ns", type=float, default=20.0)
@@ -243,6 +246,31 @@ def measure_eval(pkg, args, torch, C):
             "timing": f"CUDA events on the handle's stream around {reps} calls after 3 warm-up calls"}
 
 
+def measure_rings(pkg, args, C):
+    """Workload 4: 15-stage current-starved ring oscillators (VA MOS1 + exponential
+    diodes, RC supply per stage), DC operating point + N(0, 1 mV) per node, adaptive
+    BDF2 to 50 ns, in one batched launch timed with CUDA events (DC included)."""
+    tpl, itpl, par, off, dx, dxo = pkg.generators.mc_rings(args.ring_inst, seed=args.seed)
+    f = tpl[0]
+    probes = np.array([[f.index("out1")]], np.int32)
+    sw = pkg.Sweep(tpl, itpl, par, off, inst_dx=dx, inst_dx_off=dxo, probes=probes, n_samples=501)
+    tstop = args.ring_tstop_ns * 1e-9
+    o = pkg.make_opts("bdf2", True, 0.0, tstop, 0.0, True, reltol=1e-6, abstol_v=1e-9, hmax=tstop / 50)
+    r = sw.run(o)
+    ms = C.c_double()
+    pkg.abi.check(sw.lib.cedar_batch_last_ms(sw.handle, C.byref(ms)))
+    ok = r.stats["status"] == 0
+    s = r.samples[:, 0, :]
+    osc = int(np.sum((s.max(axis=1) - s.min(axis=1)) > 1.0))
+    return {"workload": f"{args.ring_inst} x 15-stage current-starved ring oscillators (VA MOS1 + exp diodes, "
+                        f"100 Ohm / 100 fF supply per stage), DC op + N(0, 1 mV) per node, adaptive BDF2 to "
+                        f"{args.ring_tstop_ns:g} ns", "value": float(r.stats["accepted"].sum()) / (ms.value / 1e3),
+            "unit": "instance-timesteps/s", "ms": ms.value, "failed_instances": int((~ok).sum()),
+            "oscillating_instances": osc, "accepted_steps_mean": float(r.stats["accepted"].mean()),
+            "newton_iters_per_s": float(r.stats["newton_iters"].sum() + r.stats["dc_iters"].sum()) / (ms.value / 1e3),
+            "tuning": list(sw.tuning), "timing": "CUDA events around one cedar_batch_run launch (DC operating points included)"}
+
+
 def hbm_peak_gbs():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -419,6 +447,7 @@ def main():
                "timing": "CUDA events around the recording forward and the backward kernel"}
         del sw5
     eval_leg = None if args.no_eval else measure_eval(pkg, args, torch, C)
+    rings = None if args.no_rings else measure_rings(pkg, args, C)
     cpu = None
     if not args.no_cpu_baseline:
         cpu_line = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
@@ -448,7 +477,7 @@ def main():
                      "note": "algorithmic FP64 flops per Newton iteration (cedar_ckt_costs) x iterations / time; "
                              "peak = DFMA rate measured in this run by cedar_fp64_probe (MEASURED_PEAKS.json "
                              "has no FP64 entry); the kernel keeps its state on chip, so HBM is not its bound"},
-        "cpu_baseline": cpu, "e2e": e2e, "plain_gpu": plain, "adjoint": adj, "eval_hbm": eval_leg,
+        "cpu_baseline": cpu, "e2e": e2e, "plain_gpu": plain, "adjoint": adj, "eval_hbm": eval_leg, "rings": rings,
         "clocks": clk, "gpu_launches": args.steps,
     }
     print(json.dumps(line), flush=True)

@@ -8,6 +8,7 @@ prob.f.f(out, du, u, p, t) / prob.f.jac(J, du, u, p, gamma, t)
 dc!(circ)                 (src/sweeps.jl:437-448)        dc(circuit)
 tran!(circ, tspan)        (src/sweeps.jl:450-463)        tran(circuit, tspan, ...)
 CircuitSweep + tran!.     (src/sweeps.jl:390-435,488-502) Sweep(...).tran(...)
+CircuitSweep + dc!.       (src/sweeps.jl:471-486)        Sweep(...).dc()
 forward sensitivities     (test/sensitivity.jl:13-42)    Sweep(...).adjoint(...)
 
 Every computation runs in libcedar_gpu.so; nothing here falls back to the CPU.
@@ -212,9 +213,33 @@ class Sweep:
         t = BatchTuning(lanes_per_inst, warps_per_cta)
         check(self.lib.cedar_batch_set_tuning(self.handle, C.byref(t)))
 
-    def autotune(self, opts, horizon: float) -> Tuple[int, int]:
+    def autotune(self, opts, horizon: float, cache: Optional[str] = None) -> Tuple[int, int]:
+        """Time every tile shape (lanes per instance x warps per CTA) on a short
+        horizon and keep the fastest.  With `cache` (a JSON file), a result stored
+        for the same GPU, instance count and template sizes is reused instead."""
+        key = None
+        if cache:
+            import json
+            import os
+            import torch
+            sizes = sorted((f.n, sum(g[1].shape[0] for g in f.groups)) for f in self.templates)
+            key = f"{torch.cuda.get_device_name(0)}|{self.n_inst}|{sizes}"
+            table = {}
+            if os.path.exists(cache):
+                with open(cache) as fh:
+                    table = json.load(fh)
+            if key in table:
+                k, w = table[key]
+                self.set_tuning(k, w)
+                return k, w
         t = BatchTuning()
         check(self.lib.cedar_batch_autotune(self.handle, C.byref(opts), float(horizon), C.byref(t)))
+        if key is not None:
+            table[key] = [t.lanes_per_inst, t.warps_per_cta]
+            tmp = cache + ".tmp"
+            with open(tmp, "w") as fh:
+                json.dump(table, fh, indent=1, sort_keys=True)
+            os.replace(tmp, cache)
         return t.lanes_per_inst, t.warps_per_cta
 
     def run(self, opts, want_samples: bool = True) -> BatchResult:
@@ -224,6 +249,15 @@ class Sweep:
         check(self.lib.cedar_batch_run(self.handle, C.byref(opts), _dp(xf), None if samp is None else _dp(samp),
                                        st.ctypes.data_as(C.c_void_p)))
         return BatchResult(xf, samp, st)
+
+    def dc(self, reltol=1e-6, abstol_v=1e-9, **kw):
+        """DC operating point of every instance (dc!. over a CircuitSweep).
+        Returns (x_dc[n_inst, n_max], stats)."""
+        opts = make_opts("bdf2", True, 0.0, 1.0, 0.0, True, reltol, abstol_v, **kw)
+        x = np.zeros((self.n_inst, self.n_max))
+        st = np.zeros(self.n_inst, STATS_DTYPE)
+        check(self.lib.cedar_batch_dcop(self.handle, C.byref(opts), _dp(x), st.ctypes.data_as(C.c_void_p)))
+        return x, st
 
     def tran(self, tspan, method="bdf2", reltol=1e-6, abstol_v=1e-9, dcop=True, **kw) -> BatchResult:
         return self.run(make_opts(method, True, tspan[0], tspan[1], 0.0, dcop, reltol, abstol_v, **kw))

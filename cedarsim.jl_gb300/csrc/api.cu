@@ -672,7 +672,8 @@ static int launch_geometry(int K, int warps, int stride, int n_inst, bool &in_sm
 constexpr int kDenseNmax = 256;
 
 static int batch_launch(cedar_batch *b, const EngOpts &eo, const cedar_batch_tuning &tu, bool want_outputs,
-                        double t_until, bool fresh, const BatchDev *tape = nullptr, BatchDev *used = nullptr) {
+                        double t_until, bool fresh, const BatchDev *tape = nullptr, BatchDev *used = nullptr,
+                        bool dc_only = false) {
   int K = tu.lanes_per_inst, warps = tu.warps_per_cta;
   int tiles = warps * 32 / K;
   bool in_smem = false; size_t smem = 0; int grid = 1;
@@ -693,6 +694,7 @@ static int batch_launch(cedar_batch *b, const EngOpts &eo, const cedar_batch_tun
   if (dense_ok) CUDA_TRY(b->dense_ws.ensure((size_t)grid * tiles * dstride));
   BatchDev bd{};
   bd.dense_ws = dense_ok ? b->dense_ws.p : nullptr; bd.dense_stride = dstride; bd.dense_nmax = kDenseNmax;
+  bd.dc_only = dc_only ? 1 : 0;
   bd.tpls = b->d_tpls.p; bd.inst_tpl = b->inst_tpl.p; bd.inst_dpar = b->dpar_off.p; bd.dpar = b->dpar.p;
   bd.x0_off = b->has_x0 ? b->x0_off.p : nullptr; bd.x0 = b->x0.p;
   bd.dx_off = b->has_dx ? b->dx_off.p : nullptr; bd.dx = b->dx.p;
@@ -753,6 +755,25 @@ int cedar_batch_advance(cedar_batch *b, double t_until, int32_t *n_running) {
     CUDA_TRY(cudaStreamSynchronize(b->stream));
     *n_running = v;
   }
+  return 0;
+}
+
+int cedar_batch_dcop(cedar_batch *b, const cedar_tran_opts *opts, double *x_dc, cedar_stats *stats) {
+  if (!b) return fail(CEDAR_EINVAL, "null handle");
+  cedar_tran_opts o;
+  cedar_tran_opts_default(&o);
+  if (opts) o = *opts;
+  if (!(o.tstop > o.tstart)) o.tstop = o.tstart + 1.0;  // the transient span plays no part
+  int rc = check_opts(&o); if (rc) return rc;
+  if (b->n_inst == 0) return 0;
+  EngOpts eo = to_eng(&o);
+  eo.dcop = 1;
+  CUDA_TRY(cudaMemsetAsync(b->rows.p, 0, (size_t)std::max(b->n_inst, 1) * sizeof(StateRow), b->stream));
+  if ((rc = batch_launch(b, eo, b->tune, true, 1e300, true, nullptr, nullptr, true))) return rc;
+  b->started = false;
+  if (x_dc) CUDA_TRY(cudaMemcpyAsync(x_dc, b->xfinal.p, (size_t)b->n_inst * b->n_max * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  if (stats) CUDA_TRY(cudaMemcpyAsync(stats, b->stats.p, (size_t)b->n_inst * sizeof(EngStats), cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
   return 0;
 }
 

@@ -493,6 +493,8 @@ struct Slot {
       goto retire_x;
     dc_ok:
       st.dc_iters += used;
+      dense = false;  // the dense factorisation serves the DC homotopy only
+      if (b.dc_only) goto retire_x;
     tran_init:
       if (has_pert) { for (int i = rank(); i < T->n; i += K) w.x[i] += w.qn[i]; ssync(); }
       eval_q(w.x, o.tstart, w.qn);

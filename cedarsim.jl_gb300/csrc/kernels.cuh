@@ -46,6 +46,7 @@ struct BatchDev {
   // dense DC fallback scratch: per global slot dense_stride doubles (an n_max x
   // n_max matrix, a right-hand side and the pivots); null: no fallback
   double *dense_ws; long long dense_stride; int dense_nmax;
+  int dc_only;                   // retire every instance at its DC operating point
 };
 
 // slice helpers of the adjoint tape

@@ -323,6 +323,12 @@ int cedar_batch_run(cedar_batch *b, const cedar_tran_opts *opts, double *x_final
 int cedar_batch_start(cedar_batch *b, const cedar_tran_opts *opts);
 int cedar_batch_advance(cedar_batch *b, double t_until, int32_t *n_running);
 int cedar_batch_results(cedar_batch *b, double *x_final, double *samples, cedar_stats *stats);
+/* DC operating point of every instance (broadcast dc!. over a CircuitSweep,
+ * src/sweeps.jl:471-486): the batch's homotopy (Newton, pseudo-transient
+ * continuation, source stepping, dense-pivoting rerun) with opts' tolerances;
+ * inst_dx perturbations are not applied.  x_dc[n_inst * n_max] in original
+ * order; stats[n_inst].dc_iters and .status report each solve. */
+int cedar_batch_dcop(cedar_batch *b, const cedar_tran_opts *opts, double *x_dc, cedar_stats *stats);
 /* Device time of the last batch launch (CUDA events on the handle's stream). */
 int cedar_batch_last_ms(cedar_batch *b, double *ms);
 int cedar_batch_set_tuning(cedar_batch *b, const cedar_batch_tuning *t);

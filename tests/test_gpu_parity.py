@@ -200,3 +200,22 @@ def test_batch_windows_match_uninterrupted_run(gpu, pkg):
     assert np.array_equal(samp, full.samples)
     for k in STAT_KEYS:
         assert np.array_equal(st[k], full.stats[k]), k
+
+
+def test_autotune_picks_a_shape_and_caches_it(gpu, pkg, tmp_path):
+    """cedar_batch_autotune times every tile shape; the host caches the choice per
+    GPU, instance count and template sizes, and a second call reuses it."""
+    import json
+    templates, itpl, par, off, probes = small_mc(pkg, n_inst=64, seed=8)
+    sw = pkg.Sweep(templates, itpl, par, off)
+    o = pkg.make_opts("bdf2", True, 0.0, 1e-9, 0.0, True)
+    cache = str(tmp_path / "tune.json")
+    k, w = sw.autotune(o, 0.05e-9, cache=cache)
+    assert k in (1, 2, 4, 8, 16, 32) and 1 <= w <= 8
+    assert sw.tuning == (k, w)
+    table = json.load(open(cache))
+    assert list(table.values()) == [[k, w]]
+    sw2 = pkg.Sweep(templates, itpl, par, off)
+    assert sw2.autotune(o, 0.05e-9, cache=cache) == (k, w) and sw2.tuning == (k, w)
+    r = sw2.run(o)
+    assert np.all(r.stats["status"] == 0)

@@ -57,3 +57,22 @@ def test_ring_dc_single_circuit_path(gpu, pkg, oracle):
     xr, st, rc = oracle.dcop(flat)
     assert rc == 0
     np.testing.assert_allclose(x, xr, rtol=1e-9, atol=1e-12)
+
+
+def test_batched_dc_operating_points(gpu, pkg, oracle):
+    """cedar_batch_dcop (dc!. over a sweep) on ring instances and MC chains
+    against the oracle's DC operating point of each instance."""
+    tpl, itpl, par, off, dx, dxo, probes = _rings(pkg, 3)
+    cases = [(tpl, itpl, par, off, dx, dxo)]
+    ct, ci, cp, co = pkg.generators.mc_chains(6, seed=4, lengths=[5, 9, 21])
+    cases.append((ct, ci, cp, co, None, None))
+    for templates, it, p_, o_, d_, do_ in cases:
+        sw = pkg.Sweep(templates, it, p_, o_, inst_dx=d_, inst_dx_off=do_)
+        x, st = sw.dc()
+        assert np.all(st["status"] == 0)
+        for i in range(len(it)):
+            t = int(it[i])
+            flat = pkg.generators.instance_flat(templates[t], p_[o_[i]:o_[i] + templates[t].param_block().size])
+            xr, s_, rc = oracle.dcop(flat)
+            assert rc == 0
+            np.testing.assert_allclose(x[i, :flat.n], xr, rtol=1e-9, atol=1e-12)
