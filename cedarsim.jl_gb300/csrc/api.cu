@@ -124,6 +124,25 @@ int upload_template(const cedar_ckt_desc *desc, std::unique_ptr<DevTemplate> &ou
   size_t o_tf_task = P.vec(row_tasks(H.tf_row, H.tf_ptr)), o_tb_task = P.vec(row_tasks(H.tb_row, H.tb_ptr));
   size_t o_long_lu = P.vec(H.long_lu), o_long_fi = P.vec(H.long_fi), o_long_jc = P.vec(H.long_jc), o_long_fo = P.vec(H.long_fo);
   size_t o_long_off = P.vec(H.long_jc_fo_off);
+  // long LU / substitution tasks per level
+  auto long_tasks = [](const std::vector<int32_t> &lvl, const std::vector<int32_t> &ptr, std::vector<int> &lv_out,
+                       std::vector<int> &task_out) {
+    lv_out.assign(1, 0); task_out.clear();
+    for (size_t l = 0; l + 1 < lvl.size(); ++l) {
+      for (int t = lvl[l]; t < lvl[l + 1]; ++t) if (ptr[t + 1] - ptr[t] > kLongPairs) task_out.push_back(t);
+      lv_out.push_back((int)task_out.size());
+    }
+    if (task_out.empty()) task_out.push_back(0);
+  };
+  std::vector<int> llu_l, llu_t, lfw_l, lfw_t, lbw_l, lbw_t, ltf_l, ltf_t, ltb_l, ltb_t;
+  long_tasks(H.lu_lvl_ptr, H.lu_pair_ptr, llu_l, llu_t);
+  long_tasks(H.fw_lvl_ptr, H.fw_ptr, lfw_l, lfw_t);
+  long_tasks(H.bw_lvl_ptr, H.bw_ptr, lbw_l, lbw_t);
+  long_tasks(H.tf_lvl_ptr, H.tf_ptr, ltf_l, ltf_t);
+  long_tasks(H.tb_lvl_ptr, H.tb_ptr, ltb_l, ltb_t);
+  size_t o_llu_l = P.vec(llu_l), o_llu_t = P.vec(llu_t), o_lfw_l = P.vec(lfw_l), o_lfw_t = P.vec(lfw_t);
+  size_t o_lbw_l = P.vec(lbw_l), o_lbw_t = P.vec(lbw_t), o_ltf_l = P.vec(ltf_l), o_ltf_t = P.vec(ltf_t);
+  size_t o_ltb_l = P.vec(ltb_l), o_ltb_t = P.vec(ltb_t);
   CUDA_TRY(cudaMalloc(&dt->buf, P.bytes.size()));
   CUDA_TRY(cudaMemcpy(dt->buf, P.bytes.data(), P.bytes.size(), cudaMemcpyHostToDevice));
   char *b = (char *)dt->buf;
@@ -162,6 +181,11 @@ int upload_template(const cedar_ckt_desc *desc, std::unique_ptr<DevTemplate> &ou
   D.long_lu = (const int *)(b + o_long_lu); D.long_fi = (const int *)(b + o_long_fi);
   D.long_jc = (const int *)(b + o_long_jc); D.long_fo = (const int *)(b + o_long_fo);
   D.long_off = (const int *)(b + o_long_off); D.n_long_part = H.long_jc_fo_off.back();
+  D.long_lu_lvl = (const int *)(b + o_llu_l); D.long_lu_task = (const int *)(b + o_llu_t);
+  D.long_fw_lvl = (const int *)(b + o_lfw_l); D.long_fw_task = (const int *)(b + o_lfw_t);
+  D.long_bw_lvl = (const int *)(b + o_lbw_l); D.long_bw_task = (const int *)(b + o_lbw_t);
+  D.long_tf_lvl = (const int *)(b + o_ltf_l); D.long_tf_task = (const int *)(b + o_ltf_t);
+  D.long_tb_lvl = (const int *)(b + o_ltb_l); D.long_tb_task = (const int *)(b + o_ltb_t);
   CUDA_TRY(cudaMalloc(&dt->D_dev, sizeof(DTpl)));
   CUDA_TRY(cudaMemcpy(dt->D_dev, &D, sizeof(DTpl), cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMalloc(&dt->par_dev, std::max<size_t>(1, H.par.size()) * sizeof(double)));

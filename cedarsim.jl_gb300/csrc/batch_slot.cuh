@@ -778,6 +778,7 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am, const 
       int t1 = T.lu_lvl[l + 1];
       for (int t = T.lu_lvl[l] + rank; t < t1; t += K) {
         const int4 tk = T.lu_task[t];
+        if (tk.w - tk.z > kLongPairs) continue;  // summed by the whole slot below
         int q = tk.x, info = tk.y;
         double acc = lu[q], acc1 = 0.0;
         int p = tk.z;
@@ -795,6 +796,21 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am, const 
         }
         lu[q] = acc;
       }
+      for (int u = T.long_lu_lvl[l]; u < T.long_lu_lvl[l + 1]; ++u) {
+        const int4 tk = T.lu_task[T.long_lu_task[u]];
+        const double S = long_pair_sum<K>(T.lu_pair, tk.z, tk.w, lu, lu, rank, s.smask());
+        if (rank == 0) {
+          double acc = lu[tk.x] - S;
+          const int kind = tk.y & 3, j = tk.y >> 2;
+          if (kind == 2) acc *= rd[j];
+          else if (kind == 1) {
+            if (!pivot_ok(acc)) bad = true;
+            rd[j] = pivot_rcp(acc);
+          }
+          lu[tk.x] = acc;
+        }
+        s.ssync();
+      }
     }
     __syncwarp(am);
   }
@@ -806,6 +822,7 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am, const 
     if (!slot_bad && l < T.fw_nlev) {
       for (int t = T.fw_lvl[l] + rank; t < T.fw_lvl[l + 1]; t += K) {
         const int4 tk = T.fw_task[t];
+        if (tk.z - tk.y > kLongPairs) continue;  // summed by the whole slot below
         int i = tk.x; double acc = b[i];
         double acc1 = 0.0;
         int p = tk.y;
@@ -817,6 +834,12 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am, const 
         acc += acc1;
         b[i] = acc;
       }
+      for (int u = T.long_fw_lvl[l]; u < T.long_fw_lvl[l + 1]; ++u) {
+        const int4 tk = T.fw_task[T.long_fw_task[u]];
+        const double S = long_pair_sum<K>(T.fw_pair, tk.y, tk.z, lu, b, rank, s.smask());
+        if (rank == 0) { const int i = tk.x; double acc = b[i] - S; b[i] = acc; }
+        s.ssync();
+      }
     }
     __syncwarp(am);
   }
@@ -825,6 +848,7 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am, const 
     if (!slot_bad && l < T.bw_nlev) {
       for (int t = T.bw_lvl[l] + rank; t < T.bw_lvl[l + 1]; t += K) {
         const int4 tk = T.bw_task[t];
+        if (tk.z - tk.y > kLongPairs) continue;  // summed by the whole slot below
         int i = tk.x; double acc = b[i];
         double acc1 = 0.0;
         int p = tk.y;
@@ -835,6 +859,12 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am, const 
         if (p < tk.z) { const int2 p0 = T.bw_pair[p]; acc -= lu[p0.x] * b[p0.y]; }
         acc += acc1;
         b[i] = acc * rd[i];
+      }
+      for (int u = T.long_bw_lvl[l]; u < T.long_bw_lvl[l + 1]; ++u) {
+        const int4 tk = T.bw_task[T.long_bw_task[u]];
+        const double S = long_pair_sum<K>(T.bw_pair, tk.y, tk.z, lu, b, rank, s.smask());
+        if (rank == 0) { const int i = tk.x; double acc = b[i] - S; b[i] = acc * rd[i]; }
+        s.ssync();
       }
     }
     __syncwarp(am);

@@ -62,6 +62,10 @@ struct DTpl {
   // cedar_eval: chunk offsets of the long CSC slots then the long residual rows
   // (n_long_jc + n_long_fo + 1 entries); n_long_part chunks in all
   const int *long_off; int n_long_part, pad_long;
+  // LU / substitution tasks with more than kLongPairs pairs, per level: task
+  // indices long_*_task[long_*_lvl[l] .. long_*_lvl[l + 1]) (summed cooperatively)
+  const int *long_lu_lvl, *long_lu_task, *long_fw_lvl, *long_fw_task, *long_bw_lvl, *long_bw_task;
+  const int *long_tf_lvl, *long_tf_task, *long_tb_lvl, *long_tb_task;
   const int *tf_lvl, *tf_row, *tf_ptr; const int2 *tf_pair;
   const int *tb_lvl, *tb_row, *tb_ptr; const int2 *tb_pair;
   const int *ct_ptr; const int2 *ct_ent;
@@ -72,6 +76,7 @@ struct DTpl {
 // combined by a fixed pairwise tree (in-engine stamp programs / cedar_eval's).
 constexpr int kLongGather = 16;
 constexpr int kLongEval = 64;
+constexpr int kLongPairs = 16;
 
 // Sum of a long gather list (entries (out << 1) | neg into dout) by the K lanes
 // of a group (mask, rank): the list is cut into 32 fixed chunks, each summed in
@@ -90,6 +95,32 @@ __device__ __forceinline__ double long_gather(const int *ptr, const int *ent, in
     const int c0 = a + (int)(((long long)len * c) >> 5), c1 = a + (int)(((long long)len * (c + 1)) >> 5);
     double acc = 0.0;
     for (int k = c0; k < c1; ++k) { const int e = ent[k]; const double v = dout[e >> 1]; acc = (e & 1) ? acc - v : acc + v; }
+    part[j] = acc;
+  }
+#pragma unroll
+  for (int w = 1; w < PER; w <<= 1)
+#pragma unroll
+    for (int j = 0; j + w < PER; j += 2 * w) part[j] = part[j] + part[j + w];
+  double v = part[0];
+#pragma unroll
+  for (int o = 1; o < K; o <<= 1) { const double u = __shfl_xor_sync(mask, v, o, K); v = (rank & o) ? u + v : v + u; }
+  return v;
+}
+
+// Sum of A[p.x] * B[p.y] over pairs [p0, p1) by the K lanes of a group, in the
+// same 32 fixed chunks and fixed tree as long_gather (bits independent of K).
+template <int K>
+__device__ __forceinline__ double long_pair_sum(const int2 *pairs, int p0, int p1, const double *A, const double *B,
+                                                int rank, unsigned mask) {
+  const int len = p1 - p0;
+  constexpr int PER = 32 / K;
+  double part[PER];
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    const int c = rank * PER + j;
+    const int c0 = p0 + (int)(((long long)len * c) >> 5), c1 = p0 + (int)(((long long)len * (c + 1)) >> 5);
+    double acc = 0.0;
+    for (int k = c0; k < c1; ++k) { const int2 pr = pairs[k]; acc += A[pr.x] * B[pr.y]; }
     part[j] = acc;
   }
 #pragma unroll

@@ -282,6 +282,7 @@ __device__ __forceinline__ void backward_step(AdjSlot<K> &s, const AdjDev &a, un
       int t1 = T.lu_lvl[l + 1];
       for (int t = T.lu_lvl[l] + rank; t < t1; t += K) {
         const int4 tk = T.lu_task[t];
+        if (tk.w - tk.z > kLongPairs) continue;  // summed by the whole slot below
         int q = tk.x, info = tk.y;
         double acc = s.w.lu[q];
         for (int p = tk.z; p < tk.w; ++p) { int2 pr = T.lu_pair[p]; acc -= s.w.lu[pr.x] * s.w.lu[pr.y]; }
@@ -292,6 +293,21 @@ __device__ __forceinline__ void backward_step(AdjSlot<K> &s, const AdjDev &a, un
           s.w.rd[jj] = pivot_rcp(acc);
         }
         s.w.lu[q] = acc;
+      }
+      for (int u = T.long_lu_lvl[l]; u < T.long_lu_lvl[l + 1]; ++u) {
+        const int4 tk = T.lu_task[T.long_lu_task[u]];
+        const double S = long_pair_sum<K>(T.lu_pair, tk.z, tk.w, s.w.lu, s.w.lu, rank, s.smask());
+        if (rank == 0) {
+          double acc = s.w.lu[tk.x] - S;
+          const int kind = tk.y & 3, jj = tk.y >> 2;
+          if (kind == 2) acc *= s.w.rd[jj];
+          else if (kind == 1) {
+            if (!pivot_ok(acc)) bad = true;
+            s.w.rd[jj] = pivot_rcp(acc);
+          }
+          s.w.lu[tk.x] = acc;
+        }
+        s.ssync();
       }
     }
     __syncwarp(ab);
@@ -304,9 +320,16 @@ __device__ __forceinline__ void backward_step(AdjSlot<K> &s, const AdjDev &a, un
     if (!slot_bad && l < T.tf_nlev) {
       for (int t = T.tf_lvl[l] + rank; t < T.tf_lvl[l + 1]; t += K) {
         const int4 tk = T.tf_task[t];
+        if (tk.z - tk.y > kLongPairs) continue;  // summed by the whole slot below
         int i = tk.x; double acc = r[i];
         for (int p = tk.y; p < tk.z; ++p) { int2 pr = T.tf_pair[p]; acc -= s.w.lu[pr.x] * r[pr.y]; }
         r[i] = acc * s.w.rd[i];
+      }
+      for (int u = T.long_tf_lvl[l]; u < T.long_tf_lvl[l + 1]; ++u) {
+        const int4 tk = T.tf_task[T.long_tf_task[u]];
+        const double S = long_pair_sum<K>(T.tf_pair, tk.y, tk.z, s.w.lu, r, rank, s.smask());
+        if (rank == 0) { const int i = tk.x; double acc = r[i] - S; r[i] = acc * s.w.rd[i]; }
+        s.ssync();
       }
     }
     __syncwarp(ab);
@@ -316,9 +339,16 @@ __device__ __forceinline__ void backward_step(AdjSlot<K> &s, const AdjDev &a, un
     if (!slot_bad && l < T.tb_nlev) {
       for (int t = T.tb_lvl[l] + rank; t < T.tb_lvl[l + 1]; t += K) {
         const int4 tk = T.tb_task[t];
+        if (tk.z - tk.y > kLongPairs) continue;  // summed by the whole slot below
         int i = tk.x; double acc = r[i];
         for (int p = tk.y; p < tk.z; ++p) { int2 pr = T.tb_pair[p]; acc -= s.w.lu[pr.x] * r[pr.y]; }
         r[i] = acc;
+      }
+      for (int u = T.long_tb_lvl[l]; u < T.long_tb_lvl[l + 1]; ++u) {
+        const int4 tk = T.tb_task[T.long_tb_task[u]];
+        const double S = long_pair_sum<K>(T.tb_pair, tk.y, tk.z, s.w.lu, r, rank, s.smask());
+        if (rank == 0) { const int i = tk.x; double acc = r[i] - S; r[i] = acc; }
+        s.ssync();
       }
     }
     __syncwarp(ab);
