@@ -253,7 +253,7 @@ struct cedar_batch {
   std::vector<std::unique_ptr<DevTemplate>> tpls;
   cudaStream_t stream = nullptr;
   DevBuf<DTpl> d_tpls;
-  DevBuf<int> inst_tpl, queue, head, probes_int, qblk_beg, qblk_head;
+  DevBuf<int> inst_tpl, queue, probes_int, qblk_beg, qblk_head;
   int n_qblk = 0;
   DevBuf<long long> raw_off, dpar_off, x0_off, dx_off;
   DevBuf<double> raw, dpar, x0, dx, samples, xfinal, ws, dense_ws;
@@ -633,7 +633,6 @@ int cedar_batch_create(const cedar_batch_desc *d, cedar_batch **out) {
   b->n_qblk = (int)qb.size() - 1;
   if ((rc = up(b->qblk_beg, qb))) return rc;
   CUDA_TRY(b->qblk_head.ensure(std::max(b->n_qblk, 1)));
-  CUDA_TRY(b->head.ensure(1));
   CUDA_TRY(b->n_running.ensure(1));
   CUDA_TRY(b->rows.ensure(std::max(ni, 1)));
   CUDA_TRY(b->row_vec.ensure((size_t)std::max(ni, 1) * 6 * b->n_max));
@@ -725,7 +724,7 @@ static int batch_launch(cedar_batch *b, const EngOpts &eo, const cedar_batch_tun
   bd.probes_int = b->probes_int.p; bd.np = want_outputs ? b->np : 0; bd.ns = b->ns;
   bd.samples = want_outputs ? b->samples.p : nullptr;
   bd.x_final = want_outputs ? b->xfinal.p : nullptr; bd.n_max = b->n_max;
-  bd.stats = b->stats.p; bd.queue = b->queue.p; bd.head = b->head.p; bd.n_inst = b->n_inst;
+  bd.stats = b->stats.p; bd.queue = b->queue.p; bd.n_inst = b->n_inst;
   bd.qblk_beg = b->qblk_beg.p; bd.qblk_head = b->qblk_head.p; bd.n_qblk = b->n_qblk;
   bd.opts = eo; bd.ws_stride = b->ws_stride; bd.ws_global = b->ws.p; bd.ws_in_smem = in_smem ? 1 : 0;
   bd.t_until = t_until; bd.rows = b->rows.p; bd.row_vec = b->row_vec.p; bd.n_running = b->n_running.p;
@@ -734,7 +733,6 @@ static int batch_launch(cedar_batch *b, const EngOpts &eo, const cedar_batch_tun
     bd.tape_cap = tape->tape_cap; bd.ckpt = tape->ckpt; bd.ckpt_every = tape->ckpt_every; bd.obj_idx = tape->obj_idx;
   }
   if (used) *used = bd;
-  CUDA_TRY(cudaMemsetAsync(b->head.p, 0, sizeof(int), b->stream));
   CUDA_TRY(cudaMemsetAsync(b->qblk_head.p, 0, std::max(b->n_qblk, 1) * sizeof(int), b->stream));
   CUDA_TRY(cudaMemsetAsync(b->n_running.p, 0, sizeof(int), b->stream));
   if (fresh) {
@@ -894,7 +892,6 @@ int cedar_adjoint_run(cedar_batch *b, const cedar_tran_opts *opts, const cedar_o
   a.raw_off = b->raw_off.p; a.raw = b->raw.p; a.obj = b->adj_obj.p; a.tstar = tstar ? b->adj_tstar.p : nullptr;
   a.phi = b->adj_phi.p; a.grad = b->adj_grad.p; a.np_max = np_max; a.status = b->adj_status.p;
   a.segx = b->segx.p; a.fwd = b->stats.p;
-  CUDA_TRY(cudaMemsetAsync(b->head.p, 0, sizeof(int), b->stream));
   CUDA_TRY(cudaMemsetAsync(b->qblk_head.p, 0, std::max(b->n_qblk, 1) * sizeof(int), b->stream));
   if (!b->ev2) CUDA_TRY(cudaEventCreate(&b->ev2));
   CUDA_TRY(launch_adjoint(a, K, warps, grid, smem, b->stream));

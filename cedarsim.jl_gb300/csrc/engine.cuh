@@ -205,40 +205,7 @@ __device__ __forceinline__ bool pivot_ok(double a) {
 __device__ __forceinline__ long long abs_bits(double a) { return __double_as_longlong(a) & 0x7fffffffffffffffLL; }
 __device__ __forceinline__ bool finite_big(double a) { return abs_bits(a) < 0x7e37e43c8800759cLL; }  // |a| < 1e300
 
-// ------------------------------------------------------------- thread groups
-template <int K>
-struct TileGroup {
-  unsigned mask; int rank;
-  static constexpr int size = K;
-  __device__ TileGroup() {
-    int lane = threadIdx.x & 31; rank = lane % K;
-    mask = (K == 32) ? 0xffffffffu : (((1u << K) - 1u) << (lane - rank));
-  }
-  __device__ __forceinline__ void sync() const { if (K > 1) __syncwarp(mask); }
-  __device__ __forceinline__ bool any(bool p) const { return K == 1 ? p : (__any_sync(mask, p) != 0); }
-  __device__ __forceinline__ double max(double v) const {
-#pragma unroll
-    for (int o = K / 2; o > 0; o >>= 1) { double w = __shfl_xor_sync(mask, v, o, K); v = w > v ? w : v; }
-    return v;
-  }
-  __device__ __forceinline__ double min(double v) const {
-#pragma unroll
-    for (int o = K / 2; o > 0; o >>= 1) { double w = __shfl_xor_sync(mask, v, o, K); v = w < v ? w : v; }
-    return v;
-  }
-  __device__ __forceinline__ int bcast(int v) const { return K == 1 ? v : __shfl_sync(mask, v, 0, K); }
-  __device__ double ratio(MaxRatio m) const {
-#pragma unroll
-    for (int o = K / 2; o > 0; o >>= 1) {
-      double n2 = __shfl_xor_sync(mask, m.num, o, K), d2 = __shfl_xor_sync(mask, m.den, o, K);
-      bool b2 = __shfl_xor_sync(mask, (int)m.bad, o, K) != 0;
-      m.merge(n2, d2, b2);
-    }
-    if (K > 1) { m.num = __shfl_sync(mask, m.num, 0, K); m.den = __shfl_sync(mask, m.den, 0, K); m.bad = __shfl_sync(mask, (int)m.bad, 0, K) != 0; }
-    return m.value();
-  }
-};
-
+// ------------------------------------------------------------- thread group (one CTA)
 struct BlockGroup {
   int rank, size;
   double *red;  // shared scratch of >= 96 doubles

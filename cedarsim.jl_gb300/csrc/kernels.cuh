@@ -19,7 +19,6 @@ struct BatchDev {
   double *x_final; int n_max;    // [n_inst * n_max] original order
   EngStats *stats;               // [n_inst]
   const int *queue;              // dequeue order (instance ids), in blocks of one template
-  int *head;                     // (unused by the kernels; kept zero)
   const int *qblk_beg;           // [n_qblk + 1] start of each template block in queue
   int *qblk_head;                // [n_qblk] next position to take in each block
   int n_qblk;
