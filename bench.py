@@ -60,6 +60,8 @@ def parse():
     p.add_argument("--no-adjoint", action="store_true")
     p.add_argument("--no-eval", action="store_true", help="skip the cedar_eval HBM leg")
     p.add_argument("--no-rings", action="store_true", help="skip the ring-oscillator leg")
+    p.add_argument("--no-ac", action="store_true", help="skip the AC / noise sweep leg")
+    p.add_argument("--ac-freq", type=int, default=1 << 17, help="frequency points of the AC / noise leg")
     p.add_argument("--ring-inst", type=int, default=1024)
     p.add_argument("--ring-tstop-ns", type=float, default=50.0)
     p.add_argument("--eval-stages", type=int, default=1_000_000, help="inverter-chain stages of the cedar_eval leg")
@@ -271,6 +273,66 @@ def measure_rings(pkg, args, C):
             "tuning": list(sw.tuning), "timing": "CUDA events around one cedar_batch_run launch (DC operating points included)"}
 
 
+def measure_ac(pkg, args, torch, C, fp64_peak):
+    """Small-signal AC and noise sweeps (cedar_ac / cedar_noise) of the 100-section
+    RC ladder about its DC point: every frequency is one complex static-pivot LU
+    and solve, one warp per frequency.  Device time: CUDA events on the handle's
+    stream around one call (its small host copies included); the CPU column is the
+    oracle's dense complex solve per frequency (the reference's freqresp evaluates
+    the dense descriptor system per frequency) on a bounded sample."""
+    import __graft_entry__ as ge
+    f = pkg.generators.rc_ladder(100).flatten()
+    f.ac = {"V1": 1.0}
+    sy = pkg.System(f)
+    lib = sy.lib
+    x_op = pkg.dc(sy)
+    nf = args.ac_freq
+    w = 2 * np.pi * np.logspace(3, 12, nf)
+    probe = f.index(f.names[100])
+    acs, ns = pkg.ACSol(sy, x_op), pkg.NoiseSol(sy, x_op)
+    costs = pkg.abi.Costs()
+    pkg.abi.check(lib.cedar_ckt_costs(sy.handle, C.byref(costs)))
+    # complex arithmetic: one complex multiply-subtract = 4 real FMAs (8 flops)
+    flops = 4 * (costs.flops_lu + costs.flops_solve) + costs.nnz_lu
+    sp = C.c_void_p()
+    pkg.abi.check(lib.cedar_ckt_stream(sy.handle, C.byref(sp)))
+    st = torch.cuda.ExternalStream(sp.value)
+    out = {}
+    for name, call in (("ac", lambda: acs.freqresp(probe, w)), ("noise", lambda: ns.psd(probe, w))):
+        for _ in range(2):
+            call()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record(st)
+        res = call()
+        e1.record(st)
+        e1.synchronize()
+        wall = time.perf_counter() - t0
+        ms = e0.elapsed_time(e1)
+        sol = acs if name == "ac" else ns
+        kst = pkg.ac_last_stats(sy)
+        tf = flops * nf / (ms * 1e-3) / 1e12
+        out[name] = {"value": nf / (ms * 1e-3), "unit": "frequency points/s", "ms": ms,
+                     "e2e": {"value": nf / wall, "unit": "frequency points/s"},
+                     "failed_points": int((sol.status != 0).sum()), "finite": bool(np.all(np.isfinite(res))),
+                     "achieved_tflops": tf, "fp64_frac": tf / fp64_peak if fp64_peak else None,
+                     "dense_reruns": kst["n_dense"], "kernel_ms": {"sparse": kst["ms_sparse"], "dense": kst["ms_dense"]}}
+    orc = ge.load_oracle().Oracle(pkg)
+    k = min(nf, 2000)
+    ws = w[np.linspace(0, nf - 1, k).astype(int)]
+    t0 = time.perf_counter()
+    orc.ac(f, x_op, ws, [probe])
+    cpu_ac = k / (time.perf_counter() - t0)
+    out["cpu_baseline"] = {"value": cpu_ac, "unit": "frequency points/s", "kind": "port", "cores": os.cpu_count(),
+                           "sample": f"{k} of the {nf} frequencies, dense complex LU per frequency (numpy / LAPACK)"}
+    out["workload"] = (f"100-section RC ladder (n = {sy.n}, nnz(LU) = {costs.nnz_lu}) about its DC point, "
+                       f"{nf} frequencies log-spaced 1 kHz .. 1 THz, one probe")
+    out["flops_per_point"] = int(flops)
+    out["timing"] = "CUDA events on the handle's stream around one call (host copies of omega and results included)"
+    return out
+
+
 def hbm_peak_gbs():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -448,6 +510,7 @@ def main():
         del sw5
     eval_leg = None if args.no_eval else measure_eval(pkg, args, torch, C)
     rings = None if args.no_rings else measure_rings(pkg, args, C)
+    ac_leg = None if args.no_ac else measure_ac(pkg, args, torch, C, fp64_peak)
     cpu = None
     if not args.no_cpu_baseline:
         cpu_line = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
@@ -478,7 +541,7 @@ def main():
                              "peak = DFMA rate measured in this run by cedar_fp64_probe (MEASURED_PEAKS.json "
                              "has no FP64 entry); the kernel keeps its state on chip, so HBM is not its bound"},
         "cpu_baseline": cpu, "e2e": e2e, "plain_gpu": plain, "adjoint": adj, "eval_hbm": eval_leg, "rings": rings,
-        "clocks": clk, "gpu_launches": args.steps,
+        "ac": ac_leg, "clocks": clk, "gpu_launches": args.steps,
     }
     print(json.dumps(line), flush=True)
 

@@ -6,7 +6,9 @@ is not a Python identifier); see ``load()`` in the repository's ``__graft_entry_
 from .circuit import Circuit, Flat, Pulse, PWL, Sin  # noqa: F401
 from .abi import load_library, make_opts, CedarError, STATUS_NAMES  # noqa: F401
 from .api import System, Solution, Sweep, BatchResult, costs, dc, tran  # noqa: F401
+from .api import ACSol, NoiseSol, ac, acdec, ac_drive, ac_last_stats, noise  # noqa: F401
 from . import generators  # noqa: F401
 
 __all__ = ["Circuit", "Flat", "Pulse", "PWL", "Sin", "System", "Solution", "Sweep", "BatchResult", "dc", "tran",
-           "load_library", "make_opts", "generators", "CedarError", "STATUS_NAMES"]
+           "load_library", "make_opts", "generators", "CedarError", "STATUS_NAMES",
+           "ACSol", "NoiseSol", "ac", "acdec", "ac_drive", "ac_last_stats", "noise"]

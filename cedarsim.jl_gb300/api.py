@@ -10,12 +10,16 @@ tran!(circ, tspan)        (src/sweeps.jl:450-463)        tran(circuit, tspan, ..
 CircuitSweep + tran!.     (src/sweeps.jl:390-435,488-502) Sweep(...).tran(...)
 CircuitSweep + dc!.       (src/sweeps.jl:471-486)        Sweep(...).dc()
 forward sensitivities     (test/sensitivity.jl:13-42)    Sweep(...).adjoint(...)
+ac!(circ) / freqresp      (src/ac.jl:178-186,251-258)    ac(circuit).freqresp(sym, omegas)
+noise!(circ) / PSD        (src/ac.jl:188-197,263-283)    noise(circuit).psd(sym, omegas)
+acdec(nd, fstart, fstop)  (src/ac.jl:288-301)            acdec(nd, fstart, fstop)
 
 Every computation runs in libcedar_gpu.so; nothing here falls back to the CPU.
 """
 from __future__ import annotations
 
 import ctypes as C
+import math
 from dataclasses import dataclass
 from typing import Optional, Sequence, Tuple, Union
 
@@ -23,7 +27,7 @@ import numpy as np
 
 from . import abi
 from .abi import BatchHolder, BatchTuning, DescHolder, Stats, STATS_DTYPE, check, load_library, make_opts
-from .circuit import Circuit, Flat
+from .circuit import Circuit, Flat, I as _MODEL_I, V as _MODEL_V
 
 
 def _flat(c: Union[Circuit, Flat]) -> Flat:
@@ -309,3 +313,110 @@ class AdjointResult:
     fwd_ms: float            # device time of the recording forward run
     bwd_ms: float            # device time of the backward kernel
 
+
+# ---------------------------------------------------------------- AC / noise
+def acdec(nd: int, fstart: float, fstop: float) -> np.ndarray:
+    """Frequencies (Hz), nd per decade from fstart to fstop, log-spaced: SPICE's
+    `.ac dec nd fstart fstop` (acdec, src/ac.jl:288-301)."""
+    a, b = math.log10(fstart), math.log10(fstop)
+    points = int(math.ceil((b - a) * nd)) + 1
+    return 10.0 ** np.linspace(a, b, points)
+
+
+def ac_drive(flat: Flat) -> np.ndarray:
+    """b = -dFi/d(eps) of the circuit's AC sources (original equation order): in
+    :ac mode a source's value is dc + eps |ac| (src/simpledevices.jl:292-294,331-333)."""
+    b = np.zeros(flat.n)
+    for name, mag in flat.ac.items():
+        gi, ii = flat.devices[name]
+        model, term, br, par = flat.groups[gi]
+        if model == _MODEL_V:                 # V+ - V- - (dc + eps a) = 0
+            b[br[ii]] += mag
+        elif model == _MODEL_I:               # KCL(+) -= m (dc + eps a), KCL(-) += m (dc + eps a)
+            m = par[0, ii]
+            if term[ii, 0] >= 0:
+                b[term[ii, 0]] += m * mag
+            if term[ii, 1] >= 0:
+                b[term[ii, 1]] -= m * mag
+    return b
+
+
+def _unknown(sys: "System", sym) -> int:
+    return int(sym) if isinstance(sym, (int, np.integer)) else sys.flat.index(sym)
+
+
+def ac_last_stats(sys: "System") -> dict:
+    """Of the last AC / noise call on `sys`: frequencies rerun densely, and device
+    ms of the sparse kernel and of the dense rerun."""
+    nd, a, b = C.c_int32(), C.c_double(), C.c_double()
+    check(sys.lib.cedar_ac_last_stats(sys.handle, C.byref(nd), C.byref(a), C.byref(b)))
+    return {"n_dense": nd.value, "ms_sparse": a.value, "ms_dense": b.value}
+
+
+class ACSol:
+    """The circuit linearised about its DC operating point (ACSol, src/ac.jl:73-104):
+    G = dFi/dx and C = dFq/dx at x_op, driven by the AC sources."""
+
+    def __init__(self, sys: "System", x_op: np.ndarray, b: Optional[np.ndarray] = None):
+        self.sys = sys
+        self.x_op = np.ascontiguousarray(x_op, np.float64)
+        self.b = np.ascontiguousarray(ac_drive(sys.flat) if b is None else b, np.float64)
+        self.status: Optional[np.ndarray] = None
+
+    def freqresp(self, sym, omegas) -> np.ndarray:
+        """Response X(j omega) at angular frequencies `omegas` (rad/s) of an unknown
+        (name or index), of a difference (p, n) of two, or of a list of those:
+        complex [n_freq] for one, [n_freq, k] for a list (freqresp, src/ac.jl:251-258)."""
+        single = not isinstance(sym, list)
+        syms = [sym] if single else list(sym)
+        idx, pairs = [], []
+        for s_ in syms:
+            if isinstance(s_, tuple):
+                pairs.append((len(idx), len(idx) + 1))
+                idx += [_unknown(self.sys, s_[0]), _unknown(self.sys, s_[1])]
+            else:
+                pairs.append((len(idx), None))
+                idx.append(_unknown(self.sys, s_))
+        w = np.ascontiguousarray(omegas, np.float64).ravel()
+        probe = np.asarray(idx, np.int32)
+        resp = np.zeros((len(w), len(probe), 2))
+        st = np.zeros(len(w), np.int32)
+        check(self.sys.lib.cedar_ac(self.sys.handle, _dp(self.x_op), _dp(self.b), len(w), _dp(w), len(probe),
+                                    abi.ptr(probe, C.c_int32), _dp(resp), abi.ptr(st, C.c_int32)))
+        self.status = st
+        z = resp[..., 0] + 1j * resp[..., 1]
+        out = np.stack([z[:, a] if b_ is None else z[:, a] - z[:, b_] for a, b_ in pairs], axis=1)
+        return out[:, 0] if single else out
+
+
+class NoiseSol:
+    """Output noise of the circuit linearised about its DC operating point
+    (NoiseSol, src/ac.jl:107-171): white thermal noise of every resistor."""
+
+    def __init__(self, sys: "System", x_op: np.ndarray):
+        self.sys = sys
+        self.x_op = np.ascontiguousarray(x_op, np.float64)
+        self.status: Optional[np.ndarray] = None
+
+    def psd(self, sym, omegas) -> np.ndarray:
+        """Power spectral density at an unknown (V^2/Hz for a node voltage) over the
+        angular frequencies `omegas` (PSD, src/ac.jl:263-283)."""
+        w = np.ascontiguousarray(omegas, np.float64).ravel()
+        out = np.zeros(len(w))
+        st = np.zeros(len(w), np.int32)
+        check(self.sys.lib.cedar_noise(self.sys.handle, _dp(self.x_op), len(w), _dp(w), _unknown(self.sys, sym),
+                                       _dp(out), abi.ptr(st, C.c_int32)))
+        self.status = st
+        return out
+
+
+def ac(circuit: Union[Circuit, Flat, System], x_op: Optional[np.ndarray] = None) -> ACSol:
+    """ac!(circ) (src/ac.jl:178-186): DC operating point, then the linearisation."""
+    sys = circuit if isinstance(circuit, System) else System(circuit)
+    return ACSol(sys, dc(sys) if x_op is None else x_op)
+
+
+def noise(circuit: Union[Circuit, Flat, System], x_op: Optional[np.ndarray] = None) -> NoiseSol:
+    """noise!(circ) (src/ac.jl:188-197): DC operating point, then the noise analysis."""
+    sys = circuit if isinstance(circuit, System) else System(circuit)
+    return NoiseSol(sys, dc(sys) if x_op is None else x_op)

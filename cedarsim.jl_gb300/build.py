@@ -25,7 +25,7 @@ LANES = (1, 2, 4, 8, 16, 32)
 # (source, object, extra flags): the batched and adjoint kernels are compiled once
 # per lanes-per-instance value so the instantiations build in parallel
 SOURCES = ([("api.cu", "api.cu.o", []), ("k_plain.cu", "k_plain.cu.o", []), ("k_dispatch.cu", "k_dispatch.cu.o", []),
-            ("compile.cpp", "compile.cpp.o", [])]
+            ("k_ac.cu", "k_ac.cu.o", []), ("compile.cpp", "compile.cpp.o", [])]
            + [("k_batch.cu", f"k_batch.k{k}.o", [f"-DCEDAR_LANES={k}"]) for k in LANES]
            + [("k_adjoint.cu", f"k_adjoint.k{k}.o", [f"-DCEDAR_LANES={k}"]) for k in LANES])
 

@@ -104,6 +104,7 @@ class Device:
     terms: List[str]
     params: List[float]
     wave: object = None
+    ac: float = 0.0          # AC magnitude of a V / I source (small-signal drive)
 
 
 @dataclass
@@ -118,6 +119,7 @@ class Flat:
     names: List[str]                       # unknown names (nodes, then "<dev>.I" branches)
     devices: Dict[str, Tuple[int, int]]    # device name -> (group index, instance index)
     ordering: int = 0                      # LU ordering: 0 auto, 1 min degree, 2 nested dissection
+    ac: Dict[str, float] = field(default_factory=dict)  # source name -> AC magnitude
 
     @property
     def n(self) -> int:
@@ -158,13 +160,13 @@ class Circuit:
             self.node_names.append(name)
         return self._node_index[name]
 
-    def _add(self, name, model, terms, params, wave=None):
+    def _add(self, name, model, terms, params, wave=None, ac=0.0):
         if name in self._names:
             raise ValueError(f"duplicate device name {name!r}")
         self._names.add(name)
         for t in terms:
             self.node(t)
-        self.devices.append(Device(name, model, [str(t) for t in terms], [float(p) for p in params], wave))
+        self.devices.append(Device(name, model, [str(t) for t in terms], [float(p) for p in params], wave, float(ac)))
         return self
 
     # ---- devices (CedarSim src/simpledevices.jl)
@@ -195,13 +197,15 @@ class Circuit:
             raise TypeError(f"unsupported waveform {wave!r}")
         return [m, dc, kind] + a, wave
 
-    def V(self, name, p, n, dc=None, wave=None, m=1.0):
+    # `ac`: AC magnitude; like VoltageSource / CurrentSource (src/simpledevices.jl:
+    # 279-300,320-339) only |ac| enters the small-signal drive (no phase)
+    def V(self, name, p, n, dc=None, wave=None, m=1.0, ac=0.0):
         params, wave = self._src_params(dc, wave, m)
-        return self._add(name, V, [p, n], params, wave)
+        return self._add(name, V, [p, n], params, wave, abs(ac))
 
-    def I(self, name, p, n, dc=None, wave=None, m=1.0):
+    def I(self, name, p, n, dc=None, wave=None, m=1.0, ac=0.0):
         params, wave = self._src_params(dc, wave, m)
-        return self._add(name, I, [p, n], params, wave)
+        return self._add(name, I, [p, n], params, wave, abs(ac))
 
     def E(self, name, p, n, cp, cn, gain, m=1.0):
         return self._add(name, E, [p, n, cp, cn], [gain, m])
@@ -248,4 +252,4 @@ class Circuit:
                 devices[d.name] = (len(groups), i)
             groups.append((model, np.ascontiguousarray(term), br, np.ascontiguousarray(par)))
         return Flat(n_nodes, len(branch_of), groups, np.array(pwl, dtype=np.float64), self.temp_c, self.gmin,
-                    names, devices)
+                    names, devices, ac={d.name: d.ac for d in self.devices if d.ac})

@@ -98,6 +98,18 @@ int upload_template(const cedar_ckt_desc *desc, std::unique_ptr<DevTemplate> &ou
   size_t o_tf_lvl = P.vec(H.tf_lvl_ptr), o_tf_row = P.vec(H.tf_row), o_tf_ptr = P.vec(H.tf_ptr), o_tf_pair = P.vec(tf_pair);
   size_t o_tb_lvl = P.vec(H.tb_lvl_ptr), o_tb_row = P.vec(H.tb_row), o_tb_ptr = P.vec(H.tb_ptr), o_tb_pair = P.vec(tb_pair);
   size_t o_ct_ptr = P.vec(H.ct_ptr), o_ct_ent = P.vec(ct_ent), o_adj_goff = P.vec(H.adj_goff);
+  size_t o_out_q = P.vec(H.out_q);
+  std::vector<int> lu_cptr(H.n + 1, 0), lu_cslot(std::max(H.nnz_lu, 1)), lu_srow(std::max(H.nnz_lu, 1));
+  for (int p = 0; p < H.n; ++p)
+    for (int k = H.lu_rowptr[p]; k < H.lu_rowptr[p + 1]; ++k) { lu_srow[k] = p; ++lu_cptr[H.lu_colidx[k] + 1]; }
+  for (int q = 0; q < H.n; ++q) lu_cptr[q + 1] += lu_cptr[q];
+  {
+    std::vector<int> fill(lu_cptr.begin(), lu_cptr.end() - 1);
+    for (int p = 0; p < H.n; ++p)
+      for (int k = H.lu_rowptr[p]; k < H.lu_rowptr[p + 1]; ++k) lu_cslot[fill[H.lu_colidx[k]]++] = k;
+  }
+  size_t o_lu_rowptr = P.vec(H.lu_rowptr), o_lu_colidx = P.vec(H.lu_colidx), o_lu_cptr = P.vec(lu_cptr);
+  size_t o_lu_cslot = P.vec(lu_cslot), o_lu_srow = P.vec(lu_srow);
   std::vector<int> mg_grp;
   int mg_ptr[CEDAR_NMODELS + 1] = {0};
   for (int m = 0; m < CEDAR_NMODELS; ++m) {
@@ -171,6 +183,9 @@ int upload_template(const cedar_ckt_desc *desc, std::unique_ptr<DevTemplate> &ou
   D.tf_lvl = (const int *)(b + o_tf_lvl); D.tf_row = (const int *)(b + o_tf_row); D.tf_ptr = (const int *)(b + o_tf_ptr); D.tf_pair = (const int2 *)(b + o_tf_pair);
   D.tb_lvl = (const int *)(b + o_tb_lvl); D.tb_row = (const int *)(b + o_tb_row); D.tb_ptr = (const int *)(b + o_tb_ptr); D.tb_pair = (const int2 *)(b + o_tb_pair);
   D.ct_ptr = (const int *)(b + o_ct_ptr); D.ct_ent = (const int2 *)(b + o_ct_ent); D.adj_goff = (const int *)(b + o_adj_goff);
+  D.out_q = (const unsigned char *)(b + o_out_q);
+  D.lu_rowptr = (const int *)(b + o_lu_rowptr); D.lu_colidx = (const int *)(b + o_lu_colidx);
+  D.lu_cptr = (const int *)(b + o_lu_cptr); D.lu_cslot = (const int *)(b + o_lu_cslot); D.lu_srow = (const int *)(b + o_lu_srow);
   for (int m = 0; m <= CEDAR_NMODELS; ++m) D.mg_ptr[m] = mg_ptr[m];
   D.mg_grp = (const int *)(b + o_mg_grp);
   D.lu_orig = (const int2 *)(b + o_lu_orig);
@@ -244,9 +259,19 @@ struct cedar_ckt {
   DevBuf<EngStats> stats;
   DevBuf<long long> count;
   DevBuf<long long> off;
+  // AC / noise: G and C per LU slot, inputs, outputs, per-warp complex workspaces
+  DevBuf<double> ac_g, ac_c, ac_b, ac_omega, ac_out, ac_nw;
+  DevBuf<double2> ac_ws, ac_dws;
+  DevBuf<int> ac_probe, ac_status, ac_na, ac_nb, ac_ndense, ac_dpiv;
+  cudaEvent_t ac_ev[4] = {nullptr, nullptr, nullptr, nullptr};   // sparse start / end, dense start / end
+  int ac_last_dense = 0;
+  bool ac_dense_ran = false;
   int threads = 128;
   bool host_only = false;
-  ~cedar_ckt() { if (stream) cudaStreamDestroy(stream); }
+  ~cedar_ckt() {
+    for (cudaEvent_t e : ac_ev) if (e) cudaEventDestroy(e);
+    if (stream) cudaStreamDestroy(stream);
+  }
 };
 
 struct cedar_batch {
@@ -532,6 +557,161 @@ int cedar_tran_run(cedar_ckt *c, const cedar_tran_opts *opts, const double *x0, 
   int rc = check_opts(opts); if (rc) return rc;
   std::vector<double> x(x0, x0 + c->tpl->H.n);
   return run_plain(c, 0, opts, opts->tstart, 0.0, nullptr, x.data(), t_out, x_out, cap, n_out, stats);
+}
+
+// ------------------------------------------------------------------ AC / noise
+namespace {
+constexpr size_t kAcWsBudget = size_t(1) << 30;   // bytes of per-warp workspaces at most
+constexpr int kAcWarpsPerSm = 16;
+
+// G and C per LU slot at x_op, the frequencies, and the workspaces of the warps
+// that will take them; fills everything of `a` but the analysis' own inputs.
+int ac_prepare(cedar_ckt *c, const double *x_op, int32_t n_freq, const double *omega, AcDev &a) {
+  const Template &H = c->tpl->H;
+  const DTpl &D = c->tpl->D;
+  const size_t n = H.n, nlu = std::max(H.nnz_lu, 1);
+  CUDA_TRY(cudaMemcpyAsync(c->x.p, x_op, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(launch_eval(D, c->tpl->D_dev, c->dpar.p, c->x.p, nullptr, 0.0, 1.0, c->dout.p, c->part.p, nullptr, nullptr,
+                       c->stream));
+  CUDA_TRY(c->ac_g.ensure(nlu)); CUDA_TRY(c->ac_c.ensure(nlu));
+  CUDA_TRY(launch_ac_split(D, c->dout.p, c->ac_g.p, c->ac_c.p, c->stream));
+  CUDA_TRY(c->ac_omega.ensure(n_freq)); CUDA_TRY(c->ac_status.ensure(n_freq));
+  CUDA_TRY(cudaMemcpyAsync(c->ac_omega.p, omega, n_freq * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  int dev = 0, sms = 1;
+  CUDA_TRY(cudaGetDevice(&dev));
+  CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const size_t per = (size_t)H.nnz_lu + 3 * n;
+  long long nw = std::min<long long>(n_freq, (long long)sms * kAcWarpsPerSm);
+  nw = std::min<long long>(nw, std::max<long long>(1, (long long)(kAcWsBudget / (per * sizeof(double2)))));
+  CUDA_TRY(c->ac_ws.ensure((size_t)nw * per));
+  a.T = D; a.gval = c->ac_g.p; a.cval = c->ac_c.p; a.omega = c->ac_omega.p; a.n_freq = n_freq;
+  a.ws = c->ac_ws.p; a.ws_stride = (long long)per; a.n_warps = nw; a.status = c->ac_status.p;
+  CUDA_TRY(c->ac_ndense.ensure(1));
+  a.n_dense = c->ac_ndense.p;
+  return 0;
+}
+
+// Sparse solves of every frequency, then the dense rerun of those whose static
+// pivots failed or whose residual check did not pass.  Frequencies still marked
+// kAcDense afterwards (system above kAcDenseNmax) are reported as zero pivots.
+int ac_run(cedar_ckt *c, AcDev &a, bool noise, int32_t *status) {
+  const Template &H = c->tpl->H;
+  for (cudaEvent_t &e : c->ac_ev) if (!e) CUDA_TRY(cudaEventCreate(&e));
+  CUDA_TRY(cudaMemsetAsync(a.n_dense, 0, sizeof(int), c->stream));
+  CUDA_TRY(cudaEventRecord(c->ac_ev[0], c->stream));
+  CUDA_TRY(launch_ac(a, noise, c->stream));
+  CUDA_TRY(cudaEventRecord(c->ac_ev[1], c->stream));
+  int nd = 0;
+  CUDA_TRY(cudaMemcpyAsync(&nd, a.n_dense, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  c->ac_last_dense = nd;
+  c->ac_dense_ran = false;
+  if (nd > 0 && H.n <= kAcDenseNmax) {
+    int dev = 0, sms = 1;
+    CUDA_TRY(cudaGetDevice(&dev));
+    CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const size_t per = (size_t)H.n * H.n + H.n;
+    long long nw = std::min<long long>(nd, (long long)sms * 4);
+    nw = std::min<long long>(nw, std::max<long long>(1, (long long)((size_t(1) << 28) / (per * sizeof(double2)))));
+    CUDA_TRY(c->ac_dws.ensure((size_t)nw * per)); CUDA_TRY(c->ac_dpiv.ensure((size_t)nw * H.n));
+    a.dws = c->ac_dws.p; a.dws_stride = (long long)per; a.dpiv = c->ac_dpiv.p; a.n_dwarps = nw;
+    CUDA_TRY(cudaEventRecord(c->ac_ev[2], c->stream));
+    CUDA_TRY(launch_ac_dense(a, noise, c->stream));
+    CUDA_TRY(cudaEventRecord(c->ac_ev[3], c->stream));
+    c->ac_dense_ran = true;
+  }
+  if (status) {
+    CUDA_TRY(cudaMemcpyAsync(status, a.status, a.n_freq * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    for (long long f = 0; f < a.n_freq; ++f) if (status[f] == kAcDense) status[f] = CEDAR_ST_ZERO_PIVOT;
+  }
+  return 0;
+}
+}  // namespace
+
+int cedar_ac(cedar_ckt *c, const double *x_op, const double *b, int32_t n_freq, const double *omega,
+             int32_t n_probe, const int32_t *probe, double *resp, int32_t *status) {
+  if (!c || !x_op || !b || (n_freq > 0 && (!omega || !resp)) || !probe) return fail(CEDAR_EINVAL, "null argument");
+  if (c->host_only) return fail(CEDAR_EINVAL, "host-only plan handle");
+  if (n_freq < 0 || n_probe <= 0) return fail(CEDAR_EINVAL, "n_freq must be >= 0 and n_probe > 0");
+  const Template &H = c->tpl->H;
+  for (int k = 0; k < n_probe; ++k)
+    if (probe[k] < 0 || probe[k] >= H.n) return fail(CEDAR_EINVAL, "probe outside the unknowns");
+  if (n_freq == 0) return 0;
+  AcDev a{};
+  int rc = ac_prepare(c, x_op, n_freq, omega, a);
+  if (rc) return rc;
+  CUDA_TRY(c->ac_b.ensure(H.n)); CUDA_TRY(c->ac_probe.ensure(n_probe));
+  CUDA_TRY(c->ac_out.ensure((size_t)n_freq * n_probe * 2));
+  CUDA_TRY(cudaMemcpyAsync(c->ac_b.p, b, H.n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(c->ac_probe.p, probe, n_probe * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
+  a.b = c->ac_b.p; a.probe = c->ac_probe.p; a.n_probe = n_probe; a.resp = c->ac_out.p;
+  rc = ac_run(c, a, false, status);
+  if (rc) return rc;
+  CUDA_TRY(cudaMemcpyAsync(resp, c->ac_out.p, (size_t)n_freq * n_probe * 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                           c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+int cedar_noise(cedar_ckt *c, const double *x_op, int32_t n_freq, const double *omega, int32_t probe, double *psd,
+                int32_t *status) {
+  if (!c || !x_op || (n_freq > 0 && (!omega || !psd))) return fail(CEDAR_EINVAL, "null argument");
+  if (c->host_only) return fail(CEDAR_EINVAL, "host-only plan handle");
+  const Template &H = c->tpl->H;
+  if (n_freq < 0) return fail(CEDAR_EINVAL, "n_freq must be >= 0");
+  if (probe < 0 || probe >= H.n) return fail(CEDAR_EINVAL, "probe outside the unknowns");
+  if (n_freq == 0) return 0;
+  // thermal noise current of every resistor: terminals and weight m^2 4 k T / r
+  std::vector<int> na, nb;
+  std::vector<double> nw;
+  const double kT4 = 4.0 * 1.380649e-23 * (H.temp_c + 273.15);
+  for (const GroupInfo &g : H.groups) {
+    if (g.model != CEDAR_R) continue;
+    for (int i = 0; i < g.n_inst; ++i) {
+      const double r = H.par[g.par_off + i], m = H.par[g.par_off + g.n_inst + i];
+      na.push_back(H.term_orig[g.term_off + (size_t)i * g.ntx]);
+      nb.push_back(H.term_orig[g.term_off + (size_t)i * g.ntx + 1]);
+      nw.push_back(m * m * kT4 / r);
+    }
+  }
+  AcDev a{};
+  int rc = ac_prepare(c, x_op, n_freq, omega, a);
+  if (rc) return rc;
+  const size_t nr = na.size();
+  CUDA_TRY(c->ac_na.ensure(std::max<size_t>(nr, 1))); CUDA_TRY(c->ac_nb.ensure(std::max<size_t>(nr, 1)));
+  CUDA_TRY(c->ac_nw.ensure(std::max<size_t>(nr, 1))); CUDA_TRY(c->ac_probe.ensure(1));
+  CUDA_TRY(c->ac_out.ensure(n_freq));
+  if (nr) {
+    CUDA_TRY(cudaMemcpyAsync(c->ac_na.p, na.data(), nr * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(c->ac_nb.p, nb.data(), nr * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(c->ac_nw.p, nw.data(), nr * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  }
+  CUDA_TRY(cudaMemcpyAsync(c->ac_probe.p, &probe, sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
+  a.probe = c->ac_probe.p; a.n_probe = 1; a.psd = c->ac_out.p;
+  a.n_noise = (int)nr; a.noise_a = c->ac_na.p; a.noise_b = c->ac_nb.p; a.noise_w = c->ac_nw.p;
+  rc = ac_run(c, a, true, status);
+  if (rc) return rc;
+  CUDA_TRY(cudaMemcpyAsync(psd, c->ac_out.p, n_freq * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+int cedar_ac_last_stats(const cedar_ckt *c, int32_t *n_dense, double *ms_sparse, double *ms_dense) {
+  if (!c) return fail(CEDAR_EINVAL, "null argument");
+  if (n_dense) *n_dense = c->ac_last_dense;
+  float a = 0.f, b = 0.f;
+  if (c->ac_ev[0]) {
+    CUDA_TRY(cudaEventSynchronize(c->ac_ev[1]));
+    CUDA_TRY(cudaEventElapsedTime(&a, c->ac_ev[0], c->ac_ev[1]));
+    if (c->ac_dense_ran) {
+      CUDA_TRY(cudaEventSynchronize(c->ac_ev[3]));
+      CUDA_TRY(cudaEventElapsedTime(&b, c->ac_ev[2], c->ac_ev[3]));
+    }
+  }
+  if (ms_sparse) *ms_sparse = a;
+  if (ms_dense) *ms_dense = b;
+  return 0;
 }
 
 // ------------------------------------------------------------------ batch

@@ -317,6 +317,12 @@ static bool compile_with(const cedar_ckt_desc *d, Template &T, std::string &err,
     T.groups.push_back(gi);
   }
   T.par_size = par_off; T.dpar_size = dpar_off; T.n_out = out_off;
+  T.out_q.assign(std::max(out_off, 1), 0);
+  for (const GroupInfo &g : T.groups) {
+    const int no = kModels[g.model].nout;
+    for (int i = 0; i < g.n_inst; ++i)
+      for (int k = 0; k < no; ++k) T.out_q[g.out_off + i * no + k] = is_charge_partial(g.model, k) ? 1 : 0;
+  }
 
   // stamps in device order; SJq marks J stamps carrying a charge partial (cj dQ/dV)
   std::vector<Stamp> SJ, SF, SQ;

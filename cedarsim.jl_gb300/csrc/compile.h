@@ -40,6 +40,7 @@ struct Template {
   std::vector<GroupInfo> groups;
   std::vector<int32_t> term_orig, term_int;  // per device terminal (+branch) unknowns
   int par_size = 0, dpar_size = 0, n_out = 0;
+  std::vector<uint8_t> out_q;                // per device output: 1 if it holds cj * dQ/dV (C part of J)
   std::vector<double> par;                   // nominal raw parameters
   std::vector<double> pwl;
 

@@ -70,6 +70,12 @@ struct DTpl {
   const int *tb_lvl, *tb_row, *tb_ptr; const int2 *tb_pair;
   const int *ct_ptr; const int2 *ct_ent;
   const int *adj_goff;
+  // per device output: 1 if it holds cj * dQ/dV (splits J into G and C for AC)
+  const unsigned char *out_q;
+  // LU pattern by internal row (CSR: slots lu_rowptr[p] .. lu_rowptr[p + 1], column
+  // lu_colidx[slot]) and by internal column (slots lu_cslot[lu_cptr[q] ..
+  // lu_cptr[q + 1]), row lu_srow[slot]), for residuals of the assembled matrix
+  const int *lu_rowptr, *lu_colidx, *lu_cptr, *lu_cslot, *lu_srow;
 };
 
 // Gather lists longer than these are summed cooperatively in 32 fixed chunks

@@ -108,6 +108,30 @@ struct PlainArgs {
 };
 cudaError_t launch_plain(const PlainArgs &a, int ws_doubles_n, int threads, cudaStream_t s);
 
+// AC / noise analysis (k_ac.cu): one warp per angular frequency over the
+// template's LU and substitution task lists in complex FP64
+struct AcDev {
+  DTpl T;
+  const double *gval, *cval;          // [nnz_lu] G and C per LU slot at the operating point
+  const double *omega; long long n_freq;
+  const double *b;                    // [n] drive -dFi/d(eps), original equation order (AC)
+  const int *probe; int n_probe;      // original unknowns (noise: probe[0])
+  double *resp;                       // [n_freq * n_probe] complex (re, im)
+  int n_noise; const int *noise_a, *noise_b; const double *noise_w;  // thermal noise currents
+  double *psd;                        // [n_freq]
+  double2 *ws; long long ws_stride;   // per warp: lu [nnz_lu], rd [n], v [n], rhs [n]
+  long long n_warps;                  // workspaces in ws (warps that take frequencies)
+  int *status;                        // [n_freq] CEDAR_ST_*, or kAcDense while a dense rerun is due
+  int *n_dense;                       // frequencies handed to the dense rerun
+  double2 *dws; long long dws_stride; // dense rerun, per warp: A [n * n], rhs [n]
+  int *dpiv; long long n_dwarps;      // per warp: row interchanges [n]; warps of the dense rerun
+};
+constexpr int kAcDense = -1;          // status of a frequency waiting for the dense rerun
+constexpr int kAcDenseNmax = 256;     // largest system the dense rerun takes
+cudaError_t launch_ac_split(const DTpl &T, const double *dout, double *gval, double *cval, cudaStream_t s);
+cudaError_t launch_ac(const AcDev &a, bool noise, cudaStream_t s);
+cudaError_t launch_ac_dense(const AcDev &a, bool noise, cudaStream_t s);
+
 // FP64 issue-rate probe (8 DFMA chains per thread, lanes >= active_lanes idle)
 cudaError_t launch_fp64_probe(int active_lanes, int iters, double *gflops, double *ms);
 

@@ -283,7 +283,7 @@ def instance_flat(template: Flat, block: np.ndarray) -> Flat:
         groups.append((model, term, br, np.ascontiguousarray(block[p:p + par.size].reshape(par.shape))))
         p += par.size
     return Flat(template.n_nodes, template.n_branch, groups, template.pwl, template.temp_c, template.gmin,
-                template.names, template.devices, template.ordering)
+                template.names, template.devices, template.ordering, dict(template.ac))
 
 
 def chain_output_probe(flat: Flat) -> int:

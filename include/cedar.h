@@ -329,6 +329,41 @@ int cedar_batch_results(cedar_batch *b, double *x_final, double *samples, cedar_
  * inst_dx perturbations are not applied.  x_dc[n_inst * n_max] in original
  * order; stats[n_inst].dc_iters and .status report each solve. */
 int cedar_batch_dcop(cedar_batch *b, const cedar_tran_opts *opts, double *x_dc, cedar_stats *stats);
+
+/* ---- small-signal AC and noise about an operating point -------------------
+ * Replaces ACSol / freqresp and NoiseSol / PSD (src/ac.jl:73-104,251-258 and
+ * src/ac.jl:107-171,263-283), whose descriptor system is (jω M − Ju)⁻¹ B about
+ * the DC operating point.  Here G = dFi/dx and C = dFq/dx are evaluated at x_op
+ * (n doubles, original unknown order, e.g. from cedar_dcop), and every angular
+ * frequency omega[f] (rad/s) is one factorisation of G + j omega C on the GPU
+ * with the circuit's static pivot order; frequencies run in parallel.
+ * status[f] (may be NULL): CEDAR_ST_OK, or CEDAR_ST_ZERO_PIVOT when a pivot of
+ * G + j omega C is zero or not finite (that frequency's outputs are NaN). */
+
+/* AC response: X_f solves (G + j omega_f C) X_f = b.  b (n doubles, original
+ * equation order) is -dFi/d(eps) of the AC drive eps: a voltage source with AC
+ * magnitude a adds +a to its branch equation, a current source of multiplicity m
+ * adds +m a to the KCL row of its first terminal and -m a to the second
+ * (src/simpledevices.jl:292-294,331-333).  resp receives n_freq * n_probe
+ * complex values X_f[probe[k]], interleaved (re, im), frequency-major. */
+int cedar_ac(cedar_ckt *ckt, const double *x_op, const double *b, int32_t n_freq, const double *omega,
+             int32_t n_probe, const int32_t *probe, double *resp, int32_t *status);
+
+/* Output noise PSD (V^2/Hz for a node voltage) at unknown `probe`:
+ * psd[f] = sum over resistors of m^2 (4 k T / r) |H_r(j omega_f)|^2, with H_r the
+ * transfer from the resistor's white thermal noise current (src/simpledevices.jl:
+ * 70-75; multiplicity m scales that current with the branch current,
+ * src/simulate_ir.jl:54) to the probe, and T = the circuit's temp_c + 273.15.
+ * One transposed solve (G + j omega C)^T y = e_probe per frequency gives every
+ * H_r at once. */
+int cedar_noise(cedar_ckt *ckt, const double *x_op, int32_t n_freq, const double *omega, int32_t probe,
+                double *psd, int32_t *status);
+/* Of the last cedar_ac / cedar_noise call on this handle: how many frequencies
+ * the dense partial-pivoting rerun took (their sparse solve met a zero pivot or
+ * failed the residual check), and the device time (ms, CUDA events) of the
+ * sparse kernel and of the dense rerun (0 when it did not run).  Measurement
+ * helper; no counterpart in the reference. */
+int cedar_ac_last_stats(const cedar_ckt *ckt, int32_t *n_dense, double *ms_sparse, double *ms_dense);
 /* Device time of the last batch launch (CUDA events on the handle's stream). */
 int cedar_batch_last_ms(cedar_batch *b, double *ms);
 int cedar_batch_set_tuning(cedar_batch *b, const cedar_batch_tuning *t);

@@ -88,6 +88,59 @@ class Oracle:
         assert rc == 0
         return F, Fi, Fq, G, Cm
 
+    # ---- small-signal AC and noise (dense complex solves; LAPACK partial pivoting)
+    def ac_drive(self, flat, x_op):
+        """b = -dFi/d(eps) of the AC sources, from the oracle's own source equations:
+        in :ac mode a source's value is dc + eps |ac| (src/simpledevices.jl:292-294,
+        331-333), and Fi is linear in it, so a unit step of eps is exact."""
+        import copy
+        _, fi0, _, _, _ = self.eval(flat, x_op, dc=True)
+        f2 = copy.deepcopy(flat)
+        for name, mag in flat.ac.items():
+            gi, ii = f2.devices[name]
+            f2.groups[gi][3][1, ii] += mag          # raw parameter 1 = dc value
+        _, fi1, _, _, _ = self.eval(f2, x_op, dc=True)
+        return -(fi1 - fi0)
+
+    def ac(self, flat, x_op, omegas, probes, b=None):
+        """X(j omega)[probes] with (G + j omega C) X = b, G, C the oracle's dense
+        partials at x_op (ACSol + freqresp, src/ac.jl:73-104,251-258)."""
+        _, _, _, G, Cm = self.eval(flat, x_op, dc=True)
+        b = self.ac_drive(flat, x_op) if b is None else np.asarray(b, np.float64)
+        out = np.zeros((len(omegas), len(probes)), complex)
+        for k, w in enumerate(omegas):
+            out[k] = np.linalg.solve(G + 1j * w * Cm, b.astype(complex))[list(probes)]
+        return out
+
+    def noise(self, flat, x_op, omegas, probe):
+        """Output PSD at `probe` (PSD, src/ac.jl:263-283): one direct solve per
+        resistor thermal-noise current, pwr = 4 k T / r (src/simpledevices.jl:70-75),
+        scaled by the multiplicity like the branch current (src/simulate_ir.jl:54)."""
+        _, _, _, G, Cm = self.eval(flat, x_op, dc=True)
+        n = flat.n
+        kT4 = 4.0 * 1.380649e-23 * (flat.temp_c + 273.15)
+        cols, pwr = [], []
+        for (model, term, br, par) in flat.groups:
+            if model != 1:
+                continue
+            for i in range(par.shape[1]):
+                inj = np.zeros(n)
+                a, c = term[i, 0], term[i, 1]
+                if a >= 0:
+                    inj[a] += par[1, i]
+                if c >= 0:
+                    inj[c] -= par[1, i]
+                cols.append(inj)
+                pwr.append(kT4 / par[0, i])
+        out = np.zeros(len(omegas))
+        if not cols:
+            return out
+        INJ, pwr = np.array(cols).T.astype(complex), np.array(pwr)
+        for k, w in enumerate(omegas):
+            H = np.linalg.solve(G + 1j * w * Cm, INJ)[probe]
+            out[k] = float(np.sum(pwr * np.abs(H) ** 2))
+        return out
+
     def dcop(self, flat, t=0.0, x0=None, opts=None):
         h = self.pkg.abi.DescHolder(flat)
         x = np.zeros(flat.n) if x0 is None else np.ascontiguousarray(x0, np.float64).copy()

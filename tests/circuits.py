@@ -72,6 +72,23 @@ def butterworth(pkg):  # test/transients.jl:129-179
     return c
 
 
+def butterworth_ac(pkg):  # test/ac.jl:17-35: AC 1 drive, R4 split in two 2-ohm halves, temp 23, gmin 0
+    c = pkg.Circuit(temp_c=23.0, gmin=0.0)
+    c.V("V1", "vin", "0", wave=pkg.Sin(0.0, 1.0, 1.0 / (2 * math.pi)), ac=1.0)
+    c.L("L1", "vin", "n1", 1.5); c.C("C2", "n1", "0", 4.0 / 3.0); c.L("L3", "n1", "vout", 0.5)
+    c.R("R4", "vout", "0", r=2.0); c.R("R5", "vout", "0", r=2.0)
+    return c
+
+
+def butterworth_H(s):  # test/ac.jl:42-45: 1 / ((s + 1)(s^2 + s + 1))
+    return 1.0 / ((s + 1.0) * (s * s + s + 1.0))
+
+
+def butterworth_Z(s):  # test/ac.jl:77-79: impedance seen at vout, R4 || (L3 + (L1 || C2)), R4 = 1
+    par = lambda a, b: a * b / (a + b)
+    return par(par(s * 1.5, 1.0 / (s * 4.0 / 3.0)) + s * 0.5, 1.0)
+
+
 def butterworth_vout(t):
     return (math.exp(-t) - math.sin(t) - math.cos(t)) / 2 + (2 * math.sin((math.sqrt(3) * t) / 2)) / (math.sqrt(3) * math.sqrt(math.exp(t)))
 
