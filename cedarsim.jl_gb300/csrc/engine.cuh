@@ -84,6 +84,60 @@ constexpr int kLongGather = 16;
 constexpr int kLongEval = 64;
 constexpr int kLongPairs = 16;
 
+// Pairwise sum of PER (a power of two) values pushed in order 0..PER-1, built
+// as a binary counter: level b holds the sum of the last complete left subtree
+// of 2^b values, so the association is the balanced tree ((v0+v1)+(v2+v3))+...
+// with the left operand first.  It lets the chunk loop below stay rolled when a
+// lane owns many chunks (K = 1, 2), which keeps those instantiations small;
+// `total` is valid after the last push.
+template <int PER>
+struct PairwiseStack {
+  static constexpr int LOG = PER >= 32 ? 5 : PER >= 16 ? 4 : PER >= 8 ? 3 : PER >= 4 ? 2 : PER >= 2 ? 1 : 0;
+  double lvl[LOG > 0 ? LOG : 1];
+  double total;
+  __device__ __forceinline__ void push(int j, double v) {
+    bool open = true;
+#pragma unroll
+    for (int b = 0; b < LOG; ++b) {
+      if (open) {
+        if ((j >> b) & 1) v = lvl[b] + v;
+        else { lvl[b] = v; open = false; }
+      }
+    }
+    total = v;
+  }
+};
+
+// Sum, by one lane, of its chunks [rank * 32/K, (rank + 1) * 32/K) of a list of
+// len items starting at a, combined by the fixed pairwise tree.  chunk(c0, c1)
+// sums items [c0, c1) in order.  Up to 8 chunks per lane the loop is unrolled
+// with the partial sums in registers; beyond that it is rolled (same bits).
+template <int K, typename Chunk>
+__device__ __forceinline__ double lane_chunk_sum(int a, int len, int rank, const Chunk &chunk) {
+  constexpr int PER = 32 / K;
+  if constexpr (PER <= 8) {
+    double part[PER];
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+      const int c = rank * PER + j;
+      part[j] = chunk(a + (int)(((long long)len * c) >> 5), a + (int)(((long long)len * (c + 1)) >> 5));
+    }
+#pragma unroll
+    for (int w = 1; w < PER; w <<= 1)
+#pragma unroll
+      for (int j = 0; j + w < PER; j += 2 * w) part[j] = part[j] + part[j + w];
+    return part[0];
+  } else {
+    PairwiseStack<PER> tree;
+#pragma unroll 1
+    for (int j = 0; j < PER; ++j) {
+      const int c = rank * PER + j;
+      tree.push(j, chunk(a + (int)(((long long)len * c) >> 5), a + (int)(((long long)len * (c + 1)) >> 5)));
+    }
+    return tree.total;
+  }
+}
+
 // Sum of a long gather list (entries (out << 1) | neg into dout) by the K lanes
 // of a group (mask, rank): the list is cut into 32 fixed chunks, each summed in
 // order, and the chunk sums are combined by a fixed pairwise tree.  A lane owns
@@ -93,21 +147,11 @@ template <int K>
 __device__ __forceinline__ double long_gather(const int *ptr, const int *ent, int q, const double *dout, int rank,
                                               unsigned mask) {
   const int a = ptr[q], len = ptr[q + 1] - a;
-  constexpr int PER = 32 / K;
-  double part[PER];
-#pragma unroll
-  for (int j = 0; j < PER; ++j) {
-    const int c = rank * PER + j;
-    const int c0 = a + (int)(((long long)len * c) >> 5), c1 = a + (int)(((long long)len * (c + 1)) >> 5);
+  double v = lane_chunk_sum<K>(a, len, rank, [&](int c0, int c1) {
     double acc = 0.0;
-    for (int k = c0; k < c1; ++k) { const int e = ent[k]; const double v = dout[e >> 1]; acc = (e & 1) ? acc - v : acc + v; }
-    part[j] = acc;
-  }
-#pragma unroll
-  for (int w = 1; w < PER; w <<= 1)
-#pragma unroll
-    for (int j = 0; j + w < PER; j += 2 * w) part[j] = part[j] + part[j + w];
-  double v = part[0];
+    for (int k = c0; k < c1; ++k) { const int e = ent[k]; const double d = dout[e >> 1]; acc = (e & 1) ? acc - d : acc + d; }
+    return acc;
+  });
 #pragma unroll
   for (int o = 1; o < K; o <<= 1) { const double u = __shfl_xor_sync(mask, v, o, K); v = (rank & o) ? u + v : v + u; }
   return v;
@@ -118,22 +162,11 @@ __device__ __forceinline__ double long_gather(const int *ptr, const int *ent, in
 template <int K>
 __device__ __forceinline__ double long_pair_sum(const int2 *pairs, int p0, int p1, const double *A, const double *B,
                                                 int rank, unsigned mask) {
-  const int len = p1 - p0;
-  constexpr int PER = 32 / K;
-  double part[PER];
-#pragma unroll
-  for (int j = 0; j < PER; ++j) {
-    const int c = rank * PER + j;
-    const int c0 = p0 + (int)(((long long)len * c) >> 5), c1 = p0 + (int)(((long long)len * (c + 1)) >> 5);
+  double v = lane_chunk_sum<K>(p0, p1 - p0, rank, [&](int c0, int c1) {
     double acc = 0.0;
     for (int k = c0; k < c1; ++k) { const int2 pr = pairs[k]; acc += A[pr.x] * B[pr.y]; }
-    part[j] = acc;
-  }
-#pragma unroll
-  for (int w = 1; w < PER; w <<= 1)
-#pragma unroll
-    for (int j = 0; j + w < PER; j += 2 * w) part[j] = part[j] + part[j + w];
-  double v = part[0];
+    return acc;
+  });
 #pragma unroll
   for (int o = 1; o < K; o <<= 1) { const double u = __shfl_xor_sync(mask, v, o, K); v = (rank & o) ? u + v : v + u; }
   return v;
