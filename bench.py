@@ -255,7 +255,7 @@ def measure_rings(pkg, args, C):
     tpl, itpl, par, off, dx, dxo = pkg.generators.mc_rings(args.ring_inst, seed=args.seed)
     f = tpl[0]
     probes = np.array([[f.index("out1")]], np.int32)
-    sw = pkg.Sweep(tpl, itpl, par, off, inst_dx=dx, inst_dx_off=dxo, probes=probes, n_samples=501)
+    sw = pkg.Batch(tpl, itpl, par, off, inst_dx=dx, inst_dx_off=dxo, probes=probes, n_samples=501)
     tstop = args.ring_tstop_ns * 1e-9
     o = pkg.make_opts("bdf2", True, 0.0, tstop, 0.0, True, reltol=1e-6, abstol_v=1e-9, hmax=tstop / 50)
     r = sw.run(o)
@@ -401,7 +401,7 @@ def main():
     templates, itpl, par, off, probes = workload(pkg, args.n_inst, args.seed)
     mine = shard(itpl, templates, rank, world)
     n_samples = 201
-    sw = pkg.Sweep(templates, itpl[mine], par, off[mine], probes=probes, n_samples=n_samples)
+    sw = pkg.Batch(templates, itpl[mine], par, off[mine], probes=probes, n_samples=n_samples)
     if args.lanes:
         sw.set_tuning(args.lanes, args.warps or 4)
     tstop = args.tstop_ns * 1e-9
@@ -459,7 +459,7 @@ def main():
         barrier(dist)
         torch.cuda.synchronize()
         te0 = time.perf_counter()
-        sw2 = pkg.Sweep(templates, itpl[mine], par, off[mine], probes=probes, n_samples=n_samples)
+        sw2 = pkg.Batch(templates, itpl[mine], par, off[mine], probes=probes, n_samples=n_samples)
         if args.lanes:
             sw2.set_tuning(args.lanes, args.warps or 4)
         r2 = sw2.run(o)
@@ -493,7 +493,7 @@ def main():
     adj = None
     if not args.no_adjoint:
         t5, i5, p5, o5_off, obj5, ts5 = adjoint_workload(pkg, args)
-        sw5 = pkg.Sweep(t5, i5, p5, o5_off)
+        sw5 = pkg.Batch(t5, i5, p5, o5_off)
         if args.lanes:
             sw5.set_tuning(args.lanes, args.warps or 4)
         sw5.adjoint(opts_for(pkg, 0.05e-9), obj5, ts5)          # warm-up

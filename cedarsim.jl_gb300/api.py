@@ -7,9 +7,10 @@ prob.f.f(out, du, u, p, t) / prob.f.jac(J, du, u, p, gamma, t)
    (benchmarks/benchmark_common.jl:138,155)            System.f / System.jac
 dc!(circ)                 (src/sweeps.jl:437-448)        dc(circuit)
 tran!(circ, tspan)        (src/sweeps.jl:450-463)        tran(circuit, tspan, ...)
-CircuitSweep + tran!.     (src/sweeps.jl:390-435,488-502) Sweep(...).tran(...)
-CircuitSweep + dc!.       (src/sweeps.jl:471-486)        Sweep(...).dc()
-forward sensitivities     (test/sensitivity.jl:13-42)    Sweep(...).adjoint(...)
+CircuitSweep + tran!.     (src/sweeps.jl:390-435,488-502) tran(CircuitSweep(...), tspan)
+CircuitSweep + dc!.       (src/sweeps.jl:471-486)        dc(CircuitSweep(...))
+instance tables (MC)      (no counterpart)               Batch(...).tran(...), .dc()
+forward sensitivities     (test/sensitivity.jl:13-42)    Batch(...).adjoint(...)
 ac!(circ) / freqresp      (src/ac.jl:178-186,251-258)    ac(circuit).freqresp(sym, omegas)
 noise!(circ) / PSD        (src/ac.jl:188-197,263-283)    noise(circuit).psd(sym, omegas)
 acdec(nd, fstart, fstop)  (src/ac.jl:288-301)            acdec(nd, fstart, fstop)
@@ -28,6 +29,7 @@ import numpy as np
 from . import abi
 from .abi import BatchHolder, BatchTuning, DescHolder, Stats, STATS_DTYPE, check, load_library, make_opts
 from .circuit import Circuit, Flat, I as _MODEL_I, V as _MODEL_V
+from .sweeps import CircuitSweep, sweep_dc, sweep_tran
 
 
 def _flat(c: Union[Circuit, Flat]) -> Flat:
@@ -144,9 +146,15 @@ def _stats_dict(st) -> dict:
     return {k: getattr(st, k) for k, _ in Stats._fields_ if k != "pad"}
 
 
-def dc(circuit: Union[Circuit, Flat, System], t: float = 0.0, x0: Optional[np.ndarray] = None):
+def dc(circuit: Union[Circuit, Flat, System, "CircuitSweep"], t: float = 0.0, x0: Optional[np.ndarray] = None, **kw):
     """DC operating point (CedarDCOp's role): Newton, then pseudo-transient continuation, then
-    source stepping; rerun with dense partial pivoting if the static pivot order fails."""
+    source stepping; rerun with dense partial pivoting if the static pivot order fails.
+    Over a CircuitSweep this is the dc!. broadcast: every point in one batched launch,
+    keyword arguments as sweeps.sweep_dc."""
+    if isinstance(circuit, CircuitSweep):
+        return sweep_dc(circuit, **kw)
+    if kw:
+        raise TypeError(f"dc() of one circuit takes no options {sorted(kw)}")
     sys = circuit if isinstance(circuit, System) else System(circuit)
     x = np.zeros(sys.n) if x0 is None else np.ascontiguousarray(x0, np.float64).copy()
     st = Stats()
@@ -154,11 +162,14 @@ def dc(circuit: Union[Circuit, Flat, System], t: float = 0.0, x0: Optional[np.nd
     return x
 
 
-def tran(circuit: Union[Circuit, Flat, System], tspan: Tuple[float, float], method: str = "bdf2",
+def tran(circuit: Union[Circuit, Flat, System, "CircuitSweep"], tspan: Tuple[float, float], method: str = "bdf2",
          h: Optional[float] = None, adaptive: Optional[bool] = None, x0: Optional[np.ndarray] = None,
          dcop: bool = True, reltol: float = 1e-6, abstol_v: float = 1e-9, abstol_i: float = 1e-12,
          cap: int = 1 << 20, **kw) -> Solution:
-    """Transient analysis on the GPU (the counterpart of tran!(circ, tspan))."""
+    """Transient analysis on the GPU (the counterpart of tran!(circ, tspan)).  Over a
+    CircuitSweep this is the tran!. broadcast (keyword arguments as sweeps.sweep_tran)."""
+    if isinstance(circuit, CircuitSweep):
+        return sweep_tran(circuit, tspan, method=method, reltol=reltol, abstol_v=abstol_v, dcop=dcop, **kw)
     sys = circuit if isinstance(circuit, System) else System(circuit)
     if adaptive is None:
         adaptive = h is None
@@ -182,7 +193,7 @@ class BatchResult:
     stats: np.ndarray        # structured STATS_DTYPE
 
 
-class Sweep:
+class Batch:
     """Batched instances (a CircuitSweep / Monte Carlo over parameter blocks) on one GPU."""
 
     def __init__(self, templates: Sequence[Union[Circuit, Flat]], inst_template, inst_par=None, inst_par_off=None,

@@ -35,7 +35,7 @@ def _small(pkg, n_inst=6, seed=7, lengths=(5, 7, 9)):
 
 def test_two_resistor_closed_form(gpu, pkg):
     flat = K.two_resistor(pkg).flatten()
-    sw = pkg.Sweep([flat], np.zeros(1, np.int32))
+    sw = pkg.Batch([flat], np.zeros(1, np.int32))
     n = flat.names
     obj = pkg.abi.Objective(n.index("vcc"), n.index("V.I"), n.index("out"), 0, 0.25, 0.0, 0.0, 1.0)
     r = sw.adjoint(pkg.make_opts(tstop=1e-5), [obj])
@@ -47,7 +47,7 @@ def test_two_resistor_closed_form(gpu, pkg):
 
 def test_energy_closed_form(gpu, pkg):
     flat = K.two_resistor(pkg, r1=2.0, r2=3.0).flatten()
-    sw = pkg.Sweep([flat], np.zeros(1, np.int32))
+    sw = pkg.Batch([flat], np.zeros(1, np.int32))
     n = flat.names
     obj = pkg.abi.Objective(n.index("vcc"), n.index("V.I"), n.index("out"), 0, 0.25, 1.0, 0.0, 0.0)
     tf = 1e-5
@@ -58,7 +58,7 @@ def test_energy_closed_form(gpu, pkg):
 
 def test_chains_match_oracle_adjoint(gpu, pkg, oracle):
     templates, itpl, par, off, objs, tstar = _small(pkg)
-    sw = pkg.Sweep(templates, itpl, par, off)
+    sw = pkg.Batch(templates, itpl, par, off)
     o = pkg.make_opts(tstop=1.2e-9)
     objectives = [_obj(pkg, ob) for ob in objs]
     r = sw.adjoint(o, objectives, tstar)
@@ -79,7 +79,7 @@ def test_chains_vs_fd_on_gpu_steps(gpu, pkg, oracle):
     """Central differences of the objective over the GPU's own accepted steps
     (replayed by the oracle), on every width of two instances."""
     templates, itpl, par, off, objs, tstar = _small(pkg, n_inst=2, seed=3, lengths=(7,))
-    sw = pkg.Sweep(templates, itpl, par, off)
+    sw = pkg.Batch(templates, itpl, par, off)
     o = pkg.make_opts(tstop=1.2e-9)
     rep = pkg.make_opts(tstop=1.2e-9, nr_factor=1e-5)
     objectives = [_obj(pkg, ob) for ob in objs]
@@ -106,7 +106,7 @@ def test_mixed_circuit_matches_oracle(gpu, pkg, oracle):
     n = flat.names
     obj = pkg.abi.Objective(n.index("vdd"), n.index("VDD.I"), n.index("out1"), 0, 0.9, 1e12, 1e20, 1.0)
     o = pkg.make_opts(tstop=0.8e-9)
-    sw = pkg.Sweep([flat], np.zeros(1, np.int32))
+    sw = pkg.Batch([flat], np.zeros(1, np.int32))
     r = sw.adjoint(o, [obj], np.array([0.2e-9]))
     assert r.status[0] == 0
     phi, g, T, ords = oracle.adjoint(flat, o, o, obj, 0.2e-9)
@@ -119,7 +119,7 @@ def test_mixed_circuit_matches_oracle(gpu, pkg, oracle):
 
 def test_adjoint_bitwise_across_tile_shapes_and_reruns(gpu, pkg):
     templates, itpl, par, off, objs, tstar = _small(pkg, n_inst=10, seed=9)
-    sw = pkg.Sweep(templates, itpl, par, off)
+    sw = pkg.Batch(templates, itpl, par, off)
     o = pkg.make_opts(tstop=0.8e-9)
     objectives = [_obj(pkg, ob) for ob in objs]
     base = None
@@ -136,7 +136,7 @@ def test_adjoint_bitwise_across_tile_shapes_and_reruns(gpu, pkg):
 def test_adjoint_segments_longer_than_one_checkpoint(gpu, pkg, oracle):
     """A run of several hundred steps crosses many 64-step checkpoints."""
     templates, itpl, par, off, objs, tstar = _small(pkg, n_inst=1, seed=1, lengths=(5,))
-    sw = pkg.Sweep(templates, itpl, par, off)
+    sw = pkg.Batch(templates, itpl, par, off)
     o = pkg.make_opts(tstop=4e-9, hmax=4e-9 / 50)
     objectives = [_obj(pkg, ob) for ob in objs]
     r = sw.adjoint(o, objectives, tstar)
@@ -149,7 +149,7 @@ def test_adjoint_segments_longer_than_one_checkpoint(gpu, pkg, oracle):
 
 def test_adjoint_tape_overflow_is_reported(gpu, pkg):
     templates, itpl, par, off, objs, tstar = _small(pkg, n_inst=2, seed=2, lengths=(5,))
-    sw = pkg.Sweep(templates, itpl, par, off)
+    sw = pkg.Batch(templates, itpl, par, off)
     r = sw.adjoint(pkg.make_opts(tstop=1.2e-9), [_obj(pkg, ob) for ob in objs], tstar, tape_cap=16)
     assert np.all(r.status == 4)              # CEDAR_ST_MAX_STEPS
     assert np.all(np.isnan(r.phi)) and np.all(np.isnan(r.grad))
@@ -157,6 +157,6 @@ def test_adjoint_tape_overflow_is_reported(gpu, pkg):
 
 def test_adjoint_rejects_fixed_step(gpu, pkg):
     templates, itpl, par, off, objs, tstar = _small(pkg, n_inst=1, lengths=(5,))
-    sw = pkg.Sweep(templates, itpl, par, off)
+    sw = pkg.Batch(templates, itpl, par, off)
     with pytest.raises(pkg.abi.CedarError):
         sw.adjoint(pkg.make_opts(adaptive=False, h=1e-12, tstop=1e-10), [_obj(pkg, ob) for ob in objs], tstar)

@@ -24,7 +24,7 @@ def test_mc4096_full_run_properties_and_sampled_parity(gpu, pkg, oracle):
     probes = np.array([[g.chain_output_probe(f), f.index("in")] for f in templates], np.int32)
     ns = 101
     o = pkg.make_opts("bdf2", True, 0.0, TSTOP, 0.0, True, reltol=RELTOL, abstol_v=ABSTOL, hmax=TSTOP / 50)
-    sw = pkg.Sweep(templates, itpl, par, off, probes=probes, n_samples=ns)
+    sw = pkg.Batch(templates, itpl, par, off, probes=probes, n_samples=ns)
     r = sw.run(o)
     st = r.stats
     assert np.all(st["status"] == 0)
@@ -51,7 +51,7 @@ def test_rings_full_set_dc_points(gpu, pkg, oracle):
     """All 1024 ring instances reach their DC operating point (metastable points
     included, through the dense-pivoting rerun); a sample agrees with the oracle."""
     tpl, itpl, par, off, dx, dxo = pkg.generators.mc_rings(1024)
-    sw = pkg.Sweep(tpl, itpl, par, off, inst_dx=dx, inst_dx_off=dxo)
+    sw = pkg.Batch(tpl, itpl, par, off, inst_dx=dx, inst_dx_off=dxo)
     x, st = sw.dc()
     assert np.all(st["status"] == 0)
     assert np.all(np.isfinite(x))
@@ -68,7 +68,7 @@ def test_adjoint_full_horizon(gpu, pkg, oracle):
     against central differences (step 1e-6 W) on 8 sampled widths, with the GPU's
     own accepted steps replayed by the oracle; agreement 1e-5 relative."""
     templates, itpl, par, off, objs, tstar = pkg.generators.adjoint_chains(1, seed=20240607, lengths=[31])
-    sw = pkg.Sweep(templates, itpl, par, off)
+    sw = pkg.Batch(templates, itpl, par, off)
     objective = pkg.abi.Objective(*[int(v) for v in objs[0][:3]], 0, *[float(v) for v in objs[0][3:]])
     o = pkg.make_opts(tstop=TSTOP, hmax=TSTOP / 50)
     rep = pkg.make_opts(tstop=TSTOP, hmax=TSTOP / 50, nr_factor=1e-5)

@@ -140,7 +140,7 @@ def small_mc(pkg, n_inst=48, seed=11):
 
 def test_batch_mc_parity(gpu, pkg, oracle):
     templates, itpl, par, off, probes = small_mc(pkg)
-    sw = pkg.Sweep(templates, itpl, par, off, probes=probes, n_samples=41)
+    sw = pkg.Batch(templates, itpl, par, off, probes=probes, n_samples=41)
     o = pkg.make_opts("bdf2", True, 0.0, 2e-9, 0.0, True)
     res = sw.run(o)
     xf, samp, st = oracle.batch(sw.holder, o)
@@ -159,7 +159,7 @@ def test_batch_tile_shapes_bitwise_identical(gpu, pkg):
     """Every lanes-per-instance choice runs the same arithmetic: bitwise-equal results,
     and a rerun is bitwise equal too (fixed-order reductions, no atomics)."""
     templates, itpl, par, off, probes = small_mc(pkg, n_inst=40, seed=5)
-    sw = pkg.Sweep(templates, itpl, par, off, probes=probes, n_samples=21)
+    sw = pkg.Batch(templates, itpl, par, off, probes=probes, n_samples=21)
     o = pkg.make_opts("bdf2", True, 0.0, 1.5e-9, 0.0, True)
     base = None
     for K_, W in [(1, 2), (2, 4), (4, 4), (8, 4), (16, 8), (32, 2), (8, 4)]:
@@ -180,7 +180,7 @@ def test_batch_windows_match_uninterrupted_run(gpu, pkg):
     import ctypes as C
     templates, itpl, par, off, probes = small_mc(pkg, n_inst=24, seed=3)
     o = pkg.make_opts("bdf2", True, 0.0, 1.2e-9, 0.0, True)
-    sw = pkg.Sweep(templates, itpl, par, off, probes=probes, n_samples=25)
+    sw = pkg.Batch(templates, itpl, par, off, probes=probes, n_samples=25)
     full = sw.run(o)
     lib = sw.lib
     pkg.abi.check(lib.cedar_batch_start(sw.handle, C.byref(o)))
@@ -207,7 +207,7 @@ def test_autotune_picks_a_shape_and_caches_it(gpu, pkg, tmp_path):
     GPU, instance count and template sizes, and a second call reuses it."""
     import json
     templates, itpl, par, off, probes = small_mc(pkg, n_inst=64, seed=8)
-    sw = pkg.Sweep(templates, itpl, par, off)
+    sw = pkg.Batch(templates, itpl, par, off)
     o = pkg.make_opts("bdf2", True, 0.0, 1e-9, 0.0, True)
     cache = str(tmp_path / "tune.json")
     k, w = sw.autotune(o, 0.05e-9, cache=cache)
@@ -215,7 +215,7 @@ def test_autotune_picks_a_shape_and_caches_it(gpu, pkg, tmp_path):
     assert sw.tuning == (k, w)
     table = json.load(open(cache))
     assert list(table.values()) == [[k, w]]
-    sw2 = pkg.Sweep(templates, itpl, par, off)
+    sw2 = pkg.Batch(templates, itpl, par, off)
     assert sw2.autotune(o, 0.05e-9, cache=cache) == (k, w) and sw2.tuning == (k, w)
     r = sw2.run(o)
     assert np.all(r.stats["status"] == 0)

@@ -18,7 +18,7 @@ def _rings(pkg, n):
 
 def test_ring_batch_matches_oracle(gpu, pkg, oracle):
     tpl, itpl, par, off, dx, dxo, probes = _rings(pkg, 6)
-    sw = pkg.Sweep(tpl, itpl, par, off, inst_dx=dx, inst_dx_off=dxo, probes=probes, n_samples=61)
+    sw = pkg.Batch(tpl, itpl, par, off, inst_dx=dx, inst_dx_off=dxo, probes=probes, n_samples=61)
     o = pkg.make_opts(tstop=3e-9)
     res = sw.run(o)
     xf, samp, st = oracle.batch(sw.holder, o)
@@ -34,7 +34,7 @@ def test_ring_batch_matches_oracle(gpu, pkg, oracle):
 
 def test_ring_tile_shapes_bitwise(gpu, pkg):
     tpl, itpl, par, off, dx, dxo, probes = _rings(pkg, 12)
-    sw = pkg.Sweep(tpl, itpl, par, off, inst_dx=dx, inst_dx_off=dxo, probes=probes, n_samples=21)
+    sw = pkg.Batch(tpl, itpl, par, off, inst_dx=dx, inst_dx_off=dxo, probes=probes, n_samples=21)
     o = pkg.make_opts(tstop=1e-9)
     base = None
     for K_, W in [(32, 4), (4, 2), (16, 8)]:
@@ -67,7 +67,7 @@ def test_batched_dc_operating_points(gpu, pkg, oracle):
     ct, ci, cp, co = pkg.generators.mc_chains(6, seed=4, lengths=[5, 9, 21])
     cases.append((ct, ci, cp, co, None, None))
     for templates, it, p_, o_, d_, do_ in cases:
-        sw = pkg.Sweep(templates, it, p_, o_, inst_dx=d_, inst_dx_off=do_)
+        sw = pkg.Batch(templates, it, p_, o_, inst_dx=d_, inst_dx_off=do_)
         x, st = sw.dc()
         assert np.all(st["status"] == 0)
         for i in range(len(it)):
