@@ -164,7 +164,7 @@ EXPORTS = [
     "cedar_batch_get_tuning", "cedar_batch_autotune", "cedar_batch_nmax",
     "cedar_adjoint_run", "cedar_adjoint_nparams", "cedar_adjoint_tape", "cedar_adjoint_last_ms",
     "cedar_fp64_probe", "cedar_ckt_stream", "cedar_batch_dcop", "cedar_ac", "cedar_noise",
-    "cedar_ac_last_stats",
+    "cedar_ac_last_stats", "cedar_va_count", "cedar_va_name",
 ]
 
 _lib = None
@@ -226,11 +226,23 @@ def load_library(build_if_missing: bool = True):
                                c_int32_p]),
         "cedar_noise": (C.c_int, [P, c_double_p, C.c_int32, c_double_p, C.c_int32, c_double_p, c_int32_p]),
         "cedar_ac_last_stats": (C.c_int, [P, c_int32_p, c_double_p, c_double_p]),
+        "cedar_va_count": (C.c_int, []),
+        "cedar_va_name": (C.c_int, [C.c_int, C.c_char_p, C.c_size_t]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
         f.restype = res
         f.argtypes = args
+    # the library's Verilog-A models must be the ones the host registry assigns ids to
+    from . import va
+    names = []
+    buf = C.create_string_buffer(256)
+    for k in range(lib.cedar_va_count()):
+        check(lib.cedar_va_name(k, buf, 256))
+        names.append(buf.value.decode())
+    want = [m.name for m in va.models()]
+    if names != want:
+        raise RuntimeError(f"{LIB_PATH} holds Verilog-A models {names}, the sources define {want}: rebuild it")
     _lib = lib
     return lib
 

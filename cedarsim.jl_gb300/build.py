@@ -17,10 +17,11 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = BUILD / "libcedar_gpu.so"
 INCLUDE = PKG.parent / "include"
+GEN = BUILD / "gen"            # generated Verilog-A device code (va_models.gen.h)
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
-              "--expt-relaxed-constexpr", "-I", str(INCLUDE)]
+              "--expt-relaxed-constexpr", "-I", str(INCLUDE), "-I", str(CSRC), "-I", str(GEN)]
 LANES = (1, 2, 4, 8, 16, 32)
 # (source, object, extra flags): the batched and adjoint kernels are compiled once
 # per lanes-per-instance value so the instantiations build in parallel
@@ -42,10 +43,21 @@ def _stale() -> bool:
         return True
     t = LIB.stat().st_mtime
     deps = list(CSRC.glob("*")) + list(INCLUDE.glob("*.h")) + [pathlib.Path(__file__)]
+    if (GEN / "va_models.gen.h").exists():
+        deps.append(GEN / "va_models.gen.h")
+    else:
+        return True
     return any(d.stat().st_mtime > t for d in deps)
 
 
+def generate() -> pathlib.Path:
+    """Emit the Verilog-A models' device code (rewritten only when it changes)."""
+    from . import va
+    return va.generate(GEN)
+
+
 def build(force: bool = False, verbose: bool = False) -> pathlib.Path:
+    generate()
     if not force and not _stale():
         return LIB
     BUILD.mkdir(parents=True, exist_ok=True)

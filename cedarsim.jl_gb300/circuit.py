@@ -31,6 +31,21 @@ HAS_BRANCH = {L, V, E}
 GROUND = {"0", "gnd", "GND", "ground"}
 
 WAVE_DC, WAVE_PULSE, WAVE_PWL, WAVE_SIN = 0, 1, 2, 3
+VA_BASE = 11   # CEDAR_NMODELS: ids of the compiled Verilog-A models start here
+
+
+def model_nterm(model: int) -> int:
+    if model >= VA_BASE:
+        from . import va
+        return va.model(model).nterm
+    return NTERM[model]
+
+
+def model_npar(model: int) -> int:
+    if model >= VA_BASE:
+        from . import va
+        return va.model(model).npar
+    return NPAR[model]
 
 
 @dataclass
@@ -222,6 +237,17 @@ class Circuit:
     def nlvcr(self, name, d, g, s, R=1.0, m=1.0):
         return self._add(name, NLVCR, [d, g, s], [R, m])
 
+    def va(self, name, model: str, terms: Sequence[str], m: float = 1.0, **params):
+        """An instance of a compiled Verilog-A module (cedarsim.jl_gb300/va):
+        terminals in port order, parameters by name (defaults from the module's
+        declarations, ranges checked), multiplicity m."""
+        from . import va
+        mid = va.model_id(model)
+        mod = va.model(mid)
+        if len(terms) != mod.nterm:
+            raise ValueError(f"{model} has ports {mod.ports}, got {len(terms)} terminals")
+        return self._add(name, mid, list(terms), mod.defaults(params) + [float(m)])
+
     # ---- flattening
     def flatten(self) -> Flat:
         n_nodes = len(self.node_names)
@@ -236,7 +262,7 @@ class Circuit:
         devices: Dict[str, Tuple[int, int]] = {}
         for model in sorted({d.model for d in self.devices}):
             devs = [d for d in self.devices if d.model == model]
-            nt, npar = NTERM[model], NPAR[model]
+            nt, npar = model_nterm(model), model_npar(model)
             term = np.array([[self._node_index.get(t, -1) if t not in GROUND else -1 for t in d.terms] for d in devs],
                             dtype=np.int32).reshape(len(devs), nt)
             br = np.array([branch_of[d.name] for d in devs], dtype=np.int32) if model in HAS_BRANCH else None

@@ -111,12 +111,12 @@ int upload_template(const cedar_ckt_desc *desc, std::unique_ptr<DevTemplate> &ou
   size_t o_lu_rowptr = P.vec(H.lu_rowptr), o_lu_colidx = P.vec(H.lu_colidx), o_lu_cptr = P.vec(lu_cptr);
   size_t o_lu_cslot = P.vec(lu_cslot), o_lu_srow = P.vec(lu_srow);
   std::vector<int> mg_grp;
-  int mg_ptr[CEDAR_NMODELS + 1] = {0};
-  for (int m = 0; m < CEDAR_NMODELS; ++m) {
+  int mg_ptr[kNumModels + 1] = {0};
+  for (int m = 0; m < kNumModels; ++m) {
     mg_ptr[m] = (int)mg_grp.size();
     for (size_t g = 0; g < H.groups.size(); ++g) if (H.groups[g].model == m) mg_grp.push_back((int)g);
   }
-  mg_ptr[CEDAR_NMODELS] = (int)mg_grp.size();
+  mg_ptr[kNumModels] = (int)mg_grp.size();
   size_t o_mg_grp = P.vec(mg_grp);
   std::vector<int> eq_of_pos(H.n);
   for (int e = 0; e < H.n; ++e) eq_of_pos[H.eq_pos[e]] = e;
@@ -186,7 +186,7 @@ int upload_template(const cedar_ckt_desc *desc, std::unique_ptr<DevTemplate> &ou
   D.out_q = (const unsigned char *)(b + o_out_q);
   D.lu_rowptr = (const int *)(b + o_lu_rowptr); D.lu_colidx = (const int *)(b + o_lu_colidx);
   D.lu_cptr = (const int *)(b + o_lu_cptr); D.lu_cslot = (const int *)(b + o_lu_cslot); D.lu_srow = (const int *)(b + o_lu_srow);
-  for (int m = 0; m <= CEDAR_NMODELS; ++m) D.mg_ptr[m] = mg_ptr[m];
+  for (int m = 0; m <= kNumModels; ++m) D.mg_ptr[m] = mg_ptr[m];
   D.mg_grp = (const int *)(b + o_mg_grp);
   D.lu_orig = (const int2 *)(b + o_lu_orig);
   D.lu_task = (const int4 *)(b + o_lu_task); D.fw_task = (const int4 *)(b + o_fw_task); D.bw_task = (const int4 *)(b + o_bw_task);
@@ -317,9 +317,15 @@ int cedar_last_error(char *buf, size_t len) {
   return (int)g_err.size();
 }
 int cedar_version(void) { return 10000; }
-int cedar_model_nterm(int m) { return (m > 0 && m < CEDAR_NMODELS) ? model_info(m).nterm : -1; }
-int cedar_model_npar(int m) { return (m > 0 && m < CEDAR_NMODELS) ? model_info(m).npar : -1; }
-int cedar_model_has_branch(int m) { return (m > 0 && m < CEDAR_NMODELS) ? model_info(m).has_br : -1; }
+int cedar_model_nterm(int m) { return (m > 0 && m < kNumModels) ? model_info(m).nterm : -1; }
+int cedar_model_npar(int m) { return (m > 0 && m < kNumModels) ? model_info(m).npar : -1; }
+int cedar_model_has_branch(int m) { return (m > 0 && m < kNumModels) ? model_info(m).has_br : -1; }
+int cedar_va_count(void) { return va::kCount; }
+int cedar_va_name(int k, char *buf, size_t len) {
+  if (k < 0 || k >= va::kCount || !buf || len == 0) return fail(CEDAR_EINVAL, "Verilog-A model index out of range");
+  std::snprintf(buf, len, "%s", va::kName[k]);
+  return CEDAR_OK;
+}
 
 void cedar_tran_opts_default(cedar_tran_opts *o) {
   if (!o) return;
@@ -395,6 +401,8 @@ static int model_flops(int m) {
     case CEDAR_DIODE: return 13;
     case CEDAR_NLVCR: return 10;
   }
+  // Verilog-A: the module's operations, each carried with its terminal partials
+  if (m >= va::kBase && m < kNumModels) return va::kFlops[m - va::kBase] * (1 + va::kNTerm[m - va::kBase]);
   return 0;
 }
 

@@ -39,13 +39,13 @@ __device__ __forceinline__ void for_devices_by_model(const DTpl &T, int rank, un
     // template order without the per-model bookkeeping
     for (int gi = 0; gi < T.n_groups; ++gi) {
       const DGroup gr = T.grp[gi];
-      if (charges_only && gr.model != CEDAR_C && gr.model != CEDAR_L) continue;
+      if (charges_only && !model_has_q(gr.model)) continue;
       const int dbase = gi > 0 ? T.dev_end[gi - 1] : 0;
       for (int i = rank; i < gr.n_inst; i += K) fn(gr, i, dbase + i);
     }
   } else {
-  for (int m = 1; m < CEDAR_NMODELS; ++m) {
-    if (charges_only && m != CEDAR_C && m != CEDAR_L) continue;
+  for (int m = 1; m < kNumModels; ++m) {
+    if (charges_only && !model_has_q(m)) continue;
     const int g0 = T.mg_ptr[m], ng = T.mg_ptr[m + 1] - g0;
     const int ngmax = __reduce_max_sync(mask, ng);
     for (int q = 0; q < ngmax; ++q) {

@@ -17,6 +17,8 @@
 //      grouped into dependency levels so that a thread group runs one level at a
 //      time with no atomics and a fixed summation order (bitwise reproducible).
 #include "compile.h"
+#include <math.h>
+#include "va_models.gen.h"
 #include <algorithm>
 #include <cmath>
 #include <map>
@@ -39,7 +41,22 @@ static const ModelInfo kModels[CEDAR_NMODELS] = {
     {3, 2, 0, 4, 2},   // NLVCR out: mI, m dI/dVd, m dI/dVg, m dI/dVs(neg)  dpar: 2R, m
 };
 
-const ModelInfo &model_info(int model) { return kModels[model]; }
+// Verilog-A models (cedarsim.jl_gb300/va): terminals = ports, raw parameters =
+// module parameters + m, derived = raw + thermal voltage, outputs as emitted
+static const std::vector<ModelInfo> &va_infos() {
+  static const std::vector<ModelInfo> t = [] {
+    std::vector<ModelInfo> v;
+    for (int k = 0; k < va::kCount; ++k) v.push_back({va::kNTerm[k], va::kNPar[k], 0, va::kNOut[k], va::kNDPar[k]});
+    return v;
+  }();
+  return t;
+}
+
+const ModelInfo &model_info(int model) {
+  return model < CEDAR_NMODELS ? kModels[model] : va_infos()[model - va::kBase];
+}
+
+int num_models() { return CEDAR_NMODELS + va::kCount; }
 
 void device_stamps(int model, const int *t, int ob, std::vector<Stamp> &J, std::vector<Stamp> &F,
                    std::vector<Stamp> &Q) {
@@ -87,6 +104,16 @@ void device_stamps(int model, const int *t, int ob, std::vector<Stamp> &J, std::
       j(t[0], t[0], 1, 1); j(t[0], t[1], 2, 1); j(t[0], t[2], 3, 0);
       j(t[2], t[0], 1, 0); j(t[2], t[1], 2, 0); j(t[2], t[2], 3, 1);
       break;
+    default: {  // Verilog-A: the emitted outputs already carry the KCL sign
+      const int k = model - va::kBase;
+      if (k < 0 || k >= va::kCount) break;
+      for (int e = va::kStampPtr[k]; e < va::kStampPtr[k + 1]; ++e) {
+        const int *st = va::kStamps + 4 * e;  // kind, row port, column port, output
+        if (st[0] == 0) f(t[st[1]], st[3], 0);
+        else if (st[0] == 2) q(t[st[1]], st[3], 0);
+        else j(t[st[1]], t[st[2]], st[3], 0);
+      }
+    } break;
   }
 }
 
@@ -107,6 +134,12 @@ static int32_t enc(const Stamp &s) { return (s.out << 1) | (s.neg ? 1 : 0); }
 // Outputs that hold cj * dQ/dV (the C part of J = G + cj C): capacitor out 1,
 // inductor out 4 (see eval_device).
 static bool is_charge_partial(int model, int local_out) {
+  if (model >= va::kBase) {  // Verilog-A: stamps of kind 3 (cj dQ/dV)
+    const int k = model - va::kBase;
+    for (int e = va::kStampPtr[k]; e < va::kStampPtr[k + 1]; ++e)
+      if (va::kStamps[4 * e] == 3 && va::kStamps[4 * e + 3] == local_out) return true;
+    return false;
+  }
   return (model == CEDAR_C && local_out == 1) || (model == CEDAR_L && local_out == 4);
 }
 
@@ -280,9 +313,9 @@ static bool compile_with(const cedar_ckt_desc *d, Template &T, std::string &err,
   int term_off = 0, par_off = 0, dpar_off = 0, out_off = 0;
   for (int g = 0; g < d->n_groups; ++g) {
     const cedar_devgroup &s = d->groups[g];
-    if (s.model <= 0 || s.model >= CEDAR_NMODELS) { err = "unknown model id " + std::to_string(s.model); return false; }
+    if (s.model <= 0 || s.model >= num_models()) { err = "unknown model id " + std::to_string(s.model); return false; }
     if (s.n_inst < 0) { err = "negative instance count"; return false; }
-    const ModelInfo &mi = kModels[s.model];
+    const ModelInfo &mi = model_info(s.model);
     if (s.n_inst > 0 && (!s.term || !s.par || (mi.has_br && !s.branch))) { err = "group missing arrays"; return false; }
     GroupInfo gi{};
     gi.model = s.model; gi.n_inst = s.n_inst; gi.ntx = mi.nterm + mi.has_br;
@@ -319,7 +352,7 @@ static bool compile_with(const cedar_ckt_desc *d, Template &T, std::string &err,
   T.par_size = par_off; T.dpar_size = dpar_off; T.n_out = out_off;
   T.out_q.assign(std::max(out_off, 1), 0);
   for (const GroupInfo &g : T.groups) {
-    const int no = kModels[g.model].nout;
+    const int no = model_info(g.model).nout;
     for (int i = 0; i < g.n_inst; ++i)
       for (int k = 0; k < no; ++k) T.out_q[g.out_off + i * no + k] = is_charge_partial(g.model, k) ? 1 : 0;
   }
@@ -329,7 +362,7 @@ static bool compile_with(const cedar_ckt_desc *d, Template &T, std::string &err,
   std::vector<char> SJq;
   T.adj_goff.clear(); T.n_adj = 0;
   for (const GroupInfo &g : T.groups) {
-    const ModelInfo &mi = kModels[g.model];
+    const ModelInfo &mi = model_info(g.model);
     for (int i = 0; i < g.n_inst; ++i) {
       const int ob = g.out_off + i * mi.nout;
       size_t before = SJ.size();

@@ -17,6 +17,8 @@ struct ModelInfo {
   int ndpar;     // derived parameters
 };
 const ModelInfo &model_info(int model);
+// number of model ids (built-in models, then the compiled Verilog-A models)
+int num_models();
 
 // One stamp: contribution of output `out` (sign -1/+1) of a device to
 // J[row_eq][col_unknown] (col >= 0) or to a residual/charge row (col = -1).

@@ -48,7 +48,7 @@ struct DTpl {
   // the first gradient index of each group (-1: no differentiable parameter)
   int tf_nlev, tb_nlev, n_adj, pad_adj;
   // groups by model: mg_grp[mg_ptr[m] .. mg_ptr[m + 1]) are the groups of model m
-  int mg_ptr[CEDAR_NMODELS + 1];
+  int mg_ptr[kNumModels + 1];
   const int *mg_grp;
   // original (equation, unknown) of every LU slot, for the dense DC fallback
   const int2 *lu_orig;
@@ -385,7 +385,7 @@ struct Engine {
       int gi = 0;
       while (d >= T.dev_end[gi]) ++gi;
       const DGroup gr = T.grp[gi];
-      if (q_only && gr.model != CEDAR_C && gr.model != CEDAR_L) continue;
+      if (q_only && !model_has_q(gr.model)) continue;
       int i = d - (gi ? T.dev_end[gi - 1] : 0);
       const int *tm = T.term + gr.term_off + i * gr.ntx;
       double v[5];

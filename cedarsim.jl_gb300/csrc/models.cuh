@@ -21,6 +21,9 @@
 #include <cmath>
 #endif
 #include "../../include/cedar.h"
+// Verilog-A models compiled by cedarsim.jl_gb300/va (the build writes this
+// header into its own directory and puts it on the include path)
+#include "va_models.gen.h"
 
 namespace cedar {
 
@@ -29,8 +32,15 @@ namespace cedar {
 CEDAR_HD int model_nout(int m) {
   switch (m) { case 1: return 2; case 2: return 3; case 3: return 6; case 4: return 4; case 5: return 1;
                case 6: return 5; case 7: return 2; case 8: return 4; case 9: return 2; case 10: return 4; }
-  return 0;
+  return va::nout(m - va::kBase);
 }
+
+// built-in models followed by the Verilog-A models (ids CEDAR_NMODELS ...)
+static_assert(va::kBase == CEDAR_NMODELS, "Verilog-A model ids must follow the built-in ones");
+constexpr int kNumModels = CEDAR_NMODELS + va::kCount;
+
+// models whose devices carry charges (evaluated again for the integrator history)
+CEDAR_HD bool model_has_q(int m) { return m == CEDAR_C || m == CEDAR_L || va::has_q(m - va::kBase); }
 
 // thermal voltage k T / q at temperature temp_c (Celsius), $temperature = T+273.15
 CEDAR_HD double thermal_voltage(double temp_c) {
@@ -52,6 +62,7 @@ CEDAR_HD void derive_one(int model, const double *raw, int rs, double *dp, int d
     } break;
     case CEDAR_DIODE: dp[0] = raw[0] * raw[2 * rs]; dp[ds] = 1.0 / (raw[rs] * vt); dp[2 * ds] = raw[3 * rs]; break;
     case CEDAR_NLVCR: dp[0] = 2.0 * raw[0]; dp[ds] = raw[rs]; break;
+    default: va::derive(model - va::kBase, raw, rs, dp, ds, vt); break;
   }
 }
 
@@ -223,6 +234,9 @@ CEDAR_HD void eval_device(int model, const double *dp, int ds, const double *v, 
       double vgs = v[1] - v[2], vds = v[0] - v[2];
       out[0] = m * (vds * (tR * vgs)); out[1] = m * (tR * vgs); out[2] = m * (tR * vds); out[3] = m * (tR * (vgs + vds));
     } break;
+    default:  // Verilog-A models
+      va::eval(model - va::kBase, dp, ds, v, vd, ctx.xdot, ctx.cj, ctx.gmin, out);
+      break;
   }
 }
 

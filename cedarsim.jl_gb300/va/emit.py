@@ -1,0 +1,624 @@
+"""Verilog-A to CUDA/C++ device-code emitter.
+
+For every module the emitter writes
+  * body_<m><D>(P, ps, ctx, V, Fi, Fq): the analog block over dual numbers D
+    (cedar::va::Dual, csrc/va_dual.cuh), accumulating each port's KCL residual
+    from I(a,b) <+ contributions: the resistive part into Fi, the ddt() part (a
+    charge) into Fq.  A branch current flowing a -> b adds -I to KCL(a) and +I to
+    KCL(b) (src/simulate_ir.jl:54,112-120, contribution lowering of
+    src/vasim.jl:128-180);
+  * eval_<m>(...): the per-device outputs the GPU engine stamps, only for the
+    structurally nonzero Jacobian entries found by a dependency analysis;
+  * full_<m>(...): dense residuals and Jacobians of one device (the oracle's
+    entry point);
+  * dispatch functions over the model index and a stamp table for the host
+    compiler.
+Parameters are the module's parameters in declaration order followed by the
+multiplicity m; the derived block appends the thermal voltage.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+from typing import Dict, FrozenSet, List, Optional, Set, Tuple
+
+from .parser import (Assign, Bin, Call, Cond, Contrib, If, Module, Name, Num, Param, Probe, SysCall, Unary,
+                     VAError)
+
+MAX_PORTS = 5   # the engines stage at most 5 terminal values per device
+
+FUNCS = {  # VA name -> (C++ name, arity)
+    "exp": ("exp", 1), "ln": ("log", 1), "log": ("log10", 1), "sqrt": ("sqrt", 1), "pow": ("pow", 2),
+    "abs": ("fabs", 1), "min": ("vmin", 2), "max": ("vmax", 2), "tanh": ("tanh", 1), "sinh": ("sinh", 1),
+    "cosh": ("cosh", 1), "sin": ("sin", 1), "cos": ("cos", 1), "tan": ("tan", 1), "atan": ("atan", 1),
+    "atan2": ("atan2", 2), "asin": ("asin", 1), "acos": ("acos", 1), "hypot": ("hypot", 2),
+    "floor": ("floor", 1), "ceil": ("ceil", 1), "limexp": ("limexp", 1),
+}
+P_Q, P_K = 1.602176634e-19, 1.380649e-23
+
+
+@dataclasses.dataclass
+class VAModel:
+    name: str
+    module: Module
+    ports: List[str]
+    params: List[Param]
+    second_order: bool
+    frows: List[int]
+    gents: List[Tuple[int, int]]
+    qrows: List[int]
+    cents: List[Tuple[int, int]]
+    flops: int
+
+    @property
+    def nterm(self) -> int:
+        return len(self.ports)
+
+    @property
+    def npar(self) -> int:          # raw: parameters + m
+        return len(self.params) + 1
+
+    @property
+    def ndpar(self) -> int:         # derived: raw + vt
+        return len(self.params) + 2
+
+    @property
+    def nout(self) -> int:
+        return len(self.frows) + len(self.gents) + len(self.qrows) + len(self.cents)
+
+    def param_index(self, name: str) -> int:
+        for k, p in enumerate(self.params):
+            if p.name == name:
+                return k
+        raise KeyError(name)
+
+    def defaults(self, overrides: Optional[Dict[str, float]] = None) -> List[float]:
+        """Parameter values with defaults evaluated in declaration order (a default
+        may use earlier parameters); integer parameters rounded half away from zero."""
+        overrides = dict(overrides or {})
+        known = {p.name for p in self.params}
+        bad = set(overrides) - known
+        if bad:
+            raise VAError(f"{self.name}: unknown parameters {sorted(bad)}")
+        env: Dict[str, float] = {}
+        for p in self.params:
+            v = float(overrides[p.name]) if p.name in overrides else float(const_eval(p.default, env))
+            if p.type == "integer":
+                v = float(math.floor(abs(v) + 0.5) * (1 if v >= 0 else -1))
+            check_range(self.name, p, v, env)
+            env[p.name] = v
+        return [env[p.name] for p in self.params]
+
+
+# ------------------------------------------------------------ host evaluation
+def const_eval(e, env: Dict[str, float]) -> float:
+    """Evaluate a parameter expression (numbers, earlier parameters, arithmetic,
+    the math functions) on the host."""
+    if isinstance(e, Num):
+        return e.v
+    if isinstance(e, Name):
+        if e.id not in env:
+            raise VAError(f"line {e.line}: {e.id!r} is not a parameter defined before its use")
+        return env[e.id]
+    if isinstance(e, Unary):
+        x = const_eval(e.x, env)
+        return -x if e.op == "-" else float(x == 0.0)
+    if isinstance(e, Bin):
+        a, b = const_eval(e.a, env), const_eval(e.b, env)
+        ops = {"+": lambda: a + b, "-": lambda: a - b, "*": lambda: a * b,
+               "/": lambda: (math.trunc(a / b) if _is_int_const(e.a) and _is_int_const(e.b) else a / b),
+               "**": lambda: a ** b, "<": lambda: float(a < b), ">": lambda: float(a > b),
+               "<=": lambda: float(a <= b), ">=": lambda: float(a >= b), "==": lambda: float(a == b),
+               "!=": lambda: float(a != b), "&&": lambda: float(a != 0 and b != 0),
+               "||": lambda: float(a != 0 or b != 0)}
+        return float(ops[e.op]())
+    if isinstance(e, Cond):
+        return const_eval(e.a, env) if const_eval(e.c, env) != 0 else const_eval(e.b, env)
+    if isinstance(e, Call) and e.fn in FUNCS:
+        args = [const_eval(a, env) for a in e.args]
+        py = {"exp": math.exp, "ln": math.log, "log": math.log10, "sqrt": math.sqrt, "pow": math.pow,
+              "abs": abs, "min": min, "max": max, "tanh": math.tanh, "sinh": math.sinh, "cosh": math.cosh,
+              "sin": math.sin, "cos": math.cos, "tan": math.tan, "atan": math.atan, "atan2": math.atan2,
+              "asin": math.asin, "acos": math.acos, "hypot": math.hypot, "floor": math.floor, "ceil": math.ceil,
+              "limexp": math.exp}[e.fn]
+        return float(py(*args))
+    raise VAError(f"unsupported expression in a parameter default: {e}")
+
+
+def _is_int_const(e) -> bool:
+    return isinstance(e, Num) and e.is_int
+
+
+def check_range(model: str, p: Param, v: float, env: Dict[str, float]):
+    """`from` / `exclude` ranges of a parameter declaration."""
+    for r in p.ranges:
+        if len(r) == 2:
+            kind, x = r
+            inside = v == const_eval(x, env)
+        else:
+            kind, lo, hi, li, hi_i = r
+            lo_v = -math.inf if _is_inf(lo) else const_eval(lo, env)
+            hi_v = math.inf if _is_inf(hi) else const_eval(hi, env)
+            inside = (v > lo_v or (li and v == lo_v)) and (v < hi_v or (hi_i and v == hi_v))
+        if (kind == "from" and not inside) or (kind == "exclude" and inside):
+            raise VAError(f"{model}: parameter {p.name} = {v} violates its `{kind}` range")
+
+
+def _is_inf(e) -> bool:
+    return isinstance(e, Name) and e.id == "inf" or (isinstance(e, Unary) and _is_inf(e.x))
+
+
+# ------------------------------------------------------------------ analysis
+class _Analysis:
+    def __init__(self, mod: Module):
+        self.mod = mod
+        self.port = {p: k for k, p in enumerate(mod.ports)}
+        self.params = {p.name for p in mod.params}
+        self.vars = dict(mod.variables)
+        self.var_deps: Dict[str, FrozenSet[int]] = {v: frozenset() for v in self.vars}
+        self.second_order = False
+        self.contribs: List[Tuple[Contrib, Optional[object], List[Tuple[int, object]]]] = []
+
+    def port_index(self, n: str, line: int) -> int:
+        if n not in self.port:
+            raise VAError(f"{self.mod.name}: line {line}: {n!r} is not a port")
+        return self.port[n]
+
+    def deps(self, e) -> FrozenSet[int]:
+        if isinstance(e, Num) or isinstance(e, SysCall):
+            return frozenset()
+        if isinstance(e, Name):
+            if e.id in self.params:
+                return frozenset()
+            if e.id in self.vars:
+                return self.var_deps[e.id]
+            raise VAError(f"{self.mod.name}: line {e.line}: undeclared name {e.id!r}")
+        if isinstance(e, Probe):
+            s = {self.port_index(e.a, 0)}
+            if e.b is not None:
+                s.add(self.port_index(e.b, 0))
+            return frozenset(s)
+        if isinstance(e, Unary):
+            return self.deps(e.x) if e.op == "-" else frozenset()
+        if isinstance(e, Bin):
+            if e.op in ("+", "-", "*", "/", "**"):
+                return self.deps(e.a) | self.deps(e.b)
+            return frozenset()       # comparisons and logic are piecewise constant
+        if isinstance(e, Cond):
+            return self.deps(e.a) | self.deps(e.b)
+        if isinstance(e, Call):
+            if e.fn == "ddx":
+                self.second_order = True
+                return self.deps(e.args[0])
+            if e.fn == "ddt":
+                return self.deps(e.args[0])
+            if e.fn in ("floor", "ceil"):
+                return frozenset()
+            out = frozenset()
+            for a in e.args:
+                out |= self.deps(a)
+            return out
+        raise VAError(f"{self.mod.name}: unsupported expression {e!r}")
+
+    def walk(self, stmts, collect: bool):
+        for s in stmts:
+            if isinstance(s, Assign):
+                if s.name in self.params:
+                    raise VAError(f"{self.mod.name}: line {s.line}: assignment to parameter {s.name!r}")
+                if s.name not in self.vars:
+                    raise VAError(f"{self.mod.name}: line {s.line}: assignment to undeclared {s.name!r}")
+                d = self.deps(s.expr) if self.vars[s.name] == "real" else frozenset()
+                self.var_deps[s.name] = self.var_deps[s.name] | d
+            elif isinstance(s, If):
+                self.deps(s.c)
+                self.walk(s.then, collect)
+                self.walk(s.other, collect)
+            elif isinstance(s, Contrib):
+                self.port_index(s.a, s.line)
+                if s.b is not None:
+                    self.port_index(s.b, s.line)
+                if collect:
+                    res, charges = split_ddt(s.expr, s.line)
+                    self.contribs.append((s, res, charges))
+                self.deps(s.expr)
+
+    def run(self):
+        # dependency sets of variables to a fixed point (flow-insensitive)
+        for _ in range(len(self.vars) + 2):
+            before = dict(self.var_deps)
+            self.walk(self.mod.body, collect=False)
+            if before == self.var_deps:
+                break
+        self.walk(self.mod.body, collect=True)
+
+
+def split_ddt(e, line: int):
+    """Split a contribution into its resistive part and its ddt() terms, which
+    must be additive (optionally negated): expr = res + sum(sign * ddt(q))."""
+    terms: List[Tuple[int, object]] = []
+
+    def rec(x, sign):
+        if isinstance(x, Bin) and x.op in ("+", "-"):
+            rec(x.a, sign)
+            rec(x.b, sign if x.op == "+" else -sign)
+        elif isinstance(x, Unary) and x.op == "-":
+            rec(x.x, -sign)
+        else:
+            terms.append((sign, x))
+    rec(e, 1)
+    res = None
+    charges = []
+    for sign, t in terms:
+        if isinstance(t, Call) and t.fn == "ddt":
+            if len(t.args) != 1 or _has_ddt(t.args[0]):
+                raise VAError(f"line {line}: ddt() takes one argument without ddt()")
+            charges.append((sign, t.args[0]))
+        else:
+            if _has_ddt(t):
+                raise VAError(f"line {line}: ddt() must be an additive term of a contribution")
+            tt = t if sign > 0 else Unary("-", t)
+            res = tt if res is None else Bin("+", res, tt)
+    return res, charges
+
+
+def _has_ddt(e) -> bool:
+    if isinstance(e, Call):
+        return e.fn == "ddt" or any(_has_ddt(a) for a in e.args)
+    if isinstance(e, Unary):
+        return _has_ddt(e.x)
+    if isinstance(e, Bin):
+        return _has_ddt(e.a) or _has_ddt(e.b)
+    if isinstance(e, Cond):
+        return _has_ddt(e.c) or _has_ddt(e.a) or _has_ddt(e.b)
+    return False
+
+
+def analyze(mod: Module) -> Tuple[VAModel, _Analysis]:
+    if not mod.ports:
+        raise VAError(f"{mod.name}: a device needs ports")
+    if len(mod.ports) > MAX_PORTS:
+        raise VAError(f"{mod.name}: {len(mod.ports)} ports (at most {MAX_PORTS})")
+    names = [p.name for p in mod.params]
+    if len(set(names)) != len(names):
+        raise VAError(f"{mod.name}: duplicate parameter names")
+    for v in mod.variables:
+        if v in names:
+            raise VAError(f"{mod.name}: {v!r} is both a parameter and a variable")
+    a = _Analysis(mod)
+    a.run()
+    frows: Set[int] = set()
+    qrows: Set[int] = set()
+    gents: Set[Tuple[int, int]] = set()
+    cents: Set[Tuple[int, int]] = set()
+    for c, res, charges in a.contribs:
+        rows = [a.port[c.a]] + ([a.port[c.b]] if c.b is not None else [])
+        frows.update(rows)
+        if res is not None:
+            d = a.deps(res)
+            gents.update((r, k) for r in rows for k in d)
+        if charges:
+            qrows.update(rows)
+            d = frozenset()
+            for _, q in charges:
+                d |= a.deps(q)
+            cents.update((r, k) for r in rows for k in d)
+    flops = _count_flops(mod.body)
+    m = VAModel(mod.name, mod, list(mod.ports), list(mod.params), a.second_order, sorted(frows), sorted(gents),
+                sorted(qrows), sorted(cents), flops)
+    if m.nout == 0:
+        raise VAError(f"{mod.name}: the analog block makes no contribution")
+    m.defaults()  # defaults must evaluate and satisfy their ranges
+    return m, a
+
+
+def _count_flops(stmts) -> int:
+    n = 0
+
+    def ex(e):
+        nonlocal n
+        if isinstance(e, Bin):
+            n += 1
+            ex(e.a)
+            ex(e.b)
+        elif isinstance(e, Unary):
+            n += 1
+            ex(e.x)
+        elif isinstance(e, Cond):
+            ex(e.c)
+            ex(e.a)
+            ex(e.b)
+        elif isinstance(e, Call):
+            n += 1
+            for x in e.args:
+                ex(x)
+        elif isinstance(e, Probe):
+            n += 1 if e.b is not None else 0
+
+    def st(ss):
+        for s in ss:
+            if isinstance(s, (Assign, Contrib)):
+                ex(s.expr)
+            elif isinstance(s, If):
+                ex(s.c)
+                st(s.then)
+                st(s.other)
+    st(stmts)
+    return n
+
+
+# ------------------------------------------------------------------ C++ code
+def _lit(v: float) -> str:
+    r = repr(float(v))
+    return r if any(ch in r for ch in ".einf") else r + ".0"
+
+
+class _Emitter:
+    def __init__(self, m: VAModel, a: _Analysis):
+        self.m = m
+        self.a = a
+
+    def is_int(self, e) -> bool:
+        if isinstance(e, Num):
+            return e.is_int
+        if isinstance(e, Name):
+            if e.id in self.a.params:
+                return next(p for p in self.m.params if p.name == e.id).type == "integer"
+            return self.a.vars.get(e.id) == "integer"
+        if isinstance(e, Unary):
+            return e.op == "!" or self.is_int(e.x)
+        if isinstance(e, Bin):
+            if e.op in ("+", "-", "*", "/"):
+                return self.is_int(e.a) and self.is_int(e.b)
+            return e.op != "**"
+        if isinstance(e, Cond):
+            return self.is_int(e.a) and self.is_int(e.b)
+        return False
+
+    def x(self, e) -> str:
+        if isinstance(e, Num):
+            return _lit(e.v)
+        if isinstance(e, Name):
+            return ("p_" if e.id in self.a.params else "v_") + e.id
+        if isinstance(e, Probe):
+            ia = self.a.port[e.a]
+            if e.b is None:
+                return f"V[{ia}]"
+            return f"(V[{ia}] - V[{self.a.port[e.b]}])"
+        if isinstance(e, Unary):
+            if e.op == "-":
+                return f"(-{self.x(e.x)})"
+            return f"((val({self.x(e.x)}) == 0.0) ? 1.0 : 0.0)"
+        if isinstance(e, Bin):
+            a, b = self.x(e.a), self.x(e.b)
+            if e.op in ("+", "-", "*"):
+                return f"({a} {e.op} {b})"
+            if e.op == "/":
+                if self.is_int(e.a) and self.is_int(e.b):
+                    return f"vidiv(val({a}), val({b}))"
+                return f"({a} / {b})"
+            if e.op == "**":
+                return f"pow({a}, {b})"
+            if e.op in ("&&", "||"):
+                return f"((val({a}) != 0.0 {e.op} val({b}) != 0.0) ? 1.0 : 0.0)"
+            return f"((val({a}) {e.op} val({b})) ? 1.0 : 0.0)"
+        if isinstance(e, Cond):
+            return f"vsel(val({self.x(e.c)}) != 0.0, {self.x(e.a)}, {self.x(e.b)})"
+        if isinstance(e, Call):
+            if e.fn == "ddt":
+                raise VAError(f"{self.m.name}: line {e.line}: ddt() outside an additive contribution term")
+            if e.fn == "ddx":
+                if len(e.args) != 2 or not isinstance(e.args[1], Probe):
+                    raise VAError(f"{self.m.name}: line {e.line}: ddx(expr, V(node)) expected")
+                p = e.args[1]
+                inner = self.x(e.args[0])
+                ia = self.a.port[p.a]
+                if p.b is None:
+                    return f"ddx({inner}, {ia})"
+                # two-node probe: the mean of the two one-sided partials, as
+                # CedarSim defines it (src/vasim.jl:400-411)
+                return f"((ddx({inner}, {ia}) - ddx({inner}, {self.a.port[p.b]})) * 0.5)"
+            if e.fn not in FUNCS:
+                raise VAError(f"{self.m.name}: line {e.line}: unsupported function {e.fn}()")
+            cname, ar = FUNCS[e.fn]
+            if len(e.args) != ar:
+                raise VAError(f"{self.m.name}: line {e.line}: {e.fn}() takes {ar} argument(s)")
+            return f"{cname}({', '.join(self.x(a) for a in e.args)})"
+        if isinstance(e, SysCall):
+            if e.name == "$vt":
+                if e.args:
+                    return f"({_lit(P_K)} * val({self.x(e.args[0])}) / {_lit(P_Q)})"
+                return "c.vt"
+            if e.name == "$temperature":
+                return "c.temp"
+            if e.name == "$mfactor":
+                return "c.m"
+            if e.name == "$simparam":
+                if not e.args or not isinstance(e.args[0], str):
+                    raise VAError(f"{self.m.name}: $simparam needs a name")
+                if e.args[0] == "gmin":
+                    return "c.gmin"
+                if len(e.args) > 1:
+                    return self.x(e.args[1])
+                raise VAError(f"{self.m.name}: $simparam(\"{e.args[0]}\") has no value here and no default")
+        raise VAError(f"{self.m.name}: unsupported expression {e!r}")
+
+    def stmts(self, ss, ind: str) -> List[str]:
+        out = []
+        for s in ss:
+            if isinstance(s, Assign):
+                if self.a.vars[s.name] == "integer":
+                    out.append(f"{ind}v_{s.name} = vint(val({self.x(s.expr)}));")
+                else:
+                    out.append(f"{ind}v_{s.name} = {self.x(s.expr)};")
+            elif isinstance(s, If):
+                out.append(f"{ind}if (val({self.x(s.c)}) != 0.0) {{")
+                out += self.stmts(s.then, ind + "  ")
+                if s.other:
+                    out.append(f"{ind}}} else {{")
+                    out += self.stmts(s.other, ind + "  ")
+                out.append(f"{ind}}}")
+            elif isinstance(s, Contrib):
+                res, charges = split_ddt(s.expr, s.line)
+                ia = self.a.port[s.a]
+                ib = None if s.b is None else self.a.port[s.b]
+                if res is not None:
+                    out.append(f"{ind}{{ const D i_ = {self.x(res)};")
+                    out.append(f"{ind}  Fi[{ia}] -= i_;" + (f" Fi[{ib}] += i_;" if ib is not None else "") + " }")
+                if charges:
+                    q = " + ".join(("" if sg > 0 else "-") + f"D({self.x(t)})" for sg, t in charges)
+                    out.append(f"{ind}{{ const D q_ = {q};")
+                    out.append(f"{ind}  Fq[{ia}] -= q_;" + (f" Fq[{ib}] += q_;" if ib is not None else "") + " }")
+        return out
+
+    def body(self) -> str:
+        m = self.m
+        L = [f"// module {m.name}({', '.join(m.ports)})",
+             "template <class D>",
+             f"VA_HD void body_{m.name}(const double *P, int ps, const Ctx &c, const D *V, D *Fi, D *Fq) {{"]
+        for k, p in enumerate(m.params):
+            L.append(f"  const double p_{p.name} = P[{k} * ps];")
+        for v, t in m.module.variables.items():
+            L.append(f"  D v_{v}(0.0);" if t == "real" else f"  double v_{v} = 0.0;")
+        L += self.stmts(m.module.body, "  ")
+        L.append("  (void)c; (void)V; (void)Fi; (void)Fq; (void)P; (void)ps;")
+        L.append("}")
+        return "\n".join(L)
+
+    def dtype(self) -> str:
+        n = self.m.nterm
+        return f"Dual<Dual<double, {n}>, {n}>" if self.m.second_order else f"Dual<double, {n}>"
+
+    def prologue(self) -> List[str]:
+        m = self.m
+        P = len(m.params)
+        return [f"  typedef {self.dtype()} D;",
+                "  Ctx c;",
+                f"  c.m = dp[{P} * ds]; c.vt = dp[{P + 1} * ds]; c.temp = c.vt * {_lit(P_Q / P_K)}; c.gmin = gmin;",
+                f"  D V[{m.nterm}], Fi[{m.nterm}], Fq[{m.nterm}];",
+                f"  for (int k = 0; k < {m.nterm}; ++k) V[k] = Seed<D>::make(v[k], k);",
+                f"  body_{m.name}<D>(dp, ds, c, V, Fi, Fq);"]
+
+    def eval(self) -> str:
+        m = self.m
+        L = [f"VA_HD void eval_{m.name}(const double *dp, int ds, const double *v, const double *vd, bool xdot, "
+             f"double cj, double gmin, double *out) {{"]
+        L += self.prologue()
+        L.append("  const double mf = c.m;")
+        o = 0
+        for r in m.frows:
+            if r in m.qrows:
+                qd = " + ".join(f"part(Fq[{r}], {k}) * vd[{k}]" for k in range(m.nterm))
+                L.append(f"  out[{o}] = mf * (val(Fi[{r}]) + (xdot ? ({qd}) : cj * val(Fq[{r}])));")
+            else:
+                L.append(f"  out[{o}] = mf * val(Fi[{r}]);")
+            o += 1
+        for r, k in m.gents:
+            L.append(f"  out[{o}] = mf * part(Fi[{r}], {k});")
+            o += 1
+        for r in m.qrows:
+            L.append(f"  out[{o}] = mf * val(Fq[{r}]);")
+            o += 1
+        for r, k in m.cents:
+            L.append(f"  out[{o}] = cj * (mf * part(Fq[{r}], {k}));")
+            o += 1
+        L.append("  (void)vd; (void)xdot; (void)cj;")
+        L.append("}")
+        return "\n".join(L)
+
+    def full(self) -> str:
+        m = self.m
+        n = m.nterm
+        L = [f"inline void full_{m.name}(const double *dp, int ds, const double *v, double gmin, double *fi, "
+             f"double *fq, double *G, double *C) {{"]
+        L += self.prologue()
+        L.append(f"  for (int r = 0; r < {n}; ++r) {{")
+        L.append("    fi[r] = val(Fi[r]); fq[r] = val(Fq[r]);")
+        L.append(f"    for (int k = 0; k < {n}; ++k) {{ G[r * {n} + k] = part(Fi[r], k); C[r * {n} + k] = part(Fq[r], k); }}")
+        L.append("  }")
+        L.append("}")
+        return "\n".join(L)
+
+
+def emit_header(models: List[Tuple[VAModel, _Analysis]], base_id: int) -> str:
+    """The generated header: per-model code and the dispatch over the model index."""
+    K = len(models)
+    L = ["// Generated by cedarsim.jl_gb300/va/emit.py from Verilog-A sources; do not edit.",
+         "#pragma once",
+         '#include "va_dual.cuh"',
+         "",
+         "namespace cedar {",
+         "namespace va {",
+         "",
+         f"constexpr int kBase = {base_id};       // model id of the first Verilog-A model",
+         f"constexpr int kCount = {K};",
+         "",
+         "struct Ctx { double m, vt, temp, gmin; };",
+         ""]
+    for m, a in models:
+        e = _Emitter(m, a)
+        L += [e.body(), "", e.eval(), "", e.full(), ""]
+
+    def table(name, vals, ctype="int"):
+        vals = list(vals) or [0]
+        return f"static const {ctype} {name}[] = {{{', '.join(str(v) for v in vals)}}};"
+
+    L.append(table("kNTerm", [m.nterm for m, _ in models]))
+    L.append(table("kNPar", [m.npar for m, _ in models]))
+    L.append(table("kNDPar", [m.ndpar for m, _ in models]))
+    L.append(table("kNOut", [m.nout for m, _ in models]))
+    L.append(table("kHasQ", [int(bool(m.qrows)) for m, _ in models]))
+    L.append(table("kFlops", [m.flops for m, _ in models]))
+    names = ", ".join(f'"{m.name}"' for m, _ in models) or '""'
+    L.append(f"static const char *const kName[] = {{{names}}};")
+    # stamps: kind 0 = residual row, 1 = J (resistive), 2 = charge row, 3 = J (charge partial)
+    st, ptr = [], [0]
+    for m, _ in models:
+        o = 0
+        for r in m.frows:
+            st += [0, r, -1, o]; o += 1
+        for r, k in m.gents:
+            st += [1, r, k, o]; o += 1
+        for r in m.qrows:
+            st += [2, r, -1, o]; o += 1
+        for r, k in m.cents:
+            st += [3, r, k, o]; o += 1
+        ptr.append(len(st) // 4)
+    L.append(table("kStamps", st))
+    L.append(table("kStampPtr", ptr))
+    L.append("")
+    # device-side dispatch (switches over a warp-uniform model id)
+    # (the tables above are host data; device code reads switches)
+    def switch(fn, rtype, vals, default):
+        out = [f"VA_HD {rtype} {fn}(int k) {{", "  switch (k) {"]
+        out += [f"    case {i}: return {v};" for i, v in enumerate(vals)]
+        out += ["    default: break;", "  }", f"  return {default};", "}"]
+        return out
+    L += switch("nout", "int", [m.nout for m, _ in models], 0)
+    L += switch("has_q", "bool", ["true" if m.qrows else "false" for m, _ in models], "false")
+    L += switch("npar", "int", [m.npar for m, _ in models], 0)
+    L.append("VA_HD void derive(int k, const double *raw, int rs, double *dp, int ds, double vt) {")
+    L.append("  const int np = npar(k);")
+    L.append("  if (np == 0) return;")
+    L.append("  for (int i = 0; i < np; ++i) dp[i * ds] = raw[i * rs];")
+    L.append("  dp[np * ds] = vt;")
+    L.append("}")
+    L.append("VA_CALL void eval(int k, const double *dp, int ds, const double *v, const double *vd, bool xdot, double cj, "
+             "double gmin, double *out) {")
+    L.append("  switch (k) {")
+    for i, (m, _) in enumerate(models):
+        L.append(f"    case {i}: eval_{m.name}(dp, ds, v, vd, xdot, cj, gmin, out); break;")
+    L.append("    default: break;")
+    L.append("  }")
+    L.append("  (void)dp; (void)ds; (void)v; (void)vd; (void)xdot; (void)cj; (void)gmin; (void)out;")
+    L.append("}")
+    L.append("inline void full(int k, const double *dp, int ds, const double *v, double gmin, double *fi, double *fq, "
+             "double *G, double *C) {")
+    L.append("  switch (k) {")
+    for i, (m, _) in enumerate(models):
+        L.append(f"    case {i}: full_{m.name}(dp, ds, v, gmin, fi, fq, G, C); break;")
+    L.append("    default: break;")
+    L.append("  }")
+    L.append("  (void)dp; (void)ds; (void)v; (void)gmin; (void)fi; (void)fq; (void)G; (void)C;")
+    L.append("}")
+    L += ["", "}  // namespace va", "}  // namespace cedar", ""]
+    return "\n".join(L)

@@ -147,6 +147,15 @@ int cedar_model_nterm(int model);
 int cedar_model_npar(int model);
 int cedar_model_has_branch(int model);
 
+/* Verilog-A device models compiled into this library (the role of
+ * load_VA_model / make_spice_device, src/vasim.jl:663-875).  Model k (0-based,
+ * sorted by module name) has model id CEDAR_NMODELS + k; its parameters are the
+ * module's parameters in declaration order followed by the multiplicity m, and
+ * its terminals are the module's ports in order.  cedar_va_name copies the
+ * module name of model k into buf (CEDAR_EINVAL for k out of range). */
+int cedar_va_count(void);
+int cedar_va_name(int k, char *buf, size_t len);
+
 /* ---- transient / DC options --------------------------------------------- */
 enum { CEDAR_TRAP = 0, CEDAR_BDF2 = 1 };
 

@@ -34,6 +34,12 @@
 #include <omp.h>
 #endif
 #include "../include/cedar.h"
+// Verilog-A models: the device code the product's emitter writes from the .va
+// sources (cedarsim.jl_gb300/va), compiled here for the CPU.  The oracle runs it
+// as a black-box device evaluation; the emitter itself is checked against an
+// independent interpretation of the same sources (oracle/va_interp.py).
+#include <math.h>
+#include "va_models.gen.h"
 
 namespace orc {
 
@@ -79,6 +85,10 @@ struct Circuit {
 static const int kNTerm[CEDAR_NMODELS] = {0, 2, 2, 2, 2, 2, 4, 4, 4, 2, 3};
 static const int kNPar[CEDAR_NMODELS]  = {0, 2, 2, 2, 10, 10, 2, 2, 7, 4, 2};
 static const int kHasBr[CEDAR_NMODELS] = {0, 0, 0, 1, 1, 0, 1, 0, 0, 0, 0};
+static const int kNumModels = CEDAR_NMODELS + cedar::va::kCount;
+static int model_nterm(int m) { return m < CEDAR_NMODELS ? kNTerm[m] : cedar::va::kNTerm[m - CEDAR_NMODELS]; }
+static int model_npar(int m) { return m < CEDAR_NMODELS ? kNPar[m] : cedar::va::kNPar[m - CEDAR_NMODELS]; }
+static int model_hasbr(int m) { return m < CEDAR_NMODELS ? kHasBr[m] : 0; }
 
 static bool load_circuit(const cedar_ckt_desc *d, Circuit &c, std::string &err) {
   if (!d || d->n_nodes < 0 || d->n_branch < 0 || d->n_groups < 0) { err = "bad desc"; return false; }
@@ -87,10 +97,10 @@ static bool load_circuit(const cedar_ckt_desc *d, Circuit &c, std::string &err) 
   if (d->pwl && d->n_pwl > 0) c.pwl.assign(d->pwl, d->pwl + d->n_pwl);
   for (int g = 0; g < d->n_groups; ++g) {
     const cedar_devgroup &s = d->groups[g];
-    if (s.model <= 0 || s.model >= CEDAR_NMODELS || s.n_inst < 0) { err = "bad model"; return false; }
-    Group G; G.model = s.model; G.n_inst = s.n_inst; G.nt = kNTerm[s.model]; G.np = kNPar[s.model];
+    if (s.model <= 0 || s.model >= kNumModels || s.n_inst < 0) { err = "bad model"; return false; }
+    Group G; G.model = s.model; G.n_inst = s.n_inst; G.nt = model_nterm(s.model); G.np = model_npar(s.model);
     G.term.assign(s.term, s.term + (size_t)G.nt * G.n_inst);
-    if (kHasBr[s.model]) {
+    if (model_hasbr(s.model)) {
       if (!s.branch) { err = "missing branch"; return false; }
       G.branch.assign(s.branch, s.branch + G.n_inst);
     }
@@ -304,6 +314,27 @@ static void eval_circuit(const Circuit &c, const double *x, const EvalCtx &ctx, 
           Dual dcd = 2.0 * R * vgs;  // (2R vgs - (-2R vgs))/2
           Dual I = (in[0] - in[2]) * dcd;
           A.add(tm[0], -m * I, false); A.add(tm[2], m * I, false);
+        } break;
+        default: {
+          // Verilog-A model: dense residuals and partials of one device from the
+          // emitted code (derived block = parameters, m, thermal voltage)
+          const int k = g.model - CEDAR_NMODELS, nt = g.nt;
+          double dp[64], v[8], fi[8], fq[8], G[64], Cm[64];
+          for (int q = 0; q < g.np; ++q) dp[q] = g.p(q, i);
+          dp[g.np] = Vt;
+          for (int q = 0; q < nt; ++q) v[q] = X(tm[q]);
+          cedar::va::full(k, dp, 1, v, c.gmin, fi, fq, G, Cm);
+          const double m = g.p(g.np - 1, i);
+          for (int r = 0; r < nt; ++r) {
+            const int row = tm[r];
+            if (row < 0) continue;
+            o.Fi[row] += m * fi[r]; o.Fq[row] += m * fq[r];
+            for (int q = 0; q < nt; ++q) {
+              if (tm[q] < 0) continue;
+              o.G[(size_t)row * o.n + tm[q]] += m * G[r * nt + q];
+              o.C[(size_t)row * o.n + tm[q]] += m * Cm[r * nt + q];
+            }
+          }
         } break;
       }
     }
@@ -982,6 +1013,15 @@ int oracle_replay_phi(const cedar_ckt_desc *d, const cedar_tran_opts *replay_opt
 int oracle_n_params(const cedar_ckt_desc *d) {
   Circuit c; if (!load_circuit(d, c, g_err)) return -1;
   return n_params(c);
+}
+
+// One Verilog-A device through the emitted code: dp = parameters, m, thermal
+// voltage (stride 1); dense fi/fq[nt], G/C[nt*nt] (unscaled by m).
+int oracle_va_full(int k, const double *dp, const double *v, double gmin, double *fi, double *fq, double *G,
+                   double *Cm) {
+  if (k < 0 || k >= cedar::va::kCount) { g_err = "Verilog-A model index out of range"; return -1; }
+  cedar::va::full(k, dp, 1, v, gmin, fi, fq, G, Cm);
+  return 0;
 }
 
 double oracle_next_breakpoint(const cedar_ckt_desc *d, double t, double eps) {

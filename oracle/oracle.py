@@ -21,7 +21,11 @@ _lib = None
 def build(force: bool = False) -> pathlib.Path:
     src = HERE / "oracle.cpp"
     hdr = HERE.parent / "include" / "cedar.h"
-    if force or not LIB.exists() or max(src.stat().st_mtime, hdr.stat().st_mtime) > LIB.stat().st_mtime:
+    gen = HERE.parent / "cedarsim.jl_gb300" / "_build" / "gen" / "va_models.gen.h"
+    if not gen.exists():
+        raise RuntimeError(f"{gen} is missing: build the package first (it emits the Verilog-A device code)")
+    deps = [src, hdr, gen, HERE.parent / "cedarsim.jl_gb300" / "csrc" / "va_dual.cuh"]
+    if force or not LIB.exists() or max(d.stat().st_mtime for d in deps) > LIB.stat().st_mtime:
         subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
     return LIB
 
@@ -62,6 +66,8 @@ def load(pkg):
                                          dp, dp, C.POINTER(C.c_int32), C.c_int]
     lib.oracle_n_params.restype = C.c_int
     lib.oracle_n_params.argtypes = [cd_p]
+    lib.oracle_va_full.restype = C.c_int
+    lib.oracle_va_full.argtypes = [C.c_int, dp, dp, C.c_double, dp, dp, dp, dp]
     lib.oracle_last_error.restype = C.c_int
     lib.oracle_last_error.argtypes = [C.c_char_p, C.c_size_t]
     _lib = lib

@@ -128,3 +128,56 @@ def mixed(pkg):
     c.V("VS", "sn", "0", wave=pkg.Sin(0.2, 0.1, 2e9, 0.05e-9, 1e8, 30.0))
     c.R("RS", "sn", "out1", r=50e3)
     return c
+
+
+# ---------------------------------------------------------------- Verilog-A
+def va_nlvcr(pkg):  # test/ddx.jl with the device compiled from Verilog-A
+    c = pkg.Circuit(); c.V("V1", "vcc", "0", dc=5.0); c.V("V2", "vg", "0", dc=3.0)
+    c.va("R", "va_nlvcr", ["vcc", "vg", "0"], R=2.0)
+    return c
+
+
+def inverter_chain_va(pkg, stages=7, cload=10e-15, builtin=False):
+    """The inverter chain of workload 2 with its MOSFETs as the Verilog-A level-1
+    model (or the built-in one: same nodes, devices and parameter blocks)."""
+    g = pkg.generators
+    p = g.INV
+    c = pkg.Circuit()
+    c.node("in"); c.node("vdd")
+    c.V("VIN", "in", "0", wave=g.INV_PULSE)
+    c.V("VDD", "vdd", "0", dc=p["vdd"])
+    prev = "in"
+    for k in range(1, stages + 1):
+        out = f"out{k}"
+        if builtin:
+            c.mos1(f"MN{k}", out, prev, "0", "0", 1.0, p["wn"], p["ln"], p["kp_n"], p["vth_n"])
+            c.mos1(f"MP{k}", out, prev, "vdd", "vdd", -1.0, p["wp"], p["lp"], p["kp_p"], p["vth_p"])
+        else:
+            c.va(f"MN{k}", "va_mos1", [out, prev, "0", "0"], TYPE=1, W=p["wn"], L=p["ln"], KP=p["kp_n"],
+                 VTO=p["vth_n"])
+            c.va(f"MP{k}", "va_mos1", [out, prev, "vdd", "vdd"], TYPE=-1, W=p["wp"], L=p["lp"], KP=p["kp_p"],
+                 VTO=p["vth_p"])
+        c.C(f"CL{k}", out, "0", cload)
+        prev = out
+    return c
+
+
+def va_mixed(pkg):
+    """Every shipped Verilog-A model (resistive, charge and ddx ones) with
+    built-in sources and devices around them."""
+    c = pkg.Circuit()
+    c.V("VDD", "vdd", "0", dc=1.8)
+    c.V("VIN", "in", "0", wave=pkg.Pulse(0.0, 1.8, 0.1e-9, 50e-12, 60e-12, 0.4e-9, 1e-9))
+    c.va("R1", "va_resistor", ["in", "b"], R=1e3)
+    c.va("C1", "va_capacitor", ["b", "0"], C=20e-15)
+    c.va("D1", "va_diode", ["b", "c"], IS=1e-14, N=1.05)
+    c.va("D2", "va_diode_cj", ["c", "0"], IS=1e-15, N=1.1, TT=2e-11, CJ0=5e-15)
+    c.R("RC", "c", "0", r=20e3)
+    c.va("MN", "va_mos1", ["d", "b", "0", "0"], TYPE=1, W=2e-6, L=1e-6, KP=200e-6, VTO=0.45, LAMBDA=0.02)
+    c.va("MP", "va_mos1", ["d", "b", "vdd", "vdd"], TYPE=-1, W=4e-6, L=1e-6, KP=80e-6, VTO=-0.45, m=2.0)
+    c.va("X1", "va_nlvcr", ["d", "c", "0"], R=1e-4)
+    c.C("CD", "d", "0", 10e-15)
+    c.va("R2", "va_resistor", ["d", "e"], R=5e3, m=2.0)
+    c.mos1("MB", "e", "d", "0", "0", 1.0, 2e-6, 1e-6, 200e-6, 0.45)
+    c.va("C2", "va_capacitor", ["e", "0"], C=3e-15)
+    return c

@@ -1,0 +1,119 @@
+"""Verilog-A models on the GPU against the CPU oracle.
+
+The emitted device code runs inside every engine: the device evaluation of
+cedar_eval, the one-circuit transient, the batched Monte-Carlo kernel and the
+small-signal AC solve.  Tolerances are the parity contract's (device F and J
+within 1e-12 relative; waveforms within reltol 1e-6 / abstol 1e-9 V with the
+same step sequence)."""
+import numpy as np
+import pytest
+
+from tests import circuits as K
+from tests.test_gpu_parity import ABSTOL, RELTOL, RTOL_EVAL, compare_waves, random_state
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    "va_mixed": K.va_mixed,
+    "va_chain_7": lambda pkg: K.inverter_chain_va(pkg, 7),
+    "va_nlvcr": K.va_nlvcr,
+}
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+@pytest.mark.parametrize("t", [0.0, 0.21e-9])
+def test_va_eval_parity(gpu, pkg, oracle, case, t):
+    flat = CASES[case](pkg).flatten()
+    sys = pkg.System(flat)
+    rng = np.random.default_rng(99)
+    for _ in range(4):
+        x = random_state(flat, rng)
+        xd = rng.normal(0, 1e9, flat.n)
+        gamma = 10.0 ** rng.uniform(9, 13)
+        F, Jv = sys.eval(x, xd, t, gamma)
+        Fr, Fi, Fq, G, Cm = oracle.eval(flat, x, xd, t)
+        scale = np.abs(G) @ np.abs(x) + np.abs(Cm) @ np.abs(xd) + np.abs(Fi)
+        assert np.all(np.abs(F - Fr) <= RTOL_EVAL * (np.abs(Fr) + scale) + 1e-300), case
+        J = sys.jac_dense(Jv)
+        Jr = G + gamma * Cm
+        rows = np.abs(G).max(axis=1, keepdims=True) + gamma * np.abs(Cm).max(axis=1, keepdims=True)
+        assert np.all(np.abs(J - Jr) <= RTOL_EVAL * (np.abs(Jr) + 1e-6 * rows) + 1e-300), case
+
+
+def test_va_ddx_known_answer_on_gpu(gpu, pkg):
+    f = K.va_nlvcr(pkg).flatten()
+    x = pkg.dc(f)
+    assert abs(x[f.index("V1.I")] - (-60.0)) <= 8 * np.spacing(60.0)
+
+
+@pytest.mark.parametrize("case", ["va_mixed", "va_chain_7"])
+def test_va_transient_parity(gpu, pkg, oracle, case):
+    flat = CASES[case](pkg).flatten()
+    o = pkg.make_opts("bdf2", True, 0.0, 2e-9, 0.0, True)
+    sol = pkg.tran(flat, (0.0, 2e-9), method="bdf2")
+    t_ref, x_ref, st, rc = oracle.tran(flat, o)
+    assert rc == 0 and sol.retcode == "OK"
+    assert (sol.stats["accepted"], sol.stats["rejected"]) == (st.accepted, st.rejected)
+    assert compare_waves(sol, t_ref, x_ref, flat.n_nodes) <= 1.0
+
+
+def test_va_chain_tracks_builtin_chain(gpu, pkg):
+    """The Verilog-A level-1 MOSFET is the built-in model's equations: the two
+    chains' waveforms agree within the waveform tolerance."""
+    a = K.inverter_chain_va(pkg, 9).flatten()
+    b = K.inverter_chain_va(pkg, 9, builtin=True).flatten()
+    ha = pkg.tran(a, (0.0, 3e-9), method="bdf2", h=1e-12, adaptive=False)
+    hb = pkg.tran(b, (0.0, 3e-9), method="bdf2", h=1e-12, adaptive=False)
+    assert ha.retcode == "OK" and hb.retcode == "OK" and np.array_equal(ha.t, hb.t)
+    err = np.abs(ha.u[:, :a.n_nodes] - hb.u[:, :a.n_nodes]) / (RELTOL * np.abs(hb.u[:, :a.n_nodes]) + ABSTOL)
+    assert err.max() <= 1.0
+
+
+def test_va_batched_monte_carlo(gpu, pkg, oracle):
+    """Batched kernel with Verilog-A chains of two lengths and per-instance
+    parameter blocks (W, KP, VTO, load) against the oracle's batch run."""
+    rng = np.random.default_rng(5)
+    templates = [K.inverter_chain_va(pkg, L).flatten() for L in (3, 6)]
+    itpl = np.array([i % 2 for i in range(24)], np.int32)
+    blocks, off, pos = [], [], 0
+    for i in range(24):
+        f = templates[itpl[i]]
+        b = f.param_block().copy()
+        for gi, (model, term, br, par) in enumerate(f.groups):
+            base = sum(g[3].size for g in f.groups[:gi])
+            n = par.shape[1]
+            if model >= pkg.circuit.VA_BASE:      # va_mos1: W row 1, KP row 3, VTO row 4
+                b[base + 1 * n: base + 2 * n] *= rng.uniform(0.8, 1.2, n)
+                b[base + 3 * n: base + 4 * n] *= np.exp(0.05 * rng.normal(size=n))
+                b[base + 4 * n: base + 5 * n] += 0.03 * rng.normal(size=n) * np.sign(b[base + 4 * n: base + 5 * n])
+            elif model == 2:                          # load capacitors
+                b[base: base + n] = rng.uniform(5e-15, 20e-15)
+        blocks.append(b)
+        off.append(pos)
+        pos += b.size
+    par = np.concatenate(blocks)
+    off = np.array(off, np.int64)
+    probes = np.array([[f.index("out3"), f.index("in")] for f in templates], np.int32)
+    sw = pkg.Batch(templates, itpl, par, off, probes=probes, n_samples=31)
+    o = pkg.make_opts("bdf2", True, 0.0, 1.5e-9, 0.0, True)
+    res = sw.run(o)
+    xf, samp, st = oracle.batch(sw.holder, o)
+    assert np.all(res.stats["status"] == 0) and np.all(st["status"] == 0)
+    for k in ("accepted", "rejected"):
+        assert np.array_equal(res.stats[k], st[k]), k
+    err = np.abs(res.samples - samp) / (RELTOL * np.abs(samp) + ABSTOL)
+    assert err.max() <= 1.0
+
+
+def test_va_ac_parity(gpu, pkg, oracle):
+    """Small-signal AC through Verilog-A charges (diode diffusion + depletion
+    charge, capacitor): G and C split by the emitted charge-partial outputs."""
+    flat = K.va_mixed(pkg).flatten()
+    flat.ac = {"VIN": 1.0}
+    x_op = pkg.dc(flat)
+    w = 2 * np.pi * pkg.acdec(5, 1e6, 1e12)
+    probes = ["b", "c", "d"]
+    r = pkg.ac(flat, x_op=x_op).freqresp(probes, w)
+    ro = oracle.ac(flat, x_op, w, [flat.index(p) for p in probes])
+    err = np.max(np.abs(r - ro) / np.max(np.abs(ro), axis=0, keepdims=True))
+    assert err <= 1e-9

@@ -1,0 +1,250 @@
+"""Verilog-A front end and emitter on the CPU.
+
+* The emitted device code (compiled into the oracle library) against an
+  independent interpretation of the same parsed modules (oracle/va_interp.py)
+  at random port potentials in every operating region.
+* The Verilog-A restatements of the built-in models (R, C, diode, level-1 MOSFET,
+  NLVCR) against the built-in equations, through the oracle's circuit
+  evaluation.
+* Known answers: test/ddx.jl (the NLVCR source current is -60 A) and
+  test/varegress.jl (a resistor written in either orientation carries the same,
+  non-negative current).
+* Parameter defaults, ranges and the errors of the supported subset.
+"""
+import ctypes as C
+import importlib.util
+import pathlib
+
+import numpy as np
+import pytest
+
+from tests import circuits as K
+
+ROOT = pathlib.Path(__file__).resolve().parent.parent
+
+
+@pytest.fixture(scope="module")
+def va(pkg):
+    import importlib
+    return importlib.import_module("cedarsim_gb300.va")
+
+
+@pytest.fixture(scope="module")
+def interp():
+    spec = importlib.util.spec_from_file_location("cedar_va_interp", ROOT / "oracle" / "va_interp.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+VT = 1.380649e-23 * (27.0 + 273.15) / 1.602176634e-19
+
+
+def _params(m, rng):
+    """Random in-range parameter values around the declared defaults."""
+    out = {}
+    for p in m.params:
+        d = m.defaults()[m.param_index(p.name)]
+        if p.name == "TYPE":
+            out[p.name] = float(rng.choice([-1.0, 1.0]))
+        elif p.name in ("VTO",):
+            out[p.name] = float(rng.uniform(-0.6, 0.6))
+        elif p.name in ("LAMBDA", "TT", "CJ0"):
+            out[p.name] = float(rng.choice([0.0, abs(d) + 1e-3 * rng.uniform(0.5, 2.0)])) if p.name == "LAMBDA" \
+                else float(rng.choice([0.0, rng.uniform(1e-15, 1e-11)]))
+        elif p.name == "R":
+            out[p.name] = float(rng.uniform(0.5, 5.0) * (1 if rng.random() < 0.8 else -1))
+        else:
+            out[p.name] = float(d * rng.uniform(0.5, 2.0)) if d else float(rng.uniform(0.5, 2.0))
+    return out
+
+
+def test_emitted_code_matches_interpreter(pkg, oracle, va, interp):
+    rng = np.random.default_rng(42)
+    lib = oracle.lib
+    dp_ = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    for k, m in enumerate(va.models()):
+        n = m.nterm
+        for trial in range(60):
+            prm = _params(m, rng)
+            vals = m.defaults(prm)
+            mult = float(rng.choice([1.0, 2.0]))
+            dp = np.array(vals + [mult, VT])
+            v = rng.uniform(-2.0, 2.0, n)
+            if m.name.startswith("va_diode"):
+                v[0] = v[1] + rng.uniform(-1.0, 0.9)     # keep exp() finite but exercise forward bias
+            fi, fq, G, Cm = np.zeros(n), np.zeros(n), np.zeros(n * n), np.zeros(n * n)
+            assert lib.oracle_va_full(k, dp_(dp), dp_(v), 1e-12, dp_(fi), dp_(fq), dp_(G), dp_(Cm)) == 0
+            ri, rq, rG, rC = interp.evaluate(m.module, dict(zip([p.name for p in m.params], vals)), list(v), VT,
+                                             1e-12, mult)
+            ri, rq, rG, rC = np.array(ri), np.array(rq), np.array(rG).ravel(), np.array(rC).ravel()
+            sc = np.abs(ri).max() + 1e-30
+            assert np.all(np.abs(fi - ri) <= 1e-13 * sc), (m.name, fi, ri)
+            assert np.all(np.abs(fq - rq) <= 1e-13 * (np.abs(rq).max() + 1e-40)), (m.name, fq, rq)
+            gs = np.abs(rG).max() + 1e-30
+            assert np.all(np.abs(G - rG) <= 1e-12 * gs), (m.name, G, rG)
+            cs = np.abs(rC).max() + 1e-40
+            assert np.all(np.abs(Cm - rC) <= 1e-12 * cs), (m.name, Cm, rC)
+
+
+def _builtin_twin(pkg, which):
+    """A circuit with built-in devices and its twin with the Verilog-A models."""
+    def mk(vamodels):
+        c = pkg.Circuit()
+        c.V("VDD", "vdd", "0", dc=1.8)
+        c.V("VIN", "in", "0", dc=0.7)
+        if which == "mos":
+            for k, (d, g, s, typ, W, KP, VTO, lam) in enumerate([("o", "in", "0", 1.0, 2e-6, 2e-4, 0.45, 0.02),
+                                                                  ("o", "in", "vdd", -1.0, 4e-6, 8e-5, -0.45, 0.0),
+                                                                  ("p", "o", "0", 1.0, 3e-6, 2e-4, 0.4, 0.01)]):
+                if vamodels:
+                    c.va(f"M{k}", "va_mos1", [d, g, s, s], TYPE=typ, W=W, L=1e-6, KP=KP, VTO=VTO, LAMBDA=lam,
+                         m=1.0 + k)
+                else:
+                    c.mos1(f"M{k}", d, g, s, s, typ, W, 1e-6, KP, VTO, LAMBDA=lam, m=1.0 + k)
+            c.R("RL", "p", "vdd", r=1e4)
+        elif which == "passive":
+            (c.va("R1", "va_resistor", ["in", "o"], R=1e3, m=3.0) if vamodels else c.R("R1", "in", "o", r=1e3, m=3.0))
+            (c.va("C1", "va_capacitor", ["o", "0"], C=2e-12) if vamodels else c.C("C1", "o", "0", 2e-12))
+            (c.va("D1", "va_diode", ["o", "vdd"], IS=1e-15, N=1.1, AREA=2.0) if vamodels
+             else c.diode("D1", "o", "vdd", IS=1e-15, N=1.1, AREA=2.0))
+        elif which == "nlvcr":
+            (c.va("X", "va_nlvcr", ["vdd", "in", "0"], R=2.0) if vamodels else c.nlvcr("X", "vdd", "in", "0", R=2.0))
+        return c.flatten()
+    return mk(False), mk(True)
+
+
+@pytest.mark.parametrize("which", ["mos", "passive", "nlvcr"])
+def test_va_models_match_builtins(pkg, oracle, which):
+    fb, fv = _builtin_twin(pkg, which)
+    assert fb.names == fv.names
+    rng = np.random.default_rng(7)
+    for _ in range(40):
+        x = rng.uniform(-0.5, 2.0, fb.n)
+        x[fb.n_nodes:] = rng.uniform(-1e-3, 1e-3, fb.n - fb.n_nodes)
+        xd = rng.normal(0, 1e9, fb.n)
+        Fb, Fib, Fqb, Gb, Cb = oracle.eval(fb, x, xd)
+        Fv, Fiv, Fqv, Gv, Cv = oracle.eval(fv, x, xd)
+        sc = np.abs(Gb) @ np.abs(x) + np.abs(Fib) + 1e-30
+        assert np.all(np.abs(Fiv - Fib) <= 1e-13 * sc)
+        assert np.all(np.abs(Fqv - Fqb) <= 1e-13 * (np.abs(Cb) @ np.abs(x) + 1e-40))
+        assert np.all(np.abs(Gv - Gb) <= 1e-12 * (np.abs(Gb).max(axis=1, keepdims=True) + 1e-30))
+        assert np.all(np.abs(Cv - Cb) <= 1e-12 * (np.abs(Cb).max() + 1e-40))
+
+
+def test_ddx_known_answer(pkg, oracle):
+    """test/ddx.jl: I(d,s) <+ V(d,s) * ddx(R V(g,s)^2, V(g,s)) with V(d)=5, V(g)=3,
+    R=2 gives a source current of -5*2*2*3."""
+    f = K.va_nlvcr(pkg).flatten()
+    x, st, rc = oracle.dcop(f)
+    assert rc == 0
+    assert abs(x[f.index("V1.I")] - (-60.0)) <= 8 * np.spacing(60.0)
+
+
+def test_resistor_orientation_regression(pkg, oracle, va, interp):
+    """test/varegress.jl: a resistor written I(n,p) <+ V(n,p)/R is the same device
+    as I(p,n) <+ V(p,n)/R; in the V-R-C circuit its current stays non-negative."""
+    src = """
+    `include "disciplines.vams"
+    module rev_r(p, n); inout p, n; electrical p, n; parameter real R = 1000.0 from (0.0:inf];
+      analog I(n, p) <+ V(n, p) / R;
+    endmodule"""
+    rev = va.parse(src)[0]
+    fwd = va.model(va.model_id("va_resistor"))
+    for v in ([1.0, 0.25], [-0.3, 0.8], [0.0, 0.0]):
+        a = interp.evaluate(rev, {"R": 1e3}, v, VT, 1e-12)
+        b = interp.evaluate(fwd.module, {"R": 1e3}, v, VT, 1e-12)
+        assert np.allclose(a[0], b[0], rtol=0, atol=1e-18) and np.allclose(a[2], b[2], rtol=0, atol=1e-18)
+    from cedarsim_gb300.va.emit import analyze
+    mr, _ = analyze(rev)
+    assert (mr.frows, mr.gents, mr.qrows, mr.cents) == (fwd.frows, fwd.gents, fwd.qrows, fwd.cents)
+    # V(1) -> R(1k) -> out, C(1n) to ground, 0..10 us: branch current >= 0 throughout
+    c = pkg.Circuit()
+    c.V("V", "vcc", "gnd", dc=1.0)
+    c.va("R", "va_resistor", ["vcc", "out"], R=1000.0)
+    c.C("C", "out", "gnd", 1e-9)
+    f = c.flatten()
+    o = pkg.make_opts("bdf2", True, 0.0, 1e-5, 0.0, False)
+    t, X, st, rc = oracle.tran(f, o, np.zeros(f.n))
+    assert rc == 0 and st.status == 0
+    i_r = (X[:, f.index("vcc")] - X[:, f.index("out")]) / 1000.0
+    assert np.all(i_r[1:] >= 0.0) and X[-1, f.index("out")] == pytest.approx(1.0, abs=1e-3)
+
+
+def test_parameters_and_circuit_api(pkg, va):
+    m = va.model(va.model_id("va_mos1"))
+    assert m.ports == ["d", "g", "s", "b"] and m.npar == 7
+    assert m.defaults() == [1.0, 1e-6, 1e-6, 2e-5, 0.7, 0.0]
+    assert m.defaults({"W": 3e-6})[1] == 3e-6
+    with pytest.raises(va.VAError):
+        m.defaults({"TYPE": 0.0})          # excluded value
+    with pytest.raises(va.VAError):
+        m.defaults({"W": -1.0})            # outside (0:inf)
+    with pytest.raises(va.VAError):
+        m.defaults({"WIDTH": 1.0})         # unknown parameter
+    c = pkg.Circuit()
+    with pytest.raises(ValueError):
+        c.va("M", "va_mos1", ["a", "b", "c"])
+    with pytest.raises(KeyError):
+        c.va("M", "no_such_model", ["a", "b"])
+    c.va("M", "va_mos1", ["d", "g", "0", "0"], W=2e-6, m=3.0)
+    f = c.flatten()
+    model, term, br, par = f.groups[0]
+    assert model == va.model_id("va_mos1") and br is None
+    assert par[:, 0].tolist() == [1.0, 2e-6, 1e-6, 2e-5, 0.7, 0.0, 3.0]
+    assert term[0].tolist() == [f.index("d"), f.index("g"), -1, -1]
+
+
+def test_library_lists_the_models(pkg, va):
+    lib = pkg.load_library()
+    assert lib.cedar_va_count() == len(va.models())
+    buf = C.create_string_buffer(64)
+    for k, m in enumerate(va.models()):
+        assert lib.cedar_va_name(k, buf, 64) == 0 and buf.value.decode() == m.name
+        mid = va.BASE_ID + k
+        assert lib.cedar_model_nterm(mid) == m.nterm and lib.cedar_model_npar(mid) == m.npar
+        assert lib.cedar_model_has_branch(mid) == 0
+    assert lib.cedar_va_name(len(va.models()), buf, 64) != 0
+    assert lib.cedar_model_nterm(va.BASE_ID + len(va.models())) == -1
+
+
+@pytest.mark.parametrize("src, msg", [
+    ("module m(a, b); inout a, b; electrical a, b, x; analog I(a, b) <+ V(a, b); endmodule", "internal node"),
+    ("module m(a, b); inout a, b; electrical a, b; analog V(a, b) <+ 1.0; endmodule", "voltage contributions"),
+    ("module m(a, b); inout a, b; electrical a, b; analog I(a, b) <+ foo(V(a, b)); endmodule", "unsupported function"),
+    ("module m(a, b); inout a, b; electrical a, b; analog I(a, b) <+ V(a, b) * ddt(V(a, b)); endmodule", "additive"),
+    ("module m(a, b); inout a, b; electrical a, b; analog I(a, c) <+ V(a, b); endmodule", "not a port"),
+    ("module m(a, b); inout a, b; electrical a, b; analog begin x = 1; I(a, b) <+ x; end endmodule", "undeclared"),
+    ("module m(a, b); inout a, b; electrical a, b; parameter real R = 1; analog begin R = 2; I(a, b) <+ R; end "
+     "endmodule", "parameter"),
+])
+def test_subset_errors(va, src, msg):
+    from cedarsim_gb300.va.emit import _Emitter, analyze
+    with pytest.raises(va.VAError, match=msg):
+        for mod in va.parse(src):
+            m, a = analyze(mod)
+            _Emitter(m, a).body()
+
+
+def test_parser_details(va):
+    src = """
+    `include "disciplines.vams"
+    `include "constants.vams"
+    `define TWO 2.0
+    module t(p, n);
+      inout p, n; electrical p, n;
+      parameter integer K = 3 from [1:10];
+      parameter real G0 = 1m, G1 = G0 * `TWO;
+      real g; integer i;
+      analog begin : blk
+        i = K / 2;                 // integer division
+        g = (i == 1) ? G1 : G0;    /* ternary, comparison */
+        if (V(p, n) > 0.5 && !(K < 2)) g = g + 1u;
+        I(p, n) <+ g * V(p, n) + 1e-3 * M_PI * 0;
+      end
+    endmodule"""
+    mod = va.parse(src)[0]
+    from cedarsim_gb300.va.emit import analyze
+    m, _ = analyze(mod)
+    assert m.defaults() == [3.0, 1e-3, 2e-3]
+    assert m.gents == [(0, 0), (0, 1), (1, 0), (1, 1)]
