@@ -46,11 +46,17 @@ def test_va_ddx_known_answer_on_gpu(gpu, pkg):
     assert abs(x[f.index("V1.I")] - (-60.0)) <= 8 * np.spacing(60.0)
 
 
-@pytest.mark.parametrize("case", ["va_mixed", "va_chain_7"])
-def test_va_transient_parity(gpu, pkg, oracle, case):
+@pytest.mark.parametrize("case, adaptive", [("va_mixed", False), ("va_chain_7", True)])
+def test_va_transient_parity(gpu, pkg, oracle, case, adaptive):
+    """Fixed-step BDF2 (h = 1 ps) on the mixed circuit, adaptive BDF2 on the chain.
+    The mixed circuit's 5k adaptive steps put some LTE tests within rounding of
+    the accept / step-factor thresholds, where the sparse static-pivot LU and
+    the oracle's dense LU can choose differently (one step in 5114 on a GB300),
+    so its time points are pinned by the fixed step instead."""
     flat = CASES[case](pkg).flatten()
-    o = pkg.make_opts("bdf2", True, 0.0, 2e-9, 0.0, True)
-    sol = pkg.tran(flat, (0.0, 2e-9), method="bdf2")
+    h = 0.0 if adaptive else 1e-12
+    o = pkg.make_opts("bdf2", adaptive, 0.0, 2e-9, h, True)
+    sol = pkg.tran(flat, (0.0, 2e-9), method="bdf2", h=h or None, adaptive=adaptive)
     t_ref, x_ref, st, rc = oracle.tran(flat, o)
     assert rc == 0 and sol.retcode == "OK"
     assert (sol.stats["accepted"], sol.stats["rejected"]) == (st.accepted, st.rejected)
@@ -115,5 +121,6 @@ def test_va_ac_parity(gpu, pkg, oracle):
     probes = ["b", "c", "d"]
     r = pkg.ac(flat, x_op=x_op).freqresp(probes, w)
     ro = oracle.ac(flat, x_op, w, [flat.index(p) for p in probes])
-    err = np.max(np.abs(r - ro) / np.max(np.abs(ro), axis=0, keepdims=True))
+    # relative to the largest probed magnitude at each frequency, as the AC parity tests
+    err = np.max(np.abs(r - ro) / np.max(np.abs(ro), axis=1, keepdims=True))
     assert err <= 1e-9
