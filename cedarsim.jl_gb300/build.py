@@ -86,5 +86,10 @@ def build(force: bool = False, verbose: bool = False) -> pathlib.Path:
 
 
 if __name__ == "__main__":
+    # run as a script: load the package (its directory name is not an identifier)
+    # so that the Verilog-A emitter is importable, then build through it
     import sys
-    print(build(force="--force" in sys.argv, verbose=True))
+    sys.path.insert(0, str(PKG.parent))
+    import __graft_entry__
+    b = __import__(__graft_entry__.load().__name__ + ".build", fromlist=["build"])
+    print(b.build(force="--force" in sys.argv, verbose=True))
