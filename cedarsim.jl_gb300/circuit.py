@@ -240,13 +240,17 @@ class Circuit:
     def va(self, name, model: str, terms: Sequence[str], m: float = 1.0, **params):
         """An instance of a compiled Verilog-A module (cedarsim.jl_gb300/va):
         terminals in port order, parameters by name (defaults from the module's
-        declarations, ranges checked), multiplicity m."""
+        declarations, ranges checked), multiplicity m.  The module's internal
+        nodes become nodes named "<name>.<node>" placed after the ports in the
+        device's terminal list."""
         from . import va
         mid = va.model_id(model)
         mod = va.model(mid)
-        if len(terms) != mod.nterm:
+        if len(terms) != len(mod.ports):
             raise ValueError(f"{model} has ports {mod.ports}, got {len(terms)} terminals")
-        return self._add(name, mid, list(terms), mod.defaults(params) + [float(m)])
+        # internal nodes: one node unknown each, named "<instance>.<node>"
+        inner = [f"{name}.{n}" for n in mod.internals]
+        return self._add(name, mid, list(terms) + inner, mod.defaults(params) + [float(m)])
 
     # ---- flattening
     def flatten(self) -> Flat:

@@ -25,7 +25,7 @@ from typing import Dict, FrozenSet, List, Optional, Set, Tuple
 from .parser import (Assign, Bin, Call, Cond, Contrib, If, Module, Name, Num, Param, Probe, SysCall, Unary,
                      VAError)
 
-MAX_PORTS = 5   # the engines stage at most 5 terminal values per device
+MAX_PORTS = 5   # the engines stage at most 5 terminal values per device (ports + internal nodes)
 
 FUNCS = {  # VA name -> (C++ name, arity)
     "exp": ("exp", 1), "ln": ("log", 1), "log": ("log10", 1), "sqrt": ("sqrt", 1), "pow": ("pow", 2),
@@ -51,8 +51,12 @@ class VAModel:
     flops: int
 
     @property
-    def nterm(self) -> int:
-        return len(self.ports)
+    def internals(self) -> List[str]:
+        return list(self.module.internals)
+
+    @property
+    def nterm(self) -> int:         # device-table terminals: ports, then internal nodes
+        return len(self.ports) + len(self.module.internals)
 
     @property
     def npar(self) -> int:          # raw: parameters + m
@@ -152,7 +156,7 @@ def _is_inf(e) -> bool:
 class _Analysis:
     def __init__(self, mod: Module):
         self.mod = mod
-        self.port = {p: k for k, p in enumerate(mod.ports)}
+        self.port = {p: k for k, p in enumerate(list(mod.ports) + list(mod.internals))}
         self.params = {p.name for p in mod.params}
         self.vars = dict(mod.variables)
         self.var_deps: Dict[str, FrozenSet[int]] = {v: frozenset() for v in self.vars}
@@ -276,8 +280,9 @@ def _has_ddt(e) -> bool:
 def analyze(mod: Module) -> Tuple[VAModel, _Analysis]:
     if not mod.ports:
         raise VAError(f"{mod.name}: a device needs ports")
-    if len(mod.ports) > MAX_PORTS:
-        raise VAError(f"{mod.name}: {len(mod.ports)} ports (at most {MAX_PORTS})")
+    if len(mod.ports) + len(mod.internals) > MAX_PORTS:
+        raise VAError(f"{mod.name}: {len(mod.ports)} ports + {len(mod.internals)} internal nodes (at most "
+                      f"{MAX_PORTS} in all)")
     names = [p.name for p in mod.params]
     if len(set(names)) != len(names):
         raise VAError(f"{mod.name}: duplicate parameter names")
@@ -472,7 +477,7 @@ class _Emitter:
 
     def body(self) -> str:
         m = self.m
-        L = [f"// module {m.name}({', '.join(m.ports)})",
+        L = [f"// module {m.name}({', '.join(m.ports)})" + (f", internal {', '.join(m.internals)}" if m.internals else ""),
              "template <class D>",
              f"VA_HD void body_{m.name}(const double *P, int ps, const Ctx &c, const D *V, D *Fi, D *Fq) {{"]
         for k, p in enumerate(m.params):

@@ -3,7 +3,7 @@ parser for the compact-model subset the GPU emitter compiles.
 
 Subset (the constructs CedarSim's VA translator lowers for compact models,
 src/vasim.jl:128-180,347-412,663-875):
-  module NAME(ports); port directions; `electrical` ports;
+  module NAME(ports); port directions; `electrical` ports and internal nodes;
   parameter [real|integer] NAME = expr [from|exclude range] {, ...};
   real / integer variables (module or block scope);
   analog begin ... end with assignments, if / else, begin / end blocks,
@@ -13,8 +13,9 @@ src/vasim.jl:128-180,347-412,663-875):
   cosh sin cos tan atan atan2 asin acos hypot floor ceil limexp; ddt(expr) (additive
   in a contribution); ddx(expr, V(n)) / ddx(expr, V(a,b)); $vt, $vt(T),
   $temperature, $simparam("gmin"[, default]), $mfactor.
-Internal nodes, voltage contributions, analog functions, noise sources and
-events are outside the subset and raise VAError with the line number.
+Internal nodes (`electrical` names that are not ports) become extra device
+unknowns.  Voltage contributions, branch-current probes, analog functions, noise
+sources and events are outside the subset and raise VAError with the line number.
 """
 from __future__ import annotations
 
@@ -209,6 +210,7 @@ class Module:
     params: List[Param]
     variables: Dict[str, str]      # name -> "real" | "integer"
     body: list
+    internals: List[str] = field(default_factory=list)   # internal nodes, after the ports
 
 
 # ------------------------------------------------------------------ parser
@@ -267,6 +269,7 @@ class Parser:
         variables: Dict[str, str] = {}
         body: list = []
         electrical = set()
+        internals: List[str] = []
         while not self.at("endmodule"):
             p = self.peek()
             if p is None:
@@ -277,8 +280,8 @@ class Parser:
             elif p.text == "electrical":
                 self.take()
                 for n in self._idlist():
-                    if n not in ports:
-                        raise VAError(f"line {p.line}: internal node {n!r} (only ports are supported)")
+                    if n not in ports and n not in internals:
+                        internals.append(n)       # an internal node: one more unknown per instance
                     electrical.add(n)
             elif p.text in ("parameter", "localparam"):
                 params.extend(self._params())
@@ -297,7 +300,7 @@ class Parser:
         missing = [q for q in ports if q not in electrical]
         if missing:
             raise VAError(f"module {name}: ports without a discipline: {missing}")
-        return Module(name, ports, params, variables, body)
+        return Module(name, ports, params, variables, body, internals)
 
     def _idlist(self) -> List[str]:
         names = [self.ident()]

@@ -158,8 +158,9 @@ class _Q:
 class Interp:
     def __init__(self, module, params: Dict[str, float], v: List[float], vt: float, gmin: float, m: float = 1.0):
         self.mod = module
-        self.N = len(module.ports)
-        self.port = {p: k for k, p in enumerate(module.ports)}
+        nodes = list(module.ports) + list(getattr(module, "internals", []))
+        self.N = len(nodes)
+        self.port = {p: k for k, p in enumerate(nodes)}
         self.params = {}
         for p in module.params:
             val = params[p.name]

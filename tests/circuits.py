@@ -181,3 +181,19 @@ def va_mixed(pkg):
     c.mos1("MB", "e", "d", "0", "0", 1.0, 2e-6, 1e-6, 200e-6, 0.45)
     c.va("C2", "va_capacitor", ["e", "0"], C=3e-15)
     return c
+
+
+def va_diode_rs(pkg, twin=False):
+    """A pulse through 1 kOhm into a diode with 50 Ohm series resistance on a
+    0.5 pF load: the internal-node model, or (twin) the same network built from
+    va_resistor + va_diode around an explicit node of the same name."""
+    c = pkg.Circuit()
+    c.V("VIN", "in", "0", wave=pkg.Pulse(-1.0, 2.0, 0.05e-9, 0.1e-9, 0.1e-9, 0.5e-9, 1.2e-9))
+    c.R("R1", "in", "x", r=1e3)
+    if twin:
+        c.va("RSx", "va_resistor", ["x", "D1.ai"], R=50.0)
+        c.va("D1j", "va_diode", ["D1.ai", "0"], IS=1e-14, N=1.05)
+    else:
+        c.va("D1", "va_diode_rs", ["x", "0"], IS=1e-14, N=1.05, RS=50.0)
+    c.C("CL", "x", "0", 0.5e-12)
+    return c

@@ -17,6 +17,7 @@ CASES = {
     "va_mixed": K.va_mixed,
     "va_chain_7": lambda pkg: K.inverter_chain_va(pkg, 7),
     "va_nlvcr": K.va_nlvcr,
+    "va_diode_rs": K.va_diode_rs,      # internal node
 }
 
 
@@ -46,7 +47,7 @@ def test_va_ddx_known_answer_on_gpu(gpu, pkg):
     assert abs(x[f.index("V1.I")] - (-60.0)) <= 8 * np.spacing(60.0)
 
 
-@pytest.mark.parametrize("case, adaptive", [("va_mixed", False), ("va_chain_7", True)])
+@pytest.mark.parametrize("case, adaptive", [("va_mixed", False), ("va_chain_7", True), ("va_diode_rs", False)])
 def test_va_transient_parity(gpu, pkg, oracle, case, adaptive):
     """Fixed-step BDF2 (h = 1 ps) on the mixed circuit, adaptive BDF2 on the chain.
     The mixed circuit's 5k adaptive steps put some LTE tests within rounding of

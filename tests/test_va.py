@@ -209,7 +209,8 @@ def test_library_lists_the_models(pkg, va):
 
 
 @pytest.mark.parametrize("src, msg", [
-    ("module m(a, b); inout a, b; electrical a, b, x; analog I(a, b) <+ V(a, b); endmodule", "internal node"),
+    ("module m(a, b); inout a, b; electrical a, b, x1, x2, x3, x4; analog I(a, b) <+ V(a, b); endmodule",
+     "at most"),
     ("module m(a, b); inout a, b; electrical a, b; analog V(a, b) <+ 1.0; endmodule", "voltage contributions"),
     ("module m(a, b); inout a, b; electrical a, b; analog I(a, b) <+ foo(V(a, b)); endmodule", "unsupported function"),
     ("module m(a, b); inout a, b; electrical a, b; analog I(a, b) <+ V(a, b) * ddt(V(a, b)); endmodule", "additive"),
@@ -248,3 +249,30 @@ def test_parser_details(va):
     m, _ = analyze(mod)
     assert m.defaults() == [3.0, 1e-3, 2e-3]
     assert m.gents == [(0, 0), (0, 1), (1, 0), (1, 1)]
+
+
+def test_internal_node_model_equals_its_expanded_network(pkg, oracle, va):
+    """va_diode_rs (RS to an internal node, the junction behind it) is the same
+    network as va_resistor + va_diode around an explicit node: same unknowns
+    (the internal node is named "<instance>.<node>"), same F, J, DC point and
+    waveform."""
+    m = va.model(va.model_id("va_diode_rs"))
+    assert m.ports == ["a", "c"] and m.internals == ["ai"] and m.nterm == 3
+    fa, fb = K.va_diode_rs(pkg).flatten(), K.va_diode_rs(pkg, twin=True).flatten()
+    assert fa.names == fb.names and "D1.ai" in fa.names
+    rng = np.random.default_rng(3)
+    for _ in range(20):
+        x = rng.uniform(-1.0, 1.0, fa.n)
+        _, Fia, _, Ga, _ = oracle.eval(fa, x, t=0.3e-9)
+        _, Fib, _, Gb, _ = oracle.eval(fb, x, t=0.3e-9)
+        sc = np.abs(Gb) @ np.abs(x) + np.abs(Fib)
+        assert np.all(np.abs(Fia - Fib) <= 1e-13 * sc + 1e-300)
+        assert np.all(np.abs(Ga - Gb) <= 1e-13 * np.abs(Gb).max(axis=1, keepdims=True) + 1e-300)
+    o = pkg.make_opts("bdf2", False, 0.0, 1.2e-9, 1e-12, True)
+    ta, Xa, sa, ra = oracle.tran(fa, o)
+    tb, Xb, sb, rb = oracle.tran(fb, o)
+    assert ra == 0 and rb == 0 and np.array_equal(ta, tb)
+    assert np.max(np.abs(Xa - Xb) / (1e-9 * np.abs(Xb) + 1e-12)) <= 1.0
+    # the diode conducts through RS on the high phase: ai sits below x
+    k = np.searchsorted(ta, 0.5e-9)
+    assert Xa[k, fa.index("x")] - Xa[k, fa.index("D1.ai")] > 1e-3
