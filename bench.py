@@ -62,6 +62,9 @@ def parse():
     p.add_argument("--no-rings", action="store_true", help="skip the ring-oscillator leg")
     p.add_argument("--no-ac", action="store_true", help="skip the AC / noise sweep leg")
     p.add_argument("--ac-freq", type=int, default=1 << 17, help="frequency points of the AC / noise leg")
+    p.add_argument("--no-va", action="store_true", help="skip the Verilog-A model leg")
+    p.add_argument("--va-inst", type=int, default=1024, help="instances of the Verilog-A leg")
+    p.add_argument("--va-tstop-ns", type=float, default=5.0)
     p.add_argument("--ring-inst", type=int, default=1024)
     p.add_argument("--ring-tstop-ns", type=float, default=50.0)
     p.add_argument("--eval-stages", type=int, default=1_000_000, help="inverter-chain stages of the cedar_eval leg")
@@ -271,6 +274,41 @@ def measure_rings(pkg, args, C):
             "oscillating_instances": osc, "accepted_steps_mean": float(r.stats["accepted"].mean()),
             "newton_iters_per_s": float(r.stats["newton_iters"].sum() + r.stats["dc_iters"].sum()) / (ms.value / 1e3),
             "tuning": list(sw.tuning), "timing": "CUDA events around one cedar_batch_run launch (DC operating points included)"}
+
+
+def measure_va(pkg, args, C):
+    """The Monte Carlo chains with their MOSFETs as the Verilog-A level-1 model
+    compiled by the emitter (va_mos1: the built-in model's equations and
+    parameter block, evaluated over dual numbers), timed beside the built-in
+    model on the same instances: the cost of generic emitted device code."""
+    import copy
+    va_id = pkg.va.model_id("va_mos1")
+    templates, itpl, par, off = pkg.generators.mc_chains(args.va_inst, seed=args.seed)
+    va_tpl = []
+    for f in templates:
+        g = copy.deepcopy(f)
+        g.groups = [(va_id if m == pkg.circuit.MOS1 else m, t, b, p) for (m, t, b, p) in g.groups]
+        assert [x[0] for x in g.groups] == sorted(x[0] for x in g.groups)   # same group (block) order
+        va_tpl.append(g)
+    tstop = args.va_tstop_ns * 1e-9
+    o = pkg.make_opts("bdf2", True, 0.0, tstop, 0.0, True, reltol=1e-6, abstol_v=1e-9)
+    res = {}
+    for name, tp in (("builtin", templates), ("verilog_a", va_tpl)):
+        sw = pkg.Batch(tp, itpl, par, off)
+        sw.run(pkg.make_opts("bdf2", True, 0.0, 0.05e-9, 0.0, True))     # warm-up
+        r = sw.run(o)
+        ms = C.c_double()
+        pkg.abi.check(sw.lib.cedar_batch_last_ms(sw.handle, C.byref(ms)))
+        res[name] = {"value": float(r.stats["accepted"].sum()) / (ms.value / 1e3), "ms": ms.value,
+                     "failed_instances": int((r.stats["status"] != 0).sum()),
+                     "accepted_steps": int(r.stats["accepted"].sum())}
+        del sw
+    return {"workload": f"{args.va_inst} MC chains (L in {{5..63}}), adaptive BDF2 to {args.va_tstop_ns:g} ns, "
+                        "MOSFETs as the emitted Verilog-A va_mos1 vs the built-in level-1 model",
+            "unit": "instance-timesteps/s", "value": res["verilog_a"]["value"], "builtin": res["builtin"],
+            "verilog_a": res["verilog_a"], "va_over_builtin": res["verilog_a"]["value"] / res["builtin"]["value"],
+            "same_step_counts": res["verilog_a"]["accepted_steps"] == res["builtin"]["accepted_steps"],
+            "timing": "CUDA events around one cedar_batch_run launch each (DC operating points included)"}
 
 
 def measure_ac(pkg, args, torch, C, fp64_peak):
@@ -511,6 +549,7 @@ def main():
     eval_leg = None if args.no_eval else measure_eval(pkg, args, torch, C)
     rings = None if args.no_rings else measure_rings(pkg, args, C)
     ac_leg = None if args.no_ac else measure_ac(pkg, args, torch, C, fp64_peak)
+    va_leg = None if args.no_va else measure_va(pkg, args, C)
     cpu = None
     if not args.no_cpu_baseline:
         cpu_line = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
@@ -541,7 +580,7 @@ def main():
                              "peak = DFMA rate measured in this run by cedar_fp64_probe (MEASURED_PEAKS.json "
                              "has no FP64 entry); the kernel keeps its state on chip, so HBM is not its bound"},
         "cpu_baseline": cpu, "e2e": e2e, "plain_gpu": plain, "adjoint": adj, "eval_hbm": eval_leg, "rings": rings,
-        "ac": ac_leg, "clocks": clk, "gpu_launches": args.steps,
+        "ac": ac_leg, "verilog_a": va_leg, "clocks": clk, "gpu_launches": args.steps,
     }
     print(json.dumps(line), flush=True)
 

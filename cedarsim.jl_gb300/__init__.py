@@ -11,9 +11,10 @@ from .sweeps import (Sweep, ProductSweep, TandemSweep, SerialSweep, CircuitSweep
                      write_csv)
 from .api import ACSol, NoiseSol, ac, acdec, ac_drive, ac_last_stats, noise  # noqa: F401
 from . import generators  # noqa: F401
+from . import va  # noqa: F401
 
 __all__ = ["Circuit", "Flat", "Pulse", "PWL", "Sin", "System", "Solution", "Batch", "BatchResult", "Sweep", "ProductSweep",
            "TandemSweep", "SerialSweep", "CircuitSweep", "ParamSim", "alter", "sweepvars", "split_axes", "sweepify",
            "find_param_ranges", "nest_param_list", "flatten_param_list", "write_csv", "dc", "tran",
            "load_library", "make_opts", "generators", "CedarError", "STATUS_NAMES",
-           "ACSol", "NoiseSol", "ac", "acdec", "ac_drive", "ac_last_stats", "noise"]
+           "ACSol", "NoiseSol", "ac", "acdec", "ac_drive", "ac_last_stats", "noise", "va"]
