@@ -49,6 +49,7 @@ class VAModel:
     qrows: List[int]
     cents: List[Tuple[int, int]]
     flops: int
+    given: List[str] = dataclasses.field(default_factory=list)   # parameters queried by $param_given
 
     @property
     def internals(self) -> List[str]:
@@ -59,12 +60,12 @@ class VAModel:
         return len(self.ports) + len(self.module.internals)
 
     @property
-    def npar(self) -> int:          # raw: parameters + m
-        return len(self.params) + 1
+    def npar(self) -> int:          # raw: parameters, $param_given flags, m
+        return len(self.params) + len(self.given) + 1
 
     @property
     def ndpar(self) -> int:         # derived: raw + vt
-        return len(self.params) + 2
+        return self.npar + 1
 
     @property
     def nout(self) -> int:
@@ -91,7 +92,8 @@ class VAModel:
                 v = float(math.floor(abs(v) + 0.5) * (1 if v >= 0 else -1))
             check_range(self.name, p, v, env)
             env[p.name] = v
-        return [env[p.name] for p in self.params]
+        # $param_given(P) flags: 1 where the instance sets P
+        return [env[p.name] for p in self.params] + [1.0 if g in overrides else 0.0 for g in self.given]
 
 
 # ------------------------------------------------------------ host evaluation
@@ -161,6 +163,8 @@ class _Analysis:
         self.vars = dict(mod.variables)
         self.var_deps: Dict[str, FrozenSet[int]] = {v: frozenset() for v in self.vars}
         self.second_order = False
+        self.funcs = dict(mod.functions)
+        self.given: List[str] = []          # parameters queried by $param_given, in order of use
         self.contribs: List[Tuple[Contrib, Optional[object], List[Tuple[int, object]]]] = []
 
     def port_index(self, n: str, line: int) -> int:
@@ -169,7 +173,14 @@ class _Analysis:
         return self.port[n]
 
     def deps(self, e) -> FrozenSet[int]:
-        if isinstance(e, Num) or isinstance(e, SysCall):
+        if isinstance(e, SysCall):
+            if e.name in ("$param_given", "$given"):
+                if len(e.args) != 1 or not isinstance(e.args[0], Name) or e.args[0].id not in self.params:
+                    raise VAError(f"{self.mod.name}: $param_given takes a parameter name")
+                if e.args[0].id not in self.given:
+                    self.given.append(e.args[0].id)
+            return frozenset()
+        if isinstance(e, Num):
             return frozenset()
         if isinstance(e, Name):
             if e.id in self.params:
@@ -194,6 +205,8 @@ class _Analysis:
             if e.fn == "ddx":
                 self.second_order = True
                 return self.deps(e.args[0])
+            if e.fn in ("white_noise", "flicker_noise"):
+                return frozenset()       # noise sources: zero outside a noise analysis
             if e.fn == "ddt":
                 return self.deps(e.args[0])
             if e.fn in ("floor", "ceil"):
@@ -234,6 +247,48 @@ class _Analysis:
             if before == self.var_deps:
                 break
         self.walk(self.mod.body, collect=True)
+
+
+def _check_function(mod: Module, f):
+    """An analog function sees its arguments and locals only, assigns only
+    those, and calls neither ddt, ddx nor other analog functions' outputs by
+    reference."""
+    def ex(e):
+        if isinstance(e, Name):
+            if e.id not in f.local:
+                raise VAError(f"{mod.name}: analog function {f.name}: {e.id!r} is not an argument or local")
+        elif isinstance(e, Probe):
+            raise VAError(f"{mod.name}: analog function {f.name}: probes are not allowed in functions")
+        elif isinstance(e, Call):
+            if e.fn in ("ddt", "ddx"):
+                raise VAError(f"{mod.name}: analog function {f.name}: {e.fn}() is not allowed in functions")
+            if e.fn not in FUNCS and e.fn not in mod.functions:
+                raise VAError(f"{mod.name}: line {e.line}: unsupported function {e.fn}()")
+            for x in e.args:
+                ex(x)
+        elif isinstance(e, Unary):
+            ex(e.x)
+        elif isinstance(e, Bin):
+            ex(e.a)
+            ex(e.b)
+        elif isinstance(e, Cond):
+            ex(e.c)
+            ex(e.a)
+            ex(e.b)
+
+    def st(ss):
+        for s in ss:
+            if isinstance(s, Assign):
+                if s.name not in f.local:
+                    raise VAError(f"{mod.name}: analog function {f.name}: assignment to {s.name!r}")
+                ex(s.expr)
+            elif isinstance(s, If):
+                ex(s.c)
+                st(s.then)
+                st(s.other)
+            elif isinstance(s, Contrib):
+                raise VAError(f"{mod.name}: analog function {f.name}: contributions are not allowed in functions")
+    st(f.body)
 
 
 def split_ddt(e, line: int):
@@ -308,8 +363,10 @@ def analyze(mod: Module) -> Tuple[VAModel, _Analysis]:
                 d |= a.deps(q)
             cents.update((r, k) for r in rows for k in d)
     flops = _count_flops(mod.body)
+    for f in mod.functions.values():
+        _check_function(mod, f)
     m = VAModel(mod.name, mod, list(mod.ports), list(mod.params), a.second_order, sorted(frows), sorted(gents),
-                sorted(qrows), sorted(cents), flops)
+                sorted(qrows), sorted(cents), flops, list(a.given))
     if m.nout == 0:
         raise VAError(f"{mod.name}: the analog block makes no contribution")
     m.defaults()  # defaults must evaluate and satisfy their ranges
@@ -361,11 +418,14 @@ class _Emitter:
     def __init__(self, m: VAModel, a: _Analysis):
         self.m = m
         self.a = a
+        self.scope: Optional[Dict[str, str]] = None     # an analog function's names while emitting it
 
     def is_int(self, e) -> bool:
         if isinstance(e, Num):
             return e.is_int
         if isinstance(e, Name):
+            if self.scope is not None:
+                return self.scope.get(e.id) == "integer"
             if e.id in self.a.params:
                 return next(p for p in self.m.params if p.name == e.id).type == "integer"
             return self.a.vars.get(e.id) == "integer"
@@ -383,6 +443,8 @@ class _Emitter:
         if isinstance(e, Num):
             return _lit(e.v)
         if isinstance(e, Name):
+            if self.scope is not None:
+                return "v_" + e.id
             return ("p_" if e.id in self.a.params else "v_") + e.id
         if isinstance(e, Probe):
             ia = self.a.port[e.a]
@@ -422,6 +484,14 @@ class _Emitter:
                 # two-node probe: the mean of the two one-sided partials, as
                 # CedarSim defines it (src/vasim.jl:400-411)
                 return f"((ddx({inner}, {ia}) - ddx({inner}, {self.a.port[p.b]})) * 0.5)"
+            if e.fn in ("white_noise", "flicker_noise"):
+                return "0.0"           # noise sources are zero in DC, transient and AC
+            if e.fn in self.a.funcs:
+                f = self.a.funcs[e.fn]
+                if len(e.args) != len(f.inputs):
+                    raise VAError(f"{self.m.name}: line {e.line}: {e.fn}() takes {len(f.inputs)} argument(s)")
+                args = "".join(f", D({self.x(a)})" for a in e.args)
+                return f"fn_{self.m.name}_{e.fn}<D>(c{args})"
             if e.fn not in FUNCS:
                 raise VAError(f"{self.m.name}: line {e.line}: unsupported function {e.fn}()")
             cname, ar = FUNCS[e.fn]
@@ -437,6 +507,8 @@ class _Emitter:
                 return "c.temp"
             if e.name == "$mfactor":
                 return "c.m"
+            if e.name in ("$param_given", "$given"):
+                return f"p__given_{e.args[0].id}"
             if e.name == "$simparam":
                 if not e.args or not isinstance(e.args[0], str):
                     raise VAError(f"{self.m.name}: $simparam needs a name")
@@ -447,20 +519,21 @@ class _Emitter:
                 raise VAError(f"{self.m.name}: $simparam(\"{e.args[0]}\") has no value here and no default")
         raise VAError(f"{self.m.name}: unsupported expression {e!r}")
 
-    def stmts(self, ss, ind: str) -> List[str]:
+    def stmts(self, ss, ind: str, types: Optional[Dict[str, str]] = None) -> List[str]:
+        types = self.a.vars if types is None else types
         out = []
         for s in ss:
             if isinstance(s, Assign):
-                if self.a.vars[s.name] == "integer":
+                if types[s.name] == "integer":
                     out.append(f"{ind}v_{s.name} = vint(val({self.x(s.expr)}));")
                 else:
                     out.append(f"{ind}v_{s.name} = {self.x(s.expr)};")
             elif isinstance(s, If):
                 out.append(f"{ind}if (val({self.x(s.c)}) != 0.0) {{")
-                out += self.stmts(s.then, ind + "  ")
+                out += self.stmts(s.then, ind + "  ", types)
                 if s.other:
                     out.append(f"{ind}}} else {{")
-                    out += self.stmts(s.other, ind + "  ")
+                    out += self.stmts(s.other, ind + "  ", types)
                 out.append(f"{ind}}}")
             elif isinstance(s, Contrib):
                 res, charges = split_ddt(s.expr, s.line)
@@ -482,6 +555,8 @@ class _Emitter:
              f"VA_HD void body_{m.name}(const double *P, int ps, const Ctx &c, const D *V, D *Fi, D *Fq) {{"]
         for k, p in enumerate(m.params):
             L.append(f"  const double p_{p.name} = P[{k} * ps];")
+        for j, g in enumerate(m.given):
+            L.append(f"  const double p__given_{g} = P[{len(m.params) + j} * ps];")
         for v, t in m.module.variables.items():
             L.append(f"  D v_{v}(0.0);" if t == "real" else f"  double v_{v} = 0.0;")
         L += self.stmts(m.module.body, "  ")
@@ -489,13 +564,36 @@ class _Emitter:
         L.append("}")
         return "\n".join(L)
 
+    def functions(self) -> str:
+        """Analog functions as templates over the body's dual type: arguments by
+        value, locals zero-initialised, the result in the variable named after
+        the function."""
+        out = []
+        for f in self.m.module.functions.values():
+            args = "".join(f", D v_{a}" for a in f.inputs)
+            L = ["template <class D>", f"VA_HD D fn_{self.m.name}_{f.name}(const Ctx &c{args}) {{"]
+            for v, t in f.local.items():
+                if v in f.inputs:
+                    continue
+                L.append(f"  D v_{v}(0.0);" if t == "real" else f"  double v_{v} = 0.0;")
+            self.scope = f.local
+            try:
+                L += self.stmts(f.body, "  ", f.local)
+            finally:
+                self.scope = None
+            L.append(f"  (void)c;")
+            L.append(f"  return D(v_{f.name});")
+            L.append("}")
+            out.append("\n".join(L))
+        return "\n\n".join(out)
+
     def dtype(self) -> str:
         n = self.m.nterm
         return f"Dual<Dual<double, {n}>, {n}>" if self.m.second_order else f"Dual<double, {n}>"
 
     def prologue(self) -> List[str]:
         m = self.m
-        P = len(m.params)
+        P = m.npar - 1                 # position of m in the derived block (vt follows)
         return [f"  typedef {self.dtype()} D;",
                 "  Ctx c;",
                 f"  c.m = dp[{P} * ds]; c.vt = dp[{P + 1} * ds]; c.temp = c.vt * {_lit(P_Q / P_K)}; c.gmin = gmin;",
@@ -561,7 +659,8 @@ def emit_header(models: List[Tuple[VAModel, _Analysis]], base_id: int) -> str:
          ""]
     for m, a in models:
         e = _Emitter(m, a)
-        L += [e.body(), "", e.eval(), "", e.full(), ""]
+        fns = e.functions()
+        L += ([fns, ""] if fns else []) + [e.body(), "", e.eval(), "", e.full(), ""]
 
     def table(name, vals, ctype="int"):
         vals = list(vals) or [0]

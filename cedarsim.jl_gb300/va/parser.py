@@ -30,7 +30,7 @@ class VAError(Exception):
 
 # ------------------------------------------------------------------ lexer
 _TOKEN = re.compile(r"""
-    (?P<ws>[ \t\r\n]+)
+    (?P<ws>[ \t\r\n\x00]+)
   | (?P<lcom>//[^\n]*)
   | (?P<bcom>/\*.*?\*/)
   | (?P<num>(\d+\.\d*|\.\d+|\d+)([eE][+-]?\d+)?[TGMKkmunpfa]?)
@@ -45,6 +45,9 @@ SCALE = {"T": 1e12, "G": 1e9, "M": 1e6, "K": 1e3, "k": 1e3, "m": 1e-3, "u": 1e-6
          "f": 1e-15, "a": 1e-18}
 
 # constants of the standard constants.vams header (physical constants, SI)
+DISPLAY_TASKS = ("$strobe", "$display", "$write", "$monitor", "$debug", "$warning", "$info", "$error", "$fatal",
+                 "$finish", "$stop")
+
 CONSTANTS = {"M_PI": 3.14159265358979323846, "M_TWO_PI": 6.28318530717958647652,
              "M_PI_2": 1.57079632679489661923, "M_E": 2.7182818284590452354,
              "P_Q": 1.602176634e-19, "P_K": 1.380649e-23, "P_CELSIUS0": 273.15,
@@ -60,7 +63,7 @@ class Tok:
 
 def lex(src: str) -> List[Tok]:
     out: List[Tok] = []
-    pos, line = 0, 1
+    pos, line, pending = 0, 1, 0
     while pos < len(src):
         m = _TOKEN.match(src, pos)
         if not m:
@@ -69,22 +72,122 @@ def lex(src: str) -> List[Tok]:
         text = m.group(kind)
         if kind not in ("ws", "lcom", "bcom"):
             out.append(Tok(kind, text, line))
-        line += text.count("\n")
+        # a joined continuation (\x00) keeps the tokens on one line; its newline
+        # is counted at the next real line break
+        pending += text.count("\x00")
+        if "\n" in text:
+            line += text.count("\n") + pending
+            pending = 0
         pos = m.end()
     return out
 
 
+def _join_continuations(src: str) -> str:
+    """A backslash at the end of a line continues a `define body on the next
+    line; the newline is kept out of the body but counted for line numbers."""
+    return re.sub(r"\\[ \t]*\r?\n", " \x00", src)
+
+
 def preprocess(toks: List[Tok]) -> List[Tok]:
-    """`define NAME tokens (no arguments), `NAME expansion, `include of the
-    standard headers (disciplines.vams / constants.vams: their names are built in),
-    `undef; other directives are errors."""
-    macros: Dict[str, List[Tok]] = {}
+    """`define NAME body and `define NAME(a, b) body with `NAME / `NAME(x, y)
+    expansion (nested, up to a depth limit), `undef, `ifdef / `ifndef / `elsif /
+    `else / `endif, and `include of the standard headers (disciplines.vams /
+    constants.vams: their names are built in).  Other directives are errors."""
+    macros: Dict[str, Tuple[Optional[List[str]], List[Tok]]] = {}
     out: List[Tok] = []
+    # conditional stack: (this branch active, some branch already taken, parent active)
+    cond: List[Tuple[bool, bool, bool]] = []
+
+    def active() -> bool:
+        return not cond or cond[-1][0]
+
+    def expand(stream: List[Tok], depth: int) -> List[Tok]:
+        if depth > 32:
+            raise VAError("macro expansion too deep (recursive `define?)")
+        res: List[Tok] = []
+        k = 0
+        while k < len(stream):
+            t = stream[k]
+            if t.kind == "dir" and t.text[1:] in macros:
+                params, body = macros[t.text[1:]]
+                k += 1
+                if params is None:
+                    res.extend(expand([Tok(b.kind, b.text, t.line) for b in body], depth + 1))
+                    continue
+                if k >= len(stream) or stream[k].text != "(":
+                    raise VAError(f"line {t.line}: macro {t.text} needs arguments")
+                args: List[List[Tok]] = [[]]
+                level = 0
+                k += 1
+                while k < len(stream):
+                    a = stream[k]
+                    if a.text == "(" and a.kind == "op":
+                        level += 1
+                    elif a.text == ")" and a.kind == "op":
+                        if level == 0:
+                            break
+                        level -= 1
+                    elif a.text == "," and a.kind == "op" and level == 0:
+                        args.append([])
+                        k += 1
+                        continue
+                    args[-1].append(a)
+                    k += 1
+                if k >= len(stream):
+                    raise VAError(f"line {t.line}: unterminated arguments of macro {t.text}")
+                k += 1
+                if len(args) != len(params) and not (len(params) == 0 and args == [[]]):
+                    raise VAError(f"line {t.line}: macro {t.text} takes {len(params)} arguments, got {len(args)}")
+                sub = {p: expand(a, depth + 1) for p, a in zip(params, args)}
+                body_t: List[Tok] = []
+                for b in body:
+                    if b.kind == "id" and b.text in sub:
+                        body_t.extend(Tok(x.kind, x.text, t.line) for x in sub[b.text])
+                    else:
+                        body_t.append(Tok(b.kind, b.text, t.line))
+                res.extend(expand(body_t, depth + 1))
+                continue
+            res.append(t)
+            k += 1
+        return res
+
     i = 0
     while i < len(toks):
         t = toks[i]
         if t.kind == "dir":
             name = t.text[1:]
+            if name in ("ifdef", "ifndef", "elsif"):
+                if i + 1 >= len(toks) or toks[i + 1].kind != "id":
+                    raise VAError(f"line {t.line}: `{name} needs a macro name")
+                defined = toks[i + 1].text in macros
+                if name == "elsif":
+                    if not cond:
+                        raise VAError(f"line {t.line}: `elsif without `ifdef")
+                    _, taken, parent = cond.pop()
+                    take = parent and not taken and defined
+                    cond.append((take, taken or take, parent))
+                else:
+                    parent = active()
+                    take = parent and (defined if name == "ifdef" else not defined)
+                    cond.append((take, take, parent))
+                i += 2
+                continue
+            if name == "else":
+                if not cond:
+                    raise VAError(f"line {t.line}: `else without `ifdef")
+                _, taken, parent = cond.pop()
+                cond.append((parent and not taken, True, parent))
+                i += 1
+                continue
+            if name == "endif":
+                if not cond:
+                    raise VAError(f"line {t.line}: `endif without `ifdef")
+                cond.pop()
+                i += 1
+                continue
+            if not active():
+                i += 1
+                continue
             if name == "include":
                 if i + 1 >= len(toks) or toks[i + 1].kind != "str":
                     raise VAError(f"line {t.line}: `include needs a file name")
@@ -98,13 +201,22 @@ def preprocess(toks: List[Tok]) -> List[Tok]:
                     raise VAError(f"line {t.line}: `define needs a name")
                 mname, mline = toks[i + 1].text, toks[i + 1].line
                 j = i + 2
+                params = None
+                # a parameter list opens right after the name (no space is not
+                # visible after lexing, so any "(" on the same line starts one)
+                if j < len(toks) and toks[j].line == mline and toks[j].text == "(" and toks[j].kind == "op":
+                    params = []
+                    j += 1
+                    while j < len(toks) and toks[j].text != ")":
+                        if toks[j].kind == "id":
+                            params.append(toks[j].text)
+                        j += 1
+                    j += 1
                 body = []
                 while j < len(toks) and toks[j].line == mline:
                     body.append(toks[j])
                     j += 1
-                if body and body[0].text == "(" and body[0].line == mline:
-                    raise VAError(f"line {t.line}: `define with arguments is not supported")
-                macros[mname] = body
+                macros[mname] = (params, body)
                 i = j
                 continue
             if name == "undef":
@@ -112,12 +224,28 @@ def preprocess(toks: List[Tok]) -> List[Tok]:
                 i += 2
                 continue
             if name in macros:
-                out.extend(Tok(b.kind, b.text, t.line) for b in macros[name])
-                i += 1
+                # collect the macro call (with its argument list) and expand it
+                j = i + 1
+                if macros[name][0] is not None and j < len(toks) and toks[j].text == "(":
+                    level = 0
+                    while j < len(toks):
+                        if toks[j].text == "(":
+                            level += 1
+                        elif toks[j].text == ")":
+                            level -= 1
+                            if level == 0:
+                                j += 1
+                                break
+                        j += 1
+                out.extend(expand(toks[i:j], 0))
+                i = j
                 continue
             raise VAError(f"line {t.line}: unknown directive {t.text}")
-        out.append(t)
+        if active():
+            out.append(t)
         i += 1
+    if cond:
+        raise VAError("`ifdef without `endif")
     return out
 
 
@@ -211,6 +339,16 @@ class Module:
     variables: Dict[str, str]      # name -> "real" | "integer"
     body: list
     internals: List[str] = field(default_factory=list)   # internal nodes, after the ports
+    functions: Dict[str, "Function"] = field(default_factory=dict)
+
+
+@dataclass
+class Function:         # analog function: inputs by value, result in the variable NAME
+    name: str
+    type: str
+    inputs: List[str]
+    local: Dict[str, str]          # arguments, locals and the result variable -> type
+    body: list
 
 
 # ------------------------------------------------------------------ parser
@@ -267,6 +405,7 @@ class Parser:
         self.take(";")
         params: List[Param] = []
         variables: Dict[str, str] = {}
+        functions: Dict[str, Function] = {}
         body: list = []
         electrical = set()
         internals: List[str] = []
@@ -293,6 +432,12 @@ class Parser:
                 self.take()
                 if self.at("initial"):
                     raise VAError(f"line {p.line}: analog initial is not supported")
+                if self.at("function"):
+                    f = self._function()
+                    if f.name in functions:
+                        raise VAError(f"line {p.line}: analog function {f.name} defined twice")
+                    functions[f.name] = f
+                    continue
                 body.extend(self.statement(variables))
             else:
                 raise VAError(f"line {p.line}: unsupported module item {p.text!r}")
@@ -300,7 +445,39 @@ class Parser:
         missing = [q for q in ports if q not in electrical]
         if missing:
             raise VAError(f"module {name}: ports without a discipline: {missing}")
-        return Module(name, ports, params, variables, body, internals)
+        return Module(name, ports, params, variables, body, internals, functions)
+
+    def _function(self) -> "Function":
+        """analog function [real|integer] NAME; input a, b; real a, b, t; stmt endfunction"""
+        self.take("function")
+        ftype = "real"
+        if self.at("real") or self.at("integer"):
+            ftype = self.take().text
+        name = self.ident()
+        self.take(";")
+        inputs: List[str] = []
+        local: Dict[str, str] = {}
+        while True:
+            q = self.peek()
+            if q is None:
+                raise VAError(f"analog function {name}: missing endfunction")
+            if q.text in ("input",):
+                self.take()
+                inputs += self._idlist()
+            elif q.text in ("output", "inout"):
+                raise VAError(f"line {q.line}: analog function {name}: output arguments are not supported")
+            elif q.text in ("real", "integer"):
+                self.take()
+                for n in self._idlist():
+                    local[n] = q.text
+            else:
+                break
+        for a in inputs:
+            local.setdefault(a, "real")
+        local[name] = ftype                 # the return value is the variable named after the function
+        body = self.statement(local)
+        self.take("endfunction")
+        return Function(name, ftype, inputs, local, body)
 
     def _idlist(self) -> List[str]:
         names = [self.ident()]
@@ -376,6 +553,69 @@ class Parser:
         if p.text == ";":
             self.take()
             return []
+        if p.kind == "sys" and p.text in DISPLAY_TASKS:
+            # $strobe / $display / ... print from the simulator; no effect on the
+            # device equations, so they compile to nothing
+            self.take()
+            if self.at("("):
+                self.take("(")
+                if not self.at(")"):
+                    self._sysarg()
+                    while self.at(","):
+                        self.take(",")
+                        self._sysarg()
+                self.take(")")
+            self.take(";")
+            return []
+        if p.text == "@" and p.kind == "op":
+            # @(initial_step) / @(initial_model) / @(initial_instance) blocks
+            # compute values from parameters: evaluated at every call, which
+            # gives the same values; @(final_step) blocks only report, dropped
+            self.take()
+            self.take("(")
+            ev = self.ident()
+            if self.at("("):            # initial_step("tran") and the like
+                self.take("(")
+                while not self.at(")"):
+                    self.take()
+                self.take(")")
+            self.take(")")
+            if ev not in ("initial_step", "initial_model", "initial_instance", "final_step"):
+                raise VAError(f"line {p.line}: unsupported event @({ev})")
+            body = self.statement(variables)
+            return [] if ev == "final_step" else body
+        if p.text == "case" and p.kind == "id":
+            # case (x) v1, v2: s; ... default: s; endcase -> if / else chain
+            self.take()
+            self.take("(")
+            sel = self.expr()
+            self.take(")")
+            arms: List[Tuple[Optional[list], list]] = []
+            while not self.at("endcase"):
+                if self.peek() is None:
+                    raise VAError(f"line {p.line}: missing endcase")
+                if self.at("default"):
+                    self.take()
+                    if self.at(":"):
+                        self.take(":")
+                    arms.append((None, self.statement(variables)))
+                    continue
+                labels = [self.expr()]
+                while self.at(","):
+                    self.take(",")
+                    labels.append(self.expr())
+                self.take(":")
+                arms.append((labels, self.statement(variables)))
+            self.take("endcase")
+            default = next((s for lab, s in arms if lab is None), [])
+            out: list = default
+            for labels, body in reversed([a for a in arms if a[0] is not None]):
+                c = None
+                for lab in labels:
+                    t = Bin("==", sel, lab)
+                    c = t if c is None else Bin("||", c, t)
+                out = [If(c, body, out)]
+            return out
         if p.kind == "id" and p.text in ("I", "V") and self.peek(1) is not None and self.peek(1).text == "(":
             # contribution
             kind = self.take().text
@@ -476,7 +716,7 @@ class Parser:
                         self.take(",")
                         args.append(self._sysarg())
                 self.take(")")
-            if p.text not in ("$vt", "$temperature", "$simparam", "$mfactor"):
+            if p.text not in ("$vt", "$temperature", "$simparam", "$mfactor", "$param_given", "$given"):
                 raise VAError(f"line {p.line}: unsupported system function {p.text}")
             return SysCall(p.text, args)
         if p.kind == "id":
@@ -494,12 +734,14 @@ class Parser:
                     return Probe(a, b)
                 if p.text == "I":
                     raise VAError(f"line {p.line}: branch-current probes I(...) are not supported")
+                # noise sources take a name string after their power arguments
+                arg = self._sysarg if p.text in ("white_noise", "flicker_noise") else self.expr
                 args = []
                 if not self.at(")"):
-                    args.append(self.expr())
+                    args.append(arg())
                     while self.at(","):
                         self.take(",")
-                        args.append(self.expr())
+                        args.append(arg())
                 self.take(")")
                 return Call(p.text, args, p.line)
             return Name(p.text, p.line)
@@ -513,7 +755,7 @@ class Parser:
 
 def parse(src: str) -> List[Module]:
     """Parse Verilog-A source text into modules."""
-    return Parser(preprocess(lex(src))).modules()
+    return Parser(preprocess(lex(_join_continuations(src)))).modules()
 
 
 def parse_file(path) -> List[Module]:

@@ -156,7 +156,8 @@ class _Q:
 
 
 class Interp:
-    def __init__(self, module, params: Dict[str, float], v: List[float], vt: float, gmin: float, m: float = 1.0):
+    def __init__(self, module, params: Dict[str, float], v: List[float], vt: float, gmin: float, m: float = 1.0,
+                 given=()):
         self.mod = module
         nodes = list(module.ports) + list(getattr(module, "internals", []))
         self.N = len(nodes)
@@ -174,6 +175,8 @@ class Interp:
             outer_d = [D(1.0 if i == k else 0.0, [0.0] * N) for i in range(N)]
             self.V.append(D(inner, outer_d))
         self.vars = {name: (0 if t == "integer" else self._const(0.0)) for name, t in module.variables.items()}
+        self.types = dict(module.variables)
+        self.given = set(given)
         self.Fi = [self._const(0.0) for _ in range(N)]
         self.Fq = [self._const(0.0) for _ in range(N)]
 
@@ -236,6 +239,10 @@ class Interp:
             return self.expr(e.a) if value(self.expr(e.c)) != 0 else self.expr(e.b)
         if isinstance(e, P.Call):
             fn = e.fn
+            if fn in ("white_noise", "flicker_noise"):
+                return 0.0                      # noise sources: zero outside a noise analysis
+            if fn in getattr(self.mod, "functions", {}):
+                return self._call(self.mod.functions[fn], [self.expr(a) for a in e.args])
             if fn == "ddt":
                 return _Q(0.0, self.expr(e.args[0]))
             if fn == "ddx":
@@ -275,6 +282,8 @@ class Interp:
                 return self.vt if not e.args else 1.380649e-23 * value(self.expr(e.args[0])) / 1.602176634e-19
             if e.name == "$temperature":
                 return self.vt * 1.602176634e-19 / 1.380649e-23
+            if e.name in ("$param_given", "$given"):
+                return int(e.args[0].id in self.given)
             if e.name == "$mfactor":
                 return self.m
             if e.name == "$simparam":
@@ -289,12 +298,26 @@ class Interp:
         inner = x.d[a]
         return D(inner, [D(inner.d[i], [0.0] * N) for i in range(N)])
 
+    def _call(self, f, args):
+        """An analog function: a fresh scope of its arguments and locals."""
+        saved = (self.vars, self.types, self.params)
+        self.types = dict(f.local)
+        self.vars = {n: (0 if t == "integer" else self._const(0.0)) for n, t in f.local.items()}
+        self.params = {}
+        for n, a in zip(f.inputs, args):
+            self.vars[n] = self._dual(a) if f.local[n] == "real" else a
+        try:
+            self.block(f.body)
+            return self.vars[f.name]
+        finally:
+            self.vars, self.types, self.params = saved
+
     def block(self, stmts):
         P = self.P
         for s in stmts:
             if isinstance(s, P.Assign):
                 x = self.expr(s.expr)
-                if self.mod.variables[s.name] == "integer":
+                if self.types[s.name] == "integer":
                     v = value(x)
                     self.vars[s.name] = int(math.floor(abs(v) + 0.5)) * (1 if v >= 0 else -1)
                 else:
@@ -320,10 +343,11 @@ def _atan2_general(y, x):
     return 2.0 * _unary_fn("atan", y / (h + x))
 
 
-def evaluate(module, params: Dict[str, float], v: List[float], vt: float, gmin: float, m: float = 1.0):
+def evaluate(module, params: Dict[str, float], v: List[float], vt: float, gmin: float, m: float = 1.0,
+             given=()):
     """(fi[N], fq[N], G[N][N], C[N][N]) of one device of `module` at port
     potentials v, unscaled by the multiplicity (m is only what $mfactor reads)."""
-    it = Interp(module, params, v, vt, gmin, m)
+    it = Interp(module, params, v, vt, gmin, m, given)
     Fi, Fq = it.run()
     N = it.N
     fi = [value(x) for x in Fi]

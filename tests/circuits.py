@@ -197,3 +197,16 @@ def va_diode_rs(pkg, twin=False):
         c.va("D1", "va_diode_rs", ["x", "0"], IS=1e-14, N=1.05, RS=50.0)
     c.C("CL", "x", "0", 0.5e-12)
     return c
+
+
+def va_vccs(pkg):
+    """The saturating transconductor (analog function, macros, case,
+    $param_given) driving a resistive load from a pulse."""
+    c = pkg.Circuit()
+    c.V("VIN", "b", "0", wave=pkg.Pulse(-1.0, 1.0, 0.05e-9, 0.2e-9, 0.2e-9, 0.3e-9, 1e-9))
+    c.va("G1", "va_vccs_sat", ["0", "d", "b", "0"], GM=2e-3, VS=0.4, MODE=1)
+    c.va("G2", "va_vccs_sat", ["0", "e", "d", "0"], GMX=1e-3, VS=0.3, MODE=2)
+    c.R("RD", "d", "0", r=1e3)
+    c.R("RE", "e", "0", r=2e3)
+    c.C("CE", "e", "0", 50e-15)
+    return c

@@ -18,6 +18,7 @@ CASES = {
     "va_chain_7": lambda pkg: K.inverter_chain_va(pkg, 7),
     "va_nlvcr": K.va_nlvcr,
     "va_diode_rs": K.va_diode_rs,      # internal node
+    "va_vccs": K.va_vccs,              # analog function, macros, case, $param_given
 }
 
 
@@ -47,7 +48,8 @@ def test_va_ddx_known_answer_on_gpu(gpu, pkg):
     assert abs(x[f.index("V1.I")] - (-60.0)) <= 8 * np.spacing(60.0)
 
 
-@pytest.mark.parametrize("case, adaptive", [("va_mixed", False), ("va_chain_7", True), ("va_diode_rs", False)])
+@pytest.mark.parametrize("case, adaptive", [("va_mixed", False), ("va_chain_7", True), ("va_diode_rs", False),
+                                            ("va_vccs", False)])
 def test_va_transient_parity(gpu, pkg, oracle, case, adaptive):
     """Fixed-step BDF2 (h = 1 ps) on the mixed circuit, adaptive BDF2 on the chain.
     The mixed circuit's 5k adaptive steps put some LTE tests within rounding of

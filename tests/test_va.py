@@ -52,6 +52,8 @@ def _params(m, rng):
         elif p.name in ("LAMBDA", "TT", "CJ0"):
             out[p.name] = float(rng.choice([0.0, abs(d) + 1e-3 * rng.uniform(0.5, 2.0)])) if p.name == "LAMBDA" \
                 else float(rng.choice([0.0, rng.uniform(1e-15, 1e-11)]))
+        elif p.name == "MODE":
+            out[p.name] = float(rng.integers(0, 3))
         elif p.name == "R":
             out[p.name] = float(rng.uniform(0.5, 5.0) * (1 if rng.random() < 0.8 else -1))
         else:
@@ -75,8 +77,9 @@ def test_emitted_code_matches_interpreter(pkg, oracle, va, interp):
                 v[0] = v[1] + rng.uniform(-1.0, 0.9)     # keep exp() finite but exercise forward bias
             fi, fq, G, Cm = np.zeros(n), np.zeros(n), np.zeros(n * n), np.zeros(n * n)
             assert lib.oracle_va_full(k, dp_(dp), dp_(v), 1e-12, dp_(fi), dp_(fq), dp_(G), dp_(Cm)) == 0
+            given = [g for g in m.given if g in prm]
             ri, rq, rG, rC = interp.evaluate(m.module, dict(zip([p.name for p in m.params], vals)), list(v), VT,
-                                             1e-12, mult)
+                                             1e-12, mult, given)
             ri, rq, rG, rC = np.array(ri), np.array(rq), np.array(rG).ravel(), np.array(rC).ravel()
             sc = np.abs(ri).max() + 1e-30
             assert np.all(np.abs(fi - ri) <= 1e-13 * sc), (m.name, fi, ri)
@@ -276,3 +279,78 @@ def test_internal_node_model_equals_its_expanded_network(pkg, oracle, va):
     # the diode conducts through RS on the high phase: ai sits below x
     k = np.searchsorted(ta, 0.5e-9)
     assert Xa[k, fa.index("x")] - Xa[k, fa.index("D1.ai")] > 1e-3
+
+
+def test_functions_macros_case_and_param_given(pkg, oracle, va):
+    """va_vccs_sat uses an analog function, function-like macros, case, an
+    @(initial_step) block, $strobe, $param_given and a white_noise source: its
+    current is gm f(V(cp,cn)) with f per MODE, gm = GMX where the instance sets
+    it, and no noise contribution outside a noise analysis."""
+    import math
+    k = va.model_id("va_vccs_sat") - va.BASE_ID
+    m = va.models()[k]
+    assert m.given == ["GMX"] and m.npar == 6
+    lib = oracle.lib
+    dp_ = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    vs = 0.4
+    for mode, f in ((0, lambda x: x), (1, lambda x: vs * math.tanh(x / vs)), (2, lambda x: x / math.sqrt(1 + (x / vs) ** 2))):
+        for given, gm in ((False, 2e-3), (True, 5e-3)):
+            over = {"GM": 2e-3, "VS": vs, "MODE": mode}
+            if given:
+                over["GMX"] = 5e-3
+            dp = np.array(m.defaults(over) + [1.0, VT])
+            for vc in (-0.9, -0.1, 0.0, 0.25, 1.3):
+                v = np.array([0.7, 0.2, vc + 0.1, 0.1])
+                fi, fq, G, Cm = np.zeros(4), np.zeros(4), np.zeros(16), np.zeros(16)
+                assert lib.oracle_va_full(k, dp_(dp), dp_(v), 1e-12, dp_(fi), dp_(fq), dp_(G), dp_(Cm)) == 0
+                want = gm * f(vc)
+                assert fi[0] == pytest.approx(-want, rel=1e-14, abs=1e-30) and fi[1] == pytest.approx(want, rel=1e-14,
+                                                                                                      abs=1e-30)
+                h = 1e-6
+                slope = gm * (f(vc + h) - f(vc - h)) / (2 * h)
+                assert -G[0 * 4 + 2] == pytest.approx(slope, rel=1e-7) and G[0 * 4 + 3] == pytest.approx(slope, rel=1e-7)
+    # instance parameters and the given flag through the circuit API
+    c = pkg.Circuit()
+    c.va("X1", "va_vccs_sat", ["a", "0", "b", "0"], GM=1e-3)
+    c.va("X2", "va_vccs_sat", ["a", "0", "b", "0"], GMX=3e-3, MODE=2)
+    f = c.flatten()
+    assert f.groups[0][3][:, 0].tolist() == [1e-3, 0.0, 0.5, 1.0, 0.0, 1.0]
+    assert f.groups[0][3][:, 1].tolist() == [1e-3, 3e-3, 0.5, 2.0, 1.0, 1.0]
+
+
+def test_preprocessor_and_statement_forms(va):
+    src = r"""
+    `define SQ(x) ((x)*(x))
+    `define CLIP(x, lo, hi) (((x) < (lo)) ? (lo) : (((x) > (hi)) ? (hi) : (x)))
+    `define LONG(a, b) (`SQ(a) + \
+                        `SQ(b))
+    `ifdef NOT_DEFINED
+      `define GAIN 100.0
+    `elsif SQ
+      `define GAIN 2.0
+    `else
+      `define GAIN 3.0
+    `endif
+    module pp(p, n); inout p, n; electrical p, n;
+      parameter integer K = 2;
+      real g;
+      analog begin
+        case (K) 1, 2: g = `GAIN; default: g = 0; endcase
+        @(final_step) $strobe("never");
+        I(p, n) <+ g * `CLIP(V(p, n), -1, 1) + 1e-3 * `LONG(V(p, n), 1.0) + flicker_noise(1e-20, 1.0, "f");
+      end
+    endmodule"""
+    mod = va.parse(src)[0]
+    from cedarsim_gb300.va.emit import analyze
+    m, _ = analyze(mod)
+    assert m.gents == [(0, 0), (0, 1), (1, 0), (1, 1)]
+    with pytest.raises(va.VAError, match="takes 2 arguments"):
+        va.parse("`define F(a, b) a+b\nmodule m(p); inout p; electrical p; analog I(p) <+ `F(1); endmodule")
+    with pytest.raises(va.VAError, match="endif"):
+        va.parse("`ifdef X\nmodule m(p); inout p; electrical p; analog I(p) <+ 1; endmodule")
+    with pytest.raises(va.VAError, match="not an argument or local"):
+        src2 = """module m(p); inout p; electrical p; parameter real R = 1;
+          analog function real f; input x; real x; f = x * R; endfunction
+          analog I(p) <+ f(V(p)); endmodule"""
+        for mm in va.parse(src2):
+            analyze(mm)
