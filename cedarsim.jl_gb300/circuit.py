@@ -41,6 +41,15 @@ def model_nterm(model: int) -> int:
     return NTERM[model]
 
 
+def model_has_branch(model: int) -> bool:
+    """A branch-current unknown: L, V, E and Verilog-A modules with a
+    voltage-contributed branch."""
+    if model >= VA_BASE:
+        from . import va
+        return bool(va.model(model).has_br)
+    return model in HAS_BRANCH
+
+
 def model_npar(model: int) -> int:
     if model >= VA_BASE:
         from . import va
@@ -258,7 +267,7 @@ class Circuit:
         names = list(self.node_names)
         branch_of: Dict[str, int] = {}
         for d in self.devices:
-            if d.model in HAS_BRANCH:
+            if model_has_branch(d.model):
                 branch_of[d.name] = n_nodes + len(branch_of)
                 names.append(f"{d.name}.I")
         pwl: List[float] = []
@@ -269,7 +278,7 @@ class Circuit:
             nt, npar = model_nterm(model), model_npar(model)
             term = np.array([[self._node_index.get(t, -1) if t not in GROUND else -1 for t in d.terms] for d in devs],
                             dtype=np.int32).reshape(len(devs), nt)
-            br = np.array([branch_of[d.name] for d in devs], dtype=np.int32) if model in HAS_BRANCH else None
+            br = np.array([branch_of[d.name] for d in devs], dtype=np.int32) if model_has_branch(model) else None
             par = np.zeros((npar, len(devs)), dtype=np.float64)
             for i, d in enumerate(devs):
                 p = list(d.params)

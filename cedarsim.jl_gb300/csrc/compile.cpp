@@ -46,7 +46,7 @@ static const ModelInfo kModels[CEDAR_NMODELS] = {
 static const std::vector<ModelInfo> &va_infos() {
   static const std::vector<ModelInfo> t = [] {
     std::vector<ModelInfo> v;
-    for (int k = 0; k < va::kCount; ++k) v.push_back({va::kNTerm[k], va::kNPar[k], 0, va::kNOut[k], va::kNDPar[k]});
+    for (int k = 0; k < va::kCount; ++k) v.push_back({va::kNTerm[k], va::kNPar[k], va::kHasBr[k], va::kNOut[k], va::kNDPar[k]});
     return v;
   }();
   return t;

@@ -50,6 +50,7 @@ class VAModel:
     cents: List[Tuple[int, int]]
     flops: int
     given: List[str] = dataclasses.field(default_factory=list)   # parameters queried by $param_given
+    vbranch: Optional[Tuple[str, Optional[str]]] = None  # the voltage-contributed branch (a, b), if any
 
     @property
     def internals(self) -> List[str]:
@@ -58,6 +59,14 @@ class VAModel:
     @property
     def nterm(self) -> int:         # device-table terminals: ports, then internal nodes
         return len(self.ports) + len(self.module.internals)
+
+    @property
+    def has_br(self) -> int:        # a branch-current unknown (after the terminals)
+        return 1 if self.vbranch is not None else 0
+
+    @property
+    def nx(self) -> int:            # dual-number seeds: terminals, then the branch current
+        return self.nterm + self.has_br
 
     @property
     def npar(self) -> int:          # raw: parameters, $param_given flags, m
@@ -164,8 +173,35 @@ class _Analysis:
         self.var_deps: Dict[str, FrozenSet[int]] = {v: frozenset() for v in self.vars}
         self.second_order = False
         self.funcs = dict(mod.functions)
+        self.vbranch = None            # (a, b) of the voltage-contributed branch
+        self.nb = None                 # its seed index (after the terminals)
+        self._find_vbranch(mod.body)
+        if self.vbranch is not None:
+            self.nb = len(self.port)
         self.given: List[str] = []          # parameters queried by $param_given, in order of use
         self.contribs: List[Tuple[Contrib, Optional[object], List[Tuple[int, object]]]] = []
+
+    def _find_vbranch(self, stmts):
+        for s in stmts:
+            if isinstance(s, If):
+                self._find_vbranch(s.then)
+                self._find_vbranch(s.other)
+            elif isinstance(s, Contrib) and s.kind == "V":
+                br = (s.a, s.b)
+                if self.vbranch is None:
+                    self.vbranch = br
+                elif br != self.vbranch and (br[1], br[0]) != self.vbranch:
+                    raise VAError(f"{self.mod.name}: line {s.line}: a second voltage-contributed branch "
+                                  f"(only one per module)")
+
+    def branch_sign(self, a: str, b: Optional[str], line: int) -> int:
+        """+1 / -1 when (a, b) is the voltage branch in its own / the reverse orientation."""
+        if self.vbranch is not None:
+            if (a, b) == self.vbranch:
+                return 1
+            if b is not None and (b, a) == self.vbranch:
+                return -1
+        raise VAError(f"{self.mod.name}: line {line}: I({a}{', ' + b if b else ''}) probes no voltage-contributed branch")
 
     def port_index(self, n: str, line: int) -> int:
         if n not in self.port:
@@ -189,6 +225,9 @@ class _Analysis:
                 return self.var_deps[e.id]
             raise VAError(f"{self.mod.name}: line {e.line}: undeclared name {e.id!r}")
         if isinstance(e, Probe):
+            if e.kind == "I":
+                self.branch_sign(e.a, e.b, 0)
+                return frozenset({self.nb})
             s = {self.port_index(e.a, 0)}
             if e.b is not None:
                 s.add(self.port_index(e.b, 0))
@@ -234,6 +273,9 @@ class _Analysis:
                 self.port_index(s.a, s.line)
                 if s.b is not None:
                     self.port_index(s.b, s.line)
+                if s.kind == "I" and self.vbranch is not None and (
+                        (s.a, s.b) == self.vbranch or (s.b is not None and (s.b, s.a) == self.vbranch)):
+                    raise VAError(f"{self.mod.name}: line {s.line}: current and voltage contributions on one branch")
                 if collect:
                     res, charges = split_ddt(s.expr, s.line)
                     self.contribs.append((s, res, charges))
@@ -247,6 +289,14 @@ class _Analysis:
             if before == self.var_deps:
                 break
         self.walk(self.mod.body, collect=True)
+
+
+def _all_stmts(stmts):
+    for s in stmts:
+        yield s
+        if isinstance(s, If):
+            yield from _all_stmts(s.then)
+            yield from _all_stmts(s.other)
 
 
 def _check_function(mod: Module, f):
@@ -335,9 +385,10 @@ def _has_ddt(e) -> bool:
 def analyze(mod: Module) -> Tuple[VAModel, _Analysis]:
     if not mod.ports:
         raise VAError(f"{mod.name}: a device needs ports")
-    if len(mod.ports) + len(mod.internals) > MAX_PORTS:
-        raise VAError(f"{mod.name}: {len(mod.ports)} ports + {len(mod.internals)} internal nodes (at most "
-                      f"{MAX_PORTS} in all)")
+    nbr = 1 if any(isinstance(s, Contrib) and s.kind == "V" for s in _all_stmts(mod.body)) else 0
+    if len(mod.ports) + len(mod.internals) + nbr > MAX_PORTS:
+        raise VAError(f"{mod.name}: {len(mod.ports)} ports + {len(mod.internals)} internal nodes + {nbr} branch "
+                      f"unknown(s) (at most {MAX_PORTS} in all)")
     names = [p.name for p in mod.params]
     if len(set(names)) != len(names):
         raise VAError(f"{mod.name}: duplicate parameter names")
@@ -350,8 +401,15 @@ def analyze(mod: Module) -> Tuple[VAModel, _Analysis]:
     qrows: Set[int] = set()
     gents: Set[Tuple[int, int]] = set()
     cents: Set[Tuple[int, int]] = set()
+    if a.vbranch is not None:
+        # KCL: the branch current leaves a and enters b; branch row: V(a) - V(b) - sum(contributions)
+        va_, vb_ = a.vbranch
+        ends = [a.port[va_]] + ([a.port[vb_]] if vb_ is not None else [])
+        frows.update(ends + [a.nb])
+        gents.update((r, a.nb) for r in ends)
+        gents.update((a.nb, k) for k in ends)
     for c, res, charges in a.contribs:
-        rows = [a.port[c.a]] + ([a.port[c.b]] if c.b is not None else [])
+        rows = [a.port[c.a]] + ([a.port[c.b]] if c.b is not None else []) if c.kind == "I" else [a.nb]
         frows.update(rows)
         if res is not None:
             d = a.deps(res)
@@ -366,7 +424,7 @@ def analyze(mod: Module) -> Tuple[VAModel, _Analysis]:
     for f in mod.functions.values():
         _check_function(mod, f)
     m = VAModel(mod.name, mod, list(mod.ports), list(mod.params), a.second_order, sorted(frows), sorted(gents),
-                sorted(qrows), sorted(cents), flops, list(a.given))
+                sorted(qrows), sorted(cents), flops, list(a.given), a.vbranch)
     if m.nout == 0:
         raise VAError(f"{mod.name}: the analog block makes no contribution")
     m.defaults()  # defaults must evaluate and satisfy their ranges
@@ -447,6 +505,9 @@ class _Emitter:
                 return "v_" + e.id
             return ("p_" if e.id in self.a.params else "v_") + e.id
         if isinstance(e, Probe):
+            if e.kind == "I":
+                sg = self.a.branch_sign(e.a, e.b, 0)
+                return f"V[{self.a.nb}]" if sg > 0 else f"(-V[{self.a.nb}])"
             ia = self.a.port[e.a]
             if e.b is None:
                 return f"V[{ia}]"
@@ -535,6 +596,16 @@ class _Emitter:
                     out.append(f"{ind}}} else {{")
                     out += self.stmts(s.other, ind + "  ", types)
                 out.append(f"{ind}}}")
+            elif isinstance(s, Contrib) and s.kind == "V":
+                # V(a,b) <+ e: the branch row collects -e (its orientation folded in)
+                res, charges = split_ddt(s.expr, s.line)
+                sg = "-=" if self.a.branch_sign(s.a, s.b, s.line) > 0 else "+="
+                nb = self.a.nb
+                if res is not None:
+                    out.append(f"{ind}Fi[{nb}] {sg} D({self.x(res)});")
+                for c_sg, t in charges:
+                    op = sg if c_sg > 0 else ("+=" if sg == "-=" else "-=")
+                    out.append(f"{ind}Fq[{nb}] {op} D({self.x(t)});")
             elif isinstance(s, Contrib):
                 res, charges = split_ddt(s.expr, s.line)
                 ia = self.a.port[s.a]
@@ -559,6 +630,14 @@ class _Emitter:
             L.append(f"  const double p__given_{g} = P[{len(m.params) + j} * ps];")
         for v, t in m.module.variables.items():
             L.append(f"  D v_{v}(0.0);" if t == "real" else f"  double v_{v} = 0.0;")
+        if self.a.vbranch is not None:
+            va_, vb_ = self.a.vbranch
+            ia, nb = self.a.port[va_], self.a.nb
+            if vb_ is None:
+                L.append(f"  Fi[{ia}] -= V[{nb}]; Fi[{nb}] += V[{ia}];")
+            else:
+                ib = self.a.port[vb_]
+                L.append(f"  Fi[{ia}] -= V[{nb}]; Fi[{ib}] += V[{nb}]; Fi[{nb}] += V[{ia}] - V[{ib}];")
         L += self.stmts(m.module.body, "  ")
         L.append("  (void)c; (void)V; (void)Fi; (void)Fq; (void)P; (void)ps;")
         L.append("}")
@@ -588,7 +667,7 @@ class _Emitter:
         return "\n\n".join(out)
 
     def dtype(self) -> str:
-        n = self.m.nterm
+        n = self.m.nx
         return f"Dual<Dual<double, {n}>, {n}>" if self.m.second_order else f"Dual<double, {n}>"
 
     def prologue(self) -> List[str]:
@@ -597,8 +676,8 @@ class _Emitter:
         return [f"  typedef {self.dtype()} D;",
                 "  Ctx c;",
                 f"  c.m = dp[{P} * ds]; c.vt = dp[{P + 1} * ds]; c.temp = c.vt * {_lit(P_Q / P_K)}; c.gmin = gmin;",
-                f"  D V[{m.nterm}], Fi[{m.nterm}], Fq[{m.nterm}];",
-                f"  for (int k = 0; k < {m.nterm}; ++k) V[k] = Seed<D>::make(v[k], k);",
+                f"  D V[{m.nx}], Fi[{m.nx}], Fq[{m.nx}];",
+                f"  for (int k = 0; k < {m.nx}; ++k) V[k] = Seed<D>::make(v[k], k);",
                 f"  body_{m.name}<D>(dp, ds, c, V, Fi, Fq);"]
 
     def eval(self) -> str:
@@ -610,7 +689,7 @@ class _Emitter:
         o = 0
         for r in m.frows:
             if r in m.qrows:
-                qd = " + ".join(f"part(Fq[{r}], {k}) * vd[{k}]" for k in range(m.nterm))
+                qd = " + ".join(f"part(Fq[{r}], {k}) * vd[{k}]" for k in range(m.nx))
                 L.append(f"  out[{o}] = mf * (val(Fi[{r}]) + (xdot ? ({qd}) : cj * val(Fq[{r}])));")
             else:
                 L.append(f"  out[{o}] = mf * val(Fi[{r}]);")
@@ -630,7 +709,7 @@ class _Emitter:
 
     def full(self) -> str:
         m = self.m
-        n = m.nterm
+        n = m.nx
         L = [f"inline void full_{m.name}(const double *dp, int ds, const double *v, double gmin, double *fi, "
              f"double *fq, double *G, double *C) {{"]
         L += self.prologue()
@@ -667,6 +746,7 @@ def emit_header(models: List[Tuple[VAModel, _Analysis]], base_id: int) -> str:
         return f"static const {ctype} {name}[] = {{{', '.join(str(v) for v in vals)}}};"
 
     L.append(table("kNTerm", [m.nterm for m, _ in models]))
+    L.append(table("kHasBr", [m.has_br for m, _ in models]))
     L.append(table("kNPar", [m.npar for m, _ in models]))
     L.append(table("kNDPar", [m.ndpar for m, _ in models]))
     L.append(table("kNOut", [m.nout for m, _ in models]))

@@ -7,15 +7,17 @@ src/vasim.jl:128-180,347-412,663-875):
   parameter [real|integer] NAME = expr [from|exclude range] {, ...};
   real / integer variables (module or block scope);
   analog begin ... end with assignments, if / else, begin / end blocks,
-  current contributions I(a,b) <+ expr and I(a) <+ expr;
+  current contributions I(a,b) <+ expr and I(a) <+ expr; one voltage-contributed
+  branch V(a,b) <+ expr (a branch-current unknown; I(a,b) probes it);
   expressions: numbers with SI scale factors, + - * / ** unary - + !, comparisons,
   && || and ?:; V(a,b) / V(a) probes; exp ln log sqrt pow abs min max tanh sinh
   cosh sin cos tan atan atan2 asin acos hypot floor ceil limexp; ddt(expr) (additive
   in a contribution); ddx(expr, V(n)) / ddx(expr, V(a,b)); $vt, $vt(T),
   $temperature, $simparam("gmin"[, default]), $mfactor.
 Internal nodes (`electrical` names that are not ports) become extra device
-unknowns.  Voltage contributions, branch-current probes, analog functions, noise
-sources and events are outside the subset and raise VAError with the line number.
+unknowns.  Loops, output arguments of analog functions and more than one
+voltage-contributed branch are outside the subset and raise VAError with the
+line number.
 """
 from __future__ import annotations
 
@@ -263,9 +265,10 @@ class Name:
 
 
 @dataclass
-class Probe:            # V(a) or V(a, b)
+class Probe:            # V(a), V(a, b), or the branch current I(a, b)
     a: str
     b: Optional[str]
+    kind: str = "V"
 
 
 @dataclass
@@ -309,11 +312,12 @@ class Assign:
 
 
 @dataclass
-class Contrib:          # I(a[, b]) <+ expr
+class Contrib:          # I(a[, b]) <+ expr  or  V(a[, b]) <+ expr
     a: str
     b: Optional[str]
     expr: object
     line: int = 0
+    kind: str = "I"
 
 
 @dataclass
@@ -631,9 +635,7 @@ class Parser:
             self.take("<+")
             e = self.expr()
             self.take(";")
-            if kind == "V":
-                raise VAError(f"line {p.line}: voltage contributions V(...) <+ are not supported")
-            return [Contrib(a, b, e, p.line)]
+            return [Contrib(a, b, e, p.line, kind)]
         if p.kind == "id":
             name = self.take().text
             self.take("=")
@@ -733,7 +735,14 @@ class Parser:
                     self.take(")")
                     return Probe(a, b)
                 if p.text == "I":
-                    raise VAError(f"line {p.line}: branch-current probes I(...) are not supported")
+                    # branch-current probe: the current of a voltage-contributed branch
+                    a = self.ident()
+                    b = None
+                    if self.at(","):
+                        self.take(",")
+                        b = self.ident()
+                    self.take(")")
+                    return Probe(a, b, "I")
                 # noise sources take a name string after their power arguments
                 arg = self._sysarg if p.text in ("white_noise", "flicker_noise") else self.expr
                 args = []

@@ -88,7 +88,7 @@ static const int kHasBr[CEDAR_NMODELS] = {0, 0, 0, 1, 1, 0, 1, 0, 0, 0, 0};
 static const int kNumModels = CEDAR_NMODELS + cedar::va::kCount;
 static int model_nterm(int m) { return m < CEDAR_NMODELS ? kNTerm[m] : cedar::va::kNTerm[m - CEDAR_NMODELS]; }
 static int model_npar(int m) { return m < CEDAR_NMODELS ? kNPar[m] : cedar::va::kNPar[m - CEDAR_NMODELS]; }
-static int model_hasbr(int m) { return m < CEDAR_NMODELS ? kHasBr[m] : 0; }
+static int model_hasbr(int m) { return m < CEDAR_NMODELS ? kHasBr[m] : cedar::va::kHasBr[m - CEDAR_NMODELS]; }
 
 static bool load_circuit(const cedar_ckt_desc *d, Circuit &c, std::string &err) {
   if (!d || d->n_nodes < 0 || d->n_branch < 0 || d->n_groups < 0) { err = "bad desc"; return false; }
@@ -318,21 +318,23 @@ static void eval_circuit(const Circuit &c, const double *x, const EvalCtx &ctx, 
         default: {
           // Verilog-A model: dense residuals and partials of one device from the
           // emitted code (derived block = parameters, m, thermal voltage)
-          const int k = g.model - CEDAR_NMODELS, nt = g.nt;
+          // (idx / nin: the terminals, then the branch current of a module with a
+          // voltage-contributed branch)
+          const int k = g.model - CEDAR_NMODELS, nx = nin;
           double dp[64], v[8], fi[8], fq[8], G[64], Cm[64];
           for (int q = 0; q < g.np; ++q) dp[q] = g.p(q, i);
           dp[g.np] = Vt;
-          for (int q = 0; q < nt; ++q) v[q] = X(tm[q]);
+          for (int q = 0; q < nx; ++q) v[q] = X(idx[q]);
           cedar::va::full(k, dp, 1, v, c.gmin, fi, fq, G, Cm);
           const double m = g.p(g.np - 1, i);
-          for (int r = 0; r < nt; ++r) {
-            const int row = tm[r];
+          for (int r = 0; r < nx; ++r) {
+            const int row = idx[r];
             if (row < 0) continue;
             o.Fi[row] += m * fi[r]; o.Fq[row] += m * fq[r];
-            for (int q = 0; q < nt; ++q) {
-              if (tm[q] < 0) continue;
-              o.G[(size_t)row * o.n + tm[q]] += m * G[r * nt + q];
-              o.C[(size_t)row * o.n + tm[q]] += m * Cm[r * nt + q];
+            for (int q = 0; q < nx; ++q) {
+              if (idx[q] < 0) continue;
+              o.G[(size_t)row * o.n + idx[q]] += m * G[r * nx + q];
+              o.C[(size_t)row * o.n + idx[q]] += m * Cm[r * nx + q];
             }
           }
         } break;

@@ -160,8 +160,12 @@ class Interp:
                  given=()):
         self.mod = module
         nodes = list(module.ports) + list(getattr(module, "internals", []))
-        self.N = len(nodes)
         self.port = {p: k for k, p in enumerate(nodes)}
+        # a voltage-contributed branch V(a,b) <+ ... adds its current as one more
+        # unknown after the nodes
+        self.vbranch = _voltage_branch(module.body)
+        self.nb = len(nodes) if self.vbranch is not None else None
+        self.N = len(nodes) + (1 if self.vbranch is not None else 0)
         self.params = {}
         for p in module.params:
             val = params[p.name]
@@ -191,8 +195,25 @@ class Interp:
         from importlib import import_module
         P = import_module("cedarsim_gb300.va.parser")
         self.P = P
+        if self.vbranch is not None:
+            # the branch current flows a -> b; the branch row starts at V(a) - V(b)
+            a, b = self.vbranch
+            ib = self.V[self.nb]
+            va_ = self.V[self.port[a]]
+            vb_ = self.V[self.port[b]] if b is not None else 0.0
+            self.Fi[self.port[a]] = self.Fi[self.port[a]] - ib
+            if b is not None:
+                self.Fi[self.port[b]] = self.Fi[self.port[b]] + ib
+            self.Fi[self.nb] = self.Fi[self.nb] + (va_ - vb_)
         self.block(self.mod.body)
         return self.Fi, self.Fq
+
+    def _orient(self, a, b) -> int:
+        if (a, b) == self.vbranch:
+            return 1
+        if b is not None and (b, a) == self.vbranch:
+            return -1
+        raise ValueError(f"I({a}, {b}) is not the voltage-contributed branch")
 
     def expr(self, e):
         P = self.P
@@ -203,6 +224,8 @@ class Interp:
                 return self.params[e.id]
             return self.vars[e.id]
         if isinstance(e, P.Probe):
+            if getattr(e, "kind", "V") == "I":
+                return self.V[self.nb] * float(self._orient(e.a, e.b))
             a = self.V[self.port[e.a]]
             return a if e.b is None else a - self.V[self.port[e.b]]
         if isinstance(e, P.Unary):
@@ -324,6 +347,12 @@ class Interp:
                     self.vars[s.name] = self._dual(x)
             elif isinstance(s, P.If):
                 self.block(s.then if value(self.expr(s.c)) != 0 else s.other)
+            elif isinstance(s, P.Contrib) and getattr(s, "kind", "I") == "V":
+                x = self.expr(s.expr)
+                q = x if isinstance(x, _Q) else _Q(x, 0.0)
+                sg = float(self._orient(s.a, s.b))
+                self.Fi[self.nb] = self.Fi[self.nb] - self._dual(q.r) * sg
+                self.Fq[self.nb] = self.Fq[self.nb] - self._dual(q.q) * sg
             elif isinstance(s, P.Contrib):
                 x = self.expr(s.expr)
                 q = x if isinstance(x, _Q) else _Q(x, 0.0)
@@ -335,6 +364,17 @@ class Interp:
                 if ib is not None:
                     self.Fi[ib] = self.Fi[ib] + r
                     self.Fq[ib] = self.Fq[ib] + c
+
+
+def _voltage_branch(stmts):
+    for s in stmts:
+        if type(s).__name__ == "If":
+            br = _voltage_branch(s.then) or _voltage_branch(s.other)
+            if br:
+                return br
+        elif type(s).__name__ == "Contrib" and getattr(s, "kind", "I") == "V":
+            return (s.a, s.b)
+    return None
 
 
 def _atan2_general(y, x):

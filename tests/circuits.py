@@ -210,3 +210,25 @@ def va_vccs(pkg):
     c.R("RE", "e", "0", r=2e3)
     c.C("CE", "e", "0", 50e-15)
     return c
+
+
+def butterworth_va(pkg):
+    """test/transients.jl:129-179's third-order Butterworth with its inductors as
+    the Verilog-A voltage-branch model."""
+    c = pkg.Circuit()
+    c.V("V1", "vin", "0", wave=pkg.Sin(0.0, 1.0, 1.0 / (2 * math.pi)))
+    c.va("L1", "va_inductor", ["vin", "n1"], L=1.5); c.C("C2", "n1", "0", 4.0 / 3.0)
+    c.va("L3", "va_inductor", ["n1", "vout"], L=0.5); c.R("R4", "vout", "0", r=1.0)
+    return c
+
+
+def va_thevenin(pkg):
+    """A Verilog-A Thevenin source (1 V behind 50 Ohm) into a 50 Ohm load, with a
+    VA inductor and a capacitor after it for the transient."""
+    c = pkg.Circuit()
+    c.va("VT", "va_thevenin", ["a", "0"], VS=1.0, RS=50.0)
+    c.R("RL", "a", "0", r=50.0)
+    c.va("LX", "va_inductor", ["a", "b"], L=5e-9)
+    c.C("CB", "b", "0", 2e-12)
+    c.R("RB", "b", "0", r=1e3)
+    return c

@@ -19,6 +19,7 @@ CASES = {
     "va_nlvcr": K.va_nlvcr,
     "va_diode_rs": K.va_diode_rs,      # internal node
     "va_vccs": K.va_vccs,              # analog function, macros, case, $param_given
+    "va_thevenin": K.va_thevenin,      # voltage-contributed branches (source, inductor)
 }
 
 
@@ -49,7 +50,7 @@ def test_va_ddx_known_answer_on_gpu(gpu, pkg):
 
 
 @pytest.mark.parametrize("case, adaptive", [("va_mixed", False), ("va_chain_7", True), ("va_diode_rs", False),
-                                            ("va_vccs", False)])
+                                            ("va_vccs", False), ("va_thevenin", False)])
 def test_va_transient_parity(gpu, pkg, oracle, case, adaptive):
     """Fixed-step BDF2 (h = 1 ps) on the mixed circuit, adaptive BDF2 on the chain.
     The mixed circuit's 5k adaptive steps put some LTE tests within rounding of

@@ -66,7 +66,7 @@ def test_emitted_code_matches_interpreter(pkg, oracle, va, interp):
     lib = oracle.lib
     dp_ = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
     for k, m in enumerate(va.models()):
-        n = m.nterm
+        n = m.nx                  # terminals, then the branch current of a voltage branch
         for trial in range(60):
             prm = _params(m, rng)
             vals = m.defaults(prm)
@@ -206,7 +206,7 @@ def test_library_lists_the_models(pkg, va):
         assert lib.cedar_va_name(k, buf, 64) == 0 and buf.value.decode() == m.name
         mid = va.BASE_ID + k
         assert lib.cedar_model_nterm(mid) == m.nterm and lib.cedar_model_npar(mid) == m.npar
-        assert lib.cedar_model_has_branch(mid) == 0
+        assert lib.cedar_model_has_branch(mid) == m.has_br
     assert lib.cedar_va_name(len(va.models()), buf, 64) != 0
     assert lib.cedar_model_nterm(va.BASE_ID + len(va.models())) == -1
 
@@ -214,7 +214,8 @@ def test_library_lists_the_models(pkg, va):
 @pytest.mark.parametrize("src, msg", [
     ("module m(a, b); inout a, b; electrical a, b, x1, x2, x3, x4; analog I(a, b) <+ V(a, b); endmodule",
      "at most"),
-    ("module m(a, b); inout a, b; electrical a, b; analog V(a, b) <+ 1.0; endmodule", "voltage contributions"),
+    ("module m(a, b); inout a, b; electrical a, b; integer i; analog begin for (i = 0; i < 2; i = i + 1) "
+     "I(a, b) <+ V(a, b); end endmodule", "expected ="),
     ("module m(a, b); inout a, b; electrical a, b; analog I(a, b) <+ foo(V(a, b)); endmodule", "unsupported function"),
     ("module m(a, b); inout a, b; electrical a, b; analog I(a, b) <+ V(a, b) * ddt(V(a, b)); endmodule", "additive"),
     ("module m(a, b); inout a, b; electrical a, b; analog I(a, c) <+ V(a, b); endmodule", "not a port"),
@@ -354,3 +355,51 @@ def test_preprocessor_and_statement_forms(va):
           analog I(p) <+ f(V(p)); endmodule"""
         for mm in va.parse(src2):
             analyze(mm)
+
+
+def test_voltage_branch_models(pkg, oracle, va):
+    """V(a,b) <+ contributions add a branch-current unknown "<instance>.I":
+    va_inductor is the built-in inductor (same F, G, C with m = 1), the Butterworth
+    of test/transients.jl built with it meets the same analytic answer, and the
+    Thevenin source divides 1 V over its 50 Ohm and the load."""
+    import json
+    m = va.model(va.model_id("va_inductor"))
+    assert m.has_br == 1 and m.nx == 3
+    fb, fv = K.butterworth(pkg).flatten(), K.butterworth_va(pkg).flatten()
+    assert fb.names == fv.names
+    rng = np.random.default_rng(11)
+    for _ in range(20):
+        x = rng.uniform(-1.0, 1.0, fb.n)
+        xd = rng.normal(0, 1.0, fb.n)
+        Fb, Fib, Fqb, Gb, Cb = oracle.eval(fb, x, xd, t=0.7)
+        Fv, Fiv, Fqv, Gv, Cv = oracle.eval(fv, x, xd, t=0.7)
+        for a, b in ((Fiv, Fib), (Fqv, Fqb), (Gv, Gb), (Cv, Cb), (Fv, Fb)):
+            assert np.all(np.abs(a - b) <= 1e-14 * (np.abs(b) + 1.0))
+    gold = json.load(open(ROOT / "tests" / "golden" / "known_answers.json"))["butterworth"]
+    o = pkg.make_opts("bdf2", True, 0.0, 100.0, 0.0, False, reltol=1e-10, abstol_v=1e-12, abstol_i=1e-14, hmax=0.05)
+    t, X, st, rc = oracle.tran(fv, o, np.zeros(fv.n))
+    assert rc == 0 and st.status == 0
+    err = np.max(np.abs(X[:, fv.index("vout")] - np.array([K.butterworth_vout(tt) for tt in t])))
+    assert err < gold["max_abs_err"]
+    f = K.va_thevenin(pkg).flatten()
+    x, st, rc = oracle.dcop(f)
+    assert rc == 0
+    rp = 50.0 * 1e3 / (50.0 + 1e3)        # the inductor shorts RB across RL at DC
+    va_ = rp / (50.0 + rp)
+    assert x[f.index("a")] == pytest.approx(va_, rel=1e-12) and x[f.index("VT.I")] == pytest.approx(-va_ / rp, rel=1e-12)
+    assert x[f.index("LX.I")] == pytest.approx(x[f.index("b")] / 1e3, rel=1e-9)
+
+
+def test_voltage_branch_errors(va):
+    from cedarsim_gb300.va.emit import analyze
+    two = """module m(a, b, c); inout a, b, c; electrical a, b, c;
+      analog begin V(a, b) <+ 0; V(b, c) <+ 0; end endmodule"""
+    with pytest.raises(va.VAError, match="second voltage"):
+        analyze(va.parse(two)[0])
+    mixed = """module m(a, b); inout a, b; electrical a, b;
+      analog begin V(a, b) <+ 0; I(a, b) <+ V(a, b); end endmodule"""
+    with pytest.raises(va.VAError, match="current and voltage"):
+        analyze(va.parse(mixed)[0])
+    probe = """module m(a, b); inout a, b; electrical a, b; analog I(a, b) <+ I(a, b); endmodule"""
+    with pytest.raises(va.VAError, match="probes no voltage"):
+        analyze(va.parse(probe)[0])
