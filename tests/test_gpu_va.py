@@ -128,3 +128,16 @@ def test_va_ac_parity(gpu, pkg, oracle):
     # relative to the largest probed magnitude at each frequency, as the AC parity tests
     err = np.max(np.abs(r - ro) / np.max(np.abs(ro), axis=1, keepdims=True))
     assert err <= 1e-9
+
+
+def test_va_inductor_butterworth_transient(gpu, pkg, oracle):
+    """The Butterworth filter of test/transients.jl with Verilog-A inductors
+    (voltage-contributed branches with ddt(L I)): GPU against the oracle,
+    fixed-step BDF2 over four periods of the drive."""
+    flat = K.butterworth_va(pkg).flatten()
+    o = pkg.make_opts("bdf2", False, 0.0, 25.0, 0.01, False)
+    sol = pkg.tran(flat, (0.0, 25.0), method="bdf2", h=0.01, adaptive=False, dcop=False,
+                   x0=np.zeros(flat.n))
+    t_ref, x_ref, st, rc = oracle.tran(flat, o, np.zeros(flat.n))
+    assert rc == 0 and sol.retcode == "OK" and sol.stats["accepted"] == st.accepted == 2500
+    assert compare_waves(sol, t_ref, x_ref, flat.n_nodes) <= 1.0
