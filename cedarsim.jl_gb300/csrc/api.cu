@@ -683,6 +683,33 @@ int cedar_noise(cedar_ckt *c, const double *x_op, int32_t n_freq, const double *
       nw.push_back(m * m * kT4 / r);
     }
   }
+  // white_noise sources of Verilog-A devices: their powers at x_op from the
+  // emitted device code run on the host, weight m^2 pwr (the contribution is
+  // scaled by m, src/simulate_ir.jl:54), across the contribution's branch
+  const double vt = thermal_voltage(H.temp_c);
+  for (const GroupInfo &g : H.groups) {
+    const int k = g.model - va::kBase;
+    if (k < 0 || k >= va::kCount) continue;
+    const int n0 = va::kNoisePtr[k], nn = va::kNoisePtr[k + 1] - n0;
+    if (nn == 0) continue;
+    const int np = va::kNPar[k];
+    std::vector<double> dp(np + 1), pw(nn);
+    double v[8] = {0};
+    for (int i = 0; i < g.n_inst; ++i) {
+      for (int q = 0; q < np; ++q) dp[q] = H.par[g.par_off + (size_t)q * g.n_inst + i];
+      dp[np] = vt;
+      const int *t = &H.term_orig[g.term_off + (size_t)i * g.ntx];
+      for (int q = 0; q < g.ntx && q < 8; ++q) v[q] = t[q] < 0 ? 0.0 : x_op[t[q]];
+      va::noise(k, dp.data(), 1, v, H.gmin, pw.data());
+      const double m = dp[np - 1];
+      for (int j = 0; j < nn; ++j) {
+        const int pa = va::kNoise[2 * (n0 + j)], pb = va::kNoise[2 * (n0 + j) + 1];
+        na.push_back(t[pa]);
+        nb.push_back(pb >= 0 ? t[pb] : -1);
+        nw.push_back(m * m * pw[j]);
+      }
+    }
+  }
   AcDev a{};
   int rc = ac_prepare(c, x_op, n_freq, omega, a);
   if (rc) return rc;

@@ -266,6 +266,13 @@ VA_HD auto vsel(bool c, const A &a, const B &b) -> decltype(a + b) {
   return c ? decltype(a + b)(a) : decltype(a + b)(b);
 }
 
+// white_noise(pwr): zero in every analysis but noise; a noise evaluation passes
+// nz and collects the source's power there
+VA_HD double va_noise(double *nz, int j, double pwr) {
+  if (nz) nz[j] += pwr;
+  return 0.0;
+}
+
 // Real to integer conversion (VA-LRM 4.2.1.1: round half away from zero) and
 // integer division (truncation toward zero)
 VA_HD double vint(double x) { return round(x); }

@@ -51,6 +51,7 @@ class VAModel:
     flops: int
     given: List[str] = dataclasses.field(default_factory=list)   # parameters queried by $param_given
     vbranch: Optional[Tuple[str, Optional[str]]] = None  # the voltage-contributed branch (a, b), if any
+    noise: List[Tuple[int, int]] = dataclasses.field(default_factory=list)  # white_noise sources: (a, b or -1)
 
     @property
     def internals(self) -> List[str]:
@@ -179,6 +180,8 @@ class _Analysis:
         if self.vbranch is not None:
             self.nb = len(self.port)
         self.given: List[str] = []          # parameters queried by $param_given, in order of use
+        self.noise: List[Tuple[int, int]] = []
+        self.noise_index: Dict[int, int] = {}
         self.contribs: List[Tuple[Contrib, Optional[object], List[Tuple[int, object]]]] = []
 
     def _find_vbranch(self, stmts):
@@ -256,6 +259,35 @@ class _Analysis:
             return out
         raise VAError(f"{self.mod.name}: unsupported expression {e!r}")
 
+    def collect_noise(self, stmts):
+        """white_noise(pwr) terms of current contributions: noise current sources
+        across the contribution's branch, numbered in source order."""
+        def calls(e, out):
+            if isinstance(e, Call):
+                if e.fn == "white_noise":
+                    out.append(e)
+                for a in e.args:
+                    calls(a, out)
+            elif isinstance(e, Unary):
+                calls(e.x, out)
+            elif isinstance(e, Bin):
+                calls(e.a, out)
+                calls(e.b, out)
+            elif isinstance(e, Cond):
+                calls(e.c, out)
+                calls(e.a, out)
+                calls(e.b, out)
+        for s in stmts:
+            if isinstance(s, If):
+                self.collect_noise(s.then)
+                self.collect_noise(s.other)
+            elif isinstance(s, Contrib) and s.kind == "I":
+                found = []
+                calls(s.expr, found)
+                for c in found:
+                    self.noise_index[id(c)] = len(self.noise)
+                    self.noise.append((self.port[s.a], self.port[s.b] if s.b is not None else -1))
+
     def walk(self, stmts, collect: bool):
         for s in stmts:
             if isinstance(s, Assign):
@@ -282,6 +314,7 @@ class _Analysis:
                 self.deps(s.expr)
 
     def run(self):
+        self.collect_noise(self.mod.body)
         # dependency sets of variables to a fixed point (flow-insensitive)
         for _ in range(len(self.vars) + 2):
             before = dict(self.var_deps)
@@ -424,7 +457,7 @@ def analyze(mod: Module) -> Tuple[VAModel, _Analysis]:
     for f in mod.functions.values():
         _check_function(mod, f)
     m = VAModel(mod.name, mod, list(mod.ports), list(mod.params), a.second_order, sorted(frows), sorted(gents),
-                sorted(qrows), sorted(cents), flops, list(a.given), a.vbranch)
+                sorted(qrows), sorted(cents), flops, list(a.given), a.vbranch, list(a.noise))
     if m.nout == 0:
         raise VAError(f"{mod.name}: the analog block makes no contribution")
     m.defaults()  # defaults must evaluate and satisfy their ranges
@@ -545,8 +578,13 @@ class _Emitter:
                 # two-node probe: the mean of the two one-sided partials, as
                 # CedarSim defines it (src/vasim.jl:400-411)
                 return f"((ddx({inner}, {ia}) - ddx({inner}, {self.a.port[p.b]})) * 0.5)"
-            if e.fn in ("white_noise", "flicker_noise"):
-                return "0.0"           # noise sources are zero in DC, transient and AC
+            if e.fn == "white_noise":
+                # zero in DC, transient and AC; a noise evaluation records its power
+                if id(e) not in self.a.noise_index:
+                    raise VAError(f"{self.m.name}: line {e.line}: white_noise() outside a current contribution")
+                return f"va_noise(nz, {self.a.noise_index[id(e)]}, val({self.x(e.args[0])}))"
+            if e.fn == "flicker_noise":
+                return "0.0"           # (not part of the noise analysis)
             if e.fn in self.a.funcs:
                 f = self.a.funcs[e.fn]
                 if len(e.args) != len(f.inputs):
@@ -623,7 +661,8 @@ class _Emitter:
         m = self.m
         L = [f"// module {m.name}({', '.join(m.ports)})" + (f", internal {', '.join(m.internals)}" if m.internals else ""),
              "template <class D>",
-             f"VA_HD void body_{m.name}(const double *P, int ps, const Ctx &c, const D *V, D *Fi, D *Fq) {{"]
+             f"VA_HD void body_{m.name}(const double *P, int ps, const Ctx &c, const D *V, D *Fi, D *Fq, "
+             f"double *nz) {{"]
         for k, p in enumerate(m.params):
             L.append(f"  const double p_{p.name} = P[{k} * ps];")
         for j, g in enumerate(m.given):
@@ -639,7 +678,7 @@ class _Emitter:
                 ib = self.a.port[vb_]
                 L.append(f"  Fi[{ia}] -= V[{nb}]; Fi[{ib}] += V[{nb}]; Fi[{nb}] += V[{ia}] - V[{ib}];")
         L += self.stmts(m.module.body, "  ")
-        L.append("  (void)c; (void)V; (void)Fi; (void)Fq; (void)P; (void)ps;")
+        L.append("  (void)c; (void)V; (void)Fi; (void)Fq; (void)P; (void)ps; (void)nz;")
         L.append("}")
         return "\n".join(L)
 
@@ -670,7 +709,7 @@ class _Emitter:
         n = self.m.nx
         return f"Dual<Dual<double, {n}>, {n}>" if self.m.second_order else f"Dual<double, {n}>"
 
-    def prologue(self) -> List[str]:
+    def prologue(self, nz: str = "nullptr") -> List[str]:
         m = self.m
         P = m.npar - 1                 # position of m in the derived block (vt follows)
         return [f"  typedef {self.dtype()} D;",
@@ -678,7 +717,7 @@ class _Emitter:
                 f"  c.m = dp[{P} * ds]; c.vt = dp[{P + 1} * ds]; c.temp = c.vt * {_lit(P_Q / P_K)}; c.gmin = gmin;",
                 f"  D V[{m.nx}], Fi[{m.nx}], Fq[{m.nx}];",
                 f"  for (int k = 0; k < {m.nx}; ++k) V[k] = Seed<D>::make(v[k], k);",
-                f"  body_{m.name}<D>(dp, ds, c, V, Fi, Fq);"]
+                f"  body_{m.name}<D>(dp, ds, c, V, Fi, Fq, {nz});"]
 
     def eval(self) -> str:
         m = self.m
@@ -704,6 +743,16 @@ class _Emitter:
             L.append(f"  out[{o}] = cj * (mf * part(Fq[{r}], {k}));")
             o += 1
         L.append("  (void)vd; (void)xdot; (void)cj;")
+        L.append("}")
+        return "\n".join(L)
+
+    def noise(self) -> str:
+        """Powers (A^2/Hz, unscaled by m) of the module's white_noise sources at v."""
+        m = self.m
+        L = [f"inline int noise_{m.name}(const double *dp, int ds, const double *v, double gmin, double *pw) {{",
+             f"  for (int j = 0; j < {len(m.noise)}; ++j) pw[j] = 0.0;"]
+        L += self.prologue("pw")
+        L.append(f"  return {len(m.noise)};")
         L.append("}")
         return "\n".join(L)
 
@@ -740,6 +789,8 @@ def emit_header(models: List[Tuple[VAModel, _Analysis]], base_id: int) -> str:
         e = _Emitter(m, a)
         fns = e.functions()
         L += ([fns, ""] if fns else []) + [e.body(), "", e.eval(), "", e.full(), ""]
+        if m.noise:
+            L += [e.noise(), ""]
 
     def table(name, vals, ctype="int"):
         vals = list(vals) or [0]
@@ -768,6 +819,14 @@ def emit_header(models: List[Tuple[VAModel, _Analysis]], base_id: int) -> str:
             st += [3, r, k, o]; o += 1
         ptr.append(len(st) // 4)
     L.append(table("kStamps", st))
+    # white_noise sources: per model, (row port, column port or -1) pairs
+    nzs, nzp = [], [0]
+    for m, _ in models:
+        for a_, b_ in m.noise:
+            nzs += [a_, b_]
+        nzp.append(len(nzs) // 2)
+    L.append(table("kNoise", nzs))
+    L.append(table("kNoisePtr", nzp))
     L.append(table("kStampPtr", ptr))
     L.append("")
     # device-side dispatch (switches over a warp-uniform model id)
@@ -794,6 +853,16 @@ def emit_header(models: List[Tuple[VAModel, _Analysis]], base_id: int) -> str:
     L.append("    default: break;")
     L.append("  }")
     L.append("  (void)dp; (void)ds; (void)v; (void)vd; (void)xdot; (void)cj; (void)gmin; (void)out;")
+    L.append("}")
+    L.append("inline int noise(int k, const double *dp, int ds, const double *v, double gmin, double *pw) {")
+    L.append("  switch (k) {")
+    for i, (m, _) in enumerate(models):
+        if m.noise:
+            L.append(f"    case {i}: return noise_{m.name}(dp, ds, v, gmin, pw);")
+    L.append("    default: break;")
+    L.append("  }")
+    L.append("  (void)dp; (void)ds; (void)v; (void)gmin; (void)pw;")
+    L.append("  return 0;")
     L.append("}")
     L.append("inline void full(int k, const double *dp, int ds, const double *v, double gmin, double *fi, double *fq, "
              "double *G, double *C) {")

@@ -68,6 +68,8 @@ def load(pkg):
     lib.oracle_n_params.argtypes = [cd_p]
     lib.oracle_va_full.restype = C.c_int
     lib.oracle_va_full.argtypes = [C.c_int, dp, dp, C.c_double, dp, dp, dp, dp]
+    lib.oracle_va_noise.restype = C.c_int
+    lib.oracle_va_noise.argtypes = [C.c_int, dp, dp, C.c_double, dp]
     lib.oracle_last_error.restype = C.c_int
     lib.oracle_last_error.argtypes = [C.c_char_p, C.c_size_t]
     _lib = lib
@@ -121,11 +123,16 @@ class Oracle:
     def noise(self, flat, x_op, omegas, probe):
         """Output PSD at `probe` (PSD, src/ac.jl:263-283): one direct solve per
         resistor thermal-noise current, pwr = 4 k T / r (src/simpledevices.jl:70-75),
-        scaled by the multiplicity like the branch current (src/simulate_ir.jl:54)."""
+        and per white_noise source of a Verilog-A device (its power at x_op from
+        the interpreter), scaled by the multiplicity like the branch current
+        (src/simulate_ir.jl:54)."""
         _, _, _, G, Cm = self.eval(flat, x_op, dc=True)
         n = flat.n
         kT4 = 4.0 * 1.380649e-23 * (flat.temp_c + 273.15)
         cols, pwr = [], []
+        for inj, pw in self._va_noise(flat, x_op):
+            cols.append(inj)
+            pwr.append(pw)
         for (model, term, br, par) in flat.groups:
             if model != 1:
                 continue
@@ -145,6 +152,40 @@ class Oracle:
         for k, w in enumerate(omegas):
             H = np.linalg.solve(G + 1j * w * Cm, INJ)[probe]
             out[k] = float(np.sum(pwr * np.abs(H) ** 2))
+        return out
+
+    def _va_noise(self, flat, x_op):
+        """Injection vectors and powers (m^2 pwr) of the Verilog-A devices'
+        white_noise sources at x_op, from the independent interpretation of
+        their modules (oracle/va_interp.py)."""
+        import importlib.util
+        va = self.pkg.va
+        spec = importlib.util.spec_from_file_location("cedar_va_interp", HERE / "va_interp.py")
+        vi = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(vi)
+        vt = 1.380649e-23 * (flat.temp_c + 273.15) / 1.602176634e-19
+        out = []
+        for (model, term, br, par) in flat.groups:
+            if model < va.BASE_ID:
+                continue
+            m = va.model(model)
+            if not m.noise:
+                continue
+            names = [p.name for p in m.params]
+            for i in range(par.shape[1]):
+                vals = par[:, i]
+                prm = dict(zip(names, vals[:len(names)]))
+                given = [g for j, g in enumerate(m.given) if vals[len(names) + j] != 0.0]
+                idx = list(term[i]) + ([int(br[i])] if br is not None else [])
+                v = [x_op[u] if u >= 0 else 0.0 for u in idx]
+                mult = vals[-1]
+                for (a, b), pw in vi.noise_sources(m.module, prm, v, vt, flat.gmin, mult, given):
+                    inj = np.zeros(flat.n)
+                    if idx[a] >= 0:
+                        inj[idx[a]] += mult
+                    if b >= 0 and idx[b] >= 0:
+                        inj[idx[b]] -= mult
+                    out.append((inj, pw))
         return out
 
     def dcop(self, flat, t=0.0, x0=None, opts=None):

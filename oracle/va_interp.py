@@ -181,6 +181,8 @@ class Interp:
         self.vars = {name: (0 if t == "integer" else self._const(0.0)) for name, t in module.variables.items()}
         self.types = dict(module.variables)
         self.given = set(given)
+        self.noise = []             # ((a index, b index or -1), power) of each white_noise evaluated
+        self._branch = None
         self.Fi = [self._const(0.0) for _ in range(N)]
         self.Fq = [self._const(0.0) for _ in range(N)]
 
@@ -262,8 +264,13 @@ class Interp:
             return self.expr(e.a) if value(self.expr(e.c)) != 0 else self.expr(e.b)
         if isinstance(e, P.Call):
             fn = e.fn
-            if fn in ("white_noise", "flicker_noise"):
-                return 0.0                      # noise sources: zero outside a noise analysis
+            if fn == "white_noise":
+                # zero outside a noise analysis; record the source across the
+                # branch of the contribution being evaluated
+                self.noise.append((self._branch, value(self.expr(e.args[0]))))
+                return 0.0
+            if fn == "flicker_noise":
+                return 0.0
             if fn in getattr(self.mod, "functions", {}):
                 return self._call(self.mod.functions[fn], [self.expr(a) for a in e.args])
             if fn == "ddt":
@@ -354,6 +361,7 @@ class Interp:
                 self.Fi[self.nb] = self.Fi[self.nb] - self._dual(q.r) * sg
                 self.Fq[self.nb] = self.Fq[self.nb] - self._dual(q.q) * sg
             elif isinstance(s, P.Contrib):
+                self._branch = (self.port[s.a], self.port[s.b] if s.b is not None else -1)
                 x = self.expr(s.expr)
                 q = x if isinstance(x, _Q) else _Q(x, 0.0)
                 ia = self.port[s.a]
@@ -395,3 +403,12 @@ def evaluate(module, params: Dict[str, float], v: List[float], vt: float, gmin: 
     G = [[value(Fi[r].v.d[k]) for k in range(N)] for r in range(N)]
     Cm = [[value(Fq[r].v.d[k]) for k in range(N)] for r in range(N)]
     return fi, fq, G, Cm
+
+
+def noise_sources(module, params: Dict[str, float], v: List[float], vt: float, gmin: float, m: float = 1.0,
+                  given=()):
+    """[((a, b), power)] of the module's white_noise sources at port potentials v
+    (b = -1 for ground), unscaled by the multiplicity."""
+    it = Interp(module, params, v, vt, gmin, m, given)
+    it.run()
+    return it.noise

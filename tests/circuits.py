@@ -232,3 +232,13 @@ def va_thevenin(pkg):
     c.C("CB", "b", "0", 2e-12)
     c.R("RB", "b", "0", r=1e3)
     return c
+
+
+def butterworth_ac_va(pkg):
+    """butterworth_ac with its two 2-Ohm load halves as Verilog-A resistors
+    (thermal noise through white_noise)."""
+    c = pkg.Circuit(temp_c=23.0, gmin=0.0)
+    c.V("V1", "vin", "0", wave=pkg.Sin(0.0, 1.0, 1.0 / (2 * math.pi)), ac=1.0)
+    c.L("L1", "vin", "n1", 1.5); c.C("C2", "n1", "0", 4.0 / 3.0); c.L("L3", "n1", "vout", 0.5)
+    c.va("R4", "va_resistor", ["vout", "0"], R=2.0); c.va("R5", "va_resistor", ["vout", "0"], R=2.0)
+    return c

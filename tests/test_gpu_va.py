@@ -141,3 +141,27 @@ def test_va_inductor_butterworth_transient(gpu, pkg, oracle):
     t_ref, x_ref, st, rc = oracle.tran(flat, o, np.zeros(flat.n))
     assert rc == 0 and sol.retcode == "OK" and sol.stats["accepted"] == st.accepted == 2500
     assert compare_waves(sol, t_ref, x_ref, flat.n_nodes) <= 1.0
+
+
+def test_va_white_noise_psd(gpu, pkg, oracle):
+    """cedar_noise with Verilog-A white_noise sources (the Butterworth of
+    test/ac.jl with VA resistors; the saturating transconductor's channel noise):
+    against the oracle, and the filter against the reference's ngspice table."""
+    import json
+    import pathlib
+    fv = K.butterworth_ac_va(pkg).flatten()
+    x = pkg.dc(fv)
+    w = 2 * np.pi * pkg.acdec(20, 0.01, 10)
+    psd = pkg.noise(fv, x_op=x).psd("vout", w)
+    po = oracle.noise(fv, x, w, fv.index("vout"))
+    np.testing.assert_allclose(psd, po, rtol=1e-9)
+    g = json.loads((pathlib.Path(__file__).with_name("golden") / "ac_noise_ngspice.json").read_text())
+    ref = np.array(g["sqrt_psd"])
+    assert np.all(np.abs(np.sqrt(psd) - ref) <= 1e-6 * np.maximum(np.abs(ref), np.abs(np.sqrt(psd))))
+    fc = K.va_vccs(pkg).flatten()
+    xc = pkg.dc(fc)
+    wc = 2 * np.pi * pkg.acdec(5, 1e6, 1e11)
+    pc = pkg.noise(fc, x_op=xc).psd("e", wc)
+    pco = oracle.noise(fc, xc, wc, fc.index("e"))
+    np.testing.assert_allclose(pc, pco, rtol=1e-9)
+    assert np.all(pc > 0)

@@ -403,3 +403,38 @@ def test_voltage_branch_errors(va):
     probe = """module m(a, b); inout a, b; electrical a, b; analog I(a, b) <+ I(a, b); endmodule"""
     with pytest.raises(va.VAError, match="probes no voltage"):
         analyze(va.parse(probe)[0])
+
+
+def test_white_noise_sources(pkg, oracle, va, interp):
+    """white_noise powers from the emitted code equal the interpreter's; the
+    Butterworth of test/ac.jl with Verilog-A resistors (thermal noise written as
+    white_noise(4 k T / R)) gives the built-in resistors' PSD and the reference's
+    ngspice table (rtol 1e-6, test/ac.jl:148-149)."""
+    import json
+    lib = oracle.lib
+    dp_ = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    rng = np.random.default_rng(17)
+    for name in ("va_resistor", "va_vccs_sat"):
+        k = va.model_id(name) - va.BASE_ID
+        m = va.models()[k]
+        assert len(m.noise) == 1
+        for _ in range(10):
+            prm = _params(m, rng)
+            vals = m.defaults(prm)
+            v = rng.uniform(-1, 1, m.nx)
+            pw = np.zeros(len(m.noise))
+            assert lib.oracle_va_noise(k, dp_(np.array(vals + [1.0, VT])), dp_(v), 1e-12, dp_(pw)) == len(m.noise)
+            src = interp.noise_sources(m.module, dict(zip([p.name for p in m.params], vals)), list(v), VT, 1e-12,
+                                       1.0, [g for g in m.given if g in prm])
+            assert [s[0] for s in src] == m.noise
+            assert pw[0] == pytest.approx(src[0][1], rel=1e-14)
+    fb, fv = K.butterworth_ac(pkg).flatten(), K.butterworth_ac_va(pkg).flatten()
+    x, _, rc = oracle.dcop(fb)
+    assert rc == 0
+    w = 2 * np.pi * pkg.acdec(20, 0.01, 10)
+    pb = oracle.noise(fb, x, w, fb.index("vout"))
+    pv = oracle.noise(fv, x, w, fv.index("vout"))
+    np.testing.assert_allclose(pv, pb, rtol=1e-12)
+    g = json.loads((ROOT / "tests" / "golden" / "ac_noise_ngspice.json").read_text())
+    ref = np.array(g["sqrt_psd"])
+    assert np.all(np.abs(np.sqrt(pv) - ref) <= 1e-6 * np.maximum(np.abs(ref), np.abs(np.sqrt(pv))))
