@@ -35,6 +35,9 @@ def load(pkg):
     global _lib
     if _lib is not None:
         return _lib
+    # the Verilog-A device code the oracle compiles in comes from the package's emitter
+    import importlib
+    importlib.import_module(pkg.__name__ + ".build").generate()
     build()
     lib = C.CDLL(str(LIB))
     abi = pkg.abi
