@@ -46,10 +46,11 @@ _TOKEN = re.compile(r"""
 SCALE = {"T": 1e12, "G": 1e9, "M": 1e6, "K": 1e3, "k": 1e3, "m": 1e-3, "u": 1e-6, "n": 1e-9, "p": 1e-12,
          "f": 1e-15, "a": 1e-18}
 
-# constants of the standard constants.vams header (physical constants, SI)
+# system tasks that only print or stop the simulator: compiled to nothing
 DISPLAY_TASKS = ("$strobe", "$display", "$write", "$monitor", "$debug", "$warning", "$info", "$error", "$fatal",
                  "$finish", "$stop")
 
+# constants of the standard constants.vams header (physical constants, SI)
 CONSTANTS = {"M_PI": 3.14159265358979323846, "M_TWO_PI": 6.28318530717958647652,
              "M_PI_2": 1.57079632679489661923, "M_E": 2.7182818284590452354,
              "P_Q": 1.602176634e-19, "P_K": 1.380649e-23, "P_CELSIUS0": 273.15,
