@@ -297,3 +297,29 @@ def test_sweep_broadcasts_host_logic(sw, pkg, oracle, monkeypatch):
     assert s.params.cload == 20e-15 and s.params.stages == 5 and s.u.shape == (7, 2)
     assert s.t[0] == 0.0 and s.t[-1] == 0.3e-9 and s.retcode == "OK"
     assert s["in"][-1] == pytest.approx(1.8)
+
+
+def test_sweep_over_verilog_a_parameters(sw, pkg, oracle, monkeypatch):
+    """A SerialSweep leaves the other variable at None (its default): through
+    ParamSim the circuit function does not set it, so $param_given sees it unset.
+    va_vccs_sat's gm is GMX where given, else GM; its output current into a 1 kOhm
+    load follows (host logic run by the oracle stand-in)."""
+    import math
+    import cedarsim_gb300.api as api
+    _OracleBatch.oracle = oracle
+    monkeypatch.setattr(api, "Batch", _OracleBatch)
+
+    def ckt(GM=None, GMX=None):
+        c = pkg.Circuit()
+        c.V("VC", "c", "0", dc=0.3)
+        kw = {k: v for k, v in (("GM", GM), ("GMX", GMX)) if v is not None}
+        c.va("G", "va_vccs_sat", ["0", "o", "c", "0"], VS=0.5, MODE=1, **kw)
+        c.R("RL", "o", "0", r=1e3)
+        return c
+    cs = sw.CircuitSweep(ckt, sw.SerialSweep(GMX=[2e-3], GM=[1e-3, 3e-3]))
+    pts = list(cs.iterator)
+    assert pts == [(("GM", None), ("GMX", 2e-3)), (("GM", 1e-3), ("GMX", None)), (("GM", 3e-3), ("GMX", None))]
+    sols = pkg.dc(cs, reltol=1e-10)
+    f = 0.5 * math.tanh(0.3 / 0.5)
+    for sol, gm in zip(sols.ravel(order="F"), (2e-3, 1e-3, 3e-3)):
+        assert sol["o"] == pytest.approx(gm * f * 1e3, rel=1e-9)
