@@ -46,9 +46,11 @@ _TOKEN = re.compile(r"""
 SCALE = {"T": 1e12, "G": 1e9, "M": 1e6, "K": 1e3, "k": 1e3, "m": 1e-3, "u": 1e-6, "n": 1e-9, "p": 1e-12,
          "f": 1e-15, "a": 1e-18}
 
-# system tasks that only print or stop the simulator: compiled to nothing
+# system tasks that only print, stop the simulator or advise its step control
+# ($bound_step, $discontinuity; the engines' LTE control and breakpoints stand
+# in for them): compiled to nothing
 DISPLAY_TASKS = ("$strobe", "$display", "$write", "$monitor", "$debug", "$warning", "$info", "$error", "$fatal",
-                 "$finish", "$stop")
+                 "$finish", "$stop", "$bound_step", "$discontinuity")
 
 # constants of the standard constants.vams header (physical constants, SI)
 CONSTANTS = {"M_PI": 3.14159265358979323846, "M_TWO_PI": 6.28318530717958647652,
@@ -719,6 +721,13 @@ class Parser:
                         self.take(",")
                         args.append(self._sysarg())
                 self.take(")")
+            if p.text == "$limit":
+                # $limit(x, "limiter", ...): Newton-step limiting, which a simulator
+                # may leave out (the engines' Newton has its own damping): the
+                # value is x itself
+                if not args or isinstance(args[0], str):
+                    raise VAError(f"line {p.line}: $limit needs an expression")
+                return args[0]
             if p.text not in ("$vt", "$temperature", "$simparam", "$mfactor", "$param_given", "$given"):
                 raise VAError(f"line {p.line}: unsupported system function {p.text}")
             return SysCall(p.text, args)

@@ -438,3 +438,20 @@ def test_white_noise_sources(pkg, oracle, va, interp):
     g = json.loads((ROOT / "tests" / "golden" / "ac_noise_ngspice.json").read_text())
     ref = np.array(g["sqrt_psd"])
     assert np.all(np.abs(np.sqrt(pv) - ref) <= 1e-6 * np.maximum(np.abs(ref), np.abs(np.sqrt(pv))))
+
+
+def test_limit_and_step_advice(va):
+    """$limit(x, ...) is x; $bound_step / $discontinuity compile to nothing."""
+    from cedarsim_gb300.va.emit import analyze
+    src = """module lim(a, c); inout a, c; electrical a, c; parameter real IS = 1e-14;
+      real vd;
+      analog begin
+        vd = $limit(V(a, c), "pnjlim", $vt, 0.6);
+        $bound_step(1e-12);
+        $discontinuity(0);
+        I(a, c) <+ IS * (limexp(vd / $vt) - 1.0);
+      end endmodule"""
+    m, _ = analyze(va.parse(src)[0])
+    assert m.gents == [(0, 0), (0, 1), (1, 0), (1, 1)]
+    body = va.parse(src)[0].body
+    assert len(body) == 2     # the assignment and the contribution
