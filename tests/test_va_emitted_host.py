@@ -1,0 +1,169 @@
+"""The Verilog-A emitter end to end on the host, for modules that are not shipped.
+
+Test-only modules that exercise the whole supported subset are emitted into a
+header, compiled with g++ into a small library, and their residuals, Jacobians
+and noise powers compared with the independent interpretation of the same
+parsed modules (oracle/va_interp.py) at random port potentials.  The device
+code the engines run is this same emitted C++."""
+import ctypes as C
+import importlib.util
+import pathlib
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = pathlib.Path(__file__).resolve().parent.parent
+CSRC = ROOT / "cedarsim.jl_gb300" / "csrc"
+VT = 1.380649e-23 * (27.0 + 273.15) / 1.602176634e-19
+
+SOURCES = r"""
+`include "disciplines.vams"
+`include "constants.vams"
+`define SQ(x) ((x) * (x))
+`define SOFTABS(x, e) sqrt(`SQ(x) + (e))
+`ifdef UNDEFINED_FLAG
+`define K0 0.0
+`else
+`define K0 0.25
+`endif
+
+// internal node, function, case, integer arithmetic, ternary, min / max
+module t_mix(a, b, c);
+  inout a, b, c;
+  electrical a, b, c, x;
+  parameter real G = 1m from (0:inf);
+  parameter real R = 100.0 from (0:inf);
+  parameter integer SEL = 1 from [0:3];
+  parameter real P = 1.5;
+  real u, w, s;
+  integer k;
+
+  analog function real soft;
+    input y, e;
+    real y, e, t;
+    begin
+      t = `SOFTABS(y, e);
+      soft = 0.5 * (y + t);
+    end
+  endfunction
+
+  analog begin
+    @(initial_step) $strobe("t_mix");
+    k = SEL / 2 + 7 / 2;          // integer division
+    u = V(a, x);
+    case (SEL)
+      0: w = G * u;
+      1, 2: w = G * soft(u, 1e-3) * `K0 * 4.0;
+      default: w = G * tanh(u) * (k > 3 ? 2.0 : 1.0);
+    endcase
+    s = min(V(b), max(V(c), -0.5)) + pow(abs(V(b, c)) + 1.0, P) * 1e-3;
+    I(a, x) <+ w + white_noise(4.0 * P_K * $temperature * G, "ch");
+    I(x, c) <+ V(x, c) / R + 1e-4 * atan2(V(b), 1.0 + `SQ(V(c))) + 1e-5 * hypot(V(a), V(b)) + 1e-4 * s;
+    I(b) <+ 1e-6 * limexp(V(b) * 10.0) + ddt(1e-12 * V(b) + 1e-13 * `SQ(V(b, c)));
+  end
+endmodule
+
+// voltage branch probing its own current, $param_given, ddt on the branch,
+// $limit, ddx on a single-node probe
+module t_branch(p, n, g);
+  inout p, n, g;
+  electrical p, n, g;
+  parameter real L = 1n from (0:inf);
+  parameter real RS = 5.0 from [0:inf);
+  parameter real K = 2.0;
+  real q, vg;
+  analog begin
+    vg = $limit(V(g), "fetlim", 0.0);
+    q = K * vg * vg;
+    if ($param_given(RS))
+      V(p, n) <+ RS * I(p, n) + ddt(L * I(p, n));
+    else
+      V(p, n) <+ 0.5 * ddx(q, V(g)) + ddt(L * I(p, n));
+    I(g) <+ V(g) * 1e-3;
+  end
+endmodule
+"""
+
+
+@pytest.fixture(scope="module")
+def emitted(pkg, tmp_path_factory):
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    import importlib
+    P = importlib.import_module("cedarsim_gb300.va.parser")
+    E = importlib.import_module("cedarsim_gb300.va.emit")
+    mods = sorted((E.analyze(m) for m in P.parse(SOURCES)), key=lambda ma: ma[0].name)
+    d = tmp_path_factory.mktemp("va_host")
+    (d / "va_models.gen.h").write_text(E.emit_header(mods, 11))
+    (d / "harness.cpp").write_text(
+        '#include <math.h>\n#include "va_models.gen.h"\n'
+        'extern "C" int h_full(int k, const double *dp, const double *v, double gmin, double *fi, double *fq,'
+        ' double *G, double *C) { cedar::va::full(k, dp, 1, v, gmin, fi, fq, G, C); return 0; }\n'
+        'extern "C" int h_noise(int k, const double *dp, const double *v, double gmin, double *pw)'
+        ' { return cedar::va::noise(k, dp, 1, v, gmin, pw); }\n')
+    lib = d / "libharness.so"
+    r = subprocess.run(["g++", "-O1", "-std=c++17", "-ffp-contract=off", "-shared", "-fPIC", "-I", str(CSRC), "-I",
+                        str(d), str(d / "harness.cpp"), "-o", str(lib)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    h = C.CDLL(str(lib))
+    dp = C.POINTER(C.c_double)
+    h.h_full.argtypes = [C.c_int, dp, dp, C.c_double, dp, dp, dp, dp]
+    h.h_noise.argtypes = [C.c_int, dp, dp, C.c_double, dp]
+    return h, [m for m, _ in mods]
+
+
+@pytest.fixture(scope="module")
+def interp():
+    spec = importlib.util.spec_from_file_location("cedar_va_interp_h", ROOT / "oracle" / "va_interp.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def test_emitted_host_code_matches_interpreter(emitted, interp):
+    h, models = emitted
+    rng = np.random.default_rng(123)
+    dp_ = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    for k, m in enumerate(models):
+        n = m.nx
+        assert (m.name, n) in (("t_branch", 4), ("t_mix", 4))
+        for trial in range(80):
+            over = {}
+            if m.name == "t_mix":
+                over = {"SEL": float(rng.integers(0, 4)), "P": float(rng.uniform(0.5, 2.5)),
+                        "G": float(rng.uniform(1e-4, 1e-2))}
+            elif rng.random() < 0.5:
+                over = {"RS": float(rng.uniform(0.0, 20.0))}
+            vals = m.defaults(over)
+            dp = np.array(vals + [1.0 + rng.integers(0, 2), VT])
+            v = rng.uniform(-1.5, 1.5, n)
+            fi, fq, G, Cm = np.zeros(n), np.zeros(n), np.zeros(n * n), np.zeros(n * n)
+            h.h_full(k, dp_(dp), dp_(v), 1e-12, dp_(fi), dp_(fq), dp_(G), dp_(Cm))
+            given = [g for g in m.given if g in over]
+            ri, rq, rG, rC = interp.evaluate(m.module, dict(zip([p.name for p in m.params], vals)), list(v), VT,
+                                             1e-12, float(dp[-2]), given)
+            ri, rq, rG, rC = map(np.asarray, (ri, rq, rG, rC))
+            assert np.all(np.abs(fi - ri) <= 1e-13 * (np.abs(ri).max() + 1e-30)), (m.name, over, fi, ri)
+            assert np.all(np.abs(fq - rq) <= 1e-13 * (np.abs(rq).max() + 1e-40)), (m.name, fq, rq)
+            assert np.all(np.abs(G - rG.ravel()) <= 1e-12 * (np.abs(rG).max() + 1e-30)), (m.name, over, G, rG)
+            assert np.all(np.abs(Cm - rC.ravel()) <= 1e-12 * (np.abs(rC).max() + 1e-40)), (m.name, Cm, rC)
+            if m.noise:
+                pw = np.zeros(len(m.noise))
+                assert h.h_noise(k, dp_(dp), dp_(v), 1e-12, dp_(pw)) == len(m.noise)
+                src = interp.noise_sources(m.module, dict(zip([p.name for p in m.params], vals)), list(v), VT, 1e-12,
+                                           float(dp[-2]), given)
+                assert [s[0] for s in src] == m.noise
+                np.testing.assert_allclose(pw, [s[1] for s in src], rtol=1e-14)
+
+
+def test_emitted_structure(emitted):
+    _, models = emitted
+    mix = next(m for m in models if m.name == "t_mix")
+    assert mix.internals == ["x"] and mix.nterm == 4 and mix.has_br == 0
+    assert mix.noise == [(0, 3)]                       # white_noise across (a, x)
+    assert (1, 1) in mix.cents and (1, 2) in mix.cents  # ddt charge of port b depends on b and c
+    br = next(m for m in models if m.name == "t_branch")
+    assert br.has_br == 1 and br.nx == 4 and br.given == ["RS"] and br.second_order
+    assert (3, 3) in br.cents                          # ddt(L I) on the branch row
