@@ -22,8 +22,8 @@ import dataclasses
 import math
 from typing import Dict, FrozenSet, List, Optional, Set, Tuple
 
-from .parser import (Assign, Bin, Call, Cond, Contrib, If, Module, Name, Num, Param, Probe, SysCall, Unary,
-                     VAError)
+from .parser import (LOOP_CAP, Assign, Bin, Call, Cond, Contrib, If, Loop, Module, Name, Num, Param, Probe,
+                     SysCall, Unary, VAError)
 
 MAX_PORTS = 5   # the engines stage at most 5 terminal values per device (ports + internal nodes)
 
@@ -186,6 +186,8 @@ class _Analysis:
 
     def _find_vbranch(self, stmts):
         for s in stmts:
+            if isinstance(s, Loop):
+                self._find_vbranch(s.body)
             if isinstance(s, If):
                 self._find_vbranch(s.then)
                 self._find_vbranch(s.other)
@@ -256,6 +258,18 @@ class _Analysis:
             out = frozenset()
             for a in e.args:
                 out |= self.deps(a)
+            f = self.funcs.get(e.fn)
+            if f is not None and f.outputs:
+                # output arguments receive values computed from every argument
+                for j, an in enumerate(f.inputs):
+                    if an not in f.outputs:
+                        continue
+                    if j >= len(e.args) or not isinstance(e.args[j], Name) or e.args[j].id not in self.vars:
+                        raise VAError(f"{self.mod.name}: line {e.line}: output argument {an} of {e.fn}() must be "
+                                      f"a variable")
+                    v = e.args[j].id
+                    if self.vars[v] == "real":
+                        self.var_deps[v] = self.var_deps[v] | out
             return out
         raise VAError(f"{self.mod.name}: unsupported expression {e!r}")
 
@@ -278,6 +292,13 @@ class _Analysis:
                 calls(e.a, out)
                 calls(e.b, out)
         for s in stmts:
+            if isinstance(s, Loop):
+                found = []
+                for x in _all_stmts(s.body):
+                    if isinstance(x, Contrib):
+                        calls(x.expr, found)
+                if found:
+                    raise VAError(f"{self.mod.name}: white_noise() inside a loop")
             if isinstance(s, If):
                 self.collect_noise(s.then)
                 self.collect_noise(s.other)
@@ -301,6 +322,16 @@ class _Analysis:
                 self.deps(s.c)
                 self.walk(s.then, collect)
                 self.walk(s.other, collect)
+            elif isinstance(s, Loop):
+                # the body may run any number of times: its assignments join the
+                # flow-insensitive fixed point like any other
+                self.walk(s.init, collect)
+                if s.cond is not None:
+                    self.deps(s.cond)
+                if s.count is not None:
+                    self.deps(s.count)
+                self.walk(s.body, collect)
+                self.walk(s.step, collect)
             elif isinstance(s, Contrib):
                 self.port_index(s.a, s.line)
                 if s.b is not None:
@@ -330,6 +361,8 @@ def _all_stmts(stmts):
         if isinstance(s, If):
             yield from _all_stmts(s.then)
             yield from _all_stmts(s.other)
+        elif isinstance(s, Loop):
+            yield from _all_stmts(s.init + s.body + s.step)
 
 
 def _check_function(mod: Module, f):
@@ -369,6 +402,11 @@ def _check_function(mod: Module, f):
                 ex(s.c)
                 st(s.then)
                 st(s.other)
+            elif isinstance(s, Loop):
+                for e in (s.cond, s.count):
+                    if e is not None:
+                        ex(e)
+                st(s.init + s.body + s.step)
             elif isinstance(s, Contrib):
                 raise VAError(f"{mod.name}: analog function {f.name}: contributions are not allowed in functions")
     st(f.body)
@@ -495,6 +533,8 @@ def _count_flops(stmts) -> int:
                 ex(s.c)
                 st(s.then)
                 st(s.other)
+            elif isinstance(s, Loop):
+                st(s.init + s.body + s.step)
     st(stmts)
     return n
 
@@ -510,6 +550,7 @@ class _Emitter:
         self.m = m
         self.a = a
         self.scope: Optional[Dict[str, str]] = None     # an analog function's names while emitting it
+        self.loops = 0                                  # loop counter names
 
     def is_int(self, e) -> bool:
         if isinstance(e, Num):
@@ -589,8 +630,15 @@ class _Emitter:
                 f = self.a.funcs[e.fn]
                 if len(e.args) != len(f.inputs):
                     raise VAError(f"{self.m.name}: line {e.line}: {e.fn}() takes {len(f.inputs)} argument(s)")
-                args = "".join(f", D({self.x(a)})" for a in e.args)
-                return f"fn_{self.m.name}_{e.fn}<D>(c{args})"
+                parts = []
+                for an, a in zip(f.inputs, e.args):
+                    if an in f.outputs:       # by reference: a variable of the caller
+                        if not isinstance(a, Name):
+                            raise VAError(f"{self.m.name}: line {e.line}: output argument {an} needs a variable")
+                        parts.append(f", v_{a.id}")
+                    else:
+                        parts.append(f", D({self.x(a)})")
+                return f"fn_{self.m.name}_{e.fn}<D>(c{''.join(parts)})"
             if e.fn not in FUNCS:
                 raise VAError(f"{self.m.name}: line {e.line}: unsupported function {e.fn}()")
             cname, ar = FUNCS[e.fn]
@@ -633,6 +681,22 @@ class _Emitter:
                 if s.other:
                     out.append(f"{ind}}} else {{")
                     out += self.stmts(s.other, ind + "  ", types)
+                out.append(f"{ind}}}")
+            elif isinstance(s, Loop):
+                # at most LOOP_CAP passes, so no model can spin on the device
+                self.loops += 1
+                it = f"it{self.loops}_"
+                out.append(f"{ind}{{")
+                out += self.stmts(s.init, ind + "  ", types)
+                if s.count is not None:
+                    cnt = f"n{self.loops}_"
+                    out.append(f"{ind}  const double {cnt} = vint(val({self.x(s.count)}));")
+                    out.append(f"{ind}  for (int {it} = 0; {it} < {LOOP_CAP} && {it} < {cnt}; ++{it}) {{")
+                else:
+                    out.append(f"{ind}  for (int {it} = 0; {it} < {LOOP_CAP} && val({self.x(s.cond)}) != 0.0; ++{it}) {{")
+                out += self.stmts(s.body, ind + "    ", types)
+                out += self.stmts(s.step, ind + "    ", types)
+                out.append(f"{ind}  }}")
                 out.append(f"{ind}}}")
             elif isinstance(s, Contrib) and s.kind == "V":
                 # V(a,b) <+ e: the branch row collects -e (its orientation folded in)
@@ -688,7 +752,8 @@ class _Emitter:
         the function."""
         out = []
         for f in self.m.module.functions.values():
-            args = "".join(f", D v_{a}" for a in f.inputs)
+            args = "".join((f", {'D' if f.local[a] == 'real' else 'double'} &v_{a}" if a in f.outputs
+                            else f", D v_{a}") for a in f.inputs)
             L = ["template <class D>", f"VA_HD D fn_{self.m.name}_{f.name}(const Ctx &c{args}) {{"]
             for v, t in f.local.items():
                 if v in f.inputs:

@@ -14,10 +14,13 @@ src/vasim.jl:128-180,347-412,663-875):
   cosh sin cos tan atan atan2 asin acos hypot floor ceil limexp; ddt(expr) (additive
   in a contribution); ddx(expr, V(n)) / ddx(expr, V(a,b)); $vt, $vt(T),
   $temperature, $simparam("gmin"[, default]), $mfactor.
-Internal nodes (`electrical` names that are not ports) become extra device
-unknowns.  Loops, output arguments of analog functions and more than one
-voltage-contributed branch are outside the subset and raise VAError with the
-line number.
+Also: `define with arguments and `ifdef; case; for / while / repeat loops
+(capped at LOOP_CAP passes); analog functions with input, output and inout
+arguments; @(initial_step)-style event blocks; $param_given; white_noise /
+flicker_noise; $limit; display tasks.  Internal nodes (`electrical` names that
+are not ports) become extra device unknowns.  More than one voltage-contributed
+branch, noise sources inside loops and other constructs outside the subset
+raise VAError with the line number.
 """
 from __future__ import annotations
 
@@ -330,6 +333,20 @@ class If:
     other: list
 
 
+# loops run at most this many times; past it they stop (and the model's
+# results are whatever the last pass left), so no device code can spin
+LOOP_CAP = 100000
+
+
+@dataclass
+class Loop:             # for (init; cond; step) body  /  while (cond) body  /  repeat (count) body
+    init: list
+    cond: object
+    step: list
+    body: list
+    count: object = None
+
+
 @dataclass
 class Param:
     name: str
@@ -350,12 +367,13 @@ class Module:
 
 
 @dataclass
-class Function:         # analog function: inputs by value, result in the variable NAME
+class Function:         # analog function: arguments in order, result in the variable NAME
     name: str
     type: str
-    inputs: List[str]
+    inputs: List[str]              # every argument, in declaration order
     local: Dict[str, str]          # arguments, locals and the result variable -> type
     body: list
+    outputs: List[str] = field(default_factory=list)   # arguments declared output / inout
 
 
 # ------------------------------------------------------------------ parser
@@ -463,16 +481,18 @@ class Parser:
         name = self.ident()
         self.take(";")
         inputs: List[str] = []
+        outputs: List[str] = []
         local: Dict[str, str] = {}
         while True:
             q = self.peek()
             if q is None:
                 raise VAError(f"analog function {name}: missing endfunction")
-            if q.text in ("input",):
+            if q.text in ("input", "output", "inout"):
                 self.take()
-                inputs += self._idlist()
-            elif q.text in ("output", "inout"):
-                raise VAError(f"line {q.line}: analog function {name}: output arguments are not supported")
+                names = self._idlist()
+                inputs += names
+                if q.text != "input":
+                    outputs += names
             elif q.text in ("real", "integer"):
                 self.take()
                 for n in self._idlist():
@@ -484,7 +504,7 @@ class Parser:
         local[name] = ftype                 # the return value is the variable named after the function
         body = self.statement(local)
         self.take("endfunction")
-        return Function(name, ftype, inputs, local, body)
+        return Function(name, ftype, inputs, local, body, outputs)
 
     def _idlist(self) -> List[str]:
         names = [self.ident()]
@@ -591,6 +611,22 @@ class Parser:
                 raise VAError(f"line {p.line}: unsupported event @({ev})")
             body = self.statement(variables)
             return [] if ev == "final_step" else body
+        if p.kind == "id" and p.text in ("for", "while", "repeat"):
+            self.take()
+            self.take("(")
+            if p.text == "for":
+                init = self._simple_assign(variables)
+                self.take(";")
+                cond = self.expr()
+                self.take(";")
+                step = self._simple_assign(variables)
+                self.take(")")
+                return [Loop(init, cond, step, self.statement(variables))]
+            e = self.expr()
+            self.take(")")
+            if p.text == "while":
+                return [Loop([], e, [], self.statement(variables))]
+            return [Loop([], None, [], self.statement(variables), count=e)]
         if p.text == "case" and p.kind == "id":
             # case (x) v1, v2: s; ... default: s; endcase -> if / else chain
             self.take()
@@ -646,6 +682,13 @@ class Parser:
             self.take(";")
             return [Assign(name, e, p.line)]
         raise VAError(f"line {p.line}: unsupported statement starting with {p.text!r}")
+
+    def _simple_assign(self, variables) -> list:
+        """name = expr (the init and step of a for loop, without a semicolon)"""
+        q = self.peek()
+        name = self.ident()
+        self.take("=")
+        return [Assign(name, self.expr(), q.line)]
 
     # expressions (precedence from low to high)
     def expr(self):

@@ -272,7 +272,7 @@ class Interp:
             if fn == "flicker_noise":
                 return 0.0
             if fn in getattr(self.mod, "functions", {}):
-                return self._call(self.mod.functions[fn], [self.expr(a) for a in e.args])
+                return self._call(self.mod.functions[fn], e.args)
             if fn == "ddt":
                 return _Q(0.0, self.expr(e.args[0]))
             if fn == "ddx":
@@ -328,8 +328,10 @@ class Interp:
         inner = x.d[a]
         return D(inner, [D(inner.d[i], [0.0] * N) for i in range(N)])
 
-    def _call(self, f, args):
-        """An analog function: a fresh scope of its arguments and locals."""
+    def _call(self, f, arg_exprs):
+        """An analog function: a fresh scope of its arguments and locals; output /
+        inout arguments are copied back into the caller's variables."""
+        args = [self.expr(a) for a in arg_exprs]
         saved = (self.vars, self.types, self.params)
         self.types = dict(f.local)
         self.vars = {n: (0 if t == "integer" else self._const(0.0)) for n, t in f.local.items()}
@@ -338,9 +340,14 @@ class Interp:
             self.vars[n] = self._dual(a) if f.local[n] == "real" else a
         try:
             self.block(f.body)
-            return self.vars[f.name]
+            result = self.vars[f.name]
+            outs = {n: self.vars[n] for n in getattr(f, "outputs", [])}
         finally:
             self.vars, self.types, self.params = saved
+        for n, a in zip(f.inputs, arg_exprs):
+            if n in outs:
+                self.vars[a.id] = outs[n] if self.types[a.id] == "real" else int(value(outs[n]))
+        return result
 
     def block(self, stmts):
         P = self.P
@@ -354,6 +361,19 @@ class Interp:
                     self.vars[s.name] = self._dual(x)
             elif isinstance(s, P.If):
                 self.block(s.then if value(self.expr(s.c)) != 0 else s.other)
+            elif isinstance(s, P.Loop):
+                self.block(s.init)
+                if s.count is not None:
+                    v = value(self.expr(s.count))
+                    n = int(math.floor(abs(v) + 0.5)) * (1 if v >= 0 else -1)
+                    for _ in range(min(max(n, 0), P.LOOP_CAP)):
+                        self.block(s.body)
+                else:
+                    it = 0
+                    while it < P.LOOP_CAP and value(self.expr(s.cond)) != 0:
+                        self.block(s.body)
+                        self.block(s.step)
+                        it += 1
             elif isinstance(s, P.Contrib) and getattr(s, "kind", "I") == "V":
                 x = self.expr(s.expr)
                 q = x if isinstance(x, _Q) else _Q(x, 0.0)

@@ -84,6 +84,42 @@ module t_branch(p, n, g);
     I(g) <+ V(g) * 1e-3;
   end
 endmodule
+
+// for / while / repeat loops, a function with output arguments
+module t_loop(a, b);
+  inout a, b;
+  electrical a, b;
+  parameter integer NSEG = 4 from [1:16];
+  parameter real G = 1m;
+  real acc, x, y, lo, hi;
+  integer i;
+
+  analog function real split;
+    input v;
+    output p, q;
+    real v, p, q;
+    begin
+      p = 0.5 * v + 0.1 * v * v;
+      q = v - p;
+      split = p * q;
+    end
+  endfunction
+
+  analog begin
+    acc = 0.0;
+    x = V(a, b);
+    for (i = 0; i < NSEG; i = i + 1)
+      acc = acc + G * x / NSEG * (1.0 + 0.1 * i);
+    i = 0;
+    while (i < 3) begin
+      acc = acc + 1e-6 * x * x;
+      i = i + 1;
+    end
+    repeat (2) acc = acc * 1.01;
+    y = split(x, lo, hi);
+    I(a, b) <+ acc + 1e-4 * (lo - hi) + 1e-5 * y;
+  end
+endmodule
 """
 
 
@@ -128,12 +164,14 @@ def test_emitted_host_code_matches_interpreter(emitted, interp):
     dp_ = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
     for k, m in enumerate(models):
         n = m.nx
-        assert (m.name, n) in (("t_branch", 4), ("t_mix", 4))
+        assert (m.name, n) in (("t_branch", 4), ("t_mix", 4), ("t_loop", 2))
         for trial in range(80):
             over = {}
             if m.name == "t_mix":
                 over = {"SEL": float(rng.integers(0, 4)), "P": float(rng.uniform(0.5, 2.5)),
                         "G": float(rng.uniform(1e-4, 1e-2))}
+            elif m.name == "t_loop":
+                over = {"NSEG": float(rng.integers(1, 17)), "G": float(rng.uniform(1e-4, 1e-2))}
             elif rng.random() < 0.5:
                 over = {"RS": float(rng.uniform(0.0, 20.0))}
             vals = m.defaults(over)
@@ -167,3 +205,22 @@ def test_emitted_structure(emitted):
     br = next(m for m in models if m.name == "t_branch")
     assert br.has_br == 1 and br.nx == 4 and br.given == ["RS"] and br.second_order
     assert (3, 3) in br.cents                          # ddt(L I) on the branch row
+
+
+def test_emitted_code_compiles_for_the_device(emitted, tmp_path):
+    """The same emitted header (functions with output arguments, loops, voltage
+    branches, second-order duals) compiles for sm_103a inside a kernel."""
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not pathlib.Path(nvcc).exists():
+        pytest.skip("nvcc not available")
+    h, models = emitted
+    gen_dir = pathlib.Path(h._name).parent
+    (tmp_path / "k.cu").write_text(
+        '#include "va_models.gen.h"\n'
+        '__global__ void k(int m, const double *dp, const double *v, double *out) {\n'
+        '  cedar::va::eval(m, dp, 1, v, v, false, 1e12, 1e-12, out);\n}\n')
+    r = subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-std=c++17", "-c", "-I", str(CSRC),
+                        "-I", str(gen_dir), str(tmp_path / "k.cu"), "-o", str(tmp_path / "k.o")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+
