@@ -238,12 +238,15 @@ class _Analysis:
                 s.add(self.port_index(e.b, 0))
             return frozenset(s)
         if isinstance(e, Unary):
-            return self.deps(e.x) if e.op == "-" else frozenset()
+            d = self.deps(e.x)       # (visited either way: names, $param_given)
+            return d if e.op == "-" else frozenset()
         if isinstance(e, Bin):
+            d = self.deps(e.a) | self.deps(e.b)
             if e.op in ("+", "-", "*", "/", "**"):
-                return self.deps(e.a) | self.deps(e.b)
+                return d
             return frozenset()       # comparisons and logic are piecewise constant
         if isinstance(e, Cond):
+            self.deps(e.c)
             return self.deps(e.a) | self.deps(e.b)
         if isinstance(e, Call):
             if e.fn == "ddx":
@@ -340,7 +343,11 @@ class _Analysis:
                         (s.a, s.b) == self.vbranch or (s.b is not None and (s.b, s.a) == self.vbranch)):
                     raise VAError(f"{self.mod.name}: line {s.line}: current and voltage contributions on one branch")
                 if collect:
-                    res, charges = split_ddt(s.expr, s.line)
+                    res, charges, factors = split_ddt(s.expr, s.line)
+                    for f_ in factors:
+                        if self.deps(f_):
+                            raise VAError(f"{self.mod.name}: line {s.line}: a factor of ddt() depends on the "
+                                          f"potentials (write it inside the ddt)")
                     self.contribs.append((s, res, charges))
                 self.deps(s.expr)
 
@@ -428,7 +435,18 @@ def split_ddt(e, line: int):
     rec(e, 1)
     res = None
     charges = []
+    factors = []
     for sign, t in terms:
+        # c * ddt(q), ddt(q) * c, ddt(q) / c with c constant in time: ddt(c q),
+        # ddt(q c), ddt(q / c) (the analysis checks that c has no voltage in it)
+        if isinstance(t, Bin) and t.op in ("*", "/"):
+            a_, b_ = t.a, t.b
+            if t.op == "*" and _is_ddt(b_) and not _has_ddt(a_):
+                factors.append(a_)
+                t = Call("ddt", [Bin("*", a_, b_.args[0])], b_.line)
+            elif _is_ddt(a_) and not _has_ddt(b_):
+                factors.append(b_)
+                t = Call("ddt", [Bin(t.op, a_.args[0], b_)], a_.line)
         if isinstance(t, Call) and t.fn == "ddt":
             if len(t.args) != 1 or _has_ddt(t.args[0]):
                 raise VAError(f"line {line}: ddt() takes one argument without ddt()")
@@ -438,7 +456,11 @@ def split_ddt(e, line: int):
                 raise VAError(f"line {line}: ddt() must be an additive term of a contribution")
             tt = t if sign > 0 else Unary("-", t)
             res = tt if res is None else Bin("+", res, tt)
-    return res, charges
+    return res, charges, factors
+
+
+def _is_ddt(e) -> bool:
+    return isinstance(e, Call) and e.fn == "ddt" and len(e.args) == 1
 
 
 def _has_ddt(e) -> bool:
@@ -700,7 +722,7 @@ class _Emitter:
                 out.append(f"{ind}}}")
             elif isinstance(s, Contrib) and s.kind == "V":
                 # V(a,b) <+ e: the branch row collects -e (its orientation folded in)
-                res, charges = split_ddt(s.expr, s.line)
+                res, charges, _ = split_ddt(s.expr, s.line)
                 sg = "-=" if self.a.branch_sign(s.a, s.b, s.line) > 0 else "+="
                 nb = self.a.nb
                 if res is not None:
@@ -709,7 +731,7 @@ class _Emitter:
                     op = sg if c_sg > 0 else ("+=" if sg == "-=" else "-=")
                     out.append(f"{ind}Fq[{nb}] {op} D({self.x(t)});")
             elif isinstance(s, Contrib):
-                res, charges = split_ddt(s.expr, s.line)
+                res, charges, _ = split_ddt(s.expr, s.line)
                 ia = self.a.port[s.a]
                 ib = None if s.b is None else self.a.port[s.b]
                 if res is not None:

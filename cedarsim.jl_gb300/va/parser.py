@@ -24,6 +24,7 @@ raise VAError with the line number.
 """
 from __future__ import annotations
 
+import pathlib
 import re
 from dataclasses import dataclass, field
 from typing import Dict, List, Optional, Tuple
@@ -42,7 +43,7 @@ _TOKEN = re.compile(r"""
   | (?P<sys>\$[A-Za-z_][A-Za-z_0-9]*)
   | (?P<dir>`[A-Za-z_][A-Za-z_0-9]*)
   | (?P<id>[A-Za-z_][A-Za-z_0-9]*)
-  | (?P<str>"[^"\n]*")
+  | (?P<str>"(?:[^"\\\n]|\\.)*")
   | (?P<op><\+|\*\*|<=|>=|==|!=|&&|\|\||[-+*/<>!?:;,()\[\]=@{}.])
 """, re.S | re.X)
 
@@ -58,8 +59,11 @@ DISPLAY_TASKS = ("$strobe", "$display", "$write", "$monitor", "$debug", "$warnin
 # constants of the standard constants.vams header (physical constants, SI)
 CONSTANTS = {"M_PI": 3.14159265358979323846, "M_TWO_PI": 6.28318530717958647652,
              "M_PI_2": 1.57079632679489661923, "M_E": 2.7182818284590452354,
+             "M_LN2": 0.69314718055994530942, "M_LN10": 2.30258509299404568402,
+             "M_SQRT2": 1.41421356237309504880, "M_1_PI": 0.31830988618379067154,
              "P_Q": 1.602176634e-19, "P_K": 1.380649e-23, "P_CELSIUS0": 273.15,
-             "P_EPS0": 8.8541878128e-12}
+             "P_EPS0": 8.8541878128e-12, "P_H": 6.62607015e-34, "P_C": 299792458.0,
+             "P_U0": 1.25663706212e-6}
 
 
 @dataclass
@@ -67,11 +71,12 @@ class Tok:
     kind: str
     text: str
     line: int
+    adj: bool = False      # no whitespace or comment since the previous token
 
 
 def lex(src: str) -> List[Tok]:
     out: List[Tok] = []
-    pos, line, pending = 0, 1, 0
+    pos, line, pending, last_end = 0, 1, 0, -1
     while pos < len(src):
         m = _TOKEN.match(src, pos)
         if not m:
@@ -79,7 +84,8 @@ def lex(src: str) -> List[Tok]:
         kind = m.lastgroup
         text = m.group(kind)
         if kind not in ("ws", "lcom", "bcom"):
-            out.append(Tok(kind, text, line))
+            out.append(Tok(kind, text, line, m.start() == last_end))
+            last_end = m.end()
         # a joined continuation (\x00) keeps the tokens on one line; its newline
         # is counted at the next real line break
         pending += text.count("\x00")
@@ -90,19 +96,28 @@ def lex(src: str) -> List[Tok]:
     return out
 
 
+def _const_tok(t: Tok) -> Tok:
+    """`P_Q and the other constants.vams macros as number tokens."""
+    return Tok("num", repr(CONSTANTS[t.text[1:]]), t.line)
+
+
 def _join_continuations(src: str) -> str:
     """A backslash at the end of a line continues a `define body on the next
     line; the newline is kept out of the body but counted for line numbers."""
-    return re.sub(r"\\[ \t]*\r?\n", " \x00", src)
+    src = re.sub(r"\\[ \t]*\r?\n", " \x00", src)
+    # attribute instances (* name = "..." *) describe items for tools; they carry
+    # no semantics here
+    return re.sub(r"\(\*[^\n]*?\*\)", " ", src)
 
 
-def preprocess(toks: List[Tok]) -> List[Tok]:
+def preprocess(toks: List[Tok], base_dir=None) -> List[Tok]:
     """`define NAME body and `define NAME(a, b) body with `NAME / `NAME(x, y)
     expansion (nested, up to a depth limit), `undef, `ifdef / `ifndef / `elsif /
     `else / `endif, and `include of the standard headers (disciplines.vams /
     constants.vams: their names are built in).  Other directives are errors."""
     macros: Dict[str, Tuple[Optional[List[str]], List[Tok]]] = {}
     out: List[Tok] = []
+    n_includes = 0
     # conditional stack: (this branch active, some branch already taken, parent active)
     cond: List[Tuple[bool, bool, bool]] = []
 
@@ -155,7 +170,10 @@ def preprocess(toks: List[Tok]) -> List[Tok]:
                         body_t.append(Tok(b.kind, b.text, t.line))
                 res.extend(expand(body_t, depth + 1))
                 continue
-            res.append(t)
+            if t.kind == "dir" and t.text[1:] in CONSTANTS:
+                res.append(_const_tok(t))
+            else:
+                res.append(t)
             k += 1
         return res
 
@@ -200,9 +218,20 @@ def preprocess(toks: List[Tok]) -> List[Tok]:
                 if i + 1 >= len(toks) or toks[i + 1].kind != "str":
                     raise VAError(f"line {t.line}: `include needs a file name")
                 fname = toks[i + 1].text.strip('"')
-                if fname not in ("disciplines.vams", "constants.vams", "discipline.h", "constants.h"):
-                    raise VAError(f"line {t.line}: `include \"{fname}\" is not supported (only the standard headers)")
-                i += 2
+                if fname in ("disciplines.vams", "constants.vams", "discipline.h", "constants.h"):
+                    i += 2
+                    continue
+                # another file: relative to the including file's directory, its
+                # tokens spliced in place of the directive
+                if base_dir is None:
+                    raise VAError(f"line {t.line}: `include \"{fname}\" needs the source's directory (parse_file)")
+                path = pathlib.Path(base_dir) / fname
+                if not path.is_file():
+                    raise VAError(f"line {t.line}: `include \"{fname}\": no such file in {base_dir}")
+                n_includes += 1
+                if n_includes > 256:
+                    raise VAError("more than 256 `include directives (recursive include?)")
+                toks = toks[:i] + lex(_join_continuations(path.read_text())) + toks[i + 2:]
                 continue
             if name == "define":
                 if i + 1 >= len(toks) or toks[i + 1].kind != "id":
@@ -210,9 +239,8 @@ def preprocess(toks: List[Tok]) -> List[Tok]:
                 mname, mline = toks[i + 1].text, toks[i + 1].line
                 j = i + 2
                 params = None
-                # a parameter list opens right after the name (no space is not
-                # visible after lexing, so any "(" on the same line starts one)
-                if j < len(toks) and toks[j].line == mline and toks[j].text == "(" and toks[j].kind == "op":
+                # a parameter list opens right after the name, with no space between
+                if j < len(toks) and toks[j].line == mline and toks[j].text == "(" and toks[j].adj:
                     params = []
                     j += 1
                     while j < len(toks) and toks[j].text != ")":
@@ -230,6 +258,11 @@ def preprocess(toks: List[Tok]) -> List[Tok]:
             if name == "undef":
                 macros.pop(toks[i + 1].text, None)
                 i += 2
+                continue
+            if name in CONSTANTS and name not in macros:
+                if active():
+                    out.append(_const_tok(t))
+                i += 1
                 continue
             if name in macros:
                 # collect the macro call (with its argument list) and expand it
@@ -815,11 +848,11 @@ class Parser:
         return self.expr()
 
 
-def parse(src: str) -> List[Module]:
-    """Parse Verilog-A source text into modules."""
-    return Parser(preprocess(lex(_join_continuations(src)))).modules()
+def parse(src: str, base_dir=None) -> List[Module]:
+    """Parse Verilog-A source text into modules (`include files relative to base_dir)."""
+    return Parser(preprocess(lex(_join_continuations(src)), base_dir)).modules()
 
 
 def parse_file(path) -> List[Module]:
-    with open(path) as fh:
-        return parse(fh.read())
+    path = pathlib.Path(path)
+    return parse(path.read_text(), path.parent)

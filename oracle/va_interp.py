@@ -243,6 +243,12 @@ class Interp:
                 qa = a if isinstance(a, _Q) else _Q(a, 0.0)
                 qb = b if isinstance(b, _Q) else _Q(b, 0.0)
                 return _Q(qa.r + qb.r, qa.q + qb.q) if e.op == "+" else _Q(qa.r - qb.r, qa.q - qb.q)
+            if e.op in ("*", "/") and (isinstance(a, _Q) != isinstance(b, _Q)):
+                # c * ddt(q), ddt(q) * c, ddt(q) / c: both channels scale
+                if isinstance(a, _Q):
+                    return _Q(a.r * b, a.q * b) if e.op == "*" else _Q(a.r / b, a.q / b)
+                if e.op == "*":
+                    return _Q(a * b.r, a * b.q)
             if isinstance(a, _Q) or isinstance(b, _Q):
                 raise ValueError("ddt() in a non-additive position")
             if e.op == "+":

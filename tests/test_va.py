@@ -217,7 +217,9 @@ def test_library_lists_the_models(pkg, va):
     ("module m(a, b); inout a, b; electrical a, b; integer i; analog begin for (i = 0; i < 2; i = i + 1) "
      "I(a, b) <+ V(a, b) + white_noise(1e-20, \"n\"); end endmodule", "inside a loop"),
     ("module m(a, b); inout a, b; electrical a, b; analog I(a, b) <+ foo(V(a, b)); endmodule", "unsupported function"),
-    ("module m(a, b); inout a, b; electrical a, b; analog I(a, b) <+ V(a, b) * ddt(V(a, b)); endmodule", "additive"),
+    ("module m(a, b); inout a, b; electrical a, b; analog I(a, b) <+ V(a, b) * ddt(V(a, b)); endmodule",
+     "factor of ddt"),
+    ("module m(a, b); inout a, b; electrical a, b; analog I(a, b) <+ exp(ddt(V(a, b))); endmodule", "additive"),
     ("module m(a, b); inout a, b; electrical a, b; analog I(a, c) <+ V(a, b); endmodule", "not a port"),
     ("module m(a, b); inout a, b; electrical a, b; analog begin x = 1; I(a, b) <+ x; end endmodule", "undeclared"),
     ("module m(a, b); inout a, b; electrical a, b; parameter real R = 1; analog begin R = 2; I(a, b) <+ R; end "
