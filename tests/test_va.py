@@ -457,3 +457,21 @@ def test_limit_and_step_advice(va):
     assert m.gents == [(0, 0), (0, 1), (1, 0), (1, 1)]
     body = va.parse(src)[0].body
     assert len(body) == 2     # the assignment and the contribution
+
+
+def test_cli_reports_and_emits(tmp_path):
+    """va/cli.py: a summary per module, the header with --emit, exit 1 on a module
+    outside the subset."""
+    import subprocess
+    import sys
+    cli = ROOT / "cedarsim.jl_gb300" / "va" / "cli.py"
+    out = tmp_path / "h.h"
+    r = subprocess.run([sys.executable, str(cli), str(ROOT / "cedarsim.jl_gb300" / "va" / "models" / "va_inductor.va"),
+                        "--emit", str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert "module va_inductor" in r.stdout and "branch unknowns 1" in r.stdout
+    assert "body_va_inductor" in out.read_text()
+    bad = tmp_path / "bad.va"
+    bad.write_text("module m(a, b); inout a, b; electrical a, b; analog I(a, b) <+ foo(V(a, b)); endmodule\n")
+    r = subprocess.run([sys.executable, str(cli), str(bad)], capture_output=True, text=True)
+    assert r.returncode == 1 and "unsupported function" in r.stderr
