@@ -35,6 +35,7 @@ def main(argv=None) -> int:
         E.MAX_PORTS = 64
     try:
         mods = [E.analyze(m) for m in P.parse_file(args.file)]
+        header = E.emit_header(sorted(mods, key=lambda ma: ma[0].name), 11)   # the emitter's own checks
     except P.VAError as e:
         print(f"{args.file}: {e}", file=sys.stderr)
         return 1
@@ -44,7 +45,7 @@ def main(argv=None) -> int:
               f"(G {len(m.gents)}, C {len(m.cents)}), noise sources {len(m.noise)}"
               + (", second-order duals (ddx)" if m.second_order else ""))
     if args.emit:
-        pathlib.Path(args.emit).write_text(E.emit_header(sorted(mods, key=lambda ma: ma[0].name), 11))
+        pathlib.Path(args.emit).write_text(header)
         print(f"wrote {args.emit}")
     return 0
 
