@@ -99,6 +99,7 @@ static bool load_circuit(const cedar_ckt_desc *d, Circuit &c, std::string &err) 
     const cedar_devgroup &s = d->groups[g];
     if (s.model <= 0 || s.model >= kNumModels || s.n_inst < 0) { err = "bad model"; return false; }
     Group G; G.model = s.model; G.n_inst = s.n_inst; G.nt = model_nterm(s.model); G.np = model_npar(s.model);
+    if (G.nt + model_hasbr(s.model) > ND) { err = "device with more terminal values than the oracle stages"; return false; }
     G.term.assign(s.term, s.term + (size_t)G.nt * G.n_inst);
     if (model_hasbr(s.model)) {
       if (!s.branch) { err = "missing branch"; return false; }
@@ -321,11 +322,12 @@ static void eval_circuit(const Circuit &c, const double *x, const EvalCtx &ctx, 
           // (idx / nin: the terminals, then the branch current of a module with a
           // voltage-contributed branch)
           const int k = g.model - CEDAR_NMODELS, nx = nin;
-          double dp[64], v[8], fi[8], fq[8], G[64], Cm[64];
+          // sized per model: compact models carry hundreds of parameters
+          std::vector<double> dp(g.np + 1), v(nx), fi(nx), fq(nx), G((size_t)nx * nx), Cm((size_t)nx * nx);
           for (int q = 0; q < g.np; ++q) dp[q] = g.p(q, i);
           dp[g.np] = Vt;
           for (int q = 0; q < nx; ++q) v[q] = X(idx[q]);
-          cedar::va::full(k, dp, 1, v, c.gmin, fi, fq, G, Cm);
+          cedar::va::full(k, dp.data(), 1, v.data(), c.gmin, fi.data(), fq.data(), G.data(), Cm.data());
           const double m = g.p(g.np - 1, i);
           for (int r = 0; r < nx; ++r) {
             const int row = idx[r];
