@@ -144,7 +144,7 @@ struct Slot {
     EvalCtx ctx{tt, 0.0, 1.0, TT.gmin, false, false};
     for_devices_by_model<K>(TT, rank(), smask(), true, [&](const DGroup &gr, int i, int) {
       const int *tm = TT.term + gr.term_off + i * gr.ntx;
-      double v[5];
+      double v[CEDAR_MAX_TERM];
       for (int kk = 0; kk < gr.ntx; ++kk) { int u = tm[kk]; v[kk] = u < 0 ? 0.0 : x[u]; }
       eval_device(gr.model, dp + gr.dpar_off + i, gr.n_inst, v, nullptr, ctx, TT.pwl, w.dout + gr.out_off + i * model_nout(gr.model));
     });
@@ -729,7 +729,7 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am, const 
     const double *x = jx;
     for_devices_by_model<K>(T, rank, am, false, [&](const DGroup &gr, int i, int d) {
       const int *tm = T.term + gr.term_off + i * gr.ntx;
-      double v[5];
+      double v[CEDAR_MAX_TERM];
       for (int kk = 0; kk < gr.ntx; ++kk) { int u = tm[kk]; v[kk] = u < 0 ? 0.0 : x[u]; }
       double *out = dout + gr.out_off + i * model_nout(gr.model);
       const int si = (gr.model == CEDAR_V || gr.model == CEDAR_I) ? T.src_of_dev[d] : -1;

@@ -231,7 +231,7 @@ __device__ __forceinline__ void backward_step(AdjSlot<K> &s, const AdjDev &a, un
     EvalCtx ctx{s.bt, 1.0, 1.0, T.gmin, false, false};
     for_devices_by_model<K>(T, rank, cm, true, [&](const DGroup &gr, int i, int) {
       const int *tm = T.term + gr.term_off + i * gr.ntx;
-      double v[5];
+      double v[CEDAR_MAX_TERM];
       for (int kk = 0; kk < gr.ntx; ++kk) { int u = tm[kk]; v[kk] = u < 0 ? 0.0 : x[u]; }
       eval_device(gr.model, s.dp + gr.dpar_off + i, gr.n_inst, v, nullptr, ctx, T.pwl, s.w.dout + gr.out_off + i * model_nout(gr.model));
     });
@@ -260,7 +260,7 @@ __device__ __forceinline__ void backward_step(AdjSlot<K> &s, const AdjDev &a, un
     EvalCtx ctx{s.bt, s.bcj, 1.0, T.gmin, s.bdc, false};
     for_devices_by_model<K>(T, rank, ab, false, [&](const DGroup &gr, int i, int) {
       const int *tm = T.term + gr.term_off + i * gr.ntx;
-      double v[5];
+      double v[CEDAR_MAX_TERM];
       for (int kk = 0; kk < gr.ntx; ++kk) { int u = tm[kk]; v[kk] = u < 0 ? 0.0 : x[u]; }
       eval_device(gr.model, s.dp + gr.dpar_off + i, gr.n_inst, v, nullptr, ctx, T.pwl, s.w.dout + gr.out_off + i * model_nout(gr.model));
     });

@@ -47,7 +47,7 @@ __global__ void eval_kernel(DTpl T, const double *dpar, const double *x, const d
   const DGroup gr = T.grp[gi];
   int i = d - (gi ? T.dev_end[gi - 1] : 0);
   const int *tm = T.term_orig + gr.term_off + i * gr.ntx;
-  double v[5], vd[5];
+  double v[CEDAR_MAX_TERM], vd[CEDAR_MAX_TERM];
   for (int k = 0; k < gr.ntx; ++k) {
     int u = tm[k];
     v[k] = u < 0 ? 0.0 : __ldg(x + u);

@@ -24,6 +24,12 @@
 // Verilog-A models compiled by cedarsim.jl_gb300/va (the build writes this
 // header into its own directory and puts it on the include path)
 #include "va_models.gen.h"
+// terminal values (terminals + branch current) the engines stage per device:
+// 5 for the built-in models, more when a compiled Verilog-A model needs them
+// (the generated header defines it then)
+#ifndef CEDAR_MAX_TERM
+#define CEDAR_MAX_TERM 5
+#endif
 
 namespace cedar {
 

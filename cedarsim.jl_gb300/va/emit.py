@@ -25,7 +25,11 @@ from typing import Dict, FrozenSet, List, Optional, Set, Tuple
 from .parser import (LOOP_CAP, Assign, Bin, Call, Cond, Contrib, If, Loop, Module, Name, Num, Param, Probe,
                      SysCall, Unary, VAError)
 
-MAX_PORTS = 5   # the engines stage at most 5 terminal values per device (ports + internal nodes)
+# terminal values per device (ports + internal nodes + a branch current) the
+# engines can stage; above the built-ins' 5 the generated header widens the
+# engines' staging (CEDAR_MAX_TERM) for the library built with such a model
+MAX_PORTS = 8
+BUILTIN_TERMS = 5
 
 FUNCS = {  # VA name -> (C++ name, arity)
     "exp": ("exp", 1), "ln": ("log", 1), "log": ("log10", 1), "sqrt": ("sqrt", 1), "pow": ("pow", 2),
@@ -863,7 +867,11 @@ def emit_header(models: List[Tuple[VAModel, _Analysis]], base_id: int) -> str:
     L = ["// Generated by cedarsim.jl_gb300/va/emit.py from Verilog-A sources; do not edit.",
          "#pragma once",
          '#include "va_dual.cuh"',
-         "",
+         ""]
+    width = max([BUILTIN_TERMS] + [m.nx for m, _ in models])
+    if width > BUILTIN_TERMS:
+        L += [f"#define CEDAR_MAX_TERM {width}   // a model here has {width} terminal values", ""]
+    L += [
          "namespace cedar {",
          "namespace va {",
          "",

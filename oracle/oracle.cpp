@@ -45,6 +45,7 @@ namespace orc {
 
 // ---------------------------------------------------------------- dual numbers
 constexpr int ND = 6;
+constexpr int kMaxIdx = 16;   // terminal values of one device (Verilog-A models can have more)
 struct Dual {
   double v;
   double d[ND];
@@ -99,7 +100,7 @@ static bool load_circuit(const cedar_ckt_desc *d, Circuit &c, std::string &err) 
     const cedar_devgroup &s = d->groups[g];
     if (s.model <= 0 || s.model >= kNumModels || s.n_inst < 0) { err = "bad model"; return false; }
     Group G; G.model = s.model; G.n_inst = s.n_inst; G.nt = model_nterm(s.model); G.np = model_npar(s.model);
-    if (G.nt + model_hasbr(s.model) > ND) { err = "device with more terminal values than the oracle stages"; return false; }
+    if (G.nt + model_hasbr(s.model) > kMaxIdx) { err = "device with more terminal values than the oracle stages"; return false; }
     G.term.assign(s.term, s.term + (size_t)G.nt * G.n_inst);
     if (model_hasbr(s.model)) {
       if (!s.branch) { err = "missing branch"; return false; }
@@ -238,12 +239,13 @@ static void eval_circuit(const Circuit &c, const double *x, const EvalCtx &ctx, 
   for (const Group &g : c.groups) {
     for (int i = 0; i < g.n_inst; ++i) {
       const int *tm = g.term.data() + (size_t)g.nt * i;
-      int idx[ND]; int nin = 0;
+      int idx[kMaxIdx]; int nin = 0;
       for (int k = 0; k < g.nt; ++k) idx[nin++] = tm[k];
       int br = -1;
       if (!g.branch.empty()) { br = g.branch[i]; idx[nin++] = br; }
-      Dual in[ND];
-      for (int k = 0; k < nin; ++k) in[k] = Dual::seed(X(idx[k]), idx[k] >= 0 ? k : -1);
+      Dual in[ND];   // (built-in models: at most 5 inputs)
+      if (g.model < CEDAR_NMODELS)
+        for (int k = 0; k < nin; ++k) in[k] = Dual::seed(X(idx[k]), idx[k] >= 0 ? k : -1);
       Acc A{o, idx, nin};
       switch (g.model) {
         case CEDAR_R: {  // I - V/res = 0; kcl!(p, -m I), kcl!(n, +m I)

@@ -212,8 +212,8 @@ def test_library_lists_the_models(pkg, va):
 
 
 @pytest.mark.parametrize("src, msg", [
-    ("module m(a, b); inout a, b; electrical a, b, x1, x2, x3, x4; analog I(a, b) <+ V(a, b); endmodule",
-     "at most"),
+    ("module m(a, b); inout a, b; electrical a, b, x1, x2, x3, x4, x5, x6, x7; analog I(a, b) <+ V(a, b); "
+     "endmodule", "at most"),
     ("module m(a, b); inout a, b; electrical a, b; integer i; analog begin for (i = 0; i < 2; i = i + 1) "
      "I(a, b) <+ V(a, b) + white_noise(1e-20, \"n\"); end endmodule", "inside a loop"),
     ("module m(a, b); inout a, b; electrical a, b; analog I(a, b) <+ foo(V(a, b)); endmodule", "unsupported function"),

@@ -8,8 +8,8 @@ nodes) is parsed, analysed and emitted; the emitted C++ is compiled with g++ and
 its residuals and Jacobians are compared with the independent interpretation of
 the same parsed module at several bias points, and the drain current is checked
 for the on / off behaviour of an n-type FinFET.  The model has 6 terminal
-values (d, g, s, e and the internal di, si), one more than the engines stage per
-device, so it runs here through the host-compiled code only."""
+values (d, g, s, e and the internal di, si); a library built with it widens the
+engines' per-device staging to 6 (CEDAR_MAX_TERM)."""
 import ctypes as C
 import importlib.util
 import os
@@ -30,17 +30,18 @@ pytestmark = pytest.mark.skipif(not SRC_DIR or not (pathlib.Path(SRC_DIR) / "bsi
 
 
 @pytest.fixture(scope="module")
-def bsim(pkg, tmp_path_factory, monkeypatch_module):
+def bsim(pkg, tmp_path_factory):
     if shutil.which("g++") is None:
         pytest.skip("g++ not available")
     import importlib
     P = importlib.import_module("cedarsim_gb300.va.parser")
     E = importlib.import_module("cedarsim_gb300.va.emit")
-    monkeypatch_module.setattr(E, "MAX_PORTS", 8)      # host-only: no engine staging limit
     mod = P.parse_file(pathlib.Path(SRC_DIR) / "bsimcmg.va")[0]
     m, a = E.analyze(mod)
     d = tmp_path_factory.mktemp("bsimcmg")
-    (d / "va_models.gen.h").write_text(E.emit_header([(m, a)], 11))
+    text = E.emit_header([(m, a)], 11)
+    assert "#define CEDAR_MAX_TERM 6" in text
+    (d / "va_models.gen.h").write_text(text)
     (d / "h.cpp").write_text('#include <math.h>\n#include "va_models.gen.h"\n'
                              'extern "C" void h_full(const double *dp, const double *v, double *fi, double *fq, '
                              'double *G, double *C) { cedar::va::full(0, dp, 1, v, 1e-12, fi, fq, G, C); }\n')
@@ -50,13 +51,6 @@ def bsim(pkg, tmp_path_factory, monkeypatch_module):
     lib = C.CDLL(str(d / "libh.so"))
     lib.h_full.argtypes = [C.POINTER(C.c_double)] * 6
     return mod, m, lib
-
-
-@pytest.fixture(scope="module")
-def monkeypatch_module():
-    mp = pytest.MonkeyPatch()
-    yield mp
-    mp.undo()
 
 
 def test_bsimcmg_structure(bsim):

@@ -224,3 +224,34 @@ def test_emitted_code_compiles_for_the_device(emitted, tmp_path):
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-2000:]
 
+
+
+def test_wide_model_widens_engine_staging(pkg, tmp_path):
+    """A module with 6 terminal values (4 ports, 2 internal nodes) makes the
+    generated header define CEDAR_MAX_TERM 6, and the one-circuit engine's
+    translation unit compiles for sm_103a with the wider staging; the shipped
+    models keep the built-ins' 5."""
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not pathlib.Path(nvcc).exists():
+        pytest.skip("nvcc not available")
+    import importlib
+    P = importlib.import_module("cedarsim_gb300.va.parser")
+    E = importlib.import_module("cedarsim_gb300.va.emit")
+    src = """module wide(d, g, s, b); inout d, g, s, b; electrical d, g, s, b, di, si;
+      parameter real RD = 10.0, RS = 10.0, K = 1m;
+      analog begin
+        I(d, di) <+ V(d, di) / RD; I(s, si) <+ V(s, si) / RS;
+        I(di, si) <+ K * V(g, si) * V(di, si) + 1e-12 * V(b, si);
+      end endmodule"""
+    mods = [E.analyze(m) for m in P.parse(src)]
+    assert mods[0][0].nx == 6
+    text = E.emit_header(mods, 11)
+    assert "#define CEDAR_MAX_TERM 6" in text
+    (tmp_path / "va_models.gen.h").write_text(text)
+    shipped = pkg.va.models()
+    assert "CEDAR_MAX_TERM" not in E.emit_header([E.analyze(m.module) for m in shipped], 11)
+    r = subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-std=c++17", "-O3",
+                        "--expt-relaxed-constexpr", "-c", "-I", str(tmp_path), "-I", str(ROOT / "include"),
+                        "-I", str(CSRC), str(CSRC / "k_plain.cu"), "-o", str(tmp_path / "k.o")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
