@@ -28,6 +28,11 @@ MODEL_NAMES = {R: "R", C: "C", L: "L", V: "V", I: "I", E: "E", G: "G", MOS1: "MO
 NTERM = {R: 2, C: 2, L: 2, V: 2, I: 2, E: 4, G: 4, MOS1: 4, DIODE: 2, NLVCR: 3}
 NPAR = {R: 2, C: 2, L: 2, V: 10, I: 10, E: 2, G: 2, MOS1: 7, DIODE: 4, NLVCR: 2}
 HAS_BRANCH = {L, V, E}
+# names of the built-in models' leading raw parameters, in device-table order
+# (a source's waveform parameters after `dc` are set through its waveform)
+PARAM_NAMES = {R: ["r", "m"], C: ["c", "m"], L: ["l", "m"], V: ["m", "dc"], I: ["m", "dc"], E: ["gain", "m"],
+               G: ["gain", "m"], MOS1: ["type", "W", "L", "KP", "VTO", "LAMBDA", "m"], DIODE: ["IS", "N", "AREA", "m"],
+               NLVCR: ["R", "m"]}
 GROUND = {"0", "gnd", "GND", "ground"}
 
 WAVE_DC, WAVE_PULSE, WAVE_PWL, WAVE_SIN = 0, 1, 2, 3
@@ -260,6 +265,57 @@ class Circuit:
         # internal nodes: one node unknown each, named "<instance>.<node>"
         inner = [f"{name}.{n}" for n in mod.internals]
         return self._add(name, mid, list(terms) + inner, mod.defaults(params) + [float(m)])
+
+    # ---- parameter overrides by device name (the alter() of a netlist)
+    def device(self, name: str) -> Device:
+        for d in self.devices:
+            if d.name == name:
+                return d
+        raise KeyError(f"no device named {name!r}")
+
+    def set_param(self, dev: str, pname: str, value: float) -> "Circuit":
+        """Set parameter `pname` of device `dev` (names as in PARAM_NAMES for the
+        built-in models, the module's parameter names and `m` for Verilog-A
+        models; setting a parameter a module queries with $param_given marks it
+        given)."""
+        d = self.device(dev)
+        if d.model >= VA_BASE:
+            from . import va
+            mod = va.model(d.model)
+            names = [p.name for p in mod.params]
+            if pname == "m":
+                d.params[-1] = float(value)
+                return self
+            if pname not in names:
+                raise KeyError(f"{dev} ({mod.name}) has no parameter {pname!r}")
+            vals = {n: d.params[k] for k, n in enumerate(names)}
+            given = {g for j, g in enumerate(mod.given) if d.params[len(names) + j] != 0.0}
+            vals[pname] = float(value)
+            given.add(pname)
+            new = mod.defaults({n: v for n, v in vals.items()})
+            flags = [1.0 if g in given else 0.0 for g in mod.given]
+            d.params = new[:len(names)] + flags + [d.params[-1]]
+            return self
+        names = PARAM_NAMES[d.model]
+        if pname not in names:
+            raise KeyError(f"{dev} has no parameter {pname!r} (parameters {names})")
+        d.params[names.index(pname)] = float(value)
+        if d.model in (V, I) and pname == "dc" and isinstance(d.wave, (int, float)):
+            d.wave = float(value)       # a DC source: its transient value is its dc value
+        return self
+
+    def altered(self, params) -> "Circuit":
+        """A copy with parameters set from {"DEV.param": value} (None keeps the value)."""
+        import copy
+        c = copy.deepcopy(self)
+        for key, v in (params.items() if isinstance(params, dict) else params):
+            if v is None:
+                continue
+            dev, _, pname = str(key).rpartition(".")
+            if not dev:
+                raise KeyError(f"{key!r}: expected DEVICE.parameter")
+            c.set_param(dev, pname, v)
+        return c
 
     # ---- flattening
     def flatten(self) -> Flat:

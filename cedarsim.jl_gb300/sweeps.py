@@ -350,9 +350,10 @@ class Params(dict):
 
 
 class ParamSim:
-    """A circuit with parameter overrides.  `circuit` is either a function
-    `f(**params) -> Circuit` (dotted names arrive as nested dicts) or a class
-    whose default instance is altered and then called to build the Circuit."""
+    """A circuit with parameter overrides.  `circuit` is a function
+    `f(**params) -> Circuit` (dotted names arrive as nested dicts), a class whose
+    default instance is altered and then called to build the Circuit, or a built
+    Circuit whose devices are altered by "DEVICE.parameter" names."""
 
     def __init__(self, circuit, **params):
         self.circuit = circuit
@@ -361,6 +362,9 @@ class ParamSim:
 
     def build(self):
         c = self.circuit
+        if hasattr(c, "altered") and hasattr(c, "flatten"):
+            # a built netlist: "DEVICE.parameter" names alter its devices
+            return c.altered(self._flat_params)
         if isinstance(c, type):
             return alter(c(), self._flat_params)()
         return c(**self.params)

@@ -323,3 +323,35 @@ def test_sweep_over_verilog_a_parameters(sw, pkg, oracle, monkeypatch):
     f = 0.5 * math.tanh(0.3 / 0.5)
     for sol, gm in zip(sols.ravel(order="F"), (2e-3, 1e-3, 3e-3)):
         assert sol["o"] == pytest.approx(gm * f * 1e3, rel=1e-9)
+
+
+def test_sweep_device_parameters_of_a_built_circuit(sw, pkg, oracle, monkeypatch):
+    """A CircuitSweep over a built Circuit alters its devices by DEVICE.parameter
+    names (built-in and Verilog-A parameters, multiplicity, a DC source's value);
+    the original circuit is left unchanged."""
+    import cedarsim_gb300.api as api
+    _OracleBatch.oracle = oracle
+    monkeypatch.setattr(api, "Batch", _OracleBatch)
+    c = pkg.Circuit()
+    c.V("V", "vcc", "0", dc=1.0)
+    c.R("R1", "vcc", "out", r=1e3)
+    c.va("R2", "va_resistor", ["out", "0"], R=1e3)
+    cs = sw.CircuitSweep(c, sw.ProductSweep(**{"R1.r": [1e3, 3e3], "R2.R": [1e3, 2e3], "V.dc": [1.0, 2.0]}))
+    sols = pkg.dc(cs, reltol=1e-10)
+    assert sols.shape == (2, 2, 2)
+    for (i, j, k), sol in np.ndenumerate(sols):
+        r1, r2, vdc = [1e3, 3e3][i], [1e3, 2e3][j], [1.0, 2.0][k]
+        assert sol["out"] == pytest.approx(vdc * r2 / (r1 + r2), rel=1e-9)
+        assert sol.params.R1.r == r1
+    assert c.device("R1").params[0] == 1e3 and c.device("V").params[1] == 1.0
+    c2 = c.altered({"R1.m": 2.0})
+    assert c2.device("R1").params[1] == 2.0 and c.device("R1").params[1] == 1.0
+    with pytest.raises(KeyError):
+        c.altered({"R1.q": 1.0})
+    with pytest.raises(KeyError):
+        c.altered({"R9.r": 1.0})
+    g = pkg.Circuit()
+    g.va("G", "va_vccs_sat", ["0", "o", "c", "0"])
+    g2 = g.altered({"G.GMX": 4e-3})
+    mod = pkg.va.model(pkg.va.model_id("va_vccs_sat"))
+    assert g2.device("G").params[len(mod.params)] == 1.0 and g.device("G").params[len(mod.params)] == 0.0
