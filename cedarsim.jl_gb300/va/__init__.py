@@ -8,7 +8,8 @@ engine kernel, so a Verilog-A device runs on the GPU like a built-in one.
 
 Models come from the `models/` directory beside this file and from the
 directories listed in the CEDAR_VA_PATH environment variable (os.pathsep
-separated), every `*.va` file, sorted by module name.  Model ids start at
+separated), every `*.va` file, and the .va files it names directly (a model
+whose other .va files are `include fragments), sorted by module name.  Model ids start at
 CEDAR_NMODELS (the first id after the built-in models) in that order; adding a
 model means rebuilding the library (`__graft_entry__.build()`).
 """
@@ -28,11 +29,17 @@ _cache: Dict[tuple, List[Tuple[VAModel, object]]] = {}
 
 
 def sources() -> List[pathlib.Path]:
-    dirs = [HERE / "models"] + [pathlib.Path(p) for p in os.environ.get("CEDAR_VA_PATH", "").split(os.pathsep) if p]
+    """The shipped models, then every CEDAR_VA_PATH entry: a directory adds its
+    *.va files, a file is taken as it is (for models whose other .va files are
+    `include fragments)."""
+    entries = [HERE / "models"] + [pathlib.Path(p) for p in os.environ.get("CEDAR_VA_PATH", "").split(os.pathsep)
+                                   if p]
     files = []
-    for d in dirs:
+    for d in entries:
         if d.is_dir():
             files += sorted(d.glob("*.va"))
+        elif d.is_file():
+            files.append(d)
     return files
 
 
