@@ -75,12 +75,17 @@ VA_HD bool all_zero(const Dual<T, N> &x) {
   return true;
 }
 
+// f'(x) * dx with a strong zero: a direction x does not move along contributes
+// 0 even where f' is infinite (sqrt, pow at 0), instead of 0 * inf = NaN
+template <class T>
+VA_HD T sz_mul(const T &fp, const T &dx) { return all_zero(dx) ? T(0.0) : fp * dx; }
+
 // r = f(x) with f(x.v) = fv and f'(x.v) = fp
 template <class T, int N>
 VA_HD Dual<T, N> chain(const Dual<T, N> &x, const T &fv, const T &fp) {
   Dual<T, N> r;
   r.v = fv;
-  for (int i = 0; i < N; ++i) r.d[i] = fp * x.d[i];
+  for (int i = 0; i < N; ++i) r.d[i] = sz_mul(fp, x.d[i]);
   return r;
 }
 
@@ -213,10 +218,10 @@ VA_HD Dual<T, N> pow(const Dual<T, N> &x, const Dual<T, N> &y) {
   for (int i = 0; i < N; ++i)
     if (!all_zero(y.d[i])) ycst = false;
   if (ycst) {
-    for (int i = 0; i < N; ++i) r.d[i] = dx * x.d[i];
+    for (int i = 0; i < N; ++i) r.d[i] = sz_mul(dx, x.d[i]);
   } else {
     const T dy = p * log(x.v);
-    for (int i = 0; i < N; ++i) r.d[i] = dx * x.d[i] + dy * y.d[i];
+    for (int i = 0; i < N; ++i) r.d[i] = sz_mul(dx, x.d[i]) + sz_mul(dy, y.d[i]);
   }
   return r;
 }

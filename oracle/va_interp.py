@@ -50,11 +50,21 @@ class D:
 
     def __truediv__(self, o):
         o = self._lift(o)
-        q = self.v / o.v
-        return D(q, [(a * o.v - self.v * b) / (o.v * o.v) for a, b in zip(self.d, o.d)])
+        q = _fdiv(self.v, o.v)
+        return D(q, [_fdiv(a * o.v - self.v * b, o.v * o.v) for a, b in zip(self.d, o.d)])
 
     def __rtruediv__(self, o):
         return self._lift(o) / self
+
+
+def _fdiv(a, b):
+    """a / b with IEEE results for a zero divisor (inf or nan), as the device code."""
+    if isinstance(a, D) or isinstance(b, D):
+        return a / b
+    try:
+        return a / b
+    except ZeroDivisionError:
+        return math.nan if a == 0 else math.copysign(math.inf, a) * math.copysign(1.0, b)
 
 
 def _zero(x):
@@ -84,7 +94,13 @@ def _fn(name):
 def _unary_fn(name, x):
     if not isinstance(x, D):
         return _fn(name)(x)
-    return D(_unary_fn(name, x.v), [_deriv(name, x.v) * a for a in x.d])
+    return D(_unary_fn(name, x.v), [_sz(_deriv(name, x.v), a) for a in x.d])
+
+
+def _sz(fp, a):
+    """fp * a with a strong zero: a zero direction stays zero even where fp is
+    infinite (the derivative of sqrt or pow at 0)."""
+    return _zero(a) if not _nonzero(a) else fp * a
 
 
 def _deriv(name, v):
@@ -92,11 +108,11 @@ def _deriv(name, v):
     if name in ("exp",):
         return _unary_fn("exp", v)
     if name == "ln":
-        return 1.0 / v if not isinstance(v, D) else D(1.0, [_zero(a) for a in v.d]) / v
+        return _fdiv(1.0, v) if not isinstance(v, D) else D(1.0, [_zero(a) for a in v.d]) / v
     if name == "log":
-        return 1.0 / (v * math.log(10.0)) if not isinstance(v, D) else D(1.0, [_zero(a) for a in v.d]) / (v * math.log(10.0))
+        return _fdiv(1.0, v * math.log(10.0)) if not isinstance(v, D) else D(1.0, [_zero(a) for a in v.d]) / (v * math.log(10.0))
     if name == "sqrt":
-        return 0.5 / _unary_fn("sqrt", v) if not isinstance(v, D) else D(0.5, [_zero(a) for a in v.d]) / _unary_fn("sqrt", v)
+        return _fdiv(0.5, _unary_fn("sqrt", v)) if not isinstance(v, D) else D(0.5, [_zero(a) for a in v.d]) / _unary_fn("sqrt", v)
     if name == "sin":
         return _unary_fn("cos", v)
     if name == "cos":
@@ -116,12 +132,14 @@ def _deriv(name, v):
     if name in ("asin", "acos"):
         s = _unary_fn("sqrt", 1.0 - v * v)
         one = 1.0 if not isinstance(v, D) else D(1.0, [_zero(a) for a in v.d])
-        return one / s if name == "asin" else -(one / s)
+        return _fdiv(one, s) if name == "asin" else -_fdiv(one, s)
     raise KeyError(name)
 
 
 def _pow(x, y):
     if not isinstance(x, D) and not isinstance(y, D):
+        if x == 0.0 and y < 0:
+            return math.inf                 # C's pow(0, y < 0)
         try:
             return math.pow(x, y)
         except (ValueError, OverflowError):
@@ -131,7 +149,7 @@ def _pow(x, y):
         yv = y if not isinstance(y, D) else y.v
         base = _pow(x.v, yv)
         dx = yv * _pow(x.v, yv - 1.0)
-        return D(base, [dx * a for a in x.d])
+        return D(base, [_sz(dx, a) for a in x.d])
     return _unary_fn("exp", y * _unary_fn("ln", x))
 
 

@@ -255,3 +255,38 @@ def test_wide_model_widens_engine_staging(pkg, tmp_path):
                         "-I", str(CSRC), str(CSRC / "k_plain.cu"), "-o", str(tmp_path / "k.o")],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-2000:]
+
+
+def test_strong_zero_partials(pkg, tmp_path):
+    """Where f' is infinite (sqrt, pow at 0) the partials along directions the
+    argument does not depend on stay 0, not 0 * inf = NaN (host-compiled code and
+    interpreter alike)."""
+    import importlib
+    P = importlib.import_module("cedarsim_gb300.va.parser")
+    E = importlib.import_module("cedarsim_gb300.va.emit")
+    src = """module sz(a, b, c); inout a, b, c; electrical a, b, c;
+      analog begin
+        I(a) <+ 1e-3 * sqrt(V(a)) + 1e-3 * V(b);
+        I(c) <+ 1e-3 * pow(V(c), 0.5) + 1e-3 * V(b);
+      end endmodule"""
+    mods = [E.analyze(m) for m in P.parse(src)]
+    (tmp_path / "va_models.gen.h").write_text(E.emit_header(mods, 11))
+    (tmp_path / "h.cpp").write_text('#include <math.h>\n#include "va_models.gen.h"\n'
+                                    'extern "C" void h(const double *dp, const double *v, double *fi, double *fq, '
+                                    'double *G, double *C) { cedar::va::full(0, dp, 1, v, 1e-12, fi, fq, G, C); }\n')
+    r = subprocess.run(["g++", "-O1", "-std=c++17", "-shared", "-fPIC", "-I", str(CSRC), "-I", str(tmp_path),
+                        str(tmp_path / "h.cpp"), "-o", str(tmp_path / "h.so")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-1500:]
+    lib = C.CDLL(str(tmp_path / "h.so"))
+    dp_ = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    dp, v = np.array([1.0, VT]), np.array([0.0, 0.3, 0.0])
+    fi, fq, G, Cm = np.zeros(3), np.zeros(3), np.zeros(9), np.zeros(9)
+    lib.h(dp_(dp), dp_(v), dp_(fi), dp_(fq), dp_(G), dp_(Cm))
+    G = G.reshape(3, 3)
+    assert G[0, 1] == -1e-3 and G[2, 1] == -1e-3            # finite cross partials
+    assert np.isinf(G[0, 0]) and np.isinf(G[2, 2])           # the genuine infinite slopes
+    spec = importlib.util.spec_from_file_location("cedar_va_interp_sz", ROOT / "oracle" / "va_interp.py")
+    vi = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(vi)
+    _, _, rG, _ = vi.evaluate(mods[0][0].module, {}, list(v), VT, 1e-12)
+    assert rG[0][1] == -1e-3 and rG[2][1] == -1e-3
