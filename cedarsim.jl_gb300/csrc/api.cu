@@ -260,7 +260,7 @@ struct cedar_ckt {
   DevBuf<long long> count;
   DevBuf<long long> off;
   // AC / noise: G and C per LU slot, inputs, outputs, per-warp complex workspaces
-  DevBuf<double> ac_g, ac_c, ac_b, ac_omega, ac_out, ac_nw;
+  DevBuf<double> ac_g, ac_c, ac_b, ac_omega, ac_out, ac_nw, ac_ne;
   DevBuf<double2> ac_ws, ac_dws;
   DevBuf<int> ac_probe, ac_status, ac_na, ac_nb, ac_ndense, ac_dpiv;
   cudaEvent_t ac_ev[4] = {nullptr, nullptr, nullptr, nullptr};   // sparse start / end, dense start / end
@@ -672,7 +672,7 @@ int cedar_noise(cedar_ckt *c, const double *x_op, int32_t n_freq, const double *
   if (n_freq == 0) return 0;
   // thermal noise current of every resistor: terminals and weight m^2 4 k T / r
   std::vector<int> na, nb;
-  std::vector<double> nw;
+  std::vector<double> nw, ne;
   const double kT4 = 4.0 * 1.380649e-23 * (H.temp_c + 273.15);
   for (const GroupInfo &g : H.groups) {
     if (g.model != CEDAR_R) continue;
@@ -681,11 +681,13 @@ int cedar_noise(cedar_ckt *c, const double *x_op, int32_t n_freq, const double *
       na.push_back(H.term_orig[g.term_off + (size_t)i * g.ntx]);
       nb.push_back(H.term_orig[g.term_off + (size_t)i * g.ntx + 1]);
       nw.push_back(m * m * kT4 / r);
+      ne.push_back(0.0);
     }
   }
-  // white_noise sources of Verilog-A devices: their powers at x_op from the
-  // emitted device code run on the host, weight m^2 pwr (the contribution is
-  // scaled by m, src/simulate_ir.jl:54), across the contribution's branch
+  // white_noise / flicker_noise sources of Verilog-A devices: their powers and
+  // exponents at x_op from the emitted device code run on the host, weight
+  // m^2 pwr (the contribution is scaled by m, src/simulate_ir.jl:54) over
+  // f^exponent (src/ac.jl:267-276), across the contribution's branch
   const double vt = thermal_voltage(H.temp_c);
   for (const GroupInfo &g : H.groups) {
     const int k = g.model - va::kBase;
@@ -693,20 +695,21 @@ int cedar_noise(cedar_ckt *c, const double *x_op, int32_t n_freq, const double *
     const int n0 = va::kNoisePtr[k], nn = va::kNoisePtr[k + 1] - n0;
     if (nn == 0) continue;
     const int np = va::kNPar[k];
-    std::vector<double> dp(np + 1), pw(nn);
+    std::vector<double> dp(np + 1), pw(nn), ex(nn);
     double v[8] = {0};
     for (int i = 0; i < g.n_inst; ++i) {
       for (int q = 0; q < np; ++q) dp[q] = H.par[g.par_off + (size_t)q * g.n_inst + i];
       dp[np] = vt;
       const int *t = &H.term_orig[g.term_off + (size_t)i * g.ntx];
       for (int q = 0; q < g.ntx && q < 8; ++q) v[q] = t[q] < 0 ? 0.0 : x_op[t[q]];
-      va::noise(k, dp.data(), 1, v, H.gmin, pw.data());
+      va::noise(k, dp.data(), 1, v, H.gmin, pw.data(), ex.data());
       const double m = dp[np - 1];
       for (int j = 0; j < nn; ++j) {
         const int pa = va::kNoise[2 * (n0 + j)], pb = va::kNoise[2 * (n0 + j) + 1];
         na.push_back(t[pa]);
         nb.push_back(pb >= 0 ? t[pb] : -1);
         nw.push_back(m * m * pw[j]);
+        ne.push_back(ex[j]);
       }
     }
   }
@@ -725,6 +728,12 @@ int cedar_noise(cedar_ckt *c, const double *x_op, int32_t n_freq, const double *
   CUDA_TRY(cudaMemcpyAsync(c->ac_probe.p, &probe, sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
   a.probe = c->ac_probe.p; a.n_probe = 1; a.psd = c->ac_out.p;
   a.n_noise = (int)nr; a.noise_a = c->ac_na.p; a.noise_b = c->ac_nb.p; a.noise_w = c->ac_nw.p;
+  a.noise_e = nullptr;
+  if (std::any_of(ne.begin(), ne.end(), [](double e) { return e != 0.0; })) {
+    CUDA_TRY(c->ac_ne.ensure(nr));
+    CUDA_TRY(cudaMemcpyAsync(c->ac_ne.p, ne.data(), nr * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    a.noise_e = c->ac_ne.p;
+  }
   rc = ac_run(c, a, true, status);
   if (rc) return rc;
   CUDA_TRY(cudaMemcpyAsync(psd, c->ac_out.p, n_freq * sizeof(double), cudaMemcpyDeviceToHost, c->stream));

@@ -110,8 +110,10 @@ __device__ bool ac_solve_suspect(const AcDev &a, double w, const double2 *x, con
   return nonfinite || rmax > kAcResidTol * (amax * xmax + bmax);
 }
 
-// output PSD from y (internal rows): Σ_r w_r |y_a − y_b|², fixed butterfly
-__device__ double noise_sum(const AcDev &a, const double2 *y, int lane) {
+// output PSD of frequency f from y (internal rows): Σ_r w_r / hz^e_r |y_a − y_b|²,
+// hz = omega / 2π, e_r = 0 for white sources (noise_e null when all are white);
+// fixed butterfly
+__device__ double noise_sum(const AcDev &a, const double2 *y, long long f, int lane) {
   const DTpl &T = a.T;
   double acc = 0.0;
   for (int r = lane; r < a.n_noise; r += 32) {
@@ -119,7 +121,12 @@ __device__ double noise_sum(const AcDev &a, const double2 *y, int lane) {
     const double2 ya = na < 0 ? make_double2(0.0, 0.0) : y[T.eq_pos[na]];
     const double2 yb = nb < 0 ? make_double2(0.0, 0.0) : y[T.eq_pos[nb]];
     const double hr = ya.x - yb.x, hi = ya.y - yb.y;
-    acc += a.noise_w[r] * (hr * hr + hi * hi);
+    double w = a.noise_w[r];
+    if (a.noise_e) {
+      const double e = a.noise_e[r];
+      if (e != 0.0) w /= pow(a.omega[f] / 6.283185307179586, e);
+    }
+    acc += w * (hr * hr + hi * hi);
   }
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
   return acc;
@@ -223,7 +230,7 @@ __global__ void __launch_bounds__(128) ac_kernel(AcDev a) {
         double2 *out = reinterpret_cast<double2 *>(a.resp) + f * a.n_probe;
         for (int k = lane; k < a.n_probe; k += 32) out[k] = v[T.iorder[a.probe[k]]];
       } else {
-        const double p = noise_sum(a, v, lane);
+        const double p = noise_sum(a, v, f, lane);
         if (lane == 0) a.psd[f] = p;
       }
     } else if (lane == 0) {
@@ -317,7 +324,7 @@ __global__ void __launch_bounds__(128) ac_dense_kernel(AcDev a) {
         if (lane == 0)
           for (int k = n - 1; k >= 0; --k) if (piv[k] != k) { const double2 t = r[k]; r[k] = r[piv[k]]; r[piv[k]] = t; }
         __syncwarp();
-        const double p = noise_sum(a, r, lane);
+        const double p = noise_sum(a, r, f, lane);
         if (lane == 0) a.psd[f] = p;
       }
     } else if (lane == 0) {

@@ -117,7 +117,8 @@ struct AcDev {
   const double *b;                    // [n] drive -dFi/d(eps), original equation order (AC)
   const int *probe; int n_probe;      // original unknowns (noise: probe[0])
   double *resp;                       // [n_freq * n_probe] complex (re, im)
-  int n_noise; const int *noise_a, *noise_b; const double *noise_w;  // thermal noise currents
+  int n_noise; const int *noise_a, *noise_b; const double *noise_w;  // noise currents: terminals, power
+  const double *noise_e;              // [n_noise] frequency exponents, or null when every source is white
   double *psd;                        // [n_freq]
   double2 *ws; long long ws_stride;   // per warp: lu [nnz_lu], rd [n], v [n], rhs [n]
   long long n_warps;                  // workspaces in ws (warps that take frequencies)

@@ -278,6 +278,14 @@ VA_HD double va_noise(double *nz, int j, double pwr) {
   return 0.0;
 }
 
+// flicker_noise(pwr, ex): likewise zero outside a noise analysis, where it is a
+// source of density pwr / f^ex; nz holds the n sources' powers, then their
+// exponents (white sources keep exponent 0)
+VA_HD double va_flicker(double *nz, int j, int n, double pwr, double ex) {
+  if (nz) { nz[j] += pwr; nz[n + j] = ex; }
+  return 0.0;
+}
+
 // Real to integer conversion (VA-LRM 4.2.1.1: round half away from zero) and
 // integer division (truncation toward zero)
 VA_HD double vint(double x) { return round(x); }

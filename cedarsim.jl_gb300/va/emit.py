@@ -55,7 +55,7 @@ class VAModel:
     flops: int
     given: List[str] = dataclasses.field(default_factory=list)   # parameters queried by $param_given
     vbranch: Optional[Tuple[str, Optional[str]]] = None  # the voltage-contributed branch (a, b), if any
-    noise: List[Tuple[int, int]] = dataclasses.field(default_factory=list)  # white_noise sources: (a, b or -1)
+    noise: List[Tuple[int, int]] = dataclasses.field(default_factory=list)  # noise sources: (a, b or -1)
 
     @property
     def internals(self) -> List[str]:
@@ -281,11 +281,12 @@ class _Analysis:
         raise VAError(f"{self.mod.name}: unsupported expression {e!r}")
 
     def collect_noise(self, stmts):
-        """white_noise(pwr) terms of current contributions: noise current sources
-        across the contribution's branch, numbered in source order."""
+        """white_noise(pwr) and flicker_noise(pwr, ex) terms of current
+        contributions: noise current sources across the contribution's branch,
+        numbered in source order."""
         def calls(e, out):
             if isinstance(e, Call):
-                if e.fn == "white_noise":
+                if e.fn in ("white_noise", "flicker_noise"):
                     out.append(e)
                 for a in e.args:
                     calls(a, out)
@@ -305,7 +306,7 @@ class _Analysis:
                     if isinstance(x, Contrib):
                         calls(x.expr, found)
                 if found:
-                    raise VAError(f"{self.mod.name}: white_noise() inside a loop")
+                    raise VAError(f"{self.mod.name}: {found[0].fn}() inside a loop")
             if isinstance(s, If):
                 self.collect_noise(s.then)
                 self.collect_noise(s.other)
@@ -651,7 +652,14 @@ class _Emitter:
                     raise VAError(f"{self.m.name}: line {e.line}: white_noise() outside a current contribution")
                 return f"va_noise(nz, {self.a.noise_index[id(e)]}, val({self.x(e.args[0])}))"
             if e.fn == "flicker_noise":
-                return "0.0"           # (not part of the noise analysis)
+                # density pwr / f^ex in a noise analysis, zero elsewhere
+                if id(e) not in self.a.noise_index:
+                    raise VAError(f"{self.m.name}: line {e.line}: flicker_noise() outside a current contribution")
+                ex = [a for a in e.args if not isinstance(a, str)]
+                if len(ex) != 2:
+                    raise VAError(f"{self.m.name}: line {e.line}: flicker_noise() takes a power and an exponent")
+                return (f"va_flicker(nz, {self.a.noise_index[id(e)]}, {len(self.a.noise)}, val({self.x(ex[0])}), "
+                        f"val({self.x(ex[1])}))")
             if e.fn in self.a.funcs:
                 f = self.a.funcs[e.fn]
                 if len(e.args) != len(f.inputs):
@@ -838,12 +846,17 @@ class _Emitter:
         return "\n".join(L)
 
     def noise(self) -> str:
-        """Powers (A^2/Hz, unscaled by m) of the module's white_noise sources at v."""
+        """Powers (A^2/Hz at 1 Hz, unscaled by m) and frequency exponents (0 for
+        white_noise, ex of flicker_noise) of the module's noise sources at v."""
         m = self.m
-        L = [f"inline int noise_{m.name}(const double *dp, int ds, const double *v, double gmin, double *pw) {{",
-             f"  for (int j = 0; j < {len(m.noise)}; ++j) pw[j] = 0.0;"]
-        L += self.prologue("pw")
-        L.append(f"  return {len(m.noise)};")
+        n = len(m.noise)
+        L = [f"inline int noise_{m.name}(const double *dp, int ds, const double *v, double gmin, double *pw, "
+             f"double *ex) {{",
+             f"  double nz[{2 * n}];",
+             f"  for (int j = 0; j < {2 * n}; ++j) nz[j] = 0.0;"]
+        L += self.prologue("nz")
+        L.append(f"  for (int j = 0; j < {n}; ++j) {{ pw[j] = nz[j]; ex[j] = nz[{n} + j]; }}")
+        L.append(f"  return {n};")
         L.append("}")
         return "\n".join(L)
 
@@ -914,7 +927,7 @@ def emit_header(models: List[Tuple[VAModel, _Analysis]], base_id: int) -> str:
             st += [3, r, k, o]; o += 1
         ptr.append(len(st) // 4)
     L.append(table("kStamps", st))
-    # white_noise sources: per model, (row port, column port or -1) pairs
+    # noise sources: per model, (row port, column port or -1) pairs
     nzs, nzp = [], [0]
     for m, _ in models:
         for a_, b_ in m.noise:
@@ -949,14 +962,15 @@ def emit_header(models: List[Tuple[VAModel, _Analysis]], base_id: int) -> str:
     L.append("  }")
     L.append("  (void)dp; (void)ds; (void)v; (void)vd; (void)xdot; (void)cj; (void)gmin; (void)out;")
     L.append("}")
-    L.append("inline int noise(int k, const double *dp, int ds, const double *v, double gmin, double *pw) {")
+    L.append("inline int noise(int k, const double *dp, int ds, const double *v, double gmin, double *pw, "
+             "double *ex) {")
     L.append("  switch (k) {")
     for i, (m, _) in enumerate(models):
         if m.noise:
-            L.append(f"    case {i}: return noise_{m.name}(dp, ds, v, gmin, pw);")
+            L.append(f"    case {i}: return noise_{m.name}(dp, ds, v, gmin, pw, ex);")
     L.append("    default: break;")
     L.append("  }")
-    L.append("  (void)dp; (void)ds; (void)v; (void)gmin; (void)pw;")
+    L.append("  (void)dp; (void)ds; (void)v; (void)gmin; (void)pw; (void)ex;")
     L.append("  return 0;")
     L.append("}")
     L.append("inline void full(int k, const double *dp, int ds, const double *v, double gmin, double *fi, double *fq, "

@@ -363,10 +363,12 @@ int cedar_ac(cedar_ckt *ckt, const double *x_op, const double *b, int32_t n_freq
  * transfer from the resistor's white thermal noise current (src/simpledevices.jl:
  * 70-75; multiplicity m scales that current with the branch current,
  * src/simulate_ir.jl:54) to the probe, and T = the circuit's temp_c + 273.15.
- * Verilog-A devices add one source per white_noise(pwr) term of a current
- * contribution (src/va_env.jl:82-85): m^2 pwr across that contribution's branch,
- * pwr evaluated at x_op.  One transposed solve (G + j omega C)^T y = e_probe per
- * frequency gives every H_r at once. */
+ * Verilog-A devices add one source per white_noise(pwr) or flicker_noise(pwr, ex)
+ * term of a current contribution (src/va_env.jl:82-90): density m^2 pwr
+ * (white) or m^2 pwr / f^ex with f = omega / 2 pi (flicker, src/ac.jl:267-276)
+ * across that contribution's branch, pwr and ex evaluated at x_op.  One
+ * transposed solve (G + j omega C)^T y = e_probe per frequency gives every H_r
+ * at once. */
 int cedar_noise(cedar_ckt *ckt, const double *x_op, int32_t n_freq, const double *omega, int32_t probe,
                 double *psd, int32_t *status);
 /* Of the last cedar_ac / cedar_noise call on this handle: how many frequencies

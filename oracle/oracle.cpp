@@ -1030,11 +1030,11 @@ int oracle_va_full(int k, const double *dp, const double *v, double gmin, double
   return 0;
 }
 
-// Powers of a Verilog-A device's white_noise sources through the emitted code
-// (dp, v as oracle_va_full); returns the number of sources.
-int oracle_va_noise(int k, const double *dp, const double *v, double gmin, double *pw) {
+// Powers and frequency exponents of a Verilog-A device's noise sources through
+// the emitted code (dp, v as oracle_va_full); returns the number of sources.
+int oracle_va_noise(int k, const double *dp, const double *v, double gmin, double *pw, double *ex) {
   if (k < 0 || k >= cedar::va::kCount) { g_err = "Verilog-A model index out of range"; return -1; }
-  return cedar::va::noise(k, dp, 1, v, gmin, pw);
+  return cedar::va::noise(k, dp, 1, v, gmin, pw, ex);
 }
 
 double oracle_next_breakpoint(const cedar_ckt_desc *d, double t, double eps) {

@@ -72,7 +72,7 @@ def load(pkg):
     lib.oracle_va_full.restype = C.c_int
     lib.oracle_va_full.argtypes = [C.c_int, dp, dp, C.c_double, dp, dp, dp, dp]
     lib.oracle_va_noise.restype = C.c_int
-    lib.oracle_va_noise.argtypes = [C.c_int, dp, dp, C.c_double, dp]
+    lib.oracle_va_noise.argtypes = [C.c_int, dp, dp, C.c_double, dp, dp]
     lib.oracle_last_error.restype = C.c_int
     lib.oracle_last_error.argtypes = [C.c_char_p, C.c_size_t]
     _lib = lib
@@ -126,16 +126,17 @@ class Oracle:
     def noise(self, flat, x_op, omegas, probe):
         """Output PSD at `probe` (PSD, src/ac.jl:263-283): one direct solve per
         resistor thermal-noise current, pwr = 4 k T / r (src/simpledevices.jl:70-75),
-        and per white_noise source of a Verilog-A device (its power at x_op from
-        the interpreter), scaled by the multiplicity like the branch current
-        (src/simulate_ir.jl:54)."""
+        and per noise source of a Verilog-A device (its power and exponent at
+        x_op from the interpreter; density pwr / f^exp, f = omega / 2 pi), scaled
+        by the multiplicity like the branch current (src/simulate_ir.jl:54)."""
         _, _, _, G, Cm = self.eval(flat, x_op, dc=True)
         n = flat.n
         kT4 = 4.0 * 1.380649e-23 * (flat.temp_c + 273.15)
-        cols, pwr = [], []
-        for inj, pw in self._va_noise(flat, x_op):
+        cols, pwr, ex = [], [], []
+        for inj, pw, e in self._va_noise(flat, x_op):
             cols.append(inj)
             pwr.append(pw)
+            ex.append(e)
         for (model, term, br, par) in flat.groups:
             if model != 1:
                 continue
@@ -148,18 +149,21 @@ class Oracle:
                     inj[c] -= par[1, i]
                 cols.append(inj)
                 pwr.append(kT4 / par[0, i])
+                ex.append(0.0)
         out = np.zeros(len(omegas))
         if not cols:
             return out
-        INJ, pwr = np.array(cols).T.astype(complex), np.array(pwr)
+        INJ, pwr, ex = np.array(cols).T.astype(complex), np.array(pwr), np.array(ex)
         for k, w in enumerate(omegas):
             H = np.linalg.solve(G + 1j * w * Cm, INJ)[probe]
-            out[k] = float(np.sum(pwr * np.abs(H) ** 2))
+            f = w / (2.0 * np.pi)
+            dens = np.array([p if e == 0.0 else p / f ** e for p, e in zip(pwr, ex)])
+            out[k] = float(np.sum(dens * np.abs(H) ** 2))
         return out
 
     def _va_noise(self, flat, x_op):
-        """Injection vectors and powers (m^2 pwr) of the Verilog-A devices'
-        white_noise sources at x_op, from the independent interpretation of
+        """Injection vectors, powers (m^2 pwr) and exponents of the Verilog-A
+        devices' noise sources at x_op, from the independent interpretation of
         their modules (oracle/va_interp.py)."""
         import importlib.util
         va = self.pkg.va
@@ -182,13 +186,13 @@ class Oracle:
                 idx = list(term[i]) + ([int(br[i])] if br is not None else [])
                 v = [x_op[u] if u >= 0 else 0.0 for u in idx]
                 mult = vals[-1]
-                for (a, b), pw in vi.noise_sources(m.module, prm, v, vt, flat.gmin, mult, given):
+                for (a, b), pw, e in vi.noise_sources(m.module, prm, v, vt, flat.gmin, mult, given):
                     inj = np.zeros(flat.n)
                     if idx[a] >= 0:
                         inj[idx[a]] += mult
                     if b >= 0 and idx[b] >= 0:
                         inj[idx[b]] -= mult
-                    out.append((inj, pw))
+                    out.append((inj, pw, e))
         return out
 
     def dcop(self, flat, t=0.0, x0=None, opts=None):

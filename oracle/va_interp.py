@@ -199,7 +199,7 @@ class Interp:
         self.vars = {name: (0 if t == "integer" else self._const(0.0)) for name, t in module.variables.items()}
         self.types = dict(module.variables)
         self.given = set(given)
-        self.noise = []             # ((a index, b index or -1), power) of each white_noise evaluated
+        self.noise = []             # ((a index, b index or -1), power, exponent) of each noise source evaluated
         self._branch = None
         self.Fi = [self._const(0.0) for _ in range(N)]
         self.Fq = [self._const(0.0) for _ in range(N)]
@@ -291,9 +291,12 @@ class Interp:
             if fn == "white_noise":
                 # zero outside a noise analysis; record the source across the
                 # branch of the contribution being evaluated
-                self.noise.append((self._branch, value(self.expr(e.args[0]))))
+                self.noise.append((self._branch, value(self.expr(e.args[0])), 0.0))
                 return 0.0
             if fn == "flicker_noise":
+                # density pwr / f^ex (PSD, src/ac.jl:267-276)
+                pw, ex = [value(self.expr(a)) for a in e.args if not isinstance(a, str)]
+                self.noise.append((self._branch, pw, ex))
                 return 0.0
             if fn in getattr(self.mod, "functions", {}):
                 return self._call(self.mod.functions[fn], e.args)
@@ -451,8 +454,10 @@ def evaluate(module, params: Dict[str, float], v: List[float], vt: float, gmin: 
 
 def noise_sources(module, params: Dict[str, float], v: List[float], vt: float, gmin: float, m: float = 1.0,
                   given=()):
-    """[((a, b), power)] of the module's white_noise sources at port potentials v
-    (b = -1 for ground), unscaled by the multiplicity."""
+    """[((a, b), power, exponent)] of the module's noise sources at port
+    potentials v (b = -1 for ground; exponent 0 for white_noise, the density of
+    a flicker_noise source being power / f^exponent), unscaled by the
+    multiplicity."""
     it = Interp(module, params, v, vt, gmin, m, given)
     it.run()
     return it.noise

@@ -424,12 +424,14 @@ def test_white_noise_sources(pkg, oracle, va, interp):
             prm = _params(m, rng)
             vals = m.defaults(prm)
             v = rng.uniform(-1, 1, m.nx)
-            pw = np.zeros(len(m.noise))
-            assert lib.oracle_va_noise(k, dp_(np.array(vals + [1.0, VT])), dp_(v), 1e-12, dp_(pw)) == len(m.noise)
+            pw, ex = np.zeros(len(m.noise)), np.full(len(m.noise), np.nan)
+            assert lib.oracle_va_noise(k, dp_(np.array(vals + [1.0, VT])), dp_(v), 1e-12, dp_(pw),
+                                       dp_(ex)) == len(m.noise)
             src = interp.noise_sources(m.module, dict(zip([p.name for p in m.params], vals)), list(v), VT, 1e-12,
                                        1.0, [g for g in m.given if g in prm])
             assert [s[0] for s in src] == m.noise
             assert pw[0] == pytest.approx(src[0][1], rel=1e-14)
+            assert ex[0] == src[0][2] == 0.0
     fb, fv = K.butterworth_ac(pkg).flatten(), K.butterworth_ac_va(pkg).flatten()
     x, _, rc = oracle.dcop(fb)
     assert rc == 0
@@ -440,6 +442,52 @@ def test_white_noise_sources(pkg, oracle, va, interp):
     g = json.loads((ROOT / "tests" / "golden" / "ac_noise_ngspice.json").read_text())
     ref = np.array(g["sqrt_psd"])
     assert np.all(np.abs(np.sqrt(pv) - ref) <= 1e-6 * np.maximum(np.abs(ref), np.abs(np.sqrt(pv))))
+
+
+def test_flicker_noise(pkg, oracle, va, interp):
+    """flicker_noise(pwr, ex) is a noise source of density pwr / f^ex (PSD,
+    src/ac.jl:267-276): the emitted code and the interpreter agree on power and
+    exponent, and a divider of a 1/f resistor over a plain one has the analytic
+    output PSD (R1 || R2)^2 (4kT/R1 + 4kT/R2 + KF |I|^AF / f^EF)."""
+    lib = oracle.lib
+    dp_ = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    k = va.model_id("va_resistor_1f") - va.BASE_ID
+    m = va.models()[k]
+    assert len(m.noise) == 2 and m.noise[0] == m.noise[1] == (0, 1)
+    prm = {"R": 3e3, "KF": 2e-21, "AF": 1.7, "EF": 1.1}
+    vals = m.defaults(prm)
+    v = np.array([0.4, -0.2])
+    pw, ex = np.zeros(2), np.zeros(2)
+    assert lib.oracle_va_noise(k, dp_(np.array(vals + [1.0, VT])), dp_(v), 1e-12, dp_(pw), dp_(ex)) == 2
+    src = interp.noise_sources(m.module, dict(zip([p.name for p in m.params], vals)), list(v), VT, 1e-12, 1.0,
+                               [g for g in m.given if g in prm])
+    i = 0.6 / 3e3
+    assert [s[2] for s in src] == [0.0, 1.1] and list(ex) == [0.0, 1.1]
+    np.testing.assert_allclose(pw, [s[1] for s in src], rtol=1e-14)
+    assert pw[1] == pytest.approx(2e-21 * i ** 1.7, rel=1e-13)
+
+    R1, R2, KF, AF, EF, vdd = 3e3, 1e3, 1e-19, 2.0, 1.0, 2.0
+    c = pkg.Circuit(temp_c=27.0, gmin=0.0)
+    c.V("V1", "vin", "0", dc=vdd)
+    c.va("R1", "va_resistor_1f", ["vin", "out"], R=R1, KF=KF, AF=AF, EF=EF)
+    c.R("R2", "out", "0", R2)
+    f = c.flatten()
+    x, _, rc = oracle.dcop(f)
+    assert rc == 0
+    hz = np.array([0.1, 1.0, 10.0, 1e3, 1e6])
+    psd = oracle.noise(f, x, 2 * np.pi * hz, f.index("out"))
+    kT4 = 4 * 1.380649e-23 * (27.0 + 273.15)
+    rp = R1 * R2 / (R1 + R2)
+    want = rp ** 2 * (kT4 / R1 + kT4 / R2 + KF * (vdd / (R1 + R2)) ** AF / hz ** EF)
+    np.testing.assert_allclose(psd, want, rtol=1e-10)
+    # zero KF leaves the thermal noise of the two resistors only
+    c0 = pkg.Circuit(temp_c=27.0, gmin=0.0)
+    c0.V("V1", "vin", "0", dc=vdd)
+    c0.va("R1", "va_resistor_1f", ["vin", "out"], R=R1)
+    c0.R("R2", "out", "0", R2)
+    f0 = c0.flatten()
+    np.testing.assert_allclose(oracle.noise(f0, x, 2 * np.pi * hz, f0.index("out")),
+                               rp ** 2 * (kT4 / R1 + kT4 / R2), rtol=1e-10)
 
 
 def test_limit_and_step_advice(va):

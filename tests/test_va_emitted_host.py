@@ -137,8 +137,8 @@ def emitted(pkg, tmp_path_factory):
         '#include <math.h>\n#include "va_models.gen.h"\n'
         'extern "C" int h_full(int k, const double *dp, const double *v, double gmin, double *fi, double *fq,'
         ' double *G, double *C) { cedar::va::full(k, dp, 1, v, gmin, fi, fq, G, C); return 0; }\n'
-        'extern "C" int h_noise(int k, const double *dp, const double *v, double gmin, double *pw)'
-        ' { return cedar::va::noise(k, dp, 1, v, gmin, pw); }\n')
+        'extern "C" int h_noise(int k, const double *dp, const double *v, double gmin, double *pw, double *ex)'
+        ' { return cedar::va::noise(k, dp, 1, v, gmin, pw, ex); }\n')
     lib = d / "libharness.so"
     r = subprocess.run(["g++", "-O1", "-std=c++17", "-ffp-contract=off", "-shared", "-fPIC", "-I", str(CSRC), "-I",
                         str(d), str(d / "harness.cpp"), "-o", str(lib)], capture_output=True, text=True)
@@ -188,12 +188,13 @@ def test_emitted_host_code_matches_interpreter(emitted, interp):
             assert np.all(np.abs(G - rG.ravel()) <= 1e-12 * (np.abs(rG).max() + 1e-30)), (m.name, over, G, rG)
             assert np.all(np.abs(Cm - rC.ravel()) <= 1e-12 * (np.abs(rC).max() + 1e-40)), (m.name, Cm, rC)
             if m.noise:
-                pw = np.zeros(len(m.noise))
-                assert h.h_noise(k, dp_(dp), dp_(v), 1e-12, dp_(pw)) == len(m.noise)
+                pw, ex = np.zeros(len(m.noise)), np.full(len(m.noise), np.nan)
+                assert h.h_noise(k, dp_(dp), dp_(v), 1e-12, dp_(pw), dp_(ex)) == len(m.noise)
                 src = interp.noise_sources(m.module, dict(zip([p.name for p in m.params], vals)), list(v), VT, 1e-12,
                                            float(dp[-2]), given)
                 assert [s[0] for s in src] == m.noise
                 np.testing.assert_allclose(pw, [s[1] for s in src], rtol=1e-14)
+                np.testing.assert_allclose(ex, [s[2] for s in src], rtol=1e-14)
 
 
 def test_emitted_structure(emitted):
