@@ -31,6 +31,33 @@ SOURCES = ([("api.cu", "api.cu.o", []), ("k_plain.cu", "k_plain.cu.o", []), ("k_
            + [("k_adjoint.cu", f"k_adjoint.k{k}.o", [f"-DCEDAR_LANES={k}"]) for k in LANES])
 
 
+# Separate mode: when the generated Verilog-A code is large (a BSIM-class model)
+# its evaluation is compiled once, in va_models.cu, and device-linked into the
+# kernels (relocatable device code), instead of once in every kernel
+# translation unit.  CEDAR_VA_SEPARATE=1 / 0 forces the mode either way.
+SEPARATE_BYTES = 128 << 10
+# registers of the separately compiled model code: at most the batched kernel's
+# own allocation, so a large model spills in its own frame and does not raise
+# the register count every engine kernel launches with
+SEPARATE_MAXRREG = 232
+
+
+def separate_mode() -> bool:
+    env = os.environ.get("CEDAR_VA_SEPARATE")
+    if env is not None:
+        return env not in ("", "0")
+    gen = GEN / "va_models.gen.h"
+    return gen.exists() and gen.stat().st_size > SEPARATE_BYTES
+
+
+def _sources(separate: bool):
+    if not separate:
+        return SOURCES
+    rdc = ["-rdc=true", "-DCEDAR_VA_SEPARATE"]
+    out = [(src, obj, extra + rdc if src.endswith(".cu") else extra) for src, obj, extra in SOURCES]
+    return out + [("va_models.cu", "va_models.cu.o", rdc + [f"-maxrregcount={SEPARATE_MAXRREG}"])]
+
+
 def _nvcc() -> str:
     p = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     if not os.path.exists(p):
@@ -38,8 +65,13 @@ def _nvcc() -> str:
     return p
 
 
+MODE = BUILD / "mode"         # the mode the library was built in
+
+
 def _stale() -> bool:
     if not LIB.exists():
+        return True
+    if not MODE.exists() or MODE.read_text() != ("separate" if separate_mode() else "whole"):
         return True
     t = LIB.stat().st_mtime
     deps = list(CSRC.glob("*")) + list(INCLUDE.glob("*.h")) + [pathlib.Path(__file__)]
@@ -74,14 +106,18 @@ def build(force: bool = False, verbose: bool = False) -> pathlib.Path:
             print(r.stdout, r.stderr)
         return str(obj)
 
-    with cf.ThreadPoolExecutor(max_workers=min(len(SOURCES), max(2, os.cpu_count() or 2))) as ex:
-        objs = list(ex.map(compile_one, SOURCES))
+    separate = separate_mode()
+    sources = _sources(separate)
+    with cf.ThreadPoolExecutor(max_workers=min(len(sources), max(2, os.cpu_count() or 2))) as ex:
+        objs = list(ex.map(compile_one, sources))
     tmp = LIB.with_suffix(".so.tmp")
-    cmd = [nvcc, *ARCH, "-shared", "-o", str(tmp), *objs, "-lcudart_static", "-lrt", "-ldl", "-lpthread"]
+    cmd = [nvcc, *ARCH, *(["-rdc=true"] if separate else []), "-shared", "-o", str(tmp), *objs, "-lcudart_static",
+           "-lrt", "-ldl", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    MODE.write_text("separate" if separate else "whole")
     return LIB
 
 

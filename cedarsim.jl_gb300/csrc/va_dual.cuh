@@ -17,7 +17,14 @@
 // the model dispatch is called, not inlined: one copy per translation unit
 // instead of one per evaluation site keeps the engine kernels' build time and
 // register allocation what they are without Verilog-A models
+#ifdef CEDAR_VA_SEPARATE
+// large models: the dispatch is compiled once, in its own translation unit
+// (va_models.cu), and device-linked into the engine kernels
+#define VA_CALL __host__ __device__ __noinline__
+#define VA_EXTERN __host__ __device__
+#else
 #define VA_CALL static __host__ __device__ __noinline__
+#endif
 #else
 #define VA_HD inline
 #define VA_CALL inline

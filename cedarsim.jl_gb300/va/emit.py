@@ -896,7 +896,8 @@ def emit_header(models: List[Tuple[VAModel, _Analysis]], base_id: int) -> str:
     for m, a in models:
         e = _Emitter(m, a)
         fns = e.functions()
-        L += ([fns, ""] if fns else []) + [e.body(), "", e.eval(), "", e.full(), ""]
+        L += ([fns, ""] if fns else []) + [e.body(), "", "#if !defined(CEDAR_VA_SEPARATE) || defined(CEDAR_VA_DEFINE)",
+                                            e.eval(), "#endif", "", e.full(), ""]
         if m.noise:
             L += [e.noise(), ""]
 
@@ -953,8 +954,12 @@ def emit_header(models: List[Tuple[VAModel, _Analysis]], base_id: int) -> str:
     L.append("  for (int i = 0; i < np; ++i) dp[i * ds] = raw[i * rs];")
     L.append("  dp[np * ds] = vt;")
     L.append("}")
-    L.append("VA_CALL void eval(int k, const double *dp, int ds, const double *v, const double *vd, bool xdot, double cj, "
-             "double gmin, double *out) {")
+    sig = ("void eval(int k, const double *dp, int ds, const double *v, const double *vd, bool xdot, double cj, "
+           "double gmin, double *out)")
+    L.append("#if defined(CEDAR_VA_SEPARATE) && !defined(CEDAR_VA_DEFINE)")
+    L.append(f"VA_EXTERN {sig};   // defined in va_models.cu")
+    L.append("#else")
+    L.append(f"VA_CALL {sig} {{")
     L.append("  switch (k) {")
     for i, (m, _) in enumerate(models):
         L.append(f"    case {i}: eval_{m.name}(dp, ds, v, vd, xdot, cj, gmin, out); break;")
@@ -962,6 +967,7 @@ def emit_header(models: List[Tuple[VAModel, _Analysis]], base_id: int) -> str:
     L.append("  }")
     L.append("  (void)dp; (void)ds; (void)v; (void)vd; (void)xdot; (void)cj; (void)gmin; (void)out;")
     L.append("}")
+    L.append("#endif")
     L.append("inline int noise(int k, const double *dp, int ds, const double *v, double gmin, double *pw, "
              "double *ex) {")
     L.append("  switch (k) {")
