@@ -267,6 +267,7 @@ struct cedar_ckt {
   int ac_last_dense = 0;
   bool ac_dense_ran = false;
   int threads = 128;
+  int device = -1;          // the CUDA device current at cedar_ckt_create
   bool host_only = false;
   ~cedar_ckt() {
     for (cudaEvent_t e : ac_ev) if (e) cudaEventDestroy(e);
@@ -341,6 +342,7 @@ int cedar_ckt_create(const cedar_ckt_desc *desc, cedar_ckt **out) {
   auto c = std::make_unique<cedar_ckt>();
   int rc = upload_template(desc, c->tpl);
   if (rc) return rc;
+  CUDA_TRY(cudaGetDevice(&c->device));
   CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   const Template &H = c->tpl->H;
   CUDA_TRY(c->dpar.ensure(H.dpar_size));
@@ -479,6 +481,15 @@ int cedar_eval_dev(cedar_ckt *c, const double *x, const double *xdot, double t, 
   return 0;
 }
 
+int cedar_eval_scratch(const cedar_ckt *c, int64_t *n_out, int64_t *n_part, int64_t *limit) {
+  if (limit) *limit = kEvalScratchMax;
+  if (!c) return (n_out || n_part) ? fail(CEDAR_EINVAL, "null handle") : 0;
+  const Template &H = c->tpl->H;
+  if (n_out) *n_out = H.n_out;
+  if (n_part) *n_part = H.long_jc_fo_off.empty() ? 0 : H.long_jc_fo_off.back();
+  return 0;
+}
+
 int cedar_eval_dev_noalloc(cedar_ckt *c, const double *x, const double *xdot, double t, double cj, double *F,
                            double *J, void *stream) {
   if (!c || !x) return fail(CEDAR_EINVAL, "null argument");
@@ -488,9 +499,23 @@ int cedar_eval_dev_noalloc(cedar_ckt *c, const double *x, const double *xdot, do
     return fail(CEDAR_EINVAL, "circuit needs " + std::to_string((long long)T.n_out + T.n_long_part) +
                 " doubles of evaluation scratch (device outputs and long-row partial sums); the allocation-free "
                 "evaluation holds at most " + std::to_string(kEvalScratchMax));
+  // the scratch address is per device: the handle's device must be current, and
+  // a caller's stream must belong to it
+  int dev = -1;
+  CUDA_TRY(cudaGetDevice(&dev));
+  if (dev != c->device)
+    return fail(CEDAR_EINVAL, "the current device (" + std::to_string(dev) + ") is not the handle's device (" +
+                std::to_string(c->device) + "); make the handle's device current before the call");
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+  if (stream) {
+    int sdev = -1;
+    CUDA_TRY(cudaStreamGetDevice(s, &sdev));
+    if (sdev != c->device)
+      return fail(CEDAR_EINVAL, "the stream belongs to device " + std::to_string(sdev) + ", the handle to device " +
+                  std::to_string(c->device));
+  }
   double *scratch = nullptr;
   CUDA_TRY(eval_scratch_address(&scratch));
-  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
   CUDA_TRY(launch_eval(T, c->tpl->D_dev, c->dpar.p, x, xdot, t, cj, scratch, scratch + T.n_out, F, J, s));
   return 0;
 }

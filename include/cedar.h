@@ -255,16 +255,23 @@ int cedar_eval_dev(cedar_ckt *ckt, const double *x, const double *xdot, double t
  * It has no counterpart in the reference.  It calls no cudaMalloc or cudaFree:
  * its scratch (the per-device model outputs plus the partial sums of
  * supply-rail rows, at most 262144 doubles = 2 MiB; a larger circuit returns
- * CEDAR_EINVAL) is a fixed array that every GPU loading
- * the library holds until the process exits.  The first call on a device looks
- * up that array's device address (cudaGetSymbolAddress with the device current)
- * and caches it, so make the first call on each device before any stream
- * capture.  All calls on a device share the array: calls whose kernels overlap
- * on the GPU race, so order them (same stream, or events).  stream: a
- * cudaStream_t, or NULL for the handle's stream.  The handle itself is created
- * (and allocates) beforehand with cedar_ckt_create. */
+ * CEDAR_EINVAL, see cedar_eval_scratch) is a fixed array that every GPU loading
+ * the library holds until the process exits.  The handle's device (the one
+ * current at cedar_ckt_create) must be current when calling, and a stream passed
+ * in must belong to it; otherwise the call returns CEDAR_EINVAL.  The first call
+ * on a device looks up that array's device address (cudaGetSymbolAddress with
+ * the device current) and caches it, so make the first call on each device
+ * before any stream capture.  All calls on a device share the array: calls whose
+ * kernels overlap on the GPU race, so order them (same stream, or events).
+ * stream: a cudaStream_t, or NULL for the handle's stream.  The handle itself is
+ * created (and allocates) beforehand with cedar_ckt_create. */
 int cedar_eval_dev_noalloc(cedar_ckt *ckt, const double *x, const double *xdot, double t, double cj,
                            double *F, double *Jvals, void *stream);
+/* Scratch that cedar_eval_dev_noalloc needs for this circuit: n_out device
+ * outputs plus n_part partial sums of supply-rail rows (any pointer may be NULL),
+ * and the fixed limit on their sum.  ckt may be NULL when only the limit is
+ * asked for.  No counterpart in the reference. */
+int cedar_eval_scratch(const cedar_ckt *ckt, int64_t *n_out, int64_t *n_part, int64_t *limit);
 
 /* One implicit step: solve Fi(x, t) + cj*Fq(x) + hist = 0 for x by Newton with
  * refactorisation every iteration.  hist (may be NULL) is the integrator history

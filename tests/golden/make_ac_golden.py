@@ -2,9 +2,9 @@
 test holds for its third-order Butterworth filter (test/ac.jl:83-145, asserted
 against the analytic PSD at rtol 1e-6 in test/ac.jl:148-149).
 
-The table is read from the CedarSim checkout given on the command line (default
-/root/reference); the JSON it writes is the committed fixture, so the tests do not
-need the checkout.  Columns: frequency (Hz) and sqrt(PSD) of V(vout) (V/sqrt(Hz)).
+The table is read from the CedarSim checkout whose directory is given on the
+command line (required); the JSON it writes is the committed fixture, so the tests
+do not need the checkout.  Usage: python make_ac_golden.py <CedarSim checkout>  Columns: frequency (Hz) and sqrt(PSD) of V(vout) (V/sqrt(Hz)).
 """
 import json
 import pathlib
@@ -24,7 +24,9 @@ def extract(path: pathlib.Path):
 
 
 if __name__ == "__main__":
-    ref = pathlib.Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python make_ac_golden.py <CedarSim checkout directory>")
+    ref = pathlib.Path(sys.argv[1])
     first, rows = extract(ref / "test" / "ac.jl")
     out = {
         "src": f"test/ac.jl:{first}-{first + len(rows) + 1}",

@@ -3,10 +3,12 @@
 cedar_eval_dev_noalloc serves callers that may not allocate device memory when
 they call (real-time loops that ban allocation after set-up, hosts whose device
 memory another runtime's pool allocator reserved up front): its scratch is a
-fixed per-device array inside the library.  This test drives both
-entry points through the C ABI on the same device buffers and checks that the
-results agree within the evaluation tolerance of the other GPU tests, on two calls
-in a row (the second with a different state, so stale scratch would show).
+fixed per-device array inside the library.  This test drives both entry points
+through the C ABI on the same device buffers and checks that the results are the
+same bits (both run the same kernels; only the scratch differs), on two calls in
+a row with different states, so stale scratch would show.  One case has supply
+rails longer than the long-row threshold, so the partial-sum region of the
+scratch is exercised as well as the device outputs.
 """
 import ctypes as C
 
@@ -17,19 +19,37 @@ from tests import circuits as K
 
 pytestmark = pytest.mark.gpu
 
-RTOL_EVAL = 1e-12
-
 
 def _ptr(t):
     return C.c_void_p(t.data_ptr())
 
 
-@pytest.mark.parametrize("case", ["inverter_chain", "mixed"])
+def _scratch(lib, handle):
+    n_out, n_part, limit = C.c_int64(), C.c_int64(), C.c_int64()
+    rc = lib.cedar_eval_scratch(handle, C.byref(n_out), C.byref(n_part), C.byref(limit))
+    assert rc == 0
+    return n_out.value, n_part.value, limit.value
+
+
+def _flat(pkg, case):
+    if case == "inverter_chain":
+        return pkg.generators.inverter_chain(9).flatten()
+    if case == "long_rails":
+        return pkg.generators.inverter_chain(100).flatten()
+    return K.mixed(pkg).flatten()
+
+
+@pytest.mark.parametrize("case", ["inverter_chain", "mixed", "long_rails"])
 def test_noalloc_eval_matches_allocating_eval(gpu, pkg, case):
     import torch
-    flat = (pkg.generators.inverter_chain(9) if case == "inverter_chain" else K.mixed(pkg)).flatten()
+    flat = _flat(pkg, case)
     sys_ = pkg.System(flat)
     lib = sys_.lib
+    n_out, n_part, limit = _scratch(lib, sys_.handle)
+    assert 0 < n_out + n_part <= limit
+    if case == "long_rails":
+        # the 100-stage chain's supply rows (200 entries) exceed the long-row threshold
+        assert n_part > 0
     n, nj = sys_.n, sys_.nnz_j
     dev = torch.device("cuda:0")
     rng = np.random.default_rng(17)
@@ -50,23 +70,46 @@ def test_noalloc_eval_matches_allocating_eval(gpu, pkg, case):
         Fr, Fn = F_ref.cpu().numpy(), F_new.cpu().numpy()
         Jr, Jn = J_ref.cpu().numpy(), J_new.cpu().numpy()
         assert np.all(np.isfinite(Fn)) and np.all(np.isfinite(Jn))
-        assert np.all(np.abs(Fn - Fr) <= RTOL_EVAL * np.abs(Fr) + 1e-300)
-        assert np.all(np.abs(Jn - Jr) <= RTOL_EVAL * np.abs(Jr) + 1e-300)
+        assert np.array_equal(Fn, Fr) and np.array_equal(Jn, Jr)
+
+
+def test_noalloc_allocates_nothing(gpu, pkg):
+    """100 calls leave the device's free memory unchanged (after one warm-up call,
+    which loads the kernels and looks up the scratch address)."""
+    import torch
+    sys_ = pkg.System(pkg.generators.inverter_chain(100).flatten())
+    lib = sys_.lib
+    dev = torch.device("cuda:0")
+    x = torch.rand(sys_.n, dtype=torch.float64, device=dev) * 1.8
+    F = torch.empty(sys_.n, dtype=torch.float64, device=dev)
+    J = torch.empty(sys_.nnz_j, dtype=torch.float64, device=dev)
+    call = lambda: pkg.abi.check(lib.cedar_eval_dev_noalloc(sys_.handle, _ptr(x), None, 1e-9, 1e12, _ptr(F), _ptr(J),
+                                                            None))
+    call()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(100):
+        call()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert bool(torch.isfinite(F).all()) and bool(torch.isfinite(J).all())
 
 
 def test_noalloc_rejects_oversized_circuit(gpu, pkg):
-    """A circuit whose device outputs exceed the fixed scratch gets a clear error
+    """A circuit whose scratch need exceeds the fixed array gets a clear error
     from the host-side size check, before anything is launched."""
     import torch
-    limit = 262144
-    n_caps = 100000                      # 3 outputs each, plus 4 for the source
-    n_out = 3 * n_caps + 4
-    assert n_out > limit + 30000         # well past the limit
+    lib = pkg.load_library()
+    _, _, limit = _scratch(lib, None)
     c = pkg.Circuit()
     c.V("V1", "a", "0", dc=1.0)
+    n_caps = limit // 3 + 1000
     for k in range(n_caps):
         c.C(f"C{k}", "a", "0", 1e-15)
     sys_ = pkg.System(c)
+    n_out, n_part, limit2 = _scratch(lib, sys_.handle)
+    assert limit2 == limit and n_out + n_part > limit
     dev = torch.device("cuda:0")
     # valid, correctly sized buffers, so that the call is well formed apart from the size
     x = torch.zeros(sys_.n, dtype=torch.float64, device=dev)
@@ -74,7 +117,7 @@ def test_noalloc_rejects_oversized_circuit(gpu, pkg):
     J = torch.zeros(sys_.nnz_j, dtype=torch.float64, device=dev)
     torch.cuda.synchronize()
     buf = C.create_string_buffer(256)
-    rc = sys_.lib.cedar_eval_dev_noalloc(sys_.handle, _ptr(x), None, 0.0, 0.0, _ptr(F), _ptr(J), None)
+    rc = lib.cedar_eval_dev_noalloc(sys_.handle, _ptr(x), None, 0.0, 0.0, _ptr(F), _ptr(J), None)
     assert rc == -1
-    sys_.lib.cedar_last_error(buf, 256)
-    assert b"at most 262144" in buf.value
+    lib.cedar_last_error(buf, 256)
+    assert f"at most {limit}".encode() in buf.value
