@@ -62,11 +62,11 @@ def parse():
     p.add_argument("--no-rings", action="store_true", help="skip the ring-oscillator leg")
     p.add_argument("--no-ac", action="store_true", help="skip the AC / noise sweep leg")
     p.add_argument("--ac-freq", type=int, default=1 << 17, help="frequency points of the AC / noise leg")
-    p.add_argument("--no-va", action="store_true", help="skip the Verilog-A model leg")
-    p.add_argument("--va-inst", type=int, default=1024, help="instances of the Verilog-A leg")
-    p.add_argument("--va-tstop-ns", type=float, default=5.0)
+    p.add_argument("--no-va", action="store_true", help="skip the Verilog-A model legs (chains and rings)")
     p.add_argument("--ring-inst", type=int, default=1024)
     p.add_argument("--ring-tstop-ns", type=float, default=50.0)
+    p.add_argument("--ring-ref-inst", type=int, default=32, help="instances in the CPU sample of the ring leg")
+    p.add_argument("--no-plain-configs", action="store_true", help="skip configurations 1 and 2 (single circuits)")
     p.add_argument("--eval-stages", type=int, default=1_000_000, help="inverter-chain stages of the cedar_eval leg")
     p.add_argument("--adj-inst", type=int, default=512, help="instances of the adjoint workload")
     p.add_argument("--adj-tstop-ns", type=float, default=20.0)
@@ -251,11 +251,14 @@ def measure_eval(pkg, args, torch, C):
             "timing": f"CUDA events on the handle's stream around {reps} calls after 3 warm-up calls"}
 
 
-def measure_rings(pkg, args, C):
-    """Workload 4: 15-stage current-starved ring oscillators (VA MOS1 + exponential
-    diodes, RC supply per stage), DC operating point + N(0, 1 mV) per node, adaptive
-    BDF2 to 50 ns, in one batched launch timed with CUDA events (DC included)."""
+def measure_rings(pkg, args, C, fp64_peak, verilog_a=False):
+    """Workload 4: 15-stage current-starved ring oscillators (level-1 MOSFETs +
+    exponential diodes, RC supply per stage), DC operating point + N(0, 1 mV) per
+    node, adaptive BDF2 to 50 ns, in one batched launch timed with CUDA events (DC
+    included).  verilog_a: the MOSFETs and diodes as the emitted va_mos1 / va_diode."""
     tpl, itpl, par, off, dx, dxo = pkg.generators.mc_rings(args.ring_inst, seed=args.seed)
+    if verilog_a:
+        tpl = [pkg.generators.as_verilog_a(f) for f in tpl]
     f = tpl[0]
     probes = np.array([[f.index("out1")]], np.int32)
     sw = pkg.Batch(tpl, itpl, par, off, inst_dx=dx, inst_dx_off=dxo, probes=probes, n_samples=501)
@@ -267,48 +270,71 @@ def measure_rings(pkg, args, C):
     ok = r.stats["status"] == 0
     s = r.samples[:, 0, :]
     osc = int(np.sum((s.max(axis=1) - s.min(axis=1)) > 1.0))
-    return {"workload": f"{args.ring_inst} x 15-stage current-starved ring oscillators (VA MOS1 + exp diodes, "
+    fl = float(flops_per_iteration(pkg, tpl)[0])
+    iters = float(r.stats["newton_iters"].sum() + r.stats["dc_iters"].sum())
+    tfl = fl * iters / (ms.value / 1e3) / 1e12
+    models = "emitted Verilog-A va_mos1 + va_diode" if verilog_a else "built-in level-1 MOSFETs + exponential diodes"
+    return {"workload": f"{args.ring_inst} x 15-stage current-starved ring oscillators ({models}, "
                         f"100 Ohm / 100 fF supply per stage), DC op + N(0, 1 mV) per node, adaptive BDF2 to "
                         f"{args.ring_tstop_ns:g} ns", "value": float(r.stats["accepted"].sum()) / (ms.value / 1e3),
             "unit": "instance-timesteps/s", "ms": ms.value, "failed_instances": int((~ok).sum()),
             "oscillating_instances": osc, "accepted_steps_mean": float(r.stats["accepted"].mean()),
-            "newton_iters_per_s": float(r.stats["newton_iters"].sum() + r.stats["dc_iters"].sum()) / (ms.value / 1e3),
+            "accepted_steps": int(r.stats["accepted"].sum()),
+            "newton_iters_per_s": iters / (ms.value / 1e3),
+            "roofline": {"bound": "fp64", "achieved": tfl, "peak": fp64_peak, "unit": "TFLOP/s",
+                         "frac": tfl / fp64_peak, "flops_per_newton_iter": fl},
             "tuning": list(sw.tuning), "timing": "CUDA events around one cedar_batch_run launch (DC operating points included)"}
 
 
-def measure_va(pkg, args, C):
-    """The Monte Carlo chains with their MOSFETs as the Verilog-A level-1 model
-    compiled by the emitter (va_mos1: the built-in model's equations and
-    parameter block, evaluated over dual numbers), timed beside the built-in
-    model on the same instances: the cost of generic emitted device code."""
-    import copy
-    va_id = pkg.va.model_id("va_mos1")
-    templates, itpl, par, off = pkg.generators.mc_chains(args.va_inst, seed=args.seed)
-    va_tpl = []
-    for f in templates:
-        g = copy.deepcopy(f)
-        g.groups = [(va_id if m == pkg.circuit.MOS1 else m, t, b, p) for (m, t, b, p) in g.groups]
-        assert [x[0] for x in g.groups] == sorted(x[0] for x in g.groups)   # same group (block) order
-        va_tpl.append(g)
-    tstop = args.va_tstop_ns * 1e-9
-    o = pkg.make_opts("bdf2", True, 0.0, tstop, 0.0, True, reltol=1e-6, abstol_v=1e-9)
-    res = {}
-    for name, tp in (("builtin", templates), ("verilog_a", va_tpl)):
-        sw = pkg.Batch(tp, itpl, par, off)
-        sw.run(pkg.make_opts("bdf2", True, 0.0, 0.05e-9, 0.0, True))     # warm-up
-        r = sw.run(o)
-        ms = C.c_double()
-        pkg.abi.check(sw.lib.cedar_batch_last_ms(sw.handle, C.byref(ms)))
-        res[name] = {"value": float(r.stats["accepted"].sum()) / (ms.value / 1e3), "ms": ms.value,
-                     "failed_instances": int((r.stats["status"] != 0).sum()),
-                     "accepted_steps": int(r.stats["accepted"].sum())}
-        del sw
-    return {"workload": f"{args.va_inst} MC chains (L in {{5..63}}), adaptive BDF2 to {args.va_tstop_ns:g} ns, "
-                        "MOSFETs as the emitted Verilog-A va_mos1 vs the built-in level-1 model",
-            "unit": "instance-timesteps/s", "value": res["verilog_a"]["value"], "builtin": res["builtin"],
-            "verilog_a": res["verilog_a"], "va_over_builtin": res["verilog_a"]["value"] / res["builtin"]["value"],
-            "same_step_counts": res["verilog_a"]["accepted_steps"] == res["builtin"]["accepted_steps"],
-            "timing": "CUDA events around one cedar_batch_run launch each (DC operating points included)"}
+def reference_rings(args, pkg, orc):
+    """The oracle (OpenMP over instances, all host threads) on a bounded random
+    sample of the ring-oscillator workload, each instance over the full horizon."""
+    tpl, itpl, par, off, dx, dxo = pkg.generators.mc_rings(args.ring_inst, seed=args.seed)
+    k = max(1, min(args.ring_ref_inst, args.ring_inst))
+    sel = np.sort(np.random.default_rng(3).choice(args.ring_inst, size=k, replace=False))
+    sub = pkg.abi.BatchHolder(tpl, itpl[sel], par, off[sel], inst_dx=dx, inst_dx_off=dxo[sel])
+    tstop = args.ring_tstop_ns * 1e-9
+    o = pkg.make_opts("bdf2", True, 0.0, tstop, 0.0, True, reltol=1e-6, abstol_v=1e-9, hmax=tstop / 50)
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    xf, samp, st = orc.batch(sub, o, 0, len(sel), nthreads=cores, want_samples=False)
+    dt = time.perf_counter() - t0
+    return {"value": float(st["accepted"].sum()) / dt, "unit": "instance-timesteps/s", "cores": cores,
+            "kind": "port", "sample": f"{k} randomly chosen instances of the {args.ring_inst}, each DC + "
+                                      f"0..{args.ring_tstop_ns:g} ns", "seconds": dt,
+            "failed": int((st["status"] != 0).sum())}
+
+
+def measure_va(pkg, args, C, builtin_ms, builtin_steps, fp64_peak):
+    """Workload 3 at full size with the MOSFETs as the Verilog-A level-1 model
+    compiled by the emitter (va_mos1: the built-in model's equations and parameter
+    block, evaluated over dual numbers), in one cedar_batch_run (DC included),
+    against the built-in model's complete run of the same instances (the e2e run's
+    kernel time): the cost of generic emitted device code."""
+    templates, itpl, par, off = pkg.generators.mc_chains(args.n_inst, seed=args.seed)
+    va_tpl = [pkg.generators.as_verilog_a(f) for f in templates]
+    o = opts_for(pkg, args.tstop_ns * 1e-9)
+    sw = pkg.Batch(va_tpl, itpl, par, off)
+    if args.lanes:
+        sw.set_tuning(args.lanes, args.warps or 4)
+    r = sw.run(o)
+    ms = C.c_double()
+    pkg.abi.check(sw.lib.cedar_batch_last_ms(sw.handle, C.byref(ms)))
+    steps = float(r.stats["accepted"].sum())
+    iters = float(r.stats["newton_iters"].sum() + r.stats["dc_iters"].sum())
+    v = steps / (ms.value / 1e3)
+    out = {"workload": f"{args.n_inst} MC chains (L in {{5..63}}), adaptive BDF2 to {args.tstop_ns:g} ns, MOSFETs as "
+                       "the emitted Verilog-A va_mos1", "unit": "instance-timesteps/s", "value": v, "ms": ms.value,
+           "accepted_steps": int(steps), "failed_instances": int((r.stats["status"] != 0).sum()),
+           "newton_iters_per_s": iters / (ms.value / 1e3),
+           "timing": "CUDA events around one cedar_batch_run launch (DC operating points included)"}
+    if builtin_ms:
+        vb = builtin_steps / (builtin_ms / 1e3)
+        out["builtin"] = {"value": vb, "ms": builtin_ms, "accepted_steps": int(builtin_steps),
+                          "source": "kernel time of the e2e run (same instances, built-in MOS1, DC included)"}
+        out["va_over_builtin"] = v / vb
+        out["same_step_counts"] = int(steps) == int(builtin_steps)
+    return out
 
 
 def measure_ac(pkg, args, torch, C, fp64_peak):
@@ -371,6 +397,94 @@ def measure_ac(pkg, args, torch, C, fp64_peak):
     return out
 
 
+def plain_leg(pkg, orc, C, name, flat, opts, fp64_peak, hbm_peak, workload):
+    """One circuit through cedar_tran_run, the single-circuit drop-in (tran!): the
+    kernel's device time (cedar_ckt_last_ms: CUDA events on the handle's stream),
+    the call's wall time with its host copies as e2e, the roofline of the
+    algorithmic Newton-iteration bytes and flops (cedar_ckt_costs x iterations),
+    the waveform error against the FP64 oracle at every recorded point, and the
+    oracle timed beside it on one host thread."""
+    sy = pkg.System(flat)
+    lib = sy.lib
+    n_pts = int(round((opts.tstop - opts.tstart) / opts.h)) + 2 if not opts.adaptive else 1 << 18
+    x = np.zeros(sy.n)
+    t_out, x_out = np.zeros(n_pts), np.zeros((n_pts, sy.n))
+    cnt, st = C.c_int64(), pkg.abi.Stats()
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+
+    def call():
+        x[:] = 0.0
+        pkg.abi.check(lib.cedar_tran_run(sy.handle, C.byref(opts), dp(x), dp(t_out), dp(x_out), n_pts, C.byref(cnt),
+                                         C.byref(st)))
+    call()                                                    # warm-up (module load, buffers)
+    reps = 3
+    ms, walls = [], []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        call()
+        walls.append(time.perf_counter() - t0)
+        m = C.c_double()
+        pkg.abi.check(lib.cedar_ckt_last_ms(sy.handle, C.byref(m)))
+        ms.append(m.value)
+    dev_s, wall_s = min(ms) / 1e3, min(walls)
+    steps, iters = st.accepted, st.newton_iters + st.dc_iters
+    costs = pkg.abi.Costs()
+    pkg.abi.check(lib.cedar_ckt_costs(sy.handle, C.byref(costs)))
+    flops = costs.flops_eval + costs.flops_stamp + costs.flops_lu + costs.flops_solve + costs.flops_update
+    gbs = costs.bytes * iters / dev_s / 1e9
+    tfl = flops * iters / dev_s / 1e12
+    # oracle: same circuit and options, one host thread
+    t0 = time.perf_counter()
+    t_ref, x_ref, st_ref, rc = orc.tran(flat, opts, cap=n_pts)
+    cpu_s = time.perf_counter() - t0
+    m = min(len(t_ref), cnt.value)
+    same_t = bool(len(t_ref) == cnt.value and np.array_equal(t_ref, t_out[:m]))
+    nn = flat.n_nodes
+    err = float(np.max(np.abs(x_out[:m, :nn] - x_ref[:m, :nn]) / (1e-6 * np.abs(x_ref[:m, :nn]) + 1e-9)))
+    return {"workload": workload, "value": steps / dev_s, "unit": "timesteps/s",
+            "newton_iters_per_s": iters / dev_s, "accepted_steps": int(steps), "newton_iters": int(iters),
+            "ms": dev_s * 1e3, "status": pkg.abi.STATUS_NAMES[st.status],
+            "e2e": {"value": steps / wall_s, "unit": "timesteps/s", "seconds": wall_s,
+                    "h2d_bytes_per_step": int(x.nbytes + C.sizeof(opts)),
+                    "d2h_bytes_per_step": int(cnt.value * (8 + 8 * sy.n) + C.sizeof(st))},
+            "roofline": {"bound": "latency (one warp)", "hbm": {"achieved_gbs": gbs, "peak_gbs": hbm_peak,
+                                                               "frac": gbs / hbm_peak},
+                         "fp64": {"achieved_tflops": tfl, "peak_tflops": fp64_peak, "frac": tfl / fp64_peak},
+                         "bytes_per_newton_iter": int(costs.bytes), "flops_per_newton_iter": int(flops),
+                         "note": "algorithmic bytes / flops of one Newton iteration (cedar_ckt_costs) x iterations "
+                                 "/ kernel time; one circuit on one warp is latency-bound, the fractions show how far"},
+            "vs_oracle": {"max_scaled_error": err, "tolerance": "reltol 1e-6, abstol 1e-9 V, every recorded point",
+                          "same_time_points": same_t, "oracle_steps": int(st_ref.accepted)},
+            "cpu_baseline": {"value": st_ref.accepted / cpu_s, "unit": "timesteps/s", "cores": 1, "kind": "port",
+                             "sample": "the whole run, oracle (dense LU with partial pivoting, as IDA's default "
+                                       "direct solve) on one host thread", "seconds": cpu_s},
+            "timing": f"best of {reps} calls after one warm-up; device time = CUDA events around the kernel"}
+
+
+def measure_plain_configs(pkg, C, fp64_peak):
+    """Configurations 1 and 2: the RC ladder (trapezoidal, h = 0.1 ns, 0..1 us) and
+    the 31-stage inverter chain (BDF2, h = 1 ps, 0..20 ns), each one circuit through
+    cedar_tran_run; the chain with built-in and with Verilog-A level-1 MOSFETs."""
+    import __graft_entry__ as ge
+    orc = ge.load_oracle().Oracle(pkg)
+    g = pkg.generators
+    hbm = hbm_peak_gbs()
+    o1 = pkg.make_opts("trap", False, 0.0, 1e-6, 0.1e-9, True)
+    o2 = pkg.make_opts("bdf2", False, 0.0, 20e-9, 1e-12, True)
+    rc = g.rc_ladder(100).flatten()
+    ch = g.inverter_chain(31).flatten()
+    return {
+        "config1": plain_leg(pkg, orc, C, "config1", rc, o1, fp64_peak, hbm,
+                             "RC ladder, 100 sections (1 kOhm, 1 pF), PULSE(0 1 0 1n 1n 50n 100n), trapezoidal "
+                             "h = 0.1 ns, 0..1 us, n = 101"),
+        "config2": plain_leg(pkg, orc, C, "config2", ch, o2, fp64_peak, hbm,
+                             "31-stage inverter chain, built-in level-1 MOSFETs, 10 fF loads, PULSE(0 1.8 0 50p 50p "
+                             "950p 2n), BDF2 h = 1 ps, 0..20 ns, n = 35"),
+        "config2_verilog_a": plain_leg(pkg, orc, C, "config2_va", g.as_verilog_a(ch), o2, fp64_peak, hbm,
+                                       "the same chain with the MOSFETs as the emitted Verilog-A va_mos1"),
+    }
+
+
 def hbm_peak_gbs():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -402,7 +516,9 @@ def run_reference(args, pkg):
     v = total_steps / total_time
     sample = f"{args.steps} x {k} randomly chosen instances of the {args.n_inst}, each run 0..20 ns (DC op included)"
     adj = None if args.no_adjoint else reference_adjoint(args, pkg, orc)
+    rings = None if args.no_rings else reference_rings(args, pkg, orc)
     return {"metric": METRIC, "impl": "reference", "value": v, "unit": UNIT, "n_gpus": args.gpus, "adjoint": adj,
+            "rings": rings,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_time / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded Philox4x32-10)",
@@ -493,6 +609,7 @@ def main():
     achieved = flops_all / dt / 1e12
     # end to end through the C ABI with host buffers (create + full run + results)
     e2e = None
+    e2e_kernel_ms, e2e_kernel_steps = None, None
     if not args.no_e2e:
         barrier(dist)
         torch.cuda.synchronize()
@@ -504,6 +621,9 @@ def main():
         torch.cuda.synchronize()
         barrier(dist)
         te = reduce_max(dist, time.perf_counter() - te0)
+        kms = C.c_double()
+        pkg.abi.check(lib.cedar_batch_last_ms(sw2.handle, C.byref(kms)))
+        e2e_kernel_ms, e2e_kernel_steps = kms.value, float(r2.stats["accepted"].sum())
         e2e_steps = reduce_sum(dist, float(r2.stats["accepted"].sum()))
         h2d = int(par.nbytes + off[mine].nbytes + itpl[mine].nbytes + probes.nbytes)
         d2h = int(r2.x_final.nbytes + (r2.samples.nbytes if r2.samples is not None else 0) + r2.stats.nbytes)
@@ -517,16 +637,26 @@ def main():
     if not args.no_plain:
         g = pkg.generators
         sel = np.random.default_rng(2).choice(args.n_inst, size=args.plain_inst, replace=False)
-        acc, tt = 0, 0.0
+        acc, tt, tk = 0, 0.0, 0.0
+        po = opts_for(pkg, args.plain_tstop)
         for i in sel:
             f = g.instance_flat(templates[itpl[i]], par[off[i]:off[i] + templates[itpl[i]].param_block().size])
             s0 = pkg.System(f)
+            xi, tb, xb = np.zeros(s0.n), np.zeros(1 << 17), np.zeros(((1 << 17), s0.n))
+            cnt, st = C.c_int64(), pkg.abi.Stats()
+            dpp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
             t0 = time.perf_counter()
-            sol = pkg.tran(s0, (0.0, args.plain_tstop), method="bdf2", cap=1 << 17)
+            pkg.abi.check(lib.cedar_tran_run(s0.handle, C.byref(po), dpp(xi), dpp(tb), dpp(xb), 1 << 17, C.byref(cnt),
+                                             C.byref(st)))
             tt += time.perf_counter() - t0
-            acc += sol.stats["accepted"]
-        plain = {"value": acc / tt, "unit": UNIT, "sample": f"{args.plain_inst} random instances, each one "
-                 f"cedar_tran_run (one CTA) from DC to {args.plain_tstop * 1e9:g} ns", "seconds": tt}
+            km = C.c_double()
+            pkg.abi.check(lib.cedar_ckt_last_ms(s0.handle, C.byref(km)))
+            tk += km.value / 1e3
+            acc += st.accepted
+        plain = {"value": acc / tk, "unit": UNIT, "e2e_value": acc / tt,
+                 "sample": f"{args.plain_inst} random instances, each one cedar_tran_run (one warp, every accepted "
+                           f"point recorded) from DC to {args.plain_tstop * 1e9:g} ns with the headline's options",
+                 "seconds_kernel": tk, "seconds_wall": tt}
     # discrete adjoint (workload 5) through the C ABI
     adj = None
     if not args.no_adjoint:
@@ -546,21 +676,47 @@ def main():
                "accepted_steps_mean": float(r5.stats["accepted"].mean()), "tuning": list(sw5.tuning),
                "timing": "CUDA events around the recording forward and the backward kernel"}
         del sw5
+        # FP64 roofline of the adjoint: the recording forward, the backward kernel's
+        # replay of every segment (the forward's Newton iterations again), and per
+        # accepted step one more refactorisation at the converged state (a Newton
+        # iteration's flops) plus the transposed substitutions
+        c5 = [pkg.costs(f) for f in t5]
+        fl5 = np.array([c["flops_eval"] + c["flops_stamp"] + c["flops_lu"] + c["flops_solve"] + c["flops_update"]
+                        for c in c5], np.float64)[i5]
+        sv5 = np.array([c["flops_solve"] for c in c5], np.float64)[i5]
+        it5 = (r5.stats["newton_iters"] + r5.stats["dc_iters"]).astype(np.float64)
+        ac5 = r5.stats["accepted"].astype(np.float64)
+        adj_flops = float(np.sum(2.0 * it5 * fl5 + ac5 * (fl5 + sv5)))
+        tf5 = adj_flops / secs / 1e12
+        adj["roofline"] = {"bound": "fp64", "achieved": tf5, "peak": fp64_peak, "unit": "TFLOP/s",
+                           "frac": tf5 / fp64_peak,
+                           "note": "flops = 2 x forward Newton iterations x flops per iteration (recording forward + "
+                                   "replay) + accepted steps x (flops per iteration + substitution flops)"}
+        del sw5
     eval_leg = None if args.no_eval else measure_eval(pkg, args, torch, C)
-    rings = None if args.no_rings else measure_rings(pkg, args, C)
+    rings = None if args.no_rings else measure_rings(pkg, args, C, fp64_peak)
+    if rings is not None and not args.no_va:
+        rv = measure_rings(pkg, args, C, fp64_peak, verilog_a=True)
+        rings["verilog_a"] = rv
+        rings["va_over_builtin"] = rv["value"] / rings["value"]
+        rings["same_step_counts"] = rv["accepted_steps"] == rings["accepted_steps"]
     ac_leg = None if args.no_ac else measure_ac(pkg, args, torch, C, fp64_peak)
-    va_leg = None if args.no_va else measure_va(pkg, args, C)
+    va_leg = None if args.no_va else measure_va(pkg, args, C, e2e_kernel_ms, e2e_kernel_steps, fp64_peak)
+    plain_cfg = None if args.no_plain_configs else measure_plain_configs(pkg, C, fp64_peak)
     cpu = None
     if not args.no_cpu_baseline:
         cpu_line = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
                                    "--steps", "1", "--warmup", "0", "--ref-inst", "64"]
-                                  + (["--no-adjoint"] if args.no_adjoint else []),
+                                  + (["--no-adjoint"] if args.no_adjoint else [])
+                                  + (["--no-rings"] if args.no_rings else []),
                                   capture_output=True, text=True, timeout=900)
         try:
             ref = json.loads(cpu_line.stdout.strip().splitlines()[-1])
             cpu = ref["cpu_baseline"]
             if adj is not None and ref.get("adjoint"):
                 adj["cpu_baseline"] = ref["adjoint"]
+            if rings is not None and ref.get("rings"):
+                rings["cpu_baseline"] = ref["rings"]
         except Exception:
             cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                    "sample": "failed: " + cpu_line.stderr[-300:]}
@@ -580,7 +736,9 @@ def main():
                              "peak = DFMA rate measured in this run by cedar_fp64_probe (MEASURED_PEAKS.json "
                              "has no FP64 entry); the kernel keeps its state on chip, so HBM is not its bound"},
         "cpu_baseline": cpu, "e2e": e2e, "plain_gpu": plain, "adjoint": adj, "eval_hbm": eval_leg, "rings": rings,
-        "ac": ac_leg, "verilog_a": va_leg, "clocks": clk, "gpu_launches": args.steps,
+        "ac": ac_leg, "verilog_a": va_leg, "config1": plain_cfg and plain_cfg["config1"],
+        "config2": plain_cfg and plain_cfg["config2"], "config2_verilog_a": plain_cfg and plain_cfg["config2_verilog_a"],
+        "clocks": clk, "gpu_launches": args.steps,
     }
     print(json.dumps(line), flush=True)
 

@@ -269,7 +269,13 @@ struct cedar_ckt {
   int threads = 128;
   int device = -1;          // the CUDA device current at cedar_ckt_create
   bool host_only = false;
+  // single-circuit transient on the one-warp engine: queue words, final state
+  DevBuf<int> wq;
+  DevBuf<double> xf;
+  cudaEvent_t run_ev[2] = {nullptr, nullptr};   // bracket the last single-circuit kernel
+  bool run_timed = false;
   ~cedar_ckt() {
+    for (cudaEvent_t e : run_ev) if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : ac_ev) if (e) cudaEventDestroy(e);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -556,7 +562,11 @@ static int run_plain(cedar_ckt *c, int mode, const cedar_tran_opts *opts, double
     a.t_out = c->tout.p; a.x_out = c->xout.p; a.cap = cap;
   }
   a.count = c->count.p; a.stats = c->stats.p; a.ws_global = c->ws.p;
+  if (!c->run_ev[0]) { CUDA_TRY(cudaEventCreate(&c->run_ev[0])); CUDA_TRY(cudaEventCreate(&c->run_ev[1])); }
+  CUDA_TRY(cudaEventRecord(c->run_ev[0], c->stream));
   CUDA_TRY(launch_plain(a, ws_doubles(H.n, H.nnz_lu, H.n_out, (int)H.src_group.size()), c->threads, c->stream));
+  CUDA_TRY(cudaEventRecord(c->run_ev[1], c->stream));
+  c->run_timed = true;
   EngStats st{}; long long cnt = 0;
   CUDA_TRY(cudaMemcpyAsync(&st, c->stats.p, sizeof(st), cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(cudaMemcpyAsync(&cnt, c->count.p, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
@@ -584,12 +594,84 @@ int cedar_dcop(cedar_ckt *c, double t, double *x, cedar_stats *stats) {
   return run_plain(c, 2, nullptr, t, 0.0, nullptr, x, nullptr, nullptr, 0, nullptr, stats);
 }
 
+// Largest workspace (doubles) for which the single-circuit transient runs on the
+// one-warp engine with its workspace in shared memory; larger circuits run on the
+// CTA engine (more lanes per level) with a global workspace.
+constexpr int kWarpTranMaxWs = 24 * 1024;
+
+// The single-circuit transient on the batched engine's slot state machine, one
+// warp, one instance, every accepted point recorded (the same step control,
+// Newton iteration and DC homotopy as every batched instance).
+static int run_tran_warp(cedar_ckt *c, const cedar_tran_opts *opts, double *x, double *t_out, double *x_out,
+                         int64_t cap, int64_t *n_out, cedar_stats *stats) {
+  const Template &H = c->tpl->H;
+  const int n = H.n;
+  const int wsd = ws_doubles(H.n, H.nnz_lu, H.n_out, (int)H.src_group.size());
+  CUDA_TRY(c->wq.ensure(8));
+  CUDA_TRY(c->xf.ensure(n));
+  // words: [0] inst_tpl, [1] queue, [2..3] qblk_beg, [4] qblk_head, [5] n_running
+  const int words[8] = {0, 0, 0, 1, 0, 0, 0, 0};
+  CUDA_TRY(cudaMemcpyAsync(c->wq.p, words, sizeof(words), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(c->x.p, x, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaMemsetAsync(c->count.p, 0, sizeof(long long), c->stream));
+  const bool rec = t_out && x_out && cap > 0;
+  if (rec) { CUDA_TRY(c->tout.ensure(cap)); CUDA_TRY(c->xout.ensure((size_t)cap * n)); }
+  const long long dstride = (long long)(n + 2) * n;
+  const bool dense_ok = n <= 256;
+  if (dense_ok) CUDA_TRY(c->dense.ensure(dstride));
+  BatchDev bd{};
+  bd.tpls = c->tpl->D_dev; bd.inst_tpl = c->wq.p; bd.inst_dpar = c->off.p; bd.dpar = c->dpar.p;
+  bd.x0_off = c->off.p; bd.x0 = c->x.p;                 // off.p[0] == 0: the state copied above
+  bd.x_final = c->xf.p; bd.n_max = n; bd.stats = c->stats.p;
+  bd.queue = c->wq.p + 1; bd.qblk_beg = c->wq.p + 2; bd.qblk_head = c->wq.p + 4; bd.n_qblk = 1; bd.n_inst = 1;
+  bd.n_running = c->wq.p + 5;
+  bd.opts = to_eng(opts);
+  bd.ws_stride = wsd;
+  bd.ws_in_smem = 1;
+  bd.t_until = 1e300;
+  bd.dense_ws = dense_ok ? c->dense.p : nullptr; bd.dense_stride = dstride; bd.dense_nmax = 256;
+  bd.rec_t = rec ? c->tout.p : nullptr; bd.rec_x = rec ? c->xout.p : nullptr; bd.rec_cap = rec ? cap : 0;
+  bd.rec_count = c->count.p;
+  if (!c->run_ev[0]) { CUDA_TRY(cudaEventCreate(&c->run_ev[0])); CUDA_TRY(cudaEventCreate(&c->run_ev[1])); }
+  CUDA_TRY(cudaEventRecord(c->run_ev[0], c->stream));
+  CUDA_TRY(launch_batch_record(bd, (size_t)wsd * sizeof(double), c->stream));
+  CUDA_TRY(cudaEventRecord(c->run_ev[1], c->stream));
+  c->run_timed = true;
+  EngStats st{}; long long cnt = 0;
+  CUDA_TRY(cudaMemcpyAsync(&st, c->stats.p, sizeof(st), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(&cnt, c->count.p, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(x, c->xf.p, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  if (rec) {
+    const long long m = std::min<long long>(cnt, cap);
+    CUDA_TRY(cudaMemcpy(t_out, c->tout.p, m * sizeof(double), cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(x_out, c->xout.p, (size_t)m * n * sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  if (n_out) *n_out = rec ? cnt : 0;
+  if (stats) std::memcpy(stats, &st, sizeof(st));
+  if (rec && cnt > cap) return fail(CEDAR_ECAPACITY, "output capacity exceeded");
+  return 0;
+}
+
 int cedar_tran_run(cedar_ckt *c, const cedar_tran_opts *opts, const double *x0, double *t_out, double *x_out,
                    int64_t cap, int64_t *n_out, cedar_stats *stats) {
   if (!c || !x0) return fail(CEDAR_EINVAL, "null argument");
   int rc = check_opts(opts); if (rc) return rc;
-  std::vector<double> x(x0, x0 + c->tpl->H.n);
+  if (c->host_only) return fail(CEDAR_EINVAL, "host-only plan handle");
+  const Template &H = c->tpl->H;
+  std::vector<double> x(x0, x0 + H.n);
+  if (ws_doubles(H.n, H.nnz_lu, H.n_out, (int)H.src_group.size()) <= kWarpTranMaxWs)
+    return run_tran_warp(c, opts, x.data(), t_out, x_out, cap, n_out, stats);
   return run_plain(c, 0, opts, opts->tstart, 0.0, nullptr, x.data(), t_out, x_out, cap, n_out, stats);
+}
+
+int cedar_ckt_last_ms(cedar_ckt *c, double *ms) {
+  if (!c || !ms) return fail(CEDAR_EINVAL, "null argument");
+  if (!c->run_timed) return fail(CEDAR_EINVAL, "no single-circuit run recorded yet");
+  CUDA_TRY(cudaEventSynchronize(c->run_ev[1]));
+  float f = 0; CUDA_TRY(cudaEventElapsedTime(&f, c->run_ev[0], c->run_ev[1]));
+  *ms = f;
+  return 0;
 }
 
 // ------------------------------------------------------------------ AC / noise

@@ -267,7 +267,22 @@ struct Slot {
     ssync();
   }
 
+  // Record mode (single instance): accepted point (tt, x) into the record buffers.
+  __device__ void rec_point(const BatchDev &b, double tt, const double *x) {
+    const long long c = *((volatile long long *)b.rec_count);
+    if (c < b.rec_cap) {
+      if (rank() == 0) b.rec_t[c] = tt;
+      double *row = b.rec_x + c * T->n;
+      for (int i = rank(); i < T->n; i += K) row[T->order[i]] = x[i];
+    }
+    ssync();
+    if (rank() == 0) *((volatile long long *)b.rec_count) = c + 1;
+    ssync();
+  }
+
   // Advance this slot's state machine until it issues a Newton job or goes idle.
+  // REC: also record every accepted point (record mode, one instance).
+  template <bool REC = false>
   __device__ void resume(const BatchDev &b, double *ws) {
     const EngOpts &o = b.opts;
     const long long budget = 20000;
@@ -375,6 +390,7 @@ struct Slot {
           double hk = t - tprev;
           tprev2 = tprev; tprev = t; have_prev = true;
           st.accepted++; st.hmin_seen = hk < st.hmin_seen ? hk : st.hmin_seen; st.hmax_seen = hk > st.hmax_seen ? hk : st.hmax_seen;
+          if constexpr (REC) rec_point(b, t, w.xn);
           if (nf) { st.status = CEDAR_ST_NAN; goto retire; }
           ++k;
           goto fix_issue;
@@ -438,6 +454,7 @@ struct Slot {
           nf = sany(nf);
           tn2 = tn1; tn1 = t; t = tnew;
           st.accepted++; st.hmin_seen = h < st.hmin_seen ? h : st.hmin_seen; st.hmax_seen = h > st.hmax_seen ? h : st.hmax_seen;
+          if constexpr (REC) rec_point(b, t, w.xn);
           if (nf) { st.status = CEDAR_ST_NAN; goto ada_end; }
           if (b.tape_t && !tape_record(b, st.accepted, t, npts < 2 ? 1 : 2)) { st.status = CEDAR_ST_MAX_STEPS; goto ada_end; }
           if (npts < 3) ++npts;
@@ -501,6 +518,7 @@ struct Slot {
       copy(w.xn, w.x);
       ssync();
       sink_start(w.x);
+      if constexpr (REC) rec_point(b, o.tstart, w.x);
       if (rank() == 0 && b.rows) b.rows[inst].flags = ROW_STARTED;
       if (!o.adaptive) {
         fill(w.qd, 0.0);

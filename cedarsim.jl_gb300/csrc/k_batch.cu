@@ -13,7 +13,8 @@ namespace cedar {
 // SMEM: the slot workspaces live in shared memory.  Fixing this at compile time
 // lets every workspace pointer derive from the shared-memory base, so the
 // compiler issues shared-memory loads and stores rather than generic ones.
-template <int K, bool SMEM>
+// REC: record mode (one instance, every accepted point; the single-circuit transient)
+template <int K, bool SMEM, bool REC = false>
 __global__ void __launch_bounds__(256, CEDAR_BATCH_MIN_BLOCKS) batch_kernel(BatchDev b) {
   extern __shared__ double smem[];
   Slot<K> s;
@@ -27,7 +28,7 @@ __global__ void __launch_bounds__(256, CEDAR_BATCH_MIN_BLOCKS) batch_kernel(Batc
   s.nrel = b.opts.nr_factor * b.opts.reltol; s.nav = b.opts.nr_factor * b.opts.abstol_v;
   s.nai = b.opts.nr_factor * b.opts.abstol_i;
   for (;;) {
-    if (!s.active && s.rp != RP_IDLE) s.resume(b, ws);
+    if (!s.active && s.rp != RP_IDLE) s.template resume<REC>(b, ws);
     __syncwarp();
     const unsigned am = __ballot_sync(FULL, s.active);
     if (am == 0) break;
@@ -82,5 +83,20 @@ cudaError_t CEDAR_CAT(configure_batch_k, CEDAR_LANES)(int warps, size_t smem, bo
   const int th = warps * 32;
   return in_smem ? configure(batch_kernel<K, true>, th, smem, per_sm) : configure(batch_kernel<K, false>, th, smem, per_sm);
 }
+
+#if CEDAR_LANES == 32
+cudaError_t launch_batch_record(const BatchDev &b, size_t smem, cudaStream_t st) {
+  cudaError_t e;
+  if (smem > 0) {
+    if ((e = cudaFuncSetAttribute(batch_kernel<32, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem)) != cudaSuccess)
+      return e;
+    batch_kernel<32, true, true><<<1, 32, smem, st>>>(b);
+  } else {
+    batch_kernel<32, false, true><<<1, 32, 0, st>>>(b);
+  }
+  return cudaGetLastError();
+}
+#endif
 
 }  // namespace cedar

@@ -46,6 +46,10 @@ struct BatchDev {
   // n_max matrix, a right-hand side and the pivots); null: no fallback
   double *dense_ws; long long dense_stride; int dense_nmax;
   int dc_only;                   // retire every instance at its DC operating point
+  // record mode (one instance only: the single-circuit transient): every accepted
+  // point's time and state (original order) into rec_t[cap] / rec_x[cap * n];
+  // *rec_count counts every point, also those past cap.  rec_t == null: off.
+  double *rec_t, *rec_x; long long rec_cap; long long *rec_count;
 };
 
 // slice helpers of the adjoint tape
@@ -138,6 +142,9 @@ cudaError_t launch_fp64_probe(int active_lanes, int iters, double *gflops, doubl
 
 // batched persistent engine with K lanes per instance
 cudaError_t launch_batch(const BatchDev &b, int K, int warps_per_cta, int grid, size_t smem, cudaStream_t s);
+// the same engine on one warp for one instance in record mode (k_batch.cu, 32 lanes):
+// the single-circuit transient; smem > 0 puts the workspace in shared memory
+cudaError_t launch_batch_record(const BatchDev &b, size_t smem, cudaStream_t s);
 // (k_dispatch.cu) set the launch attributes of batch_kernel<K> for this shape and report its
 // resident CTAs per SM (registers and shared memory both counted)
 cudaError_t configure_batch(int K, int warps_per_cta, size_t smem, bool ws_in_smem, int *per_sm);

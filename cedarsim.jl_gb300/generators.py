@@ -276,6 +276,21 @@ def mc_rings(n_inst: int = 1024, seed: int = 20240607, workload: int = 4):
     return [flat], np.zeros(n_inst, np.int32), np.concatenate(blocks), offs, np.concatenate(dxs), dx_off
 
 
+def as_verilog_a(flat: Flat) -> Flat:
+    """The same circuit with its level-1 MOSFETs and exponential diodes as the
+    Verilog-A modules va_mos1 / va_diode compiled by the emitter (their parameter
+    blocks are the built-in models' blocks, parameter for parameter), so instance
+    parameter blocks of the built-in template serve the Verilog-A one unchanged.
+    Group order is kept."""
+    import copy
+    from . import va
+    from .circuit import DIODE as MODEL_D
+    swap = {MOS1: va.model_id("va_mos1"), MODEL_D: va.model_id("va_diode")}
+    g = copy.deepcopy(flat)
+    g.groups = [(swap.get(m, m), t, b, p) for (m, t, b, p) in g.groups]
+    return g
+
+
 def instance_flat(template: Flat, block: np.ndarray) -> Flat:
     """The template with one instance's parameter block substituted (a stand-alone circuit)."""
     groups, p = [], 0

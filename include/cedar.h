@@ -291,6 +291,10 @@ int cedar_dcop(cedar_ckt *ckt, double t, double *x, cedar_stats *stats);
 int cedar_tran_run(cedar_ckt *ckt, const cedar_tran_opts *opts, const double *x0,
                    double *t_out, double *x_out, int64_t cap, int64_t *n_out,
                    cedar_stats *stats);
+/* Device time (ms) of the kernel of the last cedar_tran_run / cedar_newton_solve /
+ * cedar_dcop on this handle (CUDA events on the handle's stream around it).  No
+ * counterpart in the reference: for throughput accounting. */
+int cedar_ckt_last_ms(cedar_ckt *ckt, double *ms);
 
 /* ---- batched form ---------------------------------------------------------
  * Instances share a topology template and differ in parameters (a CircuitSweep
