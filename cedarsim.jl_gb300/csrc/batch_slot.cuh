@@ -385,7 +385,7 @@ struct Slot {
           sink_step(have_prev, tprev2, w.xm1, tprev, w.xn, t, xp);
           ssync();
           bool nf = false;
-          for (int i = rank(); i < T->n; i += K) { w.xm1[i] = w.xn[i]; w.xn[i] = xp[i]; if (!(fabs(xp[i]) < 1e300)) nf = true; }
+          for (int i = rank(); i < T->n; i += K) { w.xm1[i] = w.xn[i]; w.xn[i] = xp[i]; if (!isfinite(xp[i])) nf = true; }
           nf = sany(nf);
           double hk = t - tprev;
           tprev2 = tprev; tprev = t; have_prev = true;
@@ -449,7 +449,7 @@ struct Slot {
           bool nf = false;
           for (int i = rank(); i < n; i += K) {
             w.xm2[i] = w.xm1[i]; w.xm1[i] = w.xn[i]; w.xn[i] = xp[i];
-            if (!(fabs(xp[i]) < 1e300)) nf = true;
+            if (!isfinite(xp[i])) nf = true;
           }
           nf = sany(nf);
           tn2 = tn1; tn1 = t; t = tnew;
@@ -896,7 +896,7 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am, const 
   if (!slot_bad) {
     for (int i = rank; i < T.n; i += K) {
       long long ab = abs_bits(b[i]);
-      if (ab >= 0x7e37e43c8800759cLL) nonfinite = true;  // |d| >= 1e300 or NaN
+      if (ab >= 0x7ff0000000000000LL) nonfinite = true;  // inf or NaN
       if (damp && T.is_node[i]) mxb = ab > mxb ? ab : mxb;
     }
   }

@@ -496,7 +496,7 @@ struct Engine {
       bool nonfinite = false; double mx = 0.0;
       for (int i = g.rank; i < T.n; i += g.size) {
         double d = w.F[i];
-        if (!(fabs(d) < 1e300)) nonfinite = true;
+        if (!isfinite(d)) nonfinite = true;
         if (T.is_node[i]) { double a = fabs(d); mx = a > mx ? a : mx; }
       }
       if (g.any(nonfinite)) return -it;
@@ -699,7 +699,7 @@ struct Engine {
         sink_step(sk, have_prev, tprev2, w.xm1, tprev, w.xn, t, xp);
         g.sync();
         bool nf = false;
-        for (int i = g.rank; i < n; i += g.size) { w.xm1[i] = w.xn[i]; w.xn[i] = xp[i]; if (!(fabs(xp[i]) < 1e300)) nf = true; }
+        for (int i = g.rank; i < n; i += g.size) { w.xm1[i] = w.xn[i]; w.xn[i] = xp[i]; if (!isfinite(xp[i])) nf = true; }
         nf = g.any(nf);
         tprev2 = tprev; tprev = t; have_prev = true;
         st.accepted++; st.hmin_seen = hk < st.hmin_seen ? hk : st.hmin_seen; st.hmax_seen = hk > st.hmax_seen ? hk : st.hmax_seen;
@@ -796,7 +796,7 @@ struct Engine {
       bool nf = false;
       for (int i = g.rank; i < n; i += g.size) {
         w.xm2[i] = w.xm1[i]; w.xm1[i] = w.xn[i]; w.xn[i] = xp[i];
-        if (!(fabs(xp[i]) < 1e300)) nf = true;
+        if (!isfinite(xp[i])) nf = true;
       }
       nf = g.any(nf);
       tn2 = tn1; tn1 = t; t = tnew;
