@@ -675,7 +675,6 @@ def main():
                "params_per_instance": [int(per.min()), int(per.max())],
                "accepted_steps_mean": float(r5.stats["accepted"].mean()), "tuning": list(sw5.tuning),
                "timing": "CUDA events around the recording forward and the backward kernel"}
-        del sw5
         # FP64 roofline of the adjoint: the recording forward, the backward kernel's
         # replay of every segment (the forward's Newton iterations again), and per
         # accepted step one more refactorisation at the converged state (a Newton

@@ -140,3 +140,26 @@ def test_vectorised_chain_generator_matches_builder(pkg):
         for (ma, ta, ba, pa), (mb, tb, bb, pb) in zip(a.groups, b.groups):
             assert ma == mb and np.array_equal(ta, tb) and np.array_equal(pa, pb)
             assert (ba is None and bb is None) or np.array_equal(ba, bb)
+
+
+def test_eval_scratch_query_on_a_plan(pkg):
+    """cedar_eval_scratch reports the allocation-free evaluation's need (device
+    outputs plus supply-rail partial sums) and its fixed limit, from the host-side
+    analysis alone."""
+    import ctypes as C
+    lib = pkg.load_library()
+    limit = C.c_int64()
+    assert lib.cedar_eval_scratch(None, None, None, C.byref(limit)) == 0 and limit.value == 1 << 18
+    for stages, long_rows in ((9, False), (100, True)):
+        h = pkg.abi.DescHolder(pkg.generators.inverter_chain(stages).flatten())
+        p = C.c_void_p()
+        pkg.abi.check(lib.cedar_plan_create(C.byref(h.desc), C.byref(p)))
+        try:
+            n_out, n_part = C.c_int64(), C.c_int64()
+            pkg.abi.check(lib.cedar_eval_scratch(p, C.byref(n_out), C.byref(n_part), None))
+            # 2L MOSFETs x 4 outputs, L capacitors x 3, two V sources x 4
+            assert n_out.value == 8 * stages + 3 * stages + 8
+            assert (n_part.value > 0) == long_rows
+        finally:
+            lib.cedar_ckt_destroy(p)
+    assert lib.cedar_eval_scratch(None, C.byref(C.c_int64()), None, None) == -1

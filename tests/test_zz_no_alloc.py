@@ -31,6 +31,12 @@ def _scratch(lib, handle):
     return n_out.value, n_part.value, limit.value
 
 
+def _limit(lib):
+    limit = C.c_int64()
+    assert lib.cedar_eval_scratch(None, None, None, C.byref(limit)) == 0
+    return limit.value
+
+
 def _flat(pkg, case):
     if case == "inverter_chain":
         return pkg.generators.inverter_chain(9).flatten()
@@ -101,7 +107,7 @@ def test_noalloc_rejects_oversized_circuit(gpu, pkg):
     from the host-side size check, before anything is launched."""
     import torch
     lib = pkg.load_library()
-    _, _, limit = _scratch(lib, None)
+    limit = _limit(lib)
     c = pkg.Circuit()
     c.V("V1", "a", "0", dc=1.0)
     n_caps = limit // 3 + 1000
