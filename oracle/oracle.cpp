@@ -69,6 +69,122 @@ static inline Dual dexp_lim(const Dual &a) {
   return r;
 }
 
+// Further dual operations used by the Verilog-A restatements below.
+static inline Dual operator/(const Dual &a, const Dual &b) {
+  Dual r; r.v = a.v / b.v;
+  for (int i = 0; i < ND; ++i) r.d[i] = (a.d[i] * b.v - a.v * b.d[i]) / (b.v * b.v);
+  return r;
+}
+static inline Dual operator/(double s, const Dual &b) { return Dual(s) / b; }
+static inline Dual operator+(const Dual &a, double s) { return a + Dual(s); }
+static inline Dual operator+(double s, const Dual &a) { return Dual(s) + a; }
+static inline Dual operator-(const Dual &a, double s) { return a - Dual(s); }
+static inline Dual operator-(double s, const Dual &a) { return Dual(s) - a; }
+static inline Dual dexp(const Dual &a) {
+  Dual r; const double e = std::exp(a.v); r.v = e;
+  for (int i = 0; i < ND; ++i) r.d[i] = e * a.d[i];
+  return r;
+}
+static inline Dual dsqrt(const Dual &a) {
+  Dual r; const double q = std::sqrt(a.v); r.v = q;
+  for (int i = 0; i < ND; ++i) r.d[i] = a.d[i] == 0.0 ? 0.0 : a.d[i] * (0.5 / q);
+  return r;
+}
+// |a| with the derivative of the a >= 0 side at 0 (the Verilog-A abs of the emitter)
+static inline Dual dabs(const Dual &a) { return a.v < 0.0 ? -a : a; }
+
+// ---------------------------------------------------------------- Verilog-A, restated
+// The Verilog-A modules this project ships (cedarsim.jl_gb300/va/models/*.va),
+// written out again by hand in residual form over this file's own dual numbers,
+// so that GPU runs of circuits with these modules are checked against an
+// evaluation that shares no code with the emitter.  Contribution semantics
+// (src/vasim.jl:128-180): I(a,b) <+ e adds -e to the residual of a and +e to b;
+// a voltage-contributed branch V(a,b) <+ e carries a branch-current unknown I,
+// adds -I / +I to a / b and the branch row V(a) - V(b) - e, with ddt() terms of a
+// contribution as charges (ddt(q) enters the charge part of the same rows).
+// ddx on a two-node probe is (d/dVa - d/dVb)/2 (src/vasim.jl:400-411); real ->
+// integer parameters round half away from zero (src/va_env.jl:92-110).
+// p: the raw parameters (declaration order, then $param_given flags, then m),
+// vt: thermal voltage; V: terminal values (ports, internal nodes, branch current)
+// seeded as dual directions.  Returns false for a module not restated here.
+static bool va_restated(const char *name, const double *p, double vt, double gmin, const Dual *V, Dual *Fi,
+                        Dual *Fq) {
+  auto I_ab = [&](int a, int b, const Dual &e) { Fi[a] = Fi[a] - e; Fi[b] = Fi[b] + e; };
+  auto Q_ab = [&](int a, int b, const Dual &q) { Fq[a] = Fq[a] - q; Fq[b] = Fq[b] + q; };
+  const std::string m(name);
+  if (m == "va_resistor" || m == "va_resistor_1f") {          // I(p,n) <+ V(p,n)/R (noise only in noise analysis)
+    I_ab(0, 1, (V[0] - V[1]) / p[0]);
+  } else if (m == "va_capacitor") {                            // I(p,n) <+ ddt(C V(p,n))
+    Q_ab(0, 1, p[0] * (V[0] - V[1]));
+  } else if (m == "va_diode") {                                // IS AREA (limexp(V/(N vt)) - 1) + gmin V
+    const Dual v = V[0] - V[1];
+    I_ab(0, 1, (p[0] * p[2]) * (dexp_lim(v / (p[1] * vt)) - 1.0) + gmin * v);
+  } else if (m == "va_diode_cj") {                             // + ddt(TT id + CJ0 vd)
+    const Dual vd = V[0] - V[1];
+    const Dual id = p[0] * (dexp_lim(vd / (p[1] * vt)) - 1.0);
+    I_ab(0, 1, id + gmin * vd);
+    Q_ab(0, 1, p[2] * id + p[3] * vd);
+  } else if (m == "va_diode_rs") {                             // a -RS- ai -diode- c
+    I_ab(0, 2, (V[0] - V[2]) / p[2]);
+    const Dual vd = V[2] - V[1];
+    I_ab(2, 1, p[0] * (dexp_lim(vd / (p[1] * vt)) - 1.0) + gmin * vd);
+  } else if (m == "va_inductor") {                             // V(p,n) <+ ddt(L I(p,n))
+    const Dual &I = V[2];
+    Fi[0] = Fi[0] - I; Fi[1] = Fi[1] + I;
+    Fi[2] = Fi[2] + (V[0] - V[1]);
+    Fq[2] = Fq[2] - p[0] * I;
+  } else if (m == "va_thevenin") {                             // V(p,n) <+ VS + RS I(p,n)
+    const Dual &I = V[2];
+    Fi[0] = Fi[0] - I; Fi[1] = Fi[1] + I;
+    Fi[2] = Fi[2] + (V[0] - V[1]) - (p[0] + p[1] * I);
+  } else if (m == "va_mos1") {                                 // level 1, drain/source exchange for vds < 0
+    const double type = p[0], beta = p[3] * p[1] / p[2], vto = p[4], lam = p[5];
+    const Dual vgs = type * (V[1] - V[2]), vds = type * (V[0] - V[2]);
+    Dual vov, vde; double dir;
+    if (vds.v >= 0) { vov = vgs - type * vto; vde = vds; dir = 1.0; }
+    else { vov = vgs - vds - type * vto; vde = -vds; dir = -1.0; }
+    Dual id;
+    if (vov.v <= 0) id = Dual(0.0);
+    else if (vde.v < vov.v) id = ((beta * (vov - 0.5 * vde)) * vde) * (1.0 + lam * vde);
+    else id = (((0.5 * beta) * vov) * vov) * (1.0 + lam * vde);
+    I_ab(0, 2, (type * dir) * id + gmin * (V[0] - V[2]));
+  } else if (m == "va_nlvcr") {                                // V(d,s) ddx(R V(g,s)^2, V(g,s)) = V(d,s) 2 R V(g,s)
+    I_ab(0, 2, (V[0] - V[2]) * ((2.0 * p[0]) * (V[1] - V[2])));
+  } else if (m == "va_vccs_sat") {                             // gm f(V(cp,cn)), f by MODE
+    const double gm = p[4] != 0.0 ? p[1] : p[0], vs = p[2];
+    const long mode = std::lround(p[3]);
+    const Dual vc = V[2] - V[3];
+    Dual f;
+    if (mode == 0) f = vc;
+    else if (mode == 1) {                                      // sign(x) s (1 - e)/(1 + e), e = exp(-2|x|/s)
+      const Dual e = dexp((-2.0 / vs) * dabs(vc));
+      f = (vc.v >= 0 ? 1.0 : -1.0) * vs * ((1.0 - e) / (1.0 + e));
+    } else {                                                   // x / sqrt(1 + (x/s)^2)
+      const Dual r = vc / vs;
+      f = vc / dsqrt(1.0 + r * r);
+    }
+    I_ab(0, 1, gm * f);
+  } else {
+    return false;
+  }
+  return true;
+}
+
+// Dense fi/fq[nx], G/C[nx*nx] of model k through va_restated (dp: np raw
+// parameters then the thermal voltage); false when k is not restated by hand.
+static bool va_full_restated(int k, const double *dp, int np, const double *v, int nx, double gmin, double *fi,
+                             double *fq, double *G, double *Cm) {
+  if (k < 0 || k >= cedar::va::kCount || nx > ND) return false;
+  Dual V[ND], Fi[ND], Fq[ND];
+  for (int q = 0; q < nx; ++q) V[q] = Dual::seed(v[q], q);
+  if (!va_restated(cedar::va::kName[k], dp, dp[np], gmin, V, Fi, Fq)) return false;
+  for (int r = 0; r < nx; ++r) {
+    fi[r] = Fi[r].v; fq[r] = Fq[r].v;
+    for (int q = 0; q < nx; ++q) { G[r * nx + q] = Fi[r].d[q]; Cm[r * nx + q] = Fq[r].d[q]; }
+  }
+  return true;
+}
+
 // ------------------------------------------------------------------ circuit
 struct Group {
   int model = 0, n_inst = 0, nt = 0, np = 0;
@@ -319,17 +435,19 @@ static void eval_circuit(const Circuit &c, const double *x, const EvalCtx &ctx, 
           A.add(tm[0], -m * I, false); A.add(tm[2], m * I, false);
         } break;
         default: {
-          // Verilog-A model: dense residuals and partials of one device from the
-          // emitted code (derived block = parameters, m, thermal voltage)
-          // (idx / nin: the terminals, then the branch current of a module with a
-          // voltage-contributed branch)
+          // Verilog-A model: dense residuals and partials of one device, from the
+          // hand restatement of the module when there is one (every shipped
+          // module), else from the emitted code (derived block = parameters, m,
+          // thermal voltage) (idx / nin: the terminals, then the branch current
+          // of a module with a voltage-contributed branch)
           const int k = g.model - CEDAR_NMODELS, nx = nin;
           // sized per model: compact models carry hundreds of parameters
           std::vector<double> dp(g.np + 1), v(nx), fi(nx), fq(nx), G((size_t)nx * nx), Cm((size_t)nx * nx);
           for (int q = 0; q < g.np; ++q) dp[q] = g.p(q, i);
           dp[g.np] = Vt;
           for (int q = 0; q < nx; ++q) v[q] = X(idx[q]);
-          cedar::va::full(k, dp.data(), 1, v.data(), c.gmin, fi.data(), fq.data(), G.data(), Cm.data());
+          if (!va_full_restated(k, dp.data(), g.np, v.data(), nx, c.gmin, fi.data(), fq.data(), G.data(), Cm.data()))
+            cedar::va::full(k, dp.data(), 1, v.data(), c.gmin, fi.data(), fq.data(), G.data(), Cm.data());
           const double m = g.p(g.np - 1, i);
           for (int r = 0; r < nx; ++r) {
             const int row = idx[r];
@@ -1028,6 +1146,14 @@ int oracle_va_full(int k, const double *dp, const double *v, double gmin, double
   if (k < 0 || k >= cedar::va::kCount) { g_err = "Verilog-A model index out of range"; return -1; }
   cedar::va::full(k, dp, 1, v, gmin, fi, fq, G, Cm);
   return 0;
+}
+
+// The same device through the hand restatement; returns 1 when model k is
+// restated by hand (then fi/fq/G/C are filled), 0 when it is not.
+int oracle_va_ref_full(int k, const double *dp, int np, const double *v, double gmin, double *fi, double *fq,
+                       double *G, double *Cm) {
+  if (k < 0 || k >= cedar::va::kCount) { g_err = "Verilog-A model index out of range"; return -1; }
+  return va_full_restated(k, dp, np, v, cedar::va::kNTerm[k] + cedar::va::kHasBr[k], gmin, fi, fq, G, Cm) ? 1 : 0;
 }
 
 // Powers and frequency exponents of a Verilog-A device's noise sources through

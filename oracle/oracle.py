@@ -71,6 +71,8 @@ def load(pkg):
     lib.oracle_n_params.argtypes = [cd_p]
     lib.oracle_va_full.restype = C.c_int
     lib.oracle_va_full.argtypes = [C.c_int, dp, dp, C.c_double, dp, dp, dp, dp]
+    lib.oracle_va_ref_full.restype = C.c_int
+    lib.oracle_va_ref_full.argtypes = [C.c_int, dp, C.c_int, dp, C.c_double, dp, dp, dp, dp]
     lib.oracle_va_noise.restype = C.c_int
     lib.oracle_va_noise.argtypes = [C.c_int, dp, dp, C.c_double, dp, dp]
     lib.oracle_last_error.restype = C.c_int

@@ -2,9 +2,13 @@
 
 The emitted device code runs inside every engine: the device evaluation of
 cedar_eval, the one-circuit transient, the batched Monte-Carlo kernel and the
-small-signal AC solve.  Tolerances are the parity contract's (device F and J
-within 1e-12 relative; waveforms within reltol 1e-6 / abstol 1e-9 V with the
-same step sequence)."""
+small-signal AC and noise solves.  The oracle evaluates the same modules from
+its own hand restatement of each shipped .va file (oracle/oracle.cpp,
+va_restated), which shares no code with the emitter, so every comparison here is
+emitted code against an independent evaluation (test_every_model_is_restated
+guards that).  Tolerances are the parity contract's (device F and J within
+1e-12 relative; waveforms within reltol 1e-6 / abstol 1e-9 V with the same step
+sequence)."""
 import numpy as np
 import pytest
 
@@ -21,6 +25,27 @@ CASES = {
     "va_vccs": K.va_vccs,              # analog function, macros, case, $param_given
     "va_thevenin": K.va_thevenin,      # voltage-contributed branches (source, inductor)
 }
+
+
+def test_every_model_is_restated(gpu, pkg, oracle):
+    """Every Verilog-A model the GPU tests use (and every shipped module) has a
+    hand restatement in the oracle, so no comparison runs emitted code on both
+    sides."""
+    import ctypes as C
+    va = pkg.va
+    used = set()
+    for mk in list(CASES.values()) + [K.butterworth_va, K.butterworth_ac_va, _flicker_divider]:
+        used |= {g[0] for g in mk(pkg).flatten().groups if g[0] >= va.BASE_ID}
+    used |= {va.model_id(m.name) for m in va.models()}
+    dp_ = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    for mid in sorted(used):
+        k = mid - va.BASE_ID
+        m = va.models()[k]
+        z = np.zeros(m.nx * m.nx)
+        vals = m.defaults({})
+        assert oracle.lib.oracle_va_ref_full(k, dp_(np.array(vals + [1.0, 0.025])), len(vals) + 1,
+                                             dp_(np.zeros(m.nx)), 1e-12, dp_(np.zeros(m.nx)), dp_(np.zeros(m.nx)),
+                                             dp_(z), dp_(z.copy())) == 1, m.name
 
 
 @pytest.mark.parametrize("case", sorted(CASES))
@@ -165,3 +190,32 @@ def test_va_white_noise_psd(gpu, pkg, oracle):
     pco = oracle.noise(fc, xc, wc, fc.index("e"))
     np.testing.assert_allclose(pc, pco, rtol=1e-9)
     assert np.all(pc > 0)
+
+
+def _flicker_divider(pkg):
+    """A 1/f resistor (thermal + flicker_noise(KF |I|^AF, EF)) over a plain one."""
+    c = pkg.Circuit(temp_c=27.0, gmin=0.0)
+    c.V("V1", "vin", "0", dc=2.0)
+    c.va("R1", "va_resistor_1f", ["vin", "out"], R=3e3, KF=1e-14, AF=2.0, EF=1.1)
+    c.R("R2", "out", "0", r=1e3)
+    return c
+
+
+def test_va_flicker_noise_psd(gpu, pkg, oracle):
+    """cedar_noise with a flicker_noise source (density pwr / f^exp, src/ac.jl:
+    267-276): the GPU's per-source frequency weighting against the oracle and
+    against the divider's closed form (R1 || R2)^2 (4kT/R1 + 4kT/R2 + KF |I|^AF / f^EF)."""
+    f = _flicker_divider(pkg).flatten()
+    x = pkg.dc(f)
+    hz = np.logspace(-1, 9, 41)
+    w = 2 * np.pi * hz
+    psd = pkg.noise(f, x_op=x).psd("out", w)
+    po = oracle.noise(f, x, w, f.index("out"))
+    np.testing.assert_allclose(psd, po, rtol=1e-9)
+    R1, R2, KF, AF, EF, vdd = 3e3, 1e3, 1e-14, 2.0, 1.1, 2.0
+    kT4 = 4 * 1.380649e-23 * (27.0 + 273.15)
+    rp = R1 * R2 / (R1 + R2)
+    want = rp ** 2 * (kT4 / R1 + kT4 / R2 + KF * (vdd / (R1 + R2)) ** AF / hz ** EF)
+    np.testing.assert_allclose(psd, want, rtol=1e-9)
+    # the 1/f part dominates at low frequency and vanishes at high frequency
+    assert psd[0] > 100 * psd[-1]
