@@ -267,6 +267,8 @@ struct cedar_ckt {
   int ac_last_dense = 0;
   bool ac_dense_ran = false;
   int threads = 128;
+  int auto_threads = 128;   // the thread count chosen at create (CTA engine)
+  int engine = CEDAR_ENGINE_AUTO;
   int device = -1;          // the CUDA device current at cedar_ckt_create
   bool host_only = false;
   // single-circuit transient on the one-warp engine: queue words, final state
@@ -365,6 +367,7 @@ int cedar_ckt_create(const cedar_ckt_desc *desc, cedar_ckt **out) {
   if ((wsd + 128) * sizeof(double) > 160 * 1024) CUDA_TRY(c->ws.ensure(wsd));
   int work = std::max(std::max(H.nnz_lu, n), c->tpl->D.n_dev);
   c->threads = work >= 512 ? 512 : std::max(64, ((work + 31) / 32) * 32);
+  c->auto_threads = c->threads;
   CUDA_TRY(cudaStreamSynchronize(c->stream));
   *out = c.release();
   return 0;
@@ -660,9 +663,21 @@ int cedar_tran_run(cedar_ckt *c, const cedar_tran_opts *opts, const double *x0, 
   if (c->host_only) return fail(CEDAR_EINVAL, "host-only plan handle");
   const Template &H = c->tpl->H;
   std::vector<double> x(x0, x0 + H.n);
-  if (ws_doubles(H.n, H.nnz_lu, H.n_out, (int)H.src_group.size()) <= kWarpTranMaxWs)
+  const bool fits = ws_doubles(H.n, H.nnz_lu, H.n_out, (int)H.src_group.size()) <= kWarpTranMaxWs;
+  if (c->engine == CEDAR_ENGINE_WARP || (c->engine == CEDAR_ENGINE_AUTO && fits)) {
+    if (!fits) return fail(CEDAR_EINVAL, "circuit workspace exceeds the one-warp engine's shared memory");
     return run_tran_warp(c, opts, x.data(), t_out, x_out, cap, n_out, stats);
+  }
   return run_plain(c, 0, opts, opts->tstart, 0.0, nullptr, x.data(), t_out, x_out, cap, n_out, stats);
+}
+
+int cedar_ckt_set_engine(cedar_ckt *c, int32_t engine, int32_t threads) {
+  if (!c) return fail(CEDAR_EINVAL, "null handle");
+  if (engine < CEDAR_ENGINE_AUTO || engine > CEDAR_ENGINE_CTA) return fail(CEDAR_EINVAL, "unknown engine");
+  if (threads < 0 || threads > 1024 || threads % 32) return fail(CEDAR_EINVAL, "threads must be 0 or a multiple of 32 up to 1024");
+  c->engine = engine;
+  c->threads = threads ? threads : c->auto_threads;
+  return 0;
 }
 
 int cedar_ckt_last_ms(cedar_ckt *c, double *ms) {

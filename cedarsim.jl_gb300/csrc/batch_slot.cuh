@@ -134,7 +134,7 @@ struct Slot {
 
   __device__ __forceinline__ double gather(const int *ptr, const int *ent, int s, double acc) const {
     int a = ptr[s], b = ptr[s + 1];
-    for (int q = a; q < b; ++q) { int e = ent[q]; double v = w.dout[e >> 1]; acc = (e & 1) ? acc - v : acc + v; }
+    for (int q = a; q < b; ++q) { int e = ent[q]; acc = acc + signed_out(w.dout[e >> 1], e); }
     return acc;
   }
 
@@ -727,7 +727,6 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am, const 
   const double *const srcv = s.w.srcv;
   const double jgs = s.jgs;
   // two accumulators (even / odd entries) halve the dependent add chain
-  // two accumulators (even / odd entries) halve the dependent add chain
   auto gather = [&](const int *ptr, const int *ent, int q, double acc) {
     const int a = ptr[q], e1 = ptr[q + 1];
     double acc1 = 0.0;
@@ -735,10 +734,10 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am, const 
     for (; k + 1 < e1; k += 2) {
       const int e0 = ent[k], e2 = ent[k + 1];
       const double v0 = dout[e0 >> 1], v2 = dout[e2 >> 1];
-      acc = (e0 & 1) ? acc - v0 : acc + v0;
-      acc1 = (e2 & 1) ? acc1 - v2 : acc1 + v2;
+      acc = acc + signed_out(v0, e0);
+      acc1 = acc1 + signed_out(v2, e2);
     }
-    if (k < e1) { const int e0 = ent[k]; const double v0 = dout[e0 >> 1]; acc = (e0 & 1) ? acc - v0 : acc + v0; }
+    if (k < e1) { const int e0 = ent[k]; acc = acc + signed_out(dout[e0 >> 1], e0); }
     return acc + acc1;
   };
   // K1: device evaluation, one model at a time across the warp

@@ -78,6 +78,13 @@ struct DTpl {
   const int *lu_rowptr, *lu_colidx, *lu_cptr, *lu_cslot, *lu_srow;
 };
 
+// A stamp entry's signed device output: (e & 1) flips the sign bit, so a gather
+// adds acc + signed(v, e) -- the same value as acc - v / acc + v (IEEE a - b is
+// a + (-b)) with one FP64 add instead of two and a select.
+__device__ __forceinline__ double signed_out(double v, int e) {
+  return __longlong_as_double(__double_as_longlong(v) ^ ((long long)(e & 1) << 63));
+}
+
 // Gather lists longer than these are summed cooperatively in 32 fixed chunks
 // combined by a fixed pairwise tree (in-engine stamp programs / cedar_eval's).
 constexpr int kLongGather = 16;
@@ -149,7 +156,7 @@ __device__ __forceinline__ double long_gather(const int *ptr, const int *ent, in
   const int a = ptr[q], len = ptr[q + 1] - a;
   double v = lane_chunk_sum<K>(a, len, rank, [&](int c0, int c1) {
     double acc = 0.0;
-    for (int k = c0; k < c1; ++k) { const int e = ent[k]; const double d = dout[e >> 1]; acc = (e & 1) ? acc - d : acc + d; }
+    for (int k = c0; k < c1; ++k) { const int e = ent[k]; acc = acc + signed_out(dout[e >> 1], e); }
     return acc;
   });
 #pragma unroll
@@ -397,7 +404,7 @@ struct Engine {
 
   __device__ __forceinline__ double gather(const int *ptr, const int *ent, int s, double acc) const {
     int a = ptr[s], b = ptr[s + 1];
-    for (int k = a; k < b; ++k) { int e = ent[k]; double v = w.dout[e >> 1]; acc = (e & 1) ? acc - v : acc + v; }
+    for (int k = a; k < b; ++k) { int e = ent[k]; acc = acc + signed_out(w.dout[e >> 1], e); }
     return acc;
   }
 

@@ -63,12 +63,12 @@ __global__ void stamp_kernel(DTpl T, const double *dout, double *F, double *J) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (J && s < T.n_csc && T.jcsc_ptr[s + 1] - T.jcsc_ptr[s] <= kLongEval) {
     double acc = 0.0;
-    for (int k = T.jcsc_ptr[s]; k < T.jcsc_ptr[s + 1]; ++k) { int e = __ldg(T.jcsc_ent + k); double v = __ldg(dout + (e >> 1)); acc = (e & 1) ? acc - v : acc + v; }
+    for (int k = T.jcsc_ptr[s]; k < T.jcsc_ptr[s + 1]; ++k) { int e = __ldg(T.jcsc_ent + k); acc = acc + signed_out(__ldg(dout + (e >> 1)), e); }
     J[s] = acc;
   }
   if (F && s < T.n && T.forg_ptr[s + 1] - T.forg_ptr[s] <= kLongEval) {
     double acc = 0.0;
-    for (int k = T.forg_ptr[s]; k < T.forg_ptr[s + 1]; ++k) { int e = __ldg(T.forg_ent + k); double v = __ldg(dout + (e >> 1)); acc = (e & 1) ? acc - v : acc + v; }
+    for (int k = T.forg_ptr[s]; k < T.forg_ptr[s + 1]; ++k) { int e = __ldg(T.forg_ent + k); acc = acc + signed_out(__ldg(dout + (e >> 1)), e); }
     F[s] = acc;
   }
 }
@@ -87,8 +87,20 @@ __global__ void stamp_long_part_kernel(DTpl T, const double *dout, double *part)
   const int *ptr = is_j ? T.jcsc_ptr : T.forg_ptr, *ent = is_j ? T.jcsc_ent : T.forg_ent;
   const int k0 = ptr[q] + (p - T.long_off[lo]) * kLongChunkDev;
   const int k1 = min(k0 + kLongChunkDev, ptr[q + 1]);
+  // the chunk's entries in order; loads are issued 8 at a time ahead of the adds
+  // (the add chain and its order are unchanged)
   double acc = 0.0;
-  for (int k = k0; k < k1; ++k) { const int e = __ldg(ent + k); const double v = __ldg(dout + (e >> 1)); acc = (e & 1) ? acc - v : acc + v; }
+  int k = k0;
+  for (; k + 8 <= k1; k += 8) {
+    int e[8]; double v[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) e[j] = __ldg(ent + k + j);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[j] = __ldg(dout + (e[j] >> 1));
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc = acc + signed_out(v[j], e[j]);
+  }
+  for (; k < k1; ++k) { const int e = __ldg(ent + k); acc = acc + signed_out(__ldg(dout + (e >> 1)), e); }
   part[p] = acc;
 }
 
@@ -104,7 +116,15 @@ __global__ void __launch_bounds__(kLongThreads) stamp_long_final_kernel(DTpl T, 
   const int a = p0 + (int)(((long long)np * threadIdx.x) / kLongThreads);
   const int b = p0 + (int)(((long long)np * (threadIdx.x + 1)) / kLongThreads);
   double acc = 0.0;
-  for (int k = a; k < b; ++k) acc += part[k];
+  int k = a;
+  for (; k + 8 <= b; k += 8) {             // loads ahead of the in-order adds
+    double v[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[j] = part[k + j];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc += v[j];
+  }
+  for (; k < b; ++k) acc += part[k];
   red[threadIdx.x] = acc;
   __syncthreads();
   for (int w = 1; w < kLongThreads; w <<= 1) {
