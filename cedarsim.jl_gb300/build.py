@@ -75,10 +75,10 @@ def _stale() -> bool:
         return True
     t = LIB.stat().st_mtime
     deps = list(CSRC.glob("*")) + list(INCLUDE.glob("*.h")) + [pathlib.Path(__file__)]
-    if (GEN / "va_models.gen.h").exists():
-        deps.append(GEN / "va_models.gen.h")
-    else:
-        return True
+    for g in ("va_models.gen.h", "flops.gen.h"):
+        if not (GEN / g).exists():
+            return True
+        deps.append(GEN / g)
     return any(d.stat().st_mtime > t for d in deps)
 
 
@@ -88,8 +88,33 @@ def generate() -> pathlib.Path:
     return va.generate(GEN)
 
 
+def count_flops() -> pathlib.Path:
+    """Count the FP64 operations of one device evaluation per model by running
+    the device code on an op-counting scalar (csrc/opcount.cpp, a host tool) and
+    write them as flops.gen.h, the per-device work cedar_ckt_costs sums
+    (rewritten only when it changes)."""
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        raise RuntimeError("a host C++ compiler (g++) is needed to count device flops")
+    BUILD.mkdir(parents=True, exist_ok=True)
+    tool = BUILD / "opcount"
+    cmd = [cxx, "-std=c++17", "-O1", "-I", str(INCLUDE), "-I", str(CSRC), "-I", str(GEN), "-o", str(tool),
+           str(CSRC / "opcount.cpp")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"opcount build failed:\n{r.stdout}\n{r.stderr}")
+    r = subprocess.run([str(tool)], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"opcount failed:\n{r.stderr}")
+    out = GEN / "flops.gen.h"
+    if not out.exists() or out.read_text() != r.stdout:
+        out.write_text(r.stdout)
+    return out
+
+
 def build(force: bool = False, verbose: bool = False) -> pathlib.Path:
     generate()
+    count_flops()
     if not force and not _stale():
         return LIB
     BUILD.mkdir(parents=True, exist_ok=True)

@@ -9,6 +9,8 @@
 #include <vector>
 #include "compile.h"
 #include "kernels.cuh"
+// per-model FP64 operation counts of one device evaluation (written by build.py)
+#include "flops.gen.h"
 
 using namespace cedar;
 
@@ -396,24 +398,13 @@ int cedar_ckt_size(const cedar_ckt *c, int32_t *n, int32_t *nnz_j, int32_t *nnz_
   return 0;
 }
 
-// FP64 operations of one device evaluation (add/sub/mul/div = 1, FMA = 2,
-// exp = 1; counted from the expressions in models.cuh, the source waveform as
-// 10 for a pulse/pwl/sin segment evaluation)
+// FP64 operations of one device evaluation in the engines' Newton iteration,
+// counted at build time by running the device code (models.cuh and the emitted
+// Verilog-A code) on an op-counting scalar (csrc/opcount.cpp -> flops.gen.h):
+// add / sub / mul / div 1, FMA 2, exp / log / sqrt 1.
 static int model_flops(int m) {
-  switch (m) {
-    case CEDAR_R: return 2;
-    case CEDAR_C: return 4;
-    case CEDAR_L: return 7;
-    case CEDAR_V: return 13;
-    case CEDAR_I: return 11;
-    case CEDAR_E: return 5;
-    case CEDAR_G: return 2;
-    case CEDAR_MOS1: return 32;
-    case CEDAR_DIODE: return 13;
-    case CEDAR_NLVCR: return 10;
-  }
-  // Verilog-A: the module's operations, each carried with its terminal partials
-  if (m >= va::kBase && m < kNumModels) return va::kFlops[m - va::kBase] * (1 + va::kNTerm[m - va::kBase]);
+  if (m > 0 && m < CEDAR_NMODELS) return flops::kBuiltin[m];
+  if (m >= va::kBase && m < kNumModels) return flops::kVA[m - va::kBase];
   return 0;
 }
 

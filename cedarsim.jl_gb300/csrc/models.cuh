@@ -173,9 +173,10 @@ CEDAR_HD void mos1_fwd(double vgs, double vds, double vth, double beta, double l
   const double A = (vov - 0.5 * a) * a;
   const double bc = beta * clm;
   const double i = bc * A, g = bc * a, d = bc * (vov - a) + (beta * lam) * A;
-  id = off ? 0.0 : i;
-  gm = off ? 0.0 : g;
-  gds = off ? 0.0 : d;
+  const double zero = 0.0;
+  id = off ? zero : i;
+  gm = off ? zero : g;
+  gds = off ? zero : d;
 }
 
 // Evaluate one device.  v[k]: terminal (+branch) unknown values, vd[k]: their

@@ -708,7 +708,7 @@ class _Emitter:
                 if types[s.name] == "integer":
                     out.append(f"{ind}v_{s.name} = vint(val({self.x(s.expr)}));")
                 else:
-                    out.append(f"{ind}v_{s.name} = {self.x(s.expr)};")
+                    out.append(f"{ind}v_{s.name} = D({self.x(s.expr)});")
             elif isinstance(s, If):
                 out.append(f"{ind}if (val({self.x(s.c)}) != 0.0) {{")
                 out += self.stmts(s.then, ind + "  ", types)
