@@ -209,7 +209,7 @@ def reference_adjoint(args, pkg, orc):
             "seconds": dt, "failed": k - ok}
 
 
-def measure_eval(pkg, args, torch, C):
+def measure_eval(pkg, args, torch, C, fp64_peak=None):
     """cedar_eval_dev (device evaluation + CSC stamping, the drop-in residual /
     Jacobian boundary) on one large chain: inputs resident in HBM and larger than
     L2, CUDA events on the handle's stream, algorithmic bytes from cedar_ckt_costs."""
@@ -243,10 +243,19 @@ def measure_eval(pkg, args, torch, C):
     peak = hbm_peak_gbs()
     gbs = costs.bytes_eval / (ms * 1e-3) / 1e9
     ok = bool(torch.isfinite(F).all().item() and torch.isfinite(J).all().item())
+    # the call's FP64 work: every device's evaluation (op-counted) and one add per
+    # stamp entry; on this part the device arithmetic can bound the call before HBM
+    flops = costs.flops_eval + costs.flops_stamp
+    tfl = flops / (ms * 1e-3) / 1e12
+    t_floor = max(costs.bytes_eval / (peak * 1e9), flops / (fp64_peak * 1e12)) if fp64_peak else None
     return {"workload": f"{args.eval_stages}-stage inverter chain ({3 * args.eval_stages} devices, n = {sy.n}, "
                         f"nnz(J) = {sy.nnz_j}), one cedar_eval_dev per call",
             "bytes_per_call": int(costs.bytes_eval), "ms_per_call": ms, "achieved_gbs": gbs, "peak_gbs": peak,
             "frac": gbs / peak, "finite": ok, "kernels": ["eval_kernel", "stamp_kernel"],
+            "fp64": {"flops_per_call": int(flops), "achieved_tflops": tfl, "peak_tflops": fp64_peak,
+                     "frac": tfl / fp64_peak if fp64_peak else None},
+            "roofline_frac": (t_floor / (ms * 1e-3)) if t_floor else None,
+            "roofline_note": "roofline_frac = max(bytes / HBM peak, flops / FP64 peak) / measured time",
             "l2": "inputs and outputs of one call exceed L2 (129 MB)",
             "timing": f"CUDA events on the handle's stream around {reps} calls after 3 warm-up calls"}
 
@@ -706,7 +715,7 @@ def main():
                            "note": "flops = 2 x forward Newton iterations x flops per iteration (recording forward + "
                                    "replay) + accepted steps x (flops per iteration + substitution flops)"}
         del sw5
-    eval_leg = None if args.no_eval else measure_eval(pkg, args, torch, C)
+    eval_leg = None if args.no_eval else measure_eval(pkg, args, torch, C, fp64_peak)
     rings = None if args.no_rings else measure_rings(pkg, args, C, fp64_peak)
     if rings is not None and not args.no_va:
         rv = measure_rings(pkg, args, C, fp64_peak, verilog_a=True)

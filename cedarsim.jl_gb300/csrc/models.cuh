@@ -179,8 +179,22 @@ CEDAR_HD void mos1_fwd(double vgs, double vds, double vth, double beta, double l
   gds = off ? zero : d;
 }
 
+// The source waveform out of line: the batched engines take time-varying sources'
+// values from a per-solve cache, so the waveform code on the Newton iteration's
+// path only serves constant sources; a call keeps its code out of the hot loop.
+#if defined(__CUDACC__)
+static __host__ __device__ __noinline__
+#else
+static inline
+#endif
+double source_value_cold(const double *p, int s, double t, bool dc, const double *pwl) {
+  return source_value(p, s, t, dc, pwl);
+}
+
 // Evaluate one device.  v[k]: terminal (+branch) unknown values, vd[k]: their
 // time derivatives (only when ctx.xdot).  dp: derived params with stride ds.
+// HOT_SRC false: V / I source values through source_value_cold.
+template <bool HOT_SRC = true>
 CEDAR_HD void eval_device(int model, const double *dp, int ds, const double *v, const double *vd,
                           const EvalCtx &ctx, const double *pwl, double *out) {
   switch (model) {
@@ -202,12 +216,14 @@ CEDAR_HD void eval_device(int model, const double *dp, int ds, const double *v, 
     } break;
     case CEDAR_V: {
       double m = dp[0];
-      double vs = source_value(dp, ds, ctx.t, ctx.dc, pwl) * ctx.src_scale;
+      double vs = (HOT_SRC ? source_value(dp, ds, ctx.t, ctx.dc, pwl) : source_value_cold(dp, ds, ctx.t, ctx.dc, pwl)) *
+                  ctx.src_scale;
       out[0] = m * v[2]; out[1] = (v[0] - v[1]) - vs; out[2] = m; out[3] = 1.0;
     } break;
     case CEDAR_I: {
       double m = dp[0];
-      out[0] = m * (source_value(dp, ds, ctx.t, ctx.dc, pwl) * ctx.src_scale);
+      out[0] = m * ((HOT_SRC ? source_value(dp, ds, ctx.t, ctx.dc, pwl) : source_value_cold(dp, ds, ctx.t, ctx.dc, pwl)) *
+                    ctx.src_scale);
     } break;
     case CEDAR_E: {
       double gain = dp[0], m = dp[ds];
