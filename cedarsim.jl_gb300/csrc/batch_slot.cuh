@@ -205,6 +205,7 @@ struct Slot {
         }
         sk.samp[(long long)p * sk.ns + sk.next] = v;
       }
+      ssync();   // the slot's fields may live in shared memory: every lane reads sk.next before it moves
       sk.next++;
       ts_next = sk.next < sk.ns ? sample_ts(sk.next) : 1e300;
     }
@@ -606,6 +607,7 @@ struct Slot {
       const double *prev = k == 0 ? w.xn : w.xm1;
       for (int i = rank(); i < T->n; i += K) { c[i] = w.xn[i]; c[b.n_max + i] = prev[i]; }
     }
+    ssync();
     return true;
   }
 

@@ -4,6 +4,11 @@
 
 namespace cedar {
 
+// Slot state machines of wide slots in shared memory (1) or registers (0).
+#ifndef CEDAR_SLOT_SMEM
+#define CEDAR_SLOT_SMEM 1
+#endif
+
 // Minimum resident CTAs per SM the register allocation must allow (1: up to
 // 255 registers per thread).
 #ifndef CEDAR_BATCH_MIN_BLOCKS
@@ -17,9 +22,18 @@ namespace cedar {
 template <int K, bool SMEM, bool REC = false>
 __global__ void __launch_bounds__(256, CEDAR_BATCH_MIN_BLOCKS) batch_kernel(BatchDev b) {
   extern __shared__ double smem[];
-  Slot<K> s;
   const int slots_per_block = blockDim.x / K;
   const int slot = threadIdx.x / K;
+  // The slot's state machine: in shared memory for wide slots (one copy per slot,
+  // written identically by its lanes), which leaves the registers to the Newton
+  // iteration; in each lane's registers for narrow slots (many slots per CTA).
+#if CEDAR_SLOT_SMEM
+  __shared__ Slot<K> slot_state[K >= 16 ? 256 / K : 1];
+  Slot<K> s_local;
+  Slot<K> &s = K >= 16 ? slot_state[K >= 16 ? slot : 0] : s_local;
+#else
+  Slot<K> s;
+#endif
   double *ws;
   if constexpr (SMEM) ws = smem + (size_t)slot * b.ws_stride;
   else ws = b.ws_global + ((size_t)blockIdx.x * slots_per_block + slot) * b.ws_stride;
