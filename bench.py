@@ -677,8 +677,9 @@ def main():
             tk += km.value / 1e3
             acc += st.accepted
         plain = {"value": acc / tk, "unit": UNIT, "e2e_value": acc / tt,
-                 "sample": f"{args.plain_inst} random instances, each one cedar_tran_run (one warp, every accepted "
-                           f"point recorded) from DC to {args.plain_tstop * 1e9:g} ns with the headline's options",
+                 "sample": f"{args.plain_inst} random instances, each one cedar_tran_run (default engine: one "
+                           f"CTA; every accepted point recorded) from DC to {args.plain_tstop * 1e9:g} ns with "
+                           f"the headline's options",
                  "seconds_kernel": tk, "seconds_wall": tt}
     # discrete adjoint (workload 5) through the C ABI
     adj = None

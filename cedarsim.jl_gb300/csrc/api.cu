@@ -588,9 +588,10 @@ int cedar_dcop(cedar_ckt *c, double t, double *x, cedar_stats *stats) {
   return run_plain(c, 2, nullptr, t, 0.0, nullptr, x, nullptr, nullptr, 0, nullptr, stats);
 }
 
-// Largest workspace (doubles) for which the single-circuit transient runs on the
-// one-warp engine with its workspace in shared memory; larger circuits run on the
-// CTA engine (more lanes per level) with a global workspace.
+// Largest workspace (doubles) the one-warp engine takes (its workspace is in
+// shared memory).  The CTA engine is the default for one circuit: on the RC
+// ladder and the 31-stage chain it took 0.59x and 0.72x the one-warp engine's time
+// (its levels run on more lanes), so the one-warp engine is an explicit choice.
 constexpr int kWarpTranMaxWs = 24 * 1024;
 
 // The single-circuit transient on the batched engine's slot state machine, one
@@ -655,7 +656,7 @@ int cedar_tran_run(cedar_ckt *c, const cedar_tran_opts *opts, const double *x0, 
   const Template &H = c->tpl->H;
   std::vector<double> x(x0, x0 + H.n);
   const bool fits = ws_doubles(H.n, H.nnz_lu, H.n_out, (int)H.src_group.size()) <= kWarpTranMaxWs;
-  if (c->engine == CEDAR_ENGINE_WARP || (c->engine == CEDAR_ENGINE_AUTO && fits)) {
+  if (c->engine == CEDAR_ENGINE_WARP) {
     if (!fits) return fail(CEDAR_EINVAL, "circuit workspace exceeds the one-warp engine's shared memory");
     return run_tran_warp(c, opts, x.data(), t_out, x_out, cap, n_out, stats);
   }

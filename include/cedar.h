@@ -295,9 +295,10 @@ int cedar_tran_run(cedar_ckt *ckt, const cedar_tran_opts *opts, const double *x0
  * transient on the batched engine's instance state machine, one warp per
  * circuit, workspace in shared memory; the CTA engine runs one thread block
  * (threads: a multiple of 32, 0 = chosen from the circuit's size) and also
- * serves cedar_newton_solve and cedar_dcop.  AUTO (the default) takes the
- * one-warp engine for the transient of circuits whose workspace fits its shared
- * memory.  No counterpart in the reference: a tuning knob. */
+ * serves cedar_newton_solve and cedar_dcop.  AUTO (the default) is the CTA
+ * engine, the faster of the two on the circuits measured; the one-warp engine
+ * takes circuits whose workspace fits its shared memory (else CEDAR_EINVAL).
+ * No counterpart in the reference: a tuning knob. */
 enum { CEDAR_ENGINE_AUTO = 0, CEDAR_ENGINE_WARP = 1, CEDAR_ENGINE_CTA = 2 };
 int cedar_ckt_set_engine(cedar_ckt *ckt, int32_t engine, int32_t threads);
 /* Device time (ms) of the kernel of the last cedar_tran_run / cedar_newton_solve /
