@@ -49,6 +49,7 @@ def parse():
     p.add_argument("--seed", type=int, default=20240607)
     p.add_argument("--lanes", type=int, default=0, help="lanes per instance (0 = library default)")
     p.add_argument("--warps", type=int, default=0)
+    p.add_argument("--ctas", type=int, default=0, help="resident CTAs per SM at most (0 = as many as fit)")
     p.add_argument("--ref-inst", type=int, default=64, help="instances per reference (CPU) step")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -325,7 +326,7 @@ def measure_va(pkg, args, C, builtin_ms, builtin_steps, fp64_peak):
     o = opts_for(pkg, args.tstop_ns * 1e-9)
     sw = pkg.Batch(va_tpl, itpl, par, off)
     if args.lanes:
-        sw.set_tuning(args.lanes, args.warps or 4)
+        sw.set_tuning(args.lanes, args.warps or 4, args.ctas)
     r = sw.run(o)
     ms = C.c_double()
     pkg.abi.check(sw.lib.cedar_batch_last_ms(sw.handle, C.byref(ms)))
@@ -580,7 +581,7 @@ def main():
     n_samples = 201
     sw = pkg.Batch(templates, itpl[mine], par, off[mine], probes=probes, n_samples=n_samples)
     if args.lanes:
-        sw.set_tuning(args.lanes, args.warps or 4)
+        sw.set_tuning(args.lanes, args.warps or 4, args.ctas)
     tstop = args.tstop_ns * 1e-9
     o = opts_for(pkg, tstop)
     nwin = args.warmup + args.steps
@@ -639,7 +640,7 @@ def main():
         te0 = time.perf_counter()
         sw2 = pkg.Batch(templates, itpl[mine], par, off[mine], probes=probes, n_samples=n_samples)
         if args.lanes:
-            sw2.set_tuning(args.lanes, args.warps or 4)
+            sw2.set_tuning(args.lanes, args.warps or 4, args.ctas)
         r2 = sw2.run(o)
         torch.cuda.synchronize()
         barrier(dist)
@@ -687,7 +688,7 @@ def main():
         t5, i5, p5, o5_off, obj5, ts5 = adjoint_workload(pkg, args)
         sw5 = pkg.Batch(t5, i5, p5, o5_off)
         if args.lanes:
-            sw5.set_tuning(args.lanes, args.warps or 4)
+            sw5.set_tuning(args.lanes, args.warps or 4, args.ctas)
         sw5.adjoint(opts_for(pkg, 0.05e-9), obj5, ts5)          # warm-up
         r5 = sw5.adjoint(opts_for(pkg, args.adj_tstop_ns * 1e-9), obj5, ts5)
         ok5 = r5.status == 0

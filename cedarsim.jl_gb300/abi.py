@@ -73,7 +73,8 @@ class Objective(C.Structure):
 
 
 class BatchTuning(C.Structure):
-    _fields_ = [("lanes_per_inst", C.c_int32), ("warps_per_cta", C.c_int32), ("reserved", C.c_int32 * 6)]
+    _fields_ = [("lanes_per_inst", C.c_int32), ("warps_per_cta", C.c_int32), ("ctas_per_sm", C.c_int32),
+                ("reserved", C.c_int32 * 5)]
 
 
 def ptr(a: Optional[np.ndarray], ctype):

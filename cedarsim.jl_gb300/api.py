@@ -224,8 +224,8 @@ class Batch:
         check(self.lib.cedar_batch_get_tuning(self.handle, C.byref(t)))
         return t.lanes_per_inst, t.warps_per_cta
 
-    def set_tuning(self, lanes_per_inst: int, warps_per_cta: int):
-        t = BatchTuning(lanes_per_inst, warps_per_cta)
+    def set_tuning(self, lanes_per_inst: int, warps_per_cta: int, ctas_per_sm: int = 0):
+        t = BatchTuning(lanes_per_inst, warps_per_cta, ctas_per_sm)
         check(self.lib.cedar_batch_set_tuning(self.handle, C.byref(t)))
 
     def autotune(self, opts, horizon: float, cache: Optional[str] = None) -> Tuple[int, int]:

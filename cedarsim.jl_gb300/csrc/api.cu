@@ -996,6 +996,7 @@ int cedar_batch_set_tuning(cedar_batch *b, const cedar_batch_tuning *t) {
   int K = t->lanes_per_inst;
   if (K != 1 && K != 2 && K != 4 && K != 8 && K != 16 && K != 32) return fail(CEDAR_EINVAL, "lanes_per_inst must be a power of two <= 32");
   if (t->warps_per_cta < 1 || t->warps_per_cta > 8) return fail(CEDAR_EINVAL, "warps_per_cta must be 1..8");
+  if (t->ctas_per_sm < 0) return fail(CEDAR_EINVAL, "ctas_per_sm must be >= 0");
   b->tune = *t;
   return 0;
 }
@@ -1043,7 +1044,7 @@ static int batch_launch(cedar_batch *b, const EngOpts &eo, const cedar_batch_tun
   {
     // a persistent grid of exactly the CTAs that can be resident at once
     int per_sm = 1, dev = 0, nsm = 0;
-    CUDA_TRY(configure_batch(K, warps, smem, in_smem, &per_sm));
+    CUDA_TRY(configure_batch(K, warps, smem, in_smem, tu.ctas_per_sm, &per_sm));
     CUDA_TRY(cudaGetDevice(&dev));
     CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     grid = std::max(1, std::min(nsm * per_sm, (b->n_inst + tiles - 1) / tiles));

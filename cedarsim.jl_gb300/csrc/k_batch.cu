@@ -60,16 +60,19 @@ __global__ void __launch_bounds__(256, CEDAR_BATCH_MIN_BLOCKS) batch_kernel(Batc
 // the shared-memory carve-out that holds exactly those CTAs: the rest of the
 // unified L1 / shared storage stays L1, which caches the template's task lists.
 template <class F>
-static cudaError_t configure(F *kern, int threads, size_t smem, int *per_sm) {
+static cudaError_t configure(F *kern, int threads, size_t smem, int max_per_sm, int *per_sm) {
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int nb = 0;
   if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, threads, smem)) != cudaSuccess) return e;
   if (nb < 1) nb = 1;
+  if (max_per_sm > 0 && nb > max_per_sm) nb = max_per_sm;
+  cudaFuncAttributes fa{};
+  if ((e = cudaFuncGetAttributes(&fa, kern)) != cudaSuccess) return e;
   int dev = 0, smsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&smsm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-  const double need = (double)nb * (double)(smem + 1024);
+  const double need = (double)nb * (double)(smem + fa.sharedSizeBytes + 1024);
   int pct = (int)std::ceil(100.0 * need / (double)(smsm > 0 ? smsm : 1));
   pct = pct < 1 ? 1 : (pct > 100 ? 100 : pct);
   if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, pct)) != cudaSuccess) return e;
@@ -92,10 +95,11 @@ cudaError_t CEDAR_CAT(launch_batch_k, CEDAR_LANES)(const BatchDev &b, int warps,
   return cudaGetLastError();
 }
 
-cudaError_t CEDAR_CAT(configure_batch_k, CEDAR_LANES)(int warps, size_t smem, bool in_smem, int *per_sm) {
+cudaError_t CEDAR_CAT(configure_batch_k, CEDAR_LANES)(int warps, size_t smem, bool in_smem, int max_per_sm, int *per_sm) {
   constexpr int K = CEDAR_LANES;
   const int th = warps * 32;
-  return in_smem ? configure(batch_kernel<K, true>, th, smem, per_sm) : configure(batch_kernel<K, false>, th, smem, per_sm);
+  return in_smem ? configure(batch_kernel<K, true>, th, smem, max_per_sm, per_sm)
+                 : configure(batch_kernel<K, false>, th, smem, max_per_sm, per_sm);
 }
 
 #if CEDAR_LANES == 32

@@ -7,7 +7,7 @@ namespace cedar {
 #define CEDAR_PER_K(X) X(1) X(2) X(4) X(8) X(16) X(32)
 #define CEDAR_DECL(K)                                                                                        \
   cudaError_t launch_batch_k##K(const BatchDev &b, int warps, int grid, size_t smem, cudaStream_t st);      \
-  cudaError_t configure_batch_k##K(int warps, size_t smem, bool in_smem, int *per_sm);                      \
+  cudaError_t configure_batch_k##K(int warps, size_t smem, bool in_smem, int max_per_sm, int *per_sm);                      \
   cudaError_t launch_adjoint_k##K(const AdjDev &a, int warps, int grid, size_t smem, cudaStream_t st);
 CEDAR_PER_K(CEDAR_DECL)
 #undef CEDAR_DECL
@@ -21,9 +21,9 @@ cudaError_t launch_batch(const BatchDev &b, int K, int warps, int grid, size_t s
   return cudaErrorInvalidValue;
 }
 
-cudaError_t configure_batch(int K, int warps, size_t smem, bool in_smem, int *per_sm) {
+cudaError_t configure_batch(int K, int warps, size_t smem, bool in_smem, int max_per_sm, int *per_sm) {
   switch (K) {
-#define CEDAR_CASE(K) case K: return configure_batch_k##K(warps, smem, in_smem, per_sm);
+#define CEDAR_CASE(K) case K: return configure_batch_k##K(warps, smem, in_smem, max_per_sm, per_sm);
     CEDAR_PER_K(CEDAR_CASE)
 #undef CEDAR_CASE
   }

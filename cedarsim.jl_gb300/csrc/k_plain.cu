@@ -73,17 +73,12 @@ __global__ void stamp_kernel(DTpl T, const double *dout, double *F, double *J) {
   }
 }
 
-// Long lists (supply rails), pass 1: one fixed chunk of kLongChunk entries per
-// warp, summed in order into part[] (chunk p of list i at long_off[i] + p).  The
-// warp's lanes load the chunk's entries and outputs at once (two per lane), and
-// lane 0 adds the 64 values in order, so the chunk sum has the bits of a serial
-// in-order loop while its loads overlap.
+// Long lists (supply rails), pass 1: one thread per fixed chunk of kLongChunk
+// entries, summed in order into part[] (chunk p of list i at long_off[i] + p).
 constexpr int kLongChunkDev = 64;
-static_assert(kLongChunkDev == 64, "two entries per lane");
 __global__ void stamp_long_part_kernel(DTpl T, const double *dout, double *part) {
-  const int p = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-  const int lane = threadIdx.x & 31;
-  if (p >= T.n_long_part) return;            // whole warps leave together
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= T.n_long_part) return;
   const int nl = T.n_long_jc + T.n_long_fo;
   int lo = 0, hi = nl;                       // list i with long_off[i] <= p < long_off[i + 1]
   while (hi - lo > 1) { const int mid = (lo + hi) >> 1; if (T.long_off[mid] <= p) lo = mid; else hi = mid; }
@@ -91,16 +86,22 @@ __global__ void stamp_long_part_kernel(DTpl T, const double *dout, double *part)
   const int q = is_j ? T.long_jc[lo] : T.long_fo[lo - T.n_long_jc];
   const int *ptr = is_j ? T.jcsc_ptr : T.forg_ptr, *ent = is_j ? T.jcsc_ent : T.forg_ent;
   const int k0 = ptr[q] + (p - T.long_off[lo]) * kLongChunkDev;
-  const int cnt = min(kLongChunkDev, ptr[q + 1] - k0);
-  double v0 = 0.0, v1 = 0.0;
-  if (lane < cnt) { const int e = __ldg(ent + k0 + lane); v0 = signed_out(__ldg(dout + (e >> 1)), e); }
-  if (lane + 32 < cnt) { const int e = __ldg(ent + k0 + 32 + lane); v1 = signed_out(__ldg(dout + (e >> 1)), e); }
+  const int k1 = min(k0 + kLongChunkDev, ptr[q + 1]);
+  // the chunk's entries in order; loads are issued 8 at a time ahead of the adds
+  // (the add chain and its order are unchanged)
   double acc = 0.0;
+  int k = k0;
+  for (; k + 8 <= k1; k += 8) {
+    int e[8]; double v[8];
 #pragma unroll
-  for (int j = 0; j < 32; ++j) { const double u = __shfl_sync(0xffffffffu, v0, j); if (j < cnt) acc = acc + u; }
+    for (int j = 0; j < 8; ++j) e[j] = __ldg(ent + k + j);
 #pragma unroll
-  for (int j = 0; j < 32; ++j) { const double u = __shfl_sync(0xffffffffu, v1, j); if (32 + j < cnt) acc = acc + u; }
-  if (lane == 0) part[p] = acc;
+    for (int j = 0; j < 8; ++j) v[j] = __ldg(dout + (e[j] >> 1));
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc = acc + signed_out(v[j], e[j]);
+  }
+  for (; k < k1; ++k) { const int e = __ldg(ent + k); acc = acc + signed_out(__ldg(dout + (e >> 1)), e); }
+  part[p] = acc;
 }
 
 // Pass 2: one CTA per long list; thread t sums its contiguous share of the
@@ -145,7 +146,7 @@ cudaError_t launch_eval(const DTpl &T, const DTpl *T_dev, const double *dpar, co
   stamp_kernel<<<(m + th - 1) / th, th, 0, s>>>(T, dout, F, J);
   const int nlong = T.n_long_jc + T.n_long_fo;
   if (nlong > 0) {
-    stamp_long_part_kernel<<<(int)(((long long)T.n_long_part * 32 + th - 1) / th), th, 0, s>>>(T, dout, part);
+    stamp_long_part_kernel<<<(T.n_long_part + th - 1) / th, th, 0, s>>>(T, dout, part);
     stamp_long_final_kernel<<<nlong, kLongThreads, 0, s>>>(T, part, F, J);
   }
   return cudaGetLastError();

@@ -146,8 +146,9 @@ cudaError_t launch_batch(const BatchDev &b, int K, int warps_per_cta, int grid, 
 // the single-circuit transient; smem > 0 puts the workspace in shared memory
 cudaError_t launch_batch_record(const BatchDev &b, size_t smem, cudaStream_t s);
 // (k_dispatch.cu) set the launch attributes of batch_kernel<K> for this shape and report its
-// resident CTAs per SM (registers and shared memory both counted)
-cudaError_t configure_batch(int K, int warps_per_cta, size_t smem, bool ws_in_smem, int *per_sm);
+// resident CTAs per SM (registers and shared memory both counted; at most max_per_sm when
+// positive), with the shared-memory carve-out that holds exactly those CTAs
+cudaError_t configure_batch(int K, int warps_per_cta, size_t smem, bool ws_in_smem, int max_per_sm, int *per_sm);
 int batch_max_smem_optin();
 
 }  // namespace cedar

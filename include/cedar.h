@@ -330,11 +330,15 @@ typedef struct cedar_batch_desc {
 
 typedef struct cedar_batch cedar_batch;
 
-/* Lanes per instance and instances per CTA chosen by the autotuner (0 = auto). */
+/* Lanes per instance and instances per CTA chosen by the autotuner (0 = auto),
+ * and an upper bound on resident CTAs per SM (0 = as many as registers and
+ * shared memory allow): fewer CTAs leave more of the SM's unified L1 / shared
+ * storage as L1, which caches the templates' task lists. */
 typedef struct cedar_batch_tuning {
   int32_t lanes_per_inst;         /* 1, 2, 4, 8, 16 or 32                       */
   int32_t warps_per_cta;
-  int32_t reserved[6];
+  int32_t ctas_per_sm;            /* 0 = no bound                               */
+  int32_t reserved[5];
 } cedar_batch_tuning;
 
 int cedar_batch_create(const cedar_batch_desc *desc, cedar_batch **out);
