@@ -159,7 +159,7 @@ LIB_PATH = PKG / "_build" / "libcedar_gpu.so"
 EXPORTS = [
     "cedar_last_error", "cedar_version", "cedar_model_nterm", "cedar_model_npar", "cedar_model_has_branch",
     "cedar_tran_opts_default", "cedar_ckt_create", "cedar_plan_create", "cedar_ckt_destroy", "cedar_ckt_size", "cedar_ckt_pattern",
-    "cedar_ckt_costs", "cedar_ckt_symbolic", "cedar_eval", "cedar_eval_dev", "cedar_eval_dev_noalloc", "cedar_eval_scratch", "cedar_newton_solve", "cedar_dcop", "cedar_tran_run", "cedar_ckt_last_ms", "cedar_ckt_set_engine",
+    "cedar_ckt_costs", "cedar_ckt_symbolic", "cedar_eval", "cedar_eval_dev", "cedar_eval_dev_noalloc", "cedar_eval_scratch", "cedar_newton_solve", "cedar_dcop", "cedar_tran_run", "cedar_ckt_last_ms", "cedar_ckt_set_engine", "cedar_ckt_last_blocks",
     "cedar_batch_create", "cedar_batch_destroy", "cedar_batch_run", "cedar_batch_start", "cedar_batch_advance",
     "cedar_batch_results", "cedar_batch_last_ms", "cedar_batch_set_tuning",
     "cedar_batch_get_tuning", "cedar_batch_autotune", "cedar_batch_nmax",
@@ -207,6 +207,7 @@ def load_library(build_if_missing: bool = True):
                                      c_int64_p, C.POINTER(Stats)]),
         "cedar_ckt_last_ms": (C.c_int, [P, c_double_p]),
         "cedar_ckt_set_engine": (C.c_int, [P, C.c_int32, C.c_int32]),
+        "cedar_ckt_last_blocks": (C.c_int, [P, c_int32_p]),
         "cedar_batch_create": (C.c_int, [C.POINTER(BatchDesc), C.POINTER(P)]),
         "cedar_batch_destroy": (C.c_int, [P]),
         "cedar_batch_run": (C.c_int, [P, C.POINTER(TranOpts), c_double_p, c_double_p, P]),

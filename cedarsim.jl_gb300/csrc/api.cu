@@ -276,8 +276,10 @@ struct cedar_ckt {
   // single-circuit transient on the one-warp engine: queue words, final state
   DevBuf<int> wq;
   DevBuf<double> xf;
+  DevBuf<double> gred;      // grid engine: reduction scratch (6 doubles per block)
   cudaEvent_t run_ev[2] = {nullptr, nullptr};   // bracket the last single-circuit kernel
   bool run_timed = false;
+  int last_blocks = 0;      // blocks of the last single-circuit kernel
   ~cedar_ckt() {
     for (cudaEvent_t e : run_ev) if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : ac_ev) if (e) cudaEventDestroy(e);
@@ -535,6 +537,11 @@ int cedar_eval(cedar_ckt *c, const double *x, const double *xdot, double t, doub
   return 0;
 }
 
+// Circuits at least this large run on the grid engine by default (one CTA
+// would walk their devices, slots and level tasks hundreds of times per phase).
+constexpr int kGridMinN = 4096;
+static bool use_grid(const Template &H) { return H.n >= kGridMinN; }
+
 static int run_plain(cedar_ckt *c, int mode, const cedar_tran_opts *opts, double t, double cj, const double *hist,
                      double *x, double *t_out, double *x_out, int64_t cap, int64_t *n_out, cedar_stats *stats) {
   if (c->host_only) return fail(CEDAR_EINVAL, "host-only plan handle");
@@ -556,10 +563,22 @@ static int run_plain(cedar_ckt *c, int mode, const cedar_tran_opts *opts, double
     a.t_out = c->tout.p; a.x_out = c->xout.p; a.cap = cap;
   }
   a.count = c->count.p; a.stats = c->stats.p; a.ws_global = c->ws.p;
+  const int wsd = ws_doubles(H.n, H.nnz_lu, H.n_out, (int)H.src_group.size());
+  const bool grid = c->engine == CEDAR_ENGINE_GRID || (c->engine == CEDAR_ENGINE_AUTO && use_grid(H));
+  int blocks = 1;
+  if (grid) {
+    CUDA_TRY(grid_geometry(std::max(std::max(H.nnz_lu, (int)n), c->tpl->D.n_dev), &blocks));
+    CUDA_TRY(c->ws.ensure(wsd));
+    CUDA_TRY(c->gred.ensure((size_t)6 * blocks));
+    a.ws_global = c->ws.p;
+    a.dense = nullptr;                 // the dense DC fallback is a one-block algorithm
+  }
   if (!c->run_ev[0]) { CUDA_TRY(cudaEventCreate(&c->run_ev[0])); CUDA_TRY(cudaEventCreate(&c->run_ev[1])); }
   CUDA_TRY(cudaEventRecord(c->run_ev[0], c->stream));
-  CUDA_TRY(launch_plain(a, ws_doubles(H.n, H.nnz_lu, H.n_out, (int)H.src_group.size()), c->threads, c->stream));
+  if (grid) CUDA_TRY(launch_plain_grid(a, blocks, c->gred.p, c->stream));
+  else CUDA_TRY(launch_plain(a, wsd, c->threads, c->stream));
   CUDA_TRY(cudaEventRecord(c->run_ev[1], c->stream));
+  c->last_blocks = blocks;
   c->run_timed = true;
   EngStats st{}; long long cnt = 0;
   CUDA_TRY(cudaMemcpyAsync(&st, c->stats.p, sizeof(st), cudaMemcpyDeviceToHost, c->stream));
@@ -665,10 +684,16 @@ int cedar_tran_run(cedar_ckt *c, const cedar_tran_opts *opts, const double *x0, 
 
 int cedar_ckt_set_engine(cedar_ckt *c, int32_t engine, int32_t threads) {
   if (!c) return fail(CEDAR_EINVAL, "null handle");
-  if (engine < CEDAR_ENGINE_AUTO || engine > CEDAR_ENGINE_CTA) return fail(CEDAR_EINVAL, "unknown engine");
+  if (engine < CEDAR_ENGINE_AUTO || engine > CEDAR_ENGINE_GRID) return fail(CEDAR_EINVAL, "unknown engine");
   if (threads < 0 || threads > 1024 || threads % 32) return fail(CEDAR_EINVAL, "threads must be 0 or a multiple of 32 up to 1024");
   c->engine = engine;
   c->threads = threads ? threads : c->auto_threads;
+  return 0;
+}
+
+int cedar_ckt_last_blocks(const cedar_ckt *c, int32_t *blocks) {
+  if (!c || !blocks) return fail(CEDAR_EINVAL, "null argument");
+  *blocks = c->last_blocks;
   return 0;
 }
 

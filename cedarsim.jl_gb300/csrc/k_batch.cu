@@ -4,9 +4,13 @@
 
 namespace cedar {
 
-// Slot state machines of wide slots in shared memory (1) or registers (0).
+// Slot state machines of wide slots in shared memory (1) or registers (0).  In
+// shared memory the kernel needs 118 registers instead of 234, but on the
+// 4096-chain workload that bought nothing: at 8 warps per SM both ran at 13.9 M
+// instance-steps/s, and the extra CTAs the registers allow shrink the L1 that
+// caches the task lists (12 warps per SM: 12.8 M).  Registers stay the default.
 #ifndef CEDAR_SLOT_SMEM
-#define CEDAR_SLOT_SMEM 1
+#define CEDAR_SLOT_SMEM 0
 #endif
 
 // Minimum resident CTAs per SM the register allocation must allow (1: up to

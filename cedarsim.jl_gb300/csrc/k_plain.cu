@@ -1,6 +1,7 @@
 // k_plain.cu — parameter derivation, the drop-in residual/Jacobian kernels
 // (cedar_eval) and the single-instance block engine (Newton / DC / transient).
 #include <mutex>
+#include <cooperative_groups.h>
 #include "kernels.cuh"
 
 namespace cedar {
@@ -234,15 +235,81 @@ cudaError_t launch_fp64_probe(int active_lanes, int iters, double *gflops, doubl
   return cudaGetLastError();
 }
 
-// Single instance on one CTA.  Workspace in dynamic shared memory when it fits,
-// else in global memory (a.ws_global).
-__global__ void plain_kernel(PlainArgs a) {
-  extern __shared__ double smem[];
-  double *red = smem;
-  double *ws = a.ws_global ? a.ws_global : smem + 128;
+// ---------------------------------------------------------------------------
+// One circuit on every thread of a cooperative grid (large circuits).
+//
+// The engine's group interface over the whole grid: rank / size are the global
+// thread index and count, sync() is a grid-wide barrier (cooperative launch, so
+// every block is resident), and a reduction combines each block's threads as
+// BlockGroup does, posts the block's value to global scratch, synchronises the
+// grid and lets every block combine the posted values in block order, so every
+// thread holds the same result.  max / min are exact and the step-error ratio is
+// merged as fractions, so the engine takes the decisions it takes on one CTA.
+// Two scratch buffers alternate: a block that moves on to the next reduction
+// writes the other buffer while slower blocks still read this one.
+struct GridGroup {
+  int rank, size;
+  double *red;            // shared scratch (>= 96 doubles)
+  double *gred;           // global scratch: 2 buffers of 3 doubles per block
+  mutable int ph;         // buffer of the next reduction
+  __device__ GridGroup(double *r, double *g)
+      : rank(blockIdx.x * blockDim.x + threadIdx.x), size(gridDim.x * blockDim.x), red(r), gred(g), ph(0) {}
+  __device__ void sync() const { cooperative_groups::this_grid().sync(); }
+  __device__ double *buf() const { double *b = gred + (size_t)(ph & 1) * 3 * gridDim.x; ++ph; return b; }
+  __device__ double reduce(double v, bool is_max) const {
+    BlockGroup blk(red);
+    const double bv = blk.reduce(v, is_max);
+    double *b = buf();
+    if (threadIdx.x == 0) b[blockIdx.x] = bv;
+    sync();
+    if (threadIdx.x == 0) {
+      double r = b[0];
+      for (int i = 1; i < (int)gridDim.x; ++i) { const double w = b[i]; r = is_max ? (w > r ? w : r) : (w < r ? w : r); }
+      red[0] = r;
+    }
+    __syncthreads();
+    const double r = red[0];
+    __syncthreads();
+    return r;
+  }
+  __device__ bool any(bool p) const { return reduce(p ? 1.0 : 0.0, true) != 0.0; }
+  __device__ double max(double v) const { return reduce(v, true); }
+  __device__ double min(double v) const { return reduce(v, false); }
+  __device__ double ratio(MaxRatio m) const {
+    for (int o = 16; o > 0; o >>= 1) {
+      const double n2 = __shfl_xor_sync(0xffffffffu, m.num, o), d2 = __shfl_xor_sync(0xffffffffu, m.den, o);
+      const bool b2 = __shfl_xor_sync(0xffffffffu, (int)m.bad, o) != 0;
+      m.merge(n2, d2, b2);
+    }
+    const int warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) { red[3 * warp] = m.num; red[3 * warp + 1] = m.den; red[3 * warp + 2] = m.bad ? 1.0 : 0.0; }
+    __syncthreads();
+    double *b = buf();
+    if (threadIdx.x == 0) {
+      MaxRatio r; r.num = red[0]; r.den = red[1]; r.bad = red[2] != 0.0;
+      for (int i = 1; i < nw; ++i) r.merge(red[3 * i], red[3 * i + 1], red[3 * i + 2] != 0.0);
+      b[3 * blockIdx.x] = r.num; b[3 * blockIdx.x + 1] = r.den; b[3 * blockIdx.x + 2] = r.bad ? 1.0 : 0.0;
+    }
+    sync();
+    if (threadIdx.x == 0) {
+      MaxRatio r; r.num = b[0]; r.den = b[1]; r.bad = b[2] != 0.0;
+      for (int i = 1; i < (int)gridDim.x; ++i) r.merge(b[3 * i], b[3 * i + 1], b[3 * i + 2] != 0.0);
+      red[0] = r.value();
+    }
+    __syncthreads();
+    const double r = red[0];
+    __syncthreads();
+    return r;
+  }
+};
+
+// The single-circuit body on a thread group G (one CTA or a whole grid):
+// mode 0 = transient, 1 = one Newton solve, 2 = DC operating point.
+template <class G>
+__device__ void plain_body(const PlainArgs &a, G g, double *ws) {
   const DTpl &T = *a.T;
-  BlockGroup g(red);
-  Engine<BlockGroup> E(T, a.dpar, ws, g);
+  Engine<G> E(T, a.dpar, ws, g);
   E.dense = a.dense;
   for (int i = g.rank; i < T.n; i += g.size) E.w.x[i] = a.x[T.order[i]];
   g.sync();
@@ -255,7 +322,7 @@ __global__ void plain_kernel(PlainArgs a) {
     sk.t_out = a.t_out; sk.x_out = a.x_out; sk.cap = a.cap; sk.count = 0;
     sk.tstart = o.tstart; sk.tstop = o.tstop;
     E.tran(E.w.x, o, sk, st, nullptr);
-    if (threadIdx.x == 0 && a.count) *a.count = sk.count;
+    if (g.rank == 0 && a.count) *a.count = sk.count;
   } else if (a.mode == 1) {
     for (int e = g.rank; e < T.n; e += g.size) E.w.hist[T.eq_pos[e]] = a.hist ? a.hist[e] : 0.0;
     g.sync();
@@ -270,7 +337,44 @@ __global__ void plain_kernel(PlainArgs a) {
   }
   g.sync();
   for (int i = g.rank; i < T.n; i += g.size) a.x[T.order[i]] = E.w.x[i];
-  if (threadIdx.x == 0 && a.stats) *a.stats = st;
+  if (g.rank == 0 && a.stats) *a.stats = st;
+}
+
+// Single instance on one CTA.  Workspace in dynamic shared memory when it fits,
+// else in global memory (a.ws_global).
+__global__ void plain_kernel(PlainArgs a) {
+  extern __shared__ double smem[];
+  double *ws = a.ws_global ? a.ws_global : smem + 128;
+  plain_body(a, BlockGroup(smem), ws);
+}
+
+// Single instance on a cooperative grid; workspace in global memory.
+constexpr int kGridThreads = 256;
+__global__ void __launch_bounds__(kGridThreads) plain_grid_kernel(PlainArgs a, double *gred) {
+  __shared__ double red[128];
+  plain_body(a, GridGroup(red, gred), a.ws_global);
+}
+
+cudaError_t grid_geometry(int work, int *blocks) {
+  int dev = 0, nsm = 0, per = 0, coop = 0;
+  cudaError_t e;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev)) != cudaSuccess) return e;
+  if (!coop) return cudaErrorNotSupported;
+  if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, plain_grid_kernel, kGridThreads, 0)) != cudaSuccess)
+    return e;
+  const int want = (work + kGridThreads - 1) / kGridThreads;
+  const int cap = nsm * (per < 1 ? 1 : per);
+  *blocks = want < 1 ? 1 : (want < cap ? want : cap);
+  return cudaSuccess;
+}
+
+cudaError_t launch_plain_grid(const PlainArgs &a, int blocks, double *gred, cudaStream_t s) {
+  PlainArgs aa = a;
+  double *g = gred;
+  void *args[] = {&aa, &g};
+  return cudaLaunchCooperativeKernel((const void *)plain_grid_kernel, dim3(blocks), dim3(kGridThreads), args, 0, s);
 }
 
 cudaError_t launch_plain(const PlainArgs &a, int wsd, int threads, cudaStream_t s) {

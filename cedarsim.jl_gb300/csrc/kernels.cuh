@@ -111,6 +111,10 @@ struct PlainArgs {
   int mode;
 };
 cudaError_t launch_plain(const PlainArgs &a, int ws_doubles_n, int threads, cudaStream_t s);
+// the same single-circuit engine on a cooperative grid (large circuits): blocks for
+// `work` parallel items, at most what can be resident; gred = 6 doubles per block
+cudaError_t grid_geometry(int work, int *blocks);
+cudaError_t launch_plain_grid(const PlainArgs &a, int blocks, double *gred, cudaStream_t s);
 
 // AC / noise analysis (k_ac.cu): one warp per angular frequency over the
 // template's LU and substitution task lists in complex FP64

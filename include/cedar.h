@@ -294,13 +294,19 @@ int cedar_tran_run(cedar_ckt *ckt, const cedar_tran_opts *opts, const double *x0
 /* Engine of the single-circuit entry points.  The one-warp engine runs the
  * transient on the batched engine's instance state machine, one warp per
  * circuit, workspace in shared memory; the CTA engine runs one thread block
- * (threads: a multiple of 32, 0 = chosen from the circuit's size) and also
- * serves cedar_newton_solve and cedar_dcop.  AUTO (the default) is the CTA
- * engine, the faster of the two on the circuits measured; the one-warp engine
- * takes circuits whose workspace fits its shared memory (else CEDAR_EINVAL).
- * No counterpart in the reference: a tuning knob. */
-enum { CEDAR_ENGINE_AUTO = 0, CEDAR_ENGINE_WARP = 1, CEDAR_ENGINE_CTA = 2 };
+ * (threads: a multiple of 32, 0 = chosen from the circuit's size); the grid
+ * engine runs the CTA engine's algorithm on every block of a cooperative grid
+ * (grid-wide barriers and reductions; large circuits).  The CTA and grid engines
+ * also serve cedar_newton_solve and cedar_dcop (the dense-pivoting DC rerun is
+ * one-block only).  AUTO (the default): the grid engine for circuits of 4096
+ * unknowns or more, else the CTA engine (the faster of the CTA and one-warp
+ * engines on the circuits measured); the one-warp engine takes circuits whose
+ * workspace fits its shared memory (else CEDAR_EINVAL).  No counterpart in the
+ * reference: a tuning knob. */
+enum { CEDAR_ENGINE_AUTO = 0, CEDAR_ENGINE_WARP = 1, CEDAR_ENGINE_CTA = 2, CEDAR_ENGINE_GRID = 3 };
 int cedar_ckt_set_engine(cedar_ckt *ckt, int32_t engine, int32_t threads);
+/* Thread blocks of the last single-circuit kernel (1 on the CTA engine). */
+int cedar_ckt_last_blocks(const cedar_ckt *ckt, int32_t *blocks);
 /* Device time (ms) of the kernel of the last cedar_tran_run / cedar_newton_solve /
  * cedar_dcop on this handle (CUDA events on the handle's stream around it).  No
  * counterpart in the reference: for throughput accounting. */
