@@ -35,6 +35,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "MC transient inst-steps/s, batched vs plain GPU @1e-6 reltol; adjoint grads/s"
+# DRAM bytes (read + written) of the batched kernel per accepted instance-step,
+# from one ncu capture of a 1024-chain window (7.27 MB over 988 847 steps); the
+# kernel keeps every instance's state on chip, so this is parameter and history
+# traffic only
+DRAM_BYTES_PER_STEP = 7.35
 UNIT = "instance-timesteps/s"
 TSTOP = 20e-9
 
@@ -755,7 +760,11 @@ def main():
         "newton_iters_per_s": iters_all / dt, "failed_instances": bad, "host_wall_s": wall,
         "launch_ms": dev_ms,
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                     "frac": achieved / fp64_peak, "traffic": None,
+                     "frac": achieved / fp64_peak,
+                     "traffic": DRAM_BYTES_PER_STEP * steps_all / max(1, len(dev_ms)),
+                     "traffic_note": f"bytes per launch: {DRAM_BYTES_PER_STEP} B of DRAM traffic per accepted "
+                                     "instance-step (ncu dram__bytes_read + write of one batch_kernel window of "
+                                     "1024 chains) x the accepted steps of a timed launch",
                      "note": "algorithmic FP64 flops per Newton iteration (cedar_ckt_costs) x iterations / time; "
                              "peak = DFMA rate measured in this run by cedar_fp64_probe (MEASURED_PEAKS.json "
                              "has no FP64 entry); the kernel keeps its state on chip, so HBM is not its bound"},
