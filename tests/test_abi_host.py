@@ -163,3 +163,26 @@ def test_eval_scratch_query_on_a_plan(pkg):
         finally:
             lib.cedar_ckt_destroy(p)
     assert lib.cedar_eval_scratch(None, C.byref(C.c_int64()), None, None) == -1
+
+
+def test_engine_selection_arguments(pkg):
+    """cedar_ckt_set_engine accepts the four engine codes and thread counts that
+    are 0 or multiples of 32 up to 1024, and refuses anything else (host-side
+    checks, on a host-only plan)."""
+    lib = pkg.load_library()
+    h = pkg.abi.DescHolder(pkg.generators.inverter_chain(5).flatten())
+    p = C.c_void_p()
+    pkg.abi.check(lib.cedar_plan_create(C.byref(h.desc), C.byref(p)))
+    try:
+        for eng in (0, 1, 2, 3):
+            assert lib.cedar_ckt_set_engine(p, eng, 0) == 0
+        assert lib.cedar_ckt_set_engine(p, 2, 256) == 0
+        assert lib.cedar_ckt_set_engine(p, 4, 0) == -1
+        assert lib.cedar_ckt_set_engine(p, -1, 0) == -1
+        assert lib.cedar_ckt_set_engine(p, 2, 48) == -1
+        assert lib.cedar_ckt_set_engine(p, 2, 2048) == -1
+        assert lib.cedar_ckt_set_engine(None, 0, 0) == -1
+        blocks = C.c_int32(7)
+        assert lib.cedar_ckt_last_blocks(p, C.byref(blocks)) == 0 and blocks.value == 0
+    finally:
+        lib.cedar_ckt_destroy(p)
