@@ -710,6 +710,12 @@ int cedar_ckt_last_ms(cedar_ckt *c, double *ms) {
 namespace {
 constexpr size_t kAcWsBudget = size_t(1) << 30;   // bytes of per-warp workspaces at most
 constexpr int kAcWarpsPerSm = 16;
+// one lane per frequency up to this many complex workspace values per frequency
+// (LU values + 3 n), with up to this many warps per SM (the lanes' dependent
+// loads are hidden by warps: on the 100-section RC ladder 4, 16 and 32 warps per SM
+// gave 15.5, 24.4 and 27.2 M frequency points/s), in at most twice kAcWsBudget
+constexpr int kAcLaneMaxPer = 8192;
+constexpr int kAcLaneWarpsPerSm = 32;
 
 // G and C per LU slot at x_op, the frequencies, and the workspaces of the warps
 // that will take them; fills everything of `a` but the analysis' own inputs.
@@ -728,11 +734,18 @@ int ac_prepare(cedar_ckt *c, const double *x_op, int32_t n_freq, const double *o
   CUDA_TRY(cudaGetDevice(&dev));
   CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const size_t per = (size_t)H.nnz_lu + 3 * n;
-  long long nw = std::min<long long>(n_freq, (long long)sms * kAcWarpsPerSm);
-  nw = std::min<long long>(nw, std::max<long long>(1, (long long)(kAcWsBudget / (per * sizeof(double2)))));
-  CUDA_TRY(c->ac_ws.ensure((size_t)nw * per));
+  // one lane per frequency when a frequency's workspace is small (32 of them per
+  // warp, interleaved), else one warp per frequency
+  const bool lane = per <= (size_t)kAcLaneMaxPer;
+  const size_t per_warp = lane ? 32 * per : per;
+  const long long units = lane ? ((long long)n_freq + 31) / 32 : (long long)n_freq;
+  long long nw = std::min<long long>(units, (long long)sms * (lane ? kAcLaneWarpsPerSm : kAcWarpsPerSm));
+  nw = std::min<long long>(nw, std::max<long long>(1, (long long)((lane ? 2 * kAcWsBudget : kAcWsBudget) /
+                                                                    (per_warp * sizeof(double2)))));
+  CUDA_TRY(c->ac_ws.ensure((size_t)nw * per_warp));
   a.T = D; a.gval = c->ac_g.p; a.cval = c->ac_c.p; a.omega = c->ac_omega.p; a.n_freq = n_freq;
   a.ws = c->ac_ws.p; a.ws_stride = (long long)per; a.n_warps = nw; a.status = c->ac_status.p;
+  a.lane_mode = lane ? 1 : 0;
   CUDA_TRY(c->ac_ndense.ensure(1));
   a.n_dense = c->ac_ndense.p;
   return 0;

@@ -12,6 +12,10 @@
 //
 //   ac_split_kernel   one thread per LU slot: G and C values of the slot, from
 //                     the device outputs at x_op (cj = 1), split by out_q
+//   ac_lane_kernel    one lane per frequency, 32 frequencies per warp in lockstep
+//                     (circuits whose per-frequency workspace is small): the
+//                     work of ac_kernel below with every FP64 instruction
+//                     serving 32 frequencies
 //   ac_kernel<false>  one warp per frequency: assemble G + jωC, LU, forward and
 //                     back substitution of b, probed unknowns out
 //   ac_kernel<true>   one warp per frequency: LU, then (G + jωC)ᵀ y = e_probe by
@@ -242,6 +246,135 @@ __global__ void __launch_bounds__(128) ac_kernel(AcDev a) {
   }
 }
 
+// One lane per frequency (circuits whose per-frequency workspace is small): a
+// warp runs 32 frequencies through the same task lists in lockstep, so every
+// task record and slot index is a broadcast load and every FP64 instruction
+// serves 32 frequencies (on this part an FP64 warp instruction costs the same
+// whatever its active mask).  The per-lane workspaces are interleaved, element e
+// of lane l at ws[e * 32 + l], so each access of the warp is one contiguous
+// 512-byte line.  Each task is summed in the pair order of ac_kernel and the
+// residual check takes the same norms, so a frequency's response has the bits
+// ac_kernel gives it; the noise PSD sums its sources in order (ac_kernel sums
+// them lane-strided, then by a butterfly).
+template <bool NOISE>
+__global__ void __launch_bounds__(128) ac_lane_kernel(AcDev a) {
+  const DTpl &T = a.T;
+  const int lane = threadIdx.x & 31;
+  const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (wid >= a.n_warps) return;
+  double2 *const base = a.ws + wid * a.ws_stride * 32 + lane;
+  const int n = T.n, nlu = T.nnz_lu;
+  auto LU = [&](int s) -> double2 & { return base[(size_t)s * 32]; };
+  auto RD = [&](int i) -> double2 & { return base[(size_t)(nlu + i) * 32]; };
+  auto V = [&](int i) -> double2 & { return base[(size_t)(nlu + n + i) * 32]; };
+  auto RHS = [&](int i) -> double2 & { return base[(size_t)(nlu + 2 * n + i) * 32]; };
+  const int n_lu = T.lu_lvl[T.lu_nlev];
+  for (long long f0 = wid * 32; f0 < a.n_freq; f0 += a.n_warps * 32) {
+    const long long f = f0 + lane;
+    const bool on = f < a.n_freq;
+    const double w = a.omega[on ? f : f0];
+    for (int s = 0; s < nlu; ++s) LU(s) = slot_val(a, s, w);
+    bool bad = false;
+    for (int t = 0; t < n_lu; ++t) {                   // level order: a level's tasks are independent
+      const int4 tk = T.lu_task[t];
+      double2 acc = LU(tk.x);
+      for (int p = tk.z; p < tk.w; ++p) { const int2 pr = T.lu_pair[p]; acc = c_fms(acc, LU(pr.x), LU(pr.y)); }
+      const int kind = tk.y & 3, j = tk.y >> 2;
+      if (kind == 2) acc = c_mul(acc, RD(j));
+      else if (kind == 1) {
+        const double m = fmax(fabs(acc.x), fabs(acc.y));
+        if (!(m > 1e-300) || !(m < 1e300)) bad = true;
+        RD(j) = c_rcp(acc);
+      }
+      LU(tk.x) = acc;
+    }
+    if (!NOISE) {
+      for (int e = 0; e < n; ++e) { const double2 b = make_double2(a.b[e], 0.0); V(T.eq_pos[e]) = b; RHS(T.eq_pos[e]) = b; }
+      const int n_fw = T.fw_lvl[T.fw_nlev], n_bw = T.bw_lvl[T.bw_nlev];
+      for (int t = 0; t < n_fw; ++t) {                 // L y = b (unit diagonal)
+        const int4 tk = T.fw_task[t];
+        double2 acc = V(tk.x);
+        for (int p = tk.y; p < tk.z; ++p) { const int2 pr = T.fw_pair[p]; acc = c_fms(acc, LU(pr.x), V(pr.y)); }
+        V(tk.x) = acc;
+      }
+      for (int t = 0; t < n_bw; ++t) {                 // U x = y
+        const int4 tk = T.bw_task[t];
+        double2 acc = V(tk.x);
+        for (int p = tk.y; p < tk.z; ++p) { const int2 pr = T.bw_pair[p]; acc = c_fms(acc, LU(pr.x), V(pr.y)); }
+        V(tk.x) = c_mul(acc, RD(tk.x));
+      }
+    } else {
+      const int c = T.iorder[a.probe[0]];
+      for (int u = 0; u < n; ++u) { const double2 e = make_double2(u == c ? 1.0 : 0.0, 0.0); V(u) = e; RHS(u) = e; }
+      const int n_tf = T.tf_lvl[T.tf_nlev], n_tb = T.tb_lvl[T.tb_nlev];
+      for (int t = 0; t < n_tf; ++t) {                 // U^T z = e_probe
+        const int4 tk = T.tf_task[t];
+        double2 acc = V(tk.x);
+        for (int p = tk.y; p < tk.z; ++p) { const int2 pr = T.tf_pair[p]; acc = c_fms(acc, LU(pr.x), V(pr.y)); }
+        V(tk.x) = c_mul(acc, RD(tk.x));
+      }
+      for (int t = 0; t < n_tb; ++t) {                 // L^T y = z (unit diagonal)
+        const int4 tk = T.tb_task[t];
+        double2 acc = V(tk.x);
+        for (int p = tk.y; p < tk.z; ++p) { const int2 pr = T.tb_pair[p]; acc = c_fms(acc, LU(pr.x), V(pr.y)); }
+        V(tk.x) = acc;
+      }
+    }
+    // backward error of the solve (the norms of ac_solve_suspect, taken by one lane)
+    double rmax = 0.0, amax = 0.0, xmax = 0.0, bmax = 0.0;
+    bool nonfinite = false;
+    for (int i = 0; i < n; ++i) {
+      double2 r = RHS(i);
+      double arow = 0.0;
+      if (!NOISE) {
+        for (int s = T.lu_rowptr[i]; s < T.lu_rowptr[i + 1]; ++s) {
+          const double2 m = slot_val(a, s, w);
+          r = c_fms(r, m, V(T.lu_colidx[s]));
+          arow += c_abs1(m);
+        }
+      } else {
+        for (int k = T.lu_cptr[i]; k < T.lu_cptr[i + 1]; ++k) {
+          const int s = T.lu_cslot[k];
+          const double2 m = slot_val(a, s, w);
+          r = c_fms(r, m, V(T.lu_srow[s]));
+          arow += c_abs1(m);
+        }
+      }
+      const double ra = c_abs1(r), xa = c_abs1(V(i));
+      if (!(ra <= 1e300) || !(xa <= 1e300)) nonfinite = true;
+      rmax = fmax(rmax, ra); amax = fmax(amax, arow); xmax = fmax(xmax, xa); bmax = fmax(bmax, c_abs1(RHS(i)));
+    }
+    if (!bad) bad = nonfinite || rmax > kAcResidTol * (amax * xmax + bmax);
+    if (on) {
+      if (!bad) {
+        if (!NOISE) {
+          double2 *out = reinterpret_cast<double2 *>(a.resp) + f * a.n_probe;
+          for (int k = 0; k < a.n_probe; ++k) out[k] = V(T.iorder[a.probe[k]]);
+        } else {
+          double acc = 0.0;
+          for (int r = 0; r < a.n_noise; ++r) {
+            const int na = a.noise_a[r], nb = a.noise_b[r];
+            const double2 ya = na < 0 ? make_double2(0.0, 0.0) : V(T.eq_pos[na]);
+            const double2 yb = nb < 0 ? make_double2(0.0, 0.0) : V(T.eq_pos[nb]);
+            const double hr = ya.x - yb.x, hi = ya.y - yb.y;
+            double wr = a.noise_w[r];
+            if (a.noise_e) {
+              const double e = a.noise_e[r];
+              if (e != 0.0) wr /= pow(w / 6.283185307179586, e);
+            }
+            acc += wr * (hr * hr + hi * hi);
+          }
+          a.psd[f] = acc;
+        }
+      } else {
+        ac_write_nan<NOISE>(a, f);
+        atomicAdd(a.n_dense, 1);
+      }
+      a.status[f] = bad ? kAcDense : CEDAR_ST_OK;
+    }
+  }
+}
+
 // Dense rerun of the frequencies marked kAcDense: LU with partial pivoting (row
 // interchanges of whole rows, pivot = largest ν in the column, lowest row on a
 // tie), one warp per frequency; P M = L U.
@@ -347,8 +480,13 @@ constexpr int kAcWarpsPerCta = 4;
 cudaError_t launch_ac(const AcDev &a, bool noise, cudaStream_t s) {
   if (a.n_freq <= 0 || a.n_warps <= 0) return cudaSuccess;
   const long long grid = (a.n_warps + kAcWarpsPerCta - 1) / kAcWarpsPerCta;
-  if (noise) ac_kernel<true><<<(unsigned)grid, 32 * kAcWarpsPerCta, 0, s>>>(a);
-  else ac_kernel<false><<<(unsigned)grid, 32 * kAcWarpsPerCta, 0, s>>>(a);
+  if (a.lane_mode) {
+    if (noise) ac_lane_kernel<true><<<(unsigned)grid, 32 * kAcWarpsPerCta, 0, s>>>(a);
+    else ac_lane_kernel<false><<<(unsigned)grid, 32 * kAcWarpsPerCta, 0, s>>>(a);
+  } else {
+    if (noise) ac_kernel<true><<<(unsigned)grid, 32 * kAcWarpsPerCta, 0, s>>>(a);
+    else ac_kernel<false><<<(unsigned)grid, 32 * kAcWarpsPerCta, 0, s>>>(a);
+  }
   return cudaGetLastError();
 }
 

@@ -134,6 +134,7 @@ struct AcDev {
   int *n_dense;                       // frequencies handed to the dense rerun
   double2 *dws; long long dws_stride; // dense rerun, per warp: A [n * n], rhs [n]
   int *dpiv; long long n_dwarps;      // per warp: row interchanges [n]; warps of the dense rerun
+  int lane_mode;                      // 1: one lane per frequency, ws interleaved by lane (ws_stride per lane)
 };
 constexpr int kAcDense = -1;          // status of a frequency waiting for the dense rerun
 constexpr int kAcDenseNmax = 256;     // largest system the dense rerun takes
