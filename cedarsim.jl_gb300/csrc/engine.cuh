@@ -253,7 +253,6 @@ __device__ __forceinline__ bool finite_big(double a) { return abs_bits(a) < 0x7e
 
 // ------------------------------------------------------------- thread group (one CTA)
 struct BlockGroup {
-  static constexpr bool kOneBlock = true;   // the group is one CTA (first warp = threads 0..31)
   int rank, size;
   double *red;  // shared scratch of >= 96 doubles
   __device__ BlockGroup(double *r) : rank(threadIdx.x), size(blockDim.x), red(r) {}
@@ -329,7 +328,6 @@ struct Engine {
 
   __device__ Engine(const DTpl &t, const double *dpar, double *ws, G grp) : T(t), dp(dpar), g(grp) {
     w.bind(ws, T.n, T.nnz_lu, T.n_out, T.n_src);
-    choose_level_mode();
   }
 
   // Dense LU with partial pivoting (first maximum of a column wins; whole rows
@@ -448,65 +446,23 @@ struct Engine {
     g.sync();
   }
 
-  // K4: level-scheduled Crout LU in place; returns false on a zero pivot.
-  // Tasks [t0, t1) of a level on threads (rank, size); the same arithmetic
-  // whichever threads run it.
-  __device__ void lu_level(int t0, int t1, int rank, int size, bool &bad) {
-    for (int t = t0 + rank; t < t1; t += size) {
-      int s = T.lu_slot[t], info = T.lu_info[t];
-      double acc = w.lu[s];
-      for (int k = T.lu_pp[t]; k < T.lu_pp[t + 1]; ++k) { int2 p = T.lu_pair[k]; acc -= w.lu[p.x] * w.lu[p.y]; }
-      int kind = info & 3, j = info >> 2;
-      if (kind == 2) acc *= w.rd[j];
-      else if (kind == 1) {
-        if (!(fabs(acc) > 1e-300) || !(fabs(acc) < 1e300)) bad = true;
-        w.rd[j] = 1.0 / acc;
-      }
-      w.lu[s] = acc;
-    }
-  }
-  __device__ void fw_level(double *b, int l, int rank, int size) {
-    for (int t = T.fw_lvl[l] + rank; t < T.fw_lvl[l + 1]; t += size) {
-      int i = T.fw_row[t]; double acc = b[i];
-      for (int k = T.fw_ptr[t]; k < T.fw_ptr[t + 1]; ++k) { int2 p = T.fw_pair[k]; acc -= w.lu[p.x] * b[p.y]; }
-      b[i] = acc;
-    }
-  }
-  __device__ void bw_level(double *b, int l, int rank, int size) {
-    for (int t = T.bw_lvl[l] + rank; t < T.bw_lvl[l + 1]; t += size) {
-      int i = T.bw_row[t]; double acc = b[i];
-      for (int k = T.bw_ptr[t]; k < T.bw_ptr[t + 1]; ++k) { int2 p = T.bw_pair[k]; acc -= w.lu[p.x] * b[p.y]; }
-      b[i] = acc * w.rd[i];
-    }
-  }
-
-  // When every level of the LU and of both substitutions is narrow, one CTA runs
-  // them on its first warp alone, with warp barriers between levels instead of
-  // CTA barriers (the other warps wait at the CTA barrier that ends the phase).
-  static constexpr int kWarpLevelMax = 96;
-  bool warp_levels = false;
-  __device__ void choose_level_mode() {
-    if constexpr (!G::kOneBlock) return;
-    int mx = 0;
-    for (int l = 0; l < T.lu_nlev; ++l) mx = max(mx, T.lu_lvl[l + 1] - T.lu_lvl[l]);
-    for (int l = 0; l < T.fw_nlev; ++l) mx = max(mx, T.fw_lvl[l + 1] - T.fw_lvl[l]);
-    for (int l = 0; l < T.bw_nlev; ++l) mx = max(mx, T.bw_lvl[l + 1] - T.bw_lvl[l]);
-    warp_levels = mx <= kWarpLevelMax;
-  }
-
+  // K4: level-scheduled Crout LU in place; returns false on a zero pivot
   __device__ bool factor() {
     bool bad = false;
-    if (G::kOneBlock && warp_levels) {
-      if (threadIdx.x < 32) {
-        for (int l = 0; l < T.lu_nlev; ++l) {
-          lu_level(T.lu_lvl[l], T.lu_lvl[l + 1], threadIdx.x, 32, bad);
-          __syncwarp();
-        }
-      }
-      return !g.any(bad);
-    }
     for (int l = 0; l < T.lu_nlev; ++l) {
-      lu_level(T.lu_lvl[l], T.lu_lvl[l + 1], g.rank, g.size, bad);
+      int t0 = T.lu_lvl[l], t1 = T.lu_lvl[l + 1];
+      for (int t = t0 + g.rank; t < t1; t += g.size) {
+        int s = T.lu_slot[t], info = T.lu_info[t];
+        double acc = w.lu[s];
+        for (int k = T.lu_pp[t]; k < T.lu_pp[t + 1]; ++k) { int2 p = T.lu_pair[k]; acc -= w.lu[p.x] * w.lu[p.y]; }
+        int kind = info & 3, j = info >> 2;
+        if (kind == 2) acc *= w.rd[j];
+        else if (kind == 1) {
+          if (!(fabs(acc) > 1e-300) || !(fabs(acc) < 1e300)) bad = true;
+          w.rd[j] = 1.0 / acc;
+        }
+        w.lu[s] = acc;
+      }
       g.sync();
     }
     return !g.any(bad);
@@ -514,16 +470,22 @@ struct Engine {
 
   // K5: solve LU y = b in place (b = F)
   __device__ void solve(double *b) {
-    if (G::kOneBlock && warp_levels) {
-      if (threadIdx.x < 32) {
-        for (int l = 0; l < T.fw_nlev; ++l) { fw_level(b, l, threadIdx.x, 32); __syncwarp(); }
-        for (int l = 0; l < T.bw_nlev; ++l) { bw_level(b, l, threadIdx.x, 32); __syncwarp(); }
+    for (int l = 0; l < T.fw_nlev; ++l) {
+      for (int t = T.fw_lvl[l] + g.rank; t < T.fw_lvl[l + 1]; t += g.size) {
+        int i = T.fw_row[t]; double acc = b[i];
+        for (int k = T.fw_ptr[t]; k < T.fw_ptr[t + 1]; ++k) { int2 p = T.fw_pair[k]; acc -= w.lu[p.x] * b[p.y]; }
+        b[i] = acc;
       }
       g.sync();
-      return;
     }
-    for (int l = 0; l < T.fw_nlev; ++l) { fw_level(b, l, g.rank, g.size); g.sync(); }
-    for (int l = 0; l < T.bw_nlev; ++l) { bw_level(b, l, g.rank, g.size); g.sync(); }
+    for (int l = 0; l < T.bw_nlev; ++l) {
+      for (int t = T.bw_lvl[l] + g.rank; t < T.bw_lvl[l + 1]; t += g.size) {
+        int i = T.bw_row[t]; double acc = b[i];
+        for (int k = T.bw_ptr[t]; k < T.bw_ptr[t + 1]; ++k) { int2 p = T.bw_pair[k]; acc -= w.lu[p.x] * b[p.y]; }
+        b[i] = acc * w.rd[i];
+      }
+      g.sync();
+    }
   }
 
   // Newton on Fi(x,t) + cj Fq(x) + hist = 0.  Returns iterations (>0), -iters on

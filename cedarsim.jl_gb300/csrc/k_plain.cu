@@ -248,7 +248,6 @@ cudaError_t launch_fp64_probe(int active_lanes, int iters, double *gflops, doubl
 // Two scratch buffers alternate: a block that moves on to the next reduction
 // writes the other buffer while slower blocks still read this one.
 struct GridGroup {
-  static constexpr bool kOneBlock = false;
   int rank, size;
   double *red;            // shared scratch (>= 96 doubles)
   double *gred;           // global scratch: 2 buffers of 3 doubles per block
