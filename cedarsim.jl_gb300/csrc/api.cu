@@ -16,7 +16,7 @@ using namespace cedar;
 
 static_assert(sizeof(EngStats) == sizeof(cedar_stats), "stats layout");
 static_assert(kLongGatherHost == kLongGather && kLongEvalHost == kLongEval, "long gather thresholds");
-static_assert(kLongChunk == 64, "cedar_eval long-list chunk (k_plain.cu kLongChunkDev)");
+static_assert(kLongChunk == 256, "cedar_eval long-list chunk (k_plain.cu kLongChunkDev)");
 
 namespace {
 

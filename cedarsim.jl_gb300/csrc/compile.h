@@ -100,8 +100,8 @@ struct Template {
 // Gather lists longer than these are summed cooperatively on the device (must
 // equal kLongGather / kLongEval of engine.cuh).
 constexpr int kLongGatherHost = 16, kLongEvalHost = 64;
-// cedar_eval sums a long list in chunks of this many entries (one thread each)
-constexpr int kLongChunk = 64;
+// cedar_eval sums a long list in chunks of this many entries (one warp each)
+constexpr int kLongChunk = 256;
 
 // Ordering strategies for the fill-reducing symmetric permutation.
 enum Ordering { ORDER_AUTO = 0, ORDER_MIN_DEGREE = 1, ORDER_NESTED_DISSECTION = 2, ORDER_NATURAL = 3 };

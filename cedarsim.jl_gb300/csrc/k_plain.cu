@@ -74,12 +74,17 @@ __global__ void stamp_kernel(DTpl T, const double *dout, double *F, double *J) {
   }
 }
 
-// Long lists (supply rails), pass 1: one thread per fixed chunk of kLongChunk
-// entries, summed in order into part[] (chunk p of list i at long_off[i] + p).
-constexpr int kLongChunkDev = 64;
+// Long lists (supply rails), pass 1: one warp per fixed chunk of kLongChunkDev
+// entries (chunk p of list i at long_off[i] + p).  Lane j sums the chunk's
+// entries j, j + 32, ... in order (the warp's index loads are coalesced), then a
+// fixed xor-butterfly over the 32 lane sums gives the chunk sum; a + b and b + a
+// round alike, so every lane holds the same bits.
+constexpr int kLongChunkDev = 256;
+constexpr int kLongLaneLoads = kLongChunkDev / 32;
 __global__ void stamp_long_part_kernel(DTpl T, const double *dout, double *part) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= T.n_long_part) return;
+  const int p = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (p >= T.n_long_part) return;           // warp-uniform
   const int nl = T.n_long_jc + T.n_long_fo;
   int lo = 0, hi = nl;                       // list i with long_off[i] <= p < long_off[i + 1]
   while (hi - lo > 1) { const int mid = (lo + hi) >> 1; if (T.long_off[mid] <= p) lo = mid; else hi = mid; }
@@ -88,53 +93,50 @@ __global__ void stamp_long_part_kernel(DTpl T, const double *dout, double *part)
   const int *ptr = is_j ? T.jcsc_ptr : T.forg_ptr, *ent = is_j ? T.jcsc_ent : T.forg_ent;
   const int k0 = ptr[q] + (p - T.long_off[lo]) * kLongChunkDev;
   const int k1 = min(k0 + kLongChunkDev, ptr[q + 1]);
-  // the chunk's entries in order; loads are issued 8 at a time ahead of the adds
-  // (the add chain and its order are unchanged)
+  // all of the lane's loads are issued ahead of its in-order adds
+  int e[kLongLaneLoads]; double v[kLongLaneLoads];
+#pragma unroll
+  for (int j = 0; j < kLongLaneLoads; ++j) { const int k = k0 + lane + 32 * j; e[j] = k < k1 ? __ldg(ent + k) : -1; }
+#pragma unroll
+  for (int j = 0; j < kLongLaneLoads; ++j) v[j] = e[j] >= 0 ? __ldg(dout + (e[j] >> 1)) : 0.0;
   double acc = 0.0;
-  int k = k0;
-  for (; k + 8 <= k1; k += 8) {
-    int e[8]; double v[8];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) e[j] = __ldg(ent + k + j);
+  for (int j = 0; j < kLongLaneLoads; ++j) if (e[j] >= 0) acc = acc + signed_out(v[j], e[j]);
 #pragma unroll
-    for (int j = 0; j < 8; ++j) v[j] = __ldg(dout + (e[j] >> 1));
-#pragma unroll
-    for (int j = 0; j < 8; ++j) acc = acc + signed_out(v[j], e[j]);
-  }
-  for (; k < k1; ++k) { const int e = __ldg(ent + k); acc = acc + signed_out(__ldg(dout + (e >> 1)), e); }
-  part[p] = acc;
+  for (int o = 16; o > 0; o >>= 1) acc = acc + __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) part[p] = acc;
 }
 
-// Pass 2: one CTA per long list; thread t sums its contiguous share of the
-// list's chunk sums in order, then a fixed pairwise tree over the threads.
+// Pass 2: one CTA per long list; thread t sums the list's chunk sums t, t + 256,
+// ... in order (coalesced), then a fixed xor-butterfly per warp and a fixed
+// pairwise tree over the 8 warp sums.
 constexpr int kLongThreads = 256;
+static_assert(kLongThreads == 256, "the final tree combines 8 warp sums");
 __global__ void __launch_bounds__(kLongThreads) stamp_long_final_kernel(DTpl T, const double *part, double *F, double *J) {
-  __shared__ double red[kLongThreads];
+  __shared__ double red[kLongThreads / 32];
   const int i = blockIdx.x;
   const bool is_j = i < T.n_long_jc;
   const int q = is_j ? T.long_jc[i] : T.long_fo[i - T.n_long_jc];
-  const int p0 = T.long_off[i], np = T.long_off[i + 1] - p0;
-  const int a = p0 + (int)(((long long)np * threadIdx.x) / kLongThreads);
-  const int b = p0 + (int)(((long long)np * (threadIdx.x + 1)) / kLongThreads);
+  const int p0 = T.long_off[i], p1 = T.long_off[i + 1];
   double acc = 0.0;
-  int k = a;
-  for (; k + 8 <= b; k += 8) {             // loads ahead of the in-order adds
+  int k = p0 + threadIdx.x;
+  for (; k + 7 * kLongThreads < p1; k += 8 * kLongThreads) {   // loads ahead of the in-order adds
     double v[8];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) v[j] = part[k + j];
+    for (int j = 0; j < 8; ++j) v[j] = part[k + j * kLongThreads];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) acc += v[j];
+    for (int j = 0; j < 8; ++j) acc = acc + v[j];
   }
-  for (; k < b; ++k) acc += part[k];
-  red[threadIdx.x] = acc;
+  for (; k < p1; k += kLongThreads) acc = acc + part[k];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc = acc + __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
   __syncthreads();
-  for (int w = 1; w < kLongThreads; w <<= 1) {
-    if ((threadIdx.x & (2 * w - 1)) == 0) red[threadIdx.x] = red[threadIdx.x] + red[threadIdx.x + w];
-    __syncthreads();
-  }
   if (threadIdx.x == 0) {
-    if (is_j) { if (J) J[q] = red[0]; }
-    else if (F) F[q] = red[0];
+    const double s01 = red[0] + red[1], s23 = red[2] + red[3], s45 = red[4] + red[5], s67 = red[6] + red[7];
+    const double r = (s01 + s23) + (s45 + s67);
+    if (is_j) { if (J) J[q] = r; }
+    else if (F) F[q] = r;
   }
 }
 
@@ -147,7 +149,8 @@ cudaError_t launch_eval(const DTpl &T, const DTpl *T_dev, const double *dpar, co
   stamp_kernel<<<(m + th - 1) / th, th, 0, s>>>(T, dout, F, J);
   const int nlong = T.n_long_jc + T.n_long_fo;
   if (nlong > 0) {
-    stamp_long_part_kernel<<<(T.n_long_part + th - 1) / th, th, 0, s>>>(T, dout, part);
+    const int warps = th / 32;
+    stamp_long_part_kernel<<<(T.n_long_part + warps - 1) / warps, th, 0, s>>>(T, dout, part);
     stamp_long_final_kernel<<<nlong, kLongThreads, 0, s>>>(T, part, F, J);
   }
   return cudaGetLastError();

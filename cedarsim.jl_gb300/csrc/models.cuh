@@ -179,6 +179,66 @@ CEDAR_HD void mos1_fwd(double vgs, double vds, double vth, double beta, double l
   gds = off ? zero : d;
 }
 
+// Sign and unit tests and the sign flip, on the bit patterns on the device (the
+// integer pipe, not the FP64 pipe).  x * s for s = +1 or -1 is exact in IEEE
+// arithmetic, so neg_if(x, s < 0) has the bits of the product.
+CEDAR_HD double neg_if(double x, bool neg) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double(__double_as_longlong(x) ^ (long long)((unsigned long long)neg << 63));
+#else
+  return neg ? -x : x;
+#endif
+}
+CEDAR_HD bool is_unit(double a) {  // a is exactly +1 or -1
+#ifdef __CUDA_ARCH__
+  return (__double_as_longlong(a) & 0x7fffffffffffffffLL) == 0x3ff0000000000000LL;
+#else
+  return a == 1.0 || a == -1.0;
+#endif
+}
+CEDAR_HD bool sign_set(double a) {
+#ifdef __CUDA_ARCH__
+  return __double_as_longlong(a) < 0;
+#else
+  return a < 0;
+#endif
+}
+CEDAR_HD bool is_one(double a) {
+#ifdef __CUDA_ARCH__
+  return __double_as_longlong(a) == 0x3ff0000000000000LL;
+#else
+  return a == 1.0;
+#endif
+}
+
+// Level-1 MOSFET terminal current and partials (outputs: Ids, dIds/dVg,
+// dIds/dVd + gmin, -dIds/dVs + gmin, each times m).  gsum = gm + gds is formed
+// without cancellation in reverse mode; the source/drain exchange for vds < 0 is
+// a selection (no divergent branch).  UNIT: type is +-1 and m is 1 (the usual
+// case), so the products by type are sign flips and those by m are left out;
+// both are exact, so the outputs have the bits of the general form.
+template <bool UNIT>
+CEDAR_HD void mos1_device(double type, double beta, double vth, double lam, double m, const double *v, double gmin,
+                          double *out) {
+  const bool pt = UNIT && sign_set(type);
+  auto tm = [&](double x) -> double {
+    if constexpr (UNIT) return neg_if(x, pt);
+    else return type * x;
+  };
+  auto mm = [&](double x) -> double {
+    if constexpr (UNIT) return x;
+    else return m * x;
+  };
+  const double vgs = tm(v[1] - v[2]), vds = tm(v[0] - v[2]);
+  const bool fwd = vds >= 0;
+  double i1, g1, g2;
+  mos1_fwd(fwd ? vgs : vgs - vds, fwd ? vds : -vds, vth, beta, lam, i1, g1, g2);
+  const double s12 = g1 + g2;
+  const double id = fwd ? i1 : -i1, gm = fwd ? g1 : -g1, gds = fwd ? g2 : s12, gsum = fwd ? s12 : g2;
+  const double ids = fma(gmin, v[0] - v[2], tm(id));
+  out[0] = mm(ids); out[1] = mm(gm); out[2] = mm(gds + gmin); out[3] = mm(gsum + gmin);
+}
+
 // The source waveform out of line: the batched engines take time-varying sources'
 // values from a per-solve cache, so the waveform code on the Newton iteration's
 // path only serves constant sources; a call keeps its code out of the hot loop.
@@ -234,18 +294,9 @@ CEDAR_HD void eval_device(int model, const double *dp, int ds, const double *v, 
       out[0] = mg * (v[2] - v[3]); out[1] = mg;
     } break;
     case CEDAR_MOS1: {
-      double type = dp[0], beta = dp[ds], vth = dp[2 * ds], lam = dp[3 * ds], m = dp[4 * ds];
-      double vgs = type * (v[1] - v[2]), vds = type * (v[0] - v[2]);
-      // gsum = -dIds/dVs - gmin = gm + gds, formed without cancellation in reverse mode
-      // source/drain exchange for vds < 0, by selection (no divergent branch)
-      const bool fwd = vds >= 0;
-      double i1, g1, g2;
-      mos1_fwd(fwd ? vgs : vgs - vds, fwd ? vds : -vds, vth, beta, lam, i1, g1, g2);
-      const double s12 = g1 + g2;
-      const double id = fwd ? i1 : -i1, gm = fwd ? g1 : -g1, gds = fwd ? g2 : s12, gsum = fwd ? s12 : g2;
-      double gmin = ctx.gmin;
-      double ids = type * id + gmin * (v[0] - v[2]);
-      out[0] = m * ids; out[1] = m * gm; out[2] = m * (gds + gmin); out[3] = m * (gsum + gmin);
+      const double type = dp[0], beta = dp[ds], vth = dp[2 * ds], lam = dp[3 * ds], m = dp[4 * ds];
+      if (is_unit(type) && is_one(m)) mos1_device<true>(type, beta, vth, lam, m, v, ctx.gmin, out);
+      else mos1_device<false>(type, beta, vth, lam, m, v, ctx.gmin, out);
     } break;
     case CEDAR_DIODE: {
       double isat = dp[0], invnvt = dp[ds], m = dp[2 * ds];

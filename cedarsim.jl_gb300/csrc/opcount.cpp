@@ -84,6 +84,7 @@ static inline Cnt atan2(Cnt a, Cnt b) { return op1(std::atan2(a.v, b.v)); }
 static inline Cnt hypot(Cnt a, Cnt b) { return op1(std::hypot(a.v, b.v)); }
 static inline Cnt fmin(Cnt a, Cnt b) { return Cnt(std::fmin(a.v, b.v)); }
 static inline Cnt fmax(Cnt a, Cnt b) { return Cnt(std::fmax(a.v, b.v)); }
+static inline Cnt fma(Cnt a, Cnt b, Cnt c) { g_ops += 2; return Cnt(std::fma(a.v, b.v, c.v)); }
 static inline bool isfinite(Cnt a) { return std::isfinite(a.v); }
 static inline bool isnan(Cnt a) { return std::isnan(a.v); }
 static inline long long llround(Cnt a) { return std::llround(a.v); }
