@@ -215,6 +215,15 @@ def reference_adjoint(args, pkg, orc):
             "seconds": dt, "failed": k - ok}
 
 
+def fp64_latency(pkg, lib, C):
+    """Latency of one dependent FP64 operation on this GPU (cedar_fp64_latency):
+    the unit of a single circuit's critical path through LU and substitutions."""
+    cyc, ns = C.c_double(), C.c_double()
+    pkg.abi.check(lib.cedar_fp64_latency(1 << 16, C.byref(cyc), C.byref(ns)))
+    return {"cycles_per_dependent_dfma": cyc.value, "ns_per_dependent_dfma": ns.value,
+            "note": "one warp, a chain of 524288 dependent DFMAs (SM clock; events incl. launch)"}
+
+
 def measure_eval(pkg, args, torch, C, fp64_peak=None):
     """cedar_eval_dev (device evaluation + CSC stamping, the drop-in residual /
     Jacobian boundary) on one large chain: inputs resident in HBM and larger than
@@ -575,12 +584,13 @@ def main():
             gf, ms = C.c_double(), C.c_double()
             pkg.abi.check(lib0.cedar_fp64_probe(lanes, 4096, C.byref(gf), C.byref(ms)))
             out[str(lanes)] = {"useful_gflops": gf.value, "ms": ms.value}
-        print(json.dumps({"fp64_probe": out}), flush=True)
+        print(json.dumps({"fp64_probe": out, "fp64_latency": fp64_latency(pkg, lib0, C)}), flush=True)
         return
     # FP64 peak measured live on this GPU (all lanes active): the roofline denominator
     gf = C.c_double()
     pkg.abi.check(lib0.cedar_fp64_probe(32, 4096, C.byref(gf), None))
     fp64_peak = gf.value / 1e3
+    fp64_lat = fp64_latency(pkg, lib0, C)
     templates, itpl, par, off, probes = workload(pkg, args.n_inst, args.seed)
     mine = shard(itpl, templates, rank, world)
     n_samples = 201
@@ -771,7 +781,7 @@ def main():
         "cpu_baseline": cpu, "e2e": e2e, "plain_gpu": plain, "adjoint": adj, "eval_hbm": eval_leg, "rings": rings,
         "ac": ac_leg, "verilog_a": va_leg, "config1": plain_cfg and plain_cfg["config1"],
         "config2": plain_cfg and plain_cfg["config2"], "config2_verilog_a": plain_cfg and plain_cfg["config2_verilog_a"],
-        "clocks": clk, "gpu_launches": args.steps,
+        "fp64_latency": fp64_lat, "clocks": clk, "gpu_launches": args.steps,
     }
     print(json.dumps(line), flush=True)
 

@@ -164,7 +164,7 @@ EXPORTS = [
     "cedar_batch_results", "cedar_batch_last_ms", "cedar_batch_set_tuning",
     "cedar_batch_get_tuning", "cedar_batch_autotune", "cedar_batch_nmax",
     "cedar_adjoint_run", "cedar_adjoint_nparams", "cedar_adjoint_tape", "cedar_adjoint_last_ms",
-    "cedar_fp64_probe", "cedar_ckt_stream", "cedar_batch_dcop", "cedar_ac", "cedar_noise",
+    "cedar_fp64_probe", "cedar_fp64_latency", "cedar_ckt_stream", "cedar_batch_dcop", "cedar_ac", "cedar_noise",
     "cedar_ac_last_stats", "cedar_va_count", "cedar_va_name",
 ]
 
@@ -225,6 +225,7 @@ def load_library(build_if_missing: bool = True):
         "cedar_adjoint_tape": (C.c_int, [P, C.c_int32, c_double_p, P, C.c_int64, c_int64_p]),
         "cedar_adjoint_last_ms": (C.c_int, [P, c_double_p, c_double_p]),
         "cedar_fp64_probe": (C.c_int, [C.c_int32, C.c_int32, c_double_p, c_double_p]),
+        "cedar_fp64_latency": (C.c_int, [C.c_int32, c_double_p, c_double_p]),
         "cedar_ckt_stream": (C.c_int, [P, C.POINTER(P)]),
         "cedar_batch_dcop": (C.c_int, [P, C.POINTER(TranOpts), c_double_p, P]),
         "cedar_ac": (C.c_int, [P, c_double_p, c_double_p, C.c_int32, c_double_p, C.c_int32, c_int32_p, c_double_p,

@@ -1314,6 +1314,12 @@ int cedar_fp64_probe(int32_t active_lanes, int32_t iters, double *gflops, double
   return 0;
 }
 
+int cedar_fp64_latency(int32_t iters, double *cycles_per_op, double *ns_per_op) {
+  if (iters < 1) return fail(CEDAR_EINVAL, "iters >= 1");
+  CUDA_TRY(launch_fp64_latency(iters, cycles_per_op, ns_per_op));
+  return 0;
+}
+
 int cedar_batch_autotune(cedar_batch *b, const cedar_tran_opts *opts, double horizon, cedar_batch_tuning *best) {
   if (!b) return fail(CEDAR_EINVAL, "null handle");
   int rc = check_opts(opts); if (rc) return rc;

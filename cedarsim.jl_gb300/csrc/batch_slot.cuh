@@ -146,7 +146,7 @@ struct Slot {
       const int *tm = TT.term + gr.term_off + i * gr.ntx;
       double v[CEDAR_MAX_TERM];
       for (int kk = 0; kk < gr.ntx; ++kk) { int u = tm[kk]; v[kk] = u < 0 ? 0.0 : x[u]; }
-      eval_device<false>(gr.model, dp + gr.dpar_off + i, gr.n_inst, v, nullptr, ctx, TT.pwl, w.dout + gr.out_off + i * model_nout(gr.model));
+      eval_device<false>(gr.model, dp + gr.dpar_off + i, gr.n_inst, v, nullptr, ctx, TT.pwl, w.dout + gr.out_off + i, gr.n_inst);
     });
     ssync();
     for (int r = rank(); r < TT.n; r += K) q[r] = gather(TT.qint_ptr, TT.qint_ent, r, 0.0);
@@ -750,10 +750,10 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am, const 
       const int *tm = T.term + gr.term_off + i * gr.ntx;
       double v[CEDAR_MAX_TERM];
       for (int kk = 0; kk < gr.ntx; ++kk) { int u = tm[kk]; v[kk] = u < 0 ? 0.0 : x[u]; }
-      double *out = dout + gr.out_off + i * model_nout(gr.model);
+      double *out = dout + gr.out_off + i;
       const int si = (gr.model == CEDAR_V || gr.model == CEDAR_I) ? T.src_of_dev[d] : -1;
-      if (si >= 0) eval_source_value(gr.model, dp + gr.dpar_off + i, v, srcv[si], out);
-      else eval_device<false>(gr.model, dp + gr.dpar_off + i, gr.n_inst, v, nullptr, ctx, T.pwl, out);
+      if (si >= 0) eval_source_value(gr.model, dp + gr.dpar_off + i, v, srcv[si], out, gr.n_inst);
+      else eval_device<false>(gr.model, dp + gr.dpar_off + i, gr.n_inst, v, nullptr, ctx, T.pwl, out, gr.n_inst);
     });
   }
   __syncwarp(am);

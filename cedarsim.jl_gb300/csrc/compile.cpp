@@ -58,11 +58,11 @@ const ModelInfo &model_info(int model) {
 
 int num_models() { return CEDAR_NMODELS + va::kCount; }
 
-void device_stamps(int model, const int *t, int ob, std::vector<Stamp> &J, std::vector<Stamp> &F,
+void device_stamps(int model, const int *t, int ob, int os, std::vector<Stamp> &J, std::vector<Stamp> &F,
                    std::vector<Stamp> &Q) {
-  auto j = [&](int r, int c, int o, int neg) { if (r >= 0 && c >= 0) J.push_back({r, c, ob + o, neg}); };
-  auto f = [&](int r, int o, int neg) { if (r >= 0) F.push_back({r, -1, ob + o, neg}); };
-  auto q = [&](int r, int o, int neg) { if (r >= 0) Q.push_back({r, -1, ob + o, neg}); };
+  auto j = [&](int r, int c, int o, int neg) { if (r >= 0 && c >= 0) J.push_back({r, c, ob + o * os, neg}); };
+  auto f = [&](int r, int o, int neg) { if (r >= 0) F.push_back({r, -1, ob + o * os, neg}); };
+  auto q = [&](int r, int o, int neg) { if (r >= 0) Q.push_back({r, -1, ob + o * os, neg}); };
   switch (model) {
     case CEDAR_R: case CEDAR_DIODE:
       f(t[0], 0, 1); f(t[1], 0, 0);
@@ -354,7 +354,7 @@ static bool compile_with(const cedar_ckt_desc *d, Template &T, std::string &err,
   for (const GroupInfo &g : T.groups) {
     const int no = model_info(g.model).nout;
     for (int i = 0; i < g.n_inst; ++i)
-      for (int k = 0; k < no; ++k) T.out_q[g.out_off + i * no + k] = is_charge_partial(g.model, k) ? 1 : 0;
+      for (int k = 0; k < no; ++k) T.out_q[g.out_off + k * g.n_inst + i] = is_charge_partial(g.model, k) ? 1 : 0;
   }
 
   // stamps in device order; SJq marks J stamps carrying a charge partial (cj dQ/dV)
@@ -364,10 +364,11 @@ static bool compile_with(const cedar_ckt_desc *d, Template &T, std::string &err,
   for (const GroupInfo &g : T.groups) {
     const ModelInfo &mi = model_info(g.model);
     for (int i = 0; i < g.n_inst; ++i) {
-      const int ob = g.out_off + i * mi.nout;
+      // output k of device i at out_off + k * n_inst + i (output-major per group)
+      const int ob = g.out_off + i, os = g.n_inst;
       size_t before = SJ.size();
-      device_stamps(g.model, &T.term_orig[g.term_off + (size_t)i * g.ntx], ob, SJ, SF, SQ);
-      for (size_t k = before; k < SJ.size(); ++k) SJq.push_back(is_charge_partial(g.model, SJ[k].out - ob) ? 1 : 0);
+      device_stamps(g.model, &T.term_orig[g.term_off + (size_t)i * g.ntx], ob, os, SJ, SF, SQ);
+      for (size_t k = before; k < SJ.size(); ++k) SJq.push_back(is_charge_partial(g.model, (SJ[k].out - ob) / os) ? 1 : 0);
     }
     const bool diff = (g.model == CEDAR_MOS1 || g.model == CEDAR_R);
     T.adj_goff.push_back(diff ? T.n_adj : -1);

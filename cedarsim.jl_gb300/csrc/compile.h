@@ -23,8 +23,9 @@ int num_models();
 // One stamp: contribution of output `out` (sign -1/+1) of a device to
 // J[row_eq][col_unknown] (col >= 0) or to a residual/charge row (col = -1).
 struct Stamp { int row, col, out, neg; };
-// Stamps of one device given its local terminal unknowns t[] (branch last).
-void device_stamps(int model, const int *t, int out_base, std::vector<Stamp> &J,
+// Stamps of one device given its local terminal unknowns t[] (branch last);
+// output k of the device is out_base + k * out_stride.
+void device_stamps(int model, const int *t, int out_base, int out_stride, std::vector<Stamp> &J,
                    std::vector<Stamp> &F, std::vector<Stamp> &Q);
 
 struct GroupInfo {

@@ -397,8 +397,8 @@ struct Engine {
       const int *tm = T.term + gr.term_off + i * gr.ntx;
       double v[CEDAR_MAX_TERM];
       for (int k = 0; k < gr.ntx; ++k) { int u = tm[k]; v[k] = u < 0 ? 0.0 : x[u]; }
-      eval_device(gr.model, dp + gr.dpar_off + i, gr.n_inst, v, nullptr, ctx, T.pwl,
-                  w.dout + gr.out_off + i * model_nout(gr.model));
+      eval_device(gr.model, dp + gr.dpar_off + i, gr.n_inst, v, nullptr, ctx, T.pwl, w.dout + gr.out_off + i,
+                  gr.n_inst);
     }
   }
 

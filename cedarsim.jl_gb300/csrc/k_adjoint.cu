@@ -233,7 +233,7 @@ __device__ __forceinline__ void backward_step(AdjSlot<K> &s, const AdjDev &a, un
       const int *tm = T.term + gr.term_off + i * gr.ntx;
       double v[CEDAR_MAX_TERM];
       for (int kk = 0; kk < gr.ntx; ++kk) { int u = tm[kk]; v[kk] = u < 0 ? 0.0 : x[u]; }
-      eval_device(gr.model, s.dp + gr.dpar_off + i, gr.n_inst, v, nullptr, ctx, T.pwl, s.w.dout + gr.out_off + i * model_nout(gr.model));
+      eval_device(gr.model, s.dp + gr.dpar_off + i, gr.n_inst, v, nullptr, ctx, T.pwl, s.w.dout + gr.out_off + i, gr.n_inst);
     });
   }
   __syncwarp(ab);
@@ -262,7 +262,7 @@ __device__ __forceinline__ void backward_step(AdjSlot<K> &s, const AdjDev &a, un
       const int *tm = T.term + gr.term_off + i * gr.ntx;
       double v[CEDAR_MAX_TERM];
       for (int kk = 0; kk < gr.ntx; ++kk) { int u = tm[kk]; v[kk] = u < 0 ? 0.0 : x[u]; }
-      eval_device(gr.model, s.dp + gr.dpar_off + i, gr.n_inst, v, nullptr, ctx, T.pwl, s.w.dout + gr.out_off + i * model_nout(gr.model));
+      eval_device(gr.model, s.dp + gr.dpar_off + i, gr.n_inst, v, nullptr, ctx, T.pwl, s.w.dout + gr.out_off + i, gr.n_inst);
     });
   }
   __syncwarp(ab);
@@ -363,7 +363,7 @@ __device__ __forceinline__ void backward_step(AdjSlot<K> &s, const AdjDev &a, un
       for (int i = rank; i < gr.n_inst; i += K) {
         const int *to = T.term_orig + gr.term_off + i * gr.ntx;
         const int *tm = T.term + gr.term_off + i * gr.ntx;
-        const double o0 = s.w.dout[gr.out_off + i * model_nout(gr.model)];
+        const double o0 = s.w.dout[gr.out_off + i];   // output 0 of device i
         if (gr.model == CEDAR_MOS1) {
           // d(m Ids)/dW = m type id / W (id is linear in beta = KP W / L); KCL(d) -, KCL(s) +
           const double W = s.raw[gr.par_off + gr.n_inst + i];

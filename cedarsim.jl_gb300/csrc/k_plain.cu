@@ -49,13 +49,14 @@ __global__ void eval_kernel(DTpl T, const double *dpar, const double *x, const d
   int i = d - (gi ? T.dev_end[gi - 1] : 0);
   const int *tm = T.term_orig + gr.term_off + i * gr.ntx;
   double v[CEDAR_MAX_TERM], vd[CEDAR_MAX_TERM];
+  const bool need_vd = xdot && model_has_q(gr.model);   // only charge models read x'
   for (int k = 0; k < gr.ntx; ++k) {
     int u = tm[k];
     v[k] = u < 0 ? 0.0 : __ldg(x + u);
-    vd[k] = (u < 0 || !xdot) ? 0.0 : __ldg(xdot + u);
+    vd[k] = (u < 0 || !need_vd) ? 0.0 : __ldg(xdot + u);
   }
   EvalCtx ctx{t, cj, 1.0, T.gmin, false, true};
-  eval_device(gr.model, dpar + gr.dpar_off + i, gr.n_inst, v, vd, ctx, T.pwl, dout + gr.out_off + i * model_nout(gr.model));
+  eval_device(gr.model, dpar + gr.dpar_off + i, gr.n_inst, v, vd, ctx, T.pwl, dout + gr.out_off + i, gr.n_inst);
 }
 
 // K2+K3 (grid-wide): J values in CSC order and residual rows, fixed-order sums.
@@ -207,6 +208,50 @@ __global__ void fp64_probe_kernel(double *sink, int iters, int active_lanes) {
   }
   const double r = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
   if (r == -1.0) sink[blockIdx.x] = r;  // never true; keeps the chains live
+}
+
+// FP64 dependent-operation latency: one warp, every lane one chain of `iters`
+// dependent DFMAs (unrolled by 8); lane 0 reads the SM clock around the chain.
+__global__ void fp64_latency_kernel(double *sink, long long *cycles, int iters) {
+  double a = 0.5 + 1e-9 * threadIdx.x;
+  const double m = 0.9999999, c = 1e-7;
+  const long long c0 = clock64();
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) a = fma(a, m, c);
+  }
+  if (a == -1.0) sink[threadIdx.x] = a;    // never true; keeps the chain live
+  const long long c1 = clock64();
+  if (threadIdx.x == 0) *cycles = c1 - c0;
+}
+
+cudaError_t launch_fp64_latency(int iters, double *cycles_per_op, double *ns_per_op) {
+  double *sink = nullptr;
+  long long *cyc = nullptr;
+  cudaError_t e = cudaMalloc(&sink, 32 * sizeof(double) + sizeof(long long));
+  if (e != cudaSuccess) return e;
+  cyc = reinterpret_cast<long long *>(sink + 32);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0); cudaEventCreate(&e1);
+  float best = 1e30f;
+  long long best_cyc = 0;
+  for (int rep = 0; rep < 4; ++rep) {   // first launch warms up; best of the rest
+    cudaEventRecord(e0);
+    fp64_latency_kernel<<<1, 32>>>(sink, cyc, iters);
+    cudaEventRecord(e1);
+    if ((e = cudaEventSynchronize(e1)) != cudaSuccess) break;
+    float t = 0; cudaEventElapsedTime(&t, e0, e1);
+    long long c = 0;
+    if ((e = cudaMemcpy(&c, cyc, sizeof c, cudaMemcpyDeviceToHost)) != cudaSuccess) break;
+    if (rep > 0 && t < best) { best = t; best_cyc = c; }
+  }
+  cudaEventDestroy(e0); cudaEventDestroy(e1);
+  cudaFree(sink);
+  if (e != cudaSuccess) return e;
+  const double ops = 8.0 * iters;
+  if (cycles_per_op) *cycles_per_op = best_cyc / ops;
+  if (ns_per_op) *ns_per_op = best * 1e6 / ops;
+  return cudaGetLastError();
 }
 
 cudaError_t launch_fp64_probe(int active_lanes, int iters, double *gflops, double *ms) {

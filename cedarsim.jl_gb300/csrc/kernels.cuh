@@ -144,6 +144,7 @@ cudaError_t launch_ac_dense(const AcDev &a, bool noise, cudaStream_t s);
 
 // FP64 issue-rate probe (8 DFMA chains per thread, lanes >= active_lanes idle)
 cudaError_t launch_fp64_probe(int active_lanes, int iters, double *gflops, double *ms);
+cudaError_t launch_fp64_latency(int iters, double *cycles_per_op, double *ns_per_op);
 
 // batched persistent engine with K lanes per instance
 cudaError_t launch_batch(const BatchDev &b, int K, int warps_per_cta, int grid, size_t smem, cudaStream_t s);

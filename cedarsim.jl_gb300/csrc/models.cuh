@@ -1,8 +1,10 @@
 // models.cuh — FP64 device-model evaluation (host + device), per-model outputs.
 //
 // Each device writes `nout` outputs (layout fixed per model, multiplicity folded
-// in); the stamp programs built by compile.cpp then add signed outputs into J
-// slots and residual rows.  Equations follow CedarSim:
+// in), output k at out[k * os]: a group's outputs are stored output-major (output
+// k of device i at out_off + k * n_inst + i), so the devices a warp evaluates
+// store each output contiguously.  The stamp programs built by compile.cpp then
+// add signed outputs into J slots and residual rows.  Equations follow CedarSim:
 //   R  I - V/res = 0                      src/simpledevices.jl:66-77
 //   C  I - C ddt(V) = 0                   src/simpledevices.jl:105-109
 //   L  V - L ddt(I) = 0                   src/simpledevices.jl:128-132
@@ -150,9 +152,9 @@ struct EvalCtx {
 
 // V / I source outputs given the source value vs (already scaled); same layout
 // as eval_device.  Used when vs is cached once per Newton solve.
-CEDAR_HD void eval_source_value(int model, const double *dp, const double *v, double vs, double *out) {
+CEDAR_HD void eval_source_value(int model, const double *dp, const double *v, double vs, double *out, int os) {
   double m = dp[0];
-  if (model == CEDAR_V) { out[0] = m * v[2]; out[1] = (v[0] - v[1]) - vs; out[2] = m; out[3] = 1.0; }
+  if (model == CEDAR_V) { out[0] = m * v[2]; out[os] = (v[0] - v[1]) - vs; out[2 * os] = m; out[3 * os] = 1.0; }
   else out[0] = m * vs;
 }
 
@@ -219,7 +221,7 @@ CEDAR_HD bool is_one(double a) {
 // both are exact, so the outputs have the bits of the general form.
 template <bool UNIT>
 CEDAR_HD void mos1_device(double type, double beta, double vth, double lam, double m, const double *v, double gmin,
-                          double *out) {
+                          double *out, int os) {
   const bool pt = UNIT && sign_set(type);
   auto tm = [&](double x) -> double {
     if constexpr (UNIT) return neg_if(x, pt);
@@ -232,11 +234,12 @@ CEDAR_HD void mos1_device(double type, double beta, double vth, double lam, doub
   const double vgs = tm(v[1] - v[2]), vds = tm(v[0] - v[2]);
   const bool fwd = vds >= 0;
   double i1, g1, g2;
-  mos1_fwd(fwd ? vgs : vgs - vds, fwd ? vds : -vds, vth, beta, lam, i1, g1, g2);
+  // the reversed-mode negations as sign flips (integer ops, exact)
+  mos1_fwd(fwd ? vgs : vgs - vds, neg_if(vds, !fwd), vth, beta, lam, i1, g1, g2);
   const double s12 = g1 + g2;
-  const double id = fwd ? i1 : -i1, gm = fwd ? g1 : -g1, gds = fwd ? g2 : s12, gsum = fwd ? s12 : g2;
+  const double id = neg_if(i1, !fwd), gm = neg_if(g1, !fwd), gds = fwd ? g2 : s12, gsum = fwd ? s12 : g2;
   const double ids = fma(gmin, v[0] - v[2], tm(id));
-  out[0] = mm(ids); out[1] = mm(gm); out[2] = mm(gds + gmin); out[3] = mm(gsum + gmin);
+  out[0] = mm(ids); out[os] = mm(gm); out[2 * os] = mm(gds + gmin); out[3 * os] = mm(gsum + gmin);
 }
 
 // The source waveform out of line: the batched engines take time-varying sources'
@@ -256,29 +259,29 @@ double source_value_cold(const double *p, int s, double t, bool dc, const double
 // HOT_SRC false: V / I source values through source_value_cold.
 template <bool HOT_SRC = true>
 CEDAR_HD void eval_device(int model, const double *dp, int ds, const double *v, const double *vd,
-                          const EvalCtx &ctx, const double *pwl, double *out) {
+                          const EvalCtx &ctx, const double *pwl, double *out, int os) {
   switch (model) {
     case CEDAR_R: {
       double gm = dp[0];
-      out[0] = gm * (v[0] - v[1]); out[1] = gm;
+      out[0] = gm * (v[0] - v[1]); out[os] = gm;
     } break;
     case CEDAR_C: {
       double mc = dp[0];
       double Q = mc * (v[0] - v[1]);
       out[0] = ctx.xdot ? mc * (vd[0] - vd[1]) : ctx.cj * Q;
-      out[1] = ctx.cj * mc; out[2] = Q;
+      out[os] = ctx.cj * mc; out[2 * os] = Q;
     } break;
     case CEDAR_L: {
       double m = dp[0], l = dp[ds], I = v[2];
       out[0] = m * I;
-      out[1] = (v[0] - v[1]) - (ctx.xdot ? l * vd[2] : ctx.cj * (l * I));
-      out[2] = m; out[3] = 1.0; out[4] = ctx.cj * l; out[5] = l * I;
+      out[os] = (v[0] - v[1]) - (ctx.xdot ? l * vd[2] : ctx.cj * (l * I));
+      out[2 * os] = m; out[3 * os] = 1.0; out[4 * os] = ctx.cj * l; out[5 * os] = l * I;
     } break;
     case CEDAR_V: {
       double m = dp[0];
       double vs = (HOT_SRC ? source_value(dp, ds, ctx.t, ctx.dc, pwl) : source_value_cold(dp, ds, ctx.t, ctx.dc, pwl)) *
                   ctx.src_scale;
-      out[0] = m * v[2]; out[1] = (v[0] - v[1]) - vs; out[2] = m; out[3] = 1.0;
+      out[0] = m * v[2]; out[os] = (v[0] - v[1]) - vs; out[2 * os] = m; out[3 * os] = 1.0;
     } break;
     case CEDAR_I: {
       double m = dp[0];
@@ -287,16 +290,16 @@ CEDAR_HD void eval_device(int model, const double *dp, int ds, const double *v, 
     } break;
     case CEDAR_E: {
       double gain = dp[0], m = dp[ds];
-      out[0] = m * v[4]; out[1] = (v[0] - v[1]) - gain * (v[2] - v[3]); out[2] = m; out[3] = 1.0; out[4] = gain;
+      out[0] = m * v[4]; out[os] = (v[0] - v[1]) - gain * (v[2] - v[3]); out[2 * os] = m; out[3 * os] = 1.0; out[4 * os] = gain;
     } break;
     case CEDAR_G: {
       double mg = dp[0];
-      out[0] = mg * (v[2] - v[3]); out[1] = mg;
+      out[0] = mg * (v[2] - v[3]); out[os] = mg;
     } break;
     case CEDAR_MOS1: {
       const double type = dp[0], beta = dp[ds], vth = dp[2 * ds], lam = dp[3 * ds], m = dp[4 * ds];
-      if (is_unit(type) && is_one(m)) mos1_device<true>(type, beta, vth, lam, m, v, ctx.gmin, out);
-      else mos1_device<false>(type, beta, vth, lam, m, v, ctx.gmin, out);
+      if (is_unit(type) && is_one(m)) mos1_device<true>(type, beta, vth, lam, m, v, ctx.gmin, out, os);
+      else mos1_device<false>(type, beta, vth, lam, m, v, ctx.gmin, out, os);
     } break;
     case CEDAR_DIODE: {
       double isat = dp[0], invnvt = dp[ds], m = dp[2 * ds];
@@ -304,15 +307,15 @@ CEDAR_HD void eval_device(int model, const double *dp, int ds, const double *v, 
       if (a <= 80.0) { e = exp(a); I = isat * (e - 1.0); gd = isat * e * invnvt; }
       else { e = exp(80.0); I = isat * (e * (1.0 + (a - 80.0)) - 1.0); gd = isat * e * invnvt; }
       I += ctx.gmin * vv; gd += ctx.gmin;
-      out[0] = m * I; out[1] = m * gd;
+      out[0] = m * I; out[os] = m * gd;
     } break;
     case CEDAR_NLVCR: {
       double tR = dp[0], m = dp[ds];
       double vgs = v[1] - v[2], vds = v[0] - v[2];
-      out[0] = m * (vds * (tR * vgs)); out[1] = m * (tR * vgs); out[2] = m * (tR * vds); out[3] = m * (tR * (vgs + vds));
+      out[0] = m * (vds * (tR * vgs)); out[os] = m * (tR * vgs); out[2 * os] = m * (tR * vds); out[3 * os] = m * (tR * (vgs + vds));
     } break;
     default:  // Verilog-A models
-      va::eval(model - va::kBase, dp, ds, v, vd, ctx.xdot, ctx.cj, ctx.gmin, out);
+      va::eval(model - va::kBase, dp, ds, v, vd, ctx.xdot, ctx.cj, ctx.gmin, out, os);
       break;
   }
 }

@@ -167,8 +167,8 @@ int main() {
     point(kIn[m], v);
     EvalCtx ctx{1e-9, 1e12, 1.0, 1e-12, false, false};
     g_ops = 0;
-    if (m == CEDAR_V || m == CEDAR_I) eval_source_value(m, dp, v, Cnt(0.8), out);
-    else eval_device(m, dp, 1, v, nullptr, ctx, nullptr, out);
+    if (m == CEDAR_V || m == CEDAR_I) eval_source_value(m, dp, v, Cnt(0.8), out, 1);
+    else eval_device(m, dp, 1, v, nullptr, ctx, nullptr, out, 1);
     std::printf(", %lld", g_ops);
   }
   std::printf("};\n");
@@ -180,7 +180,7 @@ int main() {
     derive_one(va::kBase + k, raw, 1, dp, 1, 0.025852);
     point(va::kNTerm[k] + va::kHasBr[k], v);
     g_ops = 0;
-    va::eval(k, dp, 1, v, nullptr, false, Cnt(1e12), Cnt(1e-12), out);
+    va::eval(k, dp, 1, v, nullptr, false, Cnt(1e12), Cnt(1e-12), out, 1);
     std::printf("%s%lld", k ? ", " : "", g_ops);
   }
   if (va::kCount == 0) std::printf("0");

@@ -821,25 +821,25 @@ class _Emitter:
     def eval(self) -> str:
         m = self.m
         L = [f"VA_HD void eval_{m.name}(const double *dp, int ds, const double *v, const double *vd, bool xdot, "
-             f"double cj, double gmin, double *out) {{"]
+             f"double cj, double gmin, double *out, int os) {{"]
         L += self.prologue()
         L.append("  const double mf = c.m;")
         o = 0
         for r in m.frows:
             if r in m.qrows:
                 qd = " + ".join(f"part(Fq[{r}], {k}) * vd[{k}]" for k in range(m.nx))
-                L.append(f"  out[{o}] = mf * (val(Fi[{r}]) + (xdot ? ({qd}) : cj * val(Fq[{r}])));")
+                L.append(f"  out[{o} * os] = mf * (val(Fi[{r}]) + (xdot ? ({qd}) : cj * val(Fq[{r}])));")
             else:
-                L.append(f"  out[{o}] = mf * val(Fi[{r}]);")
+                L.append(f"  out[{o} * os] = mf * val(Fi[{r}]);")
             o += 1
         for r, k in m.gents:
-            L.append(f"  out[{o}] = mf * part(Fi[{r}], {k});")
+            L.append(f"  out[{o} * os] = mf * part(Fi[{r}], {k});")
             o += 1
         for r in m.qrows:
-            L.append(f"  out[{o}] = mf * val(Fq[{r}]);")
+            L.append(f"  out[{o} * os] = mf * val(Fq[{r}]);")
             o += 1
         for r, k in m.cents:
-            L.append(f"  out[{o}] = cj * (mf * part(Fq[{r}], {k}));")
+            L.append(f"  out[{o} * os] = cj * (mf * part(Fq[{r}], {k}));")
             o += 1
         L.append("  (void)vd; (void)xdot; (void)cj;")
         L.append("}")
@@ -955,17 +955,17 @@ def emit_header(models: List[Tuple[VAModel, _Analysis]], base_id: int) -> str:
     L.append("  dp[np * ds] = vt;")
     L.append("}")
     sig = ("void eval(int k, const double *dp, int ds, const double *v, const double *vd, bool xdot, double cj, "
-           "double gmin, double *out)")
+           "double gmin, double *out, int os)")
     L.append("#if defined(CEDAR_VA_SEPARATE) && !defined(CEDAR_VA_DEFINE)")
     L.append(f"VA_EXTERN {sig};   // defined in va_models.cu")
     L.append("#else")
     L.append(f"VA_CALL {sig} {{")
     L.append("  switch (k) {")
     for i, (m, _) in enumerate(models):
-        L.append(f"    case {i}: eval_{m.name}(dp, ds, v, vd, xdot, cj, gmin, out); break;")
+        L.append(f"    case {i}: eval_{m.name}(dp, ds, v, vd, xdot, cj, gmin, out, os); break;")
     L.append("    default: break;")
     L.append("  }")
-    L.append("  (void)dp; (void)ds; (void)v; (void)vd; (void)xdot; (void)cj; (void)gmin; (void)out;")
+    L.append("  (void)dp; (void)ds; (void)v; (void)vd; (void)xdot; (void)cj; (void)gmin; (void)out; (void)os;")
     L.append("}")
     L.append("#endif")
     L.append("inline int noise(int k, const double *dp, int ds, const double *v, double gmin, double *pw, "

@@ -457,6 +457,13 @@ int cedar_adjoint_last_ms(cedar_batch *b, double *fwd_ms, double *bwd_ms);
  * per FMA on the active lanes, best of 5 timed launches (CUDA events). */
 int cedar_fp64_probe(int32_t active_lanes, int32_t iters, double *gflops, double *ms);
 
+/* FP64 dependent-operation latency (no counterpart in the reference): one warp
+ * whose lanes each run a chain of 8 * iters dependent DFMAs; cycles_per_op from
+ * the SM clock, ns_per_op from CUDA events (launch included), best of 3.  It
+ * bounds a single circuit's Newton iteration, whose LU and substitutions are
+ * chains of dependent FP64 operations. */
+int cedar_fp64_latency(int32_t iters, double *cycles_per_op, double *ns_per_op);
+
 #ifdef __cplusplus
 }
 #endif

@@ -219,7 +219,7 @@ def test_emitted_code_compiles_for_the_device(emitted, tmp_path):
     (tmp_path / "k.cu").write_text(
         '#include "va_models.gen.h"\n'
         '__global__ void k(int m, const double *dp, const double *v, double *out) {\n'
-        '  cedar::va::eval(m, dp, 1, v, v, false, 1e12, 1e-12, out);\n}\n')
+        '  cedar::va::eval(m, dp, 1, v, v, false, 1e12, 1e-12, out, 1);\n}\n')
     r = subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-std=c++17", "-c", "-I", str(CSRC),
                         "-I", str(gen_dir), str(tmp_path / "k.cu"), "-o", str(tmp_path / "k.o")],
                        capture_output=True, text=True)
