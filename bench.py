@@ -266,7 +266,7 @@ def measure_eval(pkg, args, torch, C, fp64_peak=None):
     return {"workload": f"{args.eval_stages}-stage inverter chain ({3 * args.eval_stages} devices, n = {sy.n}, "
                         f"nnz(J) = {sy.nnz_j}), one cedar_eval_dev per call",
             "bytes_per_call": int(costs.bytes_eval), "ms_per_call": ms, "achieved_gbs": gbs, "peak_gbs": peak,
-            "frac": gbs / peak, "finite": ok, "kernels": ["eval_kernel", "stamp_kernel"],
+            "frac": gbs / peak, "finite": ok, "kernels": ["eval_kernel", "stamp_kernel", "stamp_long_final_kernel"],
             "fp64": {"flops_per_call": int(flops), "achieved_tflops": tfl, "peak_tflops": fp64_peak,
                      "frac": tfl / fp64_peak if fp64_peak else None},
             "roofline_frac": (t_floor / (ms * 1e-3)) if t_floor else None,

@@ -59,10 +59,10 @@ __global__ void eval_kernel(DTpl T, const double *dpar, const double *x, const d
   eval_device(gr.model, dpar + gr.dpar_off + i, gr.n_inst, v, vd, ctx, T.pwl, dout + gr.out_off + i, gr.n_inst);
 }
 
-// K2+K3 (grid-wide): J values in CSC order and residual rows, fixed-order sums.
-// Lists longer than kLongEval (supply rails) are left to stamp_long_kernel.
-__global__ void stamp_kernel(DTpl T, const double *dout, double *F, double *J) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
+// K2+K3 (grid-wide): J values in CSC order and residual rows, fixed-order sums,
+// one thread per J slot / row.  Lists longer than kLongEval (supply rails) are
+// summed by the long-list chunk warps below.
+__device__ __forceinline__ void stamp_slot(const DTpl &T, const double *dout, double *F, double *J, int s) {
   if (J && s < T.n_csc && T.jcsc_ptr[s + 1] - T.jcsc_ptr[s] <= kLongEval) {
     double acc = 0.0;
     for (int k = T.jcsc_ptr[s]; k < T.jcsc_ptr[s + 1]; ++k) { int e = __ldg(T.jcsc_ent + k); acc = acc + signed_out(__ldg(dout + (e >> 1)), e); }
@@ -82,10 +82,7 @@ __global__ void stamp_kernel(DTpl T, const double *dout, double *F, double *J) {
 // round alike, so every lane holds the same bits.
 constexpr int kLongChunkDev = 256;
 constexpr int kLongLaneLoads = kLongChunkDev / 32;
-__global__ void stamp_long_part_kernel(DTpl T, const double *dout, double *part) {
-  const int p = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
-  const int lane = threadIdx.x & 31;
-  if (p >= T.n_long_part) return;           // warp-uniform
+__device__ __forceinline__ void stamp_long_chunk(const DTpl &T, const double *dout, double *part, int p, int lane) {
   const int nl = T.n_long_jc + T.n_long_fo;
   int lo = 0, hi = nl;                       // list i with long_off[i] <= p < long_off[i + 1]
   while (hi - lo > 1) { const int mid = (lo + hi) >> 1; if (T.long_off[mid] <= p) lo = mid; else hi = mid; }
@@ -106,6 +103,18 @@ __global__ void stamp_long_part_kernel(DTpl T, const double *dout, double *part)
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) acc = acc + __shfl_xor_sync(0xffffffffu, acc, o);
   if (lane == 0) part[p] = acc;
+}
+
+// One launch for both (they read only the device outputs): the first
+// `long_blocks` blocks run the long-list chunks (one warp each), the rest the
+// J slots and rows, so the supply-rail sums overlap the ordinary stamping.
+__global__ void stamp_kernel(DTpl T, const double *dout, double *F, double *J, double *part, int long_blocks) {
+  if ((int)blockIdx.x < long_blocks) {
+    const int p = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+    if (p < T.n_long_part) stamp_long_chunk(T, dout, part, p, threadIdx.x & 31);   // warp-uniform test
+    return;
+  }
+  stamp_slot(T, dout, F, J, (int)((blockIdx.x - long_blocks) * blockDim.x + threadIdx.x));
 }
 
 // Pass 2: one CTA per long list; thread t sums the list's chunk sums t, t + 256,
@@ -146,14 +155,11 @@ cudaError_t launch_eval(const DTpl &T, const DTpl *T_dev, const double *dpar, co
   (void)T_dev;
   const int th = 256;
   if (T.n_dev > 0) eval_kernel<<<(T.n_dev + th - 1) / th, th, 0, s>>>(T, dpar, x, xdot, t, cj, dout);
-  int m = T.n_csc > T.n ? T.n_csc : T.n;
-  stamp_kernel<<<(m + th - 1) / th, th, 0, s>>>(T, dout, F, J);
+  const int m = T.n_csc > T.n ? T.n_csc : T.n, warps = th / 32;
   const int nlong = T.n_long_jc + T.n_long_fo;
-  if (nlong > 0) {
-    const int warps = th / 32;
-    stamp_long_part_kernel<<<(T.n_long_part + warps - 1) / warps, th, 0, s>>>(T, dout, part);
-    stamp_long_final_kernel<<<nlong, kLongThreads, 0, s>>>(T, part, F, J);
-  }
+  const int long_blocks = nlong > 0 ? (T.n_long_part + warps - 1) / warps : 0;
+  stamp_kernel<<<long_blocks + (m + th - 1) / th, th, 0, s>>>(T, dout, F, J, part, long_blocks);
+  if (nlong > 0) stamp_long_final_kernel<<<nlong, kLongThreads, 0, s>>>(T, part, F, J);
   return cudaGetLastError();
 }
 
