@@ -728,19 +728,23 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am, const 
   const double *const dp = s.dp;
   const double *const srcv = s.w.srcv;
   const double jgs = s.jgs;
-  // two accumulators (even / odd entries) halve the dependent add chain
+  // Fixed-order gathers with one accumulator: the lists are short (at most
+  // kLongGather entries), and with 8 warps per SM sharing the FP64 pipe a second
+  // accumulator's combining add costs more issue time than its shorter
+  // dependency chain saves.  gather0 starts from the first entry instead of
+  // 0.0 + it (the same value; a -0.0 entry stays -0.0).
   auto gather = [&](const int *ptr, const int *ent, int q, double acc) {
-    const int a = ptr[q], e1 = ptr[q + 1];
-    double acc1 = 0.0;
-    int k = a;
-    for (; k + 1 < e1; k += 2) {
-      const int e0 = ent[k], e2 = ent[k + 1];
-      const double v0 = dout[e0 >> 1], v2 = dout[e2 >> 1];
-      acc = acc + signed_out(v0, e0);
-      acc1 = acc1 + signed_out(v2, e2);
-    }
-    if (k < e1) { const int e0 = ent[k]; acc = acc + signed_out(dout[e0 >> 1], e0); }
-    return acc + acc1;
+    const int e1 = ptr[q + 1];
+    for (int k = ptr[q]; k < e1; ++k) { const int e0 = ent[k]; acc = acc + signed_out(dout[e0 >> 1], e0); }
+    return acc;
+  };
+  auto gather0 = [&](const int *ptr, const int *ent, int q) {
+    int k = ptr[q];
+    const int e1 = ptr[q + 1];
+    double acc = 0.0;
+    if (k < e1) { const int e0 = ent[k]; acc = signed_out(dout[e0 >> 1], e0); ++k; }
+    for (; k < e1; ++k) { const int e0 = ent[k]; acc = acc + signed_out(dout[e0 >> 1], e0); }
+    return acc;
   };
   // K1: device evaluation, one model at a time across the warp
   {
@@ -761,7 +765,7 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am, const 
   // lists longer than kLongGather (supply rails) are left to the slot-collective
   // sums below
   for (int q = rank; q < T.nnz_lu; q += K)
-    if (T.jlu_ptr[q + 1] - T.jlu_ptr[q] <= kLongGather) lu[q] = gather(T.jlu_ptr, T.jlu_ent, q, 0.0);
+    if (T.jlu_ptr[q + 1] - T.jlu_ptr[q] <= kLongGather) lu[q] = gather0(T.jlu_ptr, T.jlu_ent, q);
   for (int r = rank; r < T.n; r += K)
     if (T.fint_ptr[r + 1] - T.fint_ptr[r] <= kLongGather) F[r] = gather(T.fint_ptr, T.fint_ent, r, jhist ? jhist[r] : 0.0);
   for (int t = 0; t < T.n_long_lu; ++t) {
@@ -799,14 +803,8 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am, const 
         const int4 tk = T.lu_task[t];
         if (tk.w - tk.z > kLongPairs) continue;  // summed by the whole slot below
         int q = tk.x, info = tk.y;
-        double acc = lu[q], acc1 = 0.0;
-        int p = tk.z;
-        for (; p + 1 < tk.w; p += 2) {
-          const int2 p0 = T.lu_pair[p], p1 = T.lu_pair[p + 1];
-          acc -= lu[p0.x] * lu[p0.y]; acc1 -= lu[p1.x] * lu[p1.y];
-        }
-        if (p < tk.w) { const int2 p0 = T.lu_pair[p]; acc -= lu[p0.x] * lu[p0.y]; }
-        acc += acc1;
+        double acc = lu[q];
+        for (int p = tk.z; p < tk.w; ++p) { const int2 p0 = T.lu_pair[p]; acc -= lu[p0.x] * lu[p0.y]; }
         int kind = info & 3, j = info >> 2;
         if (kind == 2) acc *= rd[j];
         else if (kind == 1) {
@@ -843,14 +841,7 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am, const 
         const int4 tk = T.fw_task[t];
         if (tk.z - tk.y > kLongPairs) continue;  // summed by the whole slot below
         int i = tk.x; double acc = b[i];
-        double acc1 = 0.0;
-        int p = tk.y;
-        for (; p + 1 < tk.z; p += 2) {
-          const int2 p0 = T.fw_pair[p], p1 = T.fw_pair[p + 1];
-          acc -= lu[p0.x] * b[p0.y]; acc1 -= lu[p1.x] * b[p1.y];
-        }
-        if (p < tk.z) { const int2 p0 = T.fw_pair[p]; acc -= lu[p0.x] * b[p0.y]; }
-        acc += acc1;
+        for (int p = tk.y; p < tk.z; ++p) { const int2 p0 = T.fw_pair[p]; acc -= lu[p0.x] * b[p0.y]; }
         b[i] = acc;
       }
       for (int u = T.long_fw_lvl[l]; u < T.long_fw_lvl[l + 1]; ++u) {
@@ -869,14 +860,7 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am, const 
         const int4 tk = T.bw_task[t];
         if (tk.z - tk.y > kLongPairs) continue;  // summed by the whole slot below
         int i = tk.x; double acc = b[i];
-        double acc1 = 0.0;
-        int p = tk.y;
-        for (; p + 1 < tk.z; p += 2) {
-          const int2 p0 = T.bw_pair[p], p1 = T.bw_pair[p + 1];
-          acc -= lu[p0.x] * b[p0.y]; acc1 -= lu[p1.x] * b[p1.y];
-        }
-        if (p < tk.z) { const int2 p0 = T.bw_pair[p]; acc -= lu[p0.x] * b[p0.y]; }
-        acc += acc1;
+        for (int p = tk.y; p < tk.z; ++p) { const int2 p0 = T.bw_pair[p]; acc -= lu[p0.x] * b[p0.y]; }
         b[i] = acc * rd[i];
       }
       for (int u = T.long_bw_lvl[l]; u < T.long_bw_lvl[l + 1]; ++u) {
