@@ -19,6 +19,7 @@
 // device-side queue (one fetch-and-add; no slot ever waits on another warp).
 #pragma once
 #include <climits>
+#include <type_traits>
 #include "kernels.cuh"
 
 namespace cedar {
@@ -895,13 +896,18 @@ __device__ __forceinline__ void newton_iteration(Slot<K> &s, unsigned am, const 
   }
   bool conv = (scale == 1.0);
   if (!slot_bad && !slot_nf) {
-    for (int i = rank; i < T.n; i += K) {
-      double d = -b[i] * scale;
-      double xi = jx[i] + d;
-      jx[i] = xi;
-      double lim = s.nrel * fabs(xi) + (T.is_node[i] ? s.nav : s.nai);
-      if (abs_bits(d) > abs_bits(lim)) conv = false;
-    }
+    // undamped (every transient iteration): -b * 1 is -b, so the product is left out
+    auto update = [&](auto scaled) {
+      for (int i = rank; i < T.n; i += K) {
+        const double d = decltype(scaled)::value ? -b[i] * scale : -b[i];
+        double xi = jx[i] + d;
+        jx[i] = xi;
+        double lim = s.nrel * fabs(xi) + (T.is_node[i] ? s.nav : s.nai);
+        if (abs_bits(d) > abs_bits(lim)) conv = false;
+      }
+    };
+    if (conv) update(std::false_type{});
+    else update(std::true_type{});
   }
   const bool slot_notconv = (__ballot_sync(am, !conv) & s.smask()) != 0;
   __syncwarp(am);
