@@ -213,6 +213,19 @@ VA_HD Dual<T, N> hypot(const Dual<T, N> &x, const Dual<T, N> &y) {
   for (int i = 0; i < N; ++i) r.d[i] = (x.v * x.d[i] + y.v * y.d[i]) / r.v;
   return r;
 }
+// d(x^p)/dx given y = x^p, by the rule CedarSim's pow derivative uses (its
+// frule, src/va_env.jl:57-68, calls ChainRules 1.69's pow gradient): p y / x
+// where x != 0 or p < 0; at x = 0, 1 for p = 1, 0 for p = 0 or p > 1, +inf
+// for 0 < p < 1.  So x^0 has zero partials everywhere (no 0 * inf at x = 0;
+// BSIM-CMG raises a smoothed V_ds that rounds to exactly 0 to the power DVTP1 = 0)
+template <class T>
+VA_HD T pow_grad_x(const T &x, const T &p, const T &y) {
+  const double xv = val(x), pv = val(p);
+  if (xv != 0.0 || pv < 0.0) return p * y / x;
+  if (pv == 1.0) return T(1.0);
+  if (pv == 0.0 || pv > 1.0) return T(0.0);
+  return T(INFINITY);
+}
 // x^y: with a constant exponent the log term is left out (a strong zero, so a
 // negative base with an integral exponent keeps finite partials)
 template <class T, int N>
@@ -220,7 +233,7 @@ VA_HD Dual<T, N> pow(const Dual<T, N> &x, const Dual<T, N> &y) {
   const T p = pow(x.v, y.v);
   Dual<T, N> r;
   r.v = p;
-  const T dx = y.v * pow(x.v, y.v - T(1.0));
+  const T dx = pow_grad_x(x.v, y.v, p);
   bool ycst = true;
   for (int i = 0; i < N; ++i)
     if (!all_zero(y.d[i])) ycst = false;

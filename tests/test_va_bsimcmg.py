@@ -16,6 +16,7 @@ import os
 import pathlib
 import shutil
 import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -83,3 +84,66 @@ def test_bsimcmg_emitted_matches_interpreter(bsim):
     on = ids[(0.5, 0.7, 0.0, 0.0, 0.5, 0.0)]
     off = ids[(0.05, 0.2, 0.0, 0.0, 0.05, 0.0)]
     assert on > 1e-6 and 0 < off < 1e-3 * on      # an n-type FinFET turns on with the gate
+
+
+_INVERTER_SCRIPT = r"""
+import json, sys
+sys.path.insert(0, sys.argv[1])
+import numpy as np
+import __graft_entry__ as ge
+pkg = ge.load()
+O = ge.load_oracle().Oracle(pkg)
+
+def inverter(vin):
+    c = pkg.Circuit()
+    c.V("VDD", "vdd", "0", dc=0.7)
+    c.V("VIN", "in", "0", dc=vin) if not isinstance(vin, pkg.Pulse) else c.V("VIN", "in", "0", wave=vin)
+    c.va("MN", "bsimcmg", ["out", "in", "0", "0"], DEVTYPE=1)
+    c.va("MP", "bsimcmg", ["out", "in", "vdd", "vdd"], DEVTYPE=0)
+    c.C("CL", "out", "0", 1e-15)
+    return c.flatten()
+
+res = {"dc": {}}
+for vin in (0.0, 0.35, 0.7):
+    f = inverter(vin)
+    x, st, rc = O.dcop(f)
+    res["dc"][str(vin)] = [rc, st.status, st.dc_iters, float(x[f.names.index("out")])]
+f = inverter(pkg.Pulse(0.0, 0.7, 10e-12, 5e-12, 5e-12, 40e-12, 100e-12))
+t, xs, st, rc = O.tran(f, pkg.make_opts("bdf2", True, 0.0, 100e-12, 0.0, True, 1e-6, 1e-9), cap=1 << 16)
+k = f.names.index("out")
+res["tran"] = [rc, st.status, len(t), float(xs[0, k]), float(xs[:, k].min()), float(xs[-1, k]),
+               float(xs[np.searchsorted(t, 50e-12), k])]
+print(json.dumps(res))
+"""
+
+
+def test_bsimcmg_inverter_dc_and_transient_on_the_oracle(tmp_path):
+    """A CMOS inverter of two BSIM-CMG devices (0.7 V supply, 1 fF load) through the
+    oracle's DC homotopy and adaptive BDF2 with the model compiled in: the DC point
+    is reached from zero with the input at 0 V, mid-rail and 0.7 V, and a 0 -> 0.7 V
+    input pulse pulls the output low and releases it.  At 0 V input the PMOS's
+    smoothed V_ds rounds to exactly 0 while its partials do not, so the DC solve
+    depends on pow's zero-exponent derivative rule (x^0 has zero partials).  The
+    oracle and package are copied to a scratch directory, so the model's generated
+    code never enters this checkout's build."""
+    if shutil.which("g++") is None or shutil.which("make") is None:
+        pytest.skip("g++ / make not available")
+    import json
+    work = tmp_path / "repo"
+    ign = shutil.ignore_patterns("_build", "__pycache__", "_work")
+    for d in ("cedarsim.jl_gb300", "oracle", "include"):
+        shutil.copytree(ROOT / d, work / d, ignore=ign)
+    shutil.copy(ROOT / "__graft_entry__.py", work / "__graft_entry__.py")
+    (tmp_path / "inv.py").write_text(_INVERTER_SCRIPT)
+    env = dict(os.environ, CEDAR_VA_PATH=str(pathlib.Path(SRC_DIR) / "bsimcmg.va"))
+    r = subprocess.run([sys.executable, str(tmp_path / "inv.py"), str(work)], capture_output=True, text=True,
+                       env=env, timeout=1800)
+    assert r.returncode == 0, r.stderr[-3000:]
+    res = json.loads(r.stdout.strip().splitlines()[-1])
+    for vin, (rc, status, iters, vout) in res["dc"].items():
+        assert rc == 0 and status == 0, (vin, rc, status, iters)
+    assert res["dc"]["0.0"][3] > 0.699 and res["dc"]["0.7"][3] < 1e-3
+    assert 0.0 < res["dc"]["0.35"][3] < 0.7
+    rc, status, npts, v0, vmin, vend, vmid = res["tran"]
+    assert rc == 0 and status == 0 and npts > 10
+    assert v0 > 0.699 and vmid < 0.1 and vmin < 0.1 and vend > 0.6

@@ -291,3 +291,54 @@ def test_strong_zero_partials(pkg, tmp_path):
     spec.loader.exec_module(vi)
     _, _, rG, _ = vi.evaluate(mods[0][0].module, {}, list(v), VT, 1e-12)
     assert rG[0][1] == -1e-3 and rG[2][1] == -1e-3
+
+
+def test_pow_gradient_rule(pkg, tmp_path):
+    """d(x^p)/dx follows the rule of CedarSim's pow derivative (src/va_env.jl:57-68,
+    ChainRules' pow gradient): p*y/x away from x = 0; at x = 0, 0 for p = 0 or
+    p > 1, 1 for p = 1, +inf for 0 < p < 1.  The base sqrt(V^2 + 0.01) - 0.1 at
+    V = 1e-10 rounds to exactly 0 while its own partial (1e-9) does not, which
+    is how BSIM-CMG's smoothed V_ds reaches pow(vdsx, DVTP1 = 0): x^0 must have
+    zero partials there, not 0 * inf = NaN."""
+    import importlib
+    P = importlib.import_module("cedarsim_gb300.va.parser")
+    E = importlib.import_module("cedarsim_gb300.va.emit")
+    src = """module pw(a, b, c, d, e, f); inout a, b, c, d, e, f; electrical a, b, c, d, e, f;
+      analog begin
+        I(a) <+ 1e-3 * pow(sqrt(V(a) * V(a) + 0.01) - 0.1, 0.0);
+        I(b) <+ 1e-3 * pow(sqrt(V(b) * V(b) + 0.01) - 0.1, 1.0);
+        I(c) <+ 1e-3 * pow(sqrt(V(c) * V(c) + 0.01) - 0.1, 2.0);
+        I(d) <+ 1e-3 * pow(sqrt(V(d) * V(d) + 0.01) - 0.1, 0.5);
+        I(e) <+ 1e-3 * pow(V(e), 3.0);
+        I(f) <+ 1e-3 * pow(V(f), 0.0);
+      end endmodule"""
+    mods = [E.analyze(m) for m in P.parse(src)]
+    (tmp_path / "va_models.gen.h").write_text(E.emit_header(mods, 11))
+    (tmp_path / "h.cpp").write_text('#include <math.h>\n#include "va_models.gen.h"\n'
+                                    'extern "C" void h(const double *dp, const double *v, double *fi, double *fq, '
+                                    'double *G, double *C) { cedar::va::full(0, dp, 1, v, 1e-12, fi, fq, G, C); }\n')
+    r = subprocess.run(["g++", "-O1", "-std=c++17", "-shared", "-fPIC", "-I", str(CSRC), "-I", str(tmp_path),
+                        str(tmp_path / "h.cpp"), "-o", str(tmp_path / "h.so")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-1500:]
+    lib = C.CDLL(str(tmp_path / "h.so"))
+    dp_ = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    vs = 1e-10
+    assert np.sqrt(vs * vs + 0.01) - 0.1 == 0.0                 # the base rounds to exactly 0
+    dbase = vs / np.sqrt(vs * vs + 0.01)                         # ... but moves with V
+    dp, v = np.array([1.0, VT]), np.array([vs, vs, vs, vs, 0.7, 0.0])
+    fi, fq, G, Cm = np.zeros(6), np.zeros(6), np.zeros(36), np.zeros(36)
+    lib.h(dp_(dp), dp_(v), dp_(fi), dp_(fq), dp_(G), dp_(Cm))
+    g = np.abs(np.diag(G.reshape(6, 6)))
+    assert g[0] == 0.0 and g[5] == 0.0                            # p = 0: x^0 is constant
+    assert g[1] == pytest.approx(1e-3 * dbase, rel=1e-15)         # p = 1: the base's own slope
+    assert g[2] == 0.0                                            # p = 2 at x = 0
+    assert np.isinf(g[3])                                         # p = 1/2 at x = 0
+    assert g[4] == pytest.approx(1e-3 * 3 * 0.7 ** 2, rel=1e-15)  # p y / x away from 0
+    spec = importlib.util.spec_from_file_location("cedar_va_interp_pw", ROOT / "oracle" / "va_interp.py")
+    vi = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(vi)
+    _, _, rG, _ = vi.evaluate(mods[0][0].module, {}, list(v), VT, 1e-12)
+    rg = np.abs(np.diag(np.asarray(rG, dtype=float)))
+    assert np.array_equal(np.isinf(rg), np.isinf(g))
+    fin = np.isfinite(g)
+    assert np.allclose(rg[fin], g[fin], rtol=1e-15, atol=0.0)
