@@ -146,19 +146,93 @@ def _stats_dict(st) -> dict:
     return {k: getattr(st, k) for k, _ in Stats._fields_ if k != "pad"}
 
 
-def dc(circuit: Union[Circuit, Flat, System, "CircuitSweep"], t: float = 0.0, x0: Optional[np.ndarray] = None, **kw):
+CEDAR_ENOCONV = -5          # include/cedar.h: Newton / DC operating point did not converge
+DC_START_SCALE = 1e-7       # the spread of a restart: x0 = 1e-7 * randn(n), as src/dcop.jl:62
+
+
+def dc_starts(n: int, seed: int = 0):
+    """The restart points of the multi-start DC solve: an endless sequence of
+    1e-7 * randn(n) vectors (src/dcop.jl:62) from a Philox generator keyed by
+    `seed`, so that a failed solve restarts from the same points on every run."""
+    rng = np.random.Generator(np.random.Philox(seed))
+    while True:
+        yield DC_START_SCALE * rng.standard_normal(n)
+
+
+def bootstrapped_dc(solve, x0: np.ndarray, trajectories: int = 10, seed: int = 0):
+    """CedarSim's bootstrapped_nlsolve (src/dcop.jl:53-94) around one DC solve.
+
+    `solve(x)` runs one DC solve in place on x and returns (rc, stats).  The
+    first trajectory starts from x0 (the caller's guess, zeros by default, where
+    the reference starts every trajectory from a random point: a solve from
+    zeros is kept first so that results where it converges do not depend on the
+    seed); each later one starts from the next point of dc_starts(n, seed).  A
+    trajectory that ends without convergence (CEDAR_ENOCONV: any non-OK status
+    of the solve, a zero pivot included, as the reference retries its
+    SingularException) moves on to the next start; any other return code ends
+    the loop at once (the caller raises it, as the reference rethrows).  Returns
+    (x, rc, stats of the last trajectory, trajectories run, DC iterations summed
+    over them); rc is CEDAR_ENOCONV if none converged."""
+    if trajectories < 1:
+        raise ValueError("trajectories must be at least 1")
+    x = np.ascontiguousarray(x0, np.float64).copy()
+    starts = dc_starts(x.size, seed)
+    iters = 0
+    for k in range(trajectories):
+        if k:
+            x = next(starts)
+        rc, st = solve(x)
+        iters += int(st.dc_iters)
+        if rc != CEDAR_ENOCONV:
+            return x, rc, st, k + 1, iters
+    return x, rc, st, trajectories, iters
+
+
+def batch_dc_restarts(x: np.ndarray, st: np.ndarray, n_of: np.ndarray, trajectories: int, seed: int, run_round):
+    """The restart rounds of a batched DC solve (bootstrapped_dc per instance).
+
+    x[n_inst, n_max] and st (STATS_DTYPE) hold the first solve of every instance,
+    n_of its unknown counts.  Each round solves the instances that have not
+    converged yet together, by run_round(idx, x0) -> (x_sub[len(idx), m], stats),
+    instance idx[j] starting from x0[j], its next point of dc_starts(n_i, seed + i);
+    at most trajectories - 1 rounds.  An instance's dc_iters add up over its
+    trajectories; its x, status and other stats are those of its last one.
+    Updates x and st in place and returns them."""
+    fail = np.flatnonzero(st["status"] != 0)
+    starts = {int(i): dc_starts(int(n_of[i]), seed + int(i)) for i in fail}
+    for _ in range(trajectories - 1):
+        if fail.size == 0:
+            break
+        xs, ss = run_round(fail, [next(starts[int(i)]) for i in fail])
+        ss = ss.copy()
+        ss["dc_iters"] += st["dc_iters"][fail]
+        x[fail, :xs.shape[1]] = xs
+        x[fail, xs.shape[1]:] = 0.0
+        st[fail] = ss
+        fail = fail[ss["status"] != 0]
+    return x, st
+
+
+def dc(circuit: Union[Circuit, Flat, System, "CircuitSweep"], t: float = 0.0, x0: Optional[np.ndarray] = None,
+       trajectories: int = 10, seed: int = 0, **kw):
     """DC operating point (CedarDCOp's role): Newton, then pseudo-transient continuation, then
-    source stepping; rerun with dense partial pivoting if the static pivot order fails.
-    Over a CircuitSweep this is the dc!. broadcast: every point in one batched launch,
-    keyword arguments as sweeps.sweep_dc."""
+    source stepping; rerun with dense partial pivoting if the static pivot order fails; a
+    solve that does not converge is restarted from up to trajectories - 1 random points
+    near zero (bootstrapped_dc).  Over a CircuitSweep this is the dc!. broadcast: every
+    point in one batched launch, keyword arguments as sweeps.sweep_dc."""
     if isinstance(circuit, CircuitSweep):
-        return sweep_dc(circuit, **kw)
+        return sweep_dc(circuit, trajectories=trajectories, seed=seed, **kw)
     if kw:
         raise TypeError(f"dc() of one circuit takes no options {sorted(kw)}")
     sys = circuit if isinstance(circuit, System) else System(circuit)
-    x = np.zeros(sys.n) if x0 is None else np.ascontiguousarray(x0, np.float64).copy()
-    st = Stats()
-    check(sys.lib.cedar_dcop(sys.handle, float(t), _dp(x), C.byref(st)))
+    x0 = np.zeros(sys.n) if x0 is None else x0
+
+    def solve(x):
+        st = Stats()
+        return sys.lib.cedar_dcop(sys.handle, float(t), _dp(x), C.byref(st)), st
+
+    x, rc, _, _, _ = bootstrapped_dc(solve, x0, trajectories, seed)
+    check(rc)
     return x
 
 
@@ -265,13 +339,50 @@ class Batch:
                                        st.ctypes.data_as(C.c_void_p)))
         return BatchResult(xf, samp, st)
 
-    def dc(self, reltol=1e-6, abstol_v=1e-9, **kw):
+    def dc(self, reltol=1e-6, abstol_v=1e-9, trajectories: int = 10, seed: int = 0, **kw):
         """DC operating point of every instance (dc!. over a CircuitSweep).
-        Returns (x_dc[n_inst, n_max], stats)."""
+        Instances whose solve does not converge are solved again, in one batched
+        launch per round, from random points near zero (up to trajectories - 1
+        rounds; instance i's k-th restart is point k of dc_starts(n_i, seed + i),
+        the bootstrapped_dc rule per instance).  stats[i].dc_iters sums the
+        iterations of every trajectory of instance i; stats[i].status is that of
+        its last one.  Returns (x_dc[n_inst, n_max], stats)."""
+        if trajectories < 1:
+            raise ValueError("trajectories must be at least 1")
         opts = make_opts("bdf2", True, 0.0, 1.0, 0.0, True, reltol, abstol_v, **kw)
         x = np.zeros((self.n_inst, self.n_max))
         st = np.zeros(self.n_inst, STATS_DTYPE)
         check(self.lib.cedar_batch_dcop(self.handle, C.byref(opts), _dp(x), st.ctypes.data_as(C.c_void_p)))
+        if trajectories == 1 or not np.any(st["status"] != 0):
+            return x, st
+        h = self.holder
+        n_of = np.array([t.n for t in self.templates])[h.inst_template]
+
+        def run_round(idx, x0):
+            off = np.concatenate([[0], np.cumsum([v.size for v in x0])[:-1]]).astype(np.int64)
+            sub = Batch(self.templates, h.inst_template[idx], h.inst_par,
+                        None if h.inst_par_off is None else h.inst_par_off[idx],
+                        inst_x0=np.concatenate(x0), inst_x0_off=off)
+            return sub.dc(reltol, abstol_v, trajectories=1, **kw)
+
+        return batch_dc_restarts(x, st, n_of, trajectories, seed, run_round)
+        h = self.holder
+        n_of = np.array([t.n for t in self.templates])[h.inst_template]
+        starts = {int(i): dc_starts(int(n_of[i]), seed + int(i)) for i in fail}
+        for _ in range(trajectories - 1):
+            if fail.size == 0:
+                break
+            x0 = [next(starts[int(i)]) for i in fail]
+            off = np.concatenate([[0], np.cumsum([v.size for v in x0])[:-1]]).astype(np.int64)
+            sub = Batch(self.templates, h.inst_template[fail], h.inst_par,
+                        None if h.inst_par_off is None else h.inst_par_off[fail],
+                        inst_x0=np.concatenate(x0), inst_x0_off=off)
+            xs, ss = sub.dc(reltol, abstol_v, trajectories=1, **kw)
+            ss["dc_iters"] += st["dc_iters"][fail]
+            x[fail, :sub.n_max] = xs
+            x[fail, sub.n_max:] = 0.0
+            st[fail] = ss
+            fail = fail[ss["status"] != 0]
         return x, st
 
     def tran(self, tspan, method="bdf2", reltol=1e-6, abstol_v=1e-9, dcop=True, **kw) -> BatchResult:
