@@ -213,18 +213,18 @@ VA_HD Dual<T, N> hypot(const Dual<T, N> &x, const Dual<T, N> &y) {
   for (int i = 0; i < N; ++i) r.d[i] = (x.v * x.d[i] + y.v * y.d[i]) / r.v;
   return r;
 }
-// d(x^p)/dx given y = x^p, by the rule CedarSim's pow derivative uses (its
-// frule, src/va_env.jl:57-68, calls ChainRules 1.69's pow gradient): p y / x
-// where x != 0 or p < 0; at x = 0, 1 for p = 1, 0 for p = 0 or p > 1, +inf
-// for 0 < p < 1.  So x^0 has zero partials everywhere (no 0 * inf at x = 0;
-// BSIM-CMG raises a smoothed V_ds that rounds to exactly 0 to the power DVTP1 = 0)
+// d(x^p)/dx.  CedarSim takes pow's derivative from ChainRules 1.69 (its pow
+// frule, src/va_env.jl:57-68): p y / x away from x = 0 and, at x = 0, 1 for
+// p = 1, 0 for p = 0 or p > 1, +inf for 0 < p < 1.  p x^(p-1) agrees with that
+// (away from 0 up to rounding) except for p = 0, where it is 0 * x^-1, NaN at
+// x = 0.  x^0 is constant, so its partials are 0 everywhere (BSIM-CMG raises a
+// smoothed V_ds that rounds to exactly 0 to the power DVTP1 = 0); any other p
+// takes p x^(p-1), which also keeps second derivatives of nested duals at
+// x = 0 (ddx of x^2).
 template <class T>
-VA_HD T pow_grad_x(const T &x, const T &p, const T &y) {
-  const double xv = val(x), pv = val(p);
-  if (xv != 0.0 || pv < 0.0) return p * y / x;
-  if (pv == 1.0) return T(1.0);
-  if (pv == 0.0 || pv > 1.0) return T(0.0);
-  return T(INFINITY);
+VA_HD T pow_grad_x(const T &x, const T &p) {
+  if (all_zero(p)) return T(0.0);
+  return p * pow(x, p - T(1.0));
 }
 // x^y: with a constant exponent the log term is left out (a strong zero, so a
 // negative base with an integral exponent keeps finite partials)
@@ -233,7 +233,7 @@ VA_HD Dual<T, N> pow(const Dual<T, N> &x, const Dual<T, N> &y) {
   const T p = pow(x.v, y.v);
   Dual<T, N> r;
   r.v = p;
-  const T dx = pow_grad_x(x.v, y.v, p);
+  const T dx = pow_grad_x(x.v, y.v);
   bool ycst = true;
   for (int i = 0; i < N; ++i)
     if (!all_zero(y.d[i])) ycst = false;

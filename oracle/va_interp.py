@@ -136,18 +136,15 @@ def _deriv(name, v):
     raise KeyError(name)
 
 
-def _pow_grad_x(x, p, y):
-    """d(x^p)/dx given y = x^p, as CedarSim's pow frule takes it (src/va_env.jl:57-68
-    calls ChainRules 1.69's pow gradient): p*y/x where x != 0 or p < 0; at x = 0,
-    1 for p = 1, 0 for p = 0 or p > 1, +inf for 0 < p < 1."""
-    xv, pv = value(x), value(p)
-    if xv != 0.0 or pv < 0.0:
-        return _fdiv(p * y, x)
-    if pv == 1.0:
-        return 1.0
-    if pv == 0.0 or pv > 1.0:
+def _pow_grad_x(x, p):
+    """d(x^p)/dx.  CedarSim's pow frule (src/va_env.jl:57-68) takes ChainRules 1.69's
+    pow gradient: p*y/x away from x = 0; at x = 0, 1 for p = 1, 0 for p = 0 or
+    p > 1, +inf for 0 < p < 1.  p*x^(p-1) agrees with it except for p = 0 (0 * inf
+    at x = 0): x^0 is constant, so its partials are 0; any other p takes
+    p*x^(p-1), which keeps second derivatives of nested duals at x = 0."""
+    if not _nonzero(p):
         return 0.0
-    return math.inf
+    return p * _pow(x, p - 1.0)
 
 
 def _pow(x, y):
@@ -162,7 +159,7 @@ def _pow(x, y):
     if not ydep:
         yv = y if not isinstance(y, D) else y.v
         base = _pow(x.v, yv)
-        return D(base, [_sz(_pow_grad_x(x.v, yv, base), a) for a in x.d])
+        return D(base, [_sz(_pow_grad_x(x.v, yv), a) for a in x.d])
     return _unary_fn("exp", y * _unary_fn("ln", x))
 
 

@@ -294,12 +294,12 @@ def test_strong_zero_partials(pkg, tmp_path):
 
 
 def test_pow_gradient_rule(pkg, tmp_path):
-    """d(x^p)/dx follows the rule of CedarSim's pow derivative (src/va_env.jl:57-68,
-    ChainRules' pow gradient): p*y/x away from x = 0; at x = 0, 0 for p = 0 or
-    p > 1, 1 for p = 1, +inf for 0 < p < 1.  The base sqrt(V^2 + 0.01) - 0.1 at
-    V = 1e-10 rounds to exactly 0 while its own partial (1e-9) does not, which
-    is how BSIM-CMG's smoothed V_ds reaches pow(vdsx, DVTP1 = 0): x^0 must have
-    zero partials there, not 0 * inf = NaN."""
+    """d(x^p)/dx takes the values of CedarSim's pow derivative (src/va_env.jl:57-68,
+    ChainRules' pow gradient): at x = 0, 0 for p = 0 or p > 1, 1 for p = 1, +inf
+    for 0 < p < 1, and p x^(p-1) away from 0.  The base sqrt(V^2 + 0.01) - 0.1
+    at V = 1e-10 rounds to exactly 0 while its own partial (1e-9) does not,
+    which is how BSIM-CMG's smoothed V_ds reaches pow(vdsx, DVTP1 = 0): x^0 must
+    have zero partials there, not 0 * inf = NaN."""
     import importlib
     P = importlib.import_module("cedarsim_gb300.va.parser")
     E = importlib.import_module("cedarsim_gb300.va.emit")
