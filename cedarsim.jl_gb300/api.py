@@ -366,24 +366,6 @@ class Batch:
             return sub.dc(reltol, abstol_v, trajectories=1, **kw)
 
         return batch_dc_restarts(x, st, n_of, trajectories, seed, run_round)
-        h = self.holder
-        n_of = np.array([t.n for t in self.templates])[h.inst_template]
-        starts = {int(i): dc_starts(int(n_of[i]), seed + int(i)) for i in fail}
-        for _ in range(trajectories - 1):
-            if fail.size == 0:
-                break
-            x0 = [next(starts[int(i)]) for i in fail]
-            off = np.concatenate([[0], np.cumsum([v.size for v in x0])[:-1]]).astype(np.int64)
-            sub = Batch(self.templates, h.inst_template[fail], h.inst_par,
-                        None if h.inst_par_off is None else h.inst_par_off[fail],
-                        inst_x0=np.concatenate(x0), inst_x0_off=off)
-            xs, ss = sub.dc(reltol, abstol_v, trajectories=1, **kw)
-            ss["dc_iters"] += st["dc_iters"][fail]
-            x[fail, :sub.n_max] = xs
-            x[fail, sub.n_max:] = 0.0
-            st[fail] = ss
-            fail = fail[ss["status"] != 0]
-        return x, st
 
     def tran(self, tspan, method="bdf2", reltol=1e-6, abstol_v=1e-9, dcop=True, **kw) -> BatchResult:
         return self.run(make_opts(method, True, tspan[0], tspan[1], 0.0, dcop, reltol, abstol_v, **kw))
