@@ -613,6 +613,158 @@ static bool compile_with(const cedar_ckt_desc *d, Template &T, std::string &err,
   return true;
 }
 
+// ------------------------------------------------------------- validation
+// Every index the kernels follow, checked against the extent of what it
+// indexes.  The kernels trust these tables (they carry no per-access bounds
+// checks on the hot path), so a compiler defect must stop here, on the host,
+// before anything is uploaded or launched.
+namespace {
+struct Checker {
+  std::string &err;
+  bool ok = true;
+  bool fail(const std::string &what) {
+    if (ok) err = "internal: template check failed: " + what;
+    ok = false;
+    return false;
+  }
+  // v[k] in [lo, hi) for every k
+  bool range(const std::vector<int32_t> &v, int64_t lo, int64_t hi, const char *name) {
+    for (size_t k = 0; k < v.size(); ++k)
+      if (v[k] < lo || v[k] >= hi)
+        return fail(std::string(name) + "[" + std::to_string(k) + "] = " + std::to_string(v[k]) + " outside [" +
+                    std::to_string(lo) + ", " + std::to_string(hi) + ")");
+    return true;
+  }
+  bool size(size_t got, size_t want, const char *name) {
+    if (got != want) return fail(std::string(name) + " has " + std::to_string(got) + " entries, expected " + std::to_string(want));
+    return true;
+  }
+  // a CSR-style pointer array: nslots + 1 entries, 0 first, nondecreasing, ends at total
+  bool ptr(const std::vector<int32_t> &p, size_t nslots, size_t total, const char *name) {
+    if (!size(p.size(), nslots + 1, name)) return false;
+    if (p[0] != 0 || (size_t)p[nslots] != total) return fail(std::string(name) + " does not span its entries");
+    for (size_t k = 0; k < nslots; ++k)
+      if (p[k + 1] < p[k]) return fail(std::string(name) + " decreases at " + std::to_string(k));
+    return true;
+  }
+  bool perm(const std::vector<int32_t> &v, int n, const char *name) {
+    if (!size(v.size(), (size_t)n, name) || !range(v, 0, n, name)) return false;
+    std::vector<char> seen(n, 0);
+    for (int32_t x : v) { if (seen[x]) return fail(std::string(name) + " is not a permutation"); seen[x] = 1; }
+    return true;
+  }
+  // a stamp program: per-slot gather lists of ((output << 1) | negate) entries
+  bool program(const std::vector<int32_t> &p, const std::vector<int32_t> &ent, size_t nslots, int n_out,
+               const char *name) {
+    if (!ptr(p, nslots, ent.size(), name)) return false;
+    for (size_t k = 0; k < ent.size(); ++k)
+      if (ent[k] < 0 || (ent[k] >> 1) >= n_out) return fail(std::string(name) + " entry " + std::to_string(k) + " names no device output");
+    return true;
+  }
+  // level-scheduled row tasks (substitutions): a permutation of the rows in
+  // levels, each with its (LU slot, column) pairs
+  bool rows(const std::vector<int32_t> &lvl, const std::vector<int32_t> &row, const std::vector<int32_t> &p,
+            const std::vector<int32_t> &lu, const std::vector<int32_t> &col, int n, int nnz_lu, const char *name) {
+    if (lvl.empty() || lvl.front() != 0 || (size_t)lvl.back() != row.size()) return fail(std::string(name) + " levels do not span the rows");
+    for (size_t l = 0; l + 1 < lvl.size(); ++l)
+      if (lvl[l + 1] < lvl[l]) return fail(std::string(name) + " levels decrease");
+    return perm(row, n, name) && ptr(p, row.size(), lu.size(), name) && size(col.size(), lu.size(), name) &&
+           range(lu, 0, nnz_lu, name) && range(col, 0, n, name);
+  }
+};
+}  // namespace
+
+bool validate_template(const Template &T, std::string &err) {
+  Checker c{err};
+  const int n = T.n, nnz = T.nnz_lu;
+  if (n <= 0 || n != T.n_nodes + T.n_branch) return c.fail("unknown counts");
+  // device groups and their slices of the terminal, parameter and output blocks
+  int term = 0, par = 0, dpar = 0, out = 0;
+  for (const GroupInfo &g : T.groups) {
+    if (g.model <= 0 || g.model >= num_models() || g.n_inst < 0) return c.fail("group model or size");
+    const ModelInfo &mi = model_info(g.model);
+    if (g.ntx != mi.nterm + mi.has_br || g.term_off != term || g.par_off != par || g.dpar_off != dpar || g.out_off != out)
+      return c.fail("group offsets");
+    term += g.ntx * g.n_inst; par += mi.npar * g.n_inst; dpar += mi.ndpar * g.n_inst; out += mi.nout * g.n_inst;
+  }
+  if (par != T.par_size || dpar != T.dpar_size || out != T.n_out) return c.fail("block sizes");
+  if (!c.size(T.term_orig.size(), (size_t)term, "term_orig") || !c.size(T.term_int.size(), (size_t)term, "term_int") ||
+      !c.range(T.term_orig, -1, n, "term_orig") || !c.range(T.term_int, -1, n, "term_int") ||
+      !c.size(T.par.size(), (size_t)T.par_size, "par") || !c.size(T.out_q.size(), (size_t)std::max(T.n_out, 1), "out_q"))
+    return false;
+  // orderings
+  if (!c.perm(T.rowmatch, n, "rowmatch") || !c.perm(T.order, n, "order") || !c.perm(T.iorder, n, "iorder") ||
+      !c.perm(T.eq_pos, n, "eq_pos") || !c.size(T.is_node_int.size(), (size_t)n, "is_node_int"))
+    return false;
+  for (int p = 0; p < n; ++p)
+    if (T.iorder[T.order[p]] != p) return c.fail("iorder is not the inverse of order");
+  // J pattern (original CSC) and LU pattern (internal CSR, sorted, with diagonals)
+  const size_t ncsc = T.j_rowidx.size();
+  if (!c.ptr(T.j_colptr, n, ncsc, "j_colptr") || !c.range(T.j_rowidx, 0, n, "j_rowidx") ||
+      !c.ptr(T.lu_rowptr, n, (size_t)nnz, "lu_rowptr") || !c.size(T.lu_colidx.size(), (size_t)nnz, "lu_colidx") ||
+      !c.range(T.lu_colidx, 0, n, "lu_colidx") || !c.size(T.lu_diag.size(), (size_t)n, "lu_diag"))
+    return false;
+  for (int p = 0; p < n; ++p) {
+    for (int k = T.lu_rowptr[p] + 1; k < T.lu_rowptr[p + 1]; ++k)
+      if (T.lu_colidx[k] <= T.lu_colidx[k - 1]) return c.fail("lu_colidx unsorted in row " + std::to_string(p));
+    const int d = T.lu_diag[p];
+    if (d < T.lu_rowptr[p] || d >= T.lu_rowptr[p + 1] || T.lu_colidx[d] != p) return c.fail("lu_diag of row " + std::to_string(p));
+  }
+  // stamp programs
+  if (!c.program(T.jlu_ptr, T.jlu_ent, (size_t)nnz, T.n_out, "jlu") ||
+      !c.program(T.jcsc_ptr, T.jcsc_ent, ncsc, T.n_out, "jcsc") ||
+      !c.program(T.fint_ptr, T.fint_ent, (size_t)n, T.n_out, "fint") ||
+      !c.program(T.qint_ptr, T.qint_ent, (size_t)n, T.n_out, "qint") ||
+      !c.program(T.forg_ptr, T.forg_ent, (size_t)n, T.n_out, "forg") ||
+      !c.program(T.ct_ptr, T.ct_ent, (size_t)n, T.n_out, "ct") || !c.size(T.ct_row.size(), T.ct_ent.size(), "ct_row") ||
+      !c.range(T.ct_row, 0, n, "ct_row"))
+    return false;
+  // long gather lists and their chunk offsets
+  if (!c.range(T.long_lu, 0, nnz, "long_lu") || !c.range(T.long_fi, 0, n, "long_fi") ||
+      !c.range(T.long_jc, 0, (int64_t)ncsc, "long_jc") || !c.range(T.long_fo, 0, n, "long_fo"))
+    return false;
+  {
+    const size_t nl = T.long_jc.size() + T.long_fo.size();
+    if (!c.size(T.long_jc_fo_off.size(), nl + 1, "long_jc_fo_off") || T.long_jc_fo_off[0] != 0) return c.fail("long_jc_fo_off");
+    for (size_t k = 0; k < nl; ++k) {
+      const bool jc = k < T.long_jc.size();
+      const int q = jc ? T.long_jc[k] : T.long_fo[k - T.long_jc.size()];
+      const int len = jc ? T.jcsc_ptr[q + 1] - T.jcsc_ptr[q] : T.forg_ptr[q + 1] - T.forg_ptr[q];
+      if (T.long_jc_fo_off[k + 1] - T.long_jc_fo_off[k] != (len + kLongChunk - 1) / kLongChunk)
+        return c.fail("long_jc_fo_off chunk count of list " + std::to_string(k));
+    }
+  }
+  // factorisation tasks by level
+  const size_t nt = T.lu_task_slot.size();
+  if (T.lu_lvl_ptr.empty() || T.lu_lvl_ptr.front() != 0 || (size_t)T.lu_lvl_ptr.back() != nt) return c.fail("lu levels do not span the tasks");
+  for (size_t l = 0; l + 1 < T.lu_lvl_ptr.size(); ++l)
+    if (T.lu_lvl_ptr[l + 1] < T.lu_lvl_ptr[l]) return c.fail("lu levels decrease");
+  if (!c.size(nt, (size_t)nnz, "lu_task_slot") || !c.perm(T.lu_task_slot, nnz, "lu_task_slot") ||
+      !c.size(T.lu_task_info.size(), nt, "lu_task_info") || !c.ptr(T.lu_pair_ptr, nt, T.lu_pair_a.size(), "lu_pair_ptr") ||
+      !c.size(T.lu_pair_b.size(), T.lu_pair_a.size(), "lu_pair_b") || !c.range(T.lu_pair_a, 0, nnz, "lu_pair_a") ||
+      !c.range(T.lu_pair_b, 0, nnz, "lu_pair_b"))
+    return false;
+  for (size_t t = 0; t < nt; ++t) {
+    const int kind = T.lu_task_info[t] & 3, col = T.lu_task_info[t] >> 2;
+    if (kind == 3 || col < 0 || col >= n) return c.fail("lu_task_info of task " + std::to_string(t));
+  }
+  // substitutions, forward / backward and transposed
+  if (!c.rows(T.fw_lvl_ptr, T.fw_row, T.fw_ptr, T.fw_lu, T.fw_col, n, nnz, "fw") ||
+      !c.rows(T.bw_lvl_ptr, T.bw_row, T.bw_ptr, T.bw_lu, T.bw_col, n, nnz, "bw") ||
+      !c.rows(T.tf_lvl_ptr, T.tf_row, T.tf_ptr, T.tf_lu, T.tf_col, n, nnz, "tf") ||
+      !c.rows(T.tb_lvl_ptr, T.tb_row, T.tb_ptr, T.tb_lu, T.tb_col, n, nnz, "tb"))
+    return false;
+  // adjoint parameter offsets, time-varying sources, gmin-stepping slots
+  if (!c.size(T.adj_goff.size(), T.groups.size(), "adj_goff") || !c.range(T.adj_goff, -1, (int64_t)T.n_adj + 1, "adj_goff") ||
+      !c.size(T.src_inst.size(), T.src_group.size(), "src_inst") ||
+      !c.range(T.src_group, 0, (int64_t)T.groups.size(), "src_group") || !c.size(T.gs_slot.size(), (size_t)T.n_nodes, "gs_slot") ||
+      !c.range(T.gs_slot, 0, nnz, "gs_slot"))
+    return false;
+  for (size_t k = 0; k < T.src_inst.size(); ++k)
+    if (T.src_inst[k] < 0 || T.src_inst[k] >= T.groups[T.src_group[k]].n_inst) return c.fail("src_inst");
+  return true;
+}
+
 bool compile_template(const cedar_ckt_desc *d, Template &T, std::string &err, int ordering) {
   if (ordering == ORDER_AUTO) {
     Template A, B;
@@ -621,11 +773,11 @@ bool compile_template(const cedar_ckt_desc *d, Template &T, std::string &err, in
     A.sched_cost = schedule_cost(A);
     B.sched_cost = schedule_cost(B);
     T = (B.sched_cost < A.sched_cost) ? std::move(B) : std::move(A);
-    return true;
+  } else {
+    if (!compile_with(d, T, err, ordering)) return false;
+    T.sched_cost = schedule_cost(T);
   }
-  if (!compile_with(d, T, err, ordering)) return false;
-  T.sched_cost = schedule_cost(T);
-  return true;
+  return validate_template(T, err);
 }
 
 }  // namespace cedar

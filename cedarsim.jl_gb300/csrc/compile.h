@@ -107,7 +107,15 @@ constexpr int kLongChunk = 256;
 // Ordering strategies for the fill-reducing symmetric permutation.
 enum Ordering { ORDER_AUTO = 0, ORDER_MIN_DEGREE = 1, ORDER_NESTED_DISSECTION = 2, ORDER_NATURAL = 3 };
 
+// Compiles and then validates the template (validate_template); false with err
+// set if either fails.
 bool compile_template(const cedar_ckt_desc *d, Template &T, std::string &err,
                       int ordering = ORDER_AUTO);
+
+// Checks every index array of a compiled template against the extent it
+// indexes (device outputs, unknowns, J and LU slots, levels, permutations).
+// The engine kernels index with these tables unchecked; this is their bounds
+// check, run on the host before anything is uploaded.
+bool validate_template(const Template &T, std::string &err);
 
 }  // namespace cedar
