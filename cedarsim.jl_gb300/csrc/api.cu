@@ -7,6 +7,7 @@
 #include <memory>
 #include <string>
 #include <vector>
+#include <nvtx3/nvToolsExt.h>
 #include "compile.h"
 #include "kernels.cuh"
 // per-model FP64 operation counts of one device evaluation (written by build.py)
@@ -23,6 +24,17 @@ namespace {
 thread_local std::string g_err;
 
 int fail(int code, const std::string &msg) { g_err = msg; return code; }
+
+// An NVTX range named after the entry point around each call that runs work on
+// the device, so that a profiler's timeline (Nsight Systems, ncu --nvtx) groups
+// the kernels and copies by C-ABI call; without a profiler attached it does
+// nothing.
+struct Range {
+  explicit Range(const char *name) { nvtxRangePushA(name); }
+  ~Range() { nvtxRangePop(); }
+  Range(const Range &) = delete;
+  Range &operator=(const Range &) = delete;
+};
 #define CUDA_TRY(expr)                                                                      \
   do {                                                                                      \
     cudaError_t _e = (expr);                                                                \
@@ -349,6 +361,7 @@ void cedar_tran_opts_default(cedar_tran_opts *o) {
 }
 
 int cedar_ckt_create(const cedar_ckt_desc *desc, cedar_ckt **out) {
+  const Range nvtx_range("cedar_ckt_create");
   if (!desc || !out) return fail(CEDAR_EINVAL, "null argument");
   *out = nullptr;
   auto c = std::make_unique<cedar_ckt>();
@@ -477,6 +490,7 @@ int cedar_ckt_stream(const cedar_ckt *c, void **stream) {
 }
 
 int cedar_eval_dev(cedar_ckt *c, const double *x, const double *xdot, double t, double cj, double *F, double *J) {
+  const Range nvtx_range("cedar_eval_dev");
   if (!c || !x) return fail(CEDAR_EINVAL, "null argument");
   if (c->host_only) return fail(CEDAR_EINVAL, "host-only plan handle");
   CUDA_TRY(launch_eval(c->tpl->D, c->tpl->D_dev, c->dpar.p, x, xdot, t, cj, c->dout.p, c->part.p, F, J, c->stream));
@@ -523,6 +537,7 @@ int cedar_eval_dev_noalloc(cedar_ckt *c, const double *x, const double *xdot, do
 }
 
 int cedar_eval(cedar_ckt *c, const double *x, const double *xdot, double t, double cj, double *F, double *J) {
+  const Range nvtx_range("cedar_eval");
   if (!c || !x) return fail(CEDAR_EINVAL, "null argument");
   if (c->host_only) return fail(CEDAR_EINVAL, "host-only plan handle");
   const Template &H = c->tpl->H;
@@ -598,11 +613,13 @@ static int run_plain(cedar_ckt *c, int mode, const cedar_tran_opts *opts, double
 }
 
 int cedar_newton_solve(cedar_ckt *c, double t, double cj, const double *hist, double *x, cedar_stats *stats) {
+  const Range nvtx_range("cedar_newton_solve");
   if (!c || !x) return fail(CEDAR_EINVAL, "null argument");
   return run_plain(c, 1, nullptr, t, cj, hist, x, nullptr, nullptr, 0, nullptr, stats);
 }
 
 int cedar_dcop(cedar_ckt *c, double t, double *x, cedar_stats *stats) {
+  const Range nvtx_range("cedar_dcop");
   if (!c || !x) return fail(CEDAR_EINVAL, "null argument");
   return run_plain(c, 2, nullptr, t, 0.0, nullptr, x, nullptr, nullptr, 0, nullptr, stats);
 }
@@ -669,6 +686,7 @@ static int run_tran_warp(cedar_ckt *c, const cedar_tran_opts *opts, double *x, d
 
 int cedar_tran_run(cedar_ckt *c, const cedar_tran_opts *opts, const double *x0, double *t_out, double *x_out,
                    int64_t cap, int64_t *n_out, cedar_stats *stats) {
+  const Range nvtx_range("cedar_tran_run");
   if (!c || !x0) return fail(CEDAR_EINVAL, "null argument");
   int rc = check_opts(opts); if (rc) return rc;
   if (c->host_only) return fail(CEDAR_EINVAL, "host-only plan handle");
@@ -791,6 +809,7 @@ int ac_run(cedar_ckt *c, AcDev &a, bool noise, int32_t *status) {
 
 int cedar_ac(cedar_ckt *c, const double *x_op, const double *b, int32_t n_freq, const double *omega,
              int32_t n_probe, const int32_t *probe, double *resp, int32_t *status) {
+  const Range nvtx_range("cedar_ac");
   if (!c || !x_op || !b || (n_freq > 0 && (!omega || !resp)) || !probe) return fail(CEDAR_EINVAL, "null argument");
   if (c->host_only) return fail(CEDAR_EINVAL, "host-only plan handle");
   if (n_freq < 0 || n_probe <= 0) return fail(CEDAR_EINVAL, "n_freq must be >= 0 and n_probe > 0");
@@ -816,6 +835,7 @@ int cedar_ac(cedar_ckt *c, const double *x_op, const double *b, int32_t n_freq, 
 
 int cedar_noise(cedar_ckt *c, const double *x_op, int32_t n_freq, const double *omega, int32_t probe, double *psd,
                 int32_t *status) {
+  const Range nvtx_range("cedar_noise");
   if (!c || !x_op || (n_freq > 0 && (!omega || !psd))) return fail(CEDAR_EINVAL, "null argument");
   if (c->host_only) return fail(CEDAR_EINVAL, "host-only plan handle");
   const Template &H = c->tpl->H;
@@ -912,6 +932,7 @@ int cedar_ac_last_stats(const cedar_ckt *c, int32_t *n_dense, double *ms_sparse,
 
 // ------------------------------------------------------------------ batch
 int cedar_batch_create(const cedar_batch_desc *d, cedar_batch **out) {
+  const Range nvtx_range("cedar_batch_create");
   if (!d || !out) return fail(CEDAR_EINVAL, "null argument");
   *out = nullptr;
   if (d->n_templates <= 0 || d->n_inst < 0 || !d->templates || (d->n_inst > 0 && !d->inst_template))
@@ -1134,6 +1155,7 @@ int cedar_batch_last_ms(cedar_batch *b, double *ms) {
 }
 
 int cedar_batch_start(cedar_batch *b, const cedar_tran_opts *opts) {
+  const Range nvtx_range("cedar_batch_start");
   if (!b) return fail(CEDAR_EINVAL, "null handle");
   int rc = check_opts(opts); if (rc) return rc;
   b->run_opts = to_eng(opts);
@@ -1144,6 +1166,7 @@ int cedar_batch_start(cedar_batch *b, const cedar_tran_opts *opts) {
 }
 
 int cedar_batch_advance(cedar_batch *b, double t_until, int32_t *n_running) {
+  const Range nvtx_range("cedar_batch_advance");
   if (!b) return fail(CEDAR_EINVAL, "null handle");
   if (!b->started) return fail(CEDAR_EINVAL, "cedar_batch_start was not called");
   int rc;
@@ -1158,6 +1181,7 @@ int cedar_batch_advance(cedar_batch *b, double t_until, int32_t *n_running) {
 }
 
 int cedar_batch_dcop(cedar_batch *b, const cedar_tran_opts *opts, double *x_dc, cedar_stats *stats) {
+  const Range nvtx_range("cedar_batch_dcop");
   if (!b) return fail(CEDAR_EINVAL, "null handle");
   cedar_tran_opts o;
   cedar_tran_opts_default(&o);
@@ -1177,6 +1201,7 @@ int cedar_batch_dcop(cedar_batch *b, const cedar_tran_opts *opts, double *x_dc, 
 }
 
 int cedar_batch_results(cedar_batch *b, double *x_final, double *samples, cedar_stats *stats) {
+  const Range nvtx_range("cedar_batch_results");
   if (!b) return fail(CEDAR_EINVAL, "null handle");
   if (x_final) CUDA_TRY(cudaMemcpyAsync(x_final, b->xfinal.p, (size_t)b->n_inst * b->n_max * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
   if (samples && b->np) CUDA_TRY(cudaMemcpyAsync(samples, b->samples.p, (size_t)b->n_inst * b->np * b->ns * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
@@ -1186,6 +1211,7 @@ int cedar_batch_results(cedar_batch *b, double *x_final, double *samples, cedar_
 }
 
 int cedar_batch_run(cedar_batch *b, const cedar_tran_opts *opts, double *x_final, double *samples, cedar_stats *stats) {
+  const Range nvtx_range("cedar_batch_run");
   if (!b) return fail(CEDAR_EINVAL, "null handle");
   int rc = check_opts(opts); if (rc) return rc;
   if (b->n_inst == 0) return 0;
@@ -1212,6 +1238,7 @@ int cedar_adjoint_nparams(const cedar_batch *b, int32_t *np_per_template, int32_
 
 int cedar_adjoint_run(cedar_batch *b, const cedar_tran_opts *opts, const cedar_objective *obj, const double *tstar,
                       int64_t tape_cap, double *phi, double *grad, int32_t *status, cedar_stats *stats) {
+  const Range nvtx_range("cedar_adjoint_run");
   if (!b || !obj) return fail(CEDAR_EINVAL, "null argument");
   int rc = check_opts(opts); if (rc) return rc;
   if (!opts->adaptive || opts->method != CEDAR_BDF2)
@@ -1321,6 +1348,7 @@ int cedar_fp64_latency(int32_t iters, double *cycles_per_op, double *ns_per_op) 
 }
 
 int cedar_batch_autotune(cedar_batch *b, const cedar_tran_opts *opts, double horizon, cedar_batch_tuning *best) {
+  const Range nvtx_range("cedar_batch_autotune");
   if (!b) return fail(CEDAR_EINVAL, "null handle");
   int rc = check_opts(opts); if (rc) return rc;
   cedar_tran_opts o = *opts;
