@@ -21,6 +21,15 @@ ANSWERS = {
     "butterworth": {"rms": 0.5, "max_abs_err": 1e-6, "src": "test/transients.jl:152-156"},
     "ddx": {"V1_I": -5.0 * 2 * 2 * 3, "src": "test/ddx.jl:21"},
     "sensitivity": {"dR1_over_V": -0.5, "src": "test/sensitivity.jl:40-41"},
+    # ParamSim overrides: V = 5 across R (default 2, overridden to 1) -> V.I = -5;
+    # the SPICE deck i1 vcc 0 'foo', l1 vcc out 1m, r1 out 0 r='foo+2000' (params
+    # foo = 1 and a subcircuit default foo + 2000): V(r1) after overriding the
+    # subcircuit's foo to 2, the global foo to 2, and r1.r to 100
+    "params": {"V_I": -5.0, "r1_V": {"sub_foo_2": -2.0, "foo_2": -4004.0, "r_100": -100.0},
+               "src": "test/params.jl:19,34,46,87-99"},
+    # subcircuit net naming: i1 0 d 1 into a 1 Ohm resistor to ground (the
+    # subcircuit's own d tied to ground is a different net) -> i1 carries 1 A
+    "subckt_nets": {"i1_I": 1.0, "src": "test/compilation.jl:58-79"},
 }
 
 if __name__ == "__main__":

@@ -137,3 +137,46 @@ def test_sensitivity_closed_form(pkg, oracle):
     d1 = (vout(1 + d, 1) - vout(1 - d, 1)) / (2 * d)
     d2 = (vout(1, 1 + d) - vout(1, 1 - d)) / (2 * d)
     assert close(d1, -d2, 1e-8) and close(d1, -v / 2, 1e-8)
+
+
+def test_param_overrides(pkg, oracle):
+    """test/params.jl: parameter overrides of a built circuit (ParamSim's role,
+    here Circuit.altered).  ParCir (V = 5 across R = 2) with R overridden to 1
+    gives V.I = -5; the SPICE deck `i1 vcc 0 'foo'`, `l1 vcc out 1m` and a
+    nested subcircuit resistor r1 from out to ground with r = 'foo' and the
+    subcircuit default foo = foo + 2000 (global foo = 1) gives V(r1) = -2 with the
+    subcircuit's foo set to 2, -4004 with the global foo set to 2, and -100 with
+    r1.r set to 100.  The decks' parameter expressions are evaluated here (the
+    netlist front end is not part of this path)."""
+    g = GOLD["params"]
+    par = pkg.Circuit()
+    par.V("V", "vcc", "gnd", dc=5.0)
+    par.R("R", "vcc", "gnd", r=2.0)
+    f = par.altered({"R.r": 1.0}).flatten()
+    x, st, rc = oracle.dcop(f)
+    assert rc == 0 and close(x[f.index("V.I")], g["V_I"])
+
+    def deck(foo=1.0, sub_foo=None):
+        c = pkg.Circuit()
+        c.I("i1", "vcc", "0", dc=foo)
+        c.L("l1", "vcc", "out", 1e-3)
+        c.R("x1.x1.r1", "out", "0", r=(foo + 2000.0) if sub_foo is None else sub_foo)
+        return c
+    decks = {"sub_foo_2": deck(sub_foo=2.0), "foo_2": deck(foo=2.0), "r_100": deck().altered({"x1.x1.r1.r": 100.0})}
+    for key, c in decks.items():
+        f = c.flatten()
+        x, st, rc = oracle.dcop(f)
+        assert rc == 0 and close(x[f.index("out")], g["r1_V"][key]), key
+
+
+def test_subcircuit_nets(pkg, oracle):
+    """test/compilation.jl:58-79: `i1 0 d 1` into a subcircuit whose own d net is
+    tied to ground (r1 from that ground to d, 1 Ohm; r2 from ground to ground):
+    the nets stay distinct, so i1 carries its 1 A through r1 (V(d) = 1 V)."""
+    c = pkg.Circuit()
+    c.I("i1", "0", "d", dc=1.0)
+    c.R("x1.r1", "0", "d", r=1.0)
+    c.R("x1.r2", "0", "0", r=2.0)
+    f = c.flatten()
+    x, st, rc = oracle.dcop(f)
+    assert rc == 0 and close(x[f.index("d")] / 1.0, GOLD["subckt_nets"]["i1_I"])
