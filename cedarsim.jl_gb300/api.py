@@ -40,6 +40,15 @@ def _dp(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
 
+def _state(x, n: int) -> np.ndarray:
+    """x as a contiguous float64 vector of the circuit's n unknowns (the library
+    reads exactly n values from it)."""
+    x = np.ascontiguousarray(x, np.float64).ravel()
+    if x.size != n:
+        raise ValueError(f"state has {x.size} values, the circuit has {n} unknowns")
+    return x
+
+
 class System:
     """A compiled circuit on the GPU (the counterpart of CircuitIRODESystem)."""
 
@@ -80,22 +89,26 @@ class System:
 
     # ---- DAECompiler-style residual / Jacobian
     def f(self, out: np.ndarray, du: Optional[np.ndarray], u: np.ndarray, t: float) -> np.ndarray:
-        u = np.ascontiguousarray(u, np.float64)
-        du = None if du is None else np.ascontiguousarray(du, np.float64)
+        u = _state(u, self.n)
+        du = None if du is None else _state(du, self.n)
+        if out.dtype != np.float64 or not out.flags.c_contiguous or out.size != self.n:
+            raise ValueError(f"out must be a contiguous float64 array of {self.n} values")
         check(self.lib.cedar_eval(self.handle, _dp(u), None if du is None else _dp(du), float(t), 0.0, _dp(out), None))
         return out
 
     def jac(self, J: np.ndarray, du: Optional[np.ndarray], u: np.ndarray, gamma: float, t: float) -> np.ndarray:
         """J (CSC values in pattern() order) = dF/du + gamma dF/du'."""
-        u = np.ascontiguousarray(u, np.float64)
+        u = _state(u, self.n)
+        if J.dtype != np.float64 or not J.flags.c_contiguous or J.size != self.nnz_j:
+            raise ValueError(f"J must be a contiguous float64 array of {self.nnz_j} values")
         check(self.lib.cedar_eval(self.handle, _dp(u), None, float(t), float(gamma), None, _dp(J)))
         return J
 
     def eval(self, u, du=None, t=0.0, gamma=0.0):
         F = np.zeros(self.n)
         J = np.zeros(self.nnz_j)
-        u = np.ascontiguousarray(u, np.float64)
-        du = None if du is None else np.ascontiguousarray(du, np.float64)
+        u = _state(u, self.n)
+        du = None if du is None else _state(du, self.n)
         check(self.lib.cedar_eval(self.handle, _dp(u), None if du is None else _dp(du), float(t), float(gamma),
                                   _dp(F), _dp(J)))
         return F, J
@@ -108,9 +121,9 @@ class System:
         return M
 
     def newton_solve(self, t: float, cj: float, hist: Optional[np.ndarray], x: np.ndarray):
-        x = np.ascontiguousarray(x, np.float64).copy()
+        x = _state(x, self.n).copy()
         st = Stats()
-        hist = None if hist is None else np.ascontiguousarray(hist, np.float64)
+        hist = None if hist is None else _state(hist, self.n)
         rc = self.lib.cedar_newton_solve(self.handle, float(t), float(cj), None if hist is None else _dp(hist), _dp(x),
                                          C.byref(st))
         return x, st, rc
@@ -225,7 +238,7 @@ def dc(circuit: Union[Circuit, Flat, System, "CircuitSweep"], t: float = 0.0, x0
     if kw:
         raise TypeError(f"dc() of one circuit takes no options {sorted(kw)}")
     sys = circuit if isinstance(circuit, System) else System(circuit)
-    x0 = np.zeros(sys.n) if x0 is None else x0
+    x0 = np.zeros(sys.n) if x0 is None else _state(x0, sys.n)
 
     def solve(x):
         st = Stats()
@@ -248,7 +261,7 @@ def tran(circuit: Union[Circuit, Flat, System, "CircuitSweep"], tspan: Tuple[flo
     if adaptive is None:
         adaptive = h is None
     opts = make_opts(method, adaptive, tspan[0], tspan[1], h or 0.0, dcop, reltol, abstol_v, abstol_i, **kw)
-    x = np.zeros(sys.n) if x0 is None else np.ascontiguousarray(x0, np.float64).copy()
+    x = np.zeros(sys.n) if x0 is None else _state(x0, sys.n).copy()
     t_out = np.zeros(cap)
     x_out = np.zeros((cap, sys.n))
     n_out = C.c_int64()
