@@ -7,7 +7,10 @@
 #include <memory>
 #include <string>
 #include <vector>
+#if __has_include(<nvtx3/nvToolsExt.h>)
 #include <nvtx3/nvToolsExt.h>
+#define CEDAR_NVTX 1
+#endif
 #include "compile.h"
 #include "kernels.cuh"
 // per-model FP64 operation counts of one device evaluation (written by build.py)
@@ -28,10 +31,14 @@ int fail(int code, const std::string &msg) { g_err = msg; return code; }
 // An NVTX range named after the entry point around each call that runs work on
 // the device, so that a profiler's timeline (Nsight Systems, ncu --nvtx) groups
 // the kernels and copies by C-ABI call; without a profiler attached it does
-// nothing.
+// nothing, and a toolkit without the NVTX headers builds it as nothing.
 struct Range {
+#ifdef CEDAR_NVTX
   explicit Range(const char *name) { nvtxRangePushA(name); }
   ~Range() { nvtxRangePop(); }
+#else
+  explicit Range(const char *) {}
+#endif
   Range(const Range &) = delete;
   Range &operator=(const Range &) = delete;
 };
