@@ -1163,6 +1163,61 @@ int oracle_va_noise(int k, const double *dp, const double *v, double gmin, doubl
   return cedar::va::noise(k, dp, 1, v, gmin, pw, ex);
 }
 
+// SimpleDiode (src/simpledevices.jl:134-271), restated line by line with its
+// defects, at one junction voltage Vd.  PARITY UNPINNED: no reference test
+// solves a circuit with it (test/basic.jl:456-468 only constructs it), and the
+// reference's own behaviour at run time is what this restates:
+//   q = -1.602176634e-19 (sign flipped, :222), T = 300 K, AREAeff = AREA * M (:226);
+//   the breakdown branch reads the undefined NVt (:238) and the forward
+//   depletion branch the undefined MJI (:260): the reference throws
+//   UndefVarError there, returned here as codes 1 and 2;
+//   a negative argument of Base.sqrt (:249,251) throws DomainError (code 3);
+//   the `else -BVeff < Vd` line (:252) is an expression with no effect;
+//   Cdiffuse = TT * ddt(Ideff) / ddt(Vd) (:256) is a ratio of time
+//   derivatives: in DC both are 0 and it is TT * 0 / 0 (NaN); outside DC it is
+//   left to the caller (out[3] = TT, the factor of that ratio).
+// p: AREA BV BVJ CJO EG FC IBV IS KF M N RS TNOM TT VJ XTI (the struct's field
+// order, :135-150).  out: Id (after the gmin term), Ideff, Cdeplete_bw +
+// Cdeplete_sw, TT, Cdiffuse in DC.  Returns 0 or the error code.
+int oracle_simple_diode(const double *p, double Vd, double *out) {
+  const double AREA = p[0], BV = p[1], CJO = p[3], IBV = p[6], IS = p[7], M = p[9], N = p[10], TT = p[13],
+               VJ = p[14], FC = p[5];
+  const double MJ = M;
+  const double CJ0 = CJO;
+  const double GMIN = 1e-12, PJ = 0.0, PHP = 1.0, FCS = 0.5, JSW = 0.0, MJSW = 1.0 / 3.0;
+  const double IKF = INFINITY, IK = IKF, IKR = INFINITY;
+  const double q = -1.602176634e-19, k = 1.380649e-23, T = 300.0;
+  const double AREAeff = AREA * M, PJeff = PJ * M;
+  const double ISeff = IS * AREAeff + JSW * PJeff;
+  double IBVeff = IBV * AREAeff;
+  const double IKeff = IK * AREAeff, IKReff = IKR * AREAeff;
+  const double CJeff = CJ0 * AREAeff;
+  const double NkT = N * k * T;
+  const double Ibdwn = ISeff * expm1(-q * BV / NkT);
+  double BVeff;
+  if (IBVeff < Ibdwn) { IBVeff = Ibdwn; BVeff = BV; }
+  else return 1;                                   // BV - NVt * ln(IBVeff / Ibdwn): NVt undefined
+  double Id;
+  if (Vd >= -3 * NkT / q) Id = ISeff * expm1(q * Vd / NkT);
+  else if (-BVeff < Vd) { const double r = 3 * NkT / (q * Vd * M_E); Id = -ISeff * (1 + r * r * r); }
+  else Id = -ISeff * exp(-q * (BVeff + Vd) / NkT);
+  Id += Vd * GMIN;
+  double Ideff;
+  const double ratio = (Vd >= -3 * N * k * T / q) ? Id / IKeff : Id / IKReff;
+  if (ratio < 0) return 3;                         // Base.sqrt of a negative number
+  Ideff = Id / (1 + sqrt(ratio));
+  if (!(Vd < FC * VJ)) return 2;                   // CJeff * (1 - FC * (1 + MJI) + ...): MJI undefined
+  const double Cbw = CJeff * pow(1 - Vd / VJ, -MJ);
+  const double Csw = (Vd < FCS * PHP) ? CJeff * pow(1 - Vd / PHP, -MJSW)
+                                      : CJeff * (1 - FCS * (1 + MJSW) + MJSW * Vd / PHP) / pow(1 - FCS, 1 + MJSW);
+  out[0] = Id;
+  out[1] = Ideff;
+  out[2] = Cbw + Csw;
+  out[3] = TT;
+  out[4] = TT * 0.0 / 0.0;
+  return 0;
+}
+
 double oracle_next_breakpoint(const cedar_ckt_desc *d, double t, double eps) {
   Circuit c; if (!load_circuit(d, c, g_err)) return -1;
   return next_breakpoint(c, t, eps);

@@ -52,6 +52,8 @@ def load(pkg):
     lib.oracle_tran.restype = C.c_int
     lib.oracle_tran.argtypes = [C.POINTER(abi.CktDesc), C.POINTER(abi.TranOpts), dp, dp, dp, C.c_int64, ip,
                                 C.POINTER(abi.Stats)]
+    lib.oracle_simple_diode.restype = C.c_int
+    lib.oracle_simple_diode.argtypes = [dp, C.c_double, dp]
     lib.oracle_next_breakpoint.restype = C.c_double
     lib.oracle_next_breakpoint.argtypes = [C.POINTER(abi.CktDesc), C.c_double, C.c_double]
     lib.oracle_source_value.restype = C.c_double
@@ -100,6 +102,25 @@ class Oracle:
         rc = self.lib.oracle_eval(C.byref(h.desc), _dp(x), _dp(xdot), t, int(dc), _dp(F), _dp(Fi), _dp(Fq), _dp(G), _dp(Cm))
         assert rc == 0
         return F, Fi, Fq, G, Cm
+
+    # SimpleDiode's defaults (src/simpledevices.jl:152-168), in the struct's field order
+    SIMPLE_DIODE_DEFAULTS = dict(AREA=1.0, BV=3.40282e38, BVJ=3.40282e38, CJO=0.0, EG=1.11, FC=0.5, IBV=1e-3,
+                                 IS=1e-14, KF=0.0, M=0.5, N=1.0, RS=0.0, TNOM=27.0, TT=0.0, VJ=1.0, XTI=3.0)
+
+    def simple_diode(self, vd, **params):
+        """The reference's SimpleDiode restated literally at junction voltage vd
+        (parity unpinned; see oracle_simple_diode).  Returns (code, Id, Ideff,
+        Cdeplete, TT, Cdiffuse in DC); code 1 / 2: the reference reads an undefined
+        name (NVt / MJI), 3: sqrt of a negative number."""
+        p = dict(self.SIMPLE_DIODE_DEFAULTS)
+        for k, v in params.items():
+            if k not in p:
+                raise KeyError(k)
+            p[k] = float(v)
+        arr = np.array(list(p.values()), np.float64)
+        out = np.full(5, np.nan)
+        rc = self.lib.oracle_simple_diode(_dp(arr), float(vd), _dp(out))
+        return (rc, *out)
 
     # ---- small-signal AC and noise (dense complex solves; LAPACK partial pivoting)
     def ac_drive(self, flat, x_op):
