@@ -149,17 +149,25 @@ def _is_int_const(e) -> bool:
     return isinstance(e, Num) and e.is_int
 
 
+def _at(v: float, bound: float) -> bool:
+    """v equals a bound up to the rounding of the bound's own expression: a
+    scale-factor literal is the decimal times the factor (0.1n is 0.1 * 1e-9 =
+    1.0000000000000001e-10, as the reference converts it, src/vasim.jl:114-126),
+    so a card value written 1e-10 meets the inclusive bound [0.1n:."""
+    return v == bound or (math.isfinite(bound) and abs(v - bound) <= 4 * math.ulp(max(abs(v), abs(bound))))
+
+
 def check_range(model: str, p: Param, v: float, env: Dict[str, float]):
     """`from` / `exclude` ranges of a parameter declaration."""
     for r in p.ranges:
         if len(r) == 2:
             kind, x = r
-            inside = v == const_eval(x, env)
+            inside = _at(v, const_eval(x, env))
         else:
             kind, lo, hi, li, hi_i = r
             lo_v = -math.inf if _is_inf(lo) else const_eval(lo, env)
             hi_v = math.inf if _is_inf(hi) else const_eval(hi, env)
-            inside = (v > lo_v or (li and v == lo_v)) and (v < hi_v or (hi_i and v == hi_v))
+            inside = (v > lo_v or (li and _at(v, lo_v))) and (v < hi_v or (hi_i and _at(v, hi_v)))
         if (kind == "from" and not inside) or (kind == "exclude" and inside):
             raise VAError(f"{model}: parameter {p.name} = {v} violates its `{kind}` range")
 

@@ -300,6 +300,29 @@ def test_parser_details(va):
     assert m.gents == [(0, 0), (0, 1), (1, 0), (1, 1)]
 
 
+def test_range_bounds_take_the_rounding_of_scale_factors(va):
+    """A scale-factor literal is the decimal times the factor, as the reference
+    converts it (0.1n = 0.1 * 1e-9 = 1.0000000000000001e-10, src/vasim.jl:114-126),
+    so a value written 1e-10 (the ASAP7 cards' EOTACC against BSIM-CMG's
+    `from [0.1n:inf)`) meets an inclusive bound up to that rounding; values
+    clearly outside, and an exclusive bound, are still refused."""
+    from cedarsim_gb300.va.emit import analyze
+    from cedarsim_gb300.va.parser import VAError
+    src = """module rb(p, n); inout p, n; electrical p, n;
+      parameter real T = 1n from [0.1n:inf);
+      parameter real U = 1n from (0.1n:1u];
+      parameter real W = 1 exclude 0.3n;
+      analog I(p, n) <+ V(p, n) * (T + U + W);
+    endmodule"""
+    m, _ = analyze(va.parse(src)[0])
+    assert 0.1 * 1e-9 != 1e-10
+    assert m.defaults({"T": 1e-10})[0] == 1e-10
+    assert m.defaults({"U": 1e-6})[1] == 1e-6
+    for bad in ({"T": 0.99e-10}, {"U": 1e-10}, {"U": 1.01e-6}, {"W": 3e-10}):
+        with pytest.raises(VAError):
+            m.defaults(bad)
+
+
 def test_internal_node_model_equals_its_expanded_network(pkg, oracle, va):
     """va_diode_rs (RS to an internal node, the junction behind it) is the same
     network as va_resistor + va_diode around an explicit node: same unknowns

@@ -9,7 +9,11 @@ its residuals and Jacobians are compared with the independent interpretation of
 the same parsed module at several bias points, and the drain current is checked
 for the on / off behaviour of an n-type FinFET.  The model has 6 terminal
 values (d, g, s, e and the internal di, si); a library built with it widens the
-engines' per-device staging to 6 (CEDAR_MAX_TERM)."""
+engines' per-device staging to 6 (CEDAR_MAX_TERM).  With the model compiled into
+a scratch copy of the oracle, a CMOS inverter of two devices runs its DC
+operating point and a transient, and, given CEDAR_ASAP7_CARD (the ASAP7 TT
+Spectre model cards), its output-noise density is compared with the ngspice
+table of CedarSim's own BSIM-CMG noise test."""
 import ctypes as C
 import importlib.util
 import os
@@ -17,6 +21,7 @@ import pathlib
 import shutil
 import subprocess
 import sys
+import zlib
 
 import numpy as np
 import pytest
@@ -117,29 +122,40 @@ print(json.dumps(res))
 """
 
 
-def test_bsimcmg_inverter_dc_and_transient_on_the_oracle(tmp_path):
+@pytest.fixture(scope="module")
+def scratch(tmp_path_factory):
+    """A copy of the package and the oracle in a scratch directory, where scripts
+    run with CEDAR_VA_PATH naming the model, so that its generated code never
+    enters this checkout's build (the oracle compiles it in on first use)."""
+    if shutil.which("g++") is None or shutil.which("make") is None:
+        pytest.skip("g++ / make not available")
+    d = tmp_path_factory.mktemp("bsim_scratch")
+    work = d / "repo"
+    ign = shutil.ignore_patterns("_build", "__pycache__", "_work")
+    for sub in ("cedarsim.jl_gb300", "oracle", "include"):
+        shutil.copytree(ROOT / sub, work / sub, ignore=ign)
+    shutil.copy(ROOT / "__graft_entry__.py", work / "__graft_entry__.py")
+    env = dict(os.environ, CEDAR_VA_PATH=str(pathlib.Path(SRC_DIR) / "bsimcmg.va"))
+
+    def run(script: str, *args: str):
+        import json
+        f = d / f"s{zlib.crc32(script.encode()):08x}.py"
+        f.write_text(script)
+        r = subprocess.run([sys.executable, str(f), str(work), *args], capture_output=True, text=True, env=env,
+                           timeout=1800)
+        assert r.returncode == 0, r.stderr[-3000:]
+        return json.loads(r.stdout.strip().splitlines()[-1])
+    return run
+
+
+def test_bsimcmg_inverter_dc_and_transient_on_the_oracle(scratch):
     """A CMOS inverter of two BSIM-CMG devices (0.7 V supply, 1 fF load) through the
     oracle's DC homotopy and adaptive BDF2 with the model compiled in: the DC point
     is reached from zero with the input at 0 V, mid-rail and 0.7 V, and a 0 -> 0.7 V
     input pulse pulls the output low and releases it.  At 0 V input the PMOS's
     smoothed V_ds rounds to exactly 0 while its partials do not, so the DC solve
-    depends on pow's zero-exponent derivative rule (x^0 has zero partials).  The
-    oracle and package are copied to a scratch directory, so the model's generated
-    code never enters this checkout's build."""
-    if shutil.which("g++") is None or shutil.which("make") is None:
-        pytest.skip("g++ / make not available")
-    import json
-    work = tmp_path / "repo"
-    ign = shutil.ignore_patterns("_build", "__pycache__", "_work")
-    for d in ("cedarsim.jl_gb300", "oracle", "include"):
-        shutil.copytree(ROOT / d, work / d, ignore=ign)
-    shutil.copy(ROOT / "__graft_entry__.py", work / "__graft_entry__.py")
-    (tmp_path / "inv.py").write_text(_INVERTER_SCRIPT)
-    env = dict(os.environ, CEDAR_VA_PATH=str(pathlib.Path(SRC_DIR) / "bsimcmg.va"))
-    r = subprocess.run([sys.executable, str(tmp_path / "inv.py"), str(work)], capture_output=True, text=True,
-                       env=env, timeout=1800)
-    assert r.returncode == 0, r.stderr[-3000:]
-    res = json.loads(r.stdout.strip().splitlines()[-1])
+    depends on pow's zero-exponent derivative rule (x^0 has zero partials)."""
+    res = scratch(_INVERTER_SCRIPT)
     for vin, (rc, status, iters, vout) in res["dc"].items():
         assert rc == 0 and status == 0, (vin, rc, status, iters)
     assert res["dc"]["0.0"][3] > 0.699 and res["dc"]["0.7"][3] < 1e-3
@@ -147,3 +163,76 @@ def test_bsimcmg_inverter_dc_and_transient_on_the_oracle(tmp_path):
     rc, status, npts, v0, vmin, vend, vmid = res["tran"]
     assert rc == 0 and status == 0 and npts > 10
     assert v0 > 0.699 and vmid < 0.1 and vmin < 0.1 and vend > 0.6
+
+
+_NOISE_SCRIPT = r"""
+import json, re, sys
+sys.path.insert(0, sys.argv[1])
+import numpy as np
+import __graft_entry__ as ge
+pkg = ge.load()
+O = ge.load_oracle().Oracle(pkg)
+
+def cards(path):
+    # Spectre `model NAME bsimcmg type=n ...` cards with `+ name = value` lines
+    out, cur = {}, None
+    for line in open(path):
+        line = line.split("//")[0].rstrip()
+        m = re.match(r"\s*model\s+(\w+)\s+bsimcmg\s+(.*)", line, re.I)
+        if m:
+            cur, rest = m.group(1).lower(), m.group(2)
+            out[cur] = {}
+        elif cur and line.strip().startswith("+"):
+            rest = line.strip()[1:]
+        else:
+            continue
+        for k, v in re.findall(r"(\w+)\s*=\s*([^\s]+)", rest):
+            out[cur][k.lower()] = v
+    return out
+
+mod = pkg.va.model(pkg.va.model_id("bsimcmg"))
+names = {p.name.lower(): p.name for p in mod.params}
+def params(card):
+    # type = n / p -> DEVTYPE; LEVEL (the simulator's model selector) is not a module parameter
+    p = {"DEVTYPE": 1 if card["type"].lower() == "n" else 0}
+    p.update({names[k]: float(v) for k, v in card.items() if k in names})
+    return p
+
+C = cards(sys.argv[2])
+c = pkg.Circuit()                              # test/bsimcmg/inverter_cmg_cedar.cir
+c.V("VVDD", "vdd", "0", dc=1.0)
+c.V("VVSS", "vss", "0", dc=0.0)
+c.C("CQ", "d", "0", 1e-15)
+c.V("VD", "d", "0", dc=0.5, ac=1.0)
+c.va("mneg", "bsimcmg", ["q", "d", "vss", "vss"], **params(C["nmos_lvt"]))
+c.va("mpos", "bsimcmg", ["q", "d", "vdd", "vdd"], **params(C["pmos_lvt"]))
+f = c.flatten()
+x, st, rc = O.dcop(f)
+f_hz = np.array(json.loads(sys.argv[3]))
+psd = O.noise(f, x, 2 * np.pi * f_hz, f.index("q")) if rc == 0 else np.full(len(f_hz), np.nan)
+print(json.dumps({"rc": rc, "dc_iters": int(st.dc_iters), "q": float(x[f.index("q")]),
+                  "sqrt_psd": np.sqrt(np.abs(psd)).tolist()}))
+"""
+
+
+def test_bsimcmg_inverter_noise_matches_ngspice(scratch):
+    """CedarSim's BSIM-CMG noise test (test/ac.jl:155-237): the output-noise density
+    of a BSIM-CMG inverter on the ASAP7 TT cards (nmos_lvt / pmos_lvt, VDD = 1 V,
+    input at 0.5 V, 1 fF on the input) against the ngspice table the reference
+    holds (tests/golden/ac_noise_bsimcmg_ngspice.json, 1 kHz .. 1 PHz), at the
+    reference's tolerance (isapprox, rtol 1e-6) and point by point.  The model's
+    currents, charges and partials come from the emitted code compiled into the
+    oracle, its noise sources from the independent interpreter, the PSD from the
+    oracle's dense small-signal solve.  Needs CEDAR_ASAP7_CARD, the path of the
+    ASAP7 TT Spectre model cards (CedarSim carries them as
+    SpectreNetlistParser.jl/test/examples/7nm_TT.scs)."""
+    import json
+    card = os.environ.get("CEDAR_ASAP7_CARD", "")
+    if not card or not pathlib.Path(card).is_file():
+        pytest.skip("CEDAR_ASAP7_CARD does not name the ASAP7 TT model cards")
+    gold = json.loads((ROOT / "tests" / "golden" / "ac_noise_bsimcmg_ngspice.json").read_text())
+    res = scratch(_NOISE_SCRIPT, card, json.dumps(gold["f_hz"]))
+    assert res["rc"] == 0 and 0.0 < res["q"] < 1.0
+    got, want = np.array(res["sqrt_psd"]), np.array(gold["sqrt_psd"])
+    assert np.linalg.norm(got - want) <= 1e-6 * max(np.linalg.norm(got), np.linalg.norm(want))
+    assert np.max(np.abs(got - want) / want) <= 1e-7
