@@ -210,8 +210,22 @@ f = c.flatten()
 x, st, rc = O.dcop(f)
 f_hz = np.array(json.loads(sys.argv[3]))
 psd = O.noise(f, x, 2 * np.pi * f_hz, f.index("q")) if rc == 0 else np.full(len(f_hz), np.nan)
+# test/bsimcmg/inverter.jl: the same inverter with VD = SIN(0.5 0.01 1e7), 0 .. 400 ns
+ct = pkg.Circuit()
+ct.V("VVDD", "vdd", "0", dc=1.0)
+ct.V("VVSS", "vss", "0", dc=0.0)
+ct.C("CQ", "d", "0", 1e-15)
+ct.V("VD", "d", "0", wave=pkg.Sin(0.5, 0.01, 1e7))
+ct.va("mneg", "bsimcmg", ["q", "d", "vss", "vss"], **params(C["nmos_lvt"]))
+ct.va("mpos", "bsimcmg", ["q", "d", "vdd", "vdd"], **params(C["pmos_lvt"]))
+ft = ct.flatten()
+t, xs, stt, rct = O.tran(ft, pkg.make_opts("bdf2", True, 0.0, 4e-7, 0.0, True, 1e-7, 1e-7), cap=1 << 18)
+qd = xs[:, ft.index("q")] - x[f.index("q")]
+dd = xs[:, ft.index("d")] - 0.5
+gain = float(np.dot(qd, dd) / np.dot(dd, dd))
 print(json.dumps({"rc": rc, "dc_iters": int(st.dc_iters), "q": float(x[f.index("q")]),
-                  "sqrt_psd": np.sqrt(np.abs(psd)).tolist()}))
+                  "sqrt_psd": np.sqrt(np.abs(psd)).tolist(),
+                  "tran": [rct, int(stt.status), len(t), gain]}))
 """
 
 
@@ -225,7 +239,9 @@ def test_bsimcmg_inverter_noise_matches_ngspice(scratch):
     oracle, its noise sources from the independent interpreter, the PSD from the
     oracle's dense small-signal solve.  Needs CEDAR_ASAP7_CARD, the path of the
     ASAP7 TT Spectre model cards (CedarSim carries them as
-    SpectreNetlistParser.jl/test/examples/7nm_TT.scs)."""
+    SpectreNetlistParser.jl/test/examples/7nm_TT.scs).  The same inverter then runs
+    the transient of test/bsimcmg/inverter.jl (a 10 mV, 10 MHz input sine about
+    0.5 V, 0 .. 400 ns, tolerances 1e-7), which the reference asserts completes."""
     import json
     card = os.environ.get("CEDAR_ASAP7_CARD", "")
     if not card or not pathlib.Path(card).is_file():
@@ -236,3 +252,7 @@ def test_bsimcmg_inverter_noise_matches_ngspice(scratch):
     got, want = np.array(res["sqrt_psd"]), np.array(gold["sqrt_psd"])
     assert np.linalg.norm(got - want) <= 1e-6 * max(np.linalg.norm(got), np.linalg.norm(want))
     assert np.max(np.abs(got - want) / want) <= 1e-7
+    # the transient of test/bsimcmg/inverter.jl completes; the output follows the
+    # 10 mV input sine inverted and amplified
+    rc, status, npts, gain = res["tran"]
+    assert rc == 0 and status == 0 and npts > 100 and gain < -1.0
