@@ -140,6 +140,11 @@ def opts_for(pkg, tstop=TSTOP):
     return pkg.make_opts("bdf2", True, 0.0, tstop, 0.0, True, reltol=1e-6, abstol_v=1e-9, hmax=TSTOP / 50)
 
 
+def mc_workload(n_inst: int, tstop_ns: float = TSTOP * 1e9) -> str:
+    """The Monte Carlo headline workload's name, the same in both arms' config."""
+    return f"{n_inst} MC ragged inverter chains (L in {{5..63}}), adaptive BDF2 to {tstop_ns:g} ns, reltol 1e-6"
+
+
 def flops_per_iteration(pkg, templates):
     out = []
     for f in templates:
@@ -483,12 +488,13 @@ def plain_leg(pkg, orc, C, name, flat, opts, fp64_peak, hbm_peak, workload):
             "e2e": {"value": steps / wall_s, "unit": "timesteps/s", "seconds": wall_s,
                     "h2d_bytes_per_step": int(x.nbytes + C.sizeof(opts)),
                     "d2h_bytes_per_step": int(cnt.value * (8 + 8 * sy.n) + C.sizeof(st))},
-            "roofline": {"bound": "latency (one warp)", "hbm": {"achieved_gbs": gbs, "peak_gbs": hbm_peak,
-                                                               "frac": gbs / hbm_peak},
+            "roofline": {"bound": f"latency (one circuit; fastest engine {best})",
+                         "hbm": {"achieved_gbs": gbs, "peak_gbs": hbm_peak, "frac": gbs / hbm_peak},
                          "fp64": {"achieved_tflops": tfl, "peak_tflops": fp64_peak, "frac": tfl / fp64_peak},
                          "bytes_per_newton_iter": int(costs.bytes), "flops_per_newton_iter": int(flops),
                          "note": "algorithmic bytes / flops of one Newton iteration (cedar_ckt_costs) x iterations "
-                                 "/ kernel time; one circuit on one warp is latency-bound, the fractions show how far"},
+                                 "/ kernel time; one circuit is latency-bound on every engine, the fractions show "
+                                 "how far"},
             "vs_oracle": {"max_scaled_error": err, "tolerance": "reltol 1e-6, abstol 1e-9 V, every recorded point",
                           "same_time_points": same_t, "oracle_steps": int(st_ref.accepted)},
             "cpu_baseline": {"value": st_ref.accepted / cpu_s, "unit": "timesteps/s", "cores": 1, "kind": "port",
@@ -560,7 +566,7 @@ def run_reference(args, pkg):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_time / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded Philox4x32-10)",
-            "config": {"workload": "4096 MC ragged inverter chains, adaptive BDF2 to 20 ns", "n_inst": args.n_inst},
+            "config": {"workload": mc_workload(args.n_inst), "n_inst": args.n_inst},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
@@ -763,7 +769,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Philox4x32-10)",
-        "config": {"workload": "4096 MC ragged inverter chains (L in {5..63}), adaptive BDF2 to 20 ns, reltol 1e-6",
+        "config": {"workload": mc_workload(args.n_inst, args.tstop_ns),
                    "n_inst": args.n_inst, "instances_per_rank": len(mine), "window_ns": tstop / nwin * 1e9, "tstop_ns": args.tstop_ns,
                    "tuning": list(sw.tuning), "l2": "state resident on chip; no HBM re-read to flush",
                    "parallelism": f"instances sharded over {world} GPU(s), no collective"},
