@@ -25,9 +25,12 @@
 #else
 #define VA_CALL static __host__ __device__ __noinline__
 #endif
+// the functions a large module is split into are called, not inlined
+#define VA_PART __host__ __device__ __noinline__
 #else
 #define VA_HD inline
 #define VA_CALL inline
+#define VA_PART inline
 #endif
 #include <cmath>
 

@@ -575,6 +575,25 @@ def _count_flops(stmts) -> int:
 
 
 # ------------------------------------------------------------------ C++ code
+# A module whose analog block holds more statements than this is emitted split
+# into functions of about PART_STMTS statements over a frame (split_body); the
+# shipped models are far below it and keep the single-function form.
+SPLIT_STMTS = 1000
+PART_STMTS = 60
+
+
+def _stmt_count(ss) -> int:
+    """Statements in ss, nested blocks included."""
+    n = 0
+    for st in ss:
+        n += 1
+        if isinstance(st, If):
+            n += _stmt_count(st.then) + _stmt_count(st.other or [])
+        elif isinstance(st, Loop):
+            n += _stmt_count(st.init) + _stmt_count(st.body) + _stmt_count(st.step)
+    return n
+
+
 def _lit(v: float) -> str:
     r = repr(float(v))
     return r if any(ch in r for ch in ".einf") else r + ".0"
@@ -586,6 +605,8 @@ class _Emitter:
         self.a = a
         self.scope: Optional[Dict[str, str]] = None     # an analog function's names while emitting it
         self.loops = 0                                  # loop counter names
+        self.fr = ""                                    # "F." while emitting a split model's frame accesses
+        self.parts: List[list] = []                     # statement chunks of a split model, one function each
 
     def is_int(self, e) -> bool:
         if isinstance(e, Num):
@@ -612,7 +633,7 @@ class _Emitter:
         if isinstance(e, Name):
             if self.scope is not None:
                 return "v_" + e.id
-            return ("p_" if e.id in self.a.params else "v_") + e.id
+            return self.fr + ("p_" if e.id in self.a.params else "v_") + e.id
         if isinstance(e, Probe):
             if e.kind == "I":
                 sg = self.a.branch_sign(e.a, e.b, 0)
@@ -677,7 +698,7 @@ class _Emitter:
                     if an in f.outputs:       # by reference: a variable of the caller
                         if not isinstance(a, Name):
                             raise VAError(f"{self.m.name}: line {e.line}: output argument {an} needs a variable")
-                        parts.append(f", v_{a.id}")
+                        parts.append(f", {self.fr if self.scope is None else ''}v_{a.id}")
                     else:
                         parts.append(f", D({self.x(a)})")
                 return f"fn_{self.m.name}_{e.fn}<D>(c{''.join(parts)})"
@@ -697,7 +718,7 @@ class _Emitter:
             if e.name == "$mfactor":
                 return "c.m"
             if e.name in ("$param_given", "$given"):
-                return f"p__given_{e.args[0].id}"
+                return f"{self.fr if self.scope is None else ''}p__given_{e.args[0].id}"
             if e.name == "$simparam":
                 if not e.args or not isinstance(e.args[0], str):
                     raise VAError(f"{self.m.name}: $simparam needs a name")
@@ -713,10 +734,11 @@ class _Emitter:
         out = []
         for s in ss:
             if isinstance(s, Assign):
+                tgt = (self.fr if self.scope is None else "") + "v_" + s.name
                 if types[s.name] == "integer":
-                    out.append(f"{ind}v_{s.name} = vint(val({self.x(s.expr)}));")
+                    out.append(f"{ind}{tgt} = vint(val({self.x(s.expr)}));")
                 else:
-                    out.append(f"{ind}v_{s.name} = D({self.x(s.expr)});")
+                    out.append(f"{ind}{tgt} = D({self.x(s.expr)});")
             elif isinstance(s, If):
                 out.append(f"{ind}if (val({self.x(s.c)}) != 0.0) {{")
                 out += self.stmts(s.then, ind + "  ", types)
@@ -764,6 +786,8 @@ class _Emitter:
         return out
 
     def body(self) -> str:
+        if _stmt_count(self.m.module.body) > SPLIT_STMTS:
+            return self.split_body()
         m = self.m
         L = [f"// module {m.name}({', '.join(m.ports)})" + (f", internal {', '.join(m.internals)}" if m.internals else ""),
              "template <class D>",
@@ -787,6 +811,82 @@ class _Emitter:
         L.append("  (void)c; (void)V; (void)Fi; (void)Fq; (void)P; (void)ps; (void)nz;")
         L.append("}")
         return "\n".join(L)
+
+    def split_body(self) -> str:
+        """A large module (a CMC compact model) as several functions: its
+        parameters, $param_given flags and variables live in a frame struct, the
+        analog block's statements are cut into chunks of about PART_STMTS
+        statements at statement boundaries (an if whose branches are larger is
+        kept in the caller and its branches cut in turn), and each chunk is a
+        function that is not inlined.  The arithmetic, its order and the results
+        are those of the single function; what changes is that no one function
+        is the whole model, which the device compiler's register allocation
+        otherwise takes tens of minutes over."""
+        m = self.m
+        self.fr = ""
+        fields = [f"  double p_{p.name};" for p in m.params]
+        fields += [f"  double p__given_{g};" for g in m.given]
+        fields += [f"  D v_{v} = D(0.0);" if t == "real" else f"  double v_{v} = 0.0;"
+                   for v, t in m.module.variables.items()]
+        frame = ["template <class D>", f"struct Frame_{m.name} {{", *fields, "};"]
+        self.fr = "F."
+        self.parts = []
+        calls = self._split(m.module.body, "  ")
+        head = [f"// module {m.name}({', '.join(m.ports)})" + (f", internal {', '.join(m.internals)}" if m.internals else "")
+                + f": split into {len(self.parts)} functions over a frame"]
+        sig = "const double *P, int ps, const Ctx &c, const D *V, D *Fi, D *Fq, double *nz"
+        defs = []
+        for k, chunk in enumerate(self.parts):
+            defs += ["template <class D>", f"VA_PART void part_{m.name}_{k}({sig}, Frame_{m.name}<D> &F) {{"]
+            defs += self.stmts(chunk, "  ")
+            defs += ["  (void)P; (void)ps; (void)c; (void)V; (void)Fi; (void)Fq; (void)nz; (void)F;", "}"]
+        B = ["template <class D>", f"VA_HD void body_{m.name}({sig}) {{", f"  Frame_{m.name}<D> F;"]
+        for k, p_ in enumerate(m.params):
+            B.append(f"  F.p_{p_.name} = P[{k} * ps];")
+        for j, g in enumerate(m.given):
+            B.append(f"  F.p__given_{g} = P[{len(m.params) + j} * ps];")
+        if self.a.vbranch is not None:
+            va_, vb_ = self.a.vbranch
+            ia, nb = self.a.port[va_], self.a.nb
+            if vb_ is None:
+                B.append(f"  Fi[{ia}] -= V[{nb}]; Fi[{nb}] += V[{ia}];")
+            else:
+                ib = self.a.port[vb_]
+                B.append(f"  Fi[{ia}] -= V[{nb}]; Fi[{ib}] += V[{nb}]; Fi[{nb}] += V[{ia}] - V[{ib}];")
+        B += calls
+        B += ["  (void)c; (void)V; (void)Fi; (void)Fq; (void)P; (void)ps; (void)nz;", "}"]
+        self.fr = ""
+        return "\n".join(head + frame + defs + B)
+
+    def _split(self, ss, ind: str) -> List[str]:
+        """The caller's lines for statements ss: runs of statements become calls of
+        new part functions; an if larger than a part stays here, its branches split."""
+        out, chunk, n = [], [], 0
+        args = "(P, ps, c, V, Fi, Fq, nz, F);"
+
+        def flush():
+            nonlocal chunk, n
+            if chunk:
+                out.append(f"{ind}part_{self.m.name}_{len(self.parts)}<D>{args}")
+                self.parts.append(chunk)
+                chunk, n = [], 0
+        for st in ss:
+            k = _stmt_count([st])
+            if isinstance(st, If) and k > PART_STMTS:
+                flush()
+                out.append(f"{ind}if (val({self.x(st.c)}) != 0.0) {{")
+                out += self._split(st.then, ind + "  ")
+                if st.other:
+                    out.append(f"{ind}}} else {{")
+                    out += self._split(st.other, ind + "  ")
+                out.append(f"{ind}}}")
+                continue
+            if n + k > PART_STMTS:
+                flush()
+            chunk.append(st)
+            n += k
+        flush()
+        return out
 
     def functions(self) -> str:
         """Analog functions as templates over the body's dual type: arguments by

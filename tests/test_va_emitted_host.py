@@ -342,3 +342,90 @@ def test_pow_gradient_rule(pkg, tmp_path):
     assert np.array_equal(np.isinf(rg), np.isinf(g))
     fin = np.isfinite(g)
     assert np.allclose(rg[fin], g[fin], rtol=1e-15, atol=0.0)
+
+
+def _big_module(n_blocks: int) -> str:
+    """A module with more statements than the split threshold: chains of
+    assignments, nested ifs (one larger than a part), a loop, an analog function
+    with an output argument, $param_given and a charge."""
+    L = ["module big(a, b, c); inout a, b, c; electrical a, b, c;",
+         "  parameter real G = 1m from (0:inf); parameter real K0 = 0.1;",
+         "  real x, y, z, w, q; integer i;",
+         "  analog function real sq; input u; real u; begin sq = u * u; end endfunction",
+         "  analog function real tw; input u, o; real u, o; begin o = 2.0 * u; tw = u + o; end endfunction",
+         "  analog begin",
+         "    x = V(a, b); y = V(b, c); z = 0.0; w = 0.0; q = 0.0;"]
+    for k in range(n_blocks):
+        L.append(f"    z = z + {0.001 * (k + 1):.6f} * sq(x + {0.01 * k:.4f}) - 0.5 * y * {1.0 / (k + 2):.8f};")
+        L.append(f"    w = w * 0.999 + tanh(z * {0.1 + 0.001 * k:.5f});")
+        if k % 7 == 0:
+            L.append(f"    if (x > {0.01 * k:.3f}) begin z = z - 0.001 * exp(-y * y); end else begin w = w + 1e-4; end")
+    L.append("    if (x > -10.0) begin")
+    for k in range(80):
+        L.append(f"      q = q + {1e-3 / (k + 1):.8f} * sqrt(x * x + {k + 1}.0) + tw(y, w) * 1e-6;")
+    L.append("    end else begin q = 0.0; end")
+    L.append("    for (i = 0; i < 3; i = i + 1) begin q = q + 1e-6 * i; end")
+    L.append("    if ($param_given(K0)) q = q * (1.0 + K0);")
+    L.append("    I(a, b) <+ G * (x + z * 1e-3 + w * 1e-3);")
+    L.append("    I(b, c) <+ G * y + ddt(1e-15 * q);")
+    L.append("  end")
+    L.append("endmodule")
+    return "\n".join(L)
+
+
+def test_split_emission_of_large_modules(pkg, tmp_path, monkeypatch):
+    """A module whose analog block is larger than the split threshold is emitted
+    as part functions over a frame (parameters, flags and variables in a
+    struct); its host-compiled residuals, charges and Jacobians are bit for bit
+    those of the same module emitted as one function, and match the
+    interpreter."""
+    import importlib
+    P = importlib.import_module("cedarsim_gb300.va.parser")
+    E = importlib.import_module("cedarsim_gb300.va.emit")
+    src = _big_module(380)
+    mod = P.parse(src)[0]
+    assert E._stmt_count(mod.body) > E.SPLIT_STMTS
+
+    def build(tag):
+        mods = [E.analyze(m) for m in P.parse(src)]
+        text = E.emit_header(mods, 11)
+        d = tmp_path / tag
+        d.mkdir()
+        (d / "va_models.gen.h").write_text(text)
+        (d / "h.cpp").write_text('#include <math.h>\n#include "va_models.gen.h"\n'
+                                 'extern "C" void h(const double *dp, const double *v, double *fi, double *fq, '
+                                 'double *G, double *C) { cedar::va::full(0, dp, 1, v, 1e-12, fi, fq, G, C); }\n')
+        r = subprocess.run(["g++", "-O1", "-std=c++17", "-shared", "-fPIC", "-I", str(CSRC), "-I", str(d),
+                            str(d / "h.cpp"), "-o", str(d / "h.so")], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr[-1500:]
+        return text, C.CDLL(str(d / "h.so"))
+    split_text, split = build("split")
+    assert split_text.count("VA_PART void part_big_") >= 5 and "struct Frame_big" in split_text
+    monkeypatch.setattr(E, "SPLIT_STMTS", 10 ** 9)
+    whole_text, whole = build("whole")
+    assert "VA_PART" not in whole_text
+    dp_ = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    m, _ = E.analyze(mod)
+    spec = importlib.util.spec_from_file_location("cedar_va_interp_big", ROOT / "oracle" / "va_interp.py")
+    vi = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(vi)
+    rng = np.random.default_rng(5)
+    for given in (False, True):
+        vals = m.defaults({"K0": 0.1} if given else {})   # parameters, then the $param_given(K0) flag
+        dp = np.array(vals + [1.0, VT])                    # then m and vt
+        for _ in range(4):
+            v = rng.uniform(-0.5, 1.0, 3)
+            outs = []
+            for lib in (split, whole):
+                fi, fq, G, Cm = np.zeros(3), np.zeros(3), np.zeros(9), np.zeros(9)
+                lib.h(dp_(dp), dp_(v), dp_(fi), dp_(fq), dp_(G), dp_(Cm))
+                outs.append((fi, fq, G, Cm))
+            for a, b in zip(*outs):
+                assert np.array_equal(a, b)
+            given_set = ["K0"] if given else []
+            ri, rq, rG, rC = map(np.asarray, vi.evaluate(mod, dict(zip([p.name for p in m.params], vals)), list(v),
+                                                          VT, 1e-12, 1.0, given_set))
+            assert vals[-1] == (1.0 if given else 0.0)
+            fi, fq, G, Cm = outs[0]
+            assert np.allclose(fi, ri, rtol=1e-12, atol=1e-18) and np.allclose(fq, rq, rtol=1e-12, atol=1e-30)
+            assert np.allclose(G, rG.ravel(), rtol=1e-11, atol=1e-18)
