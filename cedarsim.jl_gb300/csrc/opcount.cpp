@@ -85,6 +85,13 @@ static inline Cnt hypot(Cnt a, Cnt b) { return op1(std::hypot(a.v, b.v)); }
 static inline Cnt fmin(Cnt a, Cnt b) { return Cnt(std::fmin(a.v, b.v)); }
 static inline Cnt fmax(Cnt a, Cnt b) { return Cnt(std::fmax(a.v, b.v)); }
 static inline Cnt fma(Cnt a, Cnt b, Cnt c) { g_ops += 2; return Cnt(std::fma(a.v, b.v, c.v)); }
+// two-argument functions with one plain double (a literal exponent, as BSIM-CMG's
+// pow(x, 0.719)): exact overloads, as for the operators above
+#define CEDAR_CNT_F2MIX(f)                                             \
+  static inline Cnt f(Cnt a, double b) { return f(a, Cnt(b)); }        \
+  static inline Cnt f(double a, Cnt b) { return f(Cnt(a), b); }
+CEDAR_CNT_F2MIX(pow) CEDAR_CNT_F2MIX(atan2) CEDAR_CNT_F2MIX(hypot) CEDAR_CNT_F2MIX(fmod)
+#undef CEDAR_CNT_F2MIX
 static inline bool isfinite(Cnt a) { return std::isfinite(a.v); }
 static inline bool isnan(Cnt a) { return std::isnan(a.v); }
 static inline long long llround(Cnt a) { return std::llround(a.v); }
