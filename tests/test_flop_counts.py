@@ -67,3 +67,35 @@ def test_every_model_is_counted(pkg, counts):
     assert len(counts["VA"]) == len(pkg.va.models()) and all(x > 0 for x in counts["VA"])
     mos1 = pkg.circuit.MOS1
     assert counts["VA"][pkg.va.model_id("va_mos1") - pkg.va.BASE_ID] > counts["Builtin"][mos1]
+
+
+def test_counter_builds_with_literal_exponents(pkg, tmp_path):
+    """Compact models raise parameters and variables to literal powers
+    (BSIM-CMG: pow(NSD / 2.23e22, 0.719)); with every double an op-counting
+    scalar those calls mix the scalar with a plain double, which the counter
+    resolves exactly (pow, atan2, hypot and fmod), so a library build with such
+    a model gets its counts.  The counts follow the rule: one operation per
+    pow / atan2 / hypot / divide, on the value and each partial."""
+    import importlib
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no host C++ compiler")
+    P = importlib.import_module("cedarsim_gb300.va.parser")
+    E = importlib.import_module("cedarsim_gb300.va.emit")
+    src = """module lit(a, b); inout a, b; electrical a, b;
+      parameter real NSD = 2e26;
+      real x;
+      analog begin
+        x = pow(NSD / 2.23e22, 0.719) + pow(2.0, NSD * 1e-26) + atan2(NSD, 1.0) + hypot(1.0, NSD);
+        I(a, b) <+ 1e-3 * x * 1e-12 * V(a, b);
+      end endmodule"""
+    mods = [E.analyze(m) for m in P.parse(src)]
+    (tmp_path / "va_models.gen.h").write_text(E.emit_header(mods, 11))
+    exe = tmp_path / "opcount"
+    r = subprocess.run([cxx, "-std=c++17", "-O1", "-I", str(ROOT / "include"), "-I", str(PKG / "csrc"), "-I",
+                        str(tmp_path), "-o", str(exe), str(PKG / "csrc" / "opcount.cpp")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    va_counts = [int(v) for v in out.split("kVA[1] = {")[1].split("}")[0].split(",")]
+    assert len(va_counts) == 1 and va_counts[0] > 0
