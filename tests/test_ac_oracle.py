@@ -71,3 +71,55 @@ def test_ac_drive_host_matches_oracle(pkg, oracle):
     x, _, rc = oracle.dcop(flat)
     assert rc == 0
     np.testing.assert_allclose(pkg.ac_drive(flat), oracle.ac_drive(flat, x), rtol=1e-14, atol=1e-18)
+
+
+def _ladder(pkg, sections=100, r=1e3, c=1e-12):
+    """The AC / noise workload's RC ladder (the bench's AC leg), AC 1 at its input."""
+    ckt = pkg.Circuit()
+    ckt.V("V1", "n0", "0", dc=0.0, ac=1.0)
+    for k in range(1, sections + 1):
+        ckt.R(f"R{k}", f"n{k-1}", f"n{k}", r=r)
+        ckt.C(f"C{k}", f"n{k}", "0", c=c)
+    return ckt.flatten()
+
+
+def test_rc_ladder_response_and_noise_analytic(pkg, oracle):
+    """The 100-section RC ladder of the AC / noise workload against closed forms:
+    the response at sections 50 and 100 from the product of the sections' chain
+    (ABCD) matrices, and the output noise from Nyquist's theorem, 4 k T Re Z_out
+    for the resistors' thermal noise with the source shorted, over 1 kHz .. 1 THz."""
+    N, R, Cap = 100, 1e3, 1e-12
+    flat = _ladder(pkg, N, R, Cap)
+    x, st, rc = oracle.dcop(flat)
+    assert rc == 0
+    f = pkg.acdec(10, 1e3, 1e12)
+    w = 2 * np.pi * f
+    r = oracle.ac(flat, x, w, [flat.index("n50"), flat.index(f"n{N}")])
+    for q, s in enumerate(1j * w):
+        # [V_in, I_in] = M_1 ... M_N [V_out, 0], M_k = series R then shunt C, from
+        # the open output backwards, rescaled each section (log10 of the scale
+        # kept) because |V_in / V_out| reaches 1e380 at the top of the sweep
+        v, i, lg = 1.0 + 0j, 0.0 + 0j, 0.0
+        lg50 = None
+        for k in range(N, 0, -1):
+            if k == 50:                      # |v| = 1 here: V_50 = v 10^lg
+                lg50, ph50 = lg, v
+            i = i + s * Cap * v             # shunt C at node k
+            v = v + R * i                   # series R from node k-1
+            m = abs(v)
+            v, i, lg = v / m, i / m, lg + np.log10(m)
+        # H_out = V_out / V_in = 1 / (v 10^lg), H_50 = V_50 / V_in
+        for col, (lgH, ph) in enumerate(((lg50 - lg, ph50 / v), (-lg, 1.0 / v))):
+            if lgH < -250:                  # below what double precision holds: both ~0
+                assert abs(r[q, col]) < 1e-200
+                continue
+            H = 10.0 ** lgH * ph / abs(ph)
+            assert abs(r[q, col] - H) <= 1e-10 * abs(H), (f[q], col, r[q, col], H)
+    psd = oracle.noise(flat, x, w, flat.index(f"n{N}"))
+    T = flat.temp_c + 273.15
+    for q, s in enumerate(1j * w):
+        z = 0.0 + 0j                        # the shorted source
+        for _ in range(N):
+            z = z + R
+            z = z / (1.0 + s * Cap * z)     # in parallel with the shunt C
+        assert abs(psd[q] - 4 * K_B * T * z.real) <= 1e-9 * 4 * K_B * T * z.real
